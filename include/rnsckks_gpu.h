@@ -1,0 +1,194 @@
+/*
+ * rnsckks_gpu.h — C ABI of the GB300 (sm_103a) RNS-CKKS ciphertext-arithmetic
+ * library.  It is the drop-in boundary for the hot path of the Rust crate
+ * Akram275/rns-ckks-rust: each entry point names the reference function it
+ * replaces (paths relative to that crate).
+ *
+ * Conventions
+ *  - Every function returns an int status (RC_OK = 0).  On failure the message
+ *    is available from rc_last_error(ctx); nothing aborts.  Where the
+ *    reference panics on a precondition (level/scale/shape mismatch) the
+ *    library returns RC_ERR_INVALID_ARGUMENT with the reference's message.
+ *  - Polynomials are u64 residues in [0, q_i), limb-major [limbs][N], in
+ *    coefficient form (the reference's representation).  Ciphertext data is
+ *    [components][limbs][N] contiguous: 2 components for RnsCiphertext, 3 for
+ *    RnsQuadraticCiphertext.  `level` = limbs - 1, as in the reference.
+ *  - Ops on rc_ciphertext take DEVICE pointers and run on the given CUDA
+ *    stream (`void*` holding a cudaStream_t; NULL = legacy default stream).
+ *    Functions with the suffix _host take HOST pointers and include the
+ *    host<->device copies.
+ *  - Keys are uploaded once (coefficient form, reference layout) and kept
+ *    device-resident in the NTT domain.
+ *  - One context may be used from several host threads on distinct streams.
+ *    Calls on the same stream are ordered; the library's scratch memory is per
+ *    stream.
+ */
+#ifndef RNSCKKS_GPU_H
+#define RNSCKKS_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define RC_OK 0
+#define RC_ERR_INVALID_ARGUMENT 1
+#define RC_ERR_CUDA 2
+#define RC_ERR_OUT_OF_MEMORY 3
+#define RC_ERR_UNSUPPORTED 4
+
+typedef struct rc_context rc_context;
+typedef struct rc_ksk rc_ksk;
+
+/* RnsPrime{modulus, primitive_root}: src/rns/basis.rs:8-22 */
+typedef struct {
+  uint64_t modulus;
+  uint64_t primitive_root;
+} rc_prime;
+
+/* RnsCkksParams{poly_degree, primes, aux_primes, scale_bits}: src/rns/context.rs:16-21 */
+typedef struct {
+  uint64_t poly_degree;
+  const rc_prime* primes;
+  uint32_t prime_count;
+  const rc_prime* aux_primes;
+  uint32_t aux_count;
+  uint32_t scale_bits;
+} rc_params;
+
+/* RnsCiphertext / RnsQuadraticCiphertext {c0, c1[, c2], scale_bits, level}:
+ * src/rns/ciphertexts.rs:4-18.  `data` is a device pointer to
+ * [components][level+1][N] residues. */
+typedef struct {
+  uint64_t* data;
+  int32_t level;
+  int32_t scale_bits;
+} rc_ciphertext;
+
+/* ---- context: RnsCkksContext::new, src/rns/context/construction.rs:9-31,
+ *      with RnsCkksParams::validate, src/rns/context/params.rs:48-73 ---- */
+int rc_context_create(const rc_params* params, rc_context** out);
+void rc_context_destroy(rc_context* ctx);
+const char* rc_last_error(const rc_context* ctx);
+/* levels(), num_slots(), poly_degree, aux count: context.rs:57-95 */
+int rc_context_info(const rc_context* ctx, uint64_t* poly_degree, uint32_t* levels, uint32_t* aux_count,
+                    uint32_t* scale_bits);
+/* num_decomp_digits(bits(Q_level), 30): src/rns/keyswitching.rs:238-240 */
+int rc_decomp_digits(const rc_context* ctx, int32_t level, uint32_t* digits);
+/* Pre-size the per-stream scratch for ops on `max_batch` ciphertexts at
+ * `max_level` (so later calls, e.g. under CUDA graph capture, allocate nothing). */
+int rc_reserve(rc_context* ctx, int32_t max_level, uint32_t max_batch, void* stream);
+
+/* ---- keys ---- */
+/* RnsKeySwitchingKey{ksk, decomp_bits, level, aux_level_count}:
+ * src/rns/keyswitching.rs:13-18.  `host_key` = [digits][2][level+1+aux_count][N]
+ * coefficient-form residues (ksk[i].c0, ksk[i].c1), aux_count = 0 (Q-only key)
+ * or the context's aux prime count (hybrid key).  The key is transformed once
+ * on upload.  galois_element = 0 for a relinearisation key, otherwise the
+ * RnsRotationKey's element (src/rns/rotation.rs:9-12). */
+int rc_ksk_upload(rc_context* ctx, const uint64_t* host_key, uint32_t digits, int32_t level, uint32_t aux_count,
+                  uint64_t galois_element, rc_ksk** out);
+/* Same as rc_ksk_upload with the coefficient-form key already in device memory
+ * (e.g. generated on the GPU); the source buffer is not modified. */
+int rc_ksk_upload_device(rc_context* ctx, const uint64_t* device_key, uint32_t digits, int32_t level,
+                         uint32_t aux_count, uint64_t galois_element, rc_ksk** out);
+/* RnsKeySwitchingKey::truncate_levels (Q-only keys): keyswitching.rs:32-41 */
+int rc_ksk_truncate(rc_context* ctx, const rc_ksk* key, int32_t level, rc_ksk** out);
+int rc_ksk_info(const rc_ksk* key, uint32_t* digits, int32_t* level, uint32_t* aux_count, uint64_t* galois_element);
+void rc_ksk_destroy(rc_ksk* key);
+
+/* ---- polynomial-level ops (device pointers, limb-major) ---- */
+/* NttPlan::forward/inverse composed with the negacyclic twist
+ * (src/math/ntt.rs:78-89, src/poly/mod.rs:134-175): for `polys` polynomials of
+ * `limbs` limbs laid out [polys][limbs][N], limb j using prime j of the chain
+ * (limbs <= levels) or, when with_aux != 0, primes 0..limbs-aux-1 followed by
+ * the aux primes.  Output order: evaluation at psi^(2k+1) stored at
+ * bit-reversed index k. */
+int rc_ntt_forward(rc_context* ctx, uint64_t* data, uint32_t polys, uint32_t limbs, int32_t with_aux, void* stream);
+int rc_ntt_inverse(rc_context* ctx, uint64_t* data, uint32_t polys, uint32_t limbs, int32_t with_aux, void* stream);
+/* RnsPolynomial::multiply_ntt: src/rns/polynomial.rs:121-136.  with_aux != 0:
+ * the polynomial is over Q_(limbs-aux) followed by the aux primes (the
+ * eval-key basis, context.rs:104-118). */
+int rc_poly_multiply(rc_context* ctx, const uint64_t* a, const uint64_t* b, uint64_t* out, uint32_t limbs,
+                     int32_t with_aux, void* stream);
+/* RnsPolynomial::add / sub: polynomial.rs:99-119 */
+int rc_poly_add(rc_context* ctx, const uint64_t* a, const uint64_t* b, uint64_t* out, uint32_t limbs,
+                int32_t with_aux, void* stream);
+int rc_poly_sub(rc_context* ctx, const uint64_t* a, const uint64_t* b, uint64_t* out, uint32_t limbs,
+                int32_t with_aux, void* stream);
+/* out_j = a_j * scalars[j] mod q_j (scalars: host array, one per limb): the
+ * per-prime reduction of (coefficient * B^i [* P]) in key generation,
+ * src/rns/keyswitching.rs:64-68,108-112 */
+int rc_poly_mul_scalar(rc_context* ctx, const uint64_t* a, const uint64_t* scalars, uint64_t* out, uint32_t limbs,
+                       int32_t with_aux, void* stream);
+/* RnsCkksContext::apply_galois_automorphism: src/rns/context/rotation.rs:6-10,
+ * src/poly/mod.rs:110-131 */
+int rc_poly_automorphism(rc_context* ctx, const uint64_t* a, uint64_t* out, uint32_t limbs, uint64_t galois_element,
+                         void* stream);
+
+/* ---- ciphertext ops (RnsCkksContext, src/rns/context/ops.rs) ---- */
+/* RnsCiphertext::add: src/rns/ciphertexts.rs:60-69 */
+int rc_add(rc_context* ctx, const rc_ciphertext* lhs, const rc_ciphertext* rhs, rc_ciphertext* out, void* stream);
+/* mult_plain: context/ops.rs:20-30 (scale doubles) */
+int rc_mult_plain(rc_context* ctx, const rc_ciphertext* ct, const uint64_t* plain, rc_ciphertext* out, void* stream);
+/* multiply_plain_rns: src/rns/ops.rs:54-66 (scale unchanged) */
+int rc_multiply_plain_rns(rc_context* ctx, const rc_ciphertext* ct, const uint64_t* plain, rc_ciphertext* out,
+                          void* stream);
+/* mult: context/ops.rs:63-70 -> multiply_ciphertexts_rns, src/rns/ops.rs:84-100 */
+int rc_mult(rc_context* ctx, const rc_ciphertext* lhs, const rc_ciphertext* rhs, rc_ciphertext* out_quadratic,
+            void* stream);
+/* rescale: context/ops.rs:32-37 -> rescale_ciphertext_rns, src/rns/ops.rs:68-82 */
+int rc_rescale(rc_context* ctx, const rc_ciphertext* ct, rc_ciphertext* out, void* stream);
+/* rescale_quadratic: context/ops.rs:85-90 -> src/rns/ops.rs:115-133 */
+int rc_rescale_quadratic(rc_context* ctx, const rc_ciphertext* ct, rc_ciphertext* out, void* stream);
+/* keyswitch: context/ops.rs:97-109 -> keyswitch_rns / keyswitch_rns_hybrid,
+ * src/rns/keyswitching.rs:130-194.  `poly` holds level+1 limbs. */
+int rc_keyswitch(rc_context* ctx, const uint64_t* poly, int32_t level, const rc_ksk* key, rc_ciphertext* out,
+                 void* stream);
+/* relinearize: context/ops.rs:111-122 */
+int rc_relinearize(rc_context* ctx, const rc_ciphertext* quadratic, const rc_ksk* key, rc_ciphertext* out,
+                   void* stream);
+/* mult_relinearized: context/ops.rs:124-133 (tensor, relinearize, rescale) */
+int rc_mult_relinearized(rc_context* ctx, const rc_ciphertext* lhs, const rc_ciphertext* rhs, const rc_ksk* key,
+                         rc_ciphertext* out, void* stream);
+/* rotate / conjugate: context/rotation.rs:104-135 (the key carries the Galois element) */
+int rc_rotate(rc_context* ctx, const rc_ciphertext* ct, const rc_ksk* rotation_key, rc_ciphertext* out, void* stream);
+/* rotate_raw / conjugate_raw / apply_galois_automorphism on a ciphertext:
+ * src/rns/ciphertexts.rs:36-46,71-78 */
+int rc_automorphism(rc_context* ctx, const rc_ciphertext* ct, uint64_t galois_element, rc_ciphertext* out,
+                    void* stream);
+
+/* ---- batched forms: `count` independent jobs in as few launches as the
+ * (level, key) grouping allows; jobs may mix levels. ---- */
+int rc_mult_relinearized_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* lhs, const rc_ciphertext* rhs,
+                               const rc_ksk* const* keys, rc_ciphertext* out, void* stream);
+int rc_relinearize_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* quadratic, const rc_ksk* const* keys,
+                         rc_ciphertext* out, void* stream);
+int rc_rotate_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* ct, const rc_ksk* const* keys,
+                    rc_ciphertext* out, void* stream);
+
+/* ---- host-buffer entry points (what a CPU-side caller such as the Rust crate
+ * binds): host [2][level+1][N] inputs, host [2][level][N] output, copies
+ * included.  scale bookkeeping as in mult_relinearized. ---- */
+int rc_mult_relinearized_host(rc_context* ctx, const uint64_t* lhs, const uint64_t* rhs, int32_t level,
+                              int32_t scale_bits, const rc_ksk* key, uint64_t* out, int32_t* out_scale_bits,
+                              void* stream);
+int rc_mult_relinearized_batch_host(rc_context* ctx, uint32_t count, const uint64_t* const* lhs,
+                                    const uint64_t* const* rhs, const int32_t* levels, const int32_t* scale_bits,
+                                    const rc_ksk* const* keys, uint64_t* const* out, int32_t* out_scale_bits,
+                                    void* stream);
+
+/* ---- host FP64 helpers (src/rns/encoding.rs, src/math/canonical_embedding.rs) ---- */
+/* encode_integer_coeffs + poly_from_bigint_coeffs: encoding.rs:9-31,
+ * polynomial.rs:78-85.  slots: N/2 complex values as interleaved (re, im). */
+int rc_encode(const rc_context* ctx, const double* slots, int32_t level, uint32_t scale_bits, uint64_t* out_host);
+/* reconstruct_coefficients + decode_integer_coeffs: polynomial.rs:162-201, encoding.rs:33-66 */
+int rc_decode(const rc_context* ctx, const uint64_t* poly_host, int32_t level, uint32_t scale_bits,
+              double* slots_out);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* RNSCKKS_GPU_H */

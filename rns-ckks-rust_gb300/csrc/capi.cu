@@ -1,0 +1,1162 @@
+// C ABI (include/rnsckks_gpu.h): context creation with all precomputed tables,
+// device-resident keys, per-stream scratch and the per-op / batched entry
+// points.  Preconditions that the reference asserts (and panics on) become
+// RC_ERR_INVALID_ARGUMENT with the reference's message.
+#include <cmath>
+#include <cstring>
+#include <string>
+
+#include "context.hpp"
+
+using namespace rc;
+
+namespace rc {
+
+static thread_local std::string g_err;
+
+void cuda_check(cudaError_t e, const char* what) {
+  if (e != cudaSuccess) {
+    if (e == cudaErrorMemoryAllocation) fail(RC_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));
+    fail(RC_ERR_CUDA, std::string(what) + ": " + cudaGetErrorString(e));
+  }
+}
+
+DevBuf::DevBuf(size_t b) : bytes(b) {
+  if (b) cuda_check(cudaMalloc(&p, b), "cudaMalloc");
+}
+DevBuf::~DevBuf() {
+  if (p) cudaFree(p);
+}
+Workspace::~Workspace() {
+  if (host_pinned) cudaFreeHost(host_pinned);
+}
+
+}  // namespace rc
+
+template <class F>
+static int guarded(F&& f) {
+  try {
+    f();
+    return RC_OK;
+  } catch (const ApiError& e) {
+    g_err = e.what();
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    g_err = "host allocation failed";
+    return RC_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception& e) {
+    g_err = e.what();
+    return RC_ERR_CUDA;
+  }
+}
+
+namespace {
+
+typedef unsigned __int128 u128h;
+
+const char* plan_error(uint64_t size, uint64_t q, uint64_t g) {
+  // NttPlan::new checks, src/math/ntt.rs:17-60
+  if (size == 0 || (size & (size - 1))) return "NTT size must be a non-zero power of two";
+  if (q < 3) return "modulus must be an odd prime larger than 2";
+  if ((q - 1) % size) return "size must divide modulus - 1";
+  if ((q - 1) % (2 * size)) return "2 * size must divide modulus - 1 for negacyclic NTTs";
+  uint64_t w = powmod_h(g % q, (q - 1) / size, q);
+  if (powmod_h(w, size, q) != 1) return "primitive_root does not generate a size-th root of unity";
+  if (size > 1 && powmod_h(w, size / 2, q) == 1) return "root is not primitive for the requested size";
+  uint64_t psi = powmod_h(g % q, (q - 1) / (2 * size), q);
+  if (powmod_h(psi, 2 * size, q) != 1 || powmod_h(psi, size, q) != q - 1)
+    return "primitive_root does not generate a valid negacyclic twiddle";
+  return nullptr;
+}
+
+void validate_chain(uint64_t n, const std::vector<uint64_t>& m, const std::vector<uint64_t>& g) {
+  // RnsContext::new, src/rns/basis.rs:32-59
+  require(n != 0 && !(n & (n - 1)), "poly_degree must be a non-zero power of two");
+  require(!m.empty(), "RNS basis must contain at least one prime");
+  for (size_t i = 0; i < m.size(); ++i) {
+    for (size_t j = 0; j < i; ++j) require(m[j] != m[i], "duplicate RNS modulus " + std::to_string(m[i]));
+    const char* e = plan_error(n, m[i], g[i]);
+    if (e) fail(RC_ERR_INVALID_ARGUMENT, "invalid RNS prime " + std::to_string(m[i]) + ": " + e);
+  }
+}
+
+int bitrev(int x, int bits) {
+  int r = 0;
+  for (int i = 0; i < bits; ++i) r |= ((x >> i) & 1) << (bits - 1 - i);
+  return r;
+}
+
+cudaStream_t S(void* s) { return (cudaStream_t)s; }
+
+Workspace& workspace(rc_context* ctx, cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(ctx->mu);
+  auto& w = ctx->ws[s];
+  if (!w) w.reset(new Workspace());
+  return *w;
+}
+
+void* ws_device(rc_context* ctx, cudaStream_t s, size_t bytes) {
+  Workspace& w = workspace(ctx, s);
+  if (!w.dev || w.dev->bytes < bytes) {
+    cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+    cuda_check(cudaStreamIsCapturing(s, &st), "cudaStreamIsCapturing");
+    if (st != cudaStreamCaptureStatusNone)
+      fail(RC_ERR_INVALID_ARGUMENT, "scratch must be reserved (rc_reserve) before CUDA graph capture");
+    cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    w.dev.reset();
+    w.dev.reset(new DevBuf(bytes + (bytes >> 3)));
+  }
+  return w.dev->p;
+}
+
+void launch_check(const char* what) { cuda_check(cudaGetLastError(), what); }
+
+LimbMap qmap(const rc_context* c, int limbs) { return LimbMap{limbs, c->L}; }
+
+size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+struct Arena {
+  char* base;
+  size_t off = 0;
+  explicit Arena(void* b) : base((char*)b) {}
+  template <class T>
+  T* take(size_t count) {
+    off = align_up(off, 256);
+    T* p = (T*)(base + off);
+    off += count * sizeof(T);
+    return p;
+  }
+};
+
+size_t arena_size_u64(size_t count) { return align_up(count * 8, 256); }
+
+const LevelInfo& level_info(const rc_context* c, int limbs) {
+  require(limbs >= 1 && limbs <= c->L, "level out of range for this context");
+  return c->levels[limbs];
+}
+
+int floor_log2(uint64_t q) { return 63 - __builtin_clzll(q); }
+
+// ------------------------------------------------------------------------
+// keyswitch core shared by keyswitch / relinearize / mult_relinearized / rotate
+// ------------------------------------------------------------------------
+struct KsJob {
+  const uint64_t* poly;  // c2 or c1 (device), qlimbs limbs
+  const rc_ksk* key;
+  const uint64_t* add0;  // addend for component 0 (null: none)
+  const uint64_t* add1;
+  uint64_t* out0;
+  uint64_t* out1;
+};
+
+void check_key_for(const rc_context* c, const rc_ksk* key, int qlimbs) {
+  require(key != nullptr, "keyswitch key must not be null");
+  require(key->ctx == c, "keyswitch key belongs to another context");
+  const LevelInfo& li = level_info(c, qlimbs);
+  if (key->aux == 0) {
+    // keyswitch_rns, keyswitching.rs:135-137
+    require(key->level == qlimbs - 1, "keyswitch key level must match the active modulus chain");
+    require((int)key->digits >= li.digits, "keyswitch key must cover the active modulus chain");
+  } else {
+    // keyswitch_rns_hybrid, keyswitching.rs:165-168
+    require(c->K > 0, "hybrid keyswitching requires an eval-key level context");
+    require(key->level == qlimbs - 1, "keyswitch key level must match the active Q chain");
+    require((int)key->aux == c->K, "eval-key context must match the keyswitch key auxiliary basis");
+    require((int)key->digits >= li.digits, "keyswitch key must cover the active modulus chain");
+  }
+}
+
+int ks_digits(const rc_context* c, const rc_ksk* k0, int qlimbs) {
+  // Q-only: the reference decomposes into ksk.ksk.len() digits (keyswitching.rs:138);
+  // hybrid: into the active digit count (167-170)
+  const LevelInfo& li = level_info(c, qlimbs);
+  return (k0 && k0->aux) ? li.digits : (k0 ? std::max((int)k0->digits, 1) : li.digits);
+}
+
+size_t ks_scratch_elems(const rc_context* c, int J, int total, int D) {
+  size_t pairs = (size_t)J * total;
+  size_t chunk = c->scratch_budget / ((size_t)D * c->N * 8);
+  if (chunk < 1) chunk = 1;
+  if (chunk > pairs) chunk = pairs;
+  return chunk * D * c->N;
+}
+
+size_t ks_ws_bytes(const rc_context* c, int J, int qlimbs, int K, int D) {
+  const int total = qlimbs + K;
+  return align_up((size_t)J * D * c->N * 4, 256) + arena_size_u64((size_t)J * 2 * total * c->N) +
+         arena_size_u64(ks_scratch_elems(c, J, total, D)) + 1024;
+}
+
+// Runs keyswitch for `jobs` jobs at `qlimbs` limbs (all keys of the same kind);
+// the result is finalized with addends, optional automorphism on the addend and
+// optional rescale.  g_inv: automorphism applied to the keyswitched polynomial
+// and to addend 0 (rotation), 0 = none.  `ws` holds ks_ws_bytes().
+void keyswitch_core(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, uint64_t g_inv, bool rescale,
+                    void* ws, cudaStream_t s) {
+  if (jobs.empty()) return;
+  const int J = (int)jobs.size();
+  require(J <= MAXP / 2, "internal: keyswitch chunk too large");
+  const rc_ksk* k0 = jobs[0].key;
+  for (auto& j : jobs) check_key_for(c, j.key, qlimbs);
+  const int K = k0->aux ? c->K : 0;
+  const LevelInfo& li = level_info(c, qlimbs);
+  const int D = ks_digits(c, k0, qlimbs);
+  for (auto& j : jobs) {
+    require((j.key->aux ? c->K : 0) == K, "internal: mixed key kinds in one keyswitch batch");
+    if (!K) require((int)j.key->digits == D, "internal: mixed digit counts in one keyswitch batch");
+  }
+  const int N = c->N, total = qlimbs + K;
+  const size_t scratch_elems = ks_scratch_elems(c, J, total, D);
+  Arena ar(ws);
+  int32_t* digits = ar.take<int32_t>((size_t)J * D * N);
+  uint64_t* acc = ar.take<uint64_t>((size_t)J * 2 * total * N);
+  uint64_t* scratch = ar.take<uint64_t>(scratch_elems);
+
+  PtrTab src{};
+  for (int j = 0; j < J; ++j) src.p[j] = const_cast<uint64_t*>(jobs[j].poly);
+  decompose(c->d_pc, li.dt, src, J, qlimbs, D, digits, g_inv, c->log_n, s);
+  launch_check("decompose");
+
+  KsArgs ka;
+  ka.pc = c->d_pc;
+  ka.ntt = c->ntt();
+  ka.n = N;
+  ka.L = c->L;
+  ka.qlimbs = qlimbs;
+  ka.K = K;
+  ka.D = D;
+  ka.key_digits = (int)k0->digits;
+  ka.dt = &li.dt;
+  std::vector<const uint64_t*> keys(J);
+  for (int j = 0; j < J; ++j) keys[j] = jobs[j].key->data;
+  digit_ntt_mac(ka, digits, keys.data(), J, acc, scratch, scratch_elems, s);
+  launch_check("digit_ntt_mac");
+
+  // back to coefficient form: 2*J polys of `total` limbs
+  PtrTab t{};
+  for (int p = 0; p < 2 * J; ++p) t.p[p] = acc + (size_t)p * total * N;
+  ntt_inverse(c->ntt(), t, t, 2 * J, total, LimbMap{qlimbs, c->L}, s);
+  launch_check("ntt_inverse(acc)");
+
+  FinalizeArgs f;
+  f.pc = c->d_pc;
+  f.md = c->md;
+  f.rt = c->rt;
+  f.L = c->L;
+  f.n = N;
+  f.log_n = c->log_n;
+  f.qlimbs = qlimbs;
+  f.K = K;
+  f.rescale = rescale ? 1 : 0;
+  f.add_g_inv = g_inv;
+  PtrTab add{}, out{};
+  for (int j = 0; j < J; ++j) {
+    add.p[2 * j] = const_cast<uint64_t*>(jobs[j].add0);
+    add.p[2 * j + 1] = const_cast<uint64_t*>(jobs[j].add1);
+    out.p[2 * j] = jobs[j].out0;
+    out.p[2 * j + 1] = jobs[j].out1;
+  }
+  finalize(f, acc, add, out, J, s);
+  launch_check("finalize");
+}
+
+// single-call keyswitch with its own workspace
+void keyswitch_run(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, uint64_t g_inv, bool rescale,
+                   cudaStream_t s) {
+  if (jobs.empty()) return;
+  const rc_ksk* k0 = jobs[0].key;
+  check_key_for(c, k0, qlimbs);
+  const int K = k0->aux ? c->K : 0;
+  void* ws = ws_device(c, s, ks_ws_bytes(c, (int)jobs.size(), qlimbs, K, ks_digits(c, k0, qlimbs)));
+  keyswitch_core(c, jobs, qlimbs, g_inv, rescale, ws, s);
+}
+
+size_t tensor_ws_bytes(const rc_context* c, int J, int limbs) {
+  return arena_size_u64((size_t)4 * J * limbs * c->N) + 512;
+}
+
+// tensor for J jobs at `limbs` limbs; writes coefficient-form (d0,d1,d2) to
+// quad[j] (3 polys contiguous).  `ws` holds tensor_ws_bytes().
+void tensor_core(rc_context* c, const std::vector<const uint64_t*>& lhs, const std::vector<const uint64_t*>& rhs,
+                 const std::vector<uint64_t*>& quad, int limbs, void* ws, cudaStream_t s) {
+  const int J = (int)lhs.size();
+  if (!J) return;
+  require(4 * J <= MAXP, "internal: tensor chunk too large");
+  const size_t pl = (size_t)limbs * c->N;
+  Arena ar(ws);
+  uint64_t* fw = ar.take<uint64_t>(4 * J * pl);
+  PtrTab src{}, dst{};
+  for (int j = 0; j < J; ++j) {
+    src.p[4 * j + 0] = const_cast<uint64_t*>(lhs[j]);
+    src.p[4 * j + 1] = const_cast<uint64_t*>(lhs[j]) + pl;
+    src.p[4 * j + 2] = const_cast<uint64_t*>(rhs[j]);
+    src.p[4 * j + 3] = const_cast<uint64_t*>(rhs[j]) + pl;
+    for (int k = 0; k < 4; ++k) dst.p[4 * j + k] = fw + (4 * j + k) * pl;
+  }
+  ntt_forward(c->ntt(), src, dst, 4 * J, limbs, qmap(c, limbs), s);
+  launch_check("ntt_forward(tensor)");
+  PtrTab o3{};
+  for (int j = 0; j < J; ++j)
+    for (int k = 0; k < 3; ++k) o3.p[3 * j + k] = quad[j] + k * pl;
+  tensor_ntt(c->d_pc, dst, o3, J, limbs, c->N, s);
+  launch_check("tensor");
+  ntt_inverse(c->ntt(), o3, o3, 3 * J, limbs, qmap(c, limbs), s);
+  launch_check("ntt_inverse(tensor)");
+}
+
+void check_ct(const rc_context* c, const rc_ciphertext* ct, const char* name) {
+  require(ct != nullptr && ct->data != nullptr, std::string(name) + " must not be null");
+  require(ct->level >= 0 && ct->level < c->L, std::string(name) + " level out of range for this context");
+}
+
+uint64_t galois_inverse(const rc_context* c, uint64_t g) {
+  const uint64_t m = 2ull * c->N;
+  require(g % 2 == 1, "galois automorphisms require an odd exponent");
+  return invmod_h(g % m, m);
+}
+
+size_t mult_relin_ws_bytes(const rc_context* c, int J, int limbs, const rc_ksk* k0) {
+  const int K = k0 && k0->aux ? c->K : 0;
+  const size_t pl = (size_t)limbs * c->N;
+  return align_up(std::max(ks_ws_bytes(c, J, limbs, K, ks_digits(c, k0, limbs)), tensor_ws_bytes(c, J, limbs)),
+                  256) +
+         arena_size_u64((size_t)3 * J * pl) + 256;
+}
+
+// mult_relinearized for a same-level, same-key-kind group (chunked to fit the
+// pointer tables): tensor into quads at the end of the workspace, then
+// keyswitch(c2) + add (c0, c1) + rescale in the fused finalize.
+void mult_relin_group(rc_context* c, const std::vector<int>& idx, const rc_ciphertext* lhs, const rc_ciphertext* rhs,
+                      const rc_ksk* const* keys, rc_ciphertext* out, cudaStream_t s) {
+  const int limbs = lhs[idx[0]].level + 1;
+  require(limbs > 1, "rescale requires at least two levels");
+  const size_t pl = (size_t)limbs * c->N;
+  const int CH = MAXP / 4;
+  for (size_t b = 0; b < idx.size(); b += CH) {
+    const int J = (int)std::min<size_t>(CH, idx.size() - b);
+    std::vector<const uint64_t*> Lp(J), Rp(J);
+    std::vector<KsJob> jobs(J);
+    for (int j = 0; j < J; ++j) {
+      Lp[j] = lhs[idx[b + j]].data;
+      Rp[j] = rhs[idx[b + j]].data;
+      require(keys[idx[b + j]] != nullptr, "keyswitch key must not be null");
+      check_key_for(c, keys[idx[b + j]], limbs);
+    }
+    const rc_ksk* k0 = keys[idx[b]];
+    const int K = k0->aux ? c->K : 0;
+    const size_t head = align_up(
+        std::max(ks_ws_bytes(c, J, limbs, K, ks_digits(c, k0, limbs)), tensor_ws_bytes(c, J, limbs)), 256);
+    char* ws = (char*)ws_device(c, s, mult_relin_ws_bytes(c, J, limbs, k0));
+    uint64_t* quad = (uint64_t*)(ws + head);
+    std::vector<uint64_t*> Q(J);
+    for (int j = 0; j < J; ++j) Q[j] = quad + (size_t)j * 3 * pl;
+    tensor_core(c, Lp, Rp, Q, limbs, ws, s);
+    for (int j = 0; j < J; ++j) {
+      const int i = idx[b + j];
+      jobs[j].poly = Q[j] + 2 * pl;
+      jobs[j].key = keys[i];
+      jobs[j].add0 = Q[j];
+      jobs[j].add1 = Q[j] + pl;
+      jobs[j].out0 = out[i].data;
+      jobs[j].out1 = out[i].data + (size_t)(limbs - 1) * c->N;
+    }
+    keyswitch_core(c, jobs, limbs, 0, true, ws, s);
+    for (int j = 0; j < J; ++j) {
+      const int i = idx[b + j];
+      const int sb = lhs[i].scale_bits + rhs[i].scale_bits - floor_log2(c->mod[limbs - 1]);
+      out[i].level = lhs[i].level - 1;
+      out[i].scale_bits = sb < 0 ? 0 : sb;
+    }
+  }
+}
+
+void check_mult_pair(const rc_context* c, const rc_ciphertext* a, const rc_ciphertext* b) {
+  check_ct(c, a, "lhs");
+  check_ct(c, b, "rhs");
+  // RnsCkksContext::mult, context/ops.rs:64-65
+  require(a->level == b->level, "ciphertexts must be at the same level to multiply");
+  require(a->scale_bits == b->scale_bits, "ciphertexts must share the same scale to multiply");
+}
+
+}  // namespace
+
+// =========================================================================
+// context
+// =========================================================================
+extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
+  return guarded([&] {
+    require(p != nullptr && out != nullptr, "params and out must not be null");
+    *out = nullptr;
+    // RnsCkksParams::validate, src/rns/context/params.rs:48-73
+    require(p->scale_bits != 0, "scale_bits must be greater than zero");
+    require(p->scale_bits < 60, "scale_bits must stay below 60 bits per rescale step in this RNS scaffold");
+    std::vector<uint64_t> qm, qg, pm, pg;
+    for (uint32_t i = 0; i < p->prime_count; ++i) {
+      qm.push_back(p->primes[i].modulus);
+      qg.push_back(p->primes[i].primitive_root);
+    }
+    for (uint32_t i = 0; i < p->aux_count; ++i) {
+      pm.push_back(p->aux_primes[i].modulus);
+      pg.push_back(p->aux_primes[i].primitive_root);
+    }
+    for (uint64_t a : pm)
+      for (uint64_t q : qm)
+        require(a != q, "auxiliary eval-key modulus " + std::to_string(a) +
+                            " must be distinct from the ciphertext modulus chain");
+    validate_chain(p->poly_degree, qm, qg);
+    if (!pm.empty()) {
+      validate_chain(p->poly_degree, pm, pg);
+      std::vector<uint64_t> all = qm, allg = qg;
+      all.insert(all.end(), pm.begin(), pm.end());
+      allg.insert(allg.end(), pg.begin(), pg.end());
+      validate_chain(p->poly_degree, all, allg);
+    }
+    // limits of this implementation
+    const uint64_t N = p->poly_degree;
+    if (N < 2 || N > (1u << 17)) fail(RC_ERR_UNSUPPORTED, "poly_degree must be in 2..=131072 on the GPU path");
+    if (qm.size() > 64) fail(RC_ERR_UNSUPPORTED, "at most 64 ciphertext primes on the GPU path");
+    if (pm.size() > 8) fail(RC_ERR_UNSUPPORTED, "at most 8 auxiliary primes on the GPU path");
+    for (uint64_t q : qm)
+      if (q >= (1ull << 61)) fail(RC_ERR_UNSUPPORTED, "primes must be below 2^61 on the GPU path");
+    for (uint64_t q : pm)
+      if (q >= (1ull << 61)) fail(RC_ERR_UNSUPPORTED, "primes must be below 2^61 on the GPU path");
+
+    std::unique_ptr<rc_context> c(new rc_context());
+    cuda_check(cudaGetDevice(&c->device), "cudaGetDevice");
+    c->N = (int)N;
+    c->log_n = __builtin_ctzll(N);
+    c->n1 = c->log_n / 2;
+    c->L = (int)qm.size();
+    c->K = (int)pm.size();
+    c->scale_bits = (int)p->scale_bits;
+    c->mod = qm;
+    c->mod.insert(c->mod.end(), pm.begin(), pm.end());
+    c->root = qg;
+    c->root.insert(c->root.end(), pg.begin(), pg.end());
+    const int P = c->L + c->K;
+
+    // ---- per-prime constants and twiddles
+    std::vector<PrimeConst> pcs(P);
+    std::vector<Twiddle> twf((size_t)P * N), twi((size_t)P * N);
+    for (int i = 0; i < P; ++i) {
+      const uint64_t q = c->mod[i];
+      PrimeConst& k = pcs[i];
+      memset(&k, 0, sizeof(k));
+      k.q = q;
+      k.two_q = 2 * q;
+      u128h mu = (~(u128h)0) / q;
+      k.mu_hi = (uint64_t)(mu >> 64);
+      k.mu_lo = (uint64_t)mu;
+      uint64_t inv = q;  // Newton iteration for q^-1 mod 2^64
+      for (int it = 0; it < 6; ++it) inv *= 2 - q * inv;
+      k.qinv_neg = (uint64_t)0 - inv;
+      k.n_inv = invmod_h(N % q, q);
+      k.n_inv_s = shoup_h(k.n_inv, q);
+      k.r2 = (uint64_t)((((u128h)1 << 64) % q) * (((u128h)1 << 64) % q) % q);
+      k.mac_chunk = (uint64_t)(~0ull / q) - 1;
+      // psi = g^((q-1)/2N) (NttPlan::new, ntt.rs:42)
+      const uint64_t psi = powmod_h(c->root[i] % q, (q - 1) / (2 * N), q);
+      const uint64_t psi_inv = invmod_h(psi, q);
+      std::vector<uint64_t> pw(N), pwi(N);
+      pw[0] = pwi[0] = 1;
+      for (uint64_t e = 1; e < N; ++e) {
+        pw[e] = mulmod_h(pw[e - 1], psi, q);
+        pwi[e] = mulmod_h(pwi[e - 1], psi_inv, q);
+      }
+      for (uint64_t kk = 0; kk < N; ++kk) {
+        int e = bitrev((int)kk, c->log_n);
+        Twiddle& f = twf[(size_t)i * N + kk];
+        f.w = pw[e];
+        f.ws = shoup_h(f.w, q);
+        Twiddle& g = twi[(size_t)i * N + kk];
+        g.w = pwi[e];
+        g.ws = shoup_h(g.w, q);
+      }
+    }
+    c->pc_buf.reset(new DevBuf(sizeof(PrimeConst) * P));
+    c->d_pc = (PrimeConst*)c->pc_buf->p;
+    cuda_check(cudaMemcpy(c->d_pc, pcs.data(), sizeof(PrimeConst) * P, cudaMemcpyHostToDevice), "upload consts");
+    c->tw_buf.reset(new DevBuf(sizeof(Twiddle) * 2 * P * N));
+    c->d_twf = (Twiddle*)c->tw_buf->p;
+    c->d_twi = c->d_twf + (size_t)P * N;
+    cuda_check(cudaMemcpy(c->d_twf, twf.data(), sizeof(Twiddle) * P * N, cudaMemcpyHostToDevice), "upload tw");
+    cuda_check(cudaMemcpy(c->d_twi, twi.data(), sizeof(Twiddle) * P * N, cudaMemcpyHostToDevice), "upload tw");
+
+    // ---- per-level decomposition tables
+    c->levels.resize(c->L + 1);
+    for (int l = 1; l <= c->L; ++l) {
+      LevelInfo& li = c->levels[l];
+      li.limbs = l;
+      BigU Q = product(qm, 0, l);
+      li.bits = Q.bits();
+      li.digits = (int)((li.bits + 29) / 30);
+      const int W = (int)((li.bits + 8 + 63) / 64);
+      std::vector<uint64_t> blob;  // [qhat l*W][qinv l][qinv_s l][invq l][Q W][halfQ W]
+      blob.reserve((size_t)l * W + 3 * l + 2 * W);
+      for (int i = 0; i < l; ++i) {
+        auto w = Q.div_u64(qm[i]).words(W);
+        blob.insert(blob.end(), w.begin(), w.end());
+      }
+      size_t o_qinv = blob.size();
+      for (int i = 0; i < l; ++i) blob.push_back(invmod_h(Q.div_u64(qm[i]).mod_u64(qm[i]), qm[i]));
+      size_t o_qinv_s = blob.size();
+      for (int i = 0; i < l; ++i) blob.push_back(shoup_h(blob[o_qinv + i], qm[i]));
+      size_t o_invq = blob.size();
+      for (int i = 0; i < l; ++i) {
+        double d = 1.0 / (double)qm[i];
+        uint64_t bits;
+        memcpy(&bits, &d, 8);
+        blob.push_back(bits);
+      }
+      size_t o_Q = blob.size();
+      auto qw = Q.words(W);
+      blob.insert(blob.end(), qw.begin(), qw.end());
+      size_t o_hQ = blob.size();
+      auto hw = Q.shr1().words(W);
+      blob.insert(blob.end(), hw.begin(), hw.end());
+      li.buf.reset(new DevBuf(blob.size() * 8));
+      uint64_t* d = (uint64_t*)li.buf->p;
+      cuda_check(cudaMemcpy(d, blob.data(), blob.size() * 8, cudaMemcpyHostToDevice), "upload level tables");
+      li.dt.qhat = d;
+      li.dt.qhat_inv = d + o_qinv;
+      li.dt.qhat_inv_s = d + o_qinv_s;
+      li.dt.inv_q = (const double*)(d + o_invq);
+      li.dt.Q = d + o_Q;
+      li.dt.halfQ = d + o_hQ;
+      li.dt.W = W;
+      li.dt.small_q = li.bits <= 30 ? 1 : 0;
+      li.dt.Qsmall = li.bits <= 63 ? Q.words(1)[0] : 0;
+    }
+
+    // ---- ModDown tables (aux basis)
+    {
+      const int K = c->K, L = c->L;
+      std::vector<uint64_t> blob;
+      size_t o_pg = 0, o_pgs, o_half, o_pinv, o_pinvs, o_pmod, o_mk, o_mks;
+      int KW = 0;
+      if (K > 0) {
+        for (int k = 0; k < K; ++k)
+          for (int t = 0; t < K; ++t) blob.push_back(t < k ? invmod_h(pm[t] % pm[k], pm[k]) : 0);
+        o_pgs = blob.size();
+        for (int k = 0; k < K; ++k)
+          for (int t = 0; t < K; ++t) blob.push_back(shoup_h(blob[k * K + t], pm[k]));
+        BigU Pb = product(pm, 0, K);
+        KW = (int)Pb.w.size();
+        o_half = blob.size();
+        auto hw = Pb.shr1().words(8);
+        blob.insert(blob.end(), hw.begin(), hw.end());
+        o_pinv = blob.size();
+        for (int i = 0; i < L; ++i) blob.push_back(invmod_h(Pb.mod_u64(qm[i]), qm[i]));
+        o_pinvs = blob.size();
+        for (int i = 0; i < L; ++i) blob.push_back(shoup_h(blob[o_pinv + i], qm[i]));
+        o_pmod = blob.size();
+        for (int i = 0; i < L; ++i) blob.push_back(Pb.mod_u64(qm[i]));
+        o_mk = blob.size();
+        for (int i = 0; i < L; ++i)
+          for (int k = 0; k < K; ++k) blob.push_back(product(pm, 0, k).mod_u64(qm[i]));
+        o_mks = blob.size();
+        for (int i = 0; i < L; ++i)
+          for (int k = 0; k < K; ++k) blob.push_back(shoup_h(blob[o_mk + (size_t)i * K + k], qm[i]));
+        c->md_buf.reset(new DevBuf(blob.size() * 8));
+        uint64_t* d = (uint64_t*)c->md_buf->p;
+        cuda_check(cudaMemcpy(d, blob.data(), blob.size() * 8, cudaMemcpyHostToDevice), "upload moddown tables");
+        c->md.p_garner = d + o_pg;
+        c->md.p_garner_s = d + o_pgs;
+        c->md.halfP = d + o_half;
+        c->md.KW = KW;
+        c->md.pinv = d + o_pinv;
+        c->md.pinv_s = d + o_pinvs;
+        c->md.pmod = d + o_pmod;
+        c->md.mk = d + o_mk;
+        c->md.mk_s = d + o_mks;
+      }
+    }
+    // ---- rescale tables: inv[l*L + i] = q_l^-1 mod q_i (i < l)
+    {
+      const int L = c->L;
+      std::vector<uint64_t> blob((size_t)2 * L * L, 0);
+      for (int l = 0; l < L; ++l)
+        for (int i = 0; i < l; ++i) {
+          uint64_t v = invmod_h(qm[l] % qm[i], qm[i]);
+          blob[(size_t)l * L + i] = v;
+          blob[(size_t)L * L + (size_t)l * L + i] = shoup_h(v, qm[i]);
+        }
+      c->rt_buf.reset(new DevBuf(blob.size() * 8));
+      uint64_t* d = (uint64_t*)c->rt_buf->p;
+      cuda_check(cudaMemcpy(d, blob.data(), blob.size() * 8, cudaMemcpyHostToDevice), "upload rescale tables");
+      c->rt.inv = d;
+      c->rt.inv_s = d + (size_t)L * L;
+    }
+    cuda_check(cudaDeviceSynchronize(), "context setup");
+    *out = c.release();
+  });
+}
+
+extern "C" void rc_context_destroy(rc_context* ctx) {
+  if (!ctx) return;
+  cudaDeviceSynchronize();
+  delete ctx;
+}
+
+extern "C" const char* rc_last_error(const rc_context*) { return g_err.c_str(); }
+
+extern "C" int rc_context_info(const rc_context* c, uint64_t* n, uint32_t* levels, uint32_t* aux, uint32_t* sb) {
+  return guarded([&] {
+    require(c != nullptr, "context must not be null");
+    if (n) *n = (uint64_t)c->N;
+    if (levels) *levels = (uint32_t)c->L;
+    if (aux) *aux = (uint32_t)c->K;
+    if (sb) *sb = (uint32_t)c->scale_bits;
+  });
+}
+
+extern "C" int rc_decomp_digits(const rc_context* c, int32_t level, uint32_t* digits) {
+  return guarded([&] {
+    require(c != nullptr && digits != nullptr, "arguments must not be null");
+    *digits = (uint32_t)level_info(c, level + 1).digits;
+  });
+}
+
+extern "C" int rc_reserve(rc_context* c, int32_t max_level, uint32_t max_batch, void* stream) {
+  return guarded([&] {
+    require(c != nullptr, "context must not be null");
+    const int limbs = max_level + 1;
+    const LevelInfo& li = level_info(c, limbs);
+    const int J = (int)std::min<uint32_t>(max_batch ? max_batch : 1, MAXP / 4);
+    const int D = li.digits + 4;
+    const size_t pl = (size_t)limbs * c->N;
+    size_t need = align_up(std::max(ks_ws_bytes(c, J, limbs, c->K, D), tensor_ws_bytes(c, J, limbs)), 256) +
+                  arena_size_u64((size_t)3 * J * pl) + 256;
+    ws_device(c, S(stream), need);
+  });
+}
+
+// =========================================================================
+// keys
+// =========================================================================
+static int ksk_upload_impl(rc_context* c, const uint64_t* key, bool on_device, uint32_t digits, int32_t level,
+                           uint32_t aux_count, uint64_t galois_element, rc_ksk** out) {
+  return guarded([&] {
+    require(c && key && out, "arguments must not be null");
+    *out = nullptr;
+    require(level >= 0 && level < c->L, "keyswitch key level out of range for this context");
+    require(aux_count == 0 || (int)aux_count == c->K, "eval-key context must match the keyswitch key auxiliary basis");
+    require(digits >= 1, "keyswitch key must have at least one digit");
+    if (galois_element) galois_inverse(c, galois_element);
+    const int limbs = level + 1 + (int)aux_count;
+    const size_t elems = (size_t)digits * 2 * limbs * c->N;
+    DevBuf tmp(elems * 8);
+    std::shared_ptr<DevBuf> fin(new DevBuf(elems * 8));
+    cuda_check(cudaMemcpy(tmp.p, key, elems * 8, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice),
+               "key upload");
+    const LimbMap map{level + 1, c->L};
+    uint64_t* t = (uint64_t*)tmp.p;
+    const int polys = (int)digits * 2;
+    for (int p0 = 0; p0 < polys; p0 += MAXP) {
+      PtrTab tab{};
+      const int cnt = std::min(MAXP, polys - p0);
+      for (int k = 0; k < cnt; ++k) tab.p[k] = t + (size_t)(p0 + k) * limbs * c->N;
+      ntt_forward(c->ntt(), tab, tab, cnt, limbs, map, 0);
+      launch_check("key ntt");
+    }
+    key_to_device_form(c->ntt(), c->d_pc, t, (uint64_t*)fin->p, (int)digits, limbs, map, c->N, 0);
+    launch_check("key relayout");
+    cuda_check(cudaDeviceSynchronize(), "key upload");
+    rc_ksk* k = new rc_ksk();
+    k->ctx = c;
+    k->buf = fin;
+    k->data = (uint64_t*)fin->p;
+    k->digits = digits;
+    k->level = level;
+    k->aux = aux_count;
+    k->galois = galois_element;
+    *out = k;
+  });
+}
+
+extern "C" int rc_ksk_upload(rc_context* c, const uint64_t* host_key, uint32_t digits, int32_t level,
+                             uint32_t aux_count, uint64_t galois_element, rc_ksk** out) {
+  return ksk_upload_impl(c, host_key, false, digits, level, aux_count, galois_element, out);
+}
+
+extern "C" int rc_ksk_upload_device(rc_context* c, const uint64_t* dev_key, uint32_t digits, int32_t level,
+                                    uint32_t aux_count, uint64_t galois_element, rc_ksk** out) {
+  return ksk_upload_impl(c, dev_key, true, digits, level, aux_count, galois_element, out);
+}
+
+extern "C" int rc_ksk_truncate(rc_context* c, const rc_ksk* key, int32_t level, rc_ksk** out) {
+  return guarded([&] {
+    require(c && key && out, "arguments must not be null");
+    // RnsKeySwitchingKey::truncate_levels / drop_last_level, keyswitching.rs:21-41
+    require(level + 1 > 0, "level_count must be positive");
+    require(level <= key->level, "level_count cannot exceed keyswitch levels");
+    require(level == key->level || key->aux == 0, "dropping levels is only supported for Q-only keyswitch keys");
+    rc_ksk* k = new rc_ksk(*key);
+    k->level = level;  // limb-major layout: the first level+1 limbs are the truncated key
+    *out = k;
+  });
+}
+
+extern "C" int rc_ksk_info(const rc_ksk* k, uint32_t* digits, int32_t* level, uint32_t* aux, uint64_t* g) {
+  if (!k) return RC_ERR_INVALID_ARGUMENT;
+  if (digits) *digits = k->digits;
+  if (level) *level = k->level;
+  if (aux) *aux = k->aux;
+  if (g) *g = k->galois;
+  return RC_OK;
+}
+
+extern "C" void rc_ksk_destroy(rc_ksk* k) { delete k; }
+
+// =========================================================================
+// polynomial ops
+// =========================================================================
+static int ntt_entry(rc_context* c, uint64_t* data, uint32_t polys, uint32_t limbs, int32_t with_aux, void* stream,
+                     bool forward) {
+  return guarded([&] {
+    require(c && data, "arguments must not be null");
+    LimbMap map{(int)limbs, c->L};
+    if (with_aux) {
+      require((int)limbs > c->K && (int)limbs - c->K <= c->L, "limb count out of range for the extended basis");
+      map.qcount = (int)limbs - c->K;
+    } else {
+      require(limbs >= 1 && (int)limbs <= c->L, "limb count out of range for this context");
+    }
+    for (uint32_t p0 = 0; p0 < polys; p0 += MAXP) {
+      const int cnt = (int)std::min<uint32_t>(MAXP, polys - p0);
+      PtrTab t{};
+      for (int k = 0; k < cnt; ++k) t.p[k] = data + (size_t)(p0 + k) * limbs * c->N;
+      if (forward) ntt_forward(c->ntt(), t, t, cnt, (int)limbs, map, S(stream));
+      else ntt_inverse(c->ntt(), t, t, cnt, (int)limbs, map, S(stream));
+      launch_check("ntt");
+    }
+  });
+}
+
+extern "C" int rc_ntt_forward(rc_context* c, uint64_t* d, uint32_t polys, uint32_t limbs, int32_t aux, void* s) {
+  return ntt_entry(c, d, polys, limbs, aux, s, true);
+}
+extern "C" int rc_ntt_inverse(rc_context* c, uint64_t* d, uint32_t polys, uint32_t limbs, int32_t aux, void* s) {
+  return ntt_entry(c, d, polys, limbs, aux, s, false);
+}
+
+static LimbMap basis_map(const rc_context* c, uint32_t limbs, int32_t with_aux) {
+  if (with_aux) {
+    require(c->K > 0, "eval-key level context requires an auxiliary basis");
+    require((int)limbs > c->K && (int)limbs - c->K <= c->L, "limb count out of range for the extended basis");
+    return LimbMap{(int)limbs - c->K, c->L};
+  }
+  require(limbs >= 1 && (int)limbs <= c->L, "context level count must match polynomial levels");
+  return LimbMap{(int)limbs, c->L};
+}
+
+extern "C" int rc_poly_multiply(rc_context* c, const uint64_t* a, const uint64_t* b, uint64_t* out, uint32_t limbs,
+                                int32_t with_aux, void* stream) {
+  return guarded([&] {
+    require(c && a && b && out, "arguments must not be null");
+    const LimbMap map = basis_map(c, limbs, with_aux);
+    cudaStream_t s = S(stream);
+    const size_t pl = (size_t)limbs * c->N;
+    Arena ar(ws_device(c, s, 2 * arena_size_u64(pl) + 512));
+    uint64_t* ta = ar.take<uint64_t>(pl);
+    uint64_t* tb = ar.take<uint64_t>(pl);
+    PtrTab src{}, dst{};
+    src.p[0] = const_cast<uint64_t*>(a);
+    src.p[1] = const_cast<uint64_t*>(b);
+    dst.p[0] = ta;
+    dst.p[1] = tb;
+    ntt_forward(c->ntt(), src, dst, 2, (int)limbs, map, s);
+    PtrTab x{}, y{};
+    x.p[0] = ta;
+    y.p[0] = tb;
+    ew_binary(EwOp::Mul, c->d_pc, x, y, 0, x, 1, (int)limbs, map, c->N, s);
+    PtrTab o{};
+    o.p[0] = out;
+    ntt_inverse(c->ntt(), x, o, 1, (int)limbs, map, s);
+    launch_check("poly_multiply");
+  });
+}
+
+static int poly_binary(rc_context* c, const uint64_t* a, const uint64_t* b, uint64_t* out, uint32_t limbs,
+                       int32_t with_aux, void* stream, EwOp op) {
+  return guarded([&] {
+    require(c && a && b && out, "arguments must not be null");
+    const LimbMap map = basis_map(c, limbs, with_aux);
+    PtrTab x{}, y{}, o{};
+    x.p[0] = const_cast<uint64_t*>(a);
+    y.p[0] = const_cast<uint64_t*>(b);
+    o.p[0] = out;
+    ew_binary(op, c->d_pc, x, y, 0, o, 1, (int)limbs, map, c->N, S(stream));
+    launch_check("poly add/sub");
+  });
+}
+extern "C" int rc_poly_add(rc_context* c, const uint64_t* a, const uint64_t* b, uint64_t* o, uint32_t l,
+                           int32_t aux, void* s) {
+  return poly_binary(c, a, b, o, l, aux, s, EwOp::Add);
+}
+extern "C" int rc_poly_sub(rc_context* c, const uint64_t* a, const uint64_t* b, uint64_t* o, uint32_t l,
+                           int32_t aux, void* s) {
+  return poly_binary(c, a, b, o, l, aux, s, EwOp::Sub);
+}
+
+extern "C" int rc_poly_mul_scalar(rc_context* c, const uint64_t* a, const uint64_t* scalars, uint64_t* out,
+                                  uint32_t limbs, int32_t with_aux, void* stream) {
+  return guarded([&] {
+    require(c && a && scalars && out, "arguments must not be null");
+    const LimbMap map = basis_map(c, limbs, with_aux);
+    ScalarTab st{};
+    require(limbs <= (uint32_t)(sizeof(st.v) / sizeof(st.v[0])), "too many limbs for a scalar product");
+    for (uint32_t j = 0; j < limbs; ++j) st.v[j] = scalars[j] % c->mod[map.prime((int)j)];
+    mul_scalar(c->d_pc, a, st, out, (int)limbs, map, c->N, S(stream));
+    launch_check("poly_mul_scalar");
+  });
+}
+
+extern "C" int rc_poly_automorphism(rc_context* c, const uint64_t* a, uint64_t* out, uint32_t limbs, uint64_t g,
+                                    void* stream) {
+  return guarded([&] {
+    require(c && a && out, "arguments must not be null");
+    require(limbs >= 1 && (int)limbs <= c->L, "limb count out of range for this context");
+    require(a != out, "automorphism output must not alias its input");
+    require(g < 2ull * c->N, "galois element must be reduced modulo 2N");
+    const uint64_t gi = galois_inverse(c, g);
+    PtrTab x{}, o{};
+    x.p[0] = const_cast<uint64_t*>(a);
+    o.p[0] = out;
+    automorphism(c->d_pc, x, o, 1, (int)limbs, gi, c->log_n, S(stream));
+    launch_check("automorphism");
+  });
+}
+
+// =========================================================================
+// ciphertext ops
+// =========================================================================
+extern "C" int rc_add(rc_context* c, const rc_ciphertext* a, const rc_ciphertext* b, rc_ciphertext* out,
+                      void* stream) {
+  return guarded([&] {
+    require(c && out && out->data, "arguments must not be null");
+    check_ct(c, a, "lhs");
+    check_ct(c, b, "rhs");
+    // RnsCiphertext::add, ciphertexts.rs:60-62
+    require(a->scale_bits == b->scale_bits, "ciphertexts must share the same scale to add");
+    require(a->level == b->level, "ciphertexts must be at the same level to add");
+    const int limbs = a->level + 1;
+    const size_t pl = (size_t)limbs * c->N;
+    PtrTab x{}, y{}, o{};
+    for (int k = 0; k < 2; ++k) {
+      x.p[k] = a->data + k * pl;
+      y.p[k] = b->data + k * pl;
+      o.p[k] = out->data + k * pl;
+    }
+    ew_binary(EwOp::Add, c->d_pc, x, y, 0, o, 2, limbs, qmap(c, limbs), c->N, S(stream));
+    launch_check("add");
+    out->level = a->level;
+    out->scale_bits = a->scale_bits;
+  });
+}
+
+static void mult_plain_impl(rc_context* c, const rc_ciphertext* ct, const uint64_t* plain, rc_ciphertext* out,
+                            cudaStream_t s) {
+  require(c && out && out->data && plain, "arguments must not be null");
+  check_ct(c, ct, "ciphertext");
+  const int limbs = ct->level + 1;
+  const size_t pl = (size_t)limbs * c->N;
+  Arena ar(ws_device(c, s, 3 * arena_size_u64(pl) + 1024));
+  uint64_t* f = ar.take<uint64_t>(3 * pl);
+  PtrTab src{}, dst{};
+  src.p[0] = ct->data;
+  src.p[1] = ct->data + pl;
+  src.p[2] = const_cast<uint64_t*>(plain);
+  for (int k = 0; k < 3; ++k) dst.p[k] = f + k * pl;
+  ntt_forward(c->ntt(), src, dst, 3, limbs, qmap(c, limbs), s);
+  PtrTab a{}, b{};
+  a.p[0] = f;
+  a.p[1] = f + pl;
+  b.p[0] = f + 2 * pl;
+  ew_binary(EwOp::Mul, c->d_pc, a, b, 1, a, 2, limbs, qmap(c, limbs), c->N, s);
+  PtrTab o{};
+  o.p[0] = out->data;
+  o.p[1] = out->data + pl;
+  ntt_inverse(c->ntt(), a, o, 2, limbs, qmap(c, limbs), s);
+  launch_check("mult_plain");
+  out->level = ct->level;
+}
+
+extern "C" int rc_mult_plain(rc_context* c, const rc_ciphertext* ct, const uint64_t* plain, rc_ciphertext* out,
+                             void* stream) {
+  return guarded([&] {
+    const int sb = ct ? ct->scale_bits : 0;
+    mult_plain_impl(c, ct, plain, out, S(stream));
+    out->scale_bits = sb + sb;  // context/ops.rs:24-29
+  });
+}
+
+extern "C" int rc_multiply_plain_rns(rc_context* c, const rc_ciphertext* ct, const uint64_t* plain,
+                                     rc_ciphertext* out, void* stream) {
+  return guarded([&] {
+    const int sb = ct ? ct->scale_bits : 0;
+    mult_plain_impl(c, ct, plain, out, S(stream));
+    out->scale_bits = sb;
+  });
+}
+
+extern "C" int rc_mult(rc_context* c, const rc_ciphertext* a, const rc_ciphertext* b, rc_ciphertext* out,
+                       void* stream) {
+  return guarded([&] {
+    require(c && out && out->data, "arguments must not be null");
+    check_mult_pair(c, a, b);
+    const int limbs = a->level + 1;
+    void* ws = ws_device(c, S(stream), tensor_ws_bytes(c, 1, limbs));
+    tensor_core(c, {a->data}, {b->data}, {out->data}, limbs, ws, S(stream));
+    out->level = a->level;
+    out->scale_bits = a->scale_bits + b->scale_bits;
+  });
+}
+
+static void rescale_impl(rc_context* c, const rc_ciphertext* ct, rc_ciphertext* out, int comps, cudaStream_t s) {
+  require(c && out && out->data, "arguments must not be null");
+  check_ct(c, ct, "ciphertext");
+  const int limbs = ct->level + 1;
+  require(limbs > 1, comps == 3 ? "quadratic rescale requires at least two levels"
+                                : "rescale requires at least two levels");
+  require(out->data != ct->data, "rescale output must not alias its input");
+  const size_t pl = (size_t)limbs * c->N, po = (size_t)(limbs - 1) * c->N;
+  PtrTab in{}, o{};
+  for (int k = 0; k < comps; ++k) {
+    in.p[k] = ct->data + k * pl;
+    o.p[k] = out->data + k * po;
+  }
+  rescale(c->d_pc, c->rt, c->L, in, o, comps, limbs, c->N, s);
+  launch_check("rescale");
+  const int sb = ct->scale_bits - floor_log2(c->mod[limbs - 1]);
+  out->scale_bits = sb < 0 ? 0 : sb;  // saturating_sub, ops.rs:79
+  out->level = ct->level - 1;
+}
+
+extern "C" int rc_rescale(rc_context* c, const rc_ciphertext* ct, rc_ciphertext* out, void* stream) {
+  return guarded([&] { rescale_impl(c, ct, out, 2, S(stream)); });
+}
+extern "C" int rc_rescale_quadratic(rc_context* c, const rc_ciphertext* ct, rc_ciphertext* out, void* stream) {
+  return guarded([&] { rescale_impl(c, ct, out, 3, S(stream)); });
+}
+
+extern "C" int rc_keyswitch(rc_context* c, const uint64_t* poly, int32_t level, const rc_ksk* key,
+                            rc_ciphertext* out, void* stream) {
+  return guarded([&] {
+    require(c && poly && out && out->data, "arguments must not be null");
+    require(level >= 0 && level < c->L, "keyswitch level context must exist");
+    const int limbs = level + 1;
+    KsJob j{poly, key, nullptr, nullptr, out->data, out->data + (size_t)limbs * c->N};
+    keyswitch_run(c, {j}, limbs, 0, false, S(stream));
+    out->level = level;
+    out->scale_bits = limbs;  // RnsCiphertext::new(c0, c1, poly.levels()), keyswitching.rs:156,193
+  });
+}
+
+extern "C" int rc_relinearize(rc_context* c, const rc_ciphertext* qct, const rc_ksk* key, rc_ciphertext* out,
+                              void* stream) {
+  return guarded([&] {
+    require(c && out && out->data, "arguments must not be null");
+    check_ct(c, qct, "quadratic ciphertext");
+    const int limbs = qct->level + 1;
+    const size_t pl = (size_t)limbs * c->N;
+    KsJob j{qct->data + 2 * pl, key, qct->data, qct->data + pl, out->data, out->data + pl};
+    keyswitch_run(c, {j}, limbs, 0, false, S(stream));
+    out->level = qct->level;
+    out->scale_bits = qct->scale_bits;
+  });
+}
+
+extern "C" int rc_mult_relinearized(rc_context* c, const rc_ciphertext* a, const rc_ciphertext* b,
+                                    const rc_ksk* key, rc_ciphertext* out, void* stream) {
+  return guarded([&] {
+    require(c && out && out->data, "arguments must not be null");
+    check_mult_pair(c, a, b);
+    std::vector<int> idx{0};
+    mult_relin_group(c, idx, a, b, &key, out, S(stream));
+  });
+}
+
+extern "C" int rc_rotate(rc_context* c, const rc_ciphertext* ct, const rc_ksk* key, rc_ciphertext* out,
+                         void* stream) {
+  return guarded([&] {
+    require(c && out && out->data && key, "arguments must not be null");
+    check_ct(c, ct, "ciphertext");
+    // context/rotation.rs:106
+    require(key->level == ct->level, "rotation key level must match the ciphertext level");
+    require(key->galois != 0, "rotation key carries no Galois element");
+    const uint64_t gi = galois_inverse(c, key->galois);
+    const int limbs = ct->level + 1;
+    const size_t pl = (size_t)limbs * c->N;
+    require(out->data != ct->data, "rotate output must not alias its input");
+    KsJob j{ct->data + pl, key, ct->data, nullptr, out->data, out->data + pl};
+    keyswitch_run(c, {j}, limbs, gi, false, S(stream));
+    out->level = ct->level;
+    out->scale_bits = ct->scale_bits;
+  });
+}
+
+extern "C" int rc_automorphism(rc_context* c, const rc_ciphertext* ct, uint64_t g, rc_ciphertext* out,
+                               void* stream) {
+  return guarded([&] {
+    require(c && out && out->data, "arguments must not be null");
+    check_ct(c, ct, "ciphertext");
+    require(out->data != ct->data, "automorphism output must not alias its input");
+    const uint64_t gi = galois_inverse(c, g);
+    const int limbs = ct->level + 1;
+    const size_t pl = (size_t)limbs * c->N;
+    PtrTab x{}, o{};
+    x.p[0] = ct->data;
+    x.p[1] = ct->data + pl;
+    o.p[0] = out->data;
+    o.p[1] = out->data + pl;
+    automorphism(c->d_pc, x, o, 2, limbs, gi, c->log_n, S(stream));
+    launch_check("automorphism");
+    out->level = ct->level;
+    out->scale_bits = ct->scale_bits;
+  });
+}
+
+// =========================================================================
+// batched forms
+// =========================================================================
+extern "C" int rc_mult_relinearized_batch(rc_context* c, uint32_t count, const rc_ciphertext* lhs,
+                                          const rc_ciphertext* rhs, const rc_ksk* const* keys, rc_ciphertext* out,
+                                          void* stream) {
+  return guarded([&] {
+    require(c && lhs && rhs && keys && out, "arguments must not be null");
+    std::map<std::pair<int, std::pair<int, int>>, std::vector<int>> groups;
+    for (uint32_t i = 0; i < count; ++i) {
+      check_mult_pair(c, &lhs[i], &rhs[i]);
+      require(out[i].data != nullptr, "output must not be null");
+      const rc_ksk* k = keys[i];
+      require(k != nullptr, "keyswitch key must not be null");
+      groups[{lhs[i].level, {(int)k->aux, (int)k->digits}}].push_back((int)i);
+    }
+    for (auto& g : groups) mult_relin_group(c, g.second, lhs, rhs, keys, out, S(stream));
+  });
+}
+
+extern "C" int rc_relinearize_batch(rc_context* c, uint32_t count, const rc_ciphertext* qct,
+                                    const rc_ksk* const* keys, rc_ciphertext* out, void* stream) {
+  return guarded([&] {
+    require(c && qct && keys && out, "arguments must not be null");
+    std::map<std::pair<int, std::pair<int, int>>, std::vector<int>> groups;
+    for (uint32_t i = 0; i < count; ++i) {
+      check_ct(c, &qct[i], "quadratic ciphertext");
+      require(keys[i] != nullptr, "keyswitch key must not be null");
+      groups[{qct[i].level, {(int)keys[i]->aux, (int)keys[i]->digits}}].push_back((int)i);
+    }
+    for (auto& g : groups) {
+      const int limbs = g.first.first + 1;
+      const size_t pl = (size_t)limbs * c->N;
+      for (size_t b = 0; b < g.second.size(); b += MAXP / 2) {
+        std::vector<KsJob> jobs;
+        for (size_t k = b; k < g.second.size() && k < b + MAXP / 2; ++k) {
+          const int i = g.second[k];
+          jobs.push_back(KsJob{qct[i].data + 2 * pl, keys[i], qct[i].data, qct[i].data + pl, out[i].data,
+                               out[i].data + pl});
+          out[i].level = qct[i].level;
+          out[i].scale_bits = qct[i].scale_bits;
+        }
+        keyswitch_run(c, jobs, limbs, 0, false, S(stream));
+      }
+    }
+  });
+}
+
+extern "C" int rc_rotate_batch(rc_context* c, uint32_t count, const rc_ciphertext* ct, const rc_ksk* const* keys,
+                               rc_ciphertext* out, void* stream) {
+  return guarded([&] {
+    require(c && ct && keys && out, "arguments must not be null");
+    // group by (level, key kind, galois element): the gather is per launch
+    std::map<std::pair<std::pair<int, uint64_t>, std::pair<int, int>>, std::vector<int>> groups;
+    for (uint32_t i = 0; i < count; ++i) {
+      check_ct(c, &ct[i], "ciphertext");
+      const rc_ksk* k = keys[i];
+      require(k != nullptr, "rotation key must not be null");
+      require(k->level == ct[i].level, "rotation key level must match the ciphertext level");
+      require(k->galois != 0, "rotation key carries no Galois element");
+      groups[{{ct[i].level, k->galois}, {(int)k->aux, (int)k->digits}}].push_back((int)i);
+    }
+    for (auto& g : groups) {
+      const int limbs = g.first.first.first + 1;
+      const uint64_t gi = galois_inverse(c, g.first.first.second);
+      const size_t pl = (size_t)limbs * c->N;
+      for (size_t b = 0; b < g.second.size(); b += MAXP / 2) {
+        std::vector<KsJob> jobs;
+        for (size_t k = b; k < g.second.size() && k < b + MAXP / 2; ++k) {
+          const int i = g.second[k];
+          require(out[i].data != ct[i].data, "rotate output must not alias its input");
+          jobs.push_back(KsJob{ct[i].data + pl, keys[i], ct[i].data, nullptr, out[i].data, out[i].data + pl});
+          out[i].level = ct[i].level;
+          out[i].scale_bits = ct[i].scale_bits;
+        }
+        keyswitch_run(c, jobs, limbs, gi, false, S(stream));
+      }
+    }
+  });
+}
+
+// =========================================================================
+// host-buffer entry points
+// =========================================================================
+extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, const uint64_t* const* lhs,
+                                               const uint64_t* const* rhs, const int32_t* levels,
+                                               const int32_t* scale_bits, const rc_ksk* const* keys,
+                                               uint64_t* const* out, int32_t* out_scale_bits, void* stream) {
+  return guarded([&] {
+    require(c && lhs && rhs && levels && scale_bits && keys && out, "arguments must not be null");
+    cudaStream_t s = S(stream);
+    // device staging for inputs and outputs lives in its own buffer (the op's
+    // scratch is separate); kept per context+stream
+    size_t in_elems = 0, out_elems = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+      require(levels[i] >= 1 && levels[i] < c->L, "ciphertext level context must exist");
+      in_elems += (size_t)2 * 2 * (levels[i] + 1) * c->N;
+      out_elems += (size_t)2 * levels[i] * c->N;
+    }
+    static thread_local std::map<std::pair<rc_context*, cudaStream_t>, std::unique_ptr<DevBuf>> staging;
+    auto& st = staging[{c, s}];
+    const size_t need = (in_elems + out_elems) * 8;
+    if (!st || st->bytes < need) {
+      cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+      st.reset();
+      st.reset(new DevBuf(need));
+    }
+    uint64_t* dev = (uint64_t*)st->p;
+    std::vector<rc_ciphertext> L(count), R(count), O(count);
+    size_t off = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+      const size_t ce = (size_t)2 * (levels[i] + 1) * c->N;
+      L[i] = rc_ciphertext{dev + off, levels[i], scale_bits[i]};
+      cuda_check(cudaMemcpyAsync(dev + off, lhs[i], ce * 8, cudaMemcpyHostToDevice, s), "H2D");
+      off += ce;
+      R[i] = rc_ciphertext{dev + off, levels[i], scale_bits[i]};
+      cuda_check(cudaMemcpyAsync(dev + off, rhs[i], ce * 8, cudaMemcpyHostToDevice, s), "H2D");
+      off += ce;
+    }
+    for (uint32_t i = 0; i < count; ++i) {
+      O[i] = rc_ciphertext{dev + off, 0, 0};
+      off += (size_t)2 * levels[i] * c->N;
+    }
+    int rc = rc_mult_relinearized_batch(c, count, L.data(), R.data(), keys, O.data(), stream);
+    if (rc != RC_OK) fail(rc, g_err);
+    for (uint32_t i = 0; i < count; ++i) {
+      cuda_check(cudaMemcpyAsync(out[i], O[i].data, (size_t)2 * levels[i] * c->N * 8, cudaMemcpyDeviceToHost, s),
+                 "D2H");
+      if (out_scale_bits) out_scale_bits[i] = O[i].scale_bits;
+    }
+    cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+  });
+}
+
+extern "C" int rc_mult_relinearized_host(rc_context* c, const uint64_t* lhs, const uint64_t* rhs, int32_t level,
+                                         int32_t scale_bits, const rc_ksk* key, uint64_t* out,
+                                         int32_t* out_scale_bits, void* stream) {
+  const uint64_t* l[1] = {lhs};
+  const uint64_t* r[1] = {rhs};
+  uint64_t* o[1] = {out};
+  const rc_ksk* k[1] = {key};
+  return rc_mult_relinearized_batch_host(c, 1, l, r, &level, &scale_bits, k, o, out_scale_bits, stream);
+}

@@ -1,0 +1,96 @@
+// Host-side context of the GPU library: parameters, device-resident tables,
+// per-stream scratch.  Internal to the library (the ABI exposes rc_context as
+// an opaque handle).
+#pragma once
+#include <cuda_runtime.h>
+
+#include <map>
+#include <memory>
+#include <mutex>
+#include <stdexcept>
+#include <string>
+#include <vector>
+
+#include "../../include/rnsckks_gpu.h"
+#include "bignum.hpp"
+#include "kernels.cuh"
+
+namespace rc {
+
+struct ApiError : std::runtime_error {
+  int code;
+  ApiError(int c, const std::string& m) : std::runtime_error(m), code(c) {}
+};
+
+[[noreturn]] inline void fail(int code, const std::string& msg) { throw ApiError(code, msg); }
+inline void require(bool cond, const std::string& msg) {
+  if (!cond) fail(RC_ERR_INVALID_ARGUMENT, msg);
+}
+void cuda_check(cudaError_t e, const char* what);
+
+struct DevBuf {
+  void* p = nullptr;
+  size_t bytes = 0;
+  DevBuf() {}
+  explicit DevBuf(size_t b);
+  ~DevBuf();
+  DevBuf(const DevBuf&) = delete;
+  DevBuf& operator=(const DevBuf&) = delete;
+};
+
+struct LevelInfo {
+  int limbs = 0;
+  size_t bits = 0;     // bits of Q_limbs
+  int digits = 0;      // num_decomp_digits(bits, 30)
+  DecompTab dt{};
+  std::shared_ptr<DevBuf> buf;
+};
+
+struct Workspace {
+  std::unique_ptr<DevBuf> dev;
+  void* host_pinned = nullptr;
+  size_t host_bytes = 0;
+  ~Workspace();
+};
+
+}  // namespace rc
+
+struct rc_context {
+  int N = 0, log_n = 0, n1 = 0;
+  int L = 0, K = 0;
+  int scale_bits = 0;
+  int device = 0;
+  std::vector<uint64_t> mod, root;  // Q then P
+  std::unique_ptr<rc::DevBuf> pc_buf, tw_buf, md_buf, rt_buf;
+  rc::PrimeConst* d_pc = nullptr;
+  rc::Twiddle* d_twf = nullptr;
+  rc::Twiddle* d_twi = nullptr;
+  std::vector<rc::LevelInfo> levels;  // index = limb count (1..L)
+  rc::ModDownTab md{};
+  rc::RescaleTab rt{};
+  std::vector<uint64_t> host_halfP;
+  std::mutex mu;
+  std::map<cudaStream_t, std::unique_ptr<rc::Workspace>> ws;
+  size_t scratch_budget = size_t(256) << 20;
+
+  rc::NttArgs ntt() const {
+    rc::NttArgs a;
+    a.pc = d_pc;
+    a.tw_fwd = d_twf;
+    a.tw_inv = d_twi;
+    a.log_n = log_n;
+    a.n1 = n1;
+    return a;
+  }
+};
+
+struct rc_ksk {
+  rc_context* ctx = nullptr;
+  std::shared_ptr<rc::DevBuf> buf;  // [limbs][digits][2][N], NTT domain, Montgomery form
+  uint64_t* data = nullptr;
+  uint32_t digits = 0;
+  int32_t level = 0;
+  uint32_t aux = 0;
+  uint64_t galois = 0;
+  uint32_t limbs() const { return (uint32_t)level + 1 + aux; }
+};

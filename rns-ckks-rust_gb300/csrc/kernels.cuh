@@ -1,0 +1,142 @@
+// Internal interfaces between the C ABI layer and the CUDA kernels.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <cstddef>
+#include <cstdint>
+
+#include "modarith.cuh"
+
+namespace rc {
+
+// Up to MAXP polynomials per launch, addressed through a by-value pointer table
+// (kernel parameters, so launches need no extra upload and can be captured in
+// CUDA graphs).  Limb j of polynomial k lives at p[k] + j * N.
+constexpr int MAXP = 64;
+struct PtrTab {
+  u64* p[MAXP];
+};
+
+// Limb j of a polynomial uses prime prime(j) of the context's Q u P list:
+// the first `qcount` limbs are Q primes 0..qcount-1, the rest are the aux
+// primes L, L+1, ...
+struct LimbMap {
+  int qcount;
+  int L;
+  __host__ __device__ __forceinline__ int prime(int j) const { return j < qcount ? j : L + (j - qcount); }
+};
+
+struct NttArgs {
+  const PrimeConst* pc;
+  const Twiddle* tw_fwd;  // [primes][N]: psi^bitrev(k)
+  const Twiddle* tw_inv;  // [primes][N]: psi^-bitrev(k)
+  int log_n;
+  int n1;  // column-phase size 2^n1; row-phase size 2^(log_n - n1)
+};
+
+// Negacyclic NTT over `polys` x `limbs` limbs, src -> dst (may alias).
+// Forward: canonical coefficients -> canonical evaluations in bit-reversed order.
+// Inverse: the reverse, including the N^-1 scaling.
+void ntt_forward(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
+                 cudaStream_t s);
+void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
+                 cudaStream_t s);
+
+// ---- elementwise / scheme kernels (ops.cu) ----
+enum class EwOp { Add, Sub, Mul };
+// out[k] = a[k] (op) b[k] over `polys` polys of `limbs` limbs; b may be shared
+// across polys (b_shared != 0 uses b.p[0] for every poly).
+void ew_binary(EwOp op, const PrimeConst* pc, const PtrTab& a, const PtrTab& b, int b_shared, const PtrTab& out,
+               int polys, int limbs, LimbMap map, int n, cudaStream_t s);
+// out_j = a_j * v[j] mod q_j
+struct ScalarTab {
+  u64 v[80];
+};
+void mul_scalar(const PrimeConst* pc, const u64* a, const ScalarTab& v, u64* out, int limbs, LimbMap map, int n,
+                cudaStream_t s);
+// NTT-domain tensor: for each job j, in = [a0,a1,b0,b1] (4 polys) -> out = [d0,d1,d2]
+void tensor_ntt(const PrimeConst* pc, const PtrTab& in4, const PtrTab& out3, int jobs, int limbs, int n,
+                cudaStream_t s);
+// coefficient-domain Galois automorphism X -> X^g (signed permutation), g given by its inverse mod 2N
+void automorphism(const PrimeConst* pc, const PtrTab& in, const PtrTab& out, int polys, int limbs, uint64_t g_inv,
+                  int log_n, cudaStream_t s);
+
+struct RescaleTab {
+  const u64* inv;    // [L][L]: inv[(l-1)*L + i] = q_{l-1}^-1 mod q_i
+  const u64* inv_s;  // Shoup companions
+};
+// rescale_poly_rns for `polys` polys at `limbs` limbs -> limbs-1
+void rescale(const PrimeConst* pc, const RescaleTab& rt, int L, const PtrTab& in, const PtrTab& out, int polys,
+             int limbs, int n, cudaStream_t s);
+
+// ---- keyswitch (keyswitch.cu) ----
+struct DecompTab {
+  const u64* qhat;       // [limbs][W] words of Q/q_i
+  const u64* qhat_inv;   // [limbs] (Q/q_i)^-1 mod q_i
+  const u64* qhat_inv_s; // Shoup companions
+  const double* inv_q;   // [limbs] 1/q_i
+  const u64* Q;          // [W]
+  const u64* halfQ;      // [W]
+  int W;                 // words for Q (with headroom for the CRT sum)
+  int small_q;           // Q <= 2^30: digits need the general centred lift
+  u64 Qsmall;            // Q when small_q
+};
+
+struct ModDownTab {
+  // aux basis P (K primes): Garner inverses and mixed-radix weights
+  const u64* p_garner;    // [K][K]: p_garner[k*K + t] = p_t^-1 mod p_k (t < k)
+  const u64* p_garner_s;
+  const u64* halfP;       // [KW]
+  int KW;                 // words of P
+  // per Q prime i: P^-1 mod q_i, P mod q_i, M_k mod q_i (M_k = p_0..p_{k-1})
+  const u64* pinv;        // [L]
+  const u64* pinv_s;
+  const u64* pmod;        // [L]
+  const u64* mk;          // [L][K]
+  const u64* mk_s;
+};
+
+// digits[job][d][x] (int32) of the centred CRT value of src (optionally read
+// through the automorphism with inverse element g_inv; 0/1 = none)
+void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int jobs, int limbs, int D,
+               int32_t* digits, uint64_t g_inv, int log_n, cudaStream_t s);
+
+struct KsArgs {
+  const PrimeConst* pc;
+  NttArgs ntt;
+  int n;
+  int L;          // Q chain length (for the limb map)
+  int qlimbs;     // active Q limbs
+  int K;          // aux limbs used (0 = Q-only)
+  int D;          // digits decomposed (and used from the key)
+  int key_digits; // digits stored per key limb
+  const DecompTab* dt;
+};
+
+// For each job: NTT every digit into each extended-basis limb and accumulate
+// against the key -> acc[job][2][qlimbs+K][N] (NTT domain, canonical).
+// scratch must hold jobs * chunk * D * N u64 (chunk = limbs per pass).
+void digit_ntt_mac(const KsArgs& a, const int32_t* digits, const u64* const* keys, int jobs, u64* acc,
+                   u64* scratch, size_t scratch_elems, cudaStream_t s);
+
+// ModDown (if K>0) + optional addend (optionally through an automorphism) +
+// optional rescale; acc in coefficient form [job][2][qlimbs+K][N].
+// addend.p[2*job + c] (null = none); out.p[2*job + c].
+struct FinalizeArgs {
+  const PrimeConst* pc;
+  ModDownTab md;
+  RescaleTab rt;
+  int L, n, log_n;
+  int qlimbs, K;
+  int rescale;
+  uint64_t add_g_inv;  // automorphism applied to the addend (0/1 = none)
+};
+void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const PtrTab& out, int jobs,
+              cudaStream_t s);
+
+// key upload: coefficient-form key [digits][2][limbs][N] (device) ->
+// [limbs][digits][2][N] NTT domain, Montgomery form
+void key_to_device_form(const NttArgs& a, const PrimeConst* pc, const u64* src, u64* dst, int digits, int limbs,
+                        LimbMap map, int n, cudaStream_t s);
+
+}  // namespace rc

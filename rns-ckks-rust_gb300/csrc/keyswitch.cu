@@ -1,0 +1,560 @@
+// Keyswitching with the reference's gadget: balanced base-2^30 digits of the
+// centred CRT value (src/rns/keyswitching.rs:130-236, 381-467), ModUp of the
+// digits to the aux basis (lift_poly_to_context, 242-276), the key inner
+// product, and ModDown (mod_down_eval_to_q, 278-322).
+//
+// GPU formulation (exact, same residues as the reference):
+//  * decompose: one thread per coefficient builds X = sum_i y_i * (Q/q_i) with
+//    y_i = c_i * (Q/q_i)^-1 mod q_i in 64-bit words, removes floor(sum y_i/q_i)
+//    multiples of Q (exact fix-up), centres it, and emits the balanced digits
+//    of its two's complement: identical to the reference's Garner +
+//    sign-magnitude digits + carry normalisation (including the dropped final
+//    carry when the digits run out).
+//  * digit NTT + key product: a digit d in [-2^29, 2^29) has residue d (or
+//    d + q) in every limb, so ModUp of a digit polynomial is just that residue
+//    in each aux prime.  Each digit is NTT'd per limb (column pass to scratch,
+//    row pass fused with the multiply-accumulate against the key, which lives
+//    in the NTT domain and Montgomery form), so neither the lifted digits nor
+//    the per-digit products ever reach HBM.
+//  * finalize: ModDown by exact centred Garner over the aux primes, optional
+//    addend (relinearize / rotate) and optional rescale in one pass.
+#include "kernels.cuh"
+
+namespace rc {
+
+namespace {
+
+// ---------------------------------------------------------------------------
+// decomposition
+// ---------------------------------------------------------------------------
+template <int WM>
+__global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int limbs, int D, int32_t* digits,
+                            u64 g_inv, int log_n) {
+  const u64 N = 1ull << log_n;
+  const u64 x = blockIdx.x * (u64)blockDim.x + threadIdx.x;
+  if (x >= N) return;
+  const int job = blockIdx.y;
+  const u64* in = src.p[job];
+  const int W = dt.W;
+
+  u64 sidx = x;
+  bool neg = false;
+  if (g_inv > 1) {
+    sidx = (x * g_inv) & (2 * N - 1);
+    neg = sidx >= N;
+    if (neg) sidx -= N;
+  }
+
+  u64 X[WM];
+#pragma unroll
+  for (int w = 0; w < WM; ++w) X[w] = 0;
+  double kf = 0.0;
+  for (int l = 0; l < limbs; ++l) {
+    const u64 q = pc[l].q;
+    u64 r = in[(u64)l * N + sidx];
+    if (neg && r) r = q - r;
+    const u64 y = mul_shoup(r, dt.qhat_inv[l], dt.qhat_inv_s[l], q);
+    kf += (double)y * dt.inv_q[l];
+    const u64* qh = dt.qhat + (size_t)l * W;
+    u64 carry = 0;
+#pragma unroll
+    for (int w = 0; w < WM; ++w) {
+      if (w < W) {
+        U128 p = mul_wide(y, qh[w]);
+        u64 lo = p.lo + X[w];
+        u64 c1 = lo < X[w] ? 1ull : 0ull;
+        u64 lo2 = lo + carry;
+        u64 c2 = lo2 < carry ? 1ull : 0ull;
+        X[w] = lo2;
+        carry = p.hi + c1 + c2;
+      }
+    }
+  }
+  // X' = X - k*Q with k = floor(sum y_i / q_i) (exact up to +-1, fixed below)
+  u64 k = (u64)kf;
+  {
+    u64 borrow = 0, carry = 0;
+#pragma unroll
+    for (int w = 0; w < WM; ++w) {
+      if (w < W) {
+        U128 p = mul_wide(k, dt.Q[w]);
+        u64 sub = p.lo + carry;
+        carry = p.hi + (sub < carry ? 1ull : 0ull);
+        u64 xw = X[w];
+        u64 d = xw - sub;
+        u64 b1 = xw < sub ? 1ull : 0ull;
+        u64 d2 = d - borrow;
+        u64 b2 = d < borrow ? 1ull : 0ull;
+        X[w] = d2;
+        borrow = b1 + b2;
+      }
+    }
+  }
+  // X is now in [-Q, 2Q) as a W-word two's complement value
+  auto top_neg = [&]() -> bool {
+    bool n = false;
+#pragma unroll
+    for (int w = 0; w < WM; ++w)
+      if (w == W - 1) n = (X[w] >> 63) != 0;
+    return n;
+  };
+  auto add_Q = [&](bool subtract) {
+    u64 c = 0;
+#pragma unroll
+    for (int w = 0; w < WM; ++w) {
+      if (w < W) {
+        u64 qw = dt.Q[w];
+        if (!subtract) {
+          u64 s = X[w] + qw;
+          u64 c1 = s < qw ? 1ull : 0ull;
+          u64 s2 = s + c;
+          u64 c2 = s2 < c ? 1ull : 0ull;
+          X[w] = s2;
+          c = c1 + c2;
+        } else {
+          u64 d = X[w] - qw;
+          u64 b1 = X[w] < qw ? 1ull : 0ull;
+          u64 d2 = d - c;
+          u64 b2 = d < c ? 1ull : 0ull;
+          X[w] = d2;
+          c = b1 + b2;
+        }
+      }
+    }
+  };
+  // compare X (non-negative) with a W-word constant: returns X > C
+  auto greater_than = [&](const u64* C, bool or_equal) -> bool {
+    int res = 0;  // 0 equal so far, 1 greater, -1 less (from the top)
+#pragma unroll
+    for (int w = WM - 1; w >= 0; --w) {
+      if (w < W && res == 0) {
+        if (X[w] > C[w]) res = 1;
+        else if (X[w] < C[w]) res = -1;
+      }
+    }
+    return res > 0 || (or_equal && res == 0);
+  };
+  if (top_neg()) add_Q(false);
+  else if (greater_than(dt.Q, true)) add_Q(true);
+  // centre: X > floor(Q/2) -> X - Q
+  if (greater_than(dt.halfQ, false)) add_Q(true);
+  const u64 ext = top_neg() ? ~0ull : 0ull;
+
+  // balanced base-2^30 digits of the two's complement value
+  int32_t* out = digits + (size_t)job * D * N + x;
+  u64 carry = 0;
+  constexpr int DMAX = (64 * WM) / 30 + 2;
+#pragma unroll
+  for (int d = 0; d < DMAX; ++d) {
+    if (d < D) {
+      const int bit = 30 * d;
+      const int w0 = bit / 64, sh = bit % 64;
+      u64 lo = (w0 < WM) ? (w0 < W ? X[w0 < WM ? w0 : 0] : ext) : ext;
+      u64 chunk = lo >> sh;
+      if (sh > 34) {
+        const int w1 = w0 + 1;
+        u64 hi = (w1 < WM) ? (w1 < W ? X[w1 < WM ? w1 : 0] : ext) : ext;
+        chunk |= hi << (64 - sh);
+      }
+      chunk &= (1ull << 30) - 1;
+      u64 v = chunk + carry;
+      int64_t dig;
+      if (v >= (1ull << 29)) {
+        dig = (int64_t)v - (1ll << 30);
+        carry = 1;
+      } else {
+        dig = (int64_t)v;
+        carry = 0;
+      }
+      out[(size_t)d * N] = (int32_t)dig;
+    }
+  }
+  // digits beyond DMAX (only for keys with far more digits than the modulus
+  // needs) are pure sign extension
+  for (int d = DMAX; d < D; ++d) {
+    u64 chunk = ext & ((1ull << 30) - 1);
+    u64 v = chunk + carry;
+    int64_t dig;
+    if (v >= (1ull << 29)) {
+      dig = (int64_t)v - (1ll << 30);
+      carry = 1;
+    } else {
+      dig = (int64_t)v;
+      carry = 0;
+    }
+    out[(size_t)d * N] = (int32_t)dig;
+  }
+}
+
+// signed_digit_mod_q (keyswitching.rs:456-467) for |d| <= 2^29
+__device__ __forceinline__ u64 digit_residue(int32_t d, u64 q) {
+  if (q > (1ull << 29)) return d >= 0 ? (u64)d : q - (u64)(-(int64_t)d);
+  u64 m = (u64)(d >= 0 ? (int64_t)d : -(int64_t)d) % q;
+  return d >= 0 ? m : (m ? q - m : 0);
+}
+
+// Residue of the lifted digit in aux prime p: the centred representative of
+// (d mod Q) reduced mod p (convert_centered_residues_to_target).  For Q > 2^30
+// that representative is d itself.
+__device__ __forceinline__ u64 lifted_residue(int32_t d, u64 p, const DecompTab& dt) {
+  if (!dt.small_q) return digit_residue(d, p);
+  const int64_t Qs = (int64_t)dt.Qsmall;
+  int64_t x = (int64_t)d % Qs;
+  if (x < 0) x += Qs;
+  if ((u64)x > (dt.Qsmall >> 1)) x -= Qs;
+  int64_t r = x % (int64_t)p;
+  if (r < 0) r += (int64_t)p;
+  return (u64)r;
+}
+
+// ---------------------------------------------------------------------------
+// digit NTT: column pass (digit -> residue -> stages 0..n1-1 -> scratch)
+// ---------------------------------------------------------------------------
+__global__ void k_digit_cols(KsArgs a, DecompTab dt, const int32_t* digits, u64* scratch, int p0, int pc_count) {
+  extern __shared__ u64 sm[];
+  const int log_n = a.ntt.log_n, n1 = a.ntt.n1;
+  const int N = 1 << log_n, N1 = 1 << n1, N2 = N >> n1;
+  const int COLS = N2 < 16 ? N2 : 16;
+  const int c0 = blockIdx.x * COLS;
+  const int digit = blockIdx.y / pc_count, pl = blockIdx.y % pc_count;
+  const int total = a.qlimbs + a.K;
+  const int pair = p0 + pl;
+  const int job = pair / total, limb = pair % total;
+  const LimbMap map{a.qlimbs, a.L};
+  const int prime = map.prime(limb);
+  const u64 q = a.pc[prime].q, two_q = q << 1;
+  const bool aux = limb >= a.qlimbs;
+  const Twiddle* tw = a.ntt.tw_fwd + (size_t)prime * N;
+  const int32_t* in = digits + ((size_t)job * a.D + digit) * N;
+  u64* out = scratch + ((size_t)pl * a.D + digit) * N;
+
+  for (int idx = threadIdx.x; idx < N1 * COLS; idx += blockDim.x) {
+    int r = idx / COLS, c = idx % COLS;
+    int32_t d = in[(size_t)r * N2 + c0 + c];
+    sm[idx] = aux ? lifted_residue(d, q, dt) : digit_residue(d, q);
+  }
+  __syncthreads();
+  for (int s = 0; s < n1; ++s) {
+    const int t = N1 >> (s + 1);
+    for (int idx = threadIdx.x; idx < (N1 / 2) * COLS; idx += blockDim.x) {
+      int p = idx / COLS, c = idx % COLS;
+      int r = (p / t) * 2 * t + (p % t);
+      Twiddle w = tw[(1 << s) + (r >> (n1 - s))];
+      u64 x = sm[r * COLS + c], y = sm[(r + t) * COLS + c];
+      x = x >= two_q ? x - two_q : x;
+      u64 v = mul_shoup_lazy(y, w.w, w.ws, q);
+      sm[r * COLS + c] = x + v;
+      sm[(r + t) * COLS + c] = x - v + two_q;
+    }
+    __syncthreads();
+  }
+  for (int idx = threadIdx.x; idx < N1 * COLS; idx += blockDim.x) {
+    int r = idx / COLS, c = idx % COLS;
+    out[(size_t)r * N2 + c0 + c] = sm[idx];
+  }
+}
+
+// ---------------------------------------------------------------------------
+// digit NTT row pass fused with the key multiply-accumulate
+// ---------------------------------------------------------------------------
+constexpr int MAC_E = 4;  // elements per thread
+
+struct KeyTab {
+  const u64* k[MAXP];
+};
+
+__global__ void k_digit_rows_mac(KsArgs a, const u64* scratch, KeyTab keys, u64* acc, int p0) {
+  extern __shared__ u64 sm[];
+  const int log_n = a.ntt.log_n, n1 = a.ntt.n1;
+  const int N = 1 << log_n, N2 = N >> n1;
+  const int tile = blockDim.x * MAC_E;  // ROWS * N2
+  const int ROWS = tile / N2;
+  const int r0 = blockIdx.x * ROWS;
+  const int pl = blockIdx.y;
+  const int limbs_total = a.qlimbs + a.K;
+  const int pair = p0 + pl;
+  const int job = pair / limbs_total, limb = pair % limbs_total;
+  const LimbMap map{a.qlimbs, a.L};
+  const int prime = map.prime(limb);
+  const PrimeConst& pc = a.pc[prime];
+  const u64 q = pc.q, two_q = q << 1;
+  const Twiddle* tw = a.ntt.tw_fwd + (size_t)prime * N;
+  // key layout [limb][key_digits][2][N]
+  const u64* key = keys.k[job] + (size_t)limb * a.key_digits * 2 * N + (size_t)r0 * N2;
+
+  U128 acc0[MAC_E], acc1[MAC_E];
+  u64 red0[MAC_E], red1[MAC_E];
+#pragma unroll
+  for (int e = 0; e < MAC_E; ++e) {
+    acc0[e].lo = acc0[e].hi = acc1[e].lo = acc1[e].hi = 0;
+    red0[e] = red1[e] = 0;
+  }
+  const int half = N2 / 2;
+  const u64 chunk = pc.mac_chunk;
+  u64 since = 0;
+  for (int digit = 0; digit < a.D; ++digit) {
+    const u64* in = scratch + ((size_t)pl * a.D + digit) * N + (size_t)r0 * N2;
+    for (int idx = threadIdx.x; idx < tile; idx += blockDim.x) sm[idx] = in[idx];
+    __syncthreads();
+    for (int s = n1; s < log_n; ++s) {
+      const int t = N2 >> (s - n1 + 1);
+      for (int idx = threadIdx.x; idx < tile / 2; idx += blockDim.x) {
+        int rl = idx / half, p = idx % half;
+        int c = (p / t) * 2 * t + (p % t);
+        int j = (r0 + rl) * N2 + c;
+        Twiddle w = tw[(1 << s) + (j >> (log_n - s))];
+        u64* base = sm + rl * N2;
+        u64 x = base[c], y = base[c + t];
+        x = x >= two_q ? x - two_q : x;
+        u64 v = mul_shoup_lazy(y, w.w, w.ws, q);
+        base[c] = x + v;
+        base[c + t] = x - v + two_q;
+      }
+      __syncthreads();
+    }
+    const u64* k0 = key + (size_t)digit * 2 * N;
+    const u64* k1 = k0 + N;
+#pragma unroll
+    for (int e = 0; e < MAC_E; ++e) {
+      const int idx = threadIdx.x + e * blockDim.x;
+      const u64 v = reduce_4q(sm[idx], q);
+      add_to(acc0[e], mul_wide(v, k0[idx]));
+      add_to(acc1[e], mul_wide(v, k1[idx]));
+    }
+    if (++since == chunk) {
+#pragma unroll
+      for (int e = 0; e < MAC_E; ++e) {
+        red0[e] = add_mod(red0[e], mont_reduce(acc0[e], pc), q);
+        red1[e] = add_mod(red1[e], mont_reduce(acc1[e], pc), q);
+        acc0[e].lo = acc0[e].hi = acc1[e].lo = acc1[e].hi = 0;
+      }
+      since = 0;
+    }
+    __syncthreads();
+  }
+  u64* out0 = acc + ((size_t)job * 2 * limbs_total + limb) * N + (size_t)r0 * N2;
+  u64* out1 = out0 + (size_t)limbs_total * N;
+#pragma unroll
+  for (int e = 0; e < MAC_E; ++e) {
+    const int idx = threadIdx.x + e * blockDim.x;
+    out0[idx] = add_mod(red0[e], mont_reduce(acc0[e], pc), q);
+    out1[idx] = add_mod(red1[e], mont_reduce(acc1[e], pc), q);
+  }
+}
+
+// ---------------------------------------------------------------------------
+// finalize: ModDown + addend + rescale
+// ---------------------------------------------------------------------------
+constexpr int KMAX = 8;
+
+__global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab out) {
+  const u64 N = 1ull << f.log_n;
+  const u64 x = blockIdx.x * (u64)blockDim.x + threadIdx.x;
+  if (x >= N) return;
+  const int comp = blockIdx.y & 1, job = blockIdx.y >> 1;
+  const int lq = f.qlimbs, K = f.K;
+  const u64* a = acc + ((size_t)job * 2 + comp) * (size_t)(lq + K) * N;
+  const u64* add = addend.p[2 * job + comp];
+  u64* dst = out.p[2 * job + comp];
+
+  u64 addsrc = x;
+  bool addneg = false;
+  if (add && f.add_g_inv > 1) {
+    addsrc = (x * f.add_g_inv) & (2 * N - 1);
+    addneg = addsrc >= N;
+    if (addneg) addsrc -= N;
+  }
+
+  // Garner over the aux primes: mixed-radix digits v_k of [x]_P
+  u64 v[KMAX];
+  bool pneg = false;
+  if (K > 0) {
+#pragma unroll
+    for (int k = 0; k < KMAX; ++k) {
+      if (k < K) {
+        const PrimeConst& pk = f.pc[f.L + k];
+        u64 val = a[(size_t)(lq + k) * N + x];
+#pragma unroll
+        for (int t = 0; t < KMAX; ++t) {
+          if (t < k) {
+            U128 vt;
+            vt.lo = v[t];
+            vt.hi = 0;
+            u64 vr = v[t] < pk.q ? v[t] : barrett_reduce(vt, pk);
+            val = sub_mod(val, vr, pk.q);
+            val = mul_shoup(val, f.md.p_garner[k * K + t], f.md.p_garner_s[k * K + t], pk.q);
+          }
+        }
+        v[k] = val;
+      }
+    }
+    // X_P = sum v_k M_k by Horner (K words max); compare with floor(P/2)
+    u64 X[KMAX];
+#pragma unroll
+    for (int w = 0; w < KMAX; ++w) X[w] = 0;
+#pragma unroll
+    for (int k = KMAX - 1; k >= 0; --k) {
+      if (k < K) {
+        const u64 pk = f.pc[f.L + k].q;
+        u64 carry = v[k];
+#pragma unroll
+        for (int w = 0; w < KMAX; ++w) {
+          U128 p = mul_wide(X[w], pk);
+          u64 lo = p.lo + carry;
+          carry = p.hi + (lo < carry ? 1ull : 0ull);
+          X[w] = lo;
+        }
+      }
+    }
+    int res = 0;
+#pragma unroll
+    for (int w = KMAX - 1; w >= 0; --w) {
+      if (res == 0) {
+        u64 h = w < f.md.KW ? f.md.halfP[w < KMAX ? w : 0] : 0ull;
+        if (X[w] > h) res = 1;
+        else if (X[w] < h) res = -1;
+      }
+    }
+    pneg = res > 0;
+  }
+
+  auto limb_value = [&](int i) -> u64 {
+    const PrimeConst& c = f.pc[i];
+    u64 val = a[(size_t)i * N + x];
+    if (K > 0) {
+      // centred [x]_P mod q_i
+      U128 s;
+      s.lo = 0;
+      s.hi = 0;
+#pragma unroll
+      for (int k = 0; k < KMAX; ++k) {
+        if (k < K) {
+          U128 vt;
+          vt.lo = v[k];
+          vt.hi = 0;
+          u64 vr = v[k] < c.q ? v[k] : barrett_reduce(vt, c);
+          u64 t = mul_shoup(vr, f.md.mk[(size_t)i * K + k], f.md.mk_s[(size_t)i * K + k], c.q);
+          s.lo = add_mod(s.lo, t, c.q);
+        }
+      }
+      u64 conv = s.lo;
+      if (pneg) conv = sub_mod(conv, f.md.pmod[i], c.q);
+      val = sub_mod(val, conv, c.q);
+      val = mul_shoup(val, f.md.pinv[i], f.md.pinv_s[i], c.q);
+    }
+    if (add) {
+      u64 av = add[(size_t)i * N + addsrc];
+      if (addneg && av) av = c.q - av;
+      val = add_mod(val, av, c.q);
+    }
+    return val;
+  };
+
+  if (!f.rescale) {
+    for (int i = 0; i < lq; ++i) dst[(size_t)i * N + x] = limb_value(i);
+    return;
+  }
+  const int last = lq - 1;
+  const u64 vl = limb_value(last);
+  const u64 ql = f.pc[last].q, half = ql >> 1;
+  const bool pos = vl <= half;
+  const u64 dist = pos ? vl : ql - vl;
+  for (int i = 0; i < last; ++i) {
+    const PrimeConst& c = f.pc[i];
+    U128 dt;
+    dt.lo = dist;
+    dt.hi = 0;
+    u64 d = dist < c.q ? dist : barrett_reduce(dt, c);
+    u64 cd = pos ? d : (d == 0 ? 0 : c.q - d);
+    u64 num = sub_mod(limb_value(i), cd, c.q);
+    size_t k = (size_t)last * f.L + i;
+    dst[(size_t)i * N + x] = mul_shoup(num, f.rt.inv[k], f.rt.inv_s[k], c.q);
+  }
+}
+
+// key relayout [digits][2][limbs][N] (NTT domain) -> [limbs][digits][2][N] in Montgomery form
+__global__ void k_key_relayout(const PrimeConst* pc, const u64* src, u64* dst, int digits, int limbs, LimbMap map,
+                               int log_n) {
+  const u64 N = 1ull << log_n;
+  const size_t total = (size_t)digits * 2 * limbs * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const u64 x = e & (N - 1);
+    size_t r = e >> log_n;
+    const int j = (int)(r % limbs);
+    r /= limbs;
+    const int c = (int)(r % 2);
+    const int i = (int)(r / 2);
+    const PrimeConst& p = pc[map.prime(j)];
+    U128 t;
+    t.lo = 0;
+    t.hi = src[e];  // v * 2^64 mod q = Montgomery form of v
+    dst[(((size_t)j * digits + i) * 2 + c) * N + x] = barrett_reduce(t, p);
+  }
+}
+
+}  // namespace
+
+void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int jobs, int limbs, int D,
+               int32_t* digits, uint64_t g_inv, int log_n, cudaStream_t s) {
+  if (jobs <= 0) return;
+  const int N = 1 << log_n;
+  const int threads = N < 128 ? N : 128;
+  dim3 g((N + threads - 1) / threads, jobs);
+  const int W = dt.W;
+  if (W <= 4) k_decompose<4><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  else if (W <= 8) k_decompose<8><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  else if (W <= 16) k_decompose<16><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  else if (W <= 24) k_decompose<24><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  else if (W <= 32) k_decompose<32><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  else k_decompose<64><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+}
+
+void digit_ntt_mac(const KsArgs& a, const int32_t* digits, const u64* const* keys, int jobs, u64* acc,
+                   u64* scratch, size_t scratch_elems, cudaStream_t s) {
+  if (jobs <= 0) return;
+  const int N = a.n, N1 = 1 << a.ntt.n1, N2 = N >> a.ntt.n1;
+  const int total = a.qlimbs + a.K;
+  const int pairs = jobs * total;
+  int chunk = (int)(scratch_elems / ((size_t)a.D * N));
+  if (chunk < 1) chunk = 1;
+  if (chunk > pairs) chunk = pairs;
+  if (chunk > 65535 / a.D) chunk = 65535 / a.D;
+  KeyTab kt;
+  for (int j = 0; j < jobs && j < MAXP; ++j) kt.k[j] = keys[j];
+  const int COLS = N2 < 16 ? N2 : 16;
+  int threads_c = 32;
+  while (threads_c < 256 && threads_c < N1 * COLS / 2) threads_c <<= 1;
+  // row pass: tile = threads * MAC_E elements, whole rows
+  int tile = N < 1024 ? N : 1024;
+  if (tile < N2) tile = N2;
+  int threads_r = tile / MAC_E;
+  if (threads_r < 1) threads_r = 1;
+  tile = threads_r * MAC_E;
+  const int rows = tile / N2;
+  for (int p0 = 0; p0 < pairs; p0 += chunk) {
+    const int pc_count = (pairs - p0) < chunk ? (pairs - p0) : chunk;
+    dim3 g1(N2 / COLS, a.D * pc_count);
+    k_digit_cols<<<g1, threads_c, N1 * COLS * sizeof(u64), s>>>(a, *a.dt, digits, scratch, p0, pc_count);
+    dim3 g2(N1 / rows, pc_count);
+    k_digit_rows_mac<<<g2, threads_r, tile * sizeof(u64), s>>>(a, scratch, kt, acc, p0);
+  }
+}
+
+void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const PtrTab& out, int jobs,
+              cudaStream_t s) {
+  if (jobs <= 0) return;
+  const int N = f.n;
+  const int threads = N < 128 ? N : 128;
+  dim3 g((N + threads - 1) / threads, 2 * jobs);
+  k_finalize<<<g, threads, 0, s>>>(f, acc, addend, out);
+}
+
+void key_to_device_form(const NttArgs& a, const PrimeConst* pc, const u64* src, u64* dst, int digits, int limbs,
+                        LimbMap map, int n, cudaStream_t s) {
+  const size_t total = (size_t)digits * 2 * limbs * n;
+  int g = (int)((total + 255) / 256);
+  if (g > 65535 * 8) g = 65535 * 8;
+  k_key_relayout<<<g, 256, 0, s>>>(pc, src, dst, digits, limbs, map, a.log_n);
+}
+
+}  // namespace rc

@@ -1,0 +1,108 @@
+// Device-side 64-bit modular arithmetic for RNS primes q < 2^61.
+//
+// The reference computes every product as `(a as u128 * b as u128) % q`
+// (src/math/ntt.rs:149-151).  On the GPU a 128-bit division per product is far
+// too slow, so this header provides exact replacements that return the same
+// canonical residues:
+//   * Shoup multiplication by a precomputed constant w (w' = floor(w 2^64 / q)),
+//     result in [0, 2q) for any 64-bit input (Harvey's lazy butterflies);
+//   * Barrett reduction of a 128-bit value with mu = floor(2^128 / q);
+//   * Montgomery reduction (R = 2^64) for the keyswitch inner product, whose
+//     key operand is stored premultiplied by R.
+#pragma once
+#include <cstdint>
+
+#include <cuda_runtime.h>  // defines __device__/__host__ for host-only compilers too
+
+namespace rc {
+
+typedef uint64_t u64;
+typedef uint32_t u32;
+
+struct Twiddle {
+  u64 w;   // twiddle value in [0, q)
+  u64 ws;  // floor(w * 2^64 / q)
+};
+
+// Per-prime constants; one entry per prime of the Q u P chain.
+struct PrimeConst {
+  u64 q;
+  u64 two_q;
+  u64 mu_hi, mu_lo;   // floor(2^128 / q) = mu_hi * 2^64 + mu_lo
+  u64 qinv_neg;       // -q^-1 mod 2^64
+  u64 n_inv, n_inv_s; // N^-1 mod q and its Shoup companion
+  u64 r2;             // 2^128 mod q (R^2 for Montgomery conversion)
+  u64 mac_chunk;      // products (each < q^2) that can be summed below q * 2^64
+  u64 pad[7];
+};
+
+#ifdef __CUDACC__
+__device__ __forceinline__ u64 mulhi(u64 a, u64 b) { return __umul64hi(a, b); }
+#else
+inline u64 mulhi(u64 a, u64 b) { return (u64)(((unsigned __int128)a * b) >> 64); }
+#endif
+
+// a * w mod q lazily: result in [0, 2q) for any a < 2^64 (requires q < 2^63).
+__device__ __forceinline__ u64 mul_shoup_lazy(u64 a, u64 w, u64 ws, u64 q) {
+  u64 hi = mulhi(a, ws);
+  return a * w - hi * q;
+}
+__device__ __forceinline__ u64 reduce_2q(u64 x, u64 q) { return x >= q ? x - q : x; }
+__device__ __forceinline__ u64 reduce_4q(u64 x, u64 q) {
+  u64 two_q = q << 1;
+  x = x >= two_q ? x - two_q : x;
+  return x >= q ? x - q : x;
+}
+__device__ __forceinline__ u64 mul_shoup(u64 a, u64 w, u64 ws, u64 q) {
+  return reduce_2q(mul_shoup_lazy(a, w, ws, q), q);
+}
+__device__ __forceinline__ u64 add_mod(u64 a, u64 b, u64 q) {
+  u64 s = a + b;
+  return s >= q ? s - q : s;
+}
+__device__ __forceinline__ u64 sub_mod(u64 a, u64 b, u64 q) { return a >= b ? a - b : a + q - b; }
+
+// 128-bit helpers -------------------------------------------------------------
+struct U128 {
+  u64 lo, hi;
+};
+__device__ __forceinline__ U128 mul_wide(u64 a, u64 b) {
+  U128 r;
+  r.lo = a * b;
+  r.hi = mulhi(a, b);
+  return r;
+}
+__device__ __forceinline__ void add_to(U128& acc, const U128& x) {
+  u64 lo = acc.lo + x.lo;
+  acc.hi += x.hi + (lo < x.lo ? 1ull : 0ull);
+  acc.lo = lo;
+}
+
+// Barrett: t mod q for t < q * 2^64, q < 2^61.  The quotient estimate keeps the
+// middle-word carries, so it is at most 2 below the true quotient.
+__device__ __forceinline__ u64 barrett_reduce(U128 t, const PrimeConst& c) {
+  u64 a = mulhi(t.lo, c.mu_lo);
+  u64 b_lo = t.lo * c.mu_hi, b_hi = mulhi(t.lo, c.mu_hi);
+  u64 c_lo = t.hi * c.mu_lo, c_hi = mulhi(t.hi, c.mu_lo);
+  u64 s = a + b_lo;
+  u64 carry = s < a ? 1ull : 0ull;
+  u64 s2 = s + c_lo;
+  carry += s2 < s ? 1ull : 0ull;
+  u64 qhat = t.hi * c.mu_hi + b_hi + c_hi + carry;
+  u64 r = t.lo - qhat * c.q;
+  r = r >= c.q ? r - c.q : r;
+  r = r >= c.q ? r - c.q : r;
+  return r;
+}
+__device__ __forceinline__ u64 mul_mod(u64 a, u64 b, const PrimeConst& c) { return barrett_reduce(mul_wide(a, b), c); }
+
+// Montgomery: t * 2^-64 mod q for t < q * 2^64; result in [0, q).
+__device__ __forceinline__ u64 mont_reduce(U128 t, const PrimeConst& c) {
+  u64 m = t.lo * c.qinv_neg;
+  U128 mq = mul_wide(m, c.q);
+  // t + m*q is divisible by 2^64; its low word is zero, carry out iff t.lo != 0
+  u64 hi = t.hi + mq.hi + (t.lo != 0 ? 1ull : 0ull);
+  return hi >= c.q ? hi - c.q : hi;
+}
+
+}  // namespace rc
