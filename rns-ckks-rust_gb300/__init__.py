@@ -15,6 +15,7 @@ def __getattr__(name):
     if name in ("context", "RnsCkksContext", "RnsCiphertext", "RnsQuadraticCiphertext", "RnsPolynomial",
                 "RnsKeySwitchingKey", "RnsRotationKey", "Sampler", "galois_element_for_rotation",
                 "to_device", "to_host"):
-        from . import context as _c
+        import importlib
+        _c = importlib.import_module(__name__ + ".context")
         return _c if name == "context" else getattr(_c, name)
     raise AttributeError(name)
