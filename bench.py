@@ -1,0 +1,462 @@
+#!/usr/bin/env python3
+"""HMult+relin throughput at N=2^16, L=24 on GB300 (one JSON line on rank 0).
+
+Workload: `mult_relinearized` (tensor + relinearize + rescale,
+src/rns/context/ops.rs:124-133 of the reference) on B independent ciphertext
+pairs at the top level of a 24-limb chain of 50-bit NTT-friendly primes, with a
+2-prime auxiliary basis (hybrid keyswitching, 40 base-2^30 gadget digits).
+A step is one batched call over the B pairs (rc_mult_relinearized_batch).
+
+  value  : batched HMult+relin/s with inputs resident in HBM (device-timed)
+  e2e    : the same through the host-buffer C entry point
+           rc_mult_relinearized_batch_host (H2D + op + D2H inside the timed region)
+  per_op : one rc_mult_relinearized call per pair (p50/p99 latency per op)
+
+`--impl reference` times the CPU restatement of the reference path (the
+oracle, faithful mode: per-call NTT round trips, u128 % arithmetic, Garner
+gadget) on the host's cores on the same workload.
+Multi-GPU: replicas only (each rank runs its own batch; no collective on the
+data path), launched by torchrun.
+"""
+from __future__ import annotations
+
+import argparse
+import ctypes
+import importlib.util
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+ROOT = Path(__file__).resolve().parent
+PKG_DIR = ROOT / "rns-ckks-rust_gb300"
+METRIC = "HMult+relin/sec at N=2^16,L=24: batched vs per-op GPU, bit-exact; p50/p99 ms"
+UNIT = "HMult+relin/s"
+
+
+def load_package():
+    name = "rnsckks_gb300"
+    if name in sys.modules:
+        return sys.modules[name]
+    spec = importlib.util.spec_from_file_location(name, PKG_DIR / "__init__.py",
+                                                  submodule_search_locations=[str(PKG_DIR)])
+    mod = importlib.util.module_from_spec(spec)
+    sys.modules[name] = mod
+    spec.loader.exec_module(mod)
+    return mod
+
+
+def load_oracle():
+    sys.path.insert(0, str(ROOT / "oracle"))
+    import oracle as O
+    O.lib()
+    return O
+
+
+# ----------------------------------------------------------------------------------------
+# distributed (replicas only)
+# ----------------------------------------------------------------------------------------
+
+def dist_setup(n_gpus: int):
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch
+        import torch.distributed as dist
+        torch.cuda.set_device(local)
+        os.environ.setdefault("MASTER_ADDR", "127.0.0.1")
+        dist.init_process_group("nccl" if torch.cuda.is_available() else "gloo")
+    return rank, world, local
+
+
+def barrier(world: int):
+    if world > 1:
+        import torch.distributed as dist
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+    t = torch.tensor([x], dtype=torch.float64, device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+# ----------------------------------------------------------------------------------------
+# clocks during the timed region
+# ----------------------------------------------------------------------------------------
+
+class ClockSampler:
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}", "--format=csv,noheader,nounits",
+                 "-lms", "200"], stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except FileNotFoundError:
+            self.proc = None
+        time.sleep(0.3)
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *a):
+        if self.proc:
+            time.sleep(0.25)
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sms, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for ln in self.lines:
+            f = [x.strip() for x in ln.split(",")]
+            if len(f) < 9:
+                continue
+            try:
+                sms.append(float(f[1]))
+                mx = float(f[2])
+            except ValueError:
+                continue
+            for name, v in zip(names, f[5:9]):
+                if v.lower() == "active":
+                    reasons.add(name)
+        return {"sm_mhz": statistics.median(sms) if sms else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sms)}
+
+
+# ----------------------------------------------------------------------------------------
+# workload
+# ----------------------------------------------------------------------------------------
+
+def make_workload(pkg, batch: int, seed: int):
+    import torch
+    from rnsckks_gb300 import context as C
+    params = pkg.params.bench_params()
+    ctx = C.RnsCkksContext(params)
+    n = params.poly_degree
+    sampler = C.Sampler(seed)
+    kp = ctx.keygen(64, sampler)
+    key, key_coeff = ctx.generate_relinearization_key(kp.secret_key, kp.public_key, sampler, return_coeff=True)
+    slots_a, slots_b, lhs, rhs = [], [], [], []
+    rng = np.random.default_rng(seed + 1)
+    for _ in range(batch):
+        sa = rng.uniform(-1, 1, n // 2) + 1j * rng.uniform(-1, 1, n // 2)
+        sb = rng.uniform(-1, 1, n // 2) + 1j * rng.uniform(-1, 1, n // 2)
+        lhs.append(ctx.encrypt(ctx.encode(sa), kp.public_key, sampler))
+        rhs.append(ctx.encrypt(ctx.encode(sb), kp.public_key, sampler))
+        slots_a.append(sa)
+        slots_b.append(sb)
+    torch.cuda.synchronize()
+    return dict(C=C, ctx=ctx, params=params, kp=kp, key=key, key_coeff=key_coeff, lhs=lhs, rhs=rhs,
+                slots_a=slots_a, slots_b=slots_b)
+
+
+def raw_batch(C, lhs, rhs, key, outs):
+    n = len(lhs)
+    L = (C.RcCiphertext * n)(*[a.raw() for a in lhs])
+    R = (C.RcCiphertext * n)(*[b.raw() for b in rhs])
+    O = (C.RcCiphertext * n)(*[C.RcCiphertext(o.data_ptr(), 0, 0) for o in outs])
+    K = (ctypes.c_void_p * n)(*[key.handle for _ in range(n)])
+    return L, R, K, O
+
+
+def cpu_oracle_op(O, params, lhs_np, rhs_np, key_np, threads: int):
+    """One faithful CPU HMult+relin (the reference algorithm restated in C)."""
+    O.set_threads(threads)
+    n = params.poly_degree
+    qpl, ppl = O.Plans(n, params.primes), O.Plans(n, params.aux_primes)
+    D = key_np.shape[0]
+    t0 = time.perf_counter()
+    out = O.mult_relinearized(qpl, ppl, lhs_np[0], lhs_np[1], rhs_np[0], rhs_np[1], key_np, D)
+    return time.perf_counter() - t0, out
+
+
+# algorithmic bytes per launch for the kernels the roofline may name
+def algorithmic_bytes(kernel: str, batch: int, n: int, limbs: int, aux: int, digits: int, launches: int):
+    ext = limbs + aux
+    per_job = {
+        # digit NTT row pass + key product: key (2 comps, all digits, extended basis) in, accumulators out
+        "digit_rows_mac": digits * 2 * ext * n * 8 + 2 * ext * n * 8,
+        # digit column pass: int32 digits in, per (digit, limb) residues out (counted as the
+        # algorithmic half of each digit transform: N*8 per digit per limb)
+        "digit_cols": digits * n * 4 + digits * ext * n * 8,
+        "decompose": limbs * n * 8 + digits * n * 4,
+        "finalize": 2 * ext * n * 8 + 2 * limbs * n * 8 + 2 * (limbs - 1) * n * 8,
+        "tensor": 4 * limbs * n * 8 + 3 * limbs * n * 8,
+        # one phase of a transform reads and writes the limb once: half of 2*N*8 per transform
+        "ntt_fwd_cols": 4 * limbs * n * 8, "ntt_fwd_rows": 4 * limbs * n * 8,
+        "ntt_inv_rows": (3 * limbs + 2 * ext) * n * 8, "ntt_inv_cols": (3 * limbs + 2 * ext) * n * 8,
+    }.get(kernel)
+    if per_job is None or launches == 0:
+        return None
+    return per_job * batch / launches
+
+
+def hmult_algorithmic_bytes(n, limbs, aux, digits):
+    """HMult+relin: 2 input ciphertexts, 1 output ciphertext, the key read once."""
+    return 4 * limbs * n * 8 + 2 * (limbs - 1) * n * 8 + digits * 2 * (limbs + aux) * n * 8
+
+
+def peaks():
+    p = ROOT / "MEASURED_PEAKS.json"
+    if p.exists():
+        d = json.loads(p.read_text())
+        return float(d["hbm_gbs"]), "measured"
+    return 6800.0, "fallback"
+
+
+# ----------------------------------------------------------------------------------------
+# arms
+# ----------------------------------------------------------------------------------------
+
+def run_gpu(args):
+    import torch
+    rank, world, local = dist_setup(args.gpus)
+    pkg = load_package()
+    pkg.lib()
+    W = make_workload(pkg, args.batch, args.seed + rank)
+    C, ctx, params, key = W["C"], W["ctx"], W["params"], W["key"]
+    lhs, rhs = W["lhs"], W["rhs"]
+    B, n = args.batch, params.poly_degree
+    limbs, aux = len(params.primes), len(params.aux_primes)
+    digits = ctx.decomp_digits(limbs - 1)
+    lib = pkg.lib()
+    stream = torch.cuda.current_stream()
+    s_ptr = ctypes.c_void_p(stream.cuda_stream)
+    outs = [torch.empty((2, limbs - 1, n), dtype=torch.int64, device="cuda") for _ in range(B)]
+    L, R, K, O = raw_batch(C, lhs, rhs, key, outs)
+    ctx.reserve(limbs - 1, B)
+
+    def step():
+        C.call("rc_mult_relinearized_batch", ctx.handle, B, L, R, K, O, s_ptr)
+
+    for _ in range(max(args.warmup, 3)):
+        step()
+    torch.cuda.synchronize()
+
+    # ---- batched, device-resident (inputs 50 MB per pair: far larger than L2 in total) ----
+    lib.rc_profile_enable(1)
+    buf = ctypes.create_string_buffer(1 << 16)
+    lib.rc_profile_report(buf, len(buf))  # reset
+    barrier(world)
+    torch.cuda.synchronize()
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local) as clk:
+        torch.cuda.nvtx.range_push("hmult_timed")
+        ev0.record(stream)
+        for _ in range(args.steps):
+            step()
+        ev1.record(stream)
+        torch.cuda.synchronize()
+        torch.cuda.nvtx.range_pop()
+    barrier(world)
+    lib.rc_profile_report(buf, len(buf))
+    lib.rc_profile_enable(0)
+    prof = json.loads(buf.value.decode())
+    ms = max_over_ranks(ev0.elapsed_time(ev1), world)
+    ms_per_step = ms / args.steps
+    value = world * B * args.steps / (ms / 1e3)
+
+    # ---- per-op path (drop-in: one call per pair), latency distribution ----
+    per_op_ms = []
+    torch.cuda.synchronize()
+    t_total0 = torch.cuda.Event(enable_timing=True)
+    t_total1 = torch.cuda.Event(enable_timing=True)
+    evs = [(torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)) for _ in range(B)]
+    per_op_outs = [C.RcCiphertext(o.data_ptr(), 0, 0) for o in outs]
+    for i in range(min(B, 4)):  # warm
+        C.call("rc_mult_relinearized", ctx.handle, ctypes.byref(L[i]), ctypes.byref(R[i]), key.handle,
+               ctypes.byref(per_op_outs[i]), s_ptr)
+    torch.cuda.synchronize()
+    t_total0.record(stream)
+    for i in range(B):
+        evs[i][0].record(stream)
+        C.call("rc_mult_relinearized", ctx.handle, ctypes.byref(L[i]), ctypes.byref(R[i]), key.handle,
+               ctypes.byref(per_op_outs[i]), s_ptr)
+        evs[i][1].record(stream)
+    t_total1.record(stream)
+    torch.cuda.synchronize()
+    per_op_ms = [a.elapsed_time(b) for a, b in evs]
+    per_op_value = B / (t_total0.elapsed_time(t_total1) / 1e3)
+
+    # ---- e2e through the host-buffer entry point (pinned host memory) ----
+    host_l = [torch.empty((2, limbs, n), dtype=torch.int64, pin_memory=True) for _ in range(B)]
+    host_r = [torch.empty((2, limbs, n), dtype=torch.int64, pin_memory=True) for _ in range(B)]
+    host_o = [torch.empty((2, limbs - 1, n), dtype=torch.int64, pin_memory=True) for _ in range(B)]
+    for i in range(B):
+        host_l[i].copy_(lhs[i].data)
+        host_r[i].copy_(rhs[i].data)
+    HL = (ctypes.c_void_p * B)(*[t.data_ptr() for t in host_l])
+    HR = (ctypes.c_void_p * B)(*[t.data_ptr() for t in host_r])
+    HO = (ctypes.c_void_p * B)(*[t.data_ptr() for t in host_o])
+    LV = (ctypes.c_int32 * B)(*([limbs - 1] * B))
+    SB = (ctypes.c_int32 * B)(*[x.scale_bits for x in lhs])
+    OSB = (ctypes.c_int32 * B)()
+
+    def e2e_step():
+        C.call("rc_mult_relinearized_batch_host", ctx.handle, B, HL, HR, LV, SB, K, HO, OSB, s_ptr)
+
+    e2e_step()
+    torch.cuda.synchronize()
+    e_steps = max(1, min(args.steps, 5))
+    barrier(world)
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(e_steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e_ms = max_over_ranks(e0.elapsed_time(e1), world)
+    e2e_value = world * B * e_steps / (e_ms / 1e3)
+    h2d = B * 2 * 2 * limbs * n * 8
+    d2h = B * 2 * (limbs - 1) * n * 8
+
+    # ---- checks: bit-exact vs the CPU oracle (one pair), decoded slot error vs FP64 ----
+    result = {
+        "metric": METRIC, "value": round(value, 3), "unit": UNIT, "n_gpus": world, "steps": args.steps,
+        "warmup": max(args.warmup, 3), "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "u64 (exact modular integer)",
+        "data": "synthetic: seeded encryptions of uniform [-1,1] complex slots; seeded keys",
+        "config": {"workload": "mult_relinearized (tensor+relinearize+rescale), hybrid keyswitch",
+                   "poly_degree": n, "limbs": limbs, "aux_limbs": aux, "prime_bits": 50,
+                   "gadget": "balanced base-2^30", "digits": digits, "batch": B,
+                   "parallelism": f"replicas x{world}",
+                   "l2": "no flush: each step reads ~%.1f GB of inputs and key (L2 129 MB)"
+                         % ((B * 4 * limbs + digits * 2 * (limbs + aux)) * n * 8 / 1e9)},
+        "per_op": {"value": round(per_op_value, 3), "unit": UNIT,
+                   "p50_ms": round(float(np.percentile(per_op_ms, 50)), 4),
+                   "p99_ms": round(float(np.percentile(per_op_ms, 99)), 4)},
+        "batched_vs_per_op": round(value / world / per_op_value, 3),
+        "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
+        "gpu_launches": int(sum(v["launches"] for v in prof.values())),
+        "clocks": clk.summary(),
+    }
+    # roofline of the dominant kernel
+    peak, peak_kind = peaks()
+    dom = max(prof.items(), key=lambda kv: kv[1]["ms"]) if prof else None
+    if dom:
+        name, st = dom
+        per_launch_ms = st["ms"] / st["launches"]
+        ab = algorithmic_bytes(name, B * args.steps, n, limbs, aux, digits, st["launches"])
+        achieved = (ab / (per_launch_ms / 1e3) / 1e9) if ab else None
+        result["roofline"] = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1) if achieved else None,
+                              "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
+                              "peak_kind": peak_kind, "traffic": None,
+                              "share": round(st["ms"] / sum(v["ms"] for v in prof.values()), 4)}
+    hm = hmult_algorithmic_bytes(n, limbs, aux, digits)
+    result["hmult_roofline"] = {"algorithmic_bytes_per_op": hm,
+                                "achieved_GBs": round(hm * value / world / 1e9, 1),
+                                "frac": round(hm * value / world / 1e9 / peak, 4)}
+    result["kernels"] = {k: {"launches": v["launches"], "ms_per_step": round(v["ms"] / args.steps, 4)}
+                         for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}
+
+    # decoded error of pair 0
+    out0 = C.RnsCiphertext(outs[0], OSB[0], limbs - 2)
+    dec = ctx.decode_at_scale(ctx.decrypt(out0, W["kp"].secret_key), OSB[0])
+    ref = W["slots_a"][0] * W["slots_b"][0]
+    result["decoded_max_abs_err"] = float(np.max(np.abs(dec - ref)))
+
+    if rank == 0 and world == 1 and not args.no_cpu:
+        O = load_oracle()
+        threads = os.cpu_count() or 1
+        key_np = C.to_host(W["key_coeff"])
+        lnp, rnp = lhs[0].numpy(), rhs[0].numpy()
+        secs, ref_out = cpu_oracle_op(O, params, lnp, rnp, key_np, threads)
+        got = C.to_host(outs[0])
+        result["bit_exact_vs_cpu"] = bool(np.array_equal(got[0], ref_out[0]) and np.array_equal(got[1], ref_out[1]))
+        result["cpu_baseline"] = {"value": round(1.0 / secs, 5), "unit": UNIT, "cores": threads, "kind": "port",
+                                  "sample": "1 faithful HMult+relin (pair 0 of the batch, same key) on the oracle "
+                                            f"(C restatement of the reference CPU path), {secs:.1f} s"}
+    if rank == 0:
+        print(json.dumps(result), flush=True)
+    if world > 1:
+        import torch.distributed as dist
+        dist.destroy_process_group()
+
+
+def run_reference(args):
+    rank, world, local = dist_setup(args.gpus)
+    if rank != 0:
+        return
+    pkg = load_package()
+    O = load_oracle()
+    params = pkg.params.bench_params()
+    n = params.poly_degree
+    q = params.q_moduli()
+    allm = q + params.p_moduli()
+    rng = np.random.default_rng(args.seed)
+    D = pkg.params.num_decomp_digits(pkg.params.modulus_bits(q))
+
+    def rp(m):
+        return np.stack([rng.integers(0, x, n, dtype=np.uint64) for x in m])
+
+    lhs, rhs = np.stack([rp(q), rp(q)]), np.stack([rp(q), rp(q)])
+    key = np.stack([np.stack([rp(allm), rp(allm)]) for _ in range(D)])
+    threads = os.cpu_count() or 1
+    for _ in range(min(args.warmup, 1)):
+        cpu_oracle_op(O, params, lhs, rhs, key, threads)
+    t0 = time.perf_counter()
+    for _ in range(args.steps):
+        cpu_oracle_op(O, params, lhs, rhs, key, threads)
+    secs = time.perf_counter() - t0
+    value = args.steps / secs
+    print(json.dumps({
+        "impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": world,
+        "steps": args.steps, "warmup": min(args.warmup, 1), "ms_per_step": round(secs / args.steps * 1e3, 1),
+        "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (exact modular integer)",
+        "data": "synthetic: seeded uniform residues and key",
+        "config": {"workload": "mult_relinearized (tensor+relinearize+rescale), hybrid keyswitch", "poly_degree": n,
+                   "limbs": len(q), "aux_limbs": len(params.aux_primes), "prime_bits": 50,
+                   "gadget": "balanced base-2^30", "digits": D, "batch": 1, "parallelism": "host threads"},
+        "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": "one faithful HMult+relin per step on the oracle (C restatement of the "
+                                   "reference CPU path: per-call NTT round trips, u128 %, Garner gadget); "
+                                   "the Rust crate itself cannot be built here (no Rust toolchain)"},
+        "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
+    }), flush=True)
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=10)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--batch", type=int, default=32)
+    ap.add_argument("--seed", type=int, default=0x5EED + 2)
+    ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
+    ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_gpu(args)
+
+
+if __name__ == "__main__":
+    main()

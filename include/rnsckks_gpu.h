@@ -188,6 +188,14 @@ int rc_encode(const rc_context* ctx, const double* slots, int32_t level, uint32_
 int rc_decode(const rc_context* ctx, const uint64_t* poly_host, int32_t level, uint32_t scale_bits,
               double* slots_out);
 
+/* ---- instrumentation (no reference counterpart: the reference only has
+ * std::time::Instant around whole ops, examples/operations/timings.rs:282-308) ----
+ * When enabled, every kernel launch is bracketed by CUDA events on its stream;
+ * rc_profile_report synchronizes the device and writes a JSON object
+ * {"kernel": {"launches": n, "ms": total}, ...} into buf, then resets. */
+int rc_profile_enable(int on);
+int rc_profile_report(char* buf, size_t len);
+
 #ifdef __cplusplus
 }
 #endif

@@ -9,6 +9,17 @@
 
 namespace rc {
 
+// per-kernel event timing (profile.cu); no-ops unless rc_profile_enable(1)
+bool prof_enabled();
+void prof_begin(const char* name, cudaStream_t s);
+void prof_end(const char* name, cudaStream_t s);
+struct ProfScope {
+  const char* n;
+  cudaStream_t s;
+  ProfScope(const char* name, cudaStream_t st) : n(name), s(st) { prof_begin(n, s); }
+  ~ProfScope() { prof_end(n, s); }
+};
+
 // Up to MAXP polynomials per launch, addressed through a by-value pointer table
 // (kernel parameters, so launches need no extra upload and can be captured in
 // CUDA graphs).  Limb j of polynomial k lives at p[k] + j * N.

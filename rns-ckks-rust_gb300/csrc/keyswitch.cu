@@ -501,6 +501,7 @@ void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int
   const int threads = N < 128 ? N : 128;
   dim3 g((N + threads - 1) / threads, jobs);
   const int W = dt.W;
+  ProfScope p("decompose", s);
   if (W <= 4) k_decompose<4><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
   else if (W <= 8) k_decompose<8><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
   else if (W <= 16) k_decompose<16><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
@@ -534,9 +535,15 @@ void digit_ntt_mac(const KsArgs& a, const int32_t* digits, const u64* const* key
   for (int p0 = 0; p0 < pairs; p0 += chunk) {
     const int pc_count = (pairs - p0) < chunk ? (pairs - p0) : chunk;
     dim3 g1(N2 / COLS, a.D * pc_count);
-    k_digit_cols<<<g1, threads_c, N1 * COLS * sizeof(u64), s>>>(a, *a.dt, digits, scratch, p0, pc_count);
+    {
+      ProfScope p("digit_cols", s);
+      k_digit_cols<<<g1, threads_c, N1 * COLS * sizeof(u64), s>>>(a, *a.dt, digits, scratch, p0, pc_count);
+    }
     dim3 g2(N1 / rows, pc_count);
-    k_digit_rows_mac<<<g2, threads_r, tile * sizeof(u64), s>>>(a, scratch, kt, acc, p0);
+    {
+      ProfScope p("digit_rows_mac", s);
+      k_digit_rows_mac<<<g2, threads_r, tile * sizeof(u64), s>>>(a, scratch, kt, acc, p0);
+    }
   }
 }
 
@@ -546,6 +553,7 @@ void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const
   const int N = f.n;
   const int threads = N < 128 ? N : 128;
   dim3 g((N + threads - 1) / threads, 2 * jobs);
+  ProfScope p("finalize", s);
   k_finalize<<<g, threads, 0, s>>>(f, acc, addend, out);
 }
 

@@ -191,8 +191,14 @@ void ntt_forward(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int pol
   const int N = 1 << a.log_n, N1 = 1 << a.n1, N2 = N >> a.n1;
   const int COLS = cols_per_cta(N2), ROWS = rows_per_cta(N1, N2);
   dim3 g1(N2 / COLS, limbs, polys), g2(N1 / ROWS, limbs, polys);
-  k_fwd_cols<<<g1, threads_for(N1 * COLS / 2), N1 * COLS * sizeof(u64), s>>>(a, src, dst, map);
-  k_fwd_rows<<<g2, threads_for(ROWS * N2 / 2), ROWS * N2 * sizeof(u64), s>>>(a, dst, dst, map);
+  {
+    ProfScope p("ntt_fwd_cols", s);
+    k_fwd_cols<<<g1, threads_for(N1 * COLS / 2), N1 * COLS * sizeof(u64), s>>>(a, src, dst, map);
+  }
+  {
+    ProfScope p("ntt_fwd_rows", s);
+    k_fwd_rows<<<g2, threads_for(ROWS * N2 / 2), ROWS * N2 * sizeof(u64), s>>>(a, dst, dst, map);
+  }
 }
 
 void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
@@ -201,8 +207,14 @@ void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int pol
   const int N = 1 << a.log_n, N1 = 1 << a.n1, N2 = N >> a.n1;
   const int COLS = cols_per_cta(N2), ROWS = rows_per_cta(N1, N2);
   dim3 g1(N2 / COLS, limbs, polys), g2(N1 / ROWS, limbs, polys);
-  k_inv_rows<<<g2, threads_for(ROWS * N2 / 2), ROWS * N2 * sizeof(u64), s>>>(a, src, dst, map);
-  k_inv_cols<<<g1, threads_for(N1 * COLS / 2), N1 * COLS * sizeof(u64), s>>>(a, dst, dst, map);
+  {
+    ProfScope p("ntt_inv_rows", s);
+    k_inv_rows<<<g2, threads_for(ROWS * N2 / 2), ROWS * N2 * sizeof(u64), s>>>(a, src, dst, map);
+  }
+  {
+    ProfScope p("ntt_inv_cols", s);
+    k_inv_cols<<<g1, threads_for(N1 * COLS / 2), N1 * COLS * sizeof(u64), s>>>(a, dst, dst, map);
+  }
 }
 
 }  // namespace rc

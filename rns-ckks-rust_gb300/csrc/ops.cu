@@ -124,6 +124,7 @@ void ew_binary(EwOp op, const PrimeConst* pc, const PtrTab& a, const PtrTab& b, 
   if (polys <= 0) return;
   int log_n = __builtin_ctz(n);
   dim3 g(grid_for((size_t)limbs * n, 256), polys);
+  ProfScope p("elementwise", s);
   k_ew_binary<<<g, 256, 0, s>>>(op == EwOp::Add ? 0 : op == EwOp::Sub ? 1 : 2, pc, a, b, b_shared, out, limbs, map,
                                 log_n);
 }
@@ -137,6 +138,7 @@ void tensor_ntt(const PrimeConst* pc, const PtrTab& in4, const PtrTab& out3, int
                 cudaStream_t s) {
   if (jobs <= 0) return;
   dim3 g(grid_for((size_t)limbs * n, 256), jobs);
+  ProfScope p("tensor", s);
   k_tensor<<<g, 256, 0, s>>>(pc, in4, out3, limbs, __builtin_ctz(n));
 }
 
@@ -144,6 +146,7 @@ void automorphism(const PrimeConst* pc, const PtrTab& in, const PtrTab& out, int
                   int log_n, cudaStream_t s) {
   if (polys <= 0) return;
   dim3 g(grid_for((size_t)limbs << log_n, 256), polys);
+  ProfScope p("automorphism", s);
   k_automorphism<<<g, 256, 0, s>>>(pc, in, out, limbs, g_inv, log_n);
 }
 
@@ -151,6 +154,7 @@ void rescale(const PrimeConst* pc, const RescaleTab& rt, int L, const PtrTab& in
              int limbs, int n, cudaStream_t s) {
   if (polys <= 0) return;
   dim3 g((n + 255) / 256, polys);
+  ProfScope p("rescale", s);
   k_rescale<<<g, 256, 0, s>>>(pc, rt, L, in, out, limbs, __builtin_ctz(n));
 }
 
