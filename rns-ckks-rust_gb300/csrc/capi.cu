@@ -3,6 +3,7 @@
 // points.  Preconditions that the reference asserts (and panics on) become
 // RC_ERR_INVALID_ARGUMENT with the reference's message.
 #include <cmath>
+#include <cstdlib>
 #include <cstring>
 #include <string>
 
@@ -226,6 +227,7 @@ void keyswitch_core(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, u
   ka.K = K;
   ka.D = D;
   ka.key_digits = (int)k0->digits;
+  ka.mac64 = c->mac64 ? 1 : 0;
   ka.dt = &li.dt;
   std::vector<const uint64_t*> keys(J);
   for (int j = 0; j < J; ++j) keys[j] = jobs[j].key->data;
@@ -434,9 +436,18 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
     c->root = qg;
     c->root.insert(c->root.end(), pg.begin(), pg.end());
     const int P = c->L + c->K;
+    // Lazy (unreduced) forward butterflies need every prime < 2^58; they are
+    // opt-in because the compiler schedules them with far more live registers.
+    c->lazy = false;
+    if (const char* e = getenv("RNSCKKS_LAZY_NTT")) c->lazy = atoi(e) != 0;
+    for (uint64_t q : c->mod) c->lazy = c->lazy && q < (1ull << 58);
+    if (const char* e = getenv("RNSCKKS_MAC64")) c->mac64 = atoi(e) != 0;
 
     // ---- per-prime constants and twiddles
     std::vector<PrimeConst> pcs(P);
+    // bound (in multiples of q) of a forward-NTT output fed to the key product:
+    // 2q per stage above q when lazy, 4q otherwise
+    const uint64_t out_bound = c->lazy ? (uint64_t)(2 * c->log_n + 1) : 4;
     std::vector<Twiddle> twf((size_t)P * N), twi((size_t)P * N);
     for (int i = 0; i < P; ++i) {
       const uint64_t q = c->mod[i];
@@ -453,7 +464,10 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
       k.n_inv = invmod_h(N % q, q);
       k.n_inv_s = shoup_h(k.n_inv, q);
       k.r2 = (uint64_t)((((u128h)1 << 64) % q) * (((u128h)1 << 64) % q) % q);
-      k.mac_chunk = (uint64_t)(~0ull / q) - 1;
+      k.one_s = shoup_h(1, q);
+      // key words are < q: sum of chunk products stays below q * 2^64
+      k.mac_chunk = (uint64_t)((~0ull) / (out_bound * q));
+      k.mac_chunk64 = (uint64_t)((~0ull) / (2 * q));
       // psi = g^((q-1)/2N) (NttPlan::new, ntt.rs:42)
       const uint64_t psi = powmod_h(c->root[i] % q, (q - 1) / (2 * N), q);
       const uint64_t psi_inv = invmod_h(psi, q);

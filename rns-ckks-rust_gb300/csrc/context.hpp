@@ -60,6 +60,8 @@ struct rc_context {
   int L = 0, K = 0;
   int scale_bits = 0;
   int device = 0;
+  bool lazy = false;   // every prime < 2^58
+  bool mac64 = false;  // 64-bit per-term Montgomery accumulation in the key product
   std::vector<uint64_t> mod, root;  // Q then P
   std::unique_ptr<rc::DevBuf> pc_buf, tw_buf, md_buf, rt_buf;
   rc::PrimeConst* d_pc = nullptr;
@@ -80,6 +82,7 @@ struct rc_context {
     a.tw_inv = d_twi;
     a.log_n = log_n;
     a.n1 = n1;
+    a.lazy = lazy ? 1 : 0;
     return a;
   }
 };

@@ -42,7 +42,8 @@ struct NttArgs {
   const Twiddle* tw_fwd;  // [primes][N]: psi^bitrev(k)
   const Twiddle* tw_inv;  // [primes][N]: psi^-bitrev(k)
   int log_n;
-  int n1;  // column-phase size 2^n1; row-phase size 2^(log_n - n1)
+  int n1;    // column-phase size 2^n1; row-phase size 2^(log_n - n1)
+  int lazy;  // all primes < 2^58: forward butterflies skip the [0,4q) correction
 };
 
 // Negacyclic NTT over `polys` x `limbs` limbs, src -> dst (may alias).
@@ -121,6 +122,7 @@ struct KsArgs {
   int K;          // aux limbs used (0 = Q-only)
   int D;          // digits decomposed (and used from the key)
   int key_digits; // digits stored per key limb
+  int mac64;      // key product with 64-bit per-term Montgomery accumulators
   const DecompTab* dt;
 };
 

@@ -19,6 +19,7 @@
 //  * finalize: ModDown by exact centred Garner over the aux primes, optional
 //    addend (relinearize / rotate) and optional rescale in one pass.
 #include "kernels.cuh"
+#include "nttcore.cuh"
 
 namespace rc {
 
@@ -343,6 +344,251 @@ __global__ void k_digit_rows_mac(KsArgs a, const u64* scratch, KeyTab keys, u64*
 }
 
 // ---------------------------------------------------------------------------
+// fast path (log N in 12..16): warp-level register-blocked digit transforms
+// ---------------------------------------------------------------------------
+template <int M>
+struct DigitColTile {
+  static constexpr int COLS = (8 * core::Geo<M>::SUBS) > 16 ? 8 * core::Geo<M>::SUBS : 16;
+};
+
+template <int M1, int M2, bool LAZY>
+__global__ __launch_bounds__(256, 2) void k_digit_cols_f(KsArgs a, DecompTab dt, const int32_t* digits, u64* scratch,
+                                                      int p0, int pc_count) {
+  using G = core::Geo<M1>;
+  constexpr int COLS = DigitColTile<M1>::COLS, N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2;
+  __shared__ u64 tile[COLS * G::STRIDE];
+  const int c0 = blockIdx.x * COLS;
+  const int digit = blockIdx.y / pc_count, pl = blockIdx.y % pc_count;
+  const int total = a.qlimbs + a.K;
+  const int pair = p0 + pl;
+  const int job = pair / total, limb = pair % total;
+  const LimbMap map{a.qlimbs, a.L};
+  const int prime = map.prime(limb);
+  const u64 q = a.pc[prime].q;
+  const bool aux = limb >= a.qlimbs;
+  const Twiddle* tw = a.ntt.tw_fwd + (size_t)prime * N;
+  const int32_t* in = digits + ((size_t)job * a.D + digit) * N;
+  u64* out = scratch + ((size_t)pl * a.D + digit) * N;
+  for (int idx = threadIdx.x; idx < N1 * COLS; idx += 256) {
+    const int r = idx / COLS, c = idx % COLS;
+    const int32_t d = in[(size_t)r * N2 + c0 + c];
+    tile[c * G::STRIDE + core::swz<M1>(r)] = aux ? lifted_residue(d, q, dt) : digit_residue(d, q);
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / G::LANES, l = lane % G::LANES;
+#pragma unroll 1
+  for (int cb = warp * G::SUBS; cb < COLS; cb += 8 * G::SUBS) {
+    const int lv = core::lane_id_volatile();
+    const int sub = lv / G::LANES, l = lv % G::LANES;
+    u64* buf = tile + (cb + sub) * G::STRIDE;
+    u64 v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::first_idx<M1>(l, k))];
+    __syncwarp();
+    core::fwd_sub<M1, LAZY>(v, buf, l, tw, 1, q);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::last_idx<M1>(l, k))] = v[k];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < N1 * COLS; idx += 256) {
+    const int r = idx / COLS, c = idx % COLS;
+    out[(size_t)r * N2 + c0 + c] = tile[c * G::STRIDE + core::swz<M1>(r)];
+  }
+}
+
+constexpr int MAC_WARPS = 4;
+
+template <int M1, int M2, bool LAZY>
+__global__ __launch_bounds__(32 * MAC_WARPS, 3) void k_digit_rows_mac_f(KsArgs a, const u64* scratch, KeyTab keys,
+                                                                      u64* acc, int p0) {
+  using G = core::Geo<M2>;
+  constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = MAC_WARPS * G::SUBS;
+  __shared__ u64 bufs[MAC_WARPS * G::SUBS * G::STRIDE];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / G::LANES, l = lane % G::LANES;
+  const int row = blockIdx.x * ROWS + warp * G::SUBS + sub;
+  const int pl = blockIdx.y;
+  const int total = a.qlimbs + a.K;
+  const int pair = p0 + pl;
+  const int job = pair / total, limb = pair % total;
+  const LimbMap map{a.qlimbs, a.L};
+  const int prime = map.prime(limb);
+  const PrimeConst& pc = a.pc[prime];
+  const u64 q = pc.q;
+  const Twiddle* tw = a.ntt.tw_fwd + (size_t)prime * N;
+  const u64* key = keys.k[job] + (size_t)limb * a.key_digits * 2 * N + (size_t)row * N2;
+  u64* buf = bufs + (warp * G::SUBS + sub) * G::STRIDE;
+
+  U128 acc0[8], acc1[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc0[k].lo = acc0[k].hi = acc1[k].lo = acc1[k].hi = 0;
+  const u64 chunk = pc.mac_chunk;
+  u64 since = 0;
+#pragma unroll 1
+  for (int digit = 0; digit < a.D; ++digit) {
+    const int l = core::lane_id_volatile() % G::LANES;
+    const u64* in = scratch + ((size_t)pl * a.D + digit) * N + (size_t)row * N2;
+    u64 v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = in[core::first_idx<M2>(l, k)];
+    core::fwd_sub<M2, LAZY>(v, buf, l, tw, (u64)(N1 + row), q);
+    const u64* k0 = key + (size_t)digit * 2 * N;
+    const u64* k1 = k0 + N;
+#pragma unroll
+    for (int k = 0; k < 8; k += 2) {
+      const int pos = core::last_idx<M2>(l, k);  // pos, pos+1 hold elements k, k+1
+      const ulonglong2 w0 = *reinterpret_cast<const ulonglong2*>(k0 + pos);
+      const ulonglong2 w1 = *reinterpret_cast<const ulonglong2*>(k1 + pos);
+      add_to(acc0[k], mul_wide(v[k], w0.x));
+      add_to(acc0[k + 1], mul_wide(v[k + 1], w0.y));
+      add_to(acc1[k], mul_wide(v[k], w1.x));
+      add_to(acc1[k + 1], mul_wide(v[k + 1], w1.y));
+    }
+    if (++since == chunk) {  // fold: keep the sums congruent mod q and small
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        acc0[k].lo = barrett_reduce(acc0[k], pc);
+        acc0[k].hi = 0;
+        acc1[k].lo = barrett_reduce(acc1[k], pc);
+        acc1[k].hi = 0;
+      }
+      since = 1;
+    }
+  }
+  u64* out0 = acc + ((size_t)job * 2 * total + limb) * N + (size_t)row * N2;
+  u64* out1 = out0 + (size_t)total * N;
+#pragma unroll
+  for (int k = 0; k < 8; k += 2) {
+    const int pos = core::last_idx<M2>(l, k);
+    ulonglong2 o0, o1;
+    o0.x = mont_reduce(acc0[k], pc);
+    o0.y = mont_reduce(acc0[k + 1], pc);
+    o1.x = mont_reduce(acc1[k], pc);
+    o1.y = mont_reduce(acc1[k + 1], pc);
+    *reinterpret_cast<ulonglong2*>(out0 + pos) = o0;
+    *reinterpret_cast<ulonglong2*>(out1 + pos) = o1;
+  }
+}
+
+// Same transform with 64-bit accumulators: each product is Montgomery-reduced
+// on the fly without the final subtraction (a term is < 2q), halving the
+// accumulator registers at the cost of one extra 64x64 high product per term.
+template <int M1, int M2, bool LAZY>
+__global__ __launch_bounds__(32 * MAC_WARPS, 4) void k_digit_rows_mac64_f(KsArgs a, const u64* scratch,
+                                                                          KeyTab keys, u64* acc, int p0) {
+  using G = core::Geo<M2>;
+  constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = MAC_WARPS * G::SUBS;
+  __shared__ u64 bufs[MAC_WARPS * G::SUBS * G::STRIDE];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / G::LANES, l = lane % G::LANES;
+  const int row = blockIdx.x * ROWS + warp * G::SUBS + sub;
+  const int pl = blockIdx.y;
+  const int total = a.qlimbs + a.K;
+  const int pair = p0 + pl;
+  const int job = pair / total, limb = pair % total;
+  const LimbMap map{a.qlimbs, a.L};
+  const int prime = map.prime(limb);
+  const PrimeConst& pc = a.pc[prime];
+  const u64 q = pc.q, qn = pc.qinv_neg;
+  const Twiddle* tw = a.ntt.tw_fwd + (size_t)prime * N;
+  const u64* key = keys.k[job] + (size_t)limb * a.key_digits * 2 * N + (size_t)row * N2;
+  u64* buf = bufs + (warp * G::SUBS + sub) * G::STRIDE;
+  u64 acc0[8], acc1[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) acc0[k] = acc1[k] = 0;
+  const u64 chunk = pc.mac_chunk64;
+  u64 since = 0;
+  auto term = [&](u64 x, u64 y) -> u64 {  // (x*y + m*q) / 2^64 with m = -(x*y) q^-1 mod 2^64: < 2q
+    const u64 lo = x * y, hi = mulhi(x, y);
+    const u64 m = lo * qn;
+    return hi + mulhi(m, q) + (lo != 0 ? 1ull : 0ull);
+  };
+#pragma unroll 1
+  for (int digit = 0; digit < a.D; ++digit) {
+    const int l = core::lane_id_volatile() % G::LANES;
+    const u64* in = scratch + ((size_t)pl * a.D + digit) * N + (size_t)row * N2;
+    u64 v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = in[core::first_idx<M2>(l, k)];
+    core::fwd_sub<M2, LAZY>(v, buf, l, tw, (u64)(N1 + row), q);
+    const u64* k0 = key + (size_t)digit * 2 * N;
+    const u64* k1 = k0 + N;
+#pragma unroll
+    for (int k = 0; k < 8; k += 2) {
+      const int pos = core::last_idx<M2>(l, k);
+      const ulonglong2 w0 = *reinterpret_cast<const ulonglong2*>(k0 + pos);
+      const ulonglong2 w1 = *reinterpret_cast<const ulonglong2*>(k1 + pos);
+      acc0[k] += term(v[k], w0.x);
+      acc0[k + 1] += term(v[k + 1], w0.y);
+      acc1[k] += term(v[k], w1.x);
+      acc1[k + 1] += term(v[k + 1], w1.y);
+    }
+    if (++since == chunk) {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        U128 t0, t1;
+        t0.lo = acc0[k];
+        t0.hi = 0;
+        t1.lo = acc1[k];
+        t1.hi = 0;
+        acc0[k] = barrett_reduce(t0, pc);
+        acc1[k] = barrett_reduce(t1, pc);
+      }
+      since = 1;
+    }
+  }
+  u64* out0 = acc + ((size_t)job * 2 * total + limb) * N + (size_t)row * N2;
+  u64* out1 = out0 + (size_t)total * N;
+#pragma unroll
+  for (int k = 0; k < 8; k += 2) {
+    const int pos = core::last_idx<M2>(l, k);
+    U128 t;
+    t.hi = 0;
+    ulonglong2 o0, o1;
+    t.lo = acc0[k];
+    o0.x = barrett_reduce(t, pc);
+    t.lo = acc0[k + 1];
+    o0.y = barrett_reduce(t, pc);
+    t.lo = acc1[k];
+    o1.x = barrett_reduce(t, pc);
+    t.lo = acc1[k + 1];
+    o1.y = barrett_reduce(t, pc);
+    *reinterpret_cast<ulonglong2*>(out0 + pos) = o0;
+    *reinterpret_cast<ulonglong2*>(out1 + pos) = o1;
+  }
+}
+
+template <int M1, int M2, bool LAZY>
+void digit_fast(const KsArgs& a, const int32_t* digits, const KeyTab& kt, u64* acc, u64* scratch, int p0, int pcc,
+                cudaStream_t s) {
+  {
+    ProfScope p("digit_cols", s);
+    dim3 g1((1 << M2) / DigitColTile<M1>::COLS, a.D * pcc);
+    k_digit_cols_f<M1, M2, LAZY><<<g1, 256, 0, s>>>(a, *a.dt, digits, scratch, p0, pcc);
+  }
+  {
+    ProfScope p("digit_rows_mac", s);
+    dim3 g2((1 << M1) / (MAC_WARPS * core::Geo<M2>::SUBS), pcc);
+    if (a.mac64) k_digit_rows_mac64_f<M1, M2, LAZY><<<g2, 32 * MAC_WARPS, 0, s>>>(a, scratch, kt, acc, p0);
+    else k_digit_rows_mac_f<M1, M2, LAZY><<<g2, 32 * MAC_WARPS, 0, s>>>(a, scratch, kt, acc, p0);
+  }
+}
+
+template <bool LAZY>
+bool digit_dispatch(const KsArgs& a, const int32_t* digits, const KeyTab& kt, u64* acc, u64* scratch, int p0,
+                    int pcc, cudaStream_t s) {
+  switch (a.ntt.log_n) {
+    case 12: digit_fast<6, 6, LAZY>(a, digits, kt, acc, scratch, p0, pcc, s); return true;
+    case 13: digit_fast<6, 7, LAZY>(a, digits, kt, acc, scratch, p0, pcc, s); return true;
+    case 14: digit_fast<7, 7, LAZY>(a, digits, kt, acc, scratch, p0, pcc, s); return true;
+    case 15: digit_fast<7, 8, LAZY>(a, digits, kt, acc, scratch, p0, pcc, s); return true;
+    case 16: digit_fast<8, 8, LAZY>(a, digits, kt, acc, scratch, p0, pcc, s); return true;
+    default: return false;
+  }
+}
+
+// ---------------------------------------------------------------------------
 // finalize: ModDown + addend + rescale
 // ---------------------------------------------------------------------------
 constexpr int KMAX = 8;
@@ -534,6 +780,9 @@ void digit_ntt_mac(const KsArgs& a, const int32_t* digits, const u64* const* key
   const int rows = tile / N2;
   for (int p0 = 0; p0 < pairs; p0 += chunk) {
     const int pc_count = (pairs - p0) < chunk ? (pairs - p0) : chunk;
+    if (a.ntt.lazy ? digit_dispatch<true>(a, digits, kt, acc, scratch, p0, pc_count, s)
+                   : digit_dispatch<false>(a, digits, kt, acc, scratch, p0, pc_count, s))
+      continue;
     dim3 g1(N2 / COLS, a.D * pc_count);
     {
       ProfScope p("digit_cols", s);

@@ -32,8 +32,10 @@ struct PrimeConst {
   u64 qinv_neg;       // -q^-1 mod 2^64
   u64 n_inv, n_inv_s; // N^-1 mod q and its Shoup companion
   u64 r2;             // 2^128 mod q (R^2 for Montgomery conversion)
-  u64 mac_chunk;      // products (each < q^2) that can be summed below q * 2^64
-  u64 pad[7];
+  u64 mac_chunk;      // products of a lazy NTT output and a key word that sum below q * 2^64
+  u64 one_s;          // floor(2^64 / q): Shoup companion of 1 (reduces x < 2^64 to [0, 2q))
+  u64 mac_chunk64;    // per-term Montgomery values (< 2q each) that sum below 2^64
+  u64 pad[5];
 };
 
 #ifdef __CUDACC__

@@ -16,6 +16,7 @@
 // the row kernel a tile of rows.  Arithmetic is Harvey's lazy Shoup butterfly
 // (values in [0, 4q) forward, [0, 2q) inverse; q < 2^61).
 #include "kernels.cuh"
+#include "nttcore.cuh"
 
 namespace rc {
 
@@ -177,6 +178,203 @@ __global__ void k_inv_cols(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
   }
 }
 
+// ---------------------------------------------------------------------------
+// fast path, log N in 12..16: warp-level register-blocked sub-transforms
+// ---------------------------------------------------------------------------
+template <int M>
+struct ColTile {
+  static constexpr int COLS = (8 * core::Geo<M>::SUBS) > 16 ? 8 * core::Geo<M>::SUBS : 16;
+};
+
+// x < 33q (lazy) or < 4q -> [0, q)
+template <bool LAZY>
+__device__ __forceinline__ u64 reduce_out(u64 x, const PrimeConst& c) {
+  if (LAZY) {
+    x = mul_shoup_lazy(x, 1, c.one_s, c.q);
+    return x >= c.q ? x - c.q : x;
+  }
+  return reduce_4q(x, c.q);
+}
+
+template <int M1, int M2, bool LAZY>
+__global__ __launch_bounds__(256, 2) void k_fwd_cols_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
+  using G = core::Geo<M1>;
+  constexpr int COLS = ColTile<M1>::COLS, N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2;
+  __shared__ u64 tile[COLS * G::STRIDE];
+  const int c0 = blockIdx.x * COLS;
+  const int limb = blockIdx.y, poly = blockIdx.z;
+  const int prime = map.prime(limb);
+  const u64 q = a.pc[prime].q;
+  const Twiddle* tw = a.tw_fwd + (size_t)prime * N;
+  const u64* in = src.p[poly] + (size_t)limb * N;
+  u64* out = dst.p[poly] + (size_t)limb * N;
+  for (int idx = threadIdx.x; idx < N1 * COLS; idx += 256) {
+    const int r = idx / COLS, c = idx % COLS;
+    tile[c * G::STRIDE + core::swz<M1>(r)] = in[(size_t)r * N2 + c0 + c];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / G::LANES, l = lane % G::LANES;
+#pragma unroll 1
+  for (int cb = warp * G::SUBS; cb < COLS; cb += 8 * G::SUBS) {
+    const int lv = core::lane_id_volatile();
+    const int sub = lv / G::LANES, l = lv % G::LANES;
+    u64* buf = tile + (cb + sub) * G::STRIDE;
+    u64 v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::first_idx<M1>(l, k))];
+    __syncwarp();
+    core::fwd_sub<M1, LAZY>(v, buf, l, tw, 1, q);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::last_idx<M1>(l, k))] = v[k];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < N1 * COLS; idx += 256) {
+    const int r = idx / COLS, c = idx % COLS;
+    out[(size_t)r * N2 + c0 + c] = tile[c * G::STRIDE + core::swz<M1>(r)];
+  }
+}
+
+template <int M1, int M2, bool LAZY>
+__global__ __launch_bounds__(256) void k_fwd_rows_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
+  using G = core::Geo<M2>;
+  constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = 8 * G::SUBS;
+  __shared__ u64 bufs[8 * G::SUBS * G::STRIDE];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / G::LANES, l = lane % G::LANES;
+  const int row = blockIdx.x * ROWS + warp * G::SUBS + sub;
+  const int limb = blockIdx.y, poly = blockIdx.z;
+  const int prime = map.prime(limb);
+  const PrimeConst& pc = a.pc[prime];
+  const Twiddle* tw = a.tw_fwd + (size_t)prime * N;
+  const u64* in = src.p[poly] + (size_t)limb * N + (size_t)row * N2;
+  u64* out = dst.p[poly] + (size_t)limb * N + (size_t)row * N2;
+  u64* buf = bufs + (warp * G::SUBS + sub) * G::STRIDE;
+  u64 v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = in[core::first_idx<M2>(l, k)];
+  core::fwd_sub<M2, LAZY>(v, buf, l, tw, (u64)(N1 + row), pc.q);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) out[core::last_idx<M2>(l, k)] = reduce_out<LAZY>(v[k], pc);
+}
+
+template <int M1, int M2>
+__global__ __launch_bounds__(256) void k_inv_rows_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
+  using G = core::Geo<M2>;
+  constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = 8 * G::SUBS;
+  __shared__ u64 bufs[8 * G::SUBS * G::STRIDE];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / G::LANES, l = lane % G::LANES;
+  const int row = blockIdx.x * ROWS + warp * G::SUBS + sub;
+  const int limb = blockIdx.y, poly = blockIdx.z;
+  const int prime = map.prime(limb);
+  const u64 q = a.pc[prime].q;
+  const Twiddle* tw = a.tw_inv + (size_t)prime * N;
+  const u64* in = src.p[poly] + (size_t)limb * N + (size_t)row * N2;
+  u64* out = dst.p[poly] + (size_t)limb * N + (size_t)row * N2;
+  u64* buf = bufs + (warp * G::SUBS + sub) * G::STRIDE;
+  u64 v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = in[core::last_idx<M2>(l, k)];
+  core::inv_sub<M2>(v, buf, l, tw, (u64)(N1 + row), q);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) out[core::first_idx<M2>(l, k)] = v[k];
+}
+
+template <int M1, int M2>
+__global__ __launch_bounds__(256, 2) void k_inv_cols_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
+  using G = core::Geo<M1>;
+  constexpr int COLS = ColTile<M1>::COLS, N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2;
+  __shared__ u64 tile[COLS * G::STRIDE];
+  const int c0 = blockIdx.x * COLS;
+  const int limb = blockIdx.y, poly = blockIdx.z;
+  const int prime = map.prime(limb);
+  const PrimeConst& pc = a.pc[prime];
+  const Twiddle* tw = a.tw_inv + (size_t)prime * N;
+  const u64* in = src.p[poly] + (size_t)limb * N;
+  u64* out = dst.p[poly] + (size_t)limb * N;
+  for (int idx = threadIdx.x; idx < N1 * COLS; idx += 256) {
+    const int r = idx / COLS, c = idx % COLS;
+    tile[c * G::STRIDE + core::swz<M1>(r)] = in[(size_t)r * N2 + c0 + c];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / G::LANES, l = lane % G::LANES;
+#pragma unroll 1
+  for (int cb = warp * G::SUBS; cb < COLS; cb += 8 * G::SUBS) {
+    const int lv = core::lane_id_volatile();
+    const int sub = lv / G::LANES, l = lv % G::LANES;
+    u64* buf = tile + (cb + sub) * G::STRIDE;
+    u64 v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::last_idx<M1>(l, k))];
+    __syncwarp();
+    core::inv_sub<M1>(v, buf, l, tw, 1, pc.q);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::first_idx<M1>(l, k))] = v[k];
+  }
+  __syncthreads();
+  for (int idx = threadIdx.x; idx < N1 * COLS; idx += 256) {
+    const int r = idx / COLS, c = idx % COLS;
+    out[(size_t)r * N2 + c0 + c] = mul_shoup(tile[c * G::STRIDE + core::swz<M1>(r)], pc.n_inv, pc.n_inv_s, pc.q);
+  }
+}
+
+template <int M1, int M2, bool LAZY>
+void fwd_fast(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
+              cudaStream_t s) {
+  constexpr int N2 = 1 << M2, N1 = 1 << M1;
+  dim3 g1(N2 / ColTile<M1>::COLS, limbs, polys), g2(N1 / (8 * core::Geo<M2>::SUBS), limbs, polys);
+  {
+    ProfScope p("ntt_fwd_cols", s);
+    k_fwd_cols_f<M1, M2, LAZY><<<g1, 256, 0, s>>>(a, src, dst, map);
+  }
+  {
+    ProfScope p("ntt_fwd_rows", s);
+    k_fwd_rows_f<M1, M2, LAZY><<<g2, 256, 0, s>>>(a, dst, dst, map);
+  }
+}
+
+template <int M1, int M2>
+void inv_fast(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
+              cudaStream_t s) {
+  constexpr int N2 = 1 << M2, N1 = 1 << M1;
+  dim3 g1(N2 / ColTile<M1>::COLS, limbs, polys), g2(N1 / (8 * core::Geo<M2>::SUBS), limbs, polys);
+  {
+    ProfScope p("ntt_inv_rows", s);
+    k_inv_rows_f<M1, M2><<<g2, 256, 0, s>>>(a, src, dst, map);
+  }
+  {
+    ProfScope p("ntt_inv_cols", s);
+    k_inv_cols_f<M1, M2><<<g1, 256, 0, s>>>(a, dst, dst, map);
+  }
+}
+
+template <bool LAZY>
+bool fwd_dispatch(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
+                  cudaStream_t s) {
+  switch (a.log_n) {
+    case 12: fwd_fast<6, 6, LAZY>(a, src, dst, polys, limbs, map, s); return true;
+    case 13: fwd_fast<6, 7, LAZY>(a, src, dst, polys, limbs, map, s); return true;
+    case 14: fwd_fast<7, 7, LAZY>(a, src, dst, polys, limbs, map, s); return true;
+    case 15: fwd_fast<7, 8, LAZY>(a, src, dst, polys, limbs, map, s); return true;
+    case 16: fwd_fast<8, 8, LAZY>(a, src, dst, polys, limbs, map, s); return true;
+    default: return false;
+  }
+}
+
+bool inv_dispatch(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
+                  cudaStream_t s) {
+  switch (a.log_n) {
+    case 12: inv_fast<6, 6>(a, src, dst, polys, limbs, map, s); return true;
+    case 13: inv_fast<6, 7>(a, src, dst, polys, limbs, map, s); return true;
+    case 14: inv_fast<7, 7>(a, src, dst, polys, limbs, map, s); return true;
+    case 15: inv_fast<7, 8>(a, src, dst, polys, limbs, map, s); return true;
+    case 16: inv_fast<8, 8>(a, src, dst, polys, limbs, map, s); return true;
+    default: return false;
+  }
+}
+
 inline int threads_for(int work) {
   int t = 32;
   while (t < 256 && t < work) t <<= 1;
@@ -188,6 +386,9 @@ inline int threads_for(int work) {
 void ntt_forward(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
                  cudaStream_t s) {
   if (polys <= 0 || limbs <= 0) return;
+  if (a.lazy ? fwd_dispatch<true>(a, src, dst, polys, limbs, map, s)
+             : fwd_dispatch<false>(a, src, dst, polys, limbs, map, s))
+    return;
   const int N = 1 << a.log_n, N1 = 1 << a.n1, N2 = N >> a.n1;
   const int COLS = cols_per_cta(N2), ROWS = rows_per_cta(N1, N2);
   dim3 g1(N2 / COLS, limbs, polys), g2(N1 / ROWS, limbs, polys);
@@ -204,6 +405,7 @@ void ntt_forward(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int pol
 void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
                  cudaStream_t s) {
   if (polys <= 0 || limbs <= 0) return;
+  if (inv_dispatch(a, src, dst, polys, limbs, map, s)) return;
   const int N = 1 << a.log_n, N1 = 1 << a.n1, N2 = N >> a.n1;
   const int COLS = cols_per_cta(N2), ROWS = rows_per_cta(N1, N2);
   dim3 g1(N2 / COLS, limbs, polys), g2(N1 / ROWS, limbs, polys);

@@ -1,0 +1,209 @@
+// Warp-level register-blocked sub-NTTs of size 2^M (M = 6, 7, 8), eight
+// residues per lane.
+//
+// A 2^M-point column or row transform is done by 2^(M-3) lanes; a warp holds
+// 32 / 2^(M-3) of them side by side.  The M butterfly stages are split into
+// groups of up to three stages whose butterflies pair elements held by the
+// same lane; between groups the lane's eight values go through a warp-private
+// shared-memory buffer (XOR-swizzled so that every access pattern below is
+// free of bank conflicts for M = 7, 8) and come back in the next group's
+// assignment.  All index arithmetic is resolved at compile time except the
+// lane number.
+//
+// Twiddle index of sub-stage s for the lower element r of a pair:
+//   (TB << s) + (r >> (M - s)),   TB = 1 for the column phase, 2^n1 + row for
+// the row phase; this is the merged-twiddle Cooley-Tukey / Gentleman-Sande
+// index of the full N-point transform restricted to one column or row.
+#pragma once
+#include "modarith.cuh"
+
+namespace rc {
+namespace core {
+
+// Twiddle (w, w') pair through the read-only path.  The load is volatile so the
+// compiler keeps it at its use: hoisting the ~20 loop-invariant twiddles of a
+// sub-transform out of the per-digit loop would pin ~80 registers per thread.
+__device__ __forceinline__ Twiddle ldtw(const Twiddle* p) {
+  Twiddle t;
+  asm volatile("ld.global.nc.v2.u64 {%0, %1}, [%2];" : "=l"(t.w), "=l"(t.ws) : "l"(p));
+  return t;
+}
+
+// Lane id re-read with a volatile move: used inside long loops so that the
+// lane-dependent shared-memory addresses are recomputed per iteration instead
+// of being hoisted (and pinned in registers) across the loop.
+__device__ __forceinline__ int lane_id_volatile() {
+  int l;
+  asm volatile("mov.u32 %0, %%laneid;" : "=r"(l));
+  return l;
+}
+
+template <int M>
+struct Geo {
+  static constexpr int LB = M - 3;  // lane bits per sub-transform
+  static constexpr int LANES = 1 << LB;
+  static constexpr int SIZE = 1 << M;
+  static constexpr int SUBS = 32 / LANES;  // sub-transforms per warp
+  static constexpr int STRIDE = SIZE + 1;  // odd stride between sub-transform buffers
+};
+
+// stage groups: {S0, G}
+template <int M, int GI>
+struct Grp;
+template <int M>
+struct Grp<M, 0> {
+  static constexpr int S0 = 0, G = 3;
+};
+template <int M>
+struct Grp<M, 1> {
+  static constexpr int S0 = 3, G = 3;
+};
+template <>
+struct Grp<8, 2> {
+  static constexpr int S0 = 6, G = 2;
+};
+template <>
+struct Grp<7, 2> {
+  static constexpr int S0 = 6, G = 1;
+};
+template <int M>
+struct NGroups {
+  static constexpr int value = M == 6 ? 2 : 3;
+};
+
+// index of element k of lane l in group (S0, G): the G butterfly bits come from
+// k's low bits, the lane bits fill the lowest remaining positions, the rest of
+// k fills the highest remaining positions.
+template <int M, int S0, int G>
+__device__ __forceinline__ int gidx(int l, int k) {
+  constexpr int LB = M - 3;
+  constexpr int BLO = M - S0 - G;  // lowest butterfly bit position
+  int r = ((k & ((1 << G) - 1)) << BLO);
+  int li = 0, xi = 0;
+#pragma unroll
+  for (int p = 0; p < M; ++p) {
+    if (p >= BLO && p < BLO + G) continue;
+    if (li < LB) {
+      r |= ((l >> li) & 1) << p;
+      ++li;
+    } else {
+      r |= ((k >> (G + xi)) & 1) << p;
+      ++xi;
+    }
+  }
+  return r;
+}
+
+// conflict-free XOR swizzle (found by exhaustive search over GF(2)-linear maps)
+template <int M>
+__device__ __forceinline__ int swz(int r) {
+  const int v = r >> 4;
+  int h;
+  if (M == 8) h = ((v & 1) ? 1 : 0) ^ ((v & 2) ? 6 : 0) ^ ((v & 4) ? 8 : 0);
+  else if (M == 7) h = ((v & 1) ? 3 : 0) ^ ((v & 2) ? 4 : 0) ^ ((v & 4) ? 8 : 0);
+  else h = (v & 2) ? 2 : 0;
+  return r ^ h;
+}
+
+// Cooley-Tukey butterflies of one group.  LAZY: inputs are not reduced (values
+// grow by < 2q per stage; valid while they stay below 2^64), otherwise Harvey's
+// [0, 4q) invariant.
+template <int M, int GI, bool LAZY>
+__device__ __forceinline__ void fwd_group(u64 (&v)[8], int l, const Twiddle* __restrict__ tw, u64 tb, u64 q) {
+  constexpr int S0 = Grp<M, GI>::S0, G = Grp<M, GI>::G;
+  const u64 two_q = q << 1;
+#pragma unroll
+  for (int j = 0; j < G; ++j) {
+    const int s = S0 + j;
+    const int b = G - 1 - j;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k & (1 << b)) continue;
+      const int r = gidx<M, S0, G>(l, k);
+      const Twiddle w = ldtw(tw + ((tb << s) + (u64)(r >> (M - s))));
+      u64 x = v[k];
+      if (!LAZY) x = x >= two_q ? x - two_q : x;
+      const u64 t = mul_shoup_lazy(v[k | (1 << b)], w.w, w.ws, q);
+      v[k] = x + t;
+      v[k | (1 << b)] = x - t + two_q;
+    }
+  }
+}
+
+// Gentleman-Sande butterflies of one group, stages in decreasing order; values
+// stay in [0, 2q).
+template <int M, int GI>
+__device__ __forceinline__ void inv_group(u64 (&v)[8], int l, const Twiddle* __restrict__ tw, u64 tb, u64 q) {
+  constexpr int S0 = Grp<M, GI>::S0, G = Grp<M, GI>::G;
+  const u64 two_q = q << 1;
+#pragma unroll
+  for (int j = G - 1; j >= 0; --j) {
+    const int s = S0 + j;
+    const int b = G - 1 - j;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k & (1 << b)) continue;
+      const int r = gidx<M, S0, G>(l, k);
+      const Twiddle w = ldtw(tw + ((tb << s) + (u64)(r >> (M - s))));
+      const u64 x = v[k], y = v[k | (1 << b)];
+      u64 u = x + y;
+      u = u >= two_q ? u - two_q : u;
+      v[k] = u;
+      v[k | (1 << b)] = mul_shoup_lazy(x - y + two_q, w.w, w.ws, q);
+    }
+  }
+}
+
+// write the lane's values in group A's layout, read them back in group B's
+template <int M, int GA, int GB>
+__device__ __forceinline__ void exchange(u64 (&v)[8], u64* buf, int l) {
+#pragma unroll
+  for (int k = 0; k < 8; ++k) buf[swz<M>(gidx<M, Grp<M, GA>::S0, Grp<M, GA>::G>(l, k))] = v[k];
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = buf[swz<M>(gidx<M, Grp<M, GB>::S0, Grp<M, GB>::G>(l, k))];
+  __syncwarp();
+}
+
+// full forward sub-transform: v holds group 0's layout on entry, the last
+// group's layout on exit
+template <int M, bool LAZY>
+__device__ __forceinline__ void fwd_sub(u64 (&v)[8], u64* buf, int l, const Twiddle* tw, u64 tb, u64 q) {
+  fwd_group<M, 0, LAZY>(v, l, tw, tb, q);
+  exchange<M, 0, 1>(v, buf, l);
+  fwd_group<M, 1, LAZY>(v, l, tw, tb, q);
+  if constexpr (NGroups<M>::value == 3) {
+    exchange<M, 1, 2>(v, buf, l);
+    fwd_group<M, 2, LAZY>(v, l, tw, tb, q);
+  }
+}
+
+// full inverse sub-transform: v holds the last group's layout on entry, group 0's on exit
+template <int M>
+__device__ __forceinline__ void inv_sub(u64 (&v)[8], u64* buf, int l, const Twiddle* tw, u64 tb, u64 q) {
+  if constexpr (NGroups<M>::value == 3) {
+    inv_group<M, 2>(v, l, tw, tb, q);
+    exchange<M, 2, 1>(v, buf, l);
+  }
+  inv_group<M, 1>(v, l, tw, tb, q);
+  exchange<M, 1, 0>(v, buf, l);
+  inv_group<M, 0>(v, l, tw, tb, q);
+}
+
+template <int M>
+struct Last {
+  static constexpr int GI = NGroups<M>::value - 1;
+  static constexpr int S0 = Grp<M, GI>::S0, G = Grp<M, GI>::G;
+};
+
+template <int M>
+__device__ __forceinline__ int first_idx(int l, int k) {
+  return gidx<M, 0, 3>(l, k);
+}
+template <int M>
+__device__ __forceinline__ int last_idx(int l, int k) {
+  return gidx<M, Last<M>::S0, Last<M>::G>(l, k);
+}
+
+}  // namespace core
+}  // namespace rc
