@@ -353,10 +353,11 @@ struct DigitColTile {
 
 template <int M1, int M2, bool LAZY>
 __global__ __launch_bounds__(256, 2) void k_digit_cols_f(KsArgs a, DecompTab dt, const int32_t* digits, u64* scratch,
-                                                      int p0, int pc_count) {
+                                                         int p0, int pc_count) {
   using G = core::Geo<M1>;
   constexpr int COLS = DigitColTile<M1>::COLS, N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2;
   __shared__ u64 tile[COLS * G::STRIDE];
+  __shared__ Twiddle twl[N1];
   const int c0 = blockIdx.x * COLS;
   const int digit = blockIdx.y / pc_count, pl = blockIdx.y % pc_count;
   const int total = a.qlimbs + a.K;
@@ -366,17 +367,18 @@ __global__ __launch_bounds__(256, 2) void k_digit_cols_f(KsArgs a, DecompTab dt,
   const int prime = map.prime(limb);
   const u64 q = a.pc[prime].q;
   const bool aux = limb >= a.qlimbs;
-  const Twiddle* tw = a.ntt.tw_fwd + (size_t)prime * N;
+  core::stage_twiddles<M1>(twl, a.ntt.tw_fwd + (size_t)prime * N, 1, threadIdx.x, 256);
   const int32_t* in = digits + ((size_t)job * a.D + digit) * N;
   u64* out = scratch + ((size_t)pl * a.D + digit) * N;
-  for (int idx = threadIdx.x; idx < N1 * COLS; idx += 256) {
+#pragma unroll 4
+  for (int it = 0; it < N1 * COLS / 256; ++it) {
+    const int idx = it * 256 + threadIdx.x;
     const int r = idx / COLS, c = idx % COLS;
     const int32_t d = in[(size_t)r * N2 + c0 + c];
     tile[c * G::STRIDE + core::swz<M1>(r)] = aux ? lifted_residue(d, q, dt) : digit_residue(d, q);
   }
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int sub = lane / G::LANES, l = lane % G::LANES;
+  const int warp = threadIdx.x >> 5;
 #pragma unroll 1
   for (int cb = warp * G::SUBS; cb < COLS; cb += 8 * G::SUBS) {
     const int lv = core::lane_id_volatile();
@@ -386,12 +388,14 @@ __global__ __launch_bounds__(256, 2) void k_digit_cols_f(KsArgs a, DecompTab dt,
 #pragma unroll
     for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::first_idx<M1>(l, k))];
     __syncwarp();
-    core::fwd_sub<M1, LAZY>(v, buf, l, tw, 1, q);
+    core::fwd_sub<M1, LAZY>(v, buf, l, twl, q);
 #pragma unroll
     for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::last_idx<M1>(l, k))] = v[k];
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < N1 * COLS; idx += 256) {
+#pragma unroll 4
+  for (int it = 0; it < N1 * COLS / 256; ++it) {
+    const int idx = it * 256 + threadIdx.x;
     const int r = idx / COLS, c = idx % COLS;
     out[(size_t)r * N2 + c0 + c] = tile[c * G::STRIDE + core::swz<M1>(r)];
   }
@@ -399,15 +403,22 @@ __global__ __launch_bounds__(256, 2) void k_digit_cols_f(KsArgs a, DecompTab dt,
 
 constexpr int MAC_WARPS = 4;
 
-template <int M1, int M2, bool LAZY>
-__global__ __launch_bounds__(32 * MAC_WARPS, 3) void k_digit_rows_mac_f(KsArgs a, const u64* scratch, KeyTab keys,
-                                                                      u64* acc, int p0) {
+// Row pass of every digit transform of one (job, limb) and the key product.
+// The rows' twiddle tables are staged once and reused for all digits; the next
+// digit's row is prefetched while the current one is transformed.  ACC64:
+// 64-bit accumulators with per-term Montgomery reduction (each term < 2q)
+// instead of 128-bit lazy sums.
+template <int M1, int M2, bool LAZY, bool ACC64>
+__global__ __launch_bounds__(32 * MAC_WARPS, ACC64 ? 4 : 3) void k_digit_rows_mac_f(KsArgs a, const u64* scratch,
+                                                                                     KeyTab keys, u64* acc, int p0) {
   using G = core::Geo<M2>;
   constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = MAC_WARPS * G::SUBS;
-  __shared__ u64 bufs[MAC_WARPS * G::SUBS * G::STRIDE];
+  __shared__ u64 bufs[ROWS * G::STRIDE];
+  __shared__ Twiddle twl[ROWS][N2];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int sub = lane / G::LANES, l = lane % G::LANES;
-  const int row = blockIdx.x * ROWS + warp * G::SUBS + sub;
+  const int sub = lane / G::LANES;
+  const int row0 = blockIdx.x * ROWS;
+  const int rl = warp * G::SUBS + sub, row = row0 + rl;
   const int pl = blockIdx.y;
   const int total = a.qlimbs + a.K;
   const int pair = p0 + pl;
@@ -415,24 +426,44 @@ __global__ __launch_bounds__(32 * MAC_WARPS, 3) void k_digit_rows_mac_f(KsArgs a
   const LimbMap map{a.qlimbs, a.L};
   const int prime = map.prime(limb);
   const PrimeConst& pc = a.pc[prime];
-  const u64 q = pc.q;
-  const Twiddle* tw = a.ntt.tw_fwd + (size_t)prime * N;
+  const u64 q = pc.q, qn = pc.qinv_neg;
+  const Twiddle* twg = a.ntt.tw_fwd + (size_t)prime * N;
+#pragma unroll 1
+  for (int rr = 0; rr < ROWS; ++rr)
+    core::stage_twiddles<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * MAC_WARPS);
+  __syncthreads();
   const u64* key = keys.k[job] + (size_t)limb * a.key_digits * 2 * N + (size_t)row * N2;
-  u64* buf = bufs + (warp * G::SUBS + sub) * G::STRIDE;
+  u64* buf = bufs + rl * G::STRIDE;
+  const u64* rowin = scratch + (size_t)pl * a.D * N + (size_t)row * N2;
 
-  U128 acc0[8], acc1[8];
+  U128 acc0[8], acc1[8];  // ACC64 uses only .lo
 #pragma unroll
   for (int k = 0; k < 8; ++k) acc0[k].lo = acc0[k].hi = acc1[k].lo = acc1[k].hi = 0;
-  const u64 chunk = pc.mac_chunk;
+  const u64 chunk = ACC64 ? pc.mac_chunk64 : pc.mac_chunk;
   u64 since = 0;
+  auto term = [&](u64 x, u64 y) -> u64 {  // (x*y + m*q) / 2^64, m = -(x*y) q^-1 mod 2^64: < 2q
+    const u64 lo = x * y, hi = mulhi(x, y);
+    const u64 m = lo * qn;
+    return hi + mulhi(m, q) + (lo != 0 ? 1ull : 0ull);
+  };
+  u64 nxt[8];
+  {
+    const int l = lane % G::LANES;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) nxt[k] = rowin[core::first_idx<M2>(l, k)];
+  }
 #pragma unroll 1
   for (int digit = 0; digit < a.D; ++digit) {
     const int l = core::lane_id_volatile() % G::LANES;
-    const u64* in = scratch + ((size_t)pl * a.D + digit) * N + (size_t)row * N2;
     u64 v[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) v[k] = in[core::first_idx<M2>(l, k)];
-    core::fwd_sub<M2, LAZY>(v, buf, l, tw, (u64)(N1 + row), q);
+    for (int k = 0; k < 8; ++k) v[k] = nxt[k];
+    if (digit + 1 < a.D) {
+      const u64* in = rowin + (size_t)(digit + 1) * N;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) nxt[k] = in[core::first_idx<M2>(l, k)];
+    }
+    core::fwd_sub<M2, LAZY>(v, buf, l, twl[rl], q);
     const u64* k0 = key + (size_t)digit * 2 * N;
     const u64* k1 = k0 + N;
 #pragma unroll
@@ -440,10 +471,17 @@ __global__ __launch_bounds__(32 * MAC_WARPS, 3) void k_digit_rows_mac_f(KsArgs a
       const int pos = core::last_idx<M2>(l, k);  // pos, pos+1 hold elements k, k+1
       const ulonglong2 w0 = *reinterpret_cast<const ulonglong2*>(k0 + pos);
       const ulonglong2 w1 = *reinterpret_cast<const ulonglong2*>(k1 + pos);
-      add_to(acc0[k], mul_wide(v[k], w0.x));
-      add_to(acc0[k + 1], mul_wide(v[k + 1], w0.y));
-      add_to(acc1[k], mul_wide(v[k], w1.x));
-      add_to(acc1[k + 1], mul_wide(v[k + 1], w1.y));
+      if (ACC64) {
+        acc0[k].lo += term(v[k], w0.x);
+        acc0[k + 1].lo += term(v[k + 1], w0.y);
+        acc1[k].lo += term(v[k], w1.x);
+        acc1[k + 1].lo += term(v[k + 1], w1.y);
+      } else {
+        add_to(acc0[k], mul_wide(v[k], w0.x));
+        add_to(acc0[k + 1], mul_wide(v[k + 1], w0.y));
+        add_to(acc1[k], mul_wide(v[k], w1.x));
+        add_to(acc1[k + 1], mul_wide(v[k + 1], w1.y));
+      }
     }
     if (++since == chunk) {  // fold: keep the sums congruent mod q and small
 #pragma unroll
@@ -456,104 +494,24 @@ __global__ __launch_bounds__(32 * MAC_WARPS, 3) void k_digit_rows_mac_f(KsArgs a
       since = 1;
     }
   }
+  const int l = lane % G::LANES;
   u64* out0 = acc + ((size_t)job * 2 * total + limb) * N + (size_t)row * N2;
   u64* out1 = out0 + (size_t)total * N;
 #pragma unroll
   for (int k = 0; k < 8; k += 2) {
     const int pos = core::last_idx<M2>(l, k);
     ulonglong2 o0, o1;
-    o0.x = mont_reduce(acc0[k], pc);
-    o0.y = mont_reduce(acc0[k + 1], pc);
-    o1.x = mont_reduce(acc1[k], pc);
-    o1.y = mont_reduce(acc1[k + 1], pc);
-    *reinterpret_cast<ulonglong2*>(out0 + pos) = o0;
-    *reinterpret_cast<ulonglong2*>(out1 + pos) = o1;
-  }
-}
-
-// Same transform with 64-bit accumulators: each product is Montgomery-reduced
-// on the fly without the final subtraction (a term is < 2q), halving the
-// accumulator registers at the cost of one extra 64x64 high product per term.
-template <int M1, int M2, bool LAZY>
-__global__ __launch_bounds__(32 * MAC_WARPS, 4) void k_digit_rows_mac64_f(KsArgs a, const u64* scratch,
-                                                                          KeyTab keys, u64* acc, int p0) {
-  using G = core::Geo<M2>;
-  constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = MAC_WARPS * G::SUBS;
-  __shared__ u64 bufs[MAC_WARPS * G::SUBS * G::STRIDE];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int sub = lane / G::LANES, l = lane % G::LANES;
-  const int row = blockIdx.x * ROWS + warp * G::SUBS + sub;
-  const int pl = blockIdx.y;
-  const int total = a.qlimbs + a.K;
-  const int pair = p0 + pl;
-  const int job = pair / total, limb = pair % total;
-  const LimbMap map{a.qlimbs, a.L};
-  const int prime = map.prime(limb);
-  const PrimeConst& pc = a.pc[prime];
-  const u64 q = pc.q, qn = pc.qinv_neg;
-  const Twiddle* tw = a.ntt.tw_fwd + (size_t)prime * N;
-  const u64* key = keys.k[job] + (size_t)limb * a.key_digits * 2 * N + (size_t)row * N2;
-  u64* buf = bufs + (warp * G::SUBS + sub) * G::STRIDE;
-  u64 acc0[8], acc1[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) acc0[k] = acc1[k] = 0;
-  const u64 chunk = pc.mac_chunk64;
-  u64 since = 0;
-  auto term = [&](u64 x, u64 y) -> u64 {  // (x*y + m*q) / 2^64 with m = -(x*y) q^-1 mod 2^64: < 2q
-    const u64 lo = x * y, hi = mulhi(x, y);
-    const u64 m = lo * qn;
-    return hi + mulhi(m, q) + (lo != 0 ? 1ull : 0ull);
-  };
-#pragma unroll 1
-  for (int digit = 0; digit < a.D; ++digit) {
-    const int l = core::lane_id_volatile() % G::LANES;
-    const u64* in = scratch + ((size_t)pl * a.D + digit) * N + (size_t)row * N2;
-    u64 v[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) v[k] = in[core::first_idx<M2>(l, k)];
-    core::fwd_sub<M2, LAZY>(v, buf, l, tw, (u64)(N1 + row), q);
-    const u64* k0 = key + (size_t)digit * 2 * N;
-    const u64* k1 = k0 + N;
-#pragma unroll
-    for (int k = 0; k < 8; k += 2) {
-      const int pos = core::last_idx<M2>(l, k);
-      const ulonglong2 w0 = *reinterpret_cast<const ulonglong2*>(k0 + pos);
-      const ulonglong2 w1 = *reinterpret_cast<const ulonglong2*>(k1 + pos);
-      acc0[k] += term(v[k], w0.x);
-      acc0[k + 1] += term(v[k + 1], w0.y);
-      acc1[k] += term(v[k], w1.x);
-      acc1[k + 1] += term(v[k + 1], w1.y);
+    if (ACC64) {
+      o0.x = barrett_reduce(acc0[k], pc);
+      o0.y = barrett_reduce(acc0[k + 1], pc);
+      o1.x = barrett_reduce(acc1[k], pc);
+      o1.y = barrett_reduce(acc1[k + 1], pc);
+    } else {
+      o0.x = mont_reduce(acc0[k], pc);
+      o0.y = mont_reduce(acc0[k + 1], pc);
+      o1.x = mont_reduce(acc1[k], pc);
+      o1.y = mont_reduce(acc1[k + 1], pc);
     }
-    if (++since == chunk) {
-#pragma unroll
-      for (int k = 0; k < 8; ++k) {
-        U128 t0, t1;
-        t0.lo = acc0[k];
-        t0.hi = 0;
-        t1.lo = acc1[k];
-        t1.hi = 0;
-        acc0[k] = barrett_reduce(t0, pc);
-        acc1[k] = barrett_reduce(t1, pc);
-      }
-      since = 1;
-    }
-  }
-  u64* out0 = acc + ((size_t)job * 2 * total + limb) * N + (size_t)row * N2;
-  u64* out1 = out0 + (size_t)total * N;
-#pragma unroll
-  for (int k = 0; k < 8; k += 2) {
-    const int pos = core::last_idx<M2>(l, k);
-    U128 t;
-    t.hi = 0;
-    ulonglong2 o0, o1;
-    t.lo = acc0[k];
-    o0.x = barrett_reduce(t, pc);
-    t.lo = acc0[k + 1];
-    o0.y = barrett_reduce(t, pc);
-    t.lo = acc1[k];
-    o1.x = barrett_reduce(t, pc);
-    t.lo = acc1[k + 1];
-    o1.y = barrett_reduce(t, pc);
     *reinterpret_cast<ulonglong2*>(out0 + pos) = o0;
     *reinterpret_cast<ulonglong2*>(out1 + pos) = o1;
   }
@@ -570,8 +528,8 @@ void digit_fast(const KsArgs& a, const int32_t* digits, const KeyTab& kt, u64* a
   {
     ProfScope p("digit_rows_mac", s);
     dim3 g2((1 << M1) / (MAC_WARPS * core::Geo<M2>::SUBS), pcc);
-    if (a.mac64) k_digit_rows_mac64_f<M1, M2, LAZY><<<g2, 32 * MAC_WARPS, 0, s>>>(a, scratch, kt, acc, p0);
-    else k_digit_rows_mac_f<M1, M2, LAZY><<<g2, 32 * MAC_WARPS, 0, s>>>(a, scratch, kt, acc, p0);
+    if (a.mac64) k_digit_rows_mac_f<M1, M2, LAZY, true><<<g2, 32 * MAC_WARPS, 0, s>>>(a, scratch, kt, acc, p0);
+    else k_digit_rows_mac_f<M1, M2, LAZY, false><<<g2, 32 * MAC_WARPS, 0, s>>>(a, scratch, kt, acc, p0);
   }
 }
 

@@ -196,127 +196,100 @@ __device__ __forceinline__ u64 reduce_out(u64 x, const PrimeConst& c) {
   return reduce_4q(x, c.q);
 }
 
-template <int M1, int M2, bool LAZY>
-__global__ __launch_bounds__(256, 2) void k_fwd_cols_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
+// Column phase: the CTA stages a tile of COLS columns (2^M1 rows each) and the
+// column twiddle table in shared memory; each warp transforms SUBS columns at
+// a time in registers.
+template <int M1, int M2, bool LAZY, bool FWD>
+__global__ __launch_bounds__(256, 2) void k_cols_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
   using G = core::Geo<M1>;
   constexpr int COLS = ColTile<M1>::COLS, N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2;
   __shared__ u64 tile[COLS * G::STRIDE];
+  __shared__ Twiddle twl[N1];
   const int c0 = blockIdx.x * COLS;
   const int limb = blockIdx.y, poly = blockIdx.z;
   const int prime = map.prime(limb);
-  const u64 q = a.pc[prime].q;
-  const Twiddle* tw = a.tw_fwd + (size_t)prime * N;
+  const PrimeConst& pc = a.pc[prime];
+  const u64 q = pc.q;
+  core::stage_twiddles<M1>(twl, (FWD ? a.tw_fwd : a.tw_inv) + (size_t)prime * N, 1, threadIdx.x, 256);
   const u64* in = src.p[poly] + (size_t)limb * N;
   u64* out = dst.p[poly] + (size_t)limb * N;
-  for (int idx = threadIdx.x; idx < N1 * COLS; idx += 256) {
+#pragma unroll 4
+  for (int it = 0; it < N1 * COLS / 256; ++it) {
+    const int idx = it * 256 + threadIdx.x;
     const int r = idx / COLS, c = idx % COLS;
     tile[c * G::STRIDE + core::swz<M1>(r)] = in[(size_t)r * N2 + c0 + c];
   }
   __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int sub = lane / G::LANES, l = lane % G::LANES;
+  const int warp = threadIdx.x >> 5;
 #pragma unroll 1
   for (int cb = warp * G::SUBS; cb < COLS; cb += 8 * G::SUBS) {
     const int lv = core::lane_id_volatile();
     const int sub = lv / G::LANES, l = lv % G::LANES;
     u64* buf = tile + (cb + sub) * G::STRIDE;
     u64 v[8];
+    if (FWD) {
 #pragma unroll
-    for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::first_idx<M1>(l, k))];
-    __syncwarp();
-    core::fwd_sub<M1, LAZY>(v, buf, l, tw, 1, q);
+      for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::first_idx<M1>(l, k))];
+      __syncwarp();
+      core::fwd_sub<M1, LAZY>(v, buf, l, twl, q);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::last_idx<M1>(l, k))] = v[k];
+      for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::last_idx<M1>(l, k))] = v[k];
+    } else {
+#pragma unroll
+      for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::last_idx<M1>(l, k))];
+      __syncwarp();
+      core::inv_sub<M1>(v, buf, l, twl, q);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::first_idx<M1>(l, k))] = v[k];
+    }
   }
   __syncthreads();
-  for (int idx = threadIdx.x; idx < N1 * COLS; idx += 256) {
+#pragma unroll 4
+  for (int it = 0; it < N1 * COLS / 256; ++it) {
+    const int idx = it * 256 + threadIdx.x;
     const int r = idx / COLS, c = idx % COLS;
-    out[(size_t)r * N2 + c0 + c] = tile[c * G::STRIDE + core::swz<M1>(r)];
+    const u64 x = tile[c * G::STRIDE + core::swz<M1>(r)];
+    out[(size_t)r * N2 + c0 + c] = FWD ? x : mul_shoup(x, pc.n_inv, pc.n_inv_s, q);
   }
 }
 
-template <int M1, int M2, bool LAZY>
-__global__ __launch_bounds__(256) void k_fwd_rows_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
+constexpr int ROW_WARPS = 4;
+
+// Row phase: each warp transforms SUBS rows of 2^M2 contiguous residues; the
+// CTA stages the rows' twiddle tables in shared memory.
+template <int M1, int M2, bool LAZY, bool FWD>
+__global__ __launch_bounds__(32 * ROW_WARPS) void k_rows_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
   using G = core::Geo<M2>;
-  constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = 8 * G::SUBS;
-  __shared__ u64 bufs[8 * G::SUBS * G::STRIDE];
+  constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = ROW_WARPS * G::SUBS;
+  __shared__ u64 bufs[ROWS * G::STRIDE];
+  __shared__ Twiddle twl[ROWS][N2];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sub = lane / G::LANES, l = lane % G::LANES;
-  const int row = blockIdx.x * ROWS + warp * G::SUBS + sub;
+  const int row0 = blockIdx.x * ROWS;
   const int limb = blockIdx.y, poly = blockIdx.z;
   const int prime = map.prime(limb);
   const PrimeConst& pc = a.pc[prime];
-  const Twiddle* tw = a.tw_fwd + (size_t)prime * N;
-  const u64* in = src.p[poly] + (size_t)limb * N + (size_t)row * N2;
-  u64* out = dst.p[poly] + (size_t)limb * N + (size_t)row * N2;
-  u64* buf = bufs + (warp * G::SUBS + sub) * G::STRIDE;
-  u64 v[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) v[k] = in[core::first_idx<M2>(l, k)];
-  core::fwd_sub<M2, LAZY>(v, buf, l, tw, (u64)(N1 + row), pc.q);
-#pragma unroll
-  for (int k = 0; k < 8; ++k) out[core::last_idx<M2>(l, k)] = reduce_out<LAZY>(v[k], pc);
-}
-
-template <int M1, int M2>
-__global__ __launch_bounds__(256) void k_inv_rows_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
-  using G = core::Geo<M2>;
-  constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = 8 * G::SUBS;
-  __shared__ u64 bufs[8 * G::SUBS * G::STRIDE];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int sub = lane / G::LANES, l = lane % G::LANES;
-  const int row = blockIdx.x * ROWS + warp * G::SUBS + sub;
-  const int limb = blockIdx.y, poly = blockIdx.z;
-  const int prime = map.prime(limb);
-  const u64 q = a.pc[prime].q;
-  const Twiddle* tw = a.tw_inv + (size_t)prime * N;
-  const u64* in = src.p[poly] + (size_t)limb * N + (size_t)row * N2;
-  u64* out = dst.p[poly] + (size_t)limb * N + (size_t)row * N2;
-  u64* buf = bufs + (warp * G::SUBS + sub) * G::STRIDE;
-  u64 v[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) v[k] = in[core::last_idx<M2>(l, k)];
-  core::inv_sub<M2>(v, buf, l, tw, (u64)(N1 + row), q);
-#pragma unroll
-  for (int k = 0; k < 8; ++k) out[core::first_idx<M2>(l, k)] = v[k];
-}
-
-template <int M1, int M2>
-__global__ __launch_bounds__(256, 2) void k_inv_cols_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
-  using G = core::Geo<M1>;
-  constexpr int COLS = ColTile<M1>::COLS, N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2;
-  __shared__ u64 tile[COLS * G::STRIDE];
-  const int c0 = blockIdx.x * COLS;
-  const int limb = blockIdx.y, poly = blockIdx.z;
-  const int prime = map.prime(limb);
-  const PrimeConst& pc = a.pc[prime];
-  const Twiddle* tw = a.tw_inv + (size_t)prime * N;
-  const u64* in = src.p[poly] + (size_t)limb * N;
-  u64* out = dst.p[poly] + (size_t)limb * N;
-  for (int idx = threadIdx.x; idx < N1 * COLS; idx += 256) {
-    const int r = idx / COLS, c = idx % COLS;
-    tile[c * G::STRIDE + core::swz<M1>(r)] = in[(size_t)r * N2 + c0 + c];
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int sub = lane / G::LANES, l = lane % G::LANES;
+  const Twiddle* twg = (FWD ? a.tw_fwd : a.tw_inv) + (size_t)prime * N;
 #pragma unroll 1
-  for (int cb = warp * G::SUBS; cb < COLS; cb += 8 * G::SUBS) {
-    const int lv = core::lane_id_volatile();
-    const int sub = lv / G::LANES, l = lv % G::LANES;
-    u64* buf = tile + (cb + sub) * G::STRIDE;
-    u64 v[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::last_idx<M1>(l, k))];
-    __syncwarp();
-    core::inv_sub<M1>(v, buf, l, tw, 1, pc.q);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::first_idx<M1>(l, k))] = v[k];
-  }
+  for (int rr = 0; rr < ROWS; ++rr) core::stage_twiddles<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * ROW_WARPS);
   __syncthreads();
-  for (int idx = threadIdx.x; idx < N1 * COLS; idx += 256) {
-    const int r = idx / COLS, c = idx % COLS;
-    out[(size_t)r * N2 + c0 + c] = mul_shoup(tile[c * G::STRIDE + core::swz<M1>(r)], pc.n_inv, pc.n_inv_s, pc.q);
+  const int rl = warp * G::SUBS + sub, row = row0 + rl;
+  const u64* in = src.p[poly] + (size_t)limb * N + (size_t)row * N2;
+  u64* out = dst.p[poly] + (size_t)limb * N + (size_t)row * N2;
+  u64* buf = bufs + rl * G::STRIDE;
+  u64 v[8];
+  if (FWD) {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = in[core::first_idx<M2>(l, k)];
+    core::fwd_sub<M2, LAZY>(v, buf, l, twl[rl], pc.q);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) out[core::last_idx<M2>(l, k)] = reduce_out<LAZY>(v[k], pc);
+  } else {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = in[core::last_idx<M2>(l, k)];
+    core::inv_sub<M2>(v, buf, l, twl[rl], pc.q);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) out[core::first_idx<M2>(l, k)] = v[k];
   }
 }
 
@@ -324,14 +297,14 @@ template <int M1, int M2, bool LAZY>
 void fwd_fast(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
               cudaStream_t s) {
   constexpr int N2 = 1 << M2, N1 = 1 << M1;
-  dim3 g1(N2 / ColTile<M1>::COLS, limbs, polys), g2(N1 / (8 * core::Geo<M2>::SUBS), limbs, polys);
+  dim3 g1(N2 / ColTile<M1>::COLS, limbs, polys), g2(N1 / (ROW_WARPS * core::Geo<M2>::SUBS), limbs, polys);
   {
     ProfScope p("ntt_fwd_cols", s);
-    k_fwd_cols_f<M1, M2, LAZY><<<g1, 256, 0, s>>>(a, src, dst, map);
+    k_cols_f<M1, M2, LAZY, true><<<g1, 256, 0, s>>>(a, src, dst, map);
   }
   {
     ProfScope p("ntt_fwd_rows", s);
-    k_fwd_rows_f<M1, M2, LAZY><<<g2, 256, 0, s>>>(a, dst, dst, map);
+    k_rows_f<M1, M2, LAZY, true><<<g2, 32 * ROW_WARPS, 0, s>>>(a, dst, dst, map);
   }
 }
 
@@ -339,14 +312,14 @@ template <int M1, int M2>
 void inv_fast(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
               cudaStream_t s) {
   constexpr int N2 = 1 << M2, N1 = 1 << M1;
-  dim3 g1(N2 / ColTile<M1>::COLS, limbs, polys), g2(N1 / (8 * core::Geo<M2>::SUBS), limbs, polys);
+  dim3 g1(N2 / ColTile<M1>::COLS, limbs, polys), g2(N1 / (ROW_WARPS * core::Geo<M2>::SUBS), limbs, polys);
   {
     ProfScope p("ntt_inv_rows", s);
-    k_inv_rows_f<M1, M2><<<g2, 256, 0, s>>>(a, src, dst, map);
+    k_rows_f<M1, M2, false, false><<<g2, 32 * ROW_WARPS, 0, s>>>(a, src, dst, map);
   }
   {
     ProfScope p("ntt_inv_cols", s);
-    k_inv_cols_f<M1, M2><<<g1, 256, 0, s>>>(a, dst, dst, map);
+    k_cols_f<M1, M2, false, false><<<g1, 256, 0, s>>>(a, dst, dst, map);
   }
 }
 

@@ -14,6 +14,9 @@
 //   (TB << s) + (r >> (M - s)),   TB = 1 for the column phase, 2^n1 + row for
 // the row phase; this is the merged-twiddle Cooley-Tukey / Gentleman-Sande
 // index of the full N-point transform restricted to one column or row.
+// Kernels stage the 2^M - 1 twiddles a column or row needs into a local
+// shared-memory table t[(1 << s) + j] = global[(TB << s) + j] (stage_twiddles)
+// and the butterflies read t[(1 << s) + (r >> (M - s))].
 #pragma once
 #include "modarith.cuh"
 
@@ -27,6 +30,19 @@ __device__ __forceinline__ Twiddle ldtw(const Twiddle* p) {
   Twiddle t;
   asm volatile("ld.global.nc.v2.u64 {%0, %1}, [%2];" : "=l"(t.w), "=l"(t.ws) : "l"(p));
   return t;
+}
+
+// local[t] = global[(TB << s) + (t - 2^s)] for t in [1, 2^M), s = floor(log2 t),
+// copied cooperatively by `nthreads` threads starting at thread `tid`
+template <int M>
+__device__ __forceinline__ void stage_twiddles(Twiddle* local, const Twiddle* global, u64 tb, int tid,
+                                               int nthreads) {
+  for (int t = 1 + tid; t < (1 << M); t += nthreads) {
+    const int s = 31 - __clz(t);
+    const ulonglong2 v = __ldg(reinterpret_cast<const ulonglong2*>(global + ((tb - 1) << s) + t));
+    local[t].w = v.x;
+    local[t].ws = v.y;
+  }
 }
 
 // Lane id re-read with a volatile move: used inside long loops so that the
@@ -109,7 +125,7 @@ __device__ __forceinline__ int swz(int r) {
 // grow by < 2q per stage; valid while they stay below 2^64), otherwise Harvey's
 // [0, 4q) invariant.
 template <int M, int GI, bool LAZY>
-__device__ __forceinline__ void fwd_group(u64 (&v)[8], int l, const Twiddle* __restrict__ tw, u64 tb, u64 q) {
+__device__ __forceinline__ void fwd_group(u64 (&v)[8], int l, const Twiddle* __restrict__ tw, u64 q) {
   constexpr int S0 = Grp<M, GI>::S0, G = Grp<M, GI>::G;
   const u64 two_q = q << 1;
 #pragma unroll
@@ -120,7 +136,7 @@ __device__ __forceinline__ void fwd_group(u64 (&v)[8], int l, const Twiddle* __r
     for (int k = 0; k < 8; ++k) {
       if (k & (1 << b)) continue;
       const int r = gidx<M, S0, G>(l, k);
-      const Twiddle w = ldtw(tw + ((tb << s) + (u64)(r >> (M - s))));
+      const Twiddle w = tw[(1 << s) + (r >> (M - s))];
       u64 x = v[k];
       if (!LAZY) x = x >= two_q ? x - two_q : x;
       const u64 t = mul_shoup_lazy(v[k | (1 << b)], w.w, w.ws, q);
@@ -133,7 +149,7 @@ __device__ __forceinline__ void fwd_group(u64 (&v)[8], int l, const Twiddle* __r
 // Gentleman-Sande butterflies of one group, stages in decreasing order; values
 // stay in [0, 2q).
 template <int M, int GI>
-__device__ __forceinline__ void inv_group(u64 (&v)[8], int l, const Twiddle* __restrict__ tw, u64 tb, u64 q) {
+__device__ __forceinline__ void inv_group(u64 (&v)[8], int l, const Twiddle* __restrict__ tw, u64 q) {
   constexpr int S0 = Grp<M, GI>::S0, G = Grp<M, GI>::G;
   const u64 two_q = q << 1;
 #pragma unroll
@@ -144,7 +160,7 @@ __device__ __forceinline__ void inv_group(u64 (&v)[8], int l, const Twiddle* __r
     for (int k = 0; k < 8; ++k) {
       if (k & (1 << b)) continue;
       const int r = gidx<M, S0, G>(l, k);
-      const Twiddle w = ldtw(tw + ((tb << s) + (u64)(r >> (M - s))));
+      const Twiddle w = tw[(1 << s) + (r >> (M - s))];
       const u64 x = v[k], y = v[k | (1 << b)];
       u64 u = x + y;
       u = u >= two_q ? u - two_q : u;
@@ -168,26 +184,26 @@ __device__ __forceinline__ void exchange(u64 (&v)[8], u64* buf, int l) {
 // full forward sub-transform: v holds group 0's layout on entry, the last
 // group's layout on exit
 template <int M, bool LAZY>
-__device__ __forceinline__ void fwd_sub(u64 (&v)[8], u64* buf, int l, const Twiddle* tw, u64 tb, u64 q) {
-  fwd_group<M, 0, LAZY>(v, l, tw, tb, q);
+__device__ __forceinline__ void fwd_sub(u64 (&v)[8], u64* buf, int l, const Twiddle* tw, u64 q) {
+  fwd_group<M, 0, LAZY>(v, l, tw, q);
   exchange<M, 0, 1>(v, buf, l);
-  fwd_group<M, 1, LAZY>(v, l, tw, tb, q);
+  fwd_group<M, 1, LAZY>(v, l, tw, q);
   if constexpr (NGroups<M>::value == 3) {
     exchange<M, 1, 2>(v, buf, l);
-    fwd_group<M, 2, LAZY>(v, l, tw, tb, q);
+    fwd_group<M, 2, LAZY>(v, l, tw, q);
   }
 }
 
 // full inverse sub-transform: v holds the last group's layout on entry, group 0's on exit
 template <int M>
-__device__ __forceinline__ void inv_sub(u64 (&v)[8], u64* buf, int l, const Twiddle* tw, u64 tb, u64 q) {
+__device__ __forceinline__ void inv_sub(u64 (&v)[8], u64* buf, int l, const Twiddle* tw, u64 q) {
   if constexpr (NGroups<M>::value == 3) {
-    inv_group<M, 2>(v, l, tw, tb, q);
+    inv_group<M, 2>(v, l, tw, q);
     exchange<M, 2, 1>(v, buf, l);
   }
-  inv_group<M, 1>(v, l, tw, tb, q);
+  inv_group<M, 1>(v, l, tw, q);
   exchange<M, 1, 0>(v, buf, l);
-  inv_group<M, 0>(v, l, tw, tb, q);
+  inv_group<M, 0>(v, l, tw, q);
 }
 
 template <int M>
