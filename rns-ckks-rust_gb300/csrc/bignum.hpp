@@ -136,4 +136,32 @@ inline uint64_t invmod_h(uint64_t v, uint64_t m) {
 }
 inline uint64_t shoup_h(uint64_t w, uint64_t q) { return (uint64_t)(((u128h)w << 64) / q); }
 
+// deterministic Miller-Rabin for 64-bit integers
+inline bool is_prime_u64(uint64_t n) {
+  if (n < 2) return false;
+  static const uint64_t small[] = {2, 3, 5, 7, 11, 13, 17, 19, 23, 29, 31, 37};
+  for (uint64_t p : small)
+    if (n % p == 0) return n == p;
+  uint64_t d = n - 1;
+  int s = 0;
+  while ((d & 1) == 0) {
+    d >>= 1;
+    ++s;
+  }
+  for (uint64_t a : small) {
+    uint64_t x = powmod_h(a, d, n);
+    if (x == 1 || x == n - 1) continue;
+    bool comp = true;
+    for (int r = 1; r < s; ++r) {
+      x = mulmod_h(x, x, n);
+      if (x == n - 1) {
+        comp = false;
+        break;
+      }
+    }
+    if (comp) return false;
+  }
+  return true;
+}
+
 }  // namespace rc

@@ -184,8 +184,27 @@ size_t ks_scratch_elems(const rc_context* c, int J, int total, int D) {
 
 size_t ks_ws_bytes(const rc_context* c, int J, int qlimbs, int K, int D) {
   const int total = qlimbs + K;
-  return align_up((size_t)J * D * c->N * 4, 256) + arena_size_u64((size_t)J * 2 * total * c->N) +
-         arena_size_u64(ks_scratch_elems(c, J, total, D)) + 1024;
+  const size_t standard = align_up((size_t)J * D * c->N * 4, 256) + arena_size_u64((size_t)J * 2 * total * c->N) +
+                          arena_size_u64(ks_scratch_elems(c, J, total, D)) + 1024;
+  const size_t wide = align_up((size_t)J * D * c->N * 4, 256) + arena_size_u64((size_t)J * D * 2 * c->N) +
+                      arena_size_u64((size_t)J * 2 * total * 2 * c->N) + 1024;
+  return std::max(standard, c->wide_ok ? wide : 0);
+}
+
+// The exact integer key product applies when the internal primes' product A
+// exceeds twice the largest possible |sum_i d_i k_ij| = D * N * 2^29 * (q_max - 1).
+bool use_wide(const rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, int K, int D) {
+  if (!c->wide_ok || c->log_n < 12 || c->log_n > 16) return false;
+  if (level_info(c, qlimbs).dt.small_q) return false;  // lifted digits are not the digits themselves
+  for (auto& j : jobs)
+    if (!j.key->wdata) return false;
+  uint64_t qmax = 0;
+  for (int i = 0; i < qlimbs; ++i) qmax = std::max(qmax, c->mod[i]);
+  for (int k = 0; k < K; ++k) qmax = std::max(qmax, c->mod[c->L + k]);
+  const u128h bound = (u128h)D * (u128h)c->N * ((u128h)1 << 29) * (u128h)(qmax - 1);
+  const u128h A = ((u128h)c->wide.A_hi << 64) | c->wide.A_lo;
+  if (bound >= ((u128h)1 << 126)) return false;
+  return 2 * bound < A;
 }
 
 // Runs keyswitch for `jobs` jobs at `qlimbs` limbs (all keys of the same kind);
@@ -207,16 +226,68 @@ void keyswitch_core(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, u
     if (!K) require((int)j.key->digits == D, "internal: mixed digit counts in one keyswitch batch");
   }
   const int N = c->N, total = qlimbs + K;
+  const bool wide = use_wide(c, jobs, qlimbs, K, D);
   const size_t scratch_elems = ks_scratch_elems(c, J, total, D);
   Arena ar(ws);
   int32_t* digits = ar.take<int32_t>((size_t)J * D * N);
-  uint64_t* acc = ar.take<uint64_t>((size_t)J * 2 * total * N);
-  uint64_t* scratch = ar.take<uint64_t>(scratch_elems);
-
   PtrTab src{};
   for (int j = 0; j < J; ++j) src.p[j] = const_cast<uint64_t*>(jobs[j].poly);
   decompose(c->d_pc, li.dt, src, J, qlimbs, D, digits, g_inv, c->log_n, s);
   launch_check("decompose");
+
+  FinalizeArgs f;
+  f.pc = c->d_pc;
+  f.md = c->md;
+  f.rt = c->rt;
+  f.L = c->L;
+  f.n = N;
+  f.log_n = c->log_n;
+  f.qlimbs = qlimbs;
+  f.K = K;
+  f.rescale = rescale ? 1 : 0;
+  f.add_g_inv = g_inv;
+  f.wide = wide ? 1 : 0;
+  f.wt = c->wide;
+  PtrTab add{}, out{};
+  for (int j = 0; j < J; ++j) {
+    add.p[2 * j] = const_cast<uint64_t*>(jobs[j].add0);
+    add.p[2 * j + 1] = const_cast<uint64_t*>(jobs[j].add1);
+    out.p[2 * j] = jobs[j].out0;
+    out.p[2 * j + 1] = jobs[j].out1;
+  }
+
+  if (wide) {
+    const int base = c->L + c->K;
+    uint64_t* dt = ar.take<uint64_t>((size_t)J * D * 2 * N);
+    uint64_t* acc = ar.take<uint64_t>((size_t)J * 2 * total * 2 * N);
+    require(wide_digit_transforms(c->ntt(), base, D, J, digits, dt, s), "internal: wide transforms unsupported");
+    launch_check("wide digit transforms");
+    // jobs sharing a key run together so that each key word is read once per group
+    const uint64_t chunk = (~0ull) / c->mod[base] - 1;
+    int b = 0;
+    while (b < J) {
+      int e = b + 1;
+      while (e < J && jobs[e].key->wdata == jobs[b].key->wdata) ++e;
+      wide_mac(c->d_pc, base, c->log_n, D, (int)jobs[b].key->digits, total, jobs[b].key->wdata, dt, acc, b, e - b,
+               chunk, s);
+      launch_check("wide mac");
+      b = e;
+    }
+    const int polys = J * 2 * total;
+    for (int p0 = 0; p0 < polys; p0 += MAXP) {
+      PtrTab t{};
+      const int cnt = std::min(MAXP, polys - p0);
+      for (int k = 0; k < cnt; ++k) t.p[k] = acc + (size_t)(p0 + k) * 2 * N;
+      ntt_inverse(c->ntt(), t, t, cnt, 2, LimbMap{0, base}, s);
+    }
+    launch_check("ntt_inverse(wide acc)");
+    finalize(f, acc, add, out, J, s);
+    launch_check("finalize");
+    return;
+  }
+
+  uint64_t* acc = ar.take<uint64_t>((size_t)J * 2 * total * N);
+  uint64_t* scratch = ar.take<uint64_t>(scratch_elems);
 
   KsArgs ka;
   ka.pc = c->d_pc;
@@ -239,25 +310,6 @@ void keyswitch_core(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, u
   for (int p = 0; p < 2 * J; ++p) t.p[p] = acc + (size_t)p * total * N;
   ntt_inverse(c->ntt(), t, t, 2 * J, total, LimbMap{qlimbs, c->L}, s);
   launch_check("ntt_inverse(acc)");
-
-  FinalizeArgs f;
-  f.pc = c->d_pc;
-  f.md = c->md;
-  f.rt = c->rt;
-  f.L = c->L;
-  f.n = N;
-  f.log_n = c->log_n;
-  f.qlimbs = qlimbs;
-  f.K = K;
-  f.rescale = rescale ? 1 : 0;
-  f.add_g_inv = g_inv;
-  PtrTab add{}, out{};
-  for (int j = 0; j < J; ++j) {
-    add.p[2 * j] = const_cast<uint64_t*>(jobs[j].add0);
-    add.p[2 * j + 1] = const_cast<uint64_t*>(jobs[j].add1);
-    out.p[2 * j] = jobs[j].out0;
-    out.p[2 * j + 1] = jobs[j].out1;
-  }
   finalize(f, acc, add, out, J, s);
   launch_check("finalize");
 }
@@ -435,10 +487,39 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
     c->mod.insert(c->mod.end(), pm.begin(), pm.end());
     c->root = qg;
     c->root.insert(c->root.end(), pg.begin(), pg.end());
-    const int P = c->L + c->K;
-    // Lazy (unreduced) forward butterflies need every prime < 2^58; they are
-    // opt-in because the compiler schedules them with far more live registers.
-    c->lazy = false;
+    // Two internal "product" primes a0 > a1 just below 2^55 (a = k*2N + 1, not in
+    // Q u P) carry the exact integer key product of the wide-CRT keyswitch; they
+    // get twiddle tables like the scheme primes, at indices L+K and L+K+1.
+    {
+      const uint64_t step = 2 * N;
+      uint64_t kk = ((1ull << 55) - 1) / step;
+      std::vector<uint64_t> found;
+      while (found.size() < 2 && kk > 1) {
+        const uint64_t a = kk * step + 1;
+        bool clash = false;
+        for (uint64_t m : c->mod) clash = clash || m == a;
+        if (!clash && is_prime_u64(a)) found.push_back(a);
+        --kk;
+      }
+      if (found.size() == 2) {
+        c->wide_ok = true;
+        for (uint64_t a : found) {
+          // any primitive 2N-th root of unity serves (these primes never meet user data)
+          uint64_t psi = 0;
+          for (uint64_t x = 2; x < 1000 && !psi; ++x) {
+            const uint64_t cand = powmod_h(x, (a - 1) / (2 * N), a);
+            if (powmod_h(cand, N, a) == a - 1) psi = cand;
+          }
+          c->mod.push_back(a);
+          c->root.push_back(0);
+          c->wide_psi.push_back(psi);
+        }
+      }
+      if (const char* e = getenv("RNSCKKS_WIDE")) c->wide_ok = c->wide_ok && atoi(e) != 0;
+    }
+    const int P = (int)c->mod.size();
+    // Lazy (unreduced) forward butterflies need every prime < 2^58
+    c->lazy = true;
     if (const char* e = getenv("RNSCKKS_LAZY_NTT")) c->lazy = atoi(e) != 0;
     for (uint64_t q : c->mod) c->lazy = c->lazy && q < (1ull << 58);
     if (const char* e = getenv("RNSCKKS_MAC64")) c->mac64 = atoi(e) != 0;
@@ -469,7 +550,8 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
       k.mac_chunk = (uint64_t)((~0ull) / (out_bound * q));
       k.mac_chunk64 = (uint64_t)((~0ull) / (2 * q));
       // psi = g^((q-1)/2N) (NttPlan::new, ntt.rs:42)
-      const uint64_t psi = powmod_h(c->root[i] % q, (q - 1) / (2 * N), q);
+      const uint64_t psi = i < c->L + c->K ? powmod_h(c->root[i] % q, (q - 1) / (2 * N), q)
+                                           : c->wide_psi[i - c->L - c->K];
       const uint64_t psi_inv = invmod_h(psi, q);
       std::vector<uint64_t> pw(N), pwi(N);
       pw[0] = pwi[0] = 1;
@@ -601,6 +683,36 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
       c->rt.inv = d;
       c->rt.inv_s = d + (size_t)L * L;
     }
+    // ---- wide-CRT reconstruction table: S = r0 + a0 * ((r1 - r0) a0^-1 mod a1), centred mod A
+    if (c->wide_ok) {
+      const int QP = c->L + c->K;
+      const uint64_t a0 = c->mod[QP], a1 = c->mod[QP + 1];
+      const u128h A = (u128h)a0 * a1;
+      std::vector<uint64_t> blob((size_t)3 * QP);
+      for (int t = 0; t < QP; ++t) {
+        const uint64_t m = c->mod[t];
+        blob[t] = a0 % m;
+        blob[QP + t] = shoup_h(a0 % m, m);
+        blob[2 * QP + t] = (uint64_t)(A % m);
+      }
+      c->wide_buf.reset(new DevBuf(blob.size() * 8));
+      uint64_t* d = (uint64_t*)c->wide_buf->p;
+      cuda_check(cudaMemcpy(d, blob.data(), blob.size() * 8, cudaMemcpyHostToDevice), "upload wide tables");
+      WideTab& w = c->wide;
+      w.base = QP;
+      w.a0 = a0;
+      w.a1 = a1;
+      w.a0inv = invmod_h(a0 % a1, a1);
+      w.a0inv_s = shoup_h(w.a0inv, a1);
+      const u128h half = A >> 1;
+      w.halfA_lo = (uint64_t)half;
+      w.halfA_hi = (uint64_t)(half >> 64);
+      w.a0_mod_t = d;
+      w.a0_mod_t_s = d + QP;
+      w.A_mod_t = d + 2 * QP;
+      w.A_lo = (uint64_t)A;
+      w.A_hi = (uint64_t)(A >> 64);
+    }
     cuda_check(cudaDeviceSynchronize(), "context setup");
     *out = c.release();
   });
@@ -665,6 +777,26 @@ static int ksk_upload_impl(rc_context* c, const uint64_t* key, bool on_device, u
                "key upload");
     const LimbMap map{level + 1, c->L};
     uint64_t* t = (uint64_t*)tmp.p;
+    // wide form (exact integer key product): the same integers under the two
+    // internal primes, transformed and in Montgomery form
+    std::shared_ptr<DevBuf> wide;
+    if (c->wide_ok && c->log_n >= 12 && c->log_n <= 16) {
+      const int base = c->L + c->K;
+      wide.reset(new DevBuf(elems * 2 * 8));
+      uint64_t* w = (uint64_t*)wide->p;
+      wide_key_prep(c->d_pc, base, t, w, (int)digits, limbs, c->log_n, 0);
+      launch_check("wide key prep");
+      const int wpolys = limbs * (int)digits * 2;
+      for (int p0 = 0; p0 < wpolys; p0 += MAXP) {
+        PtrTab tab{};
+        const int cnt = std::min(MAXP, wpolys - p0);
+        for (int k = 0; k < cnt; ++k) tab.p[k] = w + (size_t)(p0 + k) * 2 * c->N;
+        ntt_forward(c->ntt(), tab, tab, cnt, 2, LimbMap{0, base}, 0);
+        launch_check("wide key ntt");
+      }
+      wide_to_mont(c->d_pc, base, w, elems * 2, c->log_n, 0);
+      launch_check("wide key montgomery");
+    }
     const int polys = (int)digits * 2;
     for (int p0 = 0; p0 < polys; p0 += MAXP) {
       PtrTab tab{};
@@ -680,6 +812,8 @@ static int ksk_upload_impl(rc_context* c, const uint64_t* key, bool on_device, u
     k->ctx = c;
     k->buf = fin;
     k->data = (uint64_t*)fin->p;
+    k->wbuf = wide;
+    k->wdata = wide ? (uint64_t*)wide->p : nullptr;
     k->digits = digits;
     k->level = level;
     k->aux = aux_count;

@@ -62,6 +62,10 @@ struct rc_context {
   int device = 0;
   bool lazy = false;   // every prime < 2^58
   bool mac64 = false;  // 64-bit per-term Montgomery accumulation in the key product
+  bool wide_ok = false;  // exact integer key product under two internal primes available
+  std::vector<uint64_t> wide_psi;
+  rc::WideTab wide{};
+  std::unique_ptr<rc::DevBuf> wide_buf;
   std::vector<uint64_t> mod, root;  // Q then P
   std::unique_ptr<rc::DevBuf> pc_buf, tw_buf, md_buf, rt_buf;
   rc::PrimeConst* d_pc = nullptr;
@@ -91,6 +95,8 @@ struct rc_ksk {
   rc_context* ctx = nullptr;
   std::shared_ptr<rc::DevBuf> buf;  // [limbs][digits][2][N], NTT domain, Montgomery form
   uint64_t* data = nullptr;
+  std::shared_ptr<rc::DevBuf> wbuf;  // [limbs][digits][2][2 internal primes][N], NTT domain, Montgomery
+  uint64_t* wdata = nullptr;
   uint32_t digits = 0;
   int32_t level = 0;
   uint32_t aux = 0;

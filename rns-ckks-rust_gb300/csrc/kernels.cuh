@@ -54,6 +54,9 @@ void ntt_forward(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int pol
 void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
                  cudaStream_t s);
 
+// row phase of the forward transform only (input: column-phase output)
+void ntt_forward_rows(const NttArgs& a, const PtrTab& data, int polys, int limbs, LimbMap map, cudaStream_t s);
+
 // ---- elementwise / scheme kernels (ops.cu) ----
 enum class EwOp { Add, Sub, Mul };
 // out[k] = a[k] (op) b[k] over `polys` polys of `limbs` limbs; b may be shared
@@ -113,6 +116,20 @@ struct ModDownTab {
 void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int jobs, int limbs, int D,
                int32_t* digits, uint64_t g_inv, int log_n, cudaStream_t s);
 
+// Exact integer key product ("wide-CRT"): residues of S = sum_i d_i * k_i under
+// the two internal primes a0, a1 (context prime indices base, base+1) are
+// combined into the centred integer S (|S| < A/2, A = a0 a1) and reduced mod t.
+struct WideTab {
+  int base;
+  u64 a0, a1;
+  u64 a0inv, a0inv_s;       // a0^-1 mod a1 and its Shoup companion (w.r.t. a1)
+  u64 halfA_lo, halfA_hi;   // floor(A / 2)
+  u64 A_lo, A_hi;
+  const u64* a0_mod_t;      // [Q u P] a0 mod t
+  const u64* a0_mod_t_s;
+  const u64* A_mod_t;       // [Q u P] A mod t
+};
+
 struct KsArgs {
   const PrimeConst* pc;
   NttArgs ntt;
@@ -143,9 +160,24 @@ struct FinalizeArgs {
   int qlimbs, K;
   int rescale;
   uint64_t add_g_inv;  // automorphism applied to the addend (0/1 = none)
+  int wide;            // acc holds [job][2][limbs][2 wide primes][N] residues to CRT-combine
+  WideTab wt;
 };
 void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const PtrTab& out, int jobs,
               cudaStream_t s);
+
+// ---- wide-CRT key product (keyswitch.cu) ----
+// digits [job][digit][N] -> DT [job][digit][2][N]: forward transforms under the
+// two internal primes (context indices base, base+1); false if N is unsupported
+bool wide_digit_transforms(const NttArgs& nt, int base, int D, int jobs, const int32_t* digits, u64* dt,
+                           cudaStream_t s);
+// acc[b][c][j][a][N] (NTT domain) for jobs b0..b0+nb-1 sharing the wide key kw
+void wide_mac(const PrimeConst* pc, int base, int log_n, int D, int key_digits, int total, const u64* kw,
+              const u64* dt, u64* acc, int b0, int nb, u64 chunk, cudaStream_t s);
+// coefficient-form key [digits][2][limbs][N] -> [limbs][digits][2][2][N] residues mod a0, a1
+void wide_key_prep(const PrimeConst* pc, int base, const u64* src, u64* dst, int digits, int limbs, int log_n,
+                   cudaStream_t s);
+void wide_to_mont(const PrimeConst* pc, int base, u64* data, size_t total, int log_n, cudaStream_t s);
 
 // key upload: coefficient-form key [digits][2][limbs][N] (device) ->
 // [limbs][digits][2][N] NTT domain, Montgomery form

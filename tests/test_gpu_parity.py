@@ -310,3 +310,27 @@ def test_encode_decode_matches_oracle(C, pkg, oracle):
     ref_back = oracle.decode_integer_coeffs(n, 2.0 ** 40, params.q_moduli(), ref)
     assert np.max(np.abs(back - ref_back)) <= 1e-12
     assert np.max(np.abs(back - slots)) <= 1e-6
+
+
+@pytest.mark.parametrize("log_n,limbs,aux", [(12, 5, 2), (13, 4, 0), (14, 6, 2)])
+def test_wide_and_standard_key_products_agree(C, pkg, oracle, monkeypatch, log_n, limbs, aux):
+    """The exact integer key product (two internal primes) and the per-limb
+    product give the same residues, equal to the oracle's."""
+    params = pkg.params.hybrid_params(log_n, limbs, aux, 50) if aux else pkg.params.RnsCkksParams(
+        1 << log_n, [pkg.params.RnsPrime(*x) for x in pkg.params.find_ntt_primes(1 << log_n, 50, limbs)], [], 40)
+    n, q = params.poly_degree, params.q_moduli()
+    rng = np.random.default_rng(log_n * 7 + limbs)
+    key, D = _random_key(rng, params, len(q), aux > 0)
+    a, b = rand_ct(rng, q, n), rand_ct(rng, q, n)
+    outs = []
+    for wide in ("1", "0"):
+        monkeypatch.setenv("RNSCKKS_WIDE", wide)
+        ctx = C.RnsCkksContext(params)
+        ksk = ctx.upload_keyswitch_key(key, len(q) - 1, aux)
+        out = ctx.mult_relinearized(C.RnsCiphertext(C.to_device(a), 40), C.RnsCiphertext(C.to_device(b), 40), ksk)
+        outs.append(out.numpy())
+    qpl = oracle.Plans(n, params.primes)
+    ppl = oracle.Plans(n, params.aux_primes) if aux else None
+    m0, m1 = oracle.mult_relinearized(qpl, ppl, a[0], a[1], b[0], b[1], key, D)
+    for o in outs:
+        assert np.array_equal(o[0], m0) and np.array_equal(o[1], m1)
