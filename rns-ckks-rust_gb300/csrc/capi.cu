@@ -186,7 +186,7 @@ size_t ks_ws_bytes(const rc_context* c, int J, int qlimbs, int K, int D) {
   const int total = qlimbs + K;
   const size_t standard = align_up((size_t)J * D * c->N * 4, 256) + arena_size_u64((size_t)J * 2 * total * c->N) +
                           arena_size_u64(ks_scratch_elems(c, J, total, D)) + 1024;
-  const size_t wide = align_up((size_t)J * D * c->N * 4, 256) + arena_size_u64((size_t)J * D * 2 * c->N) +
+  const size_t wide = align_up((size_t)J * D * c->N * 4, 256) + 2 * arena_size_u64((size_t)J * D * 2 * c->N) +
                       arena_size_u64((size_t)J * 2 * total * 2 * c->N) + 1024;
   return std::max(standard, c->wide_ok ? wide : 0);
 }
@@ -258,9 +258,11 @@ void keyswitch_core(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, u
 
   if (wide) {
     const int base = c->L + c->K;
+    uint64_t* work = ar.take<uint64_t>((size_t)J * D * 2 * N);
     uint64_t* dt = ar.take<uint64_t>((size_t)J * D * 2 * N);
     uint64_t* acc = ar.take<uint64_t>((size_t)J * 2 * total * 2 * N);
-    require(wide_digit_transforms(c->ntt(), base, D, J, digits, dt, s), "internal: wide transforms unsupported");
+    require(wide_digit_transforms(c->ntt(), base, D, J, digits, work, dt, s),
+            "internal: wide transforms unsupported");
     launch_check("wide digit transforms");
     // jobs sharing a key run together so that each key word is read once per group
     const uint64_t chunk = (~0ull) / c->mod[base] - 1;
@@ -782,8 +784,9 @@ static int ksk_upload_impl(rc_context* c, const uint64_t* key, bool on_device, u
     std::shared_ptr<DevBuf> wide;
     if (c->wide_ok && c->log_n >= 12 && c->log_n <= 16) {
       const int base = c->L + c->K;
+      DevBuf wtmp(elems * 2 * 8);
       wide.reset(new DevBuf(elems * 2 * 8));
-      uint64_t* w = (uint64_t*)wide->p;
+      uint64_t* w = (uint64_t*)wtmp.p;
       wide_key_prep(c->d_pc, base, t, w, (int)digits, limbs, c->log_n, 0);
       launch_check("wide key prep");
       const int wpolys = limbs * (int)digits * 2;
@@ -794,8 +797,9 @@ static int ksk_upload_impl(rc_context* c, const uint64_t* key, bool on_device, u
         ntt_forward(c->ntt(), tab, tab, cnt, 2, LimbMap{0, base}, 0);
         launch_check("wide key ntt");
       }
-      wide_to_mont(c->d_pc, base, w, elems * 2, c->log_n, 0);
-      launch_check("wide key montgomery");
+      wide_key_tile(c->d_pc, base, w, (uint64_t*)wide->p, (int)digits, limbs, c->log_n, 0);
+      launch_check("wide key tile");
+      cuda_check(cudaDeviceSynchronize(), "wide key");
     }
     const int polys = (int)digits * 2;
     for (int p0 = 0; p0 < polys; p0 += MAXP) {

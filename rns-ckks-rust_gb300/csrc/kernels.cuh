@@ -57,6 +57,10 @@ void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int pol
 // row phase of the forward transform only (input: column-phase output)
 void ntt_forward_rows(const NttArgs& a, const PtrTab& data, int polys, int limbs, LimbMap map, cudaStream_t s);
 
+// row phase writing the tiled digit-transform layout of the wide key product
+void ntt_forward_rows_tiled(const NttArgs& a, const PtrTab& src, u64* out, int p0, int polys, int D, LimbMap map,
+                            cudaStream_t s);
+
 // ---- elementwise / scheme kernels (ops.cu) ----
 enum class EwOp { Add, Sub, Mul };
 // out[k] = a[k] (op) b[k] over `polys` polys of `limbs` limbs; b may be shared
@@ -167,17 +171,21 @@ void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const
               cudaStream_t s);
 
 // ---- wide-CRT key product (keyswitch.cu) ----
-// digits [job][digit][N] -> DT [job][digit][2][N]: forward transforms under the
-// two internal primes (context indices base, base+1); false if N is unsupported
-bool wide_digit_transforms(const NttArgs& nt, int base, int D, int jobs, const int32_t* digits, u64* dt,
-                           cudaStream_t s);
-// acc[b][c][j][a][N] (NTT domain) for jobs b0..b0+nb-1 sharing the wide key kw
-void wide_mac(const PrimeConst* pc, int base, int log_n, int D, int key_digits, int total, const u64* kw,
-              const u64* dt, u64* acc, int b0, int nb, u64 chunk, cudaStream_t s);
+// digits [job][digit][N] -> forward transforms under the two internal primes
+// (context indices base, base+1), written tiled: dtt[job][a][x/32][digit][32].
+// `work` holds jobs*D*2*N u64 (column-phase output).  False if N is unsupported.
+bool wide_digit_transforms(const NttArgs& nt, int base, int D, int jobs, const int32_t* digits, u64* work,
+                           u64* dtt, cudaStream_t s);
+// acc[b][c][j][a][N] (NTT domain) for jobs b0..b0+nb-1 sharing the tiled wide key
+// kwt[limb][a][x/32][digit][c][32] (Montgomery form)
+void wide_mac(const PrimeConst* pc, int base, int log_n, int D, int key_digits, int total, const u64* kwt,
+              const u64* dtt, u64* acc, int b0, int nb, u64 chunk, cudaStream_t s);
 // coefficient-form key [digits][2][limbs][N] -> [limbs][digits][2][2][N] residues mod a0, a1
 void wide_key_prep(const PrimeConst* pc, int base, const u64* src, u64* dst, int digits, int limbs, int log_n,
                    cudaStream_t s);
-void wide_to_mont(const PrimeConst* pc, int base, u64* data, size_t total, int log_n, cudaStream_t s);
+// transformed [limbs][digits][2][2][N] -> tiled kwt[limbs][a][x/32][digits][2][32] in Montgomery form
+void wide_key_tile(const PrimeConst* pc, int base, const u64* src, u64* dst, int digits, int limbs, int log_n,
+                   cudaStream_t s);
 
 // key upload: coefficient-form key [digits][2][limbs][N] (device) ->
 // [limbs][digits][2][N] NTT domain, Montgomery form

@@ -620,59 +620,96 @@ bool wide_cols_dispatch(const NttArgs& nt, int base, int D, int jobs, const int3
   }
 }
 
-constexpr int WIDE_X = 64, WIDE_J = 4, WIDE_BC = 8;
+constexpr int WIDE_BC = 8, WIDE_WARPS = 8;
 
-// acc[b][c][j][a][x] = sum_i DT[b][i][a][x] * KW[j][i][c][a][x] (Montgomery):
-// one thread per (x, limb j, prime a) accumulates both components for up to
-// WIDE_BC jobs that share the key, so each key word is read once per WIDE_BC
-// jobs.  Sums of D products < a^2 stay below a * 2^64 for D < 2^64 / a.
-__global__ __launch_bounds__(WIDE_X * WIDE_J) void k_wide_mac(const PrimeConst* pcs, int base, int log_n, int D,
-                                                            int key_digits, int total, const u64* kw, const u64* dt,
-                                                            u64* acc, int b0, int nb, u64 chunk) {
-  const int N = 1 << log_n;
-  const int x = blockIdx.x * WIDE_X + (threadIdx.x % WIDE_X);
-  const int j = blockIdx.y * WIDE_J + (threadIdx.x / WIDE_X);
-  const int a = blockIdx.z & 1;
-  const int bstart = b0 + (blockIdx.z >> 1) * WIDE_BC;
-  if (j >= total) return;
-  const PrimeConst& pc = pcs[base + a];
-  U128 s0[WIDE_BC], s1[WIDE_BC];
-#pragma unroll
-  for (int b = 0; b < WIDE_BC; ++b) s0[b].lo = s0[b].hi = s1[b].lo = s1[b].hi = 0;
-  const u64* kp = kw + ((size_t)j * key_digits * 2 * 2 + a) * N + x;  // [j][i][c][a][N]
-  const u64* dp = dt + ((size_t)bstart * D * 2 + a) * N + x;         // [b][i][a][N]
+// acc[b][c][j][a][x] = sum_i DT[b][i][a][x] * KW[j][i][c][a][x] (Montgomery).
+// CTA = one 32-position tile x one internal prime a x up to WIDE_BC jobs that
+// share the key: the jobs' digit transforms for the tile (tiled layout, one
+// contiguous run per job) sit in shared memory, and each warp sweeps limbs j,
+// streaming the key tile kwt[j][a][tile][digit][c][32] (contiguous) once for
+// all WIDE_BC jobs.  Sums of D products < a^2 stay below a * 2^64 while
+// D < 2^64 / a (folded by Barrett otherwise).
+__global__ __launch_bounds__(32 * WIDE_WARPS, 2) void k_wide_mac(const PrimeConst* pcs, int base, int log_n, int D,
+                                                                 int key_digits, int total, const u64* kwt,
+                                                                 const u64* dtt, u64* acc, int b0, int nb,
+                                                                 u64 chunk) {
+  extern __shared__ u64 dsm[];  // [WIDE_BC][D][32]
+  const int N = 1 << log_n, tiles = N >> 5;
+  const int xb = blockIdx.x, a = blockIdx.y;
+  const int bstart = b0 + blockIdx.z * WIDE_BC;
   const int nloc = min(WIDE_BC, b0 + nb - bstart);
-  u64 since = 0;
+  const int run = D * 32;
+  for (int e = threadIdx.x; e < nloc * run; e += 32 * WIDE_WARPS) {
+    const int b = e / run, r = e - b * run;
+    dsm[e] = dtt[(((size_t)(bstart + b) * 2 + a) * tiles + xb) * run + r];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const PrimeConst& pc = pcs[base + a];
+  const size_t krun = (size_t)key_digits * 2 * 32;
 #pragma unroll 1
-  for (int i = 0; i < D; ++i) {
-    const u64 k0 = kp[(size_t)i * 4 * N];
-    const u64 k1 = kp[(size_t)i * 4 * N + 2 * N];
+  for (int j = warp; j < total; j += WIDE_WARPS) {
+    const u64* kp = kwt + (((size_t)j * 2 + a) * tiles + xb) * krun + lane;
+    U128 s0[WIDE_BC], s1[WIDE_BC];
+#pragma unroll
+    for (int b = 0; b < WIDE_BC; ++b) s0[b].lo = s0[b].hi = s1[b].lo = s1[b].hi = 0;
+    u64 since = 0;
+#pragma unroll 1
+    for (int i = 0; i < D; ++i) {
+      const u64 k0 = kp[(size_t)i * 64];
+      const u64 k1 = kp[(size_t)i * 64 + 32];
+#pragma unroll
+      for (int b = 0; b < WIDE_BC; ++b) {
+        if (b < nloc) {
+          const u64 d = dsm[(b * D + i) * 32 + lane];
+          add_to(s0[b], mul_wide(d, k0));
+          add_to(s1[b], mul_wide(d, k1));
+        }
+      }
+      if (++since == chunk) {
+#pragma unroll
+        for (int b = 0; b < WIDE_BC; ++b) {
+          s0[b].lo = barrett_reduce(s0[b], pc);
+          s0[b].hi = 0;
+          s1[b].lo = barrett_reduce(s1[b], pc);
+          s1[b].hi = 0;
+        }
+        since = 1;
+      }
+    }
+    const int x = xb * 32 + lane;
 #pragma unroll
     for (int b = 0; b < WIDE_BC; ++b) {
       if (b < nloc) {
-        const u64 d = dp[((size_t)b * D + i) * 2 * N];
-        add_to(s0[b], mul_wide(d, k0));
-        add_to(s1[b], mul_wide(d, k1));
+        const size_t jb = (size_t)(bstart + b);
+        acc[(((jb * 2 + 0) * total + j) * 2 + a) * N + x] = mont_reduce(s0[b], pc);
+        acc[(((jb * 2 + 1) * total + j) * 2 + a) * N + x] = mont_reduce(s1[b], pc);
       }
-    }
-    if (++since == chunk) {
-#pragma unroll
-      for (int b = 0; b < WIDE_BC; ++b) {
-        s0[b].lo = barrett_reduce(s0[b], pc);
-        s0[b].hi = 0;
-        s1[b].lo = barrett_reduce(s1[b], pc);
-        s1[b].hi = 0;
-      }
-      since = 1;
     }
   }
-#pragma unroll
-  for (int b = 0; b < WIDE_BC; ++b) {
-    if (b < nloc) {
-      const size_t jb = (size_t)(bstart + b);
-      acc[(((jb * 2 + 0) * total + j) * 2 + a) * N + x] = mont_reduce(s0[b], pc);
-      acc[(((jb * 2 + 1) * total + j) * 2 + a) * N + x] = mont_reduce(s1[b], pc);
-    }
+}
+
+// transformed key [limbs][digits][2][2][N] -> tiled [limbs][a][x/32][digits][2][32], Montgomery form
+__global__ void k_wide_key_tile(const PrimeConst* pcs, int base, const u64* src, u64* dst, int digits, int limbs,
+                                int log_n) {
+  const size_t N = (size_t)1 << log_n;
+  const size_t total = (size_t)limbs * digits * 2 * 2 * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t lanei = e & 31;
+    size_t r = e >> 5;
+    const int c = (int)(r % 2);
+    r /= 2;
+    const int i = (int)(r % digits);
+    r /= digits;
+    const size_t xb = r % (N >> 5);
+    r /= (N >> 5);
+    const int a = (int)(r % 2);
+    const int j = (int)(r / 2);
+    const size_t x = xb * 32 + lanei;
+    U128 t;
+    t.lo = 0;
+    t.hi = src[((((size_t)j * digits + i) * 2 + c) * 2 + a) * N + x];
+    dst[e] = barrett_reduce(t, pcs[base + a]);  // v * 2^64 mod a
   }
 }
 
@@ -696,17 +733,6 @@ __global__ void k_wide_key_prep(const PrimeConst* pcs, int base, const u64* src,
       t.hi = 0;
       dst[((((size_t)j * digits + i) * 2 + c) * 2 + a) * N + x] = barrett_reduce(t, pcs[base + a]);
     }
-  }
-}
-
-// in place: v -> v * 2^64 mod a (Montgomery form) over [..][2 primes][N]
-__global__ void k_wide_to_mont(const PrimeConst* pcs, int base, u64* data, size_t total, int log_n) {
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
-    const int a = (int)((e >> log_n) & 1);
-    U128 t;
-    t.lo = 0;
-    t.hi = data[e];
-    data[e] = barrett_reduce(t, pcs[base + a]);
   }
 }
 
@@ -967,32 +993,38 @@ void key_to_device_form(const NttArgs& a, const PrimeConst* pc, const u64* src, 
   k_key_relayout<<<g, 256, 0, s>>>(pc, src, dst, digits, limbs, map, a.log_n);
 }
 
-bool wide_digit_transforms(const NttArgs& nt, int base, int D, int jobs, const int32_t* digits, u64* dt,
-                           cudaStream_t s) {
+bool wide_digit_transforms(const NttArgs& nt, int base, int D, int jobs, const int32_t* digits, u64* work,
+                           u64* dtt, cudaStream_t s) {
   {
     ProfScope p("wide_digit_cols", s);
-    const bool ok = nt.lazy ? wide_cols_dispatch<true>(nt, base, D, jobs, digits, dt, s)
-                            : wide_cols_dispatch<false>(nt, base, D, jobs, digits, dt, s);
+    const bool ok = nt.lazy ? wide_cols_dispatch<true>(nt, base, D, jobs, digits, work, s)
+                            : wide_cols_dispatch<false>(nt, base, D, jobs, digits, work, s);
     if (!ok) return false;
   }
-  // row phase over (job, digit) polynomials of 2 limbs (a0, a1)
+  // row phase over (job, digit) polynomials of 2 limbs (a0, a1), written tiled
   const int polys = jobs * D;
   const int N = 1 << nt.log_n;
   for (int p0 = 0; p0 < polys; p0 += MAXP) {
     PtrTab t{};
     const int cnt = polys - p0 < MAXP ? polys - p0 : MAXP;
-    for (int k = 0; k < cnt; ++k) t.p[k] = dt + (size_t)(p0 + k) * 2 * N;
-    ntt_forward_rows(nt, t, cnt, 2, LimbMap{0, base}, s);
+    for (int k = 0; k < cnt; ++k) t.p[k] = work + (size_t)(p0 + k) * 2 * N;
+    ntt_forward_rows_tiled(nt, t, dtt, p0, cnt, D, LimbMap{0, base}, s);
   }
   return true;
 }
 
-void wide_mac(const PrimeConst* pc, int base, int log_n, int D, int key_digits, int total, const u64* kw,
-              const u64* dt, u64* acc, int b0, int nb, u64 chunk, cudaStream_t s) {
+void wide_mac(const PrimeConst* pc, int base, int log_n, int D, int key_digits, int total, const u64* kwt,
+              const u64* dtt, u64* acc, int b0, int nb, u64 chunk, cudaStream_t s) {
   ProfScope p("wide_mac", s);
   const int N = 1 << log_n;
-  dim3 g(N / WIDE_X, (total + WIDE_J - 1) / WIDE_J, 2 * ((nb + WIDE_BC - 1) / WIDE_BC));
-  k_wide_mac<<<g, WIDE_X * WIDE_J, 0, s>>>(pc, base, log_n, D, key_digits, total, kw, dt, acc, b0, nb, chunk);
+  const size_t smem = (size_t)WIDE_BC * D * 32 * 8;
+  static size_t configured = 0;
+  if (smem > 48 * 1024 && smem > configured) {
+    cudaFuncSetAttribute(k_wide_mac, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = smem;
+  }
+  dim3 g(N / 32, 2, (nb + WIDE_BC - 1) / WIDE_BC);
+  k_wide_mac<<<g, 32 * WIDE_WARPS, smem, s>>>(pc, base, log_n, D, key_digits, total, kwt, dtt, acc, b0, nb, chunk);
 }
 
 void wide_key_prep(const PrimeConst* pc, int base, const u64* src, u64* dst, int digits, int limbs, int log_n,
@@ -1003,10 +1035,12 @@ void wide_key_prep(const PrimeConst* pc, int base, const u64* src, u64* dst, int
   k_wide_key_prep<<<g, 256, 0, s>>>(pc, base, src, dst, digits, limbs, log_n);
 }
 
-void wide_to_mont(const PrimeConst* pc, int base, u64* data, size_t total, int log_n, cudaStream_t s) {
+void wide_key_tile(const PrimeConst* pc, int base, const u64* src, u64* dst, int digits, int limbs, int log_n,
+                   cudaStream_t s) {
+  const size_t total = (size_t)limbs * digits * 2 * 2 << log_n;
   int g = (int)((total + 255) / 256);
   if (g > 65535 * 8) g = 65535 * 8;
-  k_wide_to_mont<<<g, 256, 0, s>>>(pc, base, data, total, log_n);
+  k_wide_key_tile<<<g, 256, 0, s>>>(pc, base, src, dst, digits, limbs, log_n);
 }
 
 }  // namespace rc
