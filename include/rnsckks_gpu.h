@@ -118,6 +118,16 @@ int rc_poly_add(rc_context* ctx, const uint64_t* a, const uint64_t* b, uint64_t*
                 int32_t with_aux, void* stream);
 int rc_poly_sub(rc_context* ctx, const uint64_t* a, const uint64_t* b, uint64_t* out, uint32_t limbs,
                 int32_t with_aux, void* stream);
+/* Allocation-free form of rc_poly_multiply for callers that may not allocate
+ * device memory through this library (a host that owns the whole GPU pool, or
+ * a latency-critical loop that cannot take cudaMalloc's device-wide
+ * synchronisation).  No counterpart in the reference (which has no device
+ * memory at all).  Scratch is a fixed 16 MiB array inside the library, so
+ * limbs * N must not exceed 2^20 (RC_ERR_INVALID_ARGUMENT otherwise).  The
+ * first call on a device looks the array up and should precede any CUDA graph
+ * capture; all calls share the array, so calls that overlap on the GPU race. */
+int rc_poly_multiply_noalloc(rc_context* ctx, const uint64_t* a, const uint64_t* b, uint64_t* out, uint32_t limbs,
+                             int32_t with_aux, void* stream);
 /* out_j = a_j * scalars[j] mod q_j (scalars: host array, one per limb): the
  * per-prime reduction of (coefficient * B^i [* P]) in key generation,
  * src/rns/keyswitching.rs:64-68,108-112 */

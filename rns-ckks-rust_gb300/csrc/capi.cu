@@ -15,6 +15,8 @@ namespace rc {
 
 static thread_local std::string g_err;
 
+void set_last_error(const std::string& m) { g_err = m; }
+
 void cuda_check(cudaError_t e, const char* what) {
   if (e != cudaSuccess) {
     if (e == cudaErrorMemoryAllocation) fail(RC_ERR_OUT_OF_MEMORY, std::string(what) + ": " + cudaGetErrorString(e));

@@ -27,6 +27,7 @@ inline void require(bool cond, const std::string& msg) {
   if (!cond) fail(RC_ERR_INVALID_ARGUMENT, msg);
 }
 void cuda_check(cudaError_t e, const char* what);
+void set_last_error(const std::string& m);
 
 struct DevBuf {
   void* p = nullptr;
