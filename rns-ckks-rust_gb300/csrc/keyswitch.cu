@@ -620,24 +620,26 @@ bool wide_cols_dispatch(const NttArgs& nt, int base, int D, int jobs, const int3
   }
 }
 
-constexpr int WIDE_BC = 8, WIDE_WARPS = 8;
+constexpr int WIDE_WARPS = 8;
 
 // acc[b][c][j][a][x] = sum_i DT[b][i][a][x] * KW[j][i][c][a][x] (Montgomery).
-// CTA = one 32-position tile x one internal prime a x up to WIDE_BC jobs that
-// share the key: the jobs' digit transforms for the tile (tiled layout, one
+// CTA = one 32-position tile x one internal prime a x up to BC jobs that share
+// the key: the jobs' digit transforms for the tile (tiled layout, one
 // contiguous run per job) sit in shared memory, and each warp sweeps limbs j,
 // streaming the key tile kwt[j][a][tile][digit][c][32] (contiguous) once for
-// all WIDE_BC jobs.  Sums of D products < a^2 stay below a * 2^64 while
-// D < 2^64 / a (folded by Barrett otherwise).
-__global__ __launch_bounds__(32 * WIDE_WARPS, 2) void k_wide_mac(const PrimeConst* pcs, int base, int log_n, int D,
-                                                                 int key_digits, int total, const u64* kwt,
-                                                                 const u64* dtt, u64* acc, int b0, int nb,
-                                                                 u64 chunk) {
-  extern __shared__ u64 dsm[];  // [WIDE_BC][D][32]
+// all BC jobs, with the next digit's key words loaded ahead.  Sums of D
+// products < a^2 stay below a * 2^64 while D < 2^64 / a (folded by Barrett
+// otherwise).  BC is chosen per launch (1, 2, 4 or 8): small groups keep the
+// footprint small so more CTAs stay resident to cover the key stream.
+template <int BC>
+__global__ __launch_bounds__(32 * WIDE_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : 4)) void k_wide_mac(
+    const PrimeConst* pcs, int base, int log_n, int D, int key_digits, int total, const u64* kwt, const u64* dtt,
+    u64* acc, int b0, int nb, u64 chunk) {
+  extern __shared__ u64 dsm[];  // [BC][D][32]
   const int N = 1 << log_n, tiles = N >> 5;
   const int xb = blockIdx.x, a = blockIdx.y;
-  const int bstart = b0 + blockIdx.z * WIDE_BC;
-  const int nloc = min(WIDE_BC, b0 + nb - bstart);
+  const int bstart = b0 + blockIdx.z * BC;
+  const int nloc = min(BC, b0 + nb - bstart);
   const int run = D * 32;
   for (int e = threadIdx.x; e < nloc * run; e += 32 * WIDE_WARPS) {
     const int b = e / run, r = e - b * run;
@@ -650,16 +652,20 @@ __global__ __launch_bounds__(32 * WIDE_WARPS, 2) void k_wide_mac(const PrimeCons
 #pragma unroll 1
   for (int j = warp; j < total; j += WIDE_WARPS) {
     const u64* kp = kwt + (((size_t)j * 2 + a) * tiles + xb) * krun + lane;
-    U128 s0[WIDE_BC], s1[WIDE_BC];
+    U128 s0[BC], s1[BC];
 #pragma unroll
-    for (int b = 0; b < WIDE_BC; ++b) s0[b].lo = s0[b].hi = s1[b].lo = s1[b].hi = 0;
+    for (int b = 0; b < BC; ++b) s0[b].lo = s0[b].hi = s1[b].lo = s1[b].hi = 0;
     u64 since = 0;
+    u64 n0 = kp[0], n1 = kp[32];
 #pragma unroll 1
     for (int i = 0; i < D; ++i) {
-      const u64 k0 = kp[(size_t)i * 64];
-      const u64 k1 = kp[(size_t)i * 64 + 32];
+      const u64 k0 = n0, k1 = n1;
+      if (i + 1 < D) {
+        n0 = kp[(size_t)(i + 1) * 64];
+        n1 = kp[(size_t)(i + 1) * 64 + 32];
+      }
 #pragma unroll
-      for (int b = 0; b < WIDE_BC; ++b) {
+      for (int b = 0; b < BC; ++b) {
         if (b < nloc) {
           const u64 d = dsm[(b * D + i) * 32 + lane];
           add_to(s0[b], mul_wide(d, k0));
@@ -668,7 +674,7 @@ __global__ __launch_bounds__(32 * WIDE_WARPS, 2) void k_wide_mac(const PrimeCons
       }
       if (++since == chunk) {
 #pragma unroll
-        for (int b = 0; b < WIDE_BC; ++b) {
+        for (int b = 0; b < BC; ++b) {
           s0[b].lo = barrett_reduce(s0[b], pc);
           s0[b].hi = 0;
           s1[b].lo = barrett_reduce(s1[b], pc);
@@ -679,7 +685,7 @@ __global__ __launch_bounds__(32 * WIDE_WARPS, 2) void k_wide_mac(const PrimeCons
     }
     const int x = xb * 32 + lane;
 #pragma unroll
-    for (int b = 0; b < WIDE_BC; ++b) {
+    for (int b = 0; b < BC; ++b) {
       if (b < nloc) {
         const size_t jb = (size_t)(bstart + b);
         acc[(((jb * 2 + 0) * total + j) * 2 + a) * N + x] = mont_reduce(s0[b], pc);
@@ -687,6 +693,20 @@ __global__ __launch_bounds__(32 * WIDE_WARPS, 2) void k_wide_mac(const PrimeCons
       }
     }
   }
+}
+
+template <int BC>
+void launch_wide_mac(const PrimeConst* pc, int base, int log_n, int D, int key_digits, int total, const u64* kwt,
+                     const u64* dtt, u64* acc, int b0, int nb, u64 chunk, cudaStream_t s) {
+  const size_t smem = (size_t)BC * D * 32 * 8;
+  static size_t configured = 0;
+  if (smem > 48 * 1024 && smem > configured) {
+    cudaFuncSetAttribute(k_wide_mac<BC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = smem;
+  }
+  dim3 g((1 << log_n) / 32, 2, (nb + BC - 1) / BC);
+  k_wide_mac<BC><<<g, 32 * WIDE_WARPS, smem, s>>>(pc, base, log_n, D, key_digits, total, kwt, dtt, acc, b0, nb,
+                                                  chunk);
 }
 
 // transformed key [limbs][digits][2][2][N] -> tiled [limbs][a][x/32][digits][2][32], Montgomery form
@@ -1016,15 +1036,10 @@ bool wide_digit_transforms(const NttArgs& nt, int base, int D, int jobs, const i
 void wide_mac(const PrimeConst* pc, int base, int log_n, int D, int key_digits, int total, const u64* kwt,
               const u64* dtt, u64* acc, int b0, int nb, u64 chunk, cudaStream_t s) {
   ProfScope p("wide_mac", s);
-  const int N = 1 << log_n;
-  const size_t smem = (size_t)WIDE_BC * D * 32 * 8;
-  static size_t configured = 0;
-  if (smem > 48 * 1024 && smem > configured) {
-    cudaFuncSetAttribute(k_wide_mac, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    configured = smem;
-  }
-  dim3 g(N / 32, 2, (nb + WIDE_BC - 1) / WIDE_BC);
-  k_wide_mac<<<g, 32 * WIDE_WARPS, smem, s>>>(pc, base, log_n, D, key_digits, total, kwt, dtt, acc, b0, nb, chunk);
+  if (nb <= 1) launch_wide_mac<1>(pc, base, log_n, D, key_digits, total, kwt, dtt, acc, b0, nb, chunk, s);
+  else if (nb <= 2) launch_wide_mac<2>(pc, base, log_n, D, key_digits, total, kwt, dtt, acc, b0, nb, chunk, s);
+  else if (nb <= 4) launch_wide_mac<4>(pc, base, log_n, D, key_digits, total, kwt, dtt, acc, b0, nb, chunk, s);
+  else launch_wide_mac<8>(pc, base, log_n, D, key_digits, total, kwt, dtt, acc, b0, nb, chunk, s);
 }
 
 void wide_key_prep(const PrimeConst* pc, int base, const u64* src, u64* dst, int digits, int limbs, int log_n,
