@@ -197,10 +197,23 @@ def cpu_oracle_op(O, params, lhs_np, rhs_np, key_np, threads: int):
     return time.perf_counter() - t0, out
 
 
+# ciphertexts that share one key read inside the batched entry point (jobs per key-product launch)
+JOBS_PER_LAUNCH = 16
+
+
 # algorithmic bytes per launch for the kernels the roofline may name
 def algorithmic_bytes(kernel: str, batch: int, n: int, limbs: int, aux: int, digits: int, launches: int):
     ext = limbs + aux
+    if kernel == "wide_mac":
+        # key product under the two 55-bit internal primes: the NTT-domain key (ext limbs x 2 primes x
+        # digits x 2 components) once per launch, the digit transforms (digits x 2 primes) of every job in,
+        # the exact products (ext limbs x 2 components x 2 primes) of every job out
+        key = ext * 2 * digits * 2 * n * 8
+        per_job = digits * 2 * n * 8 + ext * 2 * 2 * n * 8
+        return key + per_job * batch / launches
     per_job = {
+        # digit column pass of the wide product: int32 digits in, residues under 2 primes out
+        "wide_digit_cols": digits * n * 4 + digits * 2 * n * 8,
         # digit NTT row pass + key product: key (2 comps, all digits, extended basis) in, accumulators out
         "digit_rows_mac": digits * 2 * ext * n * 8 + 2 * ext * n * 8,
         # digit column pass: int32 digits in, per (digit, limb) residues out (counted as the
@@ -218,9 +231,9 @@ def algorithmic_bytes(kernel: str, batch: int, n: int, limbs: int, aux: int, dig
     return per_job * batch / launches
 
 
-def hmult_algorithmic_bytes(n, limbs, aux, digits):
-    """HMult+relin: 2 input ciphertexts, 1 output ciphertext, the key read once."""
-    return 4 * limbs * n * 8 + 2 * (limbs - 1) * n * 8 + digits * 2 * (limbs + aux) * n * 8
+def hmult_algorithmic_bytes(n, limbs, aux, digits, sharing=1):
+    """HMult+relin: 2 input ciphertexts, 1 output ciphertext, the key read once per `sharing` ops."""
+    return 4 * limbs * n * 8 + 2 * (limbs - 1) * n * 8 + digits * 2 * (limbs + aux) * n * 8 / sharing
 
 
 def peaks():
@@ -369,10 +382,15 @@ def run_gpu(args):
                               "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
                               "peak_kind": peak_kind, "traffic": None,
                               "share": round(st["ms"] / sum(v["ms"] for v in prof.values()), 4)}
-    hm = hmult_algorithmic_bytes(n, limbs, aux, digits)
-    result["hmult_roofline"] = {"algorithmic_bytes_per_op": hm,
+    share = min(B, JOBS_PER_LAUNCH)
+    hm = hmult_algorithmic_bytes(n, limbs, aux, digits, share)
+    hm1 = hmult_algorithmic_bytes(n, limbs, aux, digits, 1)
+    result["hmult_roofline"] = {"algorithmic_bytes_per_op": int(hm), "key_shared_by": share,
                                 "achieved_GBs": round(hm * value / world / 1e9, 1),
-                                "frac": round(hm * value / world / 1e9 / peak, 4)}
+                                "frac": round(hm * value / world / 1e9 / peak, 4),
+                                "per_op_algorithmic_bytes": int(hm1),
+                                "per_op_achieved_GBs": round(hm1 * per_op_value / 1e9, 1),
+                                "per_op_frac": round(hm1 * per_op_value / 1e9 / peak, 4)}
     result["kernels"] = {k: {"launches": v["launches"], "ms_per_step": round(v["ms"] / args.steps, 4)}
                          for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}
 
