@@ -146,6 +146,14 @@ int rc_mult_plain(rc_context* ctx, const rc_ciphertext* ct, const uint64_t* plai
 /* multiply_plain_rns: src/rns/ops.rs:54-66 (scale unchanged) */
 int rc_multiply_plain_rns(rc_context* ctx, const rc_ciphertext* ct, const uint64_t* plain, rc_ciphertext* out,
                           void* stream);
+/* Sum over k of mult_plain(cts[k], plains[k]), the inner sum of the BSGS linear transform
+ * (apply_giant_step_terms, src/ckks/bootstrapping/linear_transform.rs:234-252: mult_plain, context/ops.rs:20-30,
+ * folded with RnsCiphertext::add, ciphertexts.rs:60-69).  All cts share level and scale; out gets the level and
+ * twice the scale.  cts_ntt / plains_ntt = 1 when those inputs are already in the NTT domain (as written by
+ * rc_ntt_forward), so a caller can transform baby-step rotations and diagonals once and reuse them; the
+ * products are summed in the NTT domain and transformed back once.  Output in coefficient form. */
+int rc_mult_plain_accumulate(rc_context* ctx, uint32_t count, const rc_ciphertext* cts, int32_t cts_ntt,
+                             const uint64_t* const* plains, int32_t plains_ntt, rc_ciphertext* out, void* stream);
 /* mult: context/ops.rs:63-70 -> multiply_ciphertexts_rns, src/rns/ops.rs:84-100 */
 int rc_mult(rc_context* ctx, const rc_ciphertext* lhs, const rc_ciphertext* rhs, rc_ciphertext* out_quadratic,
             void* stream);

@@ -610,6 +610,27 @@ class RnsCkksContext:
              _stream())
         return RnsCiphertext(out, r.scale_bits, r.level)
 
+    def ntt_forward_copy(self, data: torch.Tensor) -> torch.Tensor:
+        """NTT-domain copy of a stack of Q-basis polynomials shaped (..., limbs, N) (rc_ntt_forward)."""
+        out = data.contiguous().clone()
+        limbs = out.shape[-2]
+        call("rc_ntt_forward", self.handle, _ptr(out), out.numel() // (limbs * self.params.poly_degree), limbs, 0,
+             _stream())
+        return out
+
+    def mult_plain_accumulate(self, cts: Sequence[RnsCiphertext], plains: Sequence, cts_ntt: bool = False,
+                              plains_ntt: bool = False) -> RnsCiphertext:
+        """Sum of mult_plain(cts[k], plains[k]) (linear_transform.rs:234-252), one inverse transform.
+        With cts_ntt / plains_ntt the inputs are NTT-domain tensors from `ntt_forward_copy`."""
+        n = len(cts)
+        out = self._ct_out(2, cts[0].level + 1)
+        C = (RcCiphertext * n)(*[c.raw() for c in cts])
+        P = (ctypes.c_void_p * n)(*[(p.data if isinstance(p, RnsPolynomial) else p).data_ptr() for p in plains])
+        r = RcCiphertext(out.data_ptr(), 0, 0)
+        call("rc_mult_plain_accumulate", self.handle, n, C, int(cts_ntt), P, int(plains_ntt), ctypes.byref(r),
+             _stream())
+        return RnsCiphertext(out, r.scale_bits, r.level)
+
     def rescale(self, ct: RnsCiphertext) -> RnsCiphertext:
         """context/ops.rs:32-37."""
         out = self._ct_out(2, max(ct.level, 1))

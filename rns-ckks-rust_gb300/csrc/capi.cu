@@ -1054,6 +1054,68 @@ extern "C" int rc_multiply_plain_rns(rc_context* c, const rc_ciphertext* ct, con
   });
 }
 
+extern "C" int rc_mult_plain_accumulate(rc_context* c, uint32_t count, const rc_ciphertext* cts, int32_t cts_ntt,
+                                        const uint64_t* const* plains, int32_t plains_ntt, rc_ciphertext* out,
+                                        void* stream) {
+  return guarded([&] {
+    require(c && cts && plains && out && out->data, "arguments must not be null");
+    require(count >= 1, "the inner sum needs at least one term");
+    for (uint32_t k = 0; k < count; ++k) {
+      check_ct(c, &cts[k], "ciphertext");
+      require(plains[k] != nullptr, "arguments must not be null");
+      require(cts[k].scale_bits == cts[0].scale_bits, "ciphertexts must share the same scale to add");
+      require(cts[k].level == cts[0].level, "ciphertexts must be at the same level to add");
+    }
+    cudaStream_t s = S(stream);
+    const int limbs = cts[0].level + 1;
+    const size_t pl = (size_t)limbs * c->N;
+    const LimbMap map = qmap(c, limbs);
+    constexpr int CH = 16;  // terms per pass: bounds the scratch for coefficient-form inputs
+    const int ct_buf = cts_ntt ? 0 : 2 * CH, pt_buf = plains_ntt ? 0 : CH;
+    Arena ar(ws_device(c, s, arena_size_u64(2 * pl) + arena_size_u64((size_t)(ct_buf + pt_buf) * pl) + 1024));
+    uint64_t* acc = ar.take<uint64_t>(2 * pl);
+    uint64_t* tmp = (ct_buf + pt_buf) ? ar.take<uint64_t>((size_t)(ct_buf + pt_buf) * pl) : nullptr;
+    for (uint32_t b = 0; b < count; b += CH) {
+      const int J = (int)std::min<uint32_t>(CH, count - b);
+      PtrTab ctab{}, ptab{};
+      if (cts_ntt) {
+        for (int j = 0; j < J; ++j) ctab.p[j] = cts[b + j].data;
+      } else {
+        PtrTab src{}, dst{};
+        for (int j = 0; j < J; ++j) {
+          src.p[2 * j] = cts[b + j].data;
+          src.p[2 * j + 1] = cts[b + j].data + pl;
+          dst.p[2 * j] = tmp + (size_t)2 * j * pl;
+          dst.p[2 * j + 1] = tmp + (size_t)(2 * j + 1) * pl;
+          ctab.p[j] = dst.p[2 * j];
+        }
+        ntt_forward(c->ntt(), src, dst, 2 * J, limbs, map, s);
+      }
+      if (plains_ntt) {
+        for (int j = 0; j < J; ++j) ptab.p[j] = const_cast<uint64_t*>(plains[b + j]);
+      } else {
+        PtrTab src{}, dst{};
+        for (int j = 0; j < J; ++j) {
+          src.p[j] = const_cast<uint64_t*>(plains[b + j]);
+          dst.p[j] = tmp + (size_t)(ct_buf + j) * pl;
+          ptab.p[j] = dst.p[j];
+        }
+        ntt_forward(c->ntt(), src, dst, J, limbs, map, s);
+      }
+      plain_mac(c->d_pc, ctab, ptab, J, acc, b > 0, limbs, map, c->N, s);
+    }
+    PtrTab a{}, o{};
+    a.p[0] = acc;
+    a.p[1] = acc + pl;
+    o.p[0] = out->data;
+    o.p[1] = out->data + pl;
+    ntt_inverse(c->ntt(), a, o, 2, limbs, map, s);
+    launch_check("mult_plain_accumulate");
+    out->level = cts[0].level;
+    out->scale_bits = cts[0].scale_bits + cts[0].scale_bits;  // mult_plain, context/ops.rs:24-29
+  });
+}
+
 extern "C" int rc_mult(rc_context* c, const rc_ciphertext* a, const rc_ciphertext* b, rc_ciphertext* out,
                        void* stream) {
   return guarded([&] {

@@ -67,6 +67,10 @@ enum class EwOp { Add, Sub, Mul };
 // across polys (b_shared != 0 uses b.p[0] for every poly).
 void ew_binary(EwOp op, const PrimeConst* pc, const PtrTab& a, const PtrTab& b, int b_shared, const PtrTab& out,
                int polys, int limbs, LimbMap map, int n, cudaStream_t s);
+// acc[c] (+)= sum_k ct[k][c] * pt[k] mod q for c in {0,1}: NTT-domain plaintext products summed over `count`
+// terms (ct.p[k] -> component 0 of term k, component 1 at +limbs*n); accumulate != 0 adds to acc
+void plain_mac(const PrimeConst* pc, const PtrTab& ct, const PtrTab& pt, int count, u64* acc, int accumulate,
+               int limbs, LimbMap map, int n, cudaStream_t s);
 // out_j = a_j * v[j] mod q_j
 struct ScalarTab {
   u64 v[80];

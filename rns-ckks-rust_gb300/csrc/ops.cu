@@ -34,6 +34,22 @@ __global__ void k_ew_binary(int op, const PrimeConst* pc, PtrTab a, PtrTab b, in
   }
 }
 
+__global__ void k_plain_mac(const PrimeConst* pc, PtrTab ct, PtrTab pt, int count, u64* acc, int accumulate,
+                            int limbs, LimbMap map, int log_n) {
+  const size_t total = (size_t)limbs << log_n;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const PrimeConst& c = pc[map.prime((int)(e >> log_n))];
+    u64 s0 = accumulate ? acc[e] : 0, s1 = accumulate ? acc[total + e] : 0;
+    for (int k = 0; k < count; ++k) {
+      const u64 p = pt.p[k][e];
+      s0 = add_mod(s0, mul_mod(ct.p[k][e], p, c), c.q);
+      s1 = add_mod(s1, mul_mod(ct.p[k][total + e], p, c), c.q);
+    }
+    acc[e] = s0;
+    acc[total + e] = s1;
+  }
+}
+
 __global__ void k_tensor(const PrimeConst* pc, PtrTab in4, PtrTab out3, int limbs, int log_n) {
   const size_t total = (size_t)limbs << log_n;
   const int job = blockIdx.y;
@@ -127,6 +143,14 @@ void ew_binary(EwOp op, const PrimeConst* pc, const PtrTab& a, const PtrTab& b, 
   ProfScope p("elementwise", s);
   k_ew_binary<<<g, 256, 0, s>>>(op == EwOp::Add ? 0 : op == EwOp::Sub ? 1 : 2, pc, a, b, b_shared, out, limbs, map,
                                 log_n);
+}
+
+void plain_mac(const PrimeConst* pc, const PtrTab& ct, const PtrTab& pt, int count, u64* acc, int accumulate,
+               int limbs, LimbMap map, int n, cudaStream_t s) {
+  if (count <= 0) return;
+  ProfScope p("plain_mac", s);
+  k_plain_mac<<<grid_for((size_t)limbs * n, 256), 256, 0, s>>>(pc, ct, pt, count, acc, accumulate, limbs, map,
+                                                              __builtin_ctz(n));
 }
 
 void mul_scalar(const PrimeConst* pc, const u64* a, const ScalarTab& v, u64* out, int limbs, LimbMap map, int n,
