@@ -411,11 +411,126 @@ def run_gpu(args):
         result["cpu_baseline"] = {"value": round(1.0 / secs, 5), "unit": UNIT, "cores": threads, "kind": "port",
                                   "sample": "1 faithful HMult+relin (pair 0 of the batch, same key) on the oracle "
                                             f"(C restatement of the reference CPU path), {secs:.1f} s"}
+    if not args.no_extra:
+        # the batched NTT microbenchmark (64 polys x 24 limbs) and the mixed-level relinearize+rescale batch
+        # (128 quadratic ciphertexts, limbs 8..24, CUDA graph); reported beside the headline, untimed by it
+        result["ntt_microbench"] = ntt_microbench(C, ctx, params, peak, args.seed)
+        result["mixed_level_relin"] = mixed_level_relin(C, ctx, params, load_oracle(), args.seed)
     if rank == 0:
         print(json.dumps(result), flush=True)
     if world > 1:
         import torch.distributed as dist
         dist.destroy_process_group()
+
+
+def ntt_microbench(C, ctx, params, peak, seed, reps=5):
+    """Batched NTT/INTT microbenchmark: 64 polynomials x 24 limbs at N=2^16 (uniform residues), forward then
+    inverse as one batched call each, against one call per polynomial; bit-exact round trip; HBM GB/s
+    counting one read and one write of every limb per transform."""
+    import torch
+    n, q = params.poly_degree, params.q_moduli()
+    limbs, P = len(q), 64
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    mod = torch.tensor(q, dtype=torch.int64, device="cuda").view(1, limbs, 1)
+    data = torch.randint(0, 1 << 62, (P, limbs, n), device="cuda", generator=gen) % mod
+    orig = data.clone()
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    stream = torch.cuda.current_stream()
+    step_bytes = 2 * P * limbs * n * 8 * 2
+
+    def batched():
+        C.call("rc_ntt_forward", ctx.handle, ctypes.c_void_p(data.data_ptr()), P, limbs, 0, s)
+        C.call("rc_ntt_inverse", ctx.handle, ctypes.c_void_p(data.data_ptr()), P, limbs, 0, s)
+
+    def per_poly():
+        for i in range(P):
+            p = ctypes.c_void_p(data[i].data_ptr())
+            C.call("rc_ntt_forward", ctx.handle, p, 1, limbs, 0, s)
+            C.call("rc_ntt_inverse", ctx.handle, p, 1, limbs, 0, s)
+
+    out = {"polys": P, "limbs": limbs, "poly_degree": n, "bytes_per_round_trip": step_bytes}
+    for name, fn in (("batched", batched), ("per_poly", per_poly)):
+        for _ in range(3):
+            fn()
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(stream)
+        for _ in range(reps):
+            fn()
+        e1.record(stream)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        out[f"{name}_ms"] = round(ms, 4)
+        out[f"{name}_GBs"] = round(step_bytes / (ms / 1e3) / 1e9, 1)
+        out[f"{name}_frac"] = round(step_bytes / (ms / 1e3) / 1e9 / peak, 4)
+    out["round_trip_exact"] = bool(torch.equal(data, orig))
+    out["batched_vs_per_poly"] = round(out["per_poly_ms"] / out["batched_ms"], 3)
+    del data, orig
+    return out
+
+
+def mixed_level_relin(C, ctx, params, O, seed, count=128, reps=3):
+    """Relinearize + rescale of `count` quadratic ciphertexts (uniform residues) whose limb counts are drawn
+    uniformly from 8..24, one hybrid key per level, in one rc_relinearize_rescale_batch call, captured once
+    in a CUDA graph and replayed; the direct call is timed beside it.  One job of the lowest level is
+    checked against the oracle."""
+    import torch
+    n, q, p = params.poly_degree, params.q_moduli(), params.p_moduli()
+    rng = np.random.default_rng(seed)
+    levels = [int(x) - 1 for x in rng.integers(8, 25, count)]
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+
+    def uniform(shape, moduli):
+        mod = torch.tensor(moduli, dtype=torch.int64, device="cuda").view(*([1] * (len(shape) - 2)), -1, 1)
+        return torch.randint(0, 1 << 62, shape, device="cuda", generator=gen) % mod
+
+    keys, low = {}, min(levels)
+    low_key = None
+    for lv in sorted(set(levels)):
+        D = ctx.decomp_digits(lv)
+        kc = uniform((D, 2, lv + 1 + len(p), n), q[: lv + 1] + p)
+        keys[lv] = ctx._upload_key(kc, D, lv, len(p), 0, False)
+        if lv == low:
+            low_key = C.to_host(kc)
+        del kc
+    quads = [C.RnsQuadraticCiphertext(uniform((3, lv + 1, n), q[: lv + 1]), 80) for lv in levels]
+    ks = [keys[lv] for lv in levels]
+    side = torch.cuda.Stream()
+    res = {"jobs": count, "limbs": "uniform 8..24", "levels_distinct": len(keys),
+           "key_bytes_standard_form": int(sum(ctx.decomp_digits(lv) * 2 * (lv + 1 + len(p)) * n * 8 for lv in keys))}
+    with torch.cuda.stream(side):
+        ctx.reserve(max(levels), 16)
+        outs = [torch.empty((2, lv, n), dtype=torch.int64, device="cuda") for lv in levels]
+        ctx.relinearize_rescale_batch(quads, ks, outs)  # warm
+        graph = ctx.capture_graph(lambda: ctx.relinearize_rescale_batch(quads, ks, outs))
+        st = torch.cuda.current_stream()
+        for name, fn in (("direct", lambda: ctx.relinearize_rescale_batch(quads, ks, outs)),
+                         ("graph", graph.launch)):
+            fn()
+            st.synchronize()
+            e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+            e0.record(st)
+            for _ in range(reps):
+                fn()
+            e1.record(st)
+            st.synchronize()
+            ms = e0.elapsed_time(e1) / reps
+            res[f"{name}_ms"] = round(ms, 3)
+            res[f"{name}_relin_per_s"] = round(count / (ms / 1e3), 1)
+        i = levels.index(low)
+        qpl = O.Plans(n, params.primes[: low + 1])
+        ppl = O.Plans(n, params.aux_primes)
+        d = C.to_host(quads[i].data)
+        r0, r1 = O.relinearize(qpl, ppl, d[0], d[1], d[2], low_key, low_key.shape[0])
+        got = C.to_host(outs[i])
+        res["bit_exact_vs_cpu"] = bool(np.array_equal(got[0], O.rescale_poly(qpl, r0))
+                                       and np.array_equal(got[1], O.rescale_poly(qpl, r1)))
+        res["checked_job_limbs"] = low + 1
+    del graph, quads, outs, keys
+    torch.cuda.synchronize()
+    return res
 
 
 def run_reference(args):
@@ -469,6 +584,8 @@ def main():
     ap.add_argument("--seed", type=int, default=0x5EED + 2)
     ap.add_argument("--impl", choices=["gb300", "reference"], default="gb300")
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
+    ap.add_argument("--no-extra", action="store_true",
+                    help="skip the NTT microbenchmark and the mixed-level relinearization batch")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

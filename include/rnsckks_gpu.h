@@ -41,6 +41,7 @@ extern "C" {
 
 typedef struct rc_context rc_context;
 typedef struct rc_ksk rc_ksk;
+typedef struct rc_graph rc_graph;
 
 /* RnsPrime{modulus, primitive_root}: src/rns/basis.rs:8-22 */
 typedef struct {
@@ -186,6 +187,21 @@ int rc_relinearize_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* q
                          rc_ciphertext* out, void* stream);
 int rc_rotate_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* ct, const rc_ksk* const* keys,
                     rc_ciphertext* out, void* stream);
+/* relinearize then rescale (context/ops.rs:111-122 followed by context/ops.rs:32-37) for `count`
+ * quadratic ciphertexts of any mix of levels; the rescale is fused into the keyswitch's last pass.  out[i]
+ * gets level - 1 and the rescaled scale.  After rc_reserve(ctx, top level, 16, stream) the call allocates
+ * nothing and can be captured in a CUDA graph. */
+int rc_relinearize_rescale_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* quadratic,
+                                 const rc_ksk* const* keys, rc_ciphertext* out, void* stream);
+
+/* ---- CUDA graphs of library calls (no reference counterpart: the crate is CPU-only).  Capture every
+ * call made on `stream` between begin and end (thread-local capture mode) into an executable graph;
+ * rc_reserve the scratch first (capture refuses to grow it).  Pointers and sizes are baked in: replay
+ * with rc_graph_launch on the same buffers. ---- */
+int rc_graph_begin(rc_context* ctx, void* stream);
+int rc_graph_end(rc_context* ctx, void* stream, rc_graph** out);
+int rc_graph_launch(rc_graph* graph, void* stream);
+void rc_graph_destroy(rc_graph* graph);
 
 /* ---- host-buffer entry points (what a CPU-side caller such as the Rust crate
  * binds): host [2][level+1][N] inputs, host [2][level][N] output, copies

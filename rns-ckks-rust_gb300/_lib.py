@@ -88,6 +88,11 @@ SIGNATURES = [
     ("rc_mult_relinearized_batch", ctypes.c_int, [_vp, _u32, _CT, _CT, ctypes.POINTER(_vp), _CT, _vp]),
     ("rc_relinearize_batch", ctypes.c_int, [_vp, _u32, _CT, ctypes.POINTER(_vp), _CT, _vp]),
     ("rc_rotate_batch", ctypes.c_int, [_vp, _u32, _CT, ctypes.POINTER(_vp), _CT, _vp]),
+    ("rc_relinearize_rescale_batch", ctypes.c_int, [_vp, _u32, _CT, ctypes.POINTER(_vp), _CT, _vp]),
+    ("rc_graph_begin", ctypes.c_int, [_vp, _vp]),
+    ("rc_graph_end", ctypes.c_int, [_vp, _vp, ctypes.POINTER(_vp)]),
+    ("rc_graph_launch", ctypes.c_int, [_vp, _vp]),
+    ("rc_graph_destroy", None, [_vp]),
     ("rc_mult_relinearized_host", ctypes.c_int, [_vp, _vp, _vp, _i32, _i32, _vp, _vp, ctypes.POINTER(_i32), _vp]),
     ("rc_mult_relinearized_batch_host", ctypes.c_int, [_vp, _u32, ctypes.POINTER(_vp), ctypes.POINTER(_vp),
                                                        ctypes.POINTER(_i32), ctypes.POINTER(_i32),

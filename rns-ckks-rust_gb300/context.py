@@ -703,6 +703,32 @@ class RnsCkksContext:
         call("rc_mult_relinearized_batch", self.handle, n, L, R, K, O, _stream())
         return [RnsCiphertext(o, O[i].scale_bits, O[i].level) for i, o in enumerate(outs)]
 
+    def relinearize_rescale_batch(self, cts: Sequence[RnsQuadraticCiphertext],
+                                  keys: Sequence[RnsKeySwitchingKey], outs: Optional[Sequence[torch.Tensor]] = None
+                                  ) -> List[RnsCiphertext]:
+        """relinearize + rescale of many quadratic ciphertexts (mixed levels) in one call."""
+        n = len(cts)
+        outs = list(outs) if outs is not None else [self._ct_out(2, c.level) for c in cts]
+        Q = (RcCiphertext * n)(*[c.raw() for c in cts])
+        O = (RcCiphertext * n)(*[RcCiphertext(o.data_ptr(), 0, 0) for o in outs])
+        K = (ctypes.c_void_p * n)(*[k.handle for k in keys])
+        call("rc_relinearize_rescale_batch", self.handle, n, Q, K, O, _stream())
+        return [RnsCiphertext(o, O[i].scale_bits, O[i].level) for i, o in enumerate(outs)]
+
+    def capture_graph(self, fn) -> "CudaGraph":
+        """Record every library call `fn` makes on the current (non-default) stream into a CUDA graph."""
+        s = _stream()
+        call("rc_graph_begin", self.handle, s)
+        h = ctypes.c_void_p()
+        try:
+            fn()
+        except BaseException:
+            if lib().rc_graph_end(self.handle, s, ctypes.byref(h)) == 0:
+                lib().rc_graph_destroy(h)
+            raise
+        call("rc_graph_end", self.handle, s, ctypes.byref(h))
+        return CudaGraph(h)
+
     # ---- rotation, context/rotation.rs ----
     def apply_galois_automorphism(self, poly: RnsPolynomial, galois_element: int) -> RnsPolynomial:
         """context/rotation.rs:6-10."""
@@ -746,6 +772,24 @@ class RnsCkksContext:
         K = (ctypes.c_void_p * n)(*[k.keyswitch_key.handle for k in keys])
         call("rc_rotate_batch", self.handle, n, C, K, O, _stream())
         return [RnsCiphertext(o, O[i].scale_bits, O[i].level) for i, o in enumerate(outs)]
+
+
+class CudaGraph:
+    """An executable CUDA graph of library calls (rc_graph_*): replays on the captured buffers."""
+
+    def __init__(self, handle: ctypes.c_void_p):
+        self.handle = handle
+
+    def launch(self) -> None:
+        call("rc_graph_launch", self.handle, _stream())
+
+    def __del__(self):
+        try:
+            if self.handle:
+                lib().rc_graph_destroy(self.handle)
+                self.handle = None
+        except Exception:
+            pass
 
 
 def _automorphism_signed(coeffs: np.ndarray, g: int) -> np.ndarray:

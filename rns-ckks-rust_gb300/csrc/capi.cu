@@ -1281,6 +1281,86 @@ extern "C" int rc_relinearize_batch(rc_context* c, uint32_t count, const rc_ciph
   });
 }
 
+extern "C" int rc_relinearize_rescale_batch(rc_context* c, uint32_t count, const rc_ciphertext* qct,
+                                            const rc_ksk* const* keys, rc_ciphertext* out, void* stream) {
+  return guarded([&] {
+    require(c && qct && keys && out, "arguments must not be null");
+    std::map<std::pair<int, std::pair<int, int>>, std::vector<int>> groups;
+    for (uint32_t i = 0; i < count; ++i) {
+      check_ct(c, &qct[i], "quadratic ciphertext");
+      require(out[i].data != nullptr, "arguments must not be null");
+      require(out[i].data != qct[i].data, "rescale output must not alias its input");
+      require(qct[i].level >= 1, "rescale requires at least two levels");
+      require(keys[i] != nullptr, "keyswitch key must not be null");
+      groups[{qct[i].level, {(int)keys[i]->aux, (int)keys[i]->digits}}].push_back((int)i);
+    }
+    // groups run from the highest level down, each in chunks of at most MAXP/4 jobs (the size rc_reserve
+    // provisions), so one reserve of the top level covers a whole mixed-level batch under graph capture
+    for (auto g = groups.rbegin(); g != groups.rend(); ++g) {
+      const int limbs = g->first.first + 1;
+      const size_t pl = (size_t)limbs * c->N, po = (size_t)(limbs - 1) * c->N;
+      const int drop = floor_log2(c->mod[limbs - 1]);
+      for (size_t b = 0; b < g->second.size(); b += MAXP / 4) {
+        std::vector<KsJob> jobs;
+        for (size_t k = b; k < g->second.size() && k < b + MAXP / 4; ++k) {
+          const int i = g->second[k];
+          jobs.push_back(KsJob{qct[i].data + 2 * pl, keys[i], qct[i].data, qct[i].data + pl, out[i].data,
+                               out[i].data + po});
+          out[i].level = qct[i].level - 1;
+          const int sb = qct[i].scale_bits - drop;  // rescale_ciphertext_rns, ops.rs:68-82
+          out[i].scale_bits = sb < 0 ? 0 : sb;
+        }
+        keyswitch_run(c, jobs, limbs, 0, true, S(stream));
+      }
+    }
+  });
+}
+
+// ---- CUDA graphs of library calls ----
+struct rc_graph {
+  cudaGraph_t graph = nullptr;
+  cudaGraphExec_t exec = nullptr;
+};
+
+extern "C" int rc_graph_begin(rc_context* c, void* stream) {
+  return guarded([&] {
+    require(c != nullptr, "context must not be null");
+    require(stream != nullptr, "CUDA graph capture needs a non-default stream");
+    cuda_check(cudaStreamBeginCapture(S(stream), cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
+  });
+}
+
+extern "C" int rc_graph_end(rc_context* c, void* stream, rc_graph** out) {
+  return guarded([&] {
+    require(c && out && stream, "arguments must not be null");
+    *out = nullptr;
+    std::unique_ptr<rc_graph> g(new rc_graph());
+    cuda_check(cudaStreamEndCapture(S(stream), &g->graph), "cudaStreamEndCapture");
+    cuda_check(cudaGraphInstantiate(&g->exec, g->graph, 0), "cudaGraphInstantiate");
+    *out = g.release();
+  });
+}
+
+extern "C" int rc_graph_launch(rc_graph* g, void* stream) {
+  if (!g || !g->exec) {
+    set_last_error("graph must not be null");
+    return RC_ERR_INVALID_ARGUMENT;
+  }
+  const cudaError_t e = cudaGraphLaunch(g->exec, S(stream));
+  if (e != cudaSuccess) {
+    set_last_error(std::string("cudaGraphLaunch: ") + cudaGetErrorString(e));
+    return RC_ERR_CUDA;
+  }
+  return RC_OK;
+}
+
+extern "C" void rc_graph_destroy(rc_graph* g) {
+  if (!g) return;
+  if (g->exec) cudaGraphExecDestroy(g->exec);
+  if (g->graph) cudaGraphDestroy(g->graph);
+  delete g;
+}
+
 extern "C" int rc_rotate_batch(rc_context* c, uint32_t count, const rc_ciphertext* ct, const rc_ksk* const* keys,
                                rc_ciphertext* out, void* stream) {
   return guarded([&] {

@@ -40,8 +40,14 @@ cudaEvent_t take_event() {
 
 bool prof_enabled() { return g_on; }
 
+// launches recorded into a CUDA graph are not timed (an event record would become a graph node)
+static bool capturing(cudaStream_t s) {
+  cudaStreamCaptureStatus st = cudaStreamCaptureStatusNone;
+  return cudaStreamIsCapturing(s, &st) == cudaSuccess && st != cudaStreamCaptureStatusNone;
+}
+
 void prof_begin(const char* name, cudaStream_t s) {
-  if (!g_on) return;
+  if (!g_on || capturing(s)) return;
   std::lock_guard<std::mutex> lk(g_mu);
   cudaEvent_t e = take_event();
   cudaEventRecord(e, s);
@@ -49,7 +55,7 @@ void prof_begin(const char* name, cudaStream_t s) {
 }
 
 void prof_end(const char* name, cudaStream_t s) {
-  if (!g_on) return;
+  if (!g_on || capturing(s)) return;
   std::lock_guard<std::mutex> lk(g_mu);
   auto& v = g_open[s];
   if (v.empty()) return;

@@ -1,0 +1,100 @@
+"""Mixed-level batched relinearize+rescale and CUDA-graph capture of library calls, bit-exact against the
+per-op path and the oracle (relinearize: context/ops.rs:111-122, rescale: context/ops.rs:32-37)."""
+import math
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # collected on CPU-only machines, never run there
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+
+@pytest.fixture(scope="module")
+def env(pkg, oracle):
+    pkg.lib()
+    from rnsckks_gb300 import context as C
+    params = pkg.params.hybrid_params(12, 8, 2, 50)
+    ctx = C.RnsCkksContext(params)
+    q, p = params.q_moduli(), params.p_moduli()
+    rng = np.random.default_rng(77)
+    keys, host_keys = {}, {}
+    for lv in range(1, len(q)):
+        qm = q[: lv + 1]
+        D = math.ceil(math.prod(qm).bit_length() / 30)
+        k = np.stack([np.stack([np.stack([rng.integers(0, m, params.poly_degree, dtype=np.uint64)
+                                          for m in qm + p]) for _ in range(2)]) for _ in range(D)])
+        host_keys[lv] = k
+        keys[lv] = ctx.upload_keyswitch_key(k, lv, len(p))
+    return C, ctx, params, keys, host_keys, oracle
+
+
+def _quad(C, rng, params, level, scale_bits=80):
+    q = params.q_moduli()[: level + 1]
+    d = np.stack([np.stack([rng.integers(0, m, params.poly_degree, dtype=np.uint64) for m in q]) for _ in range(3)])
+    return C.RnsQuadraticCiphertext(C.to_device(d), scale_bits), d
+
+
+def test_relinearize_rescale_batch_mixed_levels(env):
+    C, ctx, params, keys, host_keys, O = env
+    rng = np.random.default_rng(5)
+    levels = [int(x) for x in rng.integers(1, 8, 21)]
+    cts, raw = zip(*[_quad(C, rng, params, lv, 60 + lv) for lv in levels])
+    outs = ctx.relinearize_rescale_batch(list(cts), [keys[lv] for lv in levels])
+    for ct, out, lv in zip(cts, outs, levels):
+        ref = ctx.rescale(ctx.relinearize(ct, keys[lv]))
+        assert out.level == lv - 1 == ref.level and out.scale_bits == ref.scale_bits
+        assert np.array_equal(out.numpy(), ref.numpy())
+    # one job against the oracle: relinearize then rescale of both components
+    i = int(np.argmax(levels))
+    lv = levels[i]
+    qpl = O.Plans(params.poly_degree, params.primes[: lv + 1])
+    ppl = O.Plans(params.poly_degree, params.aux_primes)
+    d = raw[i]
+    r0, r1 = O.relinearize(qpl, ppl, d[0], d[1], d[2], host_keys[lv], host_keys[lv].shape[0])
+    h = outs[i].numpy()
+    assert np.array_equal(h[0], O.rescale_poly(qpl, r0)) and np.array_equal(h[1], O.rescale_poly(qpl, r1))
+    assert outs[i].scale_bits == max(0, 60 + lv - (params.q_moduli()[lv].bit_length() - 1))
+
+
+def test_graph_capture_replays_the_batch(env):
+    C, ctx, params, keys, host_keys, O = env
+    rng = np.random.default_rng(6)
+    levels = [7, 3, 5, 7, 2, 6, 4, 7, 1]
+    cts = [_quad(C, rng, params, lv)[0] for lv in levels]
+    ks = [keys[lv] for lv in levels]
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        ctx.reserve(7, 16)
+        outs = [torch.zeros((2, lv, params.poly_degree), dtype=torch.int64, device="cuda") for lv in levels]
+        direct = [r.data.clone() for r in ctx.relinearize_rescale_batch(cts, ks, [o.clone() for o in outs])]
+        graph = ctx.capture_graph(lambda: ctx.relinearize_rescale_batch(cts, ks, outs))
+        for o in outs:
+            o.zero_()
+        graph.launch()
+        side.synchronize()
+        for o, d in zip(outs, direct):
+            assert torch.equal(o, d)
+        # the graph reads the captured buffers: new contents give the new result
+        fresh = _quad(C, rng, params, levels[0])[0]
+        cts[0].data.copy_(fresh.data)
+        graph.launch()
+        side.synchronize()
+        expect = ctx.rescale(ctx.relinearize(cts[0], ks[0]))
+        assert np.array_equal(C.to_host(outs[0]), expect.numpy())
+    torch.cuda.synchronize()
+
+
+def test_graph_capture_refuses_to_grow_scratch(env):
+    C, ctx, params, keys, host_keys, O = env
+    rng = np.random.default_rng(7)
+    ct = _quad(C, rng, params, 7)[0]
+    side = torch.cuda.Stream()  # a stream with no reserved scratch
+    with torch.cuda.stream(side):
+        with pytest.raises(C.RcError, match="reserved"):
+            ctx.capture_graph(lambda: ctx.relinearize_rescale_batch([ct], [keys[7]]))
+    torch.cuda.synchronize()
+    with pytest.raises(C.RcError, match="non-default stream"):
+        ctx.capture_graph(lambda: None)
