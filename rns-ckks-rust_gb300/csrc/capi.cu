@@ -194,19 +194,26 @@ size_t ks_ws_bytes(const rc_context* c, int J, int qlimbs, int K, int D) {
 }
 
 // The exact integer key product applies when the internal primes' product A
-// exceeds twice the largest possible |sum_i d_i k_ij| = D * N * 2^29 * (q_max - 1).
-bool use_wide(const rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, int K, int D) {
-  if (!c->wide_ok || c->log_n < 12 || c->log_n > 16) return false;
-  if (level_info(c, qlimbs).dt.small_q) return false;  // lifted digits are not the digits themselves
-  for (auto& j : jobs)
-    if (!j.key->wdata) return false;
+// exceeds four times the largest possible |sum_i d_i k_ij| = D * N * 2^29 * (q_max - 1)
+// (the CRT recovers the centred value from the top mixed-radix digit) and every
+// digit is its own residue in each limb (no prime below 2^29 in Q_l).
+bool wide_applies(const rc_context* c, int qlimbs, int K, int D) {
+  if (!c->wide_ok || D > 200) return false;  // the key product keeps D digit words per job in shared memory
+  if (level_info(c, qlimbs).dt.small_q) return false;
   uint64_t qmax = 0;
   for (int i = 0; i < qlimbs; ++i) qmax = std::max(qmax, c->mod[i]);
   for (int k = 0; k < K; ++k) qmax = std::max(qmax, c->mod[c->L + k]);
   const u128h bound = (u128h)D * (u128h)c->N * ((u128h)1 << 29) * (u128h)(qmax - 1);
-  const u128h A = ((u128h)c->wide.A_hi << 64) | c->wide.A_lo;
-  if (bound >= ((u128h)1 << 126)) return false;
-  return 2 * bound < A;
+  if (bound >= ((u128h)1 << 124)) return false;
+  u128h A = 1;
+  for (int i = 0; i < 4; ++i) A *= c->wp.q[i];
+  return 4 * bound < A;
+}
+
+bool use_wide(const rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, int K, int D) {
+  for (auto& j : jobs)
+    if (!j.key->wdata) return false;
+  return wide_applies(c, qlimbs, K, D);
 }
 
 // Runs keyswitch for `jobs` jobs at `qlimbs` limbs (all keys of the same kind);
@@ -259,37 +266,28 @@ void keyswitch_core(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, u
   }
 
   if (wide) {
-    const int base = c->L + c->K;
-    uint64_t* work = ar.take<uint64_t>((size_t)J * D * 2 * N);
-    uint64_t* dt = ar.take<uint64_t>((size_t)J * D * 2 * N);
-    uint64_t* acc = ar.take<uint64_t>((size_t)J * 2 * total * 2 * N);
-    require(wide_digit_transforms(c->ntt(), base, D, J, digits, work, dt, s),
-            "internal: wide transforms unsupported");
+    uint2* work = ar.take<uint2>((size_t)J * D * 2 * N);
+    uint2* dt = ar.take<uint2>((size_t)J * D * 2 * N);
+    uint2* acc = ar.take<uint2>((size_t)J * 2 * total * 2 * N);
+    require(wide_digit_transforms(c->wp, D, J, digits, work, dt, s), "internal: wide transforms unsupported");
     launch_check("wide digit transforms");
     // jobs sharing a key run together so that each key word is read once per group
-    const uint64_t chunk = (~0ull) / c->mod[base] - 1;
     int b = 0;
     while (b < J) {
       int e = b + 1;
       while (e < J && jobs[e].key->wdata == jobs[b].key->wdata) ++e;
-      wide_mac(c->d_pc, base, c->log_n, D, (int)jobs[b].key->digits, total, jobs[b].key->wdata, dt, acc, b, e - b,
-               chunk, s);
+      wide_mac(c->wp, D, (int)jobs[b].key->digits, total, (const uint2*)jobs[b].key->wdata, dt, acc, b, e - b, s);
       launch_check("wide mac");
       b = e;
     }
-    const int polys = J * 2 * total;
-    for (int p0 = 0; p0 < polys; p0 += MAXP) {
-      PtrTab t{};
-      const int cnt = std::min(MAXP, polys - p0);
-      for (int k = 0; k < cnt; ++k) t.p[k] = acc + (size_t)(p0 + k) * 2 * N;
-      ntt_inverse(c->ntt(), t, t, cnt, 2, LimbMap{0, base}, s);
-    }
-    launch_check("ntt_inverse(wide acc)");
-    finalize(f, acc, add, out, J, s);
+    require(wide_inverse(c->wp, acc, J * 2 * total, s), "internal: wide transforms unsupported");
+    launch_check("wide inverse transforms");
+    finalize(f, (const uint64_t*)acc, add, out, J, s);
     launch_check("finalize");
     return;
   }
 
+  for (auto& j : jobs) require(j.key->data != nullptr, "internal: keyswitch key has no per-limb form");
   uint64_t* acc = ar.take<uint64_t>((size_t)J * 2 * total * N);
   uint64_t* scratch = ar.take<uint64_t>(scratch_elems);
 
@@ -491,36 +489,6 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
     c->mod.insert(c->mod.end(), pm.begin(), pm.end());
     c->root = qg;
     c->root.insert(c->root.end(), pg.begin(), pg.end());
-    // Two internal "product" primes a0 > a1 just below 2^55 (a = k*2N + 1, not in
-    // Q u P) carry the exact integer key product of the wide-CRT keyswitch; they
-    // get twiddle tables like the scheme primes, at indices L+K and L+K+1.
-    {
-      const uint64_t step = 2 * N;
-      uint64_t kk = ((1ull << 55) - 1) / step;
-      std::vector<uint64_t> found;
-      while (found.size() < 2 && kk > 1) {
-        const uint64_t a = kk * step + 1;
-        bool clash = false;
-        for (uint64_t m : c->mod) clash = clash || m == a;
-        if (!clash && is_prime_u64(a)) found.push_back(a);
-        --kk;
-      }
-      if (found.size() == 2) {
-        c->wide_ok = true;
-        for (uint64_t a : found) {
-          // any primitive 2N-th root of unity serves (these primes never meet user data)
-          uint64_t psi = 0;
-          for (uint64_t x = 2; x < 1000 && !psi; ++x) {
-            const uint64_t cand = powmod_h(x, (a - 1) / (2 * N), a);
-            if (powmod_h(cand, N, a) == a - 1) psi = cand;
-          }
-          c->mod.push_back(a);
-          c->root.push_back(0);
-          c->wide_psi.push_back(psi);
-        }
-      }
-      if (const char* e = getenv("RNSCKKS_WIDE")) c->wide_ok = c->wide_ok && atoi(e) != 0;
-    }
     const int P = (int)c->mod.size();
     // Lazy (unreduced) forward butterflies need every prime < 2^58
     c->lazy = true;
@@ -554,8 +522,7 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
       k.mac_chunk = (uint64_t)((~0ull) / (out_bound * q));
       k.mac_chunk64 = (uint64_t)((~0ull) / (2 * q));
       // psi = g^((q-1)/2N) (NttPlan::new, ntt.rs:42)
-      const uint64_t psi = i < c->L + c->K ? powmod_h(c->root[i] % q, (q - 1) / (2 * N), q)
-                                           : c->wide_psi[i - c->L - c->K];
+      const uint64_t psi = powmod_h(c->root[i] % q, (q - 1) / (2 * N), q);
       const uint64_t psi_inv = invmod_h(psi, q);
       std::vector<uint64_t> pw(N), pwi(N);
       pw[0] = pwi[0] = 1;
@@ -687,35 +654,86 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
       c->rt.inv = d;
       c->rt.inv_s = d + (size_t)L * L;
     }
-    // ---- wide-CRT reconstruction table: S = r0 + a0 * ((r1 - r0) a0^-1 mod a1), centred mod A
-    if (c->wide_ok) {
-      const int QP = c->L + c->K;
-      const uint64_t a0 = c->mod[QP], a1 = c->mod[QP + 1];
-      const u128h A = (u128h)a0 * a1;
-      std::vector<uint64_t> blob((size_t)3 * QP);
-      for (int t = 0; t < QP; ++t) {
-        const uint64_t m = c->mod[t];
-        blob[t] = a0 % m;
-        blob[QP + t] = shoup_h(a0 % m, m);
-        blob[2 * QP + t] = (uint64_t)(A % m);
+    // ---- internal primes of the exact key product: the four largest w = k * 2^17 + 1 < 2^29
+    // (w = 1 mod 2N for every N <= 2^16), with twiddle tables for the pairs (w0, w1), (w2, w3)
+    {
+      std::vector<uint64_t> w;
+      for (uint64_t k = ((1ull << 29) - 2) >> 17; k > 0 && w.size() < 4; --k)
+        if (is_prime_u64((k << 17) + 1)) w.push_back((k << 17) + 1);
+      c->wide_ok = w.size() == 4 && c->log_n >= 12 && c->log_n <= 16;
+      if (const char* e = getenv("RNSCKKS_WIDE")) c->wide_ok = c->wide_ok && atoi(e) != 0;
+      if (c->wide_ok) {
+        WidePrimes& wp = c->wp;
+        wp.log_n = c->log_n;
+        auto shoup32 = [](uint64_t x, uint64_t q) { return (uint32_t)((x << 32) / q); };
+        std::vector<Tw2> tf((size_t)2 * N), ti((size_t)2 * N);
+        for (int i = 0; i < 4; ++i) {
+          const uint64_t q = w[i];
+          wp.q[i] = (uint32_t)q;
+          wp.n_inv[i] = (uint32_t)invmod_h(N % q, q);
+          wp.n_inv_s[i] = shoup32(wp.n_inv[i], q);
+          wp.bar[i] = (~0ull) / q;
+          uint64_t psi = 0;  // any primitive 2N-th root of unity (these primes never meet user data)
+          for (uint64_t x = 2; x < 100000 && !psi; ++x) {
+            const uint64_t cand = powmod_h(x, (q - 1) / (2 * N), q);
+            if (powmod_h(cand, N, q) == q - 1) psi = cand;
+          }
+          require(psi != 0, "internal: no root of unity for an internal prime");
+          const uint64_t psi_inv = invmod_h(psi, q);
+          std::vector<uint64_t> pw(N), pwi(N);
+          pw[0] = pwi[0] = 1;
+          for (uint64_t e = 1; e < N; ++e) {
+            pw[e] = mulmod_h(pw[e - 1], psi, q);
+            pwi[e] = mulmod_h(pwi[e - 1], psi_inv, q);
+          }
+          const int pair = i >> 1, half = i & 1;
+          for (uint64_t kk = 0; kk < N; ++kk) {
+            const int e = bitrev((int)kk, c->log_n);
+            Tw2& f = tf[(size_t)pair * N + kk];
+            Tw2& g = ti[(size_t)pair * N + kk];
+            (half ? f.w1 : f.w0) = (uint32_t)pw[e];
+            (half ? f.s1 : f.s0) = shoup32(pw[e], q);
+            (half ? g.w1 : g.w0) = (uint32_t)pwi[e];
+            (half ? g.s1 : g.s0) = shoup32(pwi[e], q);
+          }
+        }
+        c->wide_tw.reset(new DevBuf(sizeof(Tw2) * 4 * N));
+        Tw2* dtw = (Tw2*)c->wide_tw->p;
+        cuda_check(cudaMemcpy(dtw, tf.data(), sizeof(Tw2) * 2 * N, cudaMemcpyHostToDevice), "upload wide tw");
+        cuda_check(cudaMemcpy(dtw + 2 * N, ti.data(), sizeof(Tw2) * 2 * N, cudaMemcpyHostToDevice), "upload wide tw");
+        wp.tw_fwd = dtw;
+        wp.tw_inv = dtw + 2 * N;
+        // Garner constants and, per scheme prime t, (w0 w1) mod t and A mod t
+        WideTab& W = c->wide;
+        for (int i = 0; i < 4; ++i) W.w[i] = (uint32_t)w[i];
+        auto inv_pair = [&](int a, int m, uint32_t& g, uint32_t& gs) {
+          g = (uint32_t)invmod_h(w[a] % w[m], w[m]);
+          gs = shoup32(g, w[m]);
+        };
+        inv_pair(0, 1, W.g01, W.g01s);
+        inv_pair(0, 2, W.g02, W.g02s);
+        inv_pair(1, 2, W.g12, W.g12s);
+        inv_pair(0, 3, W.g03, W.g03s);
+        inv_pair(1, 3, W.g13, W.g13s);
+        inv_pair(2, 3, W.g23, W.g23s);
+        W.half3 = (uint32_t)((w[3] + 1) / 2);
+        const int QP = c->L + c->K;
+        const u128h A = (u128h)w[0] * w[1] * w[2] * w[3];
+        std::vector<uint64_t> blob((size_t)3 * QP);
+        for (int t = 0; t < QP; ++t) {
+          const uint64_t m = c->mod[t];
+          const uint64_t c01 = (uint64_t)(((u128h)w[0] * w[1]) % m);
+          blob[t] = c01;
+          blob[QP + t] = shoup_h(c01, m);
+          blob[2 * QP + t] = (uint64_t)(A % m);
+        }
+        c->wide_buf.reset(new DevBuf(blob.size() * 8));
+        uint64_t* d = (uint64_t*)c->wide_buf->p;
+        cuda_check(cudaMemcpy(d, blob.data(), blob.size() * 8, cudaMemcpyHostToDevice), "upload wide tables");
+        W.c01_mod_t = d;
+        W.c01_mod_t_s = d + QP;
+        W.A_mod_t = d + 2 * QP;
       }
-      c->wide_buf.reset(new DevBuf(blob.size() * 8));
-      uint64_t* d = (uint64_t*)c->wide_buf->p;
-      cuda_check(cudaMemcpy(d, blob.data(), blob.size() * 8, cudaMemcpyHostToDevice), "upload wide tables");
-      WideTab& w = c->wide;
-      w.base = QP;
-      w.a0 = a0;
-      w.a1 = a1;
-      w.a0inv = invmod_h(a0 % a1, a1);
-      w.a0inv_s = shoup_h(w.a0inv, a1);
-      const u128h half = A >> 1;
-      w.halfA_lo = (uint64_t)half;
-      w.halfA_hi = (uint64_t)(half >> 64);
-      w.a0_mod_t = d;
-      w.a0_mod_t_s = d + QP;
-      w.A_mod_t = d + 2 * QP;
-      w.A_lo = (uint64_t)A;
-      w.A_hi = (uint64_t)(A >> 64);
     }
     cuda_check(cudaDeviceSynchronize(), "context setup");
     *out = c.release();
@@ -776,48 +794,42 @@ static int ksk_upload_impl(rc_context* c, const uint64_t* key, bool on_device, u
     const int limbs = level + 1 + (int)aux_count;
     const size_t elems = (size_t)digits * 2 * limbs * c->N;
     DevBuf tmp(elems * 8);
-    std::shared_ptr<DevBuf> fin(new DevBuf(elems * 8));
     cuda_check(cudaMemcpy(tmp.p, key, elems * 8, on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice),
                "key upload");
     const LimbMap map{level + 1, c->L};
     uint64_t* t = (uint64_t*)tmp.p;
-    // wide form (exact integer key product): the same integers under the two
-    // internal primes, transformed and in Montgomery form
-    std::shared_ptr<DevBuf> wide;
-    if (c->wide_ok && c->log_n >= 12 && c->log_n <= 16) {
-      const int base = c->L + c->K;
-      DevBuf wtmp(elems * 2 * 8);
-      wide.reset(new DevBuf(elems * 2 * 8));
-      uint64_t* w = (uint64_t*)wtmp.p;
-      wide_key_prep(c->d_pc, base, t, w, (int)digits, limbs, c->log_n, 0);
-      launch_check("wide key prep");
-      const int wpolys = limbs * (int)digits * 2;
-      for (int p0 = 0; p0 < wpolys; p0 += MAXP) {
-        PtrTab tab{};
-        const int cnt = std::min(MAXP, wpolys - p0);
-        for (int k = 0; k < cnt; ++k) tab.p[k] = w + (size_t)(p0 + k) * 2 * c->N;
-        ntt_forward(c->ntt(), tab, tab, cnt, 2, LimbMap{0, base}, 0);
-        launch_check("wide key ntt");
-      }
-      wide_key_tile(c->d_pc, base, w, (uint64_t*)wide->p, (int)digits, limbs, c->log_n, 0);
-      launch_check("wide key tile");
+    // wide form (exact integer key product) when it applies at the key's level: the same integers under
+    // the internal primes, transformed and tiled; it then replaces the per-limb form, which is built
+    // otherwise.  Q-only keys truncated to fewer levels keep qualifying (smaller q_max, same digits).
+    const int Kk = aux_count ? c->K : 0;
+    const int Dk = aux_count ? level_info(c, level + 1).digits : (int)digits;
+    std::shared_ptr<DevBuf> wide, fin;
+    if (wide_applies(c, level + 1, Kk, Dk)) {
+      const size_t welems = elems * 2;  // two uint2 pairs per coefficient
+      DevBuf wtmp(welems * 8);
+      wide.reset(new DevBuf(welems * 8));
+      require(wide_key_build(c->wp, t, (int)digits, limbs, (uint2*)wtmp.p, (uint2*)wide->p, 0),
+              "internal: wide transforms unsupported");
+      launch_check("wide key");
       cuda_check(cudaDeviceSynchronize(), "wide key");
+    } else {
+      fin.reset(new DevBuf(elems * 8));
+      const int polys = (int)digits * 2;
+      for (int p0 = 0; p0 < polys; p0 += MAXP) {
+        PtrTab tab{};
+        const int cnt = std::min(MAXP, polys - p0);
+        for (int k = 0; k < cnt; ++k) tab.p[k] = t + (size_t)(p0 + k) * limbs * c->N;
+        ntt_forward(c->ntt(), tab, tab, cnt, limbs, map, 0);
+        launch_check("key ntt");
+      }
+      key_to_device_form(c->ntt(), c->d_pc, t, (uint64_t*)fin->p, (int)digits, limbs, map, c->N, 0);
+      launch_check("key relayout");
+      cuda_check(cudaDeviceSynchronize(), "key upload");
     }
-    const int polys = (int)digits * 2;
-    for (int p0 = 0; p0 < polys; p0 += MAXP) {
-      PtrTab tab{};
-      const int cnt = std::min(MAXP, polys - p0);
-      for (int k = 0; k < cnt; ++k) tab.p[k] = t + (size_t)(p0 + k) * limbs * c->N;
-      ntt_forward(c->ntt(), tab, tab, cnt, limbs, map, 0);
-      launch_check("key ntt");
-    }
-    key_to_device_form(c->ntt(), c->d_pc, t, (uint64_t*)fin->p, (int)digits, limbs, map, c->N, 0);
-    launch_check("key relayout");
-    cuda_check(cudaDeviceSynchronize(), "key upload");
     rc_ksk* k = new rc_ksk();
     k->ctx = c;
     k->buf = fin;
-    k->data = (uint64_t*)fin->p;
+    k->data = fin ? (uint64_t*)fin->p : nullptr;
     k->wbuf = wide;
     k->wdata = wide ? (uint64_t*)wide->p : nullptr;
     k->digits = digits;

@@ -63,10 +63,10 @@ struct rc_context {
   int device = 0;
   bool lazy = false;   // every prime < 2^58
   bool mac64 = false;  // 64-bit per-term Montgomery accumulation in the key product
-  bool wide_ok = false;  // exact integer key product under two internal primes available
-  std::vector<uint64_t> wide_psi;
-  rc::WideTab wide{};
-  std::unique_ptr<rc::DevBuf> wide_buf;
+  bool wide_ok = false;  // exact integer key product under the four internal primes available
+  rc::WidePrimes wp{};    // internal primes, transform constants and twiddle tables (wide_tw)
+  rc::WideTab wide{};     // CRT back to the scheme primes (tables in wide_buf)
+  std::unique_ptr<rc::DevBuf> wide_buf, wide_tw;
   std::vector<uint64_t> mod, root;  // Q then P
   std::unique_ptr<rc::DevBuf> pc_buf, tw_buf, md_buf, rt_buf;
   rc::PrimeConst* d_pc = nullptr;
@@ -94,9 +94,11 @@ struct rc_context {
 
 struct rc_ksk {
   rc_context* ctx = nullptr;
-  std::shared_ptr<rc::DevBuf> buf;  // [limbs][digits][2][N], NTT domain, Montgomery form
+  // per-limb form [limbs][digits][2][N], NTT domain, Montgomery form (null when the wide form is kept)
+  std::shared_ptr<rc::DevBuf> buf;
   uint64_t* data = nullptr;
-  std::shared_ptr<rc::DevBuf> wbuf;  // [limbs][digits][2][2 internal primes][N], NTT domain, Montgomery
+  // wide form: uint2 residues mod the internal prime pairs, NTT domain, tiled [limbs][pair][N/32][digits][2][32]
+  std::shared_ptr<rc::DevBuf> wbuf;
   uint64_t* wdata = nullptr;
   uint32_t digits = 0;
   int32_t level = 0;

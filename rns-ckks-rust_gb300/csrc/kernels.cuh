@@ -57,10 +57,6 @@ void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int pol
 // row phase of the forward transform only (input: column-phase output)
 void ntt_forward_rows(const NttArgs& a, const PtrTab& data, int polys, int limbs, LimbMap map, cudaStream_t s);
 
-// row phase writing the tiled digit-transform layout of the wide key product
-void ntt_forward_rows_tiled(const NttArgs& a, const PtrTab& src, u64* out, int p0, int polys, int D, LimbMap map,
-                            cudaStream_t s);
-
 // ---- elementwise / scheme kernels (ops.cu) ----
 enum class EwOp { Add, Sub, Mul };
 // out[k] = a[k] (op) b[k] over `polys` polys of `limbs` limbs; b may be shared
@@ -124,18 +120,27 @@ struct ModDownTab {
 void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int jobs, int limbs, int D,
                int32_t* digits, uint64_t g_inv, int log_n, cudaStream_t s);
 
-// Exact integer key product ("wide-CRT"): residues of S = sum_i d_i * k_i under
-// the two internal primes a0, a1 (context prime indices base, base+1) are
-// combined into the centred integer S (|S| < A/2, A = a0 a1) and reduced mod t.
+// Exact integer key product ("wide-CRT"): S = sum_i d_i * k_i is carried under
+// four internal primes w0..w3 < 2^29 (product A), handled as two pairs
+// (w0, w1), (w2, w3) whose residues sit side by side in a uint2.
+struct WidePrimes {
+  uint32_t q[4];
+  uint32_t n_inv[4], n_inv_s[4];  // N^-1 mod q and its Shoup companion
+  u64 bar[4];                     // floor(2^64 / q): 64-bit -> residue reduction
+  const Tw2* tw_fwd;              // [2 pairs][N]: psi^bitrev(k)
+  const Tw2* tw_inv;              // [2 pairs][N]: psi^-bitrev(k)
+  int log_n;
+};
+// Garner CRT of (S mod w0..w3) to the centred integer S (|S| < A/4), reduced mod
+// each scheme prime t.
 struct WideTab {
-  int base;
-  u64 a0, a1;
-  u64 a0inv, a0inv_s;       // a0^-1 mod a1 and its Shoup companion (w.r.t. a1)
-  u64 halfA_lo, halfA_hi;   // floor(A / 2)
-  u64 A_lo, A_hi;
-  const u64* a0_mod_t;      // [Q u P] a0 mod t
-  const u64* a0_mod_t_s;
-  const u64* A_mod_t;       // [Q u P] A mod t
+  uint32_t w[4];
+  uint32_t g01, g01s, g02, g02s, g12, g12s;  // w0^-1 mod w1, w0^-1 mod w2, w1^-1 mod w2 (+ Shoup)
+  uint32_t g03, g03s, g13, g13s, g23, g23s;  // w0^-1, w1^-1, w2^-1 mod w3 (+ Shoup)
+  uint32_t half3;                            // top mixed-radix digit >= half3 <=> S >= A/2
+  const u64* c01_mod_t;                      // [Q u P] (w0 w1) mod t and its Shoup companion
+  const u64* c01_mod_t_s;
+  const u64* A_mod_t;                        // [Q u P] A mod t
 };
 
 struct KsArgs {
@@ -168,28 +173,28 @@ struct FinalizeArgs {
   int qlimbs, K;
   int rescale;
   uint64_t add_g_inv;  // automorphism applied to the addend (0/1 = none)
-  int wide;            // acc holds [job][2][limbs][2 wide primes][N] residues to CRT-combine
+  int wide;            // acc holds [job][2][limbs][2 pairs][N] uint2 residues mod w0..w3 to CRT-combine
   WideTab wt;
 };
 void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const PtrTab& out, int jobs,
               cudaStream_t s);
 
-// ---- wide-CRT key product (keyswitch.cu) ----
-// digits [job][digit][N] -> forward transforms under the two internal primes
-// (context indices base, base+1), written tiled: dtt[job][a][x/32][digit][32].
-// `work` holds jobs*D*2*N u64 (column-phase output).  False if N is unsupported.
-bool wide_digit_transforms(const NttArgs& nt, int base, int D, int jobs, const int32_t* digits, u64* work,
-                           u64* dtt, cudaStream_t s);
-// acc[b][c][j][a][N] (NTT domain) for jobs b0..b0+nb-1 sharing the tiled wide key
-// kwt[limb][a][x/32][digit][c][32] (Montgomery form)
-void wide_mac(const PrimeConst* pc, int base, int log_n, int D, int key_digits, int total, const u64* kwt,
-              const u64* dtt, u64* acc, int b0, int nb, u64 chunk, cudaStream_t s);
-// coefficient-form key [digits][2][limbs][N] -> [limbs][digits][2][2][N] residues mod a0, a1
-void wide_key_prep(const PrimeConst* pc, int base, const u64* src, u64* dst, int digits, int limbs, int log_n,
-                   cudaStream_t s);
-// transformed [limbs][digits][2][2][N] -> tiled kwt[limbs][a][x/32][digits][2][32] in Montgomery form
-void wide_key_tile(const PrimeConst* pc, int base, const u64* src, u64* dst, int digits, int limbs, int log_n,
-                   cudaStream_t s);
+// ---- wide-CRT key product (wide.cu) ----
+// digits [job][digit][N] -> transforms under w0..w3, written tiled:
+// dtt[job][pair][x/32][digit][32].  `work` holds jobs*D*2*N uint2.  False if N
+// is unsupported (log N outside 12..16).
+bool wide_digit_transforms(const WidePrimes& w, int D, int jobs, const int32_t* digits, uint2* work, uint2* dtt,
+                           cudaStream_t s);
+// acc[b][c][j][pair][N] (NTT domain, reduced) for jobs b0..b0+nb-1 sharing the
+// tiled key kwt[j][pair][x/32][digit][c][32]
+void wide_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt, uint2* acc,
+              int b0, int nb, cudaStream_t s);
+// inverse transforms of `polys` consecutive [pair][N] polynomials, in place
+bool wide_inverse(const WidePrimes& w, uint2* data, int polys, cudaStream_t s);
+// coefficient-form key [digits][2][limbs][N] (residues mod the scheme primes) ->
+// tiled wide key kwt; `tmp` holds digits*2*limbs*2*N uint2
+bool wide_key_build(const WidePrimes& w, const u64* key, int digits, int limbs, uint2* tmp, uint2* kwt,
+                    cudaStream_t s);
 
 // key upload: coefficient-form key [digits][2][limbs][N] (device) ->
 // [limbs][digits][2][N] NTT domain, Montgomery form

@@ -20,6 +20,7 @@
 //    addend (relinearize / rotate) and optional rescale in one pass.
 #include "kernels.cuh"
 #include "nttcore.cuh"
+#include "wide.cuh"
 
 namespace rc {
 
@@ -547,240 +548,6 @@ bool digit_dispatch(const KsArgs& a, const int32_t* digits, const KeyTab& kt, u6
 }
 
 // ---------------------------------------------------------------------------
-// wide-CRT key product: S_j = sum_i d_i * k_ij exactly (as integers), carried
-// under the internal primes a0, a1, then reduced mod each q_j in finalize.
-// |S_j| <= D * N * 2^29 * (q_j - 1) < A / 2 is checked on the host.
-// ---------------------------------------------------------------------------
-
-// digit -> residue mod a (a > 2^29) -> column phase of its transform under a.
-// blockIdx.y = (job * D + digit) * 2 + a; output DT[job][digit][a][N].
-template <int M1, int M2, bool LAZY>
-__global__ __launch_bounds__(256, 2) void k_wide_digit_cols_f(NttArgs nt, int base, int D, const int32_t* digits,
-                                                              u64* dt) {
-  using G = core::Geo<M1>;
-  constexpr int COLS = DigitColTile<M1>::COLS, N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2;
-  __shared__ u64 tile[COLS * G::STRIDE];
-  __shared__ Twiddle twl[N1];
-  const int c0 = blockIdx.x * COLS;
-  const int a = blockIdx.y & 1, jd = blockIdx.y >> 1;  // jd = job * D + digit
-  const int prime = base + a;
-  const u64 q = nt.pc[prime].q;
-  core::stage_twiddles<M1>(twl, nt.tw_fwd + (size_t)prime * N, 1, threadIdx.x, 256);
-  const int32_t* in = digits + (size_t)jd * N;
-  u64* out = dt + ((size_t)jd * 2 + a) * N;
-#pragma unroll 4
-  for (int it = 0; it < N1 * COLS / 256; ++it) {
-    const int idx = it * 256 + threadIdx.x;
-    const int r = idx / COLS, c = idx % COLS;
-    const int32_t d = in[(size_t)r * N2 + c0 + c];
-    tile[c * G::STRIDE + core::swz<M1>(r)] = d >= 0 ? (u64)d : q - (u64)(-(int64_t)d);
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5;
-#pragma unroll 1
-  for (int cb = warp * G::SUBS; cb < COLS; cb += 8 * G::SUBS) {
-    const int lv = core::lane_id_volatile();
-    const int sub = lv / G::LANES, l = lv % G::LANES;
-    u64* buf = tile + (cb + sub) * G::STRIDE;
-    u64 v[8];
-#pragma unroll
-    for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::first_idx<M1>(l, k))];
-    __syncwarp();
-    core::fwd_sub<M1, LAZY>(v, buf, l, twl, q);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::last_idx<M1>(l, k))] = v[k];
-  }
-  __syncthreads();
-#pragma unroll 4
-  for (int it = 0; it < N1 * COLS / 256; ++it) {
-    const int idx = it * 256 + threadIdx.x;
-    const int r = idx / COLS, c = idx % COLS;
-    out[(size_t)r * N2 + c0 + c] = tile[c * G::STRIDE + core::swz<M1>(r)];
-  }
-}
-
-template <bool LAZY>
-bool wide_cols_dispatch(const NttArgs& nt, int base, int D, int jobs, const int32_t* digits, u64* dt,
-                        cudaStream_t s) {
-  dim3 g(1, jobs * D * 2);
-  switch (nt.log_n) {
-#define RC_WIDE_COLS(LN, A, B)                                                  \
-  case LN:                                                                      \
-    g.x = (1 << B) / DigitColTile<A>::COLS;                                     \
-    k_wide_digit_cols_f<A, B, LAZY><<<g, 256, 0, s>>>(nt, base, D, digits, dt); \
-    return true;
-    RC_WIDE_COLS(12, 6, 6)
-    RC_WIDE_COLS(13, 6, 7)
-    RC_WIDE_COLS(14, 7, 7)
-    RC_WIDE_COLS(15, 7, 8)
-    RC_WIDE_COLS(16, 8, 8)
-#undef RC_WIDE_COLS
-    default:
-      return false;
-  }
-}
-
-constexpr int WIDE_WARPS = 8;
-
-// acc[b][c][j][a][x] = sum_i DT[b][i][a][x] * KW[j][i][c][a][x] (Montgomery).
-// CTA = one 32-position tile x one internal prime a x up to BC jobs that share
-// the key: the jobs' digit transforms for the tile (tiled layout, one
-// contiguous run per job) sit in shared memory, and each warp sweeps limbs j,
-// streaming the key tile kwt[j][a][tile][digit][c][32] (contiguous) once for
-// all BC jobs, with the next digit's key words loaded ahead.  Sums of D
-// products < a^2 stay below a * 2^64 while D < 2^64 / a (folded by Barrett
-// otherwise).  BC is chosen per launch (1, 2, 4 or 8): small groups keep the
-// footprint small so more CTAs stay resident to cover the key stream.
-template <int BC>
-__global__ __launch_bounds__(32 * WIDE_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : 4)) void k_wide_mac(
-    const PrimeConst* pcs, int base, int log_n, int D, int key_digits, int total, const u64* kwt, const u64* dtt,
-    u64* acc, int b0, int nb, u64 chunk) {
-  extern __shared__ u64 dsm[];  // [BC][D][32]
-  const int N = 1 << log_n, tiles = N >> 5;
-  const int xb = blockIdx.x, a = blockIdx.y;
-  const int bstart = b0 + blockIdx.z * BC;
-  const int nloc = min(BC, b0 + nb - bstart);
-  const int run = D * 32;
-  for (int e = threadIdx.x; e < nloc * run; e += 32 * WIDE_WARPS) {
-    const int b = e / run, r = e - b * run;
-    dsm[e] = dtt[(((size_t)(bstart + b) * 2 + a) * tiles + xb) * run + r];
-  }
-  __syncthreads();
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const PrimeConst& pc = pcs[base + a];
-  const size_t krun = (size_t)key_digits * 2 * 32;
-#pragma unroll 1
-  for (int j = warp; j < total; j += WIDE_WARPS) {
-    const u64* kp = kwt + (((size_t)j * 2 + a) * tiles + xb) * krun + lane;
-    U128 s0[BC], s1[BC];
-#pragma unroll
-    for (int b = 0; b < BC; ++b) s0[b].lo = s0[b].hi = s1[b].lo = s1[b].hi = 0;
-    u64 since = 0;
-    u64 n0 = kp[0], n1 = kp[32];
-#pragma unroll 1
-    for (int i = 0; i < D; ++i) {
-      const u64 k0 = n0, k1 = n1;
-      if (i + 1 < D) {
-        n0 = kp[(size_t)(i + 1) * 64];
-        n1 = kp[(size_t)(i + 1) * 64 + 32];
-      }
-#pragma unroll
-      for (int b = 0; b < BC; ++b) {
-        if (b < nloc) {
-          const u64 d = dsm[(b * D + i) * 32 + lane];
-          add_to(s0[b], mul_wide(d, k0));
-          add_to(s1[b], mul_wide(d, k1));
-        }
-      }
-      if (++since == chunk) {
-#pragma unroll
-        for (int b = 0; b < BC; ++b) {
-          s0[b].lo = barrett_reduce(s0[b], pc);
-          s0[b].hi = 0;
-          s1[b].lo = barrett_reduce(s1[b], pc);
-          s1[b].hi = 0;
-        }
-        since = 1;
-      }
-    }
-    const int x = xb * 32 + lane;
-#pragma unroll
-    for (int b = 0; b < BC; ++b) {
-      if (b < nloc) {
-        const size_t jb = (size_t)(bstart + b);
-        acc[(((jb * 2 + 0) * total + j) * 2 + a) * N + x] = mont_reduce(s0[b], pc);
-        acc[(((jb * 2 + 1) * total + j) * 2 + a) * N + x] = mont_reduce(s1[b], pc);
-      }
-    }
-  }
-}
-
-template <int BC>
-void launch_wide_mac(const PrimeConst* pc, int base, int log_n, int D, int key_digits, int total, const u64* kwt,
-                     const u64* dtt, u64* acc, int b0, int nb, u64 chunk, cudaStream_t s) {
-  const size_t smem = (size_t)BC * D * 32 * 8;
-  static size_t configured = 0;
-  if (smem > 48 * 1024 && smem > configured) {
-    cudaFuncSetAttribute(k_wide_mac<BC>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    configured = smem;
-  }
-  dim3 g((1 << log_n) / 32, 2, (nb + BC - 1) / BC);
-  k_wide_mac<BC><<<g, 32 * WIDE_WARPS, smem, s>>>(pc, base, log_n, D, key_digits, total, kwt, dtt, acc, b0, nb,
-                                                  chunk);
-}
-
-// transformed key [limbs][digits][2][2][N] -> tiled [limbs][a][x/32][digits][2][32], Montgomery form
-__global__ void k_wide_key_tile(const PrimeConst* pcs, int base, const u64* src, u64* dst, int digits, int limbs,
-                                int log_n) {
-  const size_t N = (size_t)1 << log_n;
-  const size_t total = (size_t)limbs * digits * 2 * 2 * N;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
-    const size_t lanei = e & 31;
-    size_t r = e >> 5;
-    const int c = (int)(r % 2);
-    r /= 2;
-    const int i = (int)(r % digits);
-    r /= digits;
-    const size_t xb = r % (N >> 5);
-    r /= (N >> 5);
-    const int a = (int)(r % 2);
-    const int j = (int)(r / 2);
-    const size_t x = xb * 32 + lanei;
-    U128 t;
-    t.lo = 0;
-    t.hi = src[((((size_t)j * digits + i) * 2 + c) * 2 + a) * N + x];
-    dst[e] = barrett_reduce(t, pcs[base + a]);  // v * 2^64 mod a
-  }
-}
-
-// coefficient-form key [digits][2][limbs][N] (canonical mod q_j) -> KW[limbs][digits][2][2][N]
-// holding the same integers reduced mod a0, a1
-__global__ void k_wide_key_prep(const PrimeConst* pcs, int base, const u64* src, u64* dst, int digits, int limbs,
-                                int log_n) {
-  const u64 N = 1ull << log_n;
-  const size_t total = (size_t)digits * 2 * limbs * N;
-  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
-    const u64 x = e & (N - 1);
-    size_t r = e >> log_n;
-    const int j = (int)(r % limbs);
-    r /= limbs;
-    const int c = (int)(r % 2);
-    const int i = (int)(r / 2);
-    const u64 v = src[e];
-    for (int a = 0; a < 2; ++a) {
-      U128 t;
-      t.lo = v;
-      t.hi = 0;
-      dst[((((size_t)j * digits + i) * 2 + c) * 2 + a) * N + x] = barrett_reduce(t, pcs[base + a]);
-    }
-  }
-}
-
-// centred S from (r0 mod a0, r1 mod a1), reduced mod the prime t
-__device__ __forceinline__ u64 wide_crt_mod(u64 r0, u64 r1, const WideTab& w, int t, const PrimeConst& c) {
-  // h = (r1 - r0) * a0^-1 mod a1; r0 < a0 < 2 a1
-  u64 r0m = r0 >= w.a1 ? r0 - w.a1 : r0;
-  u64 diff = r1 >= r0m ? r1 - r0m : r1 + w.a1 - r0m;
-  const u64 h = mul_shoup(diff, w.a0inv, w.a0inv_s, w.a1);
-  // S = r0 + a0 * h < A
-  U128 S = mul_wide(w.a0, h);
-  u64 lo = S.lo + r0;
-  S.hi += lo < r0 ? 1ull : 0ull;
-  S.lo = lo;
-  const bool neg = S.hi > w.halfA_hi || (S.hi == w.halfA_hi && S.lo > w.halfA_lo);
-  // S mod t = (r0 mod t) + (a0 mod t) * (h mod t)
-  U128 t0;
-  t0.hi = 0;
-  t0.lo = r0;
-  const u64 r0t = r0 < c.q ? r0 : barrett_reduce(t0, c);
-  t0.lo = h;
-  const u64 ht = h < c.q ? h : barrett_reduce(t0, c);
-  u64 v = add_mod(r0t, mul_shoup(ht, w.a0_mod_t[t], w.a0_mod_t_s[t], c.q), c.q);
-  if (neg) v = sub_mod(v, w.A_mod_t[t], c.q);
-  return v;
-}
-
-// ---------------------------------------------------------------------------
 // finalize: ModDown + addend + rescale
 // ---------------------------------------------------------------------------
 constexpr int KMAX = 8;
@@ -791,13 +558,14 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
   if (x >= N) return;
   const int comp = blockIdx.y & 1, job = blockIdx.y >> 1;
   const int lq = f.qlimbs, K = f.K;
-  const int wf = f.wide ? 2 : 1;  // residues per limb in acc
+  const int wf = f.wide ? 2 : 1;  // 8-byte words per limb and coefficient in acc
   const u64* a = acc + ((size_t)job * 2 + comp) * (size_t)(lq + K) * N * wf;
+  const uint2* a2 = reinterpret_cast<const uint2*>(a);
   const LimbMap fmap{lq, f.L};
   auto accv = [&](int j) -> u64 {  // value of limb j (prime fmap.prime(j)) at x
     if (!f.wide) return a[(size_t)j * N + x];
     const int t = fmap.prime(j);
-    return wide_crt_mod(a[(size_t)j * 2 * N + x], a[((size_t)j * 2 + 1) * N + x], f.wt, t, f.pc[t]);
+    return wide_crt_mod(a2[(size_t)j * 2 * N + x], a2[((size_t)j * 2 + 1) * N + x], f.wt, t, f.pc[t]);
   };
   const u64* add = addend.p[2 * job + comp];
   u64* dst = out.p[2 * job + comp];
@@ -1011,51 +779,6 @@ void key_to_device_form(const NttArgs& a, const PrimeConst* pc, const u64* src, 
   int g = (int)((total + 255) / 256);
   if (g > 65535 * 8) g = 65535 * 8;
   k_key_relayout<<<g, 256, 0, s>>>(pc, src, dst, digits, limbs, map, a.log_n);
-}
-
-bool wide_digit_transforms(const NttArgs& nt, int base, int D, int jobs, const int32_t* digits, u64* work,
-                           u64* dtt, cudaStream_t s) {
-  {
-    ProfScope p("wide_digit_cols", s);
-    const bool ok = nt.lazy ? wide_cols_dispatch<true>(nt, base, D, jobs, digits, work, s)
-                            : wide_cols_dispatch<false>(nt, base, D, jobs, digits, work, s);
-    if (!ok) return false;
-  }
-  // row phase over (job, digit) polynomials of 2 limbs (a0, a1), written tiled
-  const int polys = jobs * D;
-  const int N = 1 << nt.log_n;
-  for (int p0 = 0; p0 < polys; p0 += MAXP) {
-    PtrTab t{};
-    const int cnt = polys - p0 < MAXP ? polys - p0 : MAXP;
-    for (int k = 0; k < cnt; ++k) t.p[k] = work + (size_t)(p0 + k) * 2 * N;
-    ntt_forward_rows_tiled(nt, t, dtt, p0, cnt, D, LimbMap{0, base}, s);
-  }
-  return true;
-}
-
-void wide_mac(const PrimeConst* pc, int base, int log_n, int D, int key_digits, int total, const u64* kwt,
-              const u64* dtt, u64* acc, int b0, int nb, u64 chunk, cudaStream_t s) {
-  ProfScope p("wide_mac", s);
-  if (nb <= 1) launch_wide_mac<1>(pc, base, log_n, D, key_digits, total, kwt, dtt, acc, b0, nb, chunk, s);
-  else if (nb <= 2) launch_wide_mac<2>(pc, base, log_n, D, key_digits, total, kwt, dtt, acc, b0, nb, chunk, s);
-  else if (nb <= 4) launch_wide_mac<4>(pc, base, log_n, D, key_digits, total, kwt, dtt, acc, b0, nb, chunk, s);
-  else launch_wide_mac<8>(pc, base, log_n, D, key_digits, total, kwt, dtt, acc, b0, nb, chunk, s);
-}
-
-void wide_key_prep(const PrimeConst* pc, int base, const u64* src, u64* dst, int digits, int limbs, int log_n,
-                   cudaStream_t s) {
-  const size_t total = (size_t)digits * 2 * limbs << log_n;
-  int g = (int)((total + 255) / 256);
-  if (g > 65535 * 8) g = 65535 * 8;
-  k_wide_key_prep<<<g, 256, 0, s>>>(pc, base, src, dst, digits, limbs, log_n);
-}
-
-void wide_key_tile(const PrimeConst* pc, int base, const u64* src, u64* dst, int digits, int limbs, int log_n,
-                   cudaStream_t s) {
-  const size_t total = (size_t)limbs * digits * 2 * 2 << log_n;
-  int g = (int)((total + 255) / 256);
-  if (g > 65535 * 8) g = 65535 * 8;
-  k_wide_key_tile<<<g, 256, 0, s>>>(pc, base, src, dst, digits, limbs, log_n);
 }
 
 }  // namespace rc

@@ -24,6 +24,11 @@ struct Twiddle {
   u64 ws;  // floor(w * 2^64 / q)
 };
 
+// twiddles of a pair of 32-bit primes (q0, q1) at one index, with Shoup companions floor(w * 2^32 / q)
+struct Tw2 {
+  uint32_t w0, w1, s0, s1;
+};
+
 // Per-prime constants; one entry per prime of the Q u P chain.
 struct PrimeConst {
   u64 q;

@@ -414,66 +414,4 @@ void ntt_forward_rows(const NttArgs& a, const PtrTab& data, int polys, int limbs
   }
 }
 
-namespace {
-// Forward row phase writing "tiled" output for the key product: polynomial p =
-// job * D + digit (2 limbs = the two internal primes) lands at
-// out[((job * 2 + a) * (N / 32) + x / 32) * (D * 32) + digit * 32 + x % 32].
-template <int M1, int M2, bool LAZY>
-__global__ __launch_bounds__(32 * ROW_WARPS) void k_rows_tiled_f(NttArgs a, PtrTab src, u64* out, int p0, int D,
-                                                                 LimbMap map) {
-  using G = core::Geo<M2>;
-  constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = ROW_WARPS * G::SUBS;
-  __shared__ u64 bufs[ROWS * G::STRIDE];
-  __shared__ Twiddle twl[ROWS][N2];
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int sub = lane / G::LANES, l = lane % G::LANES;
-  const int row0 = blockIdx.x * ROWS;
-  const int limb = blockIdx.y, poly = blockIdx.z;
-  const int prime = map.prime(limb);
-  const PrimeConst& pc = a.pc[prime];
-  const Twiddle* twg = a.tw_fwd + (size_t)prime * N;
-#pragma unroll 1
-  for (int rr = 0; rr < ROWS; ++rr)
-    core::stage_twiddles<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * ROW_WARPS);
-  __syncthreads();
-  const int rl = warp * G::SUBS + sub, row = row0 + rl;
-  const u64* in = src.p[poly] + (size_t)limb * N + (size_t)row * N2;
-  u64* buf = bufs + rl * G::STRIDE;
-  u64 v[8];
-#pragma unroll
-  for (int k = 0; k < 8; ++k) v[k] = in[core::first_idx<M2>(l, k)];
-  core::fwd_sub<M2, LAZY>(v, buf, l, twl[rl], pc.q);
-  const int pg = p0 + poly, job = pg / D, digit = pg % D;
-  u64* o = out + ((size_t)job * 2 + limb) * (N / 32) * (size_t)(D * 32) + (size_t)digit * 32;
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const int x = row * N2 + core::last_idx<M2>(l, k);
-    o[(size_t)(x >> 5) * (D * 32) + (x & 31)] = reduce_out<LAZY>(v[k], pc);
-  }
-}
-}  // namespace
-
-void ntt_forward_rows_tiled(const NttArgs& a, const PtrTab& src, u64* out, int p0, int polys, int D, LimbMap map,
-                            cudaStream_t s) {
-  if (polys <= 0) return;
-  ProfScope p("ntt_fwd_rows", s);
-  switch (a.log_n) {
-#define RC_ROWS_T(LN, A, B)                                                                        \
-  case LN: {                                                                                       \
-    dim3 g((1 << A) / (ROW_WARPS * core::Geo<B>::SUBS), 2, polys);                                 \
-    if (a.lazy) k_rows_tiled_f<A, B, true><<<g, 32 * ROW_WARPS, 0, s>>>(a, src, out, p0, D, map);  \
-    else k_rows_tiled_f<A, B, false><<<g, 32 * ROW_WARPS, 0, s>>>(a, src, out, p0, D, map);        \
-    break;                                                                                         \
-  }
-    RC_ROWS_T(12, 6, 6)
-    RC_ROWS_T(13, 6, 7)
-    RC_ROWS_T(14, 7, 7)
-    RC_ROWS_T(15, 7, 8)
-    RC_ROWS_T(16, 8, 8)
-#undef RC_ROWS_T
-    default:
-      break;
-  }
-}
-
 }  // namespace rc

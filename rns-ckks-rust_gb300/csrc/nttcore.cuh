@@ -221,5 +221,109 @@ __device__ __forceinline__ int last_idx(int l, int k) {
   return gidx<M, Last<M>::S0, Last<M>::G>(l, k);
 }
 
+// ---------------------------------------------------------------------------
+// Two 32-bit primes side by side.  The internal primes of the wide key product
+// are below 2^29 and handled in pairs: an element is a uint2 of its residues
+// mod (q0, q1), so a pair occupies the 8 bytes of one 64-bit residue and the
+// shared-memory layouts, swizzles and register counts above carry over
+// unchanged.  Butterflies use 32-bit Shoup multiplication (values < 4q < 2^31).
+// ---------------------------------------------------------------------------
+// x * w mod q in [0, 2q) for any 32-bit x
+__device__ __forceinline__ uint32_t mul_shoup32_lazy(uint32_t x, uint32_t w, uint32_t ws, uint32_t q) {
+  return x * w - __umulhi(x, ws) * q;
+}
+
+template <int M>
+__device__ __forceinline__ void stage_twiddles2(Tw2* local, const Tw2* global, u64 tb, int tid, int nthreads) {
+  for (int t = 1 + tid; t < (1 << M); t += nthreads) {
+    const int s = 31 - __clz(t);
+    const uint4 v = __ldg(reinterpret_cast<const uint4*>(global + ((tb - 1) << s) + t));
+    local[t] = Tw2{v.x, v.y, v.z, v.w};
+  }
+}
+
+template <int M, int GI>
+__device__ __forceinline__ void fwd_group2(uint2 (&v)[8], int l, const Tw2* __restrict__ tw, uint32_t q0,
+                                           uint32_t q1) {
+  constexpr int S0 = Grp<M, GI>::S0, G = Grp<M, GI>::G;
+  const uint32_t t0 = q0 << 1, t1 = q1 << 1;
+#pragma unroll
+  for (int j = 0; j < G; ++j) {
+    const int s = S0 + j;
+    const int b = G - 1 - j;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k & (1 << b)) continue;
+      const int r = gidx<M, S0, G>(l, k);
+      const Tw2 w = tw[(1 << s) + (r >> (M - s))];
+      uint2 x = v[k];
+      const uint2 y = v[k | (1 << b)];
+      x.x = x.x >= t0 ? x.x - t0 : x.x;
+      x.y = x.y >= t1 ? x.y - t1 : x.y;
+      const uint32_t u0 = mul_shoup32_lazy(y.x, w.w0, w.s0, q0);
+      const uint32_t u1 = mul_shoup32_lazy(y.y, w.w1, w.s1, q1);
+      v[k] = make_uint2(x.x + u0, x.y + u1);
+      v[k | (1 << b)] = make_uint2(x.x - u0 + t0, x.y - u1 + t1);
+    }
+  }
+}
+
+template <int M, int GI>
+__device__ __forceinline__ void inv_group2(uint2 (&v)[8], int l, const Tw2* __restrict__ tw, uint32_t q0,
+                                           uint32_t q1) {
+  constexpr int S0 = Grp<M, GI>::S0, G = Grp<M, GI>::G;
+  const uint32_t t0 = q0 << 1, t1 = q1 << 1;
+#pragma unroll
+  for (int j = G - 1; j >= 0; --j) {
+    const int s = S0 + j;
+    const int b = G - 1 - j;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      if (k & (1 << b)) continue;
+      const int r = gidx<M, S0, G>(l, k);
+      const Tw2 w = tw[(1 << s) + (r >> (M - s))];
+      const uint2 x = v[k], y = v[k | (1 << b)];
+      uint32_t a0 = x.x + y.x, a1 = x.y + y.y;
+      a0 = a0 >= t0 ? a0 - t0 : a0;
+      a1 = a1 >= t1 ? a1 - t1 : a1;
+      v[k] = make_uint2(a0, a1);
+      v[k | (1 << b)] = make_uint2(mul_shoup32_lazy(x.x - y.x + t0, w.w0, w.s0, q0),
+                                   mul_shoup32_lazy(x.y - y.y + t1, w.w1, w.s1, q1));
+    }
+  }
+}
+
+template <int M, int GA, int GB>
+__device__ __forceinline__ void exchange2(uint2 (&v)[8], uint2* buf, int l) {
+#pragma unroll
+  for (int k = 0; k < 8; ++k) buf[swz<M>(gidx<M, Grp<M, GA>::S0, Grp<M, GA>::G>(l, k))] = v[k];
+  __syncwarp();
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = buf[swz<M>(gidx<M, Grp<M, GB>::S0, Grp<M, GB>::G>(l, k))];
+  __syncwarp();
+}
+
+template <int M>
+__device__ __forceinline__ void fwd_sub2(uint2 (&v)[8], uint2* buf, int l, const Tw2* tw, uint32_t q0, uint32_t q1) {
+  fwd_group2<M, 0>(v, l, tw, q0, q1);
+  exchange2<M, 0, 1>(v, buf, l);
+  fwd_group2<M, 1>(v, l, tw, q0, q1);
+  if constexpr (NGroups<M>::value == 3) {
+    exchange2<M, 1, 2>(v, buf, l);
+    fwd_group2<M, 2>(v, l, tw, q0, q1);
+  }
+}
+
+template <int M>
+__device__ __forceinline__ void inv_sub2(uint2 (&v)[8], uint2* buf, int l, const Tw2* tw, uint32_t q0, uint32_t q1) {
+  if constexpr (NGroups<M>::value == 3) {
+    inv_group2<M, 2>(v, l, tw, q0, q1);
+    exchange2<M, 2, 1>(v, buf, l);
+  }
+  inv_group2<M, 1>(v, l, tw, q0, q1);
+  exchange2<M, 1, 0>(v, buf, l);
+  inv_group2<M, 0>(v, l, tw, q0, q1);
+}
+
 }  // namespace core
 }  // namespace rc

@@ -1,0 +1,433 @@
+// Exact integer key product ("wide-CRT") for the hybrid and Q-only keyswitch.
+//
+// The reference forms sum_i d_i * k_ij mod q_j for every limb j of the key
+// (src/rns/keyswitching.rs:130-194): D digit polynomials times D key
+// polynomials per limb.  Because the balanced digits satisfy |d_i| <= 2^29 and
+// the key residues 0 <= k_ij < q_j, the negacyclic convolution
+// S_j = sum_i d_i * k_ij has integer coefficients bounded by
+// D * N * 2^29 * (q_j - 1).  Here S_j is computed exactly under four internal
+// primes w0..w3 < 2^29 (A = w0 w1 w2 w3 > 4 * bound, checked on the host) and
+// turned back into S_j mod q_j by CRT in the finalize pass, which gives the
+// reference's residues bit for bit.  The digits are transformed once per
+// internal prime (4 D transforms instead of D (l + K)), and the key product is
+// one 32 x 32 -> 64-bit multiply-add per term.
+//
+// The primes are handled in pairs (w0, w1), (w2, w3): an element is a uint2
+// of its two residues, which keeps the 8-byte element layouts and swizzles of
+// the 64-bit transforms (nttcore.cuh).  Layouts (uint2 elements):
+//   digit transforms, tiled:  dtt[job][pair][x/32][digit][32]
+//   key, tiled:               kwt[limb][pair][x/32][digit][c][32]
+//   products:                 acc[job][c][limb][pair][N]
+#include "kernels.cuh"
+#include "nttcore.cuh"
+#include "wide.cuh"
+
+namespace rc {
+namespace {
+
+constexpr int W_ROW_WARPS = 4;
+constexpr int W_MAC_WARPS = 8;
+
+template <int M>
+struct WColTile {
+  static constexpr int COLS = (8 * core::Geo<M>::SUBS) > 16 ? 8 * core::Geo<M>::SUBS : 16;
+};
+
+__device__ __forceinline__ uint2 reduce4(uint2 v, uint32_t q0, uint32_t q1) {
+  uint32_t a = v.x >= 2 * q0 ? v.x - 2 * q0 : v.x;
+  uint32_t b = v.y >= 2 * q1 ? v.y - 2 * q1 : v.y;
+  return make_uint2(fold32(a, q0), fold32(b, q1));
+}
+
+// Forward column phase of polynomial p0 + blockIdx.z under pair blockIdx.y.
+// SRC 0: int32 digits[poly][N], taken as d + 2q (in [0, 4q) since 2q > 2^29);
+// SRC 1: residues src[poly][pair][N].  Output out[poly][pair][N].
+template <int M1, int M2, int SRC>
+__global__ __launch_bounds__(256, 2) void k_w_cols_fwd(WidePrimes w, const void* src, uint2* out, int p0) {
+  using G = core::Geo<M1>;
+  constexpr int COLS = WColTile<M1>::COLS, N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2;
+  __shared__ uint2 tile[COLS * G::STRIDE];
+  __shared__ Tw2 twl[N1];
+  const int c0 = blockIdx.x * COLS;
+  const int pair = blockIdx.y;
+  const size_t poly = (size_t)p0 + blockIdx.z;
+  const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
+  core::stage_twiddles2<M1>(twl, w.tw_fwd + (size_t)pair * N, 1, threadIdx.x, 256);
+#pragma unroll 4
+  for (int it = 0; it < N1 * COLS / 256; ++it) {
+    const int idx = it * 256 + threadIdx.x;
+    const int r = idx / COLS, c = idx % COLS;
+    uint2 v;
+    if (SRC == 0) {
+      const int32_t d = static_cast<const int32_t*>(src)[poly * N + (size_t)r * N2 + c0 + c];
+      v = make_uint2((uint32_t)(d + (int32_t)(2 * q0)), (uint32_t)(d + (int32_t)(2 * q1)));
+    } else {
+      v = static_cast<const uint2*>(src)[(poly * 2 + pair) * N + (size_t)r * N2 + c0 + c];
+    }
+    tile[c * G::STRIDE + core::swz<M1>(r)] = v;
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5;
+#pragma unroll 1
+  for (int cb = warp * G::SUBS; cb < COLS; cb += 8 * G::SUBS) {
+    const int lv = core::lane_id_volatile();
+    const int sub = lv / G::LANES, l = lv % G::LANES;
+    uint2* buf = tile + (cb + sub) * G::STRIDE;
+    uint2 v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::first_idx<M1>(l, k))];
+    __syncwarp();
+    core::fwd_sub2<M1>(v, buf, l, twl, q0, q1);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::last_idx<M1>(l, k))] = v[k];
+  }
+  __syncthreads();
+  uint2* o = out + (poly * 2 + pair) * N;
+#pragma unroll 4
+  for (int it = 0; it < N1 * COLS / 256; ++it) {
+    const int idx = it * 256 + threadIdx.x;
+    const int r = idx / COLS, c = idx % COLS;
+    o[(size_t)r * N2 + c0 + c] = tile[c * G::STRIDE + core::swz<M1>(r)];
+  }
+}
+
+// Forward row phase of data[poly][pair][N] (poly = p0 + blockIdx.z), outputs
+// reduced to [0, q).  TILED: written as dtt[job][pair][x/32][digit][32] with
+// poly = job * D + digit; otherwise in place.
+template <int M1, int M2, bool TILED>
+__global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_fwd(WidePrimes w, uint2* data, uint2* dtt, int p0,
+                                                                 int D) {
+  using G = core::Geo<M2>;
+  constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = W_ROW_WARPS * G::SUBS;
+  __shared__ uint2 bufs[ROWS * G::STRIDE];
+  __shared__ Tw2 twl[ROWS][N2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / G::LANES, l = lane % G::LANES;
+  const int row0 = blockIdx.x * ROWS;
+  const int pair = blockIdx.y;
+  const size_t poly = (size_t)p0 + blockIdx.z;
+  const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
+  const Tw2* twg = w.tw_fwd + (size_t)pair * N;
+#pragma unroll 1
+  for (int rr = 0; rr < ROWS; ++rr)
+    core::stage_twiddles2<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * W_ROW_WARPS);
+  __syncthreads();
+  const int rl = warp * G::SUBS + sub, row = row0 + rl;
+  uint2* in = data + (poly * 2 + pair) * N + (size_t)row * N2;
+  uint2* buf = bufs + rl * G::STRIDE;
+  uint2 v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = in[core::first_idx<M2>(l, k)];
+  core::fwd_sub2<M2>(v, buf, l, twl[rl], q0, q1);
+  if (TILED) {
+    const size_t job = poly / D, digit = poly % D;
+    uint2* o = dtt + (job * 2 + pair) * (N / 32) * (size_t)(D * 32) + digit * 32;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int x = row * N2 + core::last_idx<M2>(l, k);
+      o[(size_t)(x >> 5) * (D * 32) + (x & 31)] = reduce4(v[k], q0, q1);
+    }
+  } else {
+#pragma unroll
+    for (int k = 0; k < 8; ++k) in[core::last_idx<M2>(l, k)] = reduce4(v[k], q0, q1);
+  }
+}
+
+// Inverse row phase, in place on data[poly][pair][N]; inputs in [0, 2q).
+template <int M1, int M2>
+__global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_inv(WidePrimes w, uint2* data) {
+  using G = core::Geo<M2>;
+  constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = W_ROW_WARPS * G::SUBS;
+  __shared__ uint2 bufs[ROWS * G::STRIDE];
+  __shared__ Tw2 twl[ROWS][N2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / G::LANES, l = lane % G::LANES;
+  const int row0 = blockIdx.x * ROWS;
+  const int pair = blockIdx.y;
+  const size_t poly = blockIdx.z;
+  const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
+  const Tw2* twg = w.tw_inv + (size_t)pair * N;
+#pragma unroll 1
+  for (int rr = 0; rr < ROWS; ++rr)
+    core::stage_twiddles2<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * W_ROW_WARPS);
+  __syncthreads();
+  const int rl = warp * G::SUBS + sub, row = row0 + rl;
+  uint2* in = data + (poly * 2 + pair) * N + (size_t)row * N2;
+  uint2* buf = bufs + rl * G::STRIDE;
+  uint2 v[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) v[k] = in[core::last_idx<M2>(l, k)];
+  core::inv_sub2<M2>(v, buf, l, twl[rl], q0, q1);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) in[core::first_idx<M2>(l, k)] = v[k];
+}
+
+// Inverse column phase, in place, times N^-1: outputs in [0, q).
+template <int M1, int M2>
+__global__ __launch_bounds__(256, 2) void k_w_cols_inv(WidePrimes w, uint2* data) {
+  using G = core::Geo<M1>;
+  constexpr int COLS = WColTile<M1>::COLS, N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2;
+  __shared__ uint2 tile[COLS * G::STRIDE];
+  __shared__ Tw2 twl[N1];
+  const int c0 = blockIdx.x * COLS;
+  const int pair = blockIdx.y;
+  const size_t poly = blockIdx.z;
+  const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
+  core::stage_twiddles2<M1>(twl, w.tw_inv + (size_t)pair * N, 1, threadIdx.x, 256);
+  uint2* io = data + (poly * 2 + pair) * N;
+#pragma unroll 4
+  for (int it = 0; it < N1 * COLS / 256; ++it) {
+    const int idx = it * 256 + threadIdx.x;
+    const int r = idx / COLS, c = idx % COLS;
+    tile[c * G::STRIDE + core::swz<M1>(r)] = io[(size_t)r * N2 + c0 + c];
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5;
+#pragma unroll 1
+  for (int cb = warp * G::SUBS; cb < COLS; cb += 8 * G::SUBS) {
+    const int lv = core::lane_id_volatile();
+    const int sub = lv / G::LANES, l = lv % G::LANES;
+    uint2* buf = tile + (cb + sub) * G::STRIDE;
+    uint2 v[8];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::last_idx<M1>(l, k))];
+    __syncwarp();
+    core::inv_sub2<M1>(v, buf, l, twl, q0, q1);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::first_idx<M1>(l, k))] = v[k];
+  }
+  __syncthreads();
+  const uint32_t n0 = w.n_inv[2 * pair], n0s = w.n_inv_s[2 * pair];
+  const uint32_t n1 = w.n_inv[2 * pair + 1], n1s = w.n_inv_s[2 * pair + 1];
+#pragma unroll 4
+  for (int it = 0; it < N1 * COLS / 256; ++it) {
+    const int idx = it * 256 + threadIdx.x;
+    const int r = idx / COLS, c = idx % COLS;
+    const uint2 x = tile[c * G::STRIDE + core::swz<M1>(r)];
+    io[(size_t)r * N2 + c0 + c] = make_uint2(mul_shoup32(x.x, n0, n0s, q0), mul_shoup32(x.y, n1, n1s, q1));
+  }
+}
+
+// acc[b][c][j][pair][x] = sum_i DT[b][pair][x][i] * KW[j][pair][x][i][c] for
+// BC jobs sharing a key.  CTA = one 32-position tile x one pair x up to BC
+// jobs: the jobs' digit transforms for the tile sit in shared memory, each warp
+// sweeps limbs j and streams the key tile (one contiguous run per limb and
+// pair) once for all BC jobs, the next digit's key words loaded ahead.  Terms
+// are < 2^58, so 64 of them fit a 64-bit sum; longer sums (FOLD, D > 64) are
+// folded every 64 terms.
+template <int BC, bool FOLD>
+__global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : 4)) void k_w_mac(
+    WidePrimes w, int D, int key_digits, int total, const uint2* __restrict__ kwt, const uint2* __restrict__ dtt,
+    uint2* acc, int b0, int nb) {
+  extern __shared__ uint2 dsm[];  // [BC][D][32]
+  const int N = 1 << w.log_n, tiles = N >> 5;
+  const int xb = blockIdx.x, pair = blockIdx.y;
+  const int bstart = b0 + blockIdx.z * BC;
+  const int nloc = min(BC, b0 + nb - bstart);
+  const int run = D * 32;
+  for (int e = threadIdx.x; e < BC * run; e += 32 * W_MAC_WARPS) {  // jobs past nloc read as zero
+    const int b = e / run, r = e - b * run;
+    dsm[e] = b < nloc ? dtt[(((size_t)(bstart + b) * 2 + pair) * tiles + xb) * run + r] : make_uint2(0, 0);
+  }
+  __syncthreads();
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
+  const u64 bar0 = w.bar[2 * pair], bar1 = w.bar[2 * pair + 1];
+  const size_t krun = (size_t)key_digits * 2 * 32;
+#pragma unroll 1
+  for (int j = warp; j < total; j += W_MAC_WARPS) {
+    const uint2* kp = kwt + (((size_t)j * 2 + pair) * tiles + xb) * krun + lane;
+    u64 a0[BC], a1[BC], c0[BC], c1[BC];
+#pragma unroll
+    for (int b = 0; b < BC; ++b) a0[b] = a1[b] = c0[b] = c1[b] = 0;
+    uint2 n0 = kp[0], n1 = kp[32];
+#pragma unroll 1
+    for (int i0 = 0; i0 < D; i0 += FOLD ? 64 : D) {
+      const int i1 = FOLD ? min(D, i0 + 64) : D;
+      if (FOLD && i0 > 0) {  // fold: the next 64 terms then stay below 2^64
+#pragma unroll
+        for (int b = 0; b < BC; ++b) {
+          a0[b] = reduce64_32(a0[b], q0, bar0);
+          a1[b] = reduce64_32(a1[b], q1, bar1);
+          c0[b] = reduce64_32(c0[b], q0, bar0);
+          c1[b] = reduce64_32(c1[b], q1, bar1);
+        }
+      }
+#pragma unroll 1
+      for (int i = i0; i < i1; ++i) {
+        const uint2 k0 = n0, k1 = n1;
+        if (i + 1 < D) {
+          n0 = kp[(size_t)(i + 1) * 64];
+          n1 = kp[(size_t)(i + 1) * 64 + 32];
+        }
+        const uint2* dp = dsm + i * 32 + lane;
+#pragma unroll
+        for (int b = 0; b < BC; ++b) {
+          const uint2 d = dp[b * run];
+          a0[b] += (u64)d.x * k0.x;
+          a1[b] += (u64)d.y * k0.y;
+          c0[b] += (u64)d.x * k1.x;
+          c1[b] += (u64)d.y * k1.y;
+        }
+      }
+    }
+    const int x = xb * 32 + lane;
+#pragma unroll
+    for (int b = 0; b < BC; ++b) {
+      if (b < nloc) {
+        const size_t jb = (size_t)(bstart + b);
+        acc[(((jb * 2 + 0) * total + j) * 2 + pair) * N + x] =
+            make_uint2(reduce64_32(a0[b], q0, bar0), reduce64_32(a1[b], q1, bar1));
+        acc[(((jb * 2 + 1) * total + j) * 2 + pair) * N + x] =
+            make_uint2(reduce64_32(c0[b], q0, bar0), reduce64_32(c1[b], q1, bar1));
+      }
+    }
+  }
+}
+
+template <int BC, bool FOLD>
+void launch_w_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt,
+                  uint2* acc, int b0, int nb, cudaStream_t s) {
+  const size_t smem = (size_t)BC * D * 32 * sizeof(uint2);
+  static size_t configured = 0;
+  if (smem > 48 * 1024 && smem > configured) {
+    cudaFuncSetAttribute(k_w_mac<BC, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    configured = smem;
+  }
+  dim3 g((1 << w.log_n) / 32, 2, (nb + BC - 1) / BC);
+  k_w_mac<BC, FOLD><<<g, 32 * W_MAC_WARPS, smem, s>>>(w, D, key_digits, total, kwt, dtt, acc, b0, nb);
+}
+
+// coefficient-form key [digits][2][limbs][N] -> kw[((j * digits + i) * 2 + c)][pair][N]
+__global__ void k_w_key_prep(WidePrimes w, const u64* src, uint2* dst, int digits, int limbs) {
+  const u64 N = 1ull << w.log_n;
+  const size_t total = (size_t)digits * 2 * limbs * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const u64 x = e & (N - 1);
+    size_t r = e >> w.log_n;
+    const int j = (int)(r % limbs);
+    r /= limbs;
+    const int c = (int)(r % 2);
+    const int i = (int)(r / 2);
+    const u64 v = src[e];
+    const size_t poly = ((size_t)j * digits + i) * 2 + c;
+#pragma unroll
+    for (int p = 0; p < 2; ++p)
+      dst[(poly * 2 + p) * N + x] =
+          make_uint2(reduce64_32(v, w.q[2 * p], w.bar[2 * p]), reduce64_32(v, w.q[2 * p + 1], w.bar[2 * p + 1]));
+  }
+}
+
+// transformed kw[((j * digits + i) * 2 + c)][pair][N] -> kwt[j][pair][x/32][i][c][32]
+__global__ void k_w_key_tile(const uint2* src, uint2* dst, int digits, int limbs, int log_n) {
+  const size_t N = (size_t)1 << log_n;
+  const size_t total = (size_t)limbs * 2 * digits * 2 * N;
+  for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
+    const size_t lanei = e & 31;
+    size_t r = e >> 5;
+    const int c = (int)(r % 2);
+    r /= 2;
+    const int i = (int)(r % digits);
+    r /= digits;
+    const size_t xb = r % (N >> 5);
+    r /= (N >> 5);
+    const int p = (int)(r % 2);
+    const int j = (int)(r / 2);
+    dst[e] = src[((((size_t)j * digits + i) * 2 + c) * 2 + p) * N + xb * 32 + lanei];
+  }
+}
+
+int grid_for_elems(size_t total) {
+  size_t g = (total + 255) / 256;
+  return (int)(g > 65535 * 8 ? 65535 * 8 : g);
+}
+
+// forward transforms of polys [p0, p0 + count) of data[poly][pair][N]; SRC as in k_w_cols_fwd
+template <int M1, int M2, int SRC, bool TILED>
+void w_forward(const WidePrimes& w, const void* src, uint2* work, uint2* dtt, int polys, int D, cudaStream_t s) {
+  constexpr int N1 = 1 << M1, N2 = 1 << M2;
+  for (int p0 = 0; p0 < polys; p0 += 65535) {
+    const int cnt = polys - p0 < 65535 ? polys - p0 : 65535;
+    k_w_cols_fwd<M1, M2, SRC><<<dim3(N2 / WColTile<M1>::COLS, 2, cnt), 256, 0, s>>>(w, src, work, p0);
+    k_w_rows_fwd<M1, M2, TILED>
+        <<<dim3(N1 / (W_ROW_WARPS * core::Geo<M2>::SUBS), 2, cnt), 32 * W_ROW_WARPS, 0, s>>>(w, work, dtt, p0, D);
+  }
+}
+
+template <int SRC, bool TILED>
+bool w_forward_dispatch(const WidePrimes& w, const void* src, uint2* work, uint2* dtt, int polys, int D,
+                        cudaStream_t s) {
+  switch (w.log_n) {
+    case 12: w_forward<6, 6, SRC, TILED>(w, src, work, dtt, polys, D, s); return true;
+    case 13: w_forward<6, 7, SRC, TILED>(w, src, work, dtt, polys, D, s); return true;
+    case 14: w_forward<7, 7, SRC, TILED>(w, src, work, dtt, polys, D, s); return true;
+    case 15: w_forward<7, 8, SRC, TILED>(w, src, work, dtt, polys, D, s); return true;
+    case 16: w_forward<8, 8, SRC, TILED>(w, src, work, dtt, polys, D, s); return true;
+    default: return false;
+  }
+}
+
+template <int M1, int M2>
+void w_inverse(const WidePrimes& w, uint2* data, int polys, cudaStream_t s) {
+  constexpr int N1 = 1 << M1, N2 = 1 << M2;
+  for (int p0 = 0; p0 < polys; p0 += 65535) {
+    const int cnt = polys - p0 < 65535 ? polys - p0 : 65535;
+    uint2* d = data + (size_t)p0 * 2 * (N1 * N2);
+    {
+      ProfScope p("wide_inv_rows", s);
+      k_w_rows_inv<M1, M2>
+          <<<dim3(N1 / (W_ROW_WARPS * core::Geo<M2>::SUBS), 2, cnt), 32 * W_ROW_WARPS, 0, s>>>(w, d);
+    }
+    {
+      ProfScope p("wide_inv_cols", s);
+      k_w_cols_inv<M1, M2><<<dim3(N2 / WColTile<M1>::COLS, 2, cnt), 256, 0, s>>>(w, d);
+    }
+  }
+}
+
+}  // namespace
+
+bool wide_digit_transforms(const WidePrimes& w, int D, int jobs, const int32_t* digits, uint2* work, uint2* dtt,
+                           cudaStream_t s) {
+  ProfScope p("wide_digit_ntt", s);
+  return w_forward_dispatch<0, true>(w, digits, work, dtt, jobs * D, D, s);
+}
+
+void wide_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt, uint2* acc,
+              int b0, int nb, cudaStream_t s) {
+  ProfScope p("wide_mac", s);
+  if (D > 64) {  // folded sums; at most 4 jobs per CTA keep the fold within the register budget
+    if (nb <= 1) launch_w_mac<1, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
+    else if (nb <= 2) launch_w_mac<2, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
+    else launch_w_mac<4, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
+    return;
+  }
+  if (nb <= 1) launch_w_mac<1, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
+  else if (nb <= 2) launch_w_mac<2, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
+  else if (nb <= 4) launch_w_mac<4, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
+  else launch_w_mac<8, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
+}
+
+bool wide_inverse(const WidePrimes& w, uint2* data, int polys, cudaStream_t s) {
+  switch (w.log_n) {
+    case 12: w_inverse<6, 6>(w, data, polys, s); return true;
+    case 13: w_inverse<6, 7>(w, data, polys, s); return true;
+    case 14: w_inverse<7, 7>(w, data, polys, s); return true;
+    case 15: w_inverse<7, 8>(w, data, polys, s); return true;
+    case 16: w_inverse<8, 8>(w, data, polys, s); return true;
+    default: return false;
+  }
+}
+
+bool wide_key_build(const WidePrimes& w, const u64* key, int digits, int limbs, uint2* tmp, uint2* kwt,
+                    cudaStream_t s) {
+  const size_t N = (size_t)1 << w.log_n;
+  const int polys = digits * 2 * limbs;
+  k_w_key_prep<<<grid_for_elems((size_t)polys * N), 256, 0, s>>>(w, key, tmp, digits, limbs);
+  // forward transforms in place (the column phase reads tmp and writes tmp)
+  if (!w_forward_dispatch<1, false>(w, tmp, tmp, nullptr, polys, 1, s)) return false;
+  k_w_key_tile<<<grid_for_elems((size_t)polys * 2 * N), 256, 0, s>>>(tmp, kwt, digits, limbs, w.log_n);
+  return true;
+}
+
+}  // namespace rc
