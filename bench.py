@@ -198,7 +198,7 @@ def cpu_oracle_op(O, params, lhs_np, rhs_np, key_np, threads: int):
 
 
 # ciphertexts that share one key read inside the batched entry point (jobs per key-product launch)
-JOBS_PER_LAUNCH = 16
+JOBS_PER_LAUNCH = 32
 
 
 # algorithmic bytes per launch for the kernels the roofline may name
@@ -317,6 +317,17 @@ def run_gpu(args):
     torch.cuda.synchronize()
     per_op_ms = [a.elapsed_time(b) for a, b in evs]
     per_op_value = B / (t_total0.elapsed_time(t_total1) / 1e3)
+    # kernel split of the per-op path (a separate pass with the library's event profiler on)
+    lib.rc_profile_enable(1)
+    lib.rc_profile_report(buf, len(buf))  # reset
+    for i in range(min(B, 8)):
+        C.call("rc_mult_relinearized", ctx.handle, ctypes.byref(L[i]), ctypes.byref(R[i]), key.handle,
+               ctypes.byref(per_op_outs[i]), s_ptr)
+    torch.cuda.synchronize()
+    lib.rc_profile_report(buf, len(buf))
+    lib.rc_profile_enable(0)
+    per_op_prof = json.loads(buf.value.decode())
+    n_prof = min(B, 8)
 
     # ---- e2e through the host-buffer entry point (pinned host memory) ----
     host_l = [torch.empty((2, limbs, n), dtype=torch.int64, pin_memory=True) for _ in range(B)]
@@ -364,7 +375,9 @@ def run_gpu(args):
                          % ((B * 4 * limbs + digits * 2 * (limbs + aux)) * n * 8 / 1e9)},
         "per_op": {"value": round(per_op_value, 3), "unit": UNIT,
                    "p50_ms": round(float(np.percentile(per_op_ms, 50)), 4),
-                   "p99_ms": round(float(np.percentile(per_op_ms, 99)), 4)},
+                   "p99_ms": round(float(np.percentile(per_op_ms, 99)), 4),
+                   "kernels_ms_per_op": {k: round(v["ms"] / n_prof, 4)
+                                         for k, v in sorted(per_op_prof.items(), key=lambda kv: -kv[1]["ms"])}},
         "batched_vs_per_op": round(value / world / per_op_value, 3),
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h},
         "gpu_launches": int(sum(v["launches"] for v in prof.values())),
@@ -501,7 +514,7 @@ def mixed_level_relin(C, ctx, params, O, seed, count=128, reps=3):
     res = {"jobs": count, "limbs": "uniform 8..24", "levels_distinct": len(keys),
            "key_bytes_standard_form": int(sum(ctx.decomp_digits(lv) * 2 * (lv + 1 + len(p)) * n * 8 for lv in keys))}
     with torch.cuda.stream(side):
-        ctx.reserve(max(levels), 16)
+        ctx.reserve(max(levels), 32)
         outs = [torch.empty((2, lv, n), dtype=torch.int64, device="cuda") for lv in levels]
         ctx.relinearize_rescale_batch(quads, ks, outs)  # warm
         graph = ctx.capture_graph(lambda: ctx.relinearize_rescale_batch(quads, ks, outs))

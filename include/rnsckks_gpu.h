@@ -189,7 +189,7 @@ int rc_rotate_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* ct, co
                     rc_ciphertext* out, void* stream);
 /* relinearize then rescale (context/ops.rs:111-122 followed by context/ops.rs:32-37) for `count`
  * quadratic ciphertexts of any mix of levels; the rescale is fused into the keyswitch's last pass.  out[i]
- * gets level - 1 and the rescaled scale.  After rc_reserve(ctx, top level, 16, stream) the call allocates
+ * gets level - 1 and the rescaled scale.  After rc_reserve(ctx, top level, 32, stream) the call allocates
  * nothing and can be captured in a CUDA graph. */
 int rc_relinearize_rescale_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* quadratic,
                                  const rc_ksk* const* keys, rc_ciphertext* out, void* stream);

@@ -371,10 +371,13 @@ uint64_t galois_inverse(const rc_context* c, uint64_t g) {
   return invmod_h(g % m, m);
 }
 
+// mult_relinearized on J jobs: the tensor runs in chunks of MAXP/4 jobs (four pointer-table entries each),
+// the keyswitch on all J <= MAXP/2 jobs at once so that one key read serves them all
 size_t mult_relin_ws_bytes(const rc_context* c, int J, int limbs, const rc_ksk* k0) {
   const int K = k0 && k0->aux ? c->K : 0;
   const size_t pl = (size_t)limbs * c->N;
-  return align_up(std::max(ks_ws_bytes(c, J, limbs, K, ks_digits(c, k0, limbs)), tensor_ws_bytes(c, J, limbs)),
+  return align_up(std::max(ks_ws_bytes(c, J, limbs, K, ks_digits(c, k0, limbs)),
+                           tensor_ws_bytes(c, std::min(J, MAXP / 4), limbs)),
                   256) +
          arena_size_u64((size_t)3 * J * pl) + 256;
 }
@@ -387,26 +390,34 @@ void mult_relin_group(rc_context* c, const std::vector<int>& idx, const rc_ciphe
   const int limbs = lhs[idx[0]].level + 1;
   require(limbs > 1, "rescale requires at least two levels");
   const size_t pl = (size_t)limbs * c->N;
-  const int CH = MAXP / 4;
+  const int CH = MAXP / 2;
   for (size_t b = 0; b < idx.size(); b += CH) {
     const int J = (int)std::min<size_t>(CH, idx.size() - b);
-    std::vector<const uint64_t*> Lp(J), Rp(J);
     std::vector<KsJob> jobs(J);
     for (int j = 0; j < J; ++j) {
-      Lp[j] = lhs[idx[b + j]].data;
-      Rp[j] = rhs[idx[b + j]].data;
       require(keys[idx[b + j]] != nullptr, "keyswitch key must not be null");
       check_key_for(c, keys[idx[b + j]], limbs);
     }
     const rc_ksk* k0 = keys[idx[b]];
     const int K = k0->aux ? c->K : 0;
-    const size_t head = align_up(
-        std::max(ks_ws_bytes(c, J, limbs, K, ks_digits(c, k0, limbs)), tensor_ws_bytes(c, J, limbs)), 256);
+    const size_t head = align_up(std::max(ks_ws_bytes(c, J, limbs, K, ks_digits(c, k0, limbs)),
+                                          tensor_ws_bytes(c, std::min(J, MAXP / 4), limbs)),
+                                 256);
     char* ws = (char*)ws_device(c, s, mult_relin_ws_bytes(c, J, limbs, k0));
     uint64_t* quad = (uint64_t*)(ws + head);
     std::vector<uint64_t*> Q(J);
     for (int j = 0; j < J; ++j) Q[j] = quad + (size_t)j * 3 * pl;
-    tensor_core(c, Lp, Rp, Q, limbs, ws, s);
+    for (int t0 = 0; t0 < J; t0 += MAXP / 4) {
+      const int T = std::min(J - t0, MAXP / 4);
+      std::vector<const uint64_t*> Lp(T), Rp(T);
+      std::vector<uint64_t*> Qt(T);
+      for (int j = 0; j < T; ++j) {
+        Lp[j] = lhs[idx[b + t0 + j]].data;
+        Rp[j] = rhs[idx[b + t0 + j]].data;
+        Qt[j] = Q[t0 + j];
+      }
+      tensor_core(c, Lp, Rp, Qt, limbs, ws, s);
+    }
     for (int j = 0; j < J; ++j) {
       const int i = idx[b + j];
       jobs[j].poly = Q[j] + 2 * pl;
@@ -770,10 +781,11 @@ extern "C" int rc_reserve(rc_context* c, int32_t max_level, uint32_t max_batch, 
     require(c != nullptr, "context must not be null");
     const int limbs = max_level + 1;
     const LevelInfo& li = level_info(c, limbs);
-    const int J = (int)std::min<uint32_t>(max_batch ? max_batch : 1, MAXP / 4);
+    const int J = (int)std::min<uint32_t>(max_batch ? max_batch : 1, MAXP / 2);
     const int D = li.digits + 4;
     const size_t pl = (size_t)limbs * c->N;
-    size_t need = align_up(std::max(ks_ws_bytes(c, J, limbs, c->K, D), tensor_ws_bytes(c, J, limbs)), 256) +
+    size_t need = align_up(std::max(ks_ws_bytes(c, J, limbs, c->K, D), tensor_ws_bytes(c, std::min(J, MAXP / 4), limbs)),
+                           256) +
                   arena_size_u64((size_t)3 * J * pl) + 256;
     ws_device(c, S(stream), need);
   });
@@ -1306,15 +1318,15 @@ extern "C" int rc_relinearize_rescale_batch(rc_context* c, uint32_t count, const
       require(keys[i] != nullptr, "keyswitch key must not be null");
       groups[{qct[i].level, {(int)keys[i]->aux, (int)keys[i]->digits}}].push_back((int)i);
     }
-    // groups run from the highest level down, each in chunks of at most MAXP/4 jobs (the size rc_reserve
+    // groups run from the highest level down, each in chunks of at most MAXP/2 jobs (the size rc_reserve
     // provisions), so one reserve of the top level covers a whole mixed-level batch under graph capture
     for (auto g = groups.rbegin(); g != groups.rend(); ++g) {
       const int limbs = g->first.first + 1;
       const size_t pl = (size_t)limbs * c->N, po = (size_t)(limbs - 1) * c->N;
       const int drop = floor_log2(c->mod[limbs - 1]);
-      for (size_t b = 0; b < g->second.size(); b += MAXP / 4) {
+      for (size_t b = 0; b < g->second.size(); b += MAXP / 2) {
         std::vector<KsJob> jobs;
-        for (size_t k = b; k < g->second.size() && k < b + MAXP / 4; ++k) {
+        for (size_t k = b; k < g->second.size() && k < b + MAXP / 2; ++k) {
           const int i = g->second[k];
           jobs.push_back(KsJob{qct[i].data + 2 * pl, keys[i], qct[i].data, qct[i].data + pl, out[i].data,
                                out[i].data + po});

@@ -590,10 +590,7 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
 #pragma unroll
         for (int t = 0; t < KMAX; ++t) {
           if (t < k) {
-            U128 vt;
-            vt.lo = v[t];
-            vt.hi = 0;
-            u64 vr = v[t] < pk.q ? v[t] : barrett_reduce(vt, pk);
+            const u64 vr = v[t] < pk.q ? v[t] : mul_shoup(v[t], 1, pk.one_s, pk.q);
             val = sub_mod(val, vr, pk.q);
             val = mul_shoup(val, f.md.p_garner[k * K + t], f.md.p_garner_s[k * K + t], pk.q);
           }
@@ -636,21 +633,15 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
     u64 val = accv(i);
     if (K > 0) {
       // centred [x]_P mod q_i
-      U128 s;
-      s.lo = 0;
-      s.hi = 0;
+      // Shoup's product is exact for any 64-bit multiplicand, so v[k] (< p_k) needs no reduction mod q_i
+      u64 conv = 0;
 #pragma unroll
       for (int k = 0; k < KMAX; ++k) {
         if (k < K) {
-          U128 vt;
-          vt.lo = v[k];
-          vt.hi = 0;
-          u64 vr = v[k] < c.q ? v[k] : barrett_reduce(vt, c);
-          u64 t = mul_shoup(vr, f.md.mk[(size_t)i * K + k], f.md.mk_s[(size_t)i * K + k], c.q);
-          s.lo = add_mod(s.lo, t, c.q);
+          const u64 t = mul_shoup(v[k], f.md.mk[(size_t)i * K + k], f.md.mk_s[(size_t)i * K + k], c.q);
+          conv = add_mod(conv, t, c.q);
         }
       }
-      u64 conv = s.lo;
       if (pneg) conv = sub_mod(conv, f.md.pmod[i], c.q);
       val = sub_mod(val, conv, c.q);
       val = mul_shoup(val, f.md.pinv[i], f.md.pinv_s[i], c.q);
@@ -715,9 +706,12 @@ void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int
   dim3 g((N + threads - 1) / threads, jobs);
   const int W = dt.W;
   ProfScope p("decompose", s);
+  // the word count is a template parameter (register-resident value); the closest instance above W runs
   if (W <= 4) k_decompose<4><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
   else if (W <= 8) k_decompose<8><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  else if (W <= 12) k_decompose<12><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
   else if (W <= 16) k_decompose<16><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  else if (W <= 20) k_decompose<20><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
   else if (W <= 24) k_decompose<24><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
   else if (W <= 32) k_decompose<32><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
   else k_decompose<64><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);

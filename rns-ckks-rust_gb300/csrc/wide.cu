@@ -216,35 +216,55 @@ __global__ __launch_bounds__(256, 2) void k_w_cols_inv(WidePrimes w, uint2* data
 // are < 2^58, so 64 of them fit a 64-bit sum; longer sums (FOLD, D > 64) are
 // folded every 64 terms.
 template <int BC, bool FOLD>
-__global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : 4)) void k_w_mac(
+__global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 4 ? 2 : (BC >= 2 ? 3 : 4)) void k_w_mac(
     WidePrimes w, int D, int key_digits, int total, const uint2* __restrict__ kwt, const uint2* __restrict__ dtt,
     uint2* acc, int b0, int nb) {
   extern __shared__ uint2 dsm[];  // [BC][D][32]
   const int N = 1 << w.log_n, tiles = N >> 5;
-  const int xb = blockIdx.x, pair = blockIdx.y;
-  const int bstart = b0 + blockIdx.z * BC;
+  // job groups vary fastest, so the CTAs that stream the same key tile run together and share it in L2
+  const int pair = blockIdx.y, xb = blockIdx.z;
+  const int bstart = b0 + blockIdx.x * BC;
   const int nloc = min(BC, b0 + nb - bstart);
   const int run = D * 32;
-  for (int e = threadIdx.x; e < BC * run; e += 32 * W_MAC_WARPS) {  // jobs past nloc read as zero
-    const int b = e / run, r = e - b * run;
-    dsm[e] = b < nloc ? dtt[(((size_t)(bstart + b) * 2 + pair) * tiles + xb) * run + r] : make_uint2(0, 0);
+  // the jobs' digit-transform runs (D * 256 bytes each, contiguous) go to shared memory by asynchronous
+  // 16-byte copies, all in flight at once; jobs past nloc read as zero
+  {
+    const int run16 = run / 2;  // 16-byte units per job
+    const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(dsm);
+    for (int e = threadIdx.x; e < BC * run16; e += 32 * W_MAC_WARPS) {
+      const int b = e / run16, r = e - b * run16;
+      if (b < nloc) {
+        const uint2* g = dtt + (((size_t)(bstart + b) * 2 + pair) * tiles + xb) * run + 2 * r;
+        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sbase + 16u * e), "l"(g) : "memory");
+      } else {
+        reinterpret_cast<uint4*>(dsm)[e] = make_uint4(0, 0, 0, 0);
+      }
+    }
+    asm volatile("cp.async.wait_all;" ::: "memory");
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
   const u64 bar0 = w.bar[2 * pair], bar1 = w.bar[2 * pair + 1];
   const size_t krun = (size_t)key_digits * 2 * 32;
+  constexpr int PF = 8;  // key words of the next PF digits in flight per lane
 #pragma unroll 1
   for (int j = warp; j < total; j += W_MAC_WARPS) {
     const uint2* kp = kwt + (((size_t)j * 2 + pair) * tiles + xb) * krun + lane;
     u64 a0[BC], a1[BC], c0[BC], c1[BC];
 #pragma unroll
     for (int b = 0; b < BC; ++b) a0[b] = a1[b] = c0[b] = c1[b] = 0;
-    uint2 n0 = kp[0], n1 = kp[32];
+    uint2 ka[PF], kb[PF];
+#pragma unroll
+    for (int u = 0; u < PF; ++u) {
+      if (u < D) {
+        ka[u] = kp[(size_t)u * 64];
+        kb[u] = kp[(size_t)u * 64 + 32];
+      }
+    }
 #pragma unroll 1
-    for (int i0 = 0; i0 < D; i0 += FOLD ? 64 : D) {
-      const int i1 = FOLD ? min(D, i0 + 64) : D;
-      if (FOLD && i0 > 0) {  // fold: the next 64 terms then stay below 2^64
+    for (int i0 = 0; i0 < D; i0 += PF) {
+      if (FOLD && i0 > 0 && (i0 & 63) == 0) {  // fold: the next 64 terms then stay below 2^64
 #pragma unroll
         for (int b = 0; b < BC; ++b) {
           a0[b] = reduce64_32(a0[b], q0, bar0);
@@ -253,21 +273,24 @@ __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : 4)) 
           c1[b] = reduce64_32(c1[b], q1, bar1);
         }
       }
-#pragma unroll 1
-      for (int i = i0; i < i1; ++i) {
-        const uint2 k0 = n0, k1 = n1;
-        if (i + 1 < D) {
-          n0 = kp[(size_t)(i + 1) * 64];
-          n1 = kp[(size_t)(i + 1) * 64 + 32];
-        }
-        const uint2* dp = dsm + i * 32 + lane;
 #pragma unroll
-        for (int b = 0; b < BC; ++b) {
-          const uint2 d = dp[b * run];
-          a0[b] += (u64)d.x * k0.x;
-          a1[b] += (u64)d.y * k0.y;
-          c0[b] += (u64)d.x * k1.x;
-          c1[b] += (u64)d.y * k1.y;
+      for (int u = 0; u < PF; ++u) {
+        const int i = i0 + u;
+        if (i < D) {
+          const uint2 k0 = ka[u], k1 = kb[u];
+          if (i + PF < D) {
+            ka[u] = kp[(size_t)(i + PF) * 64];
+            kb[u] = kp[(size_t)(i + PF) * 64 + 32];
+          }
+          const uint2* dp = dsm + i * 32 + lane;
+#pragma unroll
+          for (int b = 0; b < BC; ++b) {
+            const uint2 d = dp[b * run];
+            a0[b] += (u64)d.x * k0.x;
+            a1[b] += (u64)d.y * k0.y;
+            c0[b] += (u64)d.x * k1.x;
+            c1[b] += (u64)d.y * k1.y;
+          }
         }
       }
     }
@@ -294,7 +317,7 @@ void launch_w_mac(const WidePrimes& w, int D, int key_digits, int total, const u
     cudaFuncSetAttribute(k_w_mac<BC, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
     configured = smem;
   }
-  dim3 g((1 << w.log_n) / 32, 2, (nb + BC - 1) / BC);
+  dim3 g((nb + BC - 1) / BC, 2, (1 << w.log_n) / 32);
   k_w_mac<BC, FOLD><<<g, 32 * W_MAC_WARPS, smem, s>>>(w, D, key_digits, total, kwt, dtt, acc, b0, nb);
 }
 

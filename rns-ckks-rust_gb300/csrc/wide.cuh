@@ -37,7 +37,9 @@ __device__ __forceinline__ u64 wide_crt_mod(uint2 p01, uint2 p23, const WideTab&
   const uint32_t v3 = mul_shoup32(sub32(b, fold32(v2, w3), w3), W.g23, W.g23s, w3);
   const u64 lo = (u64)v0 + (u64)W.w[0] * v1;
   const u64 hi = (u64)v2 + (u64)w2 * v3;
-  u64 r = add_mod(mul_shoup(lo, 1, c.one_s, c.q), mul_shoup(hi, W.c01_mod_t[t], W.c01_mod_t_s[t], c.q), c.q);
+  // two lazy Shoup products in [0, 2q) each, one reduction of their sum from [0, 4q)
+  u64 r = reduce_4q(mul_shoup_lazy(lo, 1, c.one_s, c.q) + mul_shoup_lazy(hi, W.c01_mod_t[t], W.c01_mod_t_s[t], c.q),
+                    c.q);
   if (v3 >= W.half3) r = sub_mod(r, W.A_mod_t[t], c.q);
   return r;
 }
