@@ -34,6 +34,21 @@ Workspace::~Workspace() {
   if (host_pinned) cudaFreeHost(host_pinned);
 }
 
+cudaEvent_t HostPipe::event() {
+  if (next == events.size()) {
+    cudaEvent_t e;
+    cuda_check(cudaEventCreateWithFlags(&e, cudaEventDisableTiming), "cudaEventCreate");
+    events.push_back(e);
+  }
+  return events[next++];
+}
+
+HostPipe::~HostPipe() {
+  for (cudaEvent_t e : events) cudaEventDestroy(e);
+  for (cudaStream_t st : {in[0], in[1], comp, out})
+    if (st) cudaStreamDestroy(st);
+}
+
 }  // namespace rc
 
 template <class F>
@@ -1421,6 +1436,10 @@ extern "C" int rc_rotate_batch(rc_context* c, uint32_t count, const rc_ciphertex
 // =========================================================================
 // host-buffer entry points
 // =========================================================================
+// Host-buffer batch: the jobs run in chunks through a three-stage pipeline on internal streams (copy in
+// on two streams, compute, copy out) with two device staging slots, so that transfers overlap the
+// arithmetic.  The whole call is ordered after earlier work on `stream` and returns when the results are
+// in host memory.
 extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, const uint64_t* const* lhs,
                                                const uint64_t* const* rhs, const int32_t* levels,
                                                const int32_t* scale_bits, const rc_ksk* const* keys,
@@ -1428,46 +1447,89 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
   return guarded([&] {
     require(c && lhs && rhs && levels && scale_bits && keys && out, "arguments must not be null");
     cudaStream_t s = S(stream);
-    // device staging for inputs and outputs lives in its own buffer (the op's
-    // scratch is separate); kept per context+stream
-    size_t in_elems = 0, out_elems = 0;
-    for (uint32_t i = 0; i < count; ++i) {
+    for (uint32_t i = 0; i < count; ++i)
       require(levels[i] >= 1 && levels[i] < c->L, "ciphertext level context must exist");
-      in_elems += (size_t)2 * 2 * (levels[i] + 1) * c->N;
-      out_elems += (size_t)2 * levels[i] * c->N;
+    if (count == 0) return;
+    HostPipe* hp;
+    {
+      std::lock_guard<std::mutex> lk(c->mu);
+      auto& p = c->pipes[s];
+      if (!p) {
+        p.reset(new HostPipe());
+        for (cudaStream_t* st : {&p->in[0], &p->in[1], &p->comp, &p->out})
+          cuda_check(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking), "cudaStreamCreate");
+      }
+      hp = p.get();
     }
-    static thread_local std::map<std::pair<rc_context*, cudaStream_t>, std::unique_ptr<DevBuf>> staging;
-    auto& st = staging[{c, s}];
-    const size_t need = (in_elems + out_elems) * 8;
-    if (!st || st->bytes < need) {
-      cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
-      st.reset();
-      st.reset(new DevBuf(need));
+    hp->next = 0;
+    int chunk = 8;  // jobs per pipeline stage
+    if (const char* e = getenv("RNSCKKS_HOST_CHUNK")) chunk = std::max(1, atoi(e));
+    const uint32_t nchunks = (count + chunk - 1) / chunk;
+    auto in_elems = [&](uint32_t i) { return (size_t)2 * (levels[i] + 1) * c->N; };
+    auto out_elems = [&](uint32_t i) { return (size_t)2 * levels[i] * c->N; };
+    size_t need = 0;
+    for (uint32_t k = 0; k < nchunks; ++k) {
+      size_t b = 0;
+      for (uint32_t i = k * chunk; i < std::min<uint32_t>(count, (k + 1) * chunk); ++i)
+        b += 2 * in_elems(i) + out_elems(i);
+      need = std::max(need, b * 8);
     }
-    uint64_t* dev = (uint64_t*)st->p;
-    std::vector<rc_ciphertext> L(count), R(count), O(count);
-    size_t off = 0;
-    for (uint32_t i = 0; i < count; ++i) {
-      const size_t ce = (size_t)2 * (levels[i] + 1) * c->N;
-      L[i] = rc_ciphertext{dev + off, levels[i], scale_bits[i]};
-      cuda_check(cudaMemcpyAsync(dev + off, lhs[i], ce * 8, cudaMemcpyHostToDevice, s), "H2D");
-      off += ce;
-      R[i] = rc_ciphertext{dev + off, levels[i], scale_bits[i]};
-      cuda_check(cudaMemcpyAsync(dev + off, rhs[i], ce * 8, cudaMemcpyHostToDevice, s), "H2D");
-      off += ce;
+    for (int sl = 0; sl < 2; ++sl) {
+      if (!hp->slot[sl] || hp->slot[sl]->bytes < need) {
+        for (cudaStream_t st : {hp->in[0], hp->in[1], hp->comp, hp->out})
+          cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+        hp->slot[sl].reset();
+        hp->slot[sl].reset(new DevBuf(need));
+      }
     }
-    for (uint32_t i = 0; i < count; ++i) {
-      O[i] = rc_ciphertext{dev + off, 0, 0};
-      off += (size_t)2 * levels[i] * c->N;
+    cudaEvent_t start = hp->event();
+    cuda_check(cudaEventRecord(start, s), "cudaEventRecord");
+    for (cudaStream_t st : {hp->in[0], hp->in[1], hp->comp, hp->out})
+      cuda_check(cudaStreamWaitEvent(st, start, 0), "cudaStreamWaitEvent");
+    std::vector<cudaEvent_t> comp_done(nchunks), out_done(nchunks);
+    for (uint32_t k = 0; k < nchunks; ++k) {
+      const uint32_t i0 = k * chunk, i1 = std::min<uint32_t>(count, i0 + chunk), n = i1 - i0;
+      uint64_t* dev = (uint64_t*)hp->slot[k & 1]->p;
+      if (k >= 2) {  // the slot's inputs were consumed by chunk k-2's compute
+        for (int q = 0; q < 2; ++q) cuda_check(cudaStreamWaitEvent(hp->in[q], comp_done[k - 2], 0), "wait");
+      }
+      std::vector<rc_ciphertext> L(n), R(n), O(n);
+      size_t off = 0;
+      for (uint32_t j = 0; j < n; ++j) {
+        const uint32_t i = i0 + j;
+        L[j] = rc_ciphertext{dev + off, levels[i], scale_bits[i]};
+        cuda_check(cudaMemcpyAsync(dev + off, lhs[i], in_elems(i) * 8, cudaMemcpyHostToDevice, hp->in[0]), "H2D");
+        off += in_elems(i);
+        R[j] = rc_ciphertext{dev + off, levels[i], scale_bits[i]};
+        cuda_check(cudaMemcpyAsync(dev + off, rhs[i], in_elems(i) * 8, cudaMemcpyHostToDevice, hp->in[1]), "H2D");
+        off += in_elems(i);
+      }
+      for (uint32_t j = 0; j < n; ++j) {
+        O[j] = rc_ciphertext{dev + off, 0, 0};
+        off += out_elems(i0 + j);
+      }
+      for (int q = 0; q < 2; ++q) {
+        cudaEvent_t e = hp->event();
+        cuda_check(cudaEventRecord(e, hp->in[q]), "cudaEventRecord");
+        cuda_check(cudaStreamWaitEvent(hp->comp, e, 0), "wait");
+      }
+      if (k >= 2) cuda_check(cudaStreamWaitEvent(hp->comp, out_done[k - 2], 0), "wait");  // slot outputs read
+      int rc = rc_mult_relinearized_batch(c, n, L.data(), R.data(), keys + i0, O.data(), hp->comp);
+      if (rc != RC_OK) fail(rc, g_err);
+      comp_done[k] = hp->event();
+      cuda_check(cudaEventRecord(comp_done[k], hp->comp), "cudaEventRecord");
+      cuda_check(cudaStreamWaitEvent(hp->out, comp_done[k], 0), "wait");
+      for (uint32_t j = 0; j < n; ++j) {
+        const uint32_t i = i0 + j;
+        cuda_check(cudaMemcpyAsync(out[i], O[j].data, out_elems(i) * 8, cudaMemcpyDeviceToHost, hp->out), "D2H");
+        if (out_scale_bits) out_scale_bits[i] = O[j].scale_bits;
+      }
+      out_done[k] = hp->event();
+      cuda_check(cudaEventRecord(out_done[k], hp->out), "cudaEventRecord");
     }
-    int rc = rc_mult_relinearized_batch(c, count, L.data(), R.data(), keys, O.data(), stream);
-    if (rc != RC_OK) fail(rc, g_err);
-    for (uint32_t i = 0; i < count; ++i) {
-      cuda_check(cudaMemcpyAsync(out[i], O[i].data, (size_t)2 * levels[i] * c->N * 8, cudaMemcpyDeviceToHost, s),
-                 "D2H");
-      if (out_scale_bits) out_scale_bits[i] = O[i].scale_bits;
-    }
-    cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");
+    // later work on the caller's stream is ordered after the whole call
+    cuda_check(cudaStreamWaitEvent(s, out_done[nchunks - 1], 0), "wait");
+    cuda_check(cudaStreamSynchronize(hp->out), "cudaStreamSynchronize");
   });
 }
 

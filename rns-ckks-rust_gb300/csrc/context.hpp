@@ -54,6 +54,17 @@ struct Workspace {
   ~Workspace();
 };
 
+// Streams, events and two device staging slots of the pipelined host-buffer entry points: chunk k's
+// inputs are copied in on two copy streams while chunk k-1 computes and chunk k-2's results are copied out.
+struct HostPipe {
+  cudaStream_t in[2] = {nullptr, nullptr}, comp = nullptr, out = nullptr;
+  std::unique_ptr<DevBuf> slot[2];
+  std::vector<cudaEvent_t> events;
+  cudaEvent_t event();  // from the pool, created on first use
+  size_t next = 0;      // events handed out in the current call
+  ~HostPipe();
+};
+
 }  // namespace rc
 
 struct rc_context {
@@ -78,6 +89,7 @@ struct rc_context {
   std::vector<uint64_t> host_halfP;
   std::mutex mu;
   std::map<cudaStream_t, std::unique_ptr<rc::Workspace>> ws;
+  std::map<cudaStream_t, std::unique_ptr<rc::HostPipe>> pipes;  // per caller stream
   size_t scratch_budget = size_t(256) << 20;
 
   rc::NttArgs ntt() const {

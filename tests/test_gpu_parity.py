@@ -275,6 +275,32 @@ def test_host_entry_point_equals_device_path(C, pkg):
     assert np.array_equal(out, dev.numpy()) and sb.value == dev.scale_bits
 
 
+def test_pipelined_host_batch_equals_device_path(C, pkg):
+    # more jobs than one pipeline chunk, mixed levels, repeated calls reusing the staging slots
+    import ctypes
+    params = pkg.params.hybrid_params(11, 5, 2, 50)
+    ctx = C.RnsCkksContext(params)
+    n, q = params.poly_degree, params.q_moduli()
+    rng = np.random.default_rng(45)
+    keys = {lv: ctx.upload_keyswitch_key(_random_key(rng, params, lv + 1, True)[0], lv, 2) for lv in (2, 3, 4)}
+    for count in (21, 3):
+        levels = [int(x) for x in rng.integers(2, 5, count)]
+        A = [np.ascontiguousarray(rand_ct(rng, q[: lv + 1], n)) for lv in levels]
+        B = [np.ascontiguousarray(rand_ct(rng, q[: lv + 1], n)) for lv in levels]
+        outs = [np.zeros((2, lv, n), dtype=np.uint64) for lv in levels]
+        P = lambda arrs: (ctypes.c_void_p * count)(*[x.ctypes.data for x in arrs])
+        LV = (ctypes.c_int32 * count)(*levels)
+        SB = (ctypes.c_int32 * count)(*([40] * count))
+        K = (ctypes.c_void_p * count)(*[keys[lv].handle for lv in levels])
+        OSB = (ctypes.c_int32 * count)()
+        C.call("rc_mult_relinearized_batch_host", ctx.handle, count, P(A), P(B), LV, SB, K, P(outs), OSB,
+               C._stream())
+        for i, lv in enumerate(levels):
+            dev = ctx.mult_relinearized(C.RnsCiphertext(C.to_device(A[i]), 40), C.RnsCiphertext(C.to_device(B[i]), 40),
+                                        keys[lv])
+            assert np.array_equal(outs[i], dev.numpy()) and OSB[i] == dev.scale_bits
+
+
 def test_precondition_errors_carry_reference_messages(C, pkg):
     params = pkg.params.hybrid_params(11, 4, 2, 50)
     ctx = C.RnsCkksContext(params)
