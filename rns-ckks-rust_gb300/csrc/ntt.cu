@@ -204,21 +204,23 @@ __global__ __launch_bounds__(256, 2) void k_cols_f(NttArgs a, PtrTab src, PtrTab
   using G = core::Geo<M1>;
   constexpr int COLS = ColTile<M1>::COLS, N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2;
   __shared__ u64 tile[COLS * G::STRIDE];
-  __shared__ Twiddle twl[N1];
+  __shared__ __align__(16) Twiddle twl[N1];
   const int c0 = blockIdx.x * COLS;
   const int limb = blockIdx.y, poly = blockIdx.z;
   const int prime = map.prime(limb);
   const PrimeConst& pc = a.pc[prime];
   const u64 q = pc.q;
-  core::stage_twiddles<M1>(twl, (FWD ? a.tw_fwd : a.tw_inv) + (size_t)prime * N, 1, threadIdx.x, 256);
   const u64* in = src.p[poly] + (size_t)limb * N;
   u64* out = dst.p[poly] + (size_t)limb * N;
+  // tile and twiddles by asynchronous copies, all in flight together
 #pragma unroll 4
   for (int it = 0; it < N1 * COLS / 256; ++it) {
     const int idx = it * 256 + threadIdx.x;
     const int r = idx / COLS, c = idx % COLS;
-    tile[c * G::STRIDE + core::swz<M1>(r)] = in[(size_t)r * N2 + c0 + c];
+    core::cp_async8(&tile[c * G::STRIDE + core::swz<M1>(r)], &in[(size_t)r * N2 + c0 + c]);
   }
+  core::stage_twiddles_async<M1>(twl, (FWD ? a.tw_fwd : a.tw_inv) + (size_t)prime * N, 1, threadIdx.x, 256);
+  core::cp_async_wait_all();
   __syncthreads();
   const int warp = threadIdx.x >> 5;
 #pragma unroll 1
@@ -262,7 +264,7 @@ __global__ __launch_bounds__(32 * ROW_WARPS) void k_rows_f(NttArgs a, PtrTab src
   using G = core::Geo<M2>;
   constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = ROW_WARPS * G::SUBS;
   __shared__ u64 bufs[ROWS * G::STRIDE];
-  __shared__ Twiddle twl[ROWS][N2];
+  __shared__ __align__(16) Twiddle twl[ROWS][N2];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sub = lane / G::LANES, l = lane % G::LANES;
   const int row0 = blockIdx.x * ROWS;
@@ -270,23 +272,24 @@ __global__ __launch_bounds__(32 * ROW_WARPS) void k_rows_f(NttArgs a, PtrTab src
   const int prime = map.prime(limb);
   const PrimeConst& pc = a.pc[prime];
   const Twiddle* twg = (FWD ? a.tw_fwd : a.tw_inv) + (size_t)prime * N;
-#pragma unroll 1
-  for (int rr = 0; rr < ROWS; ++rr) core::stage_twiddles<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * ROW_WARPS);
-  __syncthreads();
   const int rl = warp * G::SUBS + sub, row = row0 + rl;
   const u64* in = src.p[poly] + (size_t)limb * N + (size_t)row * N2;
   u64* out = dst.p[poly] + (size_t)limb * N + (size_t)row * N2;
   u64* buf = bufs + rl * G::STRIDE;
+  // the row's values are requested before the twiddle tables, so both latencies overlap
   u64 v[8];
-  if (FWD) {
 #pragma unroll
-    for (int k = 0; k < 8; ++k) v[k] = in[core::first_idx<M2>(l, k)];
+  for (int k = 0; k < 8; ++k) v[k] = in[FWD ? core::first_idx<M2>(l, k) : core::last_idx<M2>(l, k)];
+#pragma unroll 1
+  for (int rr = 0; rr < ROWS; ++rr)
+    core::stage_twiddles_async<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * ROW_WARPS);
+  core::cp_async_wait_all();
+  __syncthreads();
+  if (FWD) {
     core::fwd_sub<M2, LAZY>(v, buf, l, twl[rl], pc.q);
 #pragma unroll
     for (int k = 0; k < 8; ++k) out[core::last_idx<M2>(l, k)] = reduce_out<LAZY>(v[k], pc);
   } else {
-#pragma unroll
-    for (int k = 0; k < 8; ++k) v[k] = in[core::last_idx<M2>(l, k)];
     core::inv_sub<M2>(v, buf, l, twl[rl], pc.q);
 #pragma unroll
     for (int k = 0; k < 8; ++k) out[core::first_idx<M2>(l, k)] = v[k];

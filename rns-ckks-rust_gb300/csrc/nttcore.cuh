@@ -45,6 +45,36 @@ __device__ __forceinline__ void stage_twiddles(Twiddle* local, const Twiddle* gl
   }
 }
 
+// Asynchronous global -> shared copies (cp.async): a thread issues all of its copies before waiting, so
+// the tile and twiddle loads of a kernel are in flight together.  Shared destinations of 16-byte copies
+// must be 16-byte aligned.
+__device__ __forceinline__ void cp_async8(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async4(void* smem, const void* gmem) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 4;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async16(void* smem, const void* gmem) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"((uint32_t)__cvta_generic_to_shared(smem)),
+               "l"(gmem)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_wait_all() { asm volatile("cp.async.wait_all;" ::: "memory"); }
+
+// stage_twiddles with asynchronous copies (completed by cp_async_wait_all); T is Twiddle or Tw2 (16 bytes)
+template <int M, class T>
+__device__ __forceinline__ void stage_twiddles_async(T* local, const T* global, u64 tb, int tid, int nthreads) {
+  static_assert(sizeof(T) == 16, "16-byte twiddle entries");
+  for (int t = 1 + tid; t < (1 << M); t += nthreads) {
+    const int s = 31 - __clz(t);
+    cp_async16(local + t, global + ((tb - 1) << s) + t);
+  }
+}
+
 // Lane id re-read with a volatile move: used inside long loops so that the
 // lane-dependent shared-memory addresses are recomputed per iteration instead
 // of being hoisted (and pinned in registers) across the loop.

@@ -47,25 +47,26 @@ __global__ __launch_bounds__(256, 2) void k_w_cols_fwd(WidePrimes w, const void*
   using G = core::Geo<M1>;
   constexpr int COLS = WColTile<M1>::COLS, N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2;
   __shared__ uint2 tile[COLS * G::STRIDE];
-  __shared__ Tw2 twl[N1];
+  __shared__ __align__(16) Tw2 twl[N1];
   const int c0 = blockIdx.x * COLS;
   const int pair = blockIdx.y;
   const size_t poly = (size_t)p0 + blockIdx.z;
   const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
-  core::stage_twiddles2<M1>(twl, w.tw_fwd + (size_t)pair * N, 1, threadIdx.x, 256);
+  // tile (digits: the int32 into the element's first word, converted at first use) and twiddles by
+  // asynchronous copies, all in flight together
 #pragma unroll 4
   for (int it = 0; it < N1 * COLS / 256; ++it) {
     const int idx = it * 256 + threadIdx.x;
     const int r = idx / COLS, c = idx % COLS;
-    uint2 v;
-    if (SRC == 0) {
-      const int32_t d = static_cast<const int32_t*>(src)[poly * N + (size_t)r * N2 + c0 + c];
-      v = make_uint2((uint32_t)(d + (int32_t)(2 * q0)), (uint32_t)(d + (int32_t)(2 * q1)));
-    } else {
-      v = static_cast<const uint2*>(src)[(poly * 2 + pair) * N + (size_t)r * N2 + c0 + c];
-    }
-    tile[c * G::STRIDE + core::swz<M1>(r)] = v;
+    if (SRC == 0)
+      core::cp_async4(&tile[c * G::STRIDE + core::swz<M1>(r)].x,
+                      static_cast<const int32_t*>(src) + poly * N + (size_t)r * N2 + c0 + c);
+    else
+      core::cp_async8(&tile[c * G::STRIDE + core::swz<M1>(r)],
+                      static_cast<const uint2*>(src) + (poly * 2 + pair) * N + (size_t)r * N2 + c0 + c);
   }
+  core::stage_twiddles_async<M1>(twl, w.tw_fwd + (size_t)pair * N, 1, threadIdx.x, 256);
+  core::cp_async_wait_all();
   __syncthreads();
   const int warp = threadIdx.x >> 5;
 #pragma unroll 1
@@ -75,7 +76,13 @@ __global__ __launch_bounds__(256, 2) void k_w_cols_fwd(WidePrimes w, const void*
     uint2* buf = tile + (cb + sub) * G::STRIDE;
     uint2 v[8];
 #pragma unroll
-    for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::first_idx<M1>(l, k))];
+    for (int k = 0; k < 8; ++k) {
+      v[k] = buf[core::swz<M1>(core::first_idx<M1>(l, k))];
+      if (SRC == 0) {  // digit d as d + 2q, in [0, 4q) since 2q > 2^29 >= |d|
+        const int32_t d = (int32_t)v[k].x;
+        v[k] = make_uint2((uint32_t)(d + (int32_t)(2 * q0)), (uint32_t)(d + (int32_t)(2 * q1)));
+      }
+    }
     __syncwarp();
     core::fwd_sub2<M1>(v, buf, l, twl, q0, q1);
 #pragma unroll
@@ -100,7 +107,7 @@ __global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_fwd(WidePrimes w, u
   using G = core::Geo<M2>;
   constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = W_ROW_WARPS * G::SUBS;
   __shared__ uint2 bufs[ROWS * G::STRIDE];
-  __shared__ Tw2 twl[ROWS][N2];
+  __shared__ __align__(16) Tw2 twl[ROWS][N2];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sub = lane / G::LANES, l = lane % G::LANES;
   const int row0 = blockIdx.x * ROWS;
@@ -108,16 +115,17 @@ __global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_fwd(WidePrimes w, u
   const size_t poly = (size_t)p0 + blockIdx.z;
   const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
   const Tw2* twg = w.tw_fwd + (size_t)pair * N;
-#pragma unroll 1
-  for (int rr = 0; rr < ROWS; ++rr)
-    core::stage_twiddles2<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * W_ROW_WARPS);
-  __syncthreads();
   const int rl = warp * G::SUBS + sub, row = row0 + rl;
   uint2* in = data + (poly * 2 + pair) * N + (size_t)row * N2;
   uint2* buf = bufs + rl * G::STRIDE;
-  uint2 v[8];
+  uint2 v[8];  // requested before the twiddle tables, so both latencies overlap
 #pragma unroll
   for (int k = 0; k < 8; ++k) v[k] = in[core::first_idx<M2>(l, k)];
+#pragma unroll 1
+  for (int rr = 0; rr < ROWS; ++rr)
+    core::stage_twiddles_async<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * W_ROW_WARPS);
+  core::cp_async_wait_all();
+  __syncthreads();
   core::fwd_sub2<M2>(v, buf, l, twl[rl], q0, q1);
   if (TILED) {
     const size_t job = poly / D, digit = poly % D;
@@ -139,7 +147,7 @@ __global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_inv(WidePrimes w, u
   using G = core::Geo<M2>;
   constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = W_ROW_WARPS * G::SUBS;
   __shared__ uint2 bufs[ROWS * G::STRIDE];
-  __shared__ Tw2 twl[ROWS][N2];
+  __shared__ __align__(16) Tw2 twl[ROWS][N2];
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sub = lane / G::LANES, l = lane % G::LANES;
   const int row0 = blockIdx.x * ROWS;
@@ -147,16 +155,17 @@ __global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_inv(WidePrimes w, u
   const size_t poly = blockIdx.z;
   const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
   const Tw2* twg = w.tw_inv + (size_t)pair * N;
-#pragma unroll 1
-  for (int rr = 0; rr < ROWS; ++rr)
-    core::stage_twiddles2<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * W_ROW_WARPS);
-  __syncthreads();
   const int rl = warp * G::SUBS + sub, row = row0 + rl;
   uint2* in = data + (poly * 2 + pair) * N + (size_t)row * N2;
   uint2* buf = bufs + rl * G::STRIDE;
-  uint2 v[8];
+  uint2 v[8];  // requested before the twiddle tables, so both latencies overlap
 #pragma unroll
   for (int k = 0; k < 8; ++k) v[k] = in[core::last_idx<M2>(l, k)];
+#pragma unroll 1
+  for (int rr = 0; rr < ROWS; ++rr)
+    core::stage_twiddles_async<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * W_ROW_WARPS);
+  core::cp_async_wait_all();
+  __syncthreads();
   core::inv_sub2<M2>(v, buf, l, twl[rl], q0, q1);
 #pragma unroll
   for (int k = 0; k < 8; ++k) in[core::first_idx<M2>(l, k)] = v[k];
@@ -168,19 +177,20 @@ __global__ __launch_bounds__(256, 2) void k_w_cols_inv(WidePrimes w, uint2* data
   using G = core::Geo<M1>;
   constexpr int COLS = WColTile<M1>::COLS, N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2;
   __shared__ uint2 tile[COLS * G::STRIDE];
-  __shared__ Tw2 twl[N1];
+  __shared__ __align__(16) Tw2 twl[N1];
   const int c0 = blockIdx.x * COLS;
   const int pair = blockIdx.y;
   const size_t poly = blockIdx.z;
   const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
-  core::stage_twiddles2<M1>(twl, w.tw_inv + (size_t)pair * N, 1, threadIdx.x, 256);
   uint2* io = data + (poly * 2 + pair) * N;
 #pragma unroll 4
   for (int it = 0; it < N1 * COLS / 256; ++it) {
     const int idx = it * 256 + threadIdx.x;
     const int r = idx / COLS, c = idx % COLS;
-    tile[c * G::STRIDE + core::swz<M1>(r)] = io[(size_t)r * N2 + c0 + c];
+    core::cp_async8(&tile[c * G::STRIDE + core::swz<M1>(r)], &io[(size_t)r * N2 + c0 + c]);
   }
+  core::stage_twiddles_async<M1>(twl, w.tw_inv + (size_t)pair * N, 1, threadIdx.x, 256);
+  core::cp_async_wait_all();
   __syncthreads();
   const int warp = threadIdx.x >> 5;
 #pragma unroll 1
@@ -215,11 +225,22 @@ __global__ __launch_bounds__(256, 2) void k_w_cols_inv(WidePrimes w, uint2* data
 // pair) once for all BC jobs, the next digit's key words loaded ahead.  Terms
 // are < 2^58, so 64 of them fit a 64-bit sum; longer sums (FOLD, D > 64) are
 // folded every 64 terms.
+constexpr int W_PF = 8;  // digits of key words in flight per warp (asynchronous copies into a ring)
+
+__device__ __forceinline__ void cp_async8(uint32_t dst, const void* src) {
+  asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
 template <int BC, bool FOLD>
 __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 4 ? 2 : (BC >= 2 ? 3 : 4)) void k_w_mac(
     WidePrimes w, int D, int key_digits, int total, const uint2* __restrict__ kwt, const uint2* __restrict__ dtt,
     uint2* acc, int b0, int nb) {
-  extern __shared__ uint2 dsm[];  // [BC][D][32]
+  extern __shared__ uint2 dsm[];  // [BC][D][32] digit transforms, then [warps][W_PF][2][32] key ring
   const int N = 1 << w.log_n, tiles = N >> 5;
   // job groups vary fastest, so the CTAs that stream the same key tile run together and share it in L2
   const int pair = blockIdx.y, xb = blockIdx.z;
@@ -247,23 +268,26 @@ __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 4 ? 2 : (BC >= 2 ? 3 : 4)) 
   const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
   const u64 bar0 = w.bar[2 * pair], bar1 = w.bar[2 * pair + 1];
   const size_t krun = (size_t)key_digits * 2 * 32;
-  constexpr int PF = 8;  // key words of the next PF digits in flight per lane
+  // this lane's slots of the warp's key ring: slot u holds (k0, k1) of one digit at ring[u][0|1][lane]
+  uint2* ring = dsm + (size_t)BC * run + (size_t)warp * W_PF * 64 + lane;
+  const uint32_t rs = (uint32_t)__cvta_generic_to_shared(ring);
 #pragma unroll 1
   for (int j = warp; j < total; j += W_MAC_WARPS) {
     const uint2* kp = kwt + (((size_t)j * 2 + pair) * tiles + xb) * krun + lane;
     u64 a0[BC], a1[BC], c0[BC], c1[BC];
 #pragma unroll
     for (int b = 0; b < BC; ++b) a0[b] = a1[b] = c0[b] = c1[b] = 0;
-    uint2 ka[PF], kb[PF];
+    // each lane copies and later reads only its own words, so the waits need no warp barrier
 #pragma unroll
-    for (int u = 0; u < PF; ++u) {
+    for (int u = 0; u < W_PF; ++u) {
       if (u < D) {
-        ka[u] = kp[(size_t)u * 64];
-        kb[u] = kp[(size_t)u * 64 + 32];
+        cp_async8(rs + 8u * (64 * u), kp + (size_t)u * 64);
+        cp_async8(rs + 8u * (64 * u + 32), kp + (size_t)u * 64 + 32);
       }
+      cp_async_commit();
     }
 #pragma unroll 1
-    for (int i0 = 0; i0 < D; i0 += PF) {
+    for (int i0 = 0; i0 < D; i0 += W_PF) {
       if (FOLD && i0 > 0 && (i0 & 63) == 0) {  // fold: the next 64 terms then stay below 2^64
 #pragma unroll
         for (int b = 0; b < BC; ++b) {
@@ -274,14 +298,11 @@ __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 4 ? 2 : (BC >= 2 ? 3 : 4)) 
         }
       }
 #pragma unroll
-      for (int u = 0; u < PF; ++u) {
+      for (int u = 0; u < W_PF; ++u) {
         const int i = i0 + u;
         if (i < D) {
-          const uint2 k0 = ka[u], k1 = kb[u];
-          if (i + PF < D) {
-            ka[u] = kp[(size_t)(i + PF) * 64];
-            kb[u] = kp[(size_t)(i + PF) * 64 + 32];
-          }
+          cp_async_wait<W_PF - 1>();  // digit i's group has landed
+          const uint2 k0 = ring[64 * u], k1 = ring[64 * u + 32];
           const uint2* dp = dsm + i * 32 + lane;
 #pragma unroll
           for (int b = 0; b < BC; ++b) {
@@ -291,9 +312,16 @@ __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 4 ? 2 : (BC >= 2 ? 3 : 4)) 
             c0[b] += (u64)d.x * k1.x;
             c1[b] += (u64)d.y * k1.y;
           }
+          // refill the slot with digit i + W_PF once its words have been used
+          if (i + W_PF < D) {
+            cp_async8(rs + 8u * (64 * u), kp + (size_t)(i + W_PF) * 64);
+            cp_async8(rs + 8u * (64 * u + 32), kp + (size_t)(i + W_PF) * 64 + 32);
+          }
+          cp_async_commit();
         }
       }
     }
+    cp_async_wait<0>();
     const int x = xb * 32 + lane;
 #pragma unroll
     for (int b = 0; b < BC; ++b) {
@@ -311,7 +339,7 @@ __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 4 ? 2 : (BC >= 2 ? 3 : 4)) 
 template <int BC, bool FOLD>
 void launch_w_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt,
                   uint2* acc, int b0, int nb, cudaStream_t s) {
-  const size_t smem = (size_t)BC * D * 32 * sizeof(uint2);
+  const size_t smem = ((size_t)BC * D * 32 + (size_t)W_MAC_WARPS * W_PF * 64) * sizeof(uint2);
   static size_t configured = 0;
   if (smem > 48 * 1024 && smem > configured) {
     cudaFuncSetAttribute(k_w_mac<BC, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
