@@ -429,6 +429,7 @@ def run_gpu(args):
         # (128 quadratic ciphertexts, limbs 8..24, CUDA graph); reported beside the headline, untimed by it
         result["ntt_microbench"] = ntt_microbench(C, ctx, params, peak, args.seed)
         result["mixed_level_relin"] = mixed_level_relin(C, ctx, params, load_oracle(), args.seed)
+        result["serving"] = serving_bench(pkg, C, args.seed)
     if rank == 0:
         print(json.dumps(result), flush=True)
     if world > 1:
@@ -544,6 +545,106 @@ def mixed_level_relin(C, ctx, params, O, seed, count=128, reps=3):
     del graph, quads, outs, keys
     torch.cuda.synchronize()
     return res
+
+
+def serving_bench(pkg, C, seed, jobs_per_phase=240):
+    """Served mixed request stream: Poisson arrivals of jobs drawn uniformly from {Paterson-Stockmeyer of a
+    degree-15 polynomial (coefficients uniform in [-1,1]) at N=2^14, 12 limbs; Halevi-Shoup dot product of
+    length 1024 at N=2^13, 6 limbs; relinearized Hadamard product at N=2^15, 16 limbs}, keys and ciphertexts
+    resident on the device, admission by device-memory footprint.  The arrival rate is swept at 50 % and 90 %
+    of the capacity measured with a burst; the per-op GPU path (the same jobs one at a time, no batching) is
+    timed beside it."""
+    import random
+    import torch
+    from rnsckks_gb300 import algorithms as A
+    from rnsckks_gb300 import server as S
+    P = pkg.params
+    rng = np.random.default_rng(seed)
+    pools = {}
+    # relinearized Hadamard at N=2^15, 16 limbs
+    ctx = C.RnsCkksContext(P.scheme_params(15, 16, 2, 40))
+    kp = ctx.keygen(64, C.Sampler(seed + 1))
+    key = ctx.generate_relinearization_key(kp.secret_key, kp.public_key)
+    cts = [ctx.encrypt(ctx.encode_real(rng.uniform(-1, 1, ctx.num_slots())), kp.public_key, C.Sampler(seed + 10 + i))
+           for i in range(16)]
+    pools["hadamard"] = lambda i, c=ctx, k=key, cts=cts: S.hadamard_job(c, cts[i % 16], cts[(i * 7 + 3) % 16], k)
+    # Halevi-Shoup dot product of length 1024 at N=2^13, 6 limbs
+    ctx = C.RnsCkksContext(P.scheme_params(13, 6, 2, 40))
+    kp = ctx.keygen(64, C.Sampler(seed + 2))
+    hkeys = A.generate_halevi_shoup_dot_product_rotation_keys(ctx, kp.secret_key, kp.public_key,
+                                                              ctx.levels() - 2, 1024)
+    hcts = [ctx.encrypt(ctx.encode_real(rng.uniform(-1, 1, ctx.num_slots())), kp.public_key,
+                        C.Sampler(seed + 100 + i)) for i in range(16)]
+    hplain = [list(rng.uniform(-1, 1, 1024)) for _ in range(16)]
+    pools["halevi_shoup"] = lambda i, c=ctx, k=hkeys, cts=hcts: S.halevi_shoup_job(c, cts[i % 16], hplain[i % 16], k)
+    # Paterson-Stockmeyer, degree 15, at N=2^14, 12 limbs
+    ctx = C.RnsCkksContext(P.scheme_params(14, 12, 2, 40))
+    kp = ctx.keygen(64, C.Sampler(seed + 3))
+    coeffs = list(rng.uniform(-1, 1, 16))
+    pkeys = A.generate_paterson_stockmeyer_relinearization_keys(ctx, kp.secret_key, kp.public_key,
+                                                                ctx.levels() - 1, 16)
+    plains = A.constant_plaintext_cache(ctx)
+    pcts = [ctx.encrypt(ctx.encode_real(rng.uniform(-0.5, 0.5, ctx.num_slots())), kp.public_key,
+                        C.Sampler(seed + 200 + i)) for i in range(16)]
+    pools["paterson_stockmeyer"] = lambda i, c=ctx, k=pkeys, cts=pcts: S.paterson_stockmeyer_job(
+        c, cts[i % 16], coeffs, k, plains)
+    torch.cuda.synchronize()
+    kinds = sorted(pools)
+
+    def make_jobs(n, r):
+        return [pools[kinds[r.randrange(3)]](i) for i in range(n)]
+
+    free, _ = torch.cuda.mem_get_info()
+    budget = int(free * 0.5)
+    # warm-up: every kind once through the batched routines (plaintext cache, scratch)
+    warm = S.Scheduler(S.GpuExecutor(3), slots=3, memory_budget=budget).start()
+    for k in kinds:
+        warm.submit(pools[k](0))
+    warm.drain()
+    warm.stop()
+    out = {"workload": "Poisson mix of PS deg-15 @ N=2^14 L=12, HS dot 1024 @ N=2^13 L=6, "
+                       "relin Hadamard @ N=2^15 L=16", "slots": 3, "memory_budget_bytes": budget}
+    # per-op GPU path: the same jobs one at a time on one stream, no batching
+    jobs = make_jobs(60, random.Random(seed))
+    ex = S.GpuExecutor(1)
+    lat = []
+    t0 = time.perf_counter()
+    for j in jobs:
+        a = time.perf_counter()
+        ex(0, [j])
+        lat.append(time.perf_counter() - a)
+    per_op_rate = len(jobs) / (time.perf_counter() - t0)
+    out["per_op"] = {"throughput_jobs_per_s": round(per_op_rate, 2),
+                     "p50_ms": round(float(np.percentile(lat, 50)) * 1e3, 3),
+                     "p99_ms": round(float(np.percentile(lat, 99)) * 1e3, 3)}
+    # capacity: a burst of jobs through the server
+    sch = S.Scheduler(S.GpuExecutor(3), slots=3, memory_budget=budget, max_batch=16).start()
+    for j in make_jobs(jobs_per_phase, random.Random(seed + 1)):
+        sch.submit(j)
+    sch.drain()
+    sch.stop()
+    cap = sch.stats()
+    out["burst"] = cap
+    rate_max = cap["throughput_jobs_per_s"]
+    sweep = []
+    for frac in (0.5, 0.9):
+        rate = rate_max * frac
+        r = random.Random(seed + int(frac * 100))
+        sch = S.Scheduler(S.GpuExecutor(3), slots=3, memory_budget=budget, max_batch=16).start()
+        t_next = time.perf_counter()
+        for j in make_jobs(jobs_per_phase, r):
+            t_next += r.expovariate(rate)
+            d = t_next - time.perf_counter()
+            if d > 0:
+                time.sleep(d)
+            sch.submit(j)
+        sch.drain()
+        sch.stop()
+        st = sch.stats()
+        st["offered_jobs_per_s"] = round(rate, 2)
+        sweep.append(st)
+    out["poisson"] = sweep
+    return out
 
 
 def run_reference(args):

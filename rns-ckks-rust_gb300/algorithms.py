@@ -481,16 +481,23 @@ def paterson_stockmeyer_eval(ctx: RnsCkksContext, ciphertext: RnsCiphertext, coe
     return paterson_stockmeyer_eval_batch(ctx, [ciphertext], coefficients, relin_keys)[0]
 
 
+def constant_plaintext_cache(ctx: RnsCkksContext) -> "_Plains":
+    """A cache of encoded constant plaintexts that callers may keep across `paterson_stockmeyer_eval_batch`
+    calls on the same context (the encodings are deterministic)."""
+    return _Plains(ctx)
+
+
 def paterson_stockmeyer_eval_batch(ctx: RnsCkksContext, ciphertexts: Sequence[RnsCiphertext],
                                    coefficients: Sequence[float],
-                                   relin_keys: Dict[int, RnsKeySwitchingKey]) -> List[RnsCiphertext]:
+                                   relin_keys: Dict[int, RnsKeySwitchingKey],
+                                   plains: Optional["_Plains"] = None) -> List[RnsCiphertext]:
     """`paterson_stockmeyer_eval` of one polynomial on many ciphertexts (same level and scale): each baby
     power and each outer product runs as one batched `mult_relinearized` over the batch."""
     coeffs = [float(c) for c in coefficients]
     if not coeffs:
         _panic("polynomial must contain at least one coefficient")
     cts = list(ciphertexts)
-    pl = _Plains(ctx)
+    pl = plains if plains is not None else _Plains(ctx)
     if len(coeffs) == 1:
         return [_constant_ciphertext(ctx, pl, ct.level, ct.scale_bits, coeffs[0]) for ct in cts]
     level, in_scale = cts[0].level, cts[0].scale_bits
