@@ -265,6 +265,9 @@ def run_gpu(args):
     outs = [torch.empty((2, limbs - 1, n), dtype=torch.int64, device="cuda") for _ in range(B)]
     L, R, K, O = raw_batch(C, lhs, rhs, key, outs)
     ctx.reserve(limbs - 1, B)
+    # launch shapes from the autotuner (measured on this batch before the timed region; results unchanged)
+    from rnsckks_gb300 import autotune as T
+    tune_dev = T.tune_mult_relinearized(ctx, lhs, rhs, [key] * B, outs, reps=2)
 
     def step():
         C.call("rc_mult_relinearized_batch", ctx.handle, B, L, R, K, O, s_ptr)
@@ -346,6 +349,7 @@ def run_gpu(args):
     def e2e_step():
         C.call("rc_mult_relinearized_batch_host", ctx.handle, B, HL, HR, LV, SB, K, HO, OSB, s_ptr)
 
+    tune_host = T.tune_host_pipeline(ctx, e2e_step, limbs - 1, B, reps=1)
     e2e_step()
     torch.cuda.synchronize()
     e_steps = max(1, min(args.steps, 5))
@@ -371,6 +375,8 @@ def run_gpu(args):
                    "poly_degree": n, "limbs": limbs, "aux_limbs": aux, "prime_bits": 50,
                    "gadget": "balanced base-2^30", "digits": digits, "batch": B,
                    "parallelism": f"replicas x{world}",
+                   "autotune": {"device": tune_dev["choice"], "host": tune_host["choice"],
+                                "cached": bool(tune_dev["cached"])},
                    "l2": "no flush: each step reads ~%.1f GB of inputs and key (L2 129 MB)"
                          % ((B * 4 * limbs + digits * 2 * (limbs + aux)) * n * 8 / 1e9)},
         "per_op": {"value": round(per_op_value, 3), "unit": UNIT,

@@ -291,7 +291,8 @@ void keyswitch_core(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, u
     while (b < J) {
       int e = b + 1;
       while (e < J && jobs[e].key->wdata == jobs[b].key->wdata) ++e;
-      wide_mac(c->wp, D, (int)jobs[b].key->digits, total, (const uint2*)jobs[b].key->wdata, dt, acc, b, e - b, s);
+      wide_mac(c->wp, D, (int)jobs[b].key->digits, total, (const uint2*)jobs[b].key->wdata, dt, acc, b, e - b,
+               c->mac_bc, s);
       launch_check("wide mac");
       b = e;
     }
@@ -405,7 +406,7 @@ void mult_relin_group(rc_context* c, const std::vector<int>& idx, const rc_ciphe
   const int limbs = lhs[idx[0]].level + 1;
   require(limbs > 1, "rescale requires at least two levels");
   const size_t pl = (size_t)limbs * c->N;
-  const int CH = MAXP / 2;
+  const int CH = c->ks_jobs;
   for (size_t b = 0; b < idx.size(); b += CH) {
     const int J = (int)std::min<size_t>(CH, idx.size() - b);
     std::vector<KsJob> jobs(J);
@@ -526,7 +527,9 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
     std::vector<PrimeConst> pcs(P);
     // bound (in multiples of q) of a forward-NTT output fed to the key product:
     // 2q per stage above q when lazy, 4q otherwise
-    const uint64_t out_bound = c->lazy ? (uint64_t)(2 * c->log_n + 1) : 4;
+    // bound of a forward-transform output in units of q for either butterfly mode (the mode can be changed
+    // later with rc_tune_set), so the key-product chunk below stays valid
+    const uint64_t out_bound = std::max<uint64_t>(2 * c->log_n + 1, 4);
     std::vector<Twiddle> twf((size_t)P * N), twi((size_t)P * N);
     for (int i = 0; i < P; ++i) {
       const uint64_t q = c->mod[i];
@@ -791,12 +794,48 @@ extern "C" int rc_decomp_digits(const rc_context* c, int32_t level, uint32_t* di
   });
 }
 
+extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
+  return guarded([&] {
+    require(c && name, "arguments must not be null");
+    const std::string n(name);
+    if (n == "ks_jobs") {
+      require(value >= 1 && value <= MAXP / 2, "ks_jobs must be in 1..32");
+      c->ks_jobs = value;
+    } else if (n == "mac_bc") {
+      require(value == 1 || value == 2 || value == 4 || value == 8, "mac_bc must be 1, 2, 4 or 8");
+      c->mac_bc = value;
+    } else if (n == "host_chunk") {
+      require(value >= 1, "host_chunk must be positive");
+      c->host_chunk = value;
+    } else if (n == "lazy_ntt") {
+      bool ok = true;
+      for (uint64_t q : c->mod) ok = ok && q < (1ull << 58);
+      require(!value || ok, "lazy_ntt needs every prime below 2^58");
+      c->lazy = value != 0;
+    } else {
+      fail(RC_ERR_INVALID_ARGUMENT, "unknown tunable " + n);
+    }
+  });
+}
+
+extern "C" int rc_tune_get(const rc_context* c, const char* name, int32_t* value) {
+  return guarded([&] {
+    require(c && name && value, "arguments must not be null");
+    const std::string n(name);
+    if (n == "ks_jobs") *value = c->ks_jobs;
+    else if (n == "mac_bc") *value = c->mac_bc;
+    else if (n == "host_chunk") *value = c->host_chunk;
+    else if (n == "lazy_ntt") *value = c->lazy ? 1 : 0;
+    else fail(RC_ERR_INVALID_ARGUMENT, "unknown tunable " + n);
+  });
+}
+
 extern "C" int rc_reserve(rc_context* c, int32_t max_level, uint32_t max_batch, void* stream) {
   return guarded([&] {
     require(c != nullptr, "context must not be null");
     const int limbs = max_level + 1;
     const LevelInfo& li = level_info(c, limbs);
-    const int J = (int)std::min<uint32_t>(max_batch ? max_batch : 1, MAXP / 2);
+    const int J = (int)std::min<uint32_t>(max_batch ? max_batch : 1, (uint32_t)c->ks_jobs);
     const int D = li.digits + 4;
     const size_t pl = (size_t)limbs * c->N;
     size_t need = align_up(std::max(ks_ws_bytes(c, J, limbs, c->K, D), tensor_ws_bytes(c, std::min(J, MAXP / 4), limbs)),
@@ -1305,9 +1344,9 @@ extern "C" int rc_relinearize_batch(rc_context* c, uint32_t count, const rc_ciph
     for (auto& g : groups) {
       const int limbs = g.first.first + 1;
       const size_t pl = (size_t)limbs * c->N;
-      for (size_t b = 0; b < g.second.size(); b += MAXP / 2) {
+      for (size_t b = 0; b < g.second.size(); b += c->ks_jobs) {
         std::vector<KsJob> jobs;
-        for (size_t k = b; k < g.second.size() && k < b + MAXP / 2; ++k) {
+        for (size_t k = b; k < g.second.size() && k < b + c->ks_jobs; ++k) {
           const int i = g.second[k];
           jobs.push_back(KsJob{qct[i].data + 2 * pl, keys[i], qct[i].data, qct[i].data + pl, out[i].data,
                                out[i].data + pl});
@@ -1339,9 +1378,9 @@ extern "C" int rc_relinearize_rescale_batch(rc_context* c, uint32_t count, const
       const int limbs = g->first.first + 1;
       const size_t pl = (size_t)limbs * c->N, po = (size_t)(limbs - 1) * c->N;
       const int drop = floor_log2(c->mod[limbs - 1]);
-      for (size_t b = 0; b < g->second.size(); b += MAXP / 2) {
+      for (size_t b = 0; b < g->second.size(); b += c->ks_jobs) {
         std::vector<KsJob> jobs;
-        for (size_t k = b; k < g->second.size() && k < b + MAXP / 2; ++k) {
+        for (size_t k = b; k < g->second.size() && k < b + c->ks_jobs; ++k) {
           const int i = g->second[k];
           jobs.push_back(KsJob{qct[i].data + 2 * pl, keys[i], qct[i].data, qct[i].data + pl, out[i].data,
                                out[i].data + po});
@@ -1418,9 +1457,9 @@ extern "C" int rc_rotate_batch(rc_context* c, uint32_t count, const rc_ciphertex
       const int limbs = g.first.first.first + 1;
       const uint64_t gi = galois_inverse(c, g.first.first.second);
       const size_t pl = (size_t)limbs * c->N;
-      for (size_t b = 0; b < g.second.size(); b += MAXP / 2) {
+      for (size_t b = 0; b < g.second.size(); b += c->ks_jobs) {
         std::vector<KsJob> jobs;
-        for (size_t k = b; k < g.second.size() && k < b + MAXP / 2; ++k) {
+        for (size_t k = b; k < g.second.size() && k < b + c->ks_jobs; ++k) {
           const int i = g.second[k];
           require(out[i].data != ct[i].data, "rotate output must not alias its input");
           jobs.push_back(KsJob{ct[i].data + pl, keys[i], ct[i].data, nullptr, out[i].data, out[i].data + pl});
@@ -1462,7 +1501,7 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
       hp = p.get();
     }
     hp->next = 0;
-    int chunk = 8;  // jobs per pipeline stage
+    int chunk = c->host_chunk;  // jobs per pipeline stage
     if (const char* e = getenv("RNSCKKS_HOST_CHUNK")) chunk = std::max(1, atoi(e));
     const uint32_t nchunks = (count + chunk - 1) / chunk;
     auto in_elems = [&](uint32_t i) { return (size_t)2 * (levels[i] + 1) * c->N; };

@@ -91,6 +91,10 @@ struct rc_context {
   std::map<cudaStream_t, std::unique_ptr<rc::Workspace>> ws;
   std::map<cudaStream_t, std::unique_ptr<rc::HostPipe>> pipes;  // per caller stream
   size_t scratch_budget = size_t(256) << 20;
+  // tunables (rc_tune_set): results never depend on them
+  int ks_jobs = 32;     // jobs per key-switch launch (one key read serves them), <= MAXP / 2
+  int mac_bc = 8;       // most jobs per CTA of the wide key product (1, 2, 4 or 8)
+  int host_chunk = 8;   // jobs per stage of the pipelined host-buffer entry
 
   rc::NttArgs ntt() const {
     rc::NttArgs a;

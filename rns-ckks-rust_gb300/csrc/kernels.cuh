@@ -188,7 +188,7 @@ bool wide_digit_transforms(const WidePrimes& w, int D, int jobs, const int32_t* 
 // acc[b][c][j][pair][N] (NTT domain, reduced) for jobs b0..b0+nb-1 sharing the
 // tiled key kwt[j][pair][x/32][digit][c][32]
 void wide_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt, uint2* acc,
-              int b0, int nb, cudaStream_t s);
+              int b0, int nb, int bc_max, cudaStream_t s);
 // inverse transforms of `polys` consecutive [pair][N] polynomials, in place
 bool wide_inverse(const WidePrimes& w, uint2* data, int polys, cudaStream_t s);
 // coefficient-form key [digits][2][limbs][N] (residues mod the scheme primes) ->

@@ -445,17 +445,18 @@ bool wide_digit_transforms(const WidePrimes& w, int D, int jobs, const int32_t* 
 }
 
 void wide_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt, uint2* acc,
-              int b0, int nb, cudaStream_t s) {
+              int b0, int nb, int bc_max, cudaStream_t s) {
   ProfScope p("wide_mac", s);
+  const int want = nb < bc_max ? nb : bc_max;  // jobs per CTA: the group size, at most bc_max
   if (D > 64) {  // folded sums; at most 4 jobs per CTA keep the fold within the register budget
-    if (nb <= 1) launch_w_mac<1, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
-    else if (nb <= 2) launch_w_mac<2, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
+    if (want <= 1) launch_w_mac<1, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
+    else if (want <= 2) launch_w_mac<2, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
     else launch_w_mac<4, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
     return;
   }
-  if (nb <= 1) launch_w_mac<1, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
-  else if (nb <= 2) launch_w_mac<2, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
-  else if (nb <= 4) launch_w_mac<4, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
+  if (want <= 1) launch_w_mac<1, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
+  else if (want <= 2) launch_w_mac<2, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
+  else if (want <= 4) launch_w_mac<4, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
   else launch_w_mac<8, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
 }
 
