@@ -349,7 +349,7 @@ def run_gpu(args):
     def e2e_step():
         C.call("rc_mult_relinearized_batch_host", ctx.handle, B, HL, HR, LV, SB, K, HO, OSB, s_ptr)
 
-    tune_host = T.tune_host_pipeline(ctx, e2e_step, limbs - 1, B, reps=1)
+    tune_host = T.tune_host_pipeline(ctx, e2e_step, limbs - 1, B, reps=3)
     e2e_step()
     torch.cuda.synchronize()
     e_steps = max(1, min(args.steps, 5))
@@ -397,9 +397,15 @@ def run_gpu(args):
         per_launch_ms = st["ms"] / st["launches"]
         ab = algorithmic_bytes(name, B * args.steps, n, limbs, aux, digits, st["launches"])
         achieved = (ab / (per_launch_ms / 1e3) / 1e9) if ab else None
+        traffic = None  # DRAM bytes per launch from the committed ncu summary, when it covers this shape
+        tpath = ROOT / "profiles" / "dram_traffic_n16_l24.json"
+        if tpath.exists() and n == 65536 and limbs == 24:
+            t = json.loads(tpath.read_text()).get(name)
+            if t and t["jobs_per_launch"] * st["launches"] == B * args.steps:
+                traffic = t["bytes_per_launch"]
         result["roofline"] = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1) if achieved else None,
                               "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
-                              "peak_kind": peak_kind, "traffic": None,
+                              "peak_kind": peak_kind, "traffic": traffic,
                               "share": round(st["ms"] / sum(v["ms"] for v in prof.values()), 4)}
     share = min(B, JOBS_PER_LAUNCH)
     hm = hmult_algorithmic_bytes(n, limbs, aux, digits, share)
