@@ -441,6 +441,7 @@ def run_gpu(args):
         # (128 quadratic ciphertexts, limbs 8..24, CUDA graph); reported beside the headline, untimed by it
         result["ntt_microbench"] = ntt_microbench(C, ctx, params, peak, args.seed)
         result["mixed_level_relin"] = mixed_level_relin(C, ctx, params, load_oracle(), args.seed)
+        result["bsgs_matvec"] = bsgs_matvec_bench(pkg, C, args.seed)
         result["serving"] = serving_bench(pkg, C, args.seed)
     if rank == 0:
         print(json.dumps(result), flush=True)
@@ -557,6 +558,53 @@ def mixed_level_relin(C, ctx, params, O, seed, count=128, reps=3):
     del graph, quads, outs, keys
     torch.cuda.synchronize()
     return res
+
+
+def bsgs_matvec_bench(pkg, C, seed, batch=32, dim=128, reps=2):
+    """Rotation-heavy BSGS packed-diagonal matvec: N=2^15 (2^14 slots), 16 limbs, a 128x128 matrix with N(0,1)
+    entries encoded by diagonals, times encrypted vectors with slots uniform in [-1,1] (tiled with period 128),
+    Galois keys from the seed, a batch of 32 independent matvecs per call.  The crate's BSGS split is
+    ceil(sqrt(128)) = 12 baby steps and 11 giant steps (linear_transform.rs:152-158), used here as is.
+    Decoded error against the FP64 matvec."""
+    import torch
+    from rnsckks_gb300 import algorithms as A
+    P = pkg.params
+    rng = np.random.default_rng(seed)
+    ctx = C.RnsCkksContext(P.scheme_params(15, 16, 2, 40))
+    kp = ctx.keygen(64, C.Sampler(seed + 5))
+    matrix = rng.standard_normal((dim, dim))
+    vectors = [rng.uniform(-1, 1, dim) for _ in range(batch)]
+    cts = [ctx.encrypt(ctx.encode_real(A.repeat_real_vector_blocks(v, ctx.num_slots())), kp.public_key,
+                       C.Sampler(seed + 50 + i)) for i, v in enumerate(vectors)]
+    t0 = time.perf_counter()
+    keys = A.generate_packed_diagonal_rotation_keys(ctx, kp.secret_key, kp.public_key, cts[0].level, dim)
+    t_keys = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    diags = A.pack_diagonal_plaintexts(ctx, matrix, cts[0].level, cts[0].scale_bits)
+    torch.cuda.synchronize()
+    t_pack = time.perf_counter() - t0
+    out = A.apply_diagonal_linear_transform_batch(ctx, cts, diags, keys)  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        out = A.apply_diagonal_linear_transform_batch(ctx, cts, diags, keys)
+    torch.cuda.synchronize()
+    secs = (time.perf_counter() - t0) / reps
+    single_t0 = time.perf_counter()
+    one = A.apply_diagonal_linear_transform(ctx, cts[0], diags, keys)
+    torch.cuda.synchronize()
+    single = time.perf_counter() - single_t0
+    err = 0.0
+    for i in (0, batch - 1):
+        dec = ctx.decode_real_at_scale(ctx.decrypt(out[i], kp.secret_key), out[i].scale_bits)
+        err = max(err, float(np.max(np.abs(dec[:dim] - matrix @ vectors[i]))))
+    same = bool(np.array_equal(one.numpy(), out[0].numpy()))
+    return {"workload": "BSGS packed-diagonal matvec 128x128, N=2^15, 16 limbs, batch 32",
+            "baby_giant": [A.diagonal_transform_bsgs_baby_step(dim), -(-dim // A.diagonal_transform_bsgs_baby_step(dim))],
+            "rotation_keys": len(keys.by_step), "matvecs_per_s": round(batch / secs, 2),
+            "ms_per_batch": round(secs * 1e3, 2), "single_matvec_ms": round(single * 1e3, 2),
+            "batched_vs_single": round(single * batch / secs, 2), "batch_equals_single": same,
+            "decoded_max_abs_err": err, "key_generation_s": round(t_keys, 2), "diagonal_packing_s": round(t_pack, 2)}
 
 
 def serving_bench(pkg, C, seed, jobs_per_phase=240):
