@@ -51,11 +51,9 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
 #pragma unroll
   for (int w = 0; w < WM; ++w) X[w] = 0;
   double kf = 0.0;
-  u64 r_next = in[sidx];  // the next limb's residue is requested one limb ahead
   for (int l = 0; l < limbs; ++l) {
     const u64 q = pc[l].q;
-    u64 r = r_next;
-    if (l + 1 < limbs) r_next = in[(u64)(l + 1) * N + sidx];
+    u64 r = in[(u64)l * N + sidx];
     if (neg && r) r = q - r;
     const u64 y = mul_shoup(r, dt.qhat_inv[l], dt.qhat_inv_s[l], q);
     kf += (double)y * dt.inv_q[l];
@@ -656,9 +654,7 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
     return val;
   };
 
-  // limbs are independent: unrolled so that several limbs' loads are in flight at once
   if (!f.rescale) {
-#pragma unroll 4
     for (int i = 0; i < lq; ++i) dst[(size_t)i * N + x] = limb_value(i);
     return;
   }
@@ -667,7 +663,6 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
   const u64 ql = f.pc[last].q, half = ql >> 1;
   const bool pos = vl <= half;
   const u64 dist = pos ? vl : ql - vl;
-#pragma unroll 4
   for (int i = 0; i < last; ++i) {
     const PrimeConst& c = f.pc[i];
     const u64 d = dist < c.q ? dist : mul_shoup(dist, 1, c.one_s, c.q);
