@@ -1,8 +1,8 @@
 """Autotuner for the library's launch-shape tunables.
 
 The tunables (`rc_tune_set`: jobs per key-switch launch, jobs per CTA of the key product, the forward
-butterfly mode, jobs per stage of the host pipeline) change how work is split into launches, never the
-results.  The tuner times each candidate on synthetic inputs of the caller's shape (ring degree, level,
+butterfly mode, the fused tensor pass, jobs per stage of the host pipeline) change how work is split into
+launches, never the results.  The tuner times each candidate on synthetic inputs of the caller's shape (ring degree, level,
 batch), keeps the fastest, applies it to the context and caches the choice per (device, shape) in a JSON
 file, so later runs apply it without measuring.
 """
@@ -18,7 +18,8 @@ from typing import Callable, Dict, Iterable, List, Optional, Sequence
 
 from ._lib import RcCiphertext, call
 
-DEVICE_CANDIDATES: Dict[str, Sequence[int]] = {"ks_jobs": (8, 16, 32), "mac_bc": (4, 8), "lazy_ntt": (0, 1)}
+DEVICE_CANDIDATES: Dict[str, Sequence[int]] = {"ks_jobs": (8, 16, 32), "mac_bc": (4, 8), "lazy_ntt": (0, 1),
+                                               "fuse_tensor": (0, 1)}
 HOST_CANDIDATES: Dict[str, Sequence[int]] = {"host_chunk": (4, 8, 16)}
 
 

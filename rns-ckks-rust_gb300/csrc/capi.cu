@@ -365,11 +365,15 @@ void tensor_core(rc_context* c, const std::vector<const uint64_t*>& lhs, const s
     src.p[4 * j + 3] = const_cast<uint64_t*>(rhs[j]) + pl;
     for (int k = 0; k < 4; ++k) dst.p[4 * j + k] = fw + (4 * j + k) * pl;
   }
-  ntt_forward(c->ntt(), src, dst, 4 * J, limbs, qmap(c, limbs), s);
-  launch_check("ntt_forward(tensor)");
   PtrTab o3{};
   for (int j = 0; j < J; ++j)
     for (int k = 0; k < 3; ++k) o3.p[3 * j + k] = quad[j] + k * pl;
+  if (c->fuse_tensor && tensor_fused(c->ntt(), c->d_pc, src, dst, o3, J, limbs, qmap(c, limbs), s)) {
+    launch_check("tensor (fused)");
+    return;
+  }
+  ntt_forward(c->ntt(), src, dst, 4 * J, limbs, qmap(c, limbs), s);
+  launch_check("ntt_forward(tensor)");
   tensor_ntt(c->d_pc, dst, o3, J, limbs, c->N, s);
   launch_check("tensor");
   ntt_inverse(c->ntt(), o3, o3, 3 * J, limbs, qmap(c, limbs), s);
@@ -807,6 +811,8 @@ extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
     } else if (n == "host_chunk") {
       require(value >= 1, "host_chunk must be positive");
       c->host_chunk = value;
+    } else if (n == "fuse_tensor") {
+      c->fuse_tensor = value != 0;
     } else if (n == "lazy_ntt") {
       bool ok = true;
       for (uint64_t q : c->mod) ok = ok && q < (1ull << 58);
@@ -826,6 +832,7 @@ extern "C" int rc_tune_get(const rc_context* c, const char* name, int32_t* value
     else if (n == "mac_bc") *value = c->mac_bc;
     else if (n == "host_chunk") *value = c->host_chunk;
     else if (n == "lazy_ntt") *value = c->lazy ? 1 : 0;
+    else if (n == "fuse_tensor") *value = c->fuse_tensor ? 1 : 0;
     else fail(RC_ERR_INVALID_ARGUMENT, "unknown tunable " + n);
   });
 }

@@ -95,6 +95,7 @@ struct rc_context {
   int ks_jobs = 32;     // jobs per key-switch launch (one key read serves them), <= MAXP / 2
   int mac_bc = 8;       // most jobs per CTA of the wide key product (1, 2, 4 or 8)
   int host_chunk = 8;   // jobs per stage of the pipelined host-buffer entry
+  bool fuse_tensor = true;  // forward rows + tensor + inverse rows in one kernel
 
   rc::NttArgs ntt() const {
     rc::NttArgs a;

@@ -54,6 +54,12 @@ void ntt_forward(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int pol
 void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
                  cudaStream_t s);
 
+// Coefficient-form ciphertext pairs in4.p[4j..4j+3] = (a0, a1, b0, b1) -> coefficient-form
+// out3.p[3j..3j+2] = (a0 b0, a0 b1 + a1 b0, a1 b1): forward column phase into work4, one fused kernel for the
+// forward row phase, the NTT-domain tensor and the inverse row phase, then the inverse column phase in place.
+// False (nothing launched) if N is not supported (log N outside 12..16).
+bool tensor_fused(const NttArgs& a, const PrimeConst* pc, const PtrTab& in4, const PtrTab& work4,
+                  const PtrTab& out3, int jobs, int limbs, LimbMap map, cudaStream_t s);
 // row phase of the forward transform only (input: column-phase output)
 void ntt_forward_rows(const NttArgs& a, const PtrTab& data, int polys, int limbs, LimbMap map, cudaStream_t s);
 

@@ -359,6 +359,108 @@ inline int threads_for(int work) {
 
 }  // namespace
 
+namespace {
+
+// Tensor product between the two phases of the transforms: for job blockIdx.z and limb blockIdx.y, each warp
+// takes a row of the column-phase outputs of (a0, a1, b0, b1), finishes their forward transforms (row
+// phase), forms d0 = a0 b0, d1 = a0 b1 + a1 b0, d2 = a1 b1 in the NTT domain and runs the row phase of the
+// inverse transforms of d0, d1, d2, so the NTT-domain values never leave the SM.  in4.p[4j..4j+3] ->
+// out3.p[3j..3j+2]; the inverse column phase follows.
+template <int M1, int M2, bool LAZY>
+__global__ __launch_bounds__(32 * ROW_WARPS) void k_tensor_rows(NttArgs a, PtrTab in4, PtrTab out3, LimbMap map) {
+  using G = core::Geo<M2>;
+  constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = ROW_WARPS * G::SUBS;
+  __shared__ u64 bufs[ROWS * G::STRIDE];
+  __shared__ __align__(16) Twiddle twf[ROWS][N2];
+  __shared__ __align__(16) Twiddle twi[ROWS][N2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / G::LANES, l = lane % G::LANES;
+  const int row0 = blockIdx.x * ROWS;
+  const int limb = blockIdx.y, job = blockIdx.z;
+  const int prime = map.prime(limb);
+  const PrimeConst& pc = a.pc[prime];
+  const u64 q = pc.q;
+  const int rl = warp * G::SUBS + sub, row = row0 + rl;
+  const size_t off = (size_t)limb * N + (size_t)row * N2;
+  u64 v[4][8];  // a0, a1, b0, b1: requested before the twiddle tables so both latencies overlap
+#pragma unroll
+  for (int p = 0; p < 4; ++p)
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[p][k] = in4.p[4 * job + p][off + core::first_idx<M2>(l, k)];
+  const Twiddle* tf = a.tw_fwd + (size_t)prime * N;
+  const Twiddle* ti = a.tw_inv + (size_t)prime * N;
+#pragma unroll 1
+  for (int rr = 0; rr < ROWS; ++rr) {
+    core::stage_twiddles_async<M2>(twf[rr], tf, (u64)(N1 + row0 + rr), threadIdx.x, 32 * ROW_WARPS);
+    core::stage_twiddles_async<M2>(twi[rr], ti, (u64)(N1 + row0 + rr), threadIdx.x, 32 * ROW_WARPS);
+  }
+  core::cp_async_wait_all();
+  __syncthreads();
+  u64* buf = bufs + rl * G::STRIDE;
+#pragma unroll
+  for (int p = 0; p < 4; ++p) {
+    core::fwd_sub<M2, LAZY>(v[p], buf, l, twf[rl], q);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[p][k] = reduce_out<LAZY>(v[p][k], pc);
+  }
+  // d1 into a0's registers after d0 and d2 take b0's and b1's
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    const u64 a0 = v[0][k], a1 = v[1][k], b0 = v[2][k], b1 = v[3][k];
+    U128 t = mul_wide(a0, b1);
+    add_to(t, mul_wide(a1, b0));
+    v[0][k] = barrett_reduce(t, pc);
+    v[2][k] = mul_mod(a0, b0, pc);
+    v[3][k] = mul_mod(a1, b1, pc);
+  }
+  const int src_of[3] = {2, 0, 3};  // d0, d1, d2
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    core::inv_sub<M2>(v[src_of[d]], buf, l, twi[rl], q);
+    u64* o = out3.p[3 * job + d] + off;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) o[core::first_idx<M2>(l, k)] = v[src_of[d]][k];
+  }
+}
+
+}  // namespace
+
+bool tensor_fused(const NttArgs& a, const PrimeConst* pc, const PtrTab& in4, const PtrTab& work4,
+                  const PtrTab& out3, int jobs, int limbs, LimbMap map, cudaStream_t s) {
+  if (jobs <= 0) return true;
+  switch (a.log_n) {
+#define RC_TENSOR(LN, A, B)                                                                                   \
+  case LN: {                                                                                                  \
+    constexpr int N2 = 1 << B, N1 = 1 << A;                                                                   \
+    dim3 g1(N2 / ColTile<A>::COLS, limbs, 4 * jobs), g2(N1 / (ROW_WARPS * core::Geo<B>::SUBS), limbs, jobs);    \
+    dim3 g3(N2 / ColTile<A>::COLS, limbs, 3 * jobs);                                                          \
+    {                                                                                                         \
+      ProfScope p("ntt_fwd_cols", s);                                                                         \
+      if (a.lazy) k_cols_f<A, B, true, true><<<g1, 256, 0, s>>>(a, in4, work4, map);                          \
+      else k_cols_f<A, B, false, true><<<g1, 256, 0, s>>>(a, in4, work4, map);                                \
+    }                                                                                                         \
+    {                                                                                                         \
+      ProfScope p("tensor_rows", s);                                                                          \
+      if (a.lazy) k_tensor_rows<A, B, true><<<g2, 32 * ROW_WARPS, 0, s>>>(a, work4, out3, map);               \
+      else k_tensor_rows<A, B, false><<<g2, 32 * ROW_WARPS, 0, s>>>(a, work4, out3, map);                     \
+    }                                                                                                         \
+    {                                                                                                         \
+      ProfScope p("ntt_inv_cols", s);                                                                         \
+      k_cols_f<A, B, false, false><<<g3, 256, 0, s>>>(a, out3, out3, map);                                    \
+    }                                                                                                         \
+    return true;                                                                                              \
+  }
+    RC_TENSOR(12, 6, 6)
+    RC_TENSOR(13, 6, 7)
+    RC_TENSOR(14, 7, 7)
+    RC_TENSOR(15, 7, 8)
+    RC_TENSOR(16, 8, 8)
+#undef RC_TENSOR
+    default:
+      return false;
+  }
+}
+
 void ntt_forward(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
                  cudaStream_t s) {
   if (polys <= 0 || limbs <= 0) return;

@@ -98,3 +98,22 @@ def test_graph_capture_refuses_to_grow_scratch(env):
     torch.cuda.synchronize()
     with pytest.raises(C.RcError, match="non-default stream"):
         ctx.capture_graph(lambda: None)
+
+
+def test_fused_and_unfused_tensor_agree(env):
+    C, ctx, params, keys, host_keys, O = env
+    rng = np.random.default_rng(9)
+    q, n = params.q_moduli(), params.poly_degree
+    mk = lambda: C.RnsCiphertext(C.to_device(np.stack([np.stack([rng.integers(0, m, n, dtype=np.uint64) for m in q])
+                                                       for _ in range(2)])), 40)
+    a, b = [mk() for _ in range(5)], [mk() for _ in range(5)]
+    import ctypes
+    got = {}
+    for fuse in (0, 1):
+        C.call("rc_tune_set", ctx.handle, b"fuse_tensor", fuse)
+        got[fuse] = ([x.numpy() for x in ctx.mult_relinearized_batch(a, b, [keys[len(q) - 1]] * 5)],
+                     ctx.mult(a[0], b[0]).numpy())
+    C.call("rc_tune_set", ctx.handle, b"fuse_tensor", 1)
+    for u, v in zip(got[0][0], got[1][0]):
+        assert np.array_equal(u, v)
+    assert np.array_equal(got[0][1], got[1][1])
