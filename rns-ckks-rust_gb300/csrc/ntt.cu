@@ -367,7 +367,8 @@ namespace {
 // inverse transforms of d0, d1, d2, so the NTT-domain values never leave the SM.  in4.p[4j..4j+3] ->
 // out3.p[3j..3j+2]; the inverse column phase follows.
 template <int M1, int M2, bool LAZY>
-__global__ __launch_bounds__(32 * ROW_WARPS) void k_tensor_rows(NttArgs a, PtrTab in4, PtrTab out3, LimbMap map) {
+__global__ __launch_bounds__(32 * ROW_WARPS, 3) void k_tensor_rows(NttArgs a, PtrTab in4, PtrTab out3,
+                                                                     LimbMap map) {
   using G = core::Geo<M2>;
   constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = ROW_WARPS * G::SUBS;
   __shared__ u64 bufs[ROWS * G::STRIDE];
@@ -382,11 +383,17 @@ __global__ __launch_bounds__(32 * ROW_WARPS) void k_tensor_rows(NttArgs a, PtrTa
   const u64 q = pc.q;
   const int rl = warp * G::SUBS + sub, row = row0 + rl;
   const size_t off = (size_t)limb * N + (size_t)row * N2;
-  u64 v[4][8];  // a0, a1, b0, b1: requested before the twiddle tables so both latencies overlap
+  const u64* a0p = in4.p[4 * job + 0] + off;
+  const u64* a1p = in4.p[4 * job + 1] + off;
+  const u64* b0p = in4.p[4 * job + 2] + off;
+  const u64* b1p = in4.p[4 * job + 3] + off;
+  // a0 and b0 are requested before the twiddle tables, so both latencies overlap
+  u64 x[8], y[8], z[8];
 #pragma unroll
-  for (int p = 0; p < 4; ++p)
-#pragma unroll
-    for (int k = 0; k < 8; ++k) v[p][k] = in4.p[4 * job + p][off + core::first_idx<M2>(l, k)];
+  for (int k = 0; k < 8; ++k) {
+    x[k] = a0p[core::first_idx<M2>(l, k)];
+    y[k] = b0p[core::first_idx<M2>(l, k)];
+  }
   const Twiddle* tf = a.tw_fwd + (size_t)prime * N;
   const Twiddle* ti = a.tw_inv + (size_t)prime * N;
 #pragma unroll 1
@@ -397,30 +404,42 @@ __global__ __launch_bounds__(32 * ROW_WARPS) void k_tensor_rows(NttArgs a, PtrTa
   core::cp_async_wait_all();
   __syncthreads();
   u64* buf = bufs + rl * G::STRIDE;
+  auto fwd = [&](u64(&v)[8]) {
+    core::fwd_sub<M2, LAZY>(v, buf, l, twf[rl], q);
 #pragma unroll
-  for (int p = 0; p < 4; ++p) {
-    core::fwd_sub<M2, LAZY>(v[p], buf, l, twf[rl], q);
-#pragma unroll
-    for (int k = 0; k < 8; ++k) v[p][k] = reduce_out<LAZY>(v[p][k], pc);
-  }
-  // d1 into a0's registers after d0 and d2 take b0's and b1's
-#pragma unroll
-  for (int k = 0; k < 8; ++k) {
-    const u64 a0 = v[0][k], a1 = v[1][k], b0 = v[2][k], b1 = v[3][k];
-    U128 t = mul_wide(a0, b1);
-    add_to(t, mul_wide(a1, b0));
-    v[0][k] = barrett_reduce(t, pc);
-    v[2][k] = mul_mod(a0, b0, pc);
-    v[3][k] = mul_mod(a1, b1, pc);
-  }
-  const int src_of[3] = {2, 0, 3};  // d0, d1, d2
-#pragma unroll
-  for (int d = 0; d < 3; ++d) {
-    core::inv_sub<M2>(v[src_of[d]], buf, l, twi[rl], q);
+    for (int k = 0; k < 8; ++k) v[k] = reduce_out<LAZY>(v[k], pc);
+  };
+  auto inv_store = [&](u64(&v)[8], int d) {
+    core::inv_sub<M2>(v, buf, l, twi[rl], q);
     u64* o = out3.p[3 * job + d] + off;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) o[core::first_idx<M2>(l, k)] = v[src_of[d]][k];
+    for (int k = 0; k < 8; ++k) o[core::first_idx<M2>(l, k)] = v[k];
+  };
+  // three rows live at a time: (a0, b0) -> d0; b1 -> a0 b1; a1 -> d1 = a0 b1 + a1 b0 and d2 = a1 b1
+  fwd(x);
+  fwd(y);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) z[k] = mul_mod(x[k], y[k], pc);  // d0
+  u64 w[8];
+#pragma unroll
+  for (int k = 0; k < 8; ++k) w[k] = b1p[core::first_idx<M2>(l, k)];  // b1, in flight during d0's inverse
+  inv_store(z, 0);
+  fwd(w);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) x[k] = mul_mod(x[k], w[k], pc);  // a0 b1
+#pragma unroll
+  for (int k = 0; k < 8; ++k) z[k] = a1p[core::first_idx<M2>(l, k)];  // a1
+  fwd(z);
+#pragma unroll
+  for (int k = 0; k < 8; ++k) {
+    U128 t = mul_wide(z[k], y[k]);  // a1 b0
+    t.lo += x[k];
+    t.hi += t.lo < x[k] ? 1ull : 0ull;
+    x[k] = barrett_reduce(t, pc);  // d1
+    y[k] = mul_mod(z[k], w[k], pc);  // d2
   }
+  inv_store(x, 1);
+  inv_store(y, 2);
 }
 
 }  // namespace
