@@ -231,6 +231,91 @@ bool use_wide(const rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, i
   return wide_applies(c, qlimbs, K, D);
 }
 
+// ---- the wide key switch in phases, for pipelines that interleave other work between them ----
+// Per-batch device buffers of the wide path: int32 digits, digit transforms and products of J jobs, plus a
+// column-phase work area for up to `chunk` jobs at a time.
+struct WideKs {
+  int J = 0, D = 0, total = 0, qlimbs = 0, K = 0, chunk = 0;
+  int32_t* digits = nullptr;
+  uint2 *work = nullptr, *dt = nullptr, *acc = nullptr;
+};
+
+size_t wide_ks_bytes(const rc_context* c, int J, int chunk, int qlimbs, int K, int D) {
+  const size_t N = c->N;
+  return align_up((size_t)J * D * N * 4, 256) + arena_size_u64((size_t)chunk * D * 2 * N) +
+         arena_size_u64((size_t)J * D * 2 * N) + arena_size_u64((size_t)J * 2 * (qlimbs + K) * 2 * N) + 1024;
+}
+
+WideKs wide_ks_layout(rc_context* c, Arena& ar, int J, int chunk, int qlimbs, int K, int D) {
+  WideKs w;
+  w.J = J, w.D = D, w.qlimbs = qlimbs, w.K = K, w.total = qlimbs + K, w.chunk = chunk;
+  const size_t N = c->N;
+  w.digits = ar.take<int32_t>((size_t)J * D * N);
+  w.work = ar.take<uint2>((size_t)chunk * D * 2 * N);
+  w.dt = ar.take<uint2>((size_t)J * D * 2 * N);
+  w.acc = ar.take<uint2>((size_t)J * 2 * w.total * 2 * N);
+  return w;
+}
+
+// decomposition and digit transforms of jobs [b0, b0 + n) (n <= chunk)
+void wide_ks_prepare(rc_context* c, const WideKs& w, const std::vector<KsJob>& jobs, int b0, int n, uint64_t g_inv,
+                     cudaStream_t s) {
+  const size_t N = c->N;
+  PtrTab src{};
+  for (int j = 0; j < n; ++j) src.p[j] = const_cast<uint64_t*>(jobs[b0 + j].poly);
+  decompose(c->d_pc, level_info(c, w.qlimbs).dt, src, n, w.qlimbs, w.D, w.digits + (size_t)b0 * w.D * N, g_inv,
+            c->log_n, s);
+  launch_check("decompose");
+  require(wide_digit_transforms(c->wp, w.D, n, w.digits + (size_t)b0 * w.D * N, w.work,
+                                w.dt + (size_t)b0 * 2 * w.D * N, s),
+          "internal: wide transforms unsupported");
+  launch_check("wide digit transforms");
+}
+
+// key products of all jobs, one launch per run of jobs sharing a key
+void wide_ks_mac(rc_context* c, const WideKs& w, const std::vector<KsJob>& jobs, cudaStream_t s) {
+  int b = 0;
+  while (b < w.J) {
+    int e = b + 1;
+    while (e < w.J && jobs[e].key->wdata == jobs[b].key->wdata) ++e;
+    wide_mac(c->wp, w.D, (int)jobs[b].key->digits, w.total, (const uint2*)jobs[b].key->wdata, w.dt, w.acc, b, e - b,
+             c->mac_bc, s);
+    launch_check("wide mac");
+    b = e;
+  }
+}
+
+// inverse transforms and finalize (ModDown, addends, optional rescale) of jobs [b0, b0 + n)
+void wide_ks_finish(rc_context* c, const WideKs& w, const std::vector<KsJob>& jobs, int b0, int n, uint64_t g_inv,
+                    bool rescale, cudaStream_t s) {
+  const size_t N = c->N;
+  uint2* acc = w.acc + (size_t)b0 * 2 * w.total * 2 * N;
+  require(wide_inverse(c->wp, acc, n * 2 * w.total, s), "internal: wide transforms unsupported");
+  launch_check("wide inverse transforms");
+  FinalizeArgs f;
+  f.pc = c->d_pc;
+  f.md = c->md;
+  f.rt = c->rt;
+  f.L = c->L;
+  f.n = c->N;
+  f.log_n = c->log_n;
+  f.qlimbs = w.qlimbs;
+  f.K = w.K;
+  f.rescale = rescale ? 1 : 0;
+  f.add_g_inv = g_inv;
+  f.wide = 1;
+  f.wt = c->wide;
+  PtrTab add{}, out{};
+  for (int j = 0; j < n; ++j) {
+    add.p[2 * j] = const_cast<uint64_t*>(jobs[b0 + j].add0);
+    add.p[2 * j + 1] = const_cast<uint64_t*>(jobs[b0 + j].add1);
+    out.p[2 * j] = jobs[b0 + j].out0;
+    out.p[2 * j + 1] = jobs[b0 + j].out1;
+  }
+  finalize(f, (const uint64_t*)acc, add, out, n, s);
+  launch_check("finalize");
+}
+
 // Runs keyswitch for `jobs` jobs at `qlimbs` limbs (all keys of the same kind);
 // the result is finalized with addends, optional automorphism on the addend and
 // optional rescale.  g_inv: automorphism applied to the keyswitched polynomial
@@ -250,7 +335,14 @@ void keyswitch_core(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, u
     if (!K) require((int)j.key->digits == D, "internal: mixed digit counts in one keyswitch batch");
   }
   const int N = c->N, total = qlimbs + K;
-  const bool wide = use_wide(c, jobs, qlimbs, K, D);
+  if (use_wide(c, jobs, qlimbs, K, D)) {
+    Arena aw(ws);
+    const WideKs w = wide_ks_layout(c, aw, J, J, qlimbs, K, D);
+    wide_ks_prepare(c, w, jobs, 0, J, g_inv, s);
+    wide_ks_mac(c, w, jobs, s);
+    wide_ks_finish(c, w, jobs, 0, J, g_inv, rescale, s);
+    return;
+  }
   const size_t scratch_elems = ks_scratch_elems(c, J, total, D);
   Arena ar(ws);
   int32_t* digits = ar.take<int32_t>((size_t)J * D * N);
@@ -270,7 +362,7 @@ void keyswitch_core(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, u
   f.K = K;
   f.rescale = rescale ? 1 : 0;
   f.add_g_inv = g_inv;
-  f.wide = wide ? 1 : 0;
+  f.wide = 0;
   f.wt = c->wide;
   PtrTab add{}, out{};
   for (int j = 0; j < J; ++j) {
@@ -278,29 +370,6 @@ void keyswitch_core(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, u
     add.p[2 * j + 1] = const_cast<uint64_t*>(jobs[j].add1);
     out.p[2 * j] = jobs[j].out0;
     out.p[2 * j + 1] = jobs[j].out1;
-  }
-
-  if (wide) {
-    uint2* work = ar.take<uint2>((size_t)J * D * 2 * N);
-    uint2* dt = ar.take<uint2>((size_t)J * D * 2 * N);
-    uint2* acc = ar.take<uint2>((size_t)J * 2 * total * 2 * N);
-    require(wide_digit_transforms(c->wp, D, J, digits, work, dt, s), "internal: wide transforms unsupported");
-    launch_check("wide digit transforms");
-    // jobs sharing a key run together so that each key word is read once per group
-    int b = 0;
-    while (b < J) {
-      int e = b + 1;
-      while (e < J && jobs[e].key->wdata == jobs[b].key->wdata) ++e;
-      wide_mac(c->wp, D, (int)jobs[b].key->digits, total, (const uint2*)jobs[b].key->wdata, dt, acc, b, e - b,
-               c->mac_bc, s);
-      launch_check("wide mac");
-      b = e;
-    }
-    require(wide_inverse(c->wp, acc, J * 2 * total, s), "internal: wide transforms unsupported");
-    launch_check("wide inverse transforms");
-    finalize(f, (const uint64_t*)acc, add, out, J, s);
-    launch_check("finalize");
-    return;
   }
 
   for (auto& j : jobs) require(j.key->data != nullptr, "internal: keyswitch key has no per-limb form");
@@ -813,6 +882,8 @@ extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
       c->host_chunk = value;
     } else if (n == "fuse_tensor") {
       c->fuse_tensor = value != 0;
+    } else if (n == "host_phased") {
+      c->host_phased = value != 0;
     } else if (n == "lazy_ntt") {
       bool ok = true;
       for (uint64_t q : c->mod) ok = ok && q < (1ull << 58);
@@ -833,6 +904,7 @@ extern "C" int rc_tune_get(const rc_context* c, const char* name, int32_t* value
     else if (n == "host_chunk") *value = c->host_chunk;
     else if (n == "lazy_ntt") *value = c->lazy ? 1 : 0;
     else if (n == "fuse_tensor") *value = c->fuse_tensor ? 1 : 0;
+    else if (n == "host_phased") *value = c->host_phased ? 1 : 0;
     else fail(RC_ERR_INVALID_ARGUMENT, "unknown tunable " + n);
   });
 }
@@ -1482,6 +1554,115 @@ extern "C" int rc_rotate_batch(rc_context* c, uint32_t count, const rc_ciphertex
 // =========================================================================
 // host-buffer entry points
 // =========================================================================
+// Host-buffer batch of up to ks_jobs same-level jobs on the wide key-switch path, in phases so that one key
+// read serves the whole batch while transfers still overlap the arithmetic: the inputs of all chunks are
+// copied in back to back; each chunk's tensor, decomposition and digit transforms start as soon as its
+// inputs have landed; one key-product pass covers all jobs; then each chunk's inverse transforms and
+// finalize run and its results are copied out while the next chunk finishes.  Returns false (nothing
+// done) when the batch does not fit this form.
+static bool mult_relin_host_phased(rc_context* c, HostPipe* hp, uint32_t count, const uint64_t* const* lhs,
+                                   const uint64_t* const* rhs, const int32_t* levels, const int32_t* scale_bits,
+                                   const rc_ksk* const* keys, uint64_t* const* out, int32_t* out_scale_bits,
+                                   cudaStream_t s, int chunk) {
+  const int level = levels[0];
+  if (count > (uint32_t)c->ks_jobs) return false;
+  for (uint32_t i = 0; i < count; ++i)
+    if (levels[i] != level) return false;
+  const int limbs = level + 1;
+  if (limbs < 2) return false;
+  const rc_ksk* k0 = keys[0];
+  for (uint32_t i = 0; i < count; ++i) {
+    require(keys[i] != nullptr, "keyswitch key must not be null");
+    check_key_for(c, keys[i], limbs);
+    if ((keys[i]->aux != 0) != (k0->aux != 0) || !keys[i]->wdata) return false;
+  }
+  const int K = k0->aux ? c->K : 0;
+  const int D = ks_digits(c, k0, limbs);
+  for (uint32_t i = 0; i < count; ++i)
+    if (!K && (int)keys[i]->digits != D) return false;
+  if (!wide_applies(c, limbs, K, D)) return false;
+  const int J = (int)count;
+  chunk = std::max(1, std::min(chunk, MAXP / 4));
+  const size_t N = c->N, pl = (size_t)limbs * N, po = (size_t)(limbs - 1) * N;
+  // staging: inputs [J][lhs, rhs][2][limbs][N], outputs [J][2][limbs-1][N]
+  const size_t stage = ((size_t)J * 4 * pl + (size_t)J * 2 * po) * 8;
+  if (!hp->slot[0] || hp->slot[0]->bytes < stage) {
+    for (cudaStream_t st : {hp->in[0], hp->in[1], hp->comp, hp->out})
+      cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    hp->slot[0].reset();
+    hp->slot[0].reset(new DevBuf(stage));
+  }
+  uint64_t* in_dev = (uint64_t*)hp->slot[0]->p;
+  uint64_t* out_dev = in_dev + (size_t)J * 4 * pl;
+  const size_t tbytes = tensor_ws_bytes(c, chunk, limbs);
+  char* ws = (char*)ws_device(c, hp->comp, arena_size_u64((size_t)3 * J * pl) + align_up(tbytes, 256) +
+                                               wide_ks_bytes(c, J, chunk, limbs, K, D) + 1024);
+  Arena ar(ws);
+  uint64_t* quads = ar.take<uint64_t>((size_t)3 * J * pl);
+  char* tscr = ar.take<char>(tbytes);
+  const WideKs w = wide_ks_layout(c, ar, J, chunk, limbs, K, D);
+
+  cudaEvent_t start = hp->event();
+  cuda_check(cudaEventRecord(start, s), "cudaEventRecord");
+  for (cudaStream_t st : {hp->in[0], hp->in[1], hp->comp, hp->out})
+    cuda_check(cudaStreamWaitEvent(st, start, 0), "cudaStreamWaitEvent");
+  const int nchunks = (J + chunk - 1) / chunk;
+  std::vector<cudaEvent_t> in_done(2 * nchunks), comp_done(nchunks);
+  for (int k = 0; k < nchunks; ++k) {  // every chunk's inputs, back to back on two copy streams
+    for (int j = k * chunk; j < std::min(J, (k + 1) * chunk); ++j) {
+      cuda_check(cudaMemcpyAsync(in_dev + (size_t)j * 4 * pl, lhs[j], 2 * pl * 8, cudaMemcpyHostToDevice, hp->in[0]),
+                 "H2D");
+      cuda_check(cudaMemcpyAsync(in_dev + (size_t)j * 4 * pl + 2 * pl, rhs[j], 2 * pl * 8, cudaMemcpyHostToDevice,
+                                 hp->in[1]),
+                 "H2D");
+    }
+    for (int q = 0; q < 2; ++q) {
+      in_done[2 * k + q] = hp->event();
+      cuda_check(cudaEventRecord(in_done[2 * k + q], hp->in[q]), "cudaEventRecord");
+    }
+  }
+  std::vector<KsJob> jobs(J);
+  for (int j = 0; j < J; ++j) {
+    uint64_t* qd = quads + (size_t)j * 3 * pl;
+    jobs[j] = KsJob{qd + 2 * pl, keys[j], qd, qd + pl, out_dev + (size_t)j * 2 * po, out_dev + (size_t)j * 2 * po + po};
+  }
+  for (int k = 0; k < nchunks; ++k) {
+    const int b0 = k * chunk, n = std::min(J, b0 + chunk) - b0;
+    for (int q = 0; q < 2; ++q) cuda_check(cudaStreamWaitEvent(hp->comp, in_done[2 * k + q], 0), "wait");
+    std::vector<const uint64_t*> Lp(n), Rp(n);
+    std::vector<uint64_t*> Q(n);
+    for (int j = 0; j < n; ++j) {
+      Lp[j] = in_dev + (size_t)(b0 + j) * 4 * pl;
+      Rp[j] = Lp[j] + 2 * pl;
+      Q[j] = quads + (size_t)(b0 + j) * 3 * pl;
+    }
+    tensor_core(c, Lp, Rp, Q, limbs, tscr, hp->comp);
+    wide_ks_prepare(c, w, jobs, b0, n, 0, hp->comp);
+  }
+  wide_ks_mac(c, w, jobs, hp->comp);
+  const int drop = floor_log2(c->mod[limbs - 1]);
+  for (int k = 0; k < nchunks; ++k) {
+    const int b0 = k * chunk, n = std::min(J, b0 + chunk) - b0;
+    wide_ks_finish(c, w, jobs, b0, n, 0, true, hp->comp);
+    comp_done[k] = hp->event();
+    cuda_check(cudaEventRecord(comp_done[k], hp->comp), "cudaEventRecord");
+    cuda_check(cudaStreamWaitEvent(hp->out, comp_done[k], 0), "wait");
+    for (int j = b0; j < b0 + n; ++j) {
+      cuda_check(cudaMemcpyAsync(out[j], out_dev + (size_t)j * 2 * po, 2 * po * 8, cudaMemcpyDeviceToHost, hp->out),
+                 "D2H");
+      if (out_scale_bits) {
+        const int sb = scale_bits[j] + scale_bits[j] - drop;  // mult_relinearized, context/ops.rs:124-133
+        out_scale_bits[j] = sb < 0 ? 0 : sb;
+      }
+    }
+  }
+  cudaEvent_t fin = hp->event();
+  cuda_check(cudaEventRecord(fin, hp->out), "cudaEventRecord");
+  cuda_check(cudaStreamWaitEvent(s, fin, 0), "wait");
+  cuda_check(cudaStreamSynchronize(hp->out), "cudaStreamSynchronize");
+  return true;
+}
+
 // Host-buffer batch: the jobs run in chunks through a three-stage pipeline on internal streams (copy in
 // on two streams, compute, copy out) with two device staging slots, so that transfers overlap the
 // arithmetic.  The whole call is ordered after earlier work on `stream` and returns when the results are
@@ -1510,6 +1691,9 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
     hp->next = 0;
     int chunk = c->host_chunk;  // jobs per pipeline stage
     if (const char* e = getenv("RNSCKKS_HOST_CHUNK")) chunk = std::max(1, atoi(e));
+    if (c->host_phased &&
+        mult_relin_host_phased(c, hp, count, lhs, rhs, levels, scale_bits, keys, out, out_scale_bits, s, chunk))
+      return;
     const uint32_t nchunks = (count + chunk - 1) / chunk;
     auto in_elems = [&](uint32_t i) { return (size_t)2 * (levels[i] + 1) * c->N; };
     auto out_elems = [&](uint32_t i) { return (size_t)2 * levels[i] * c->N; };

@@ -96,6 +96,7 @@ struct rc_context {
   int mac_bc = 8;       // most jobs per CTA of the wide key product (1, 2, 4 or 8)
   int host_chunk = 8;   // jobs per stage of the pipelined host-buffer entry
   bool fuse_tensor = true;  // forward rows + tensor + inverse rows in one kernel
+  bool host_phased = true;  // host-buffer batches: one key read for the batch, transfers overlapped per chunk
 
   rc::NttArgs ntt() const {
     rc::NttArgs a;

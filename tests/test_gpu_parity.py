@@ -276,15 +276,19 @@ def test_host_entry_point_equals_device_path(C, pkg):
 
 
 def test_pipelined_host_batch_equals_device_path(C, pkg):
-    # more jobs than one pipeline chunk, mixed levels, repeated calls reusing the staging slots
+    # more jobs than one pipeline chunk, mixed levels, repeated calls reusing the staging slots; N=2^12 so the
+    # wide key product (and with it the phased form for one-level batches) is in use
     import ctypes
-    params = pkg.params.hybrid_params(11, 5, 2, 50)
+    params = pkg.params.hybrid_params(12, 5, 2, 50)
     ctx = C.RnsCkksContext(params)
     n, q = params.poly_degree, params.q_moduli()
     rng = np.random.default_rng(45)
     keys = {lv: ctx.upload_keyswitch_key(_random_key(rng, params, lv + 1, True)[0], lv, 2) for lv in (2, 3, 4)}
-    for count in (21, 3):
-        levels = [int(x) for x in rng.integers(2, 5, count)]
+    cases = [(21, None), (3, None), (11, 4), (11, 4)]  # mixed levels (chunked pipeline); one level (phased)
+    for case, (count, fixed) in enumerate(cases):
+        if case == 3:  # the same batch with the phased form switched off
+            C.call("rc_tune_set", ctx.handle, b"host_phased", 0)
+        levels = [int(x) for x in rng.integers(2, 5, count)] if fixed is None else [fixed] * count
         A = [np.ascontiguousarray(rand_ct(rng, q[: lv + 1], n)) for lv in levels]
         B = [np.ascontiguousarray(rand_ct(rng, q[: lv + 1], n)) for lv in levels]
         outs = [np.zeros((2, lv, n), dtype=np.uint64) for lv in levels]
