@@ -376,7 +376,9 @@ def run_gpu(args):
                    "gadget": "balanced base-2^30", "digits": digits, "batch": B,
                    "parallelism": f"replicas x{world}",
                    "autotune": {"device": tune_dev["choice"], "host": tune_host["choice"],
-                                "cached": bool(tune_dev["cached"])},
+                                "cached": bool(tune_dev["cached"]),
+                                "host_trials_ms": {"/".join(f"{k}={v}" for k, v in sorted(t["config"].items())): t["ms"]
+                                                   for t in tune_host.get("trials", [])}},
                    "l2": "no flush: each step reads ~%.1f GB of inputs and key (L2 129 MB)"
                          % ((B * 4 * limbs + digits * 2 * (limbs + aux)) * n * 8 / 1e9)},
         "per_op": {"value": round(per_op_value, 3), "unit": UNIT,
