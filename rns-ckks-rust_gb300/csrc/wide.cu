@@ -237,7 +237,7 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 
 template <int BC, bool FOLD>
-__global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 4 ? 2 : (BC >= 2 ? 3 : 4)) void k_w_mac(
+__global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC >= 2 ? 4 : 5))) void k_w_mac(
     WidePrimes w, int D, int key_digits, int total, const uint2* __restrict__ kwt, const uint2* __restrict__ dtt,
     uint2* acc, int b0, int nb) {
   extern __shared__ uint2 dsm[];  // [BC][D][32] digit transforms, then [warps][W_PF][2][32] key ring
