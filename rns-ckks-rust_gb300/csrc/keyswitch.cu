@@ -32,12 +32,33 @@ namespace {
 template <int WM>
 __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int limbs, int D, int32_t* digits,
                             u64 g_inv, int log_n) {
+  // the tables every thread walks (CRT words of Q/q_l, (Q/q_l)^-1, q_l, Q, floor(Q/2)) staged in shared memory
+  extern __shared__ u64 dsm_tab[];
+  const int W = dt.W;
+  u64* s_qhat = dsm_tab;                       // [limbs][W]
+  u64* s_q = s_qhat + (size_t)limbs * W;       // [limbs]
+  u64* s_hinv = s_q + limbs;                   // [limbs]
+  u64* s_hinv_s = s_hinv + limbs;              // [limbs]
+  double* s_invq = reinterpret_cast<double*>(s_hinv_s + limbs);  // [limbs]
+  u64* s_Q = reinterpret_cast<u64*>(s_invq + limbs);  // [W]
+  u64* s_half = s_Q + W;                       // [W]
+  for (int e = threadIdx.x; e < limbs * W; e += blockDim.x) s_qhat[e] = dt.qhat[e];
+  for (int e = threadIdx.x; e < limbs; e += blockDim.x) {
+    s_q[e] = pc[e].q;
+    s_hinv[e] = dt.qhat_inv[e];
+    s_hinv_s[e] = dt.qhat_inv_s[e];
+    s_invq[e] = dt.inv_q[e];
+  }
+  for (int e = threadIdx.x; e < W; e += blockDim.x) {
+    s_Q[e] = dt.Q[e];
+    s_half[e] = dt.halfQ[e];
+  }
+  __syncthreads();
   const u64 N = 1ull << log_n;
   const u64 x = blockIdx.x * (u64)blockDim.x + threadIdx.x;
   if (x >= N) return;
   const int job = blockIdx.y;
   const u64* in = src.p[job];
-  const int W = dt.W;
 
   u64 sidx = x;
   bool neg = false;
@@ -52,12 +73,12 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
   for (int w = 0; w < WM; ++w) X[w] = 0;
   double kf = 0.0;
   for (int l = 0; l < limbs; ++l) {
-    const u64 q = pc[l].q;
+    const u64 q = s_q[l];
     u64 r = in[(u64)l * N + sidx];
     if (neg && r) r = q - r;
-    const u64 y = mul_shoup(r, dt.qhat_inv[l], dt.qhat_inv_s[l], q);
-    kf += (double)y * dt.inv_q[l];
-    const u64* qh = dt.qhat + (size_t)l * W;
+    const u64 y = mul_shoup(r, s_hinv[l], s_hinv_s[l], q);
+    kf += (double)y * s_invq[l];
+    const u64* qh = s_qhat + (size_t)l * W;
     u64 carry = 0;
 #pragma unroll
     for (int w = 0; w < WM; ++w) {
@@ -79,7 +100,7 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
 #pragma unroll
     for (int w = 0; w < WM; ++w) {
       if (w < W) {
-        U128 p = mul_wide(k, dt.Q[w]);
+        U128 p = mul_wide(k, s_Q[w]);
         u64 sub = p.lo + carry;
         carry = p.hi + (sub < carry ? 1ull : 0ull);
         u64 xw = X[w];
@@ -105,7 +126,7 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
 #pragma unroll
     for (int w = 0; w < WM; ++w) {
       if (w < W) {
-        u64 qw = dt.Q[w];
+        u64 qw = s_Q[w];
         if (!subtract) {
           u64 s = X[w] + qw;
           u64 c1 = s < qw ? 1ull : 0ull;
@@ -137,9 +158,9 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
     return res > 0 || (or_equal && res == 0);
   };
   if (top_neg()) add_Q(false);
-  else if (greater_than(dt.Q, true)) add_Q(true);
+  else if (greater_than(s_Q, true)) add_Q(true);
   // centre: X > floor(Q/2) -> X - Q
-  if (greater_than(dt.halfQ, false)) add_Q(true);
+  if (greater_than(s_half, false)) add_Q(true);
   const u64 ext = top_neg() ? ~0ull : 0ull;
 
   // balanced base-2^30 digits of the two's complement value
@@ -552,20 +573,52 @@ bool digit_dispatch(const KsArgs& a, const int32_t* digits, const KeyTab& kt, u6
 // ---------------------------------------------------------------------------
 constexpr int KMAX = 8;
 
+// Per-limb constants of k_finalize, staged once per CTA in shared memory (every thread of a CTA walks the
+// same limbs): FT fields per limb, then K Montgomery weights and their Shoup companions.
+enum FT { FT_Q, FT_ONE_S, FT_C01, FT_C01_S, FT_AMOD, FT_PINV, FT_PINV_S, FT_PMOD, FT_RINV, FT_RINV_S, FT_N };
+__host__ __device__ __forceinline__ int ft_stride(int K) { return FT_N + 2 * K; }
+
 __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab out) {
+  extern __shared__ u64 tab[];  // [lq + K][FT_N + 2K]
   const u64 N = 1ull << f.log_n;
+  const int lq = f.qlimbs, K = f.K;
+  const LimbMap fmap{lq, f.L};
+  const int st = ft_stride(K);
+  for (int e = threadIdx.x; e < (lq + K) * st; e += blockDim.x) {
+    const int i = e / st, fld = e - i * st;
+    const int t = fmap.prime(i);
+    const bool q_limb = i < lq;
+    u64 v = 0;
+    switch (fld) {
+      case FT_Q: v = f.pc[t].q; break;
+      case FT_ONE_S: v = f.pc[t].one_s; break;
+      case FT_C01: v = f.wide ? f.wt.c01_mod_t[t] : 0; break;
+      case FT_C01_S: v = f.wide ? f.wt.c01_mod_t_s[t] : 0; break;
+      case FT_AMOD: v = f.wide ? f.wt.A_mod_t[t] : 0; break;
+      case FT_PINV: v = (K && q_limb) ? f.md.pinv[i] : 0; break;
+      case FT_PINV_S: v = (K && q_limb) ? f.md.pinv_s[i] : 0; break;
+      case FT_PMOD: v = (K && q_limb) ? f.md.pmod[i] : 0; break;
+      case FT_RINV: v = (f.rescale && i < lq - 1) ? f.rt.inv[(size_t)(lq - 1) * f.L + i] : 0; break;
+      case FT_RINV_S: v = (f.rescale && i < lq - 1) ? f.rt.inv_s[(size_t)(lq - 1) * f.L + i] : 0; break;
+      default: {
+        const int k = fld - FT_N;
+        v = !q_limb ? 0 : (k < K ? f.md.mk[(size_t)i * K + k] : f.md.mk_s[(size_t)i * K + (k - K)]);
+      }
+    }
+    tab[e] = v;
+  }
+  __syncthreads();
   const u64 x = blockIdx.x * (u64)blockDim.x + threadIdx.x;
   if (x >= N) return;
   const int comp = blockIdx.y & 1, job = blockIdx.y >> 1;
-  const int lq = f.qlimbs, K = f.K;
   const int wf = f.wide ? 2 : 1;  // 8-byte words per limb and coefficient in acc
   const u64* a = acc + ((size_t)job * 2 + comp) * (size_t)(lq + K) * N * wf;
   const uint2* a2 = reinterpret_cast<const uint2*>(a);
-  const LimbMap fmap{lq, f.L};
-  auto accv = [&](int j) -> u64 {  // value of limb j (prime fmap.prime(j)) at x
+  auto T = [&](int i, int fld) -> u64 { return tab[i * st + fld]; };
+  auto accv = [&](int j) -> u64 {  // value of limb j at x
     if (!f.wide) return a[(size_t)j * N + x];
-    const int t = fmap.prime(j);
-    return wide_crt_mod(a2[(size_t)j * 2 * N + x], a2[((size_t)j * 2 + 1) * N + x], f.wt, t, f.pc[t]);
+    return wide_crt_mod_c(a2[(size_t)j * 2 * N + x], a2[((size_t)j * 2 + 1) * N + x], f.wt, T(j, FT_Q),
+                          T(j, FT_ONE_S), T(j, FT_C01), T(j, FT_C01_S), T(j, FT_AMOD));
   };
   const u64* add = addend.p[2 * job + comp];
   u64* dst = out.p[2 * job + comp];
@@ -585,14 +638,14 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
 #pragma unroll
     for (int k = 0; k < KMAX; ++k) {
       if (k < K) {
-        const PrimeConst& pk = f.pc[f.L + k];
+        const u64 pq = T(lq + k, FT_Q), pone = T(lq + k, FT_ONE_S);
         u64 val = accv(lq + k);
 #pragma unroll
         for (int t = 0; t < KMAX; ++t) {
           if (t < k) {
-            const u64 vr = v[t] < pk.q ? v[t] : mul_shoup(v[t], 1, pk.one_s, pk.q);
-            val = sub_mod(val, vr, pk.q);
-            val = mul_shoup(val, f.md.p_garner[k * K + t], f.md.p_garner_s[k * K + t], pk.q);
+            const u64 vr = v[t] < pq ? v[t] : mul_shoup(v[t], 1, pone, pq);
+            val = sub_mod(val, vr, pq);
+            val = mul_shoup(val, f.md.p_garner[k * K + t], f.md.p_garner_s[k * K + t], pq);
           }
         }
         v[k] = val;
@@ -605,7 +658,7 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
 #pragma unroll
     for (int k = KMAX - 1; k >= 0; --k) {
       if (k < K) {
-        const u64 pk = f.pc[f.L + k].q;
+        const u64 pk = T(lq + k, FT_Q);
         u64 carry = v[k];
 #pragma unroll
         for (int w = 0; w < KMAX; ++w) {
@@ -629,27 +682,24 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
   }
 
   auto limb_value = [&](int i) -> u64 {
-    const PrimeConst& c = f.pc[i];
+    const u64 q = T(i, FT_Q);
     u64 val = accv(i);
     if (K > 0) {
-      // centred [x]_P mod q_i
-      // Shoup's product is exact for any 64-bit multiplicand, so v[k] (< p_k) needs no reduction mod q_i
+      // centred [x]_P mod q_i; Shoup's product is exact for any 64-bit multiplicand, so v[k] (< p_k) needs
+      // no reduction mod q_i
       u64 conv = 0;
 #pragma unroll
       for (int k = 0; k < KMAX; ++k) {
-        if (k < K) {
-          const u64 t = mul_shoup(v[k], f.md.mk[(size_t)i * K + k], f.md.mk_s[(size_t)i * K + k], c.q);
-          conv = add_mod(conv, t, c.q);
-        }
+        if (k < K) conv = add_mod(conv, mul_shoup(v[k], T(i, FT_N + k), T(i, FT_N + K + k), q), q);
       }
-      if (pneg) conv = sub_mod(conv, f.md.pmod[i], c.q);
-      val = sub_mod(val, conv, c.q);
-      val = mul_shoup(val, f.md.pinv[i], f.md.pinv_s[i], c.q);
+      if (pneg) conv = sub_mod(conv, T(i, FT_PMOD), q);
+      val = sub_mod(val, conv, q);
+      val = mul_shoup(val, T(i, FT_PINV), T(i, FT_PINV_S), q);
     }
     if (add) {
       u64 av = add[(size_t)i * N + addsrc];
-      if (addneg && av) av = c.q - av;
-      val = add_mod(val, av, c.q);
+      if (addneg && av) av = q - av;
+      val = add_mod(val, av, q);
     }
     return val;
   };
@@ -660,16 +710,15 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
   }
   const int last = lq - 1;
   const u64 vl = limb_value(last);
-  const u64 ql = f.pc[last].q, half = ql >> 1;
+  const u64 ql = T(last, FT_Q), half = ql >> 1;
   const bool pos = vl <= half;
   const u64 dist = pos ? vl : ql - vl;
   for (int i = 0; i < last; ++i) {
-    const PrimeConst& c = f.pc[i];
-    const u64 d = dist < c.q ? dist : mul_shoup(dist, 1, c.one_s, c.q);
-    u64 cd = pos ? d : (d == 0 ? 0 : c.q - d);
-    u64 num = sub_mod(limb_value(i), cd, c.q);
-    size_t k = (size_t)last * f.L + i;
-    dst[(size_t)i * N + x] = mul_shoup(num, f.rt.inv[k], f.rt.inv_s[k], c.q);
+    const u64 q = T(i, FT_Q);
+    const u64 d = dist < q ? dist : mul_shoup(dist, 1, T(i, FT_ONE_S), q);
+    const u64 cd = pos ? d : (d == 0 ? 0 : q - d);
+    const u64 num = sub_mod(limb_value(i), cd, q);
+    dst[(size_t)i * N + x] = mul_shoup(num, T(i, FT_RINV), T(i, FT_RINV_S), q);
   }
 }
 
@@ -704,14 +753,15 @@ void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int
   const int W = dt.W;
   ProfScope p("decompose", s);
   // the word count is a template parameter (register-resident value); the closest instance above W runs
-  if (W <= 4) k_decompose<4><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
-  else if (W <= 8) k_decompose<8><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
-  else if (W <= 12) k_decompose<12><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
-  else if (W <= 16) k_decompose<16><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
-  else if (W <= 20) k_decompose<20><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
-  else if (W <= 24) k_decompose<24><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
-  else if (W <= 32) k_decompose<32><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
-  else k_decompose<64><<<g, threads, 0, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  const size_t smem = ((size_t)limbs * W + 4 * (size_t)limbs + 2 * (size_t)W) * sizeof(u64);
+  if (W <= 4) k_decompose<4><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  else if (W <= 8) k_decompose<8><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  else if (W <= 12) k_decompose<12><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  else if (W <= 16) k_decompose<16><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  else if (W <= 20) k_decompose<20><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  else if (W <= 24) k_decompose<24><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  else if (W <= 32) k_decompose<32><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  else k_decompose<64><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
 }
 
 void digit_ntt_mac(const KsArgs& a, const int32_t* digits, const u64* const* keys, int jobs, u64* acc,
@@ -761,7 +811,8 @@ void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const
   const int threads = N < 128 ? N : 128;
   dim3 g((N + threads - 1) / threads, 2 * jobs);
   ProfScope p("finalize", s);
-  k_finalize<<<g, threads, 0, s>>>(f, acc, addend, out);
+  const size_t smem = (size_t)(f.qlimbs + f.K) * ft_stride(f.K) * sizeof(u64);
+  k_finalize<<<g, threads, smem, s>>>(f, acc, addend, out);
 }
 
 void key_to_device_form(const NttArgs& a, const PrimeConst* pc, const u64* src, u64* dst, int digits, int limbs,
