@@ -60,8 +60,6 @@ void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int pol
 // False (nothing launched) if N is not supported (log N outside 12..16).
 bool tensor_fused(const NttArgs& a, const PrimeConst* pc, const PtrTab& in4, const PtrTab& work4,
                   const PtrTab& out3, int jobs, int limbs, LimbMap map, cudaStream_t s);
-// row phase of the forward transform only (input: column-phase output)
-void ntt_forward_rows(const NttArgs& a, const PtrTab& data, int polys, int limbs, LimbMap map, cudaStream_t s);
 
 // ---- elementwise / scheme kernels (ops.cu) ----
 enum class EwOp { Add, Sub, Mul };

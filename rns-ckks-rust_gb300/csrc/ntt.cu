@@ -516,26 +516,4 @@ void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int pol
   }
 }
 
-void ntt_forward_rows(const NttArgs& a, const PtrTab& data, int polys, int limbs, LimbMap map, cudaStream_t s) {
-  if (polys <= 0 || limbs <= 0) return;
-  ProfScope p("ntt_fwd_rows", s);
-  switch (a.log_n) {
-#define RC_ROWS(LN, A, B)                                                                     \
-  case LN: {                                                                                  \
-    dim3 g((1 << A) / (ROW_WARPS * core::Geo<B>::SUBS), limbs, polys);                        \
-    if (a.lazy) k_rows_f<A, B, true, true><<<g, 32 * ROW_WARPS, 0, s>>>(a, data, data, map);  \
-    else k_rows_f<A, B, false, true><<<g, 32 * ROW_WARPS, 0, s>>>(a, data, data, map);        \
-    break;                                                                                    \
-  }
-    RC_ROWS(12, 6, 6)
-    RC_ROWS(13, 6, 7)
-    RC_ROWS(14, 7, 7)
-    RC_ROWS(15, 7, 8)
-    RC_ROWS(16, 8, 8)
-#undef RC_ROWS
-    default:
-      break;
-  }
-}
-
 }  // namespace rc
