@@ -156,6 +156,12 @@ int rc_mult_plain(rc_context* ctx, const rc_ciphertext* ct, const uint64_t* plai
 /* multiply_plain_rns: src/rns/ops.rs:54-66 (scale unchanged) */
 int rc_multiply_plain_rns(rc_context* ctx, const rc_ciphertext* ct, const uint64_t* plain, rc_ciphertext* out,
                           void* stream);
+/* `count` independent RnsCiphertext::add / multiply_plain_rns jobs in one call (same rules and messages as
+ * the single forms; jobs may mix levels). */
+int rc_add_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* lhs, const rc_ciphertext* rhs,
+                 rc_ciphertext* out, void* stream);
+int rc_multiply_plain_rns_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* ct,
+                                const uint64_t* const* plains, rc_ciphertext* out, void* stream);
 /* Sum over k of mult_plain(cts[k], plains[k]), the inner sum of the BSGS linear transform
  * (apply_giant_step_terms, src/ckks/bootstrapping/linear_transform.rs:234-252: mult_plain, context/ops.rs:20-30,
  * folded with RnsCiphertext::add, ciphertexts.rs:60-69).  All cts share level and scale; out gets the level and

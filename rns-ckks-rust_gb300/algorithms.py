@@ -99,7 +99,7 @@ def _fold(ctx, accs, active_slots, rotation_keys, missing):
         if key is None:
             _panic(missing.format(step))
         rotated = _rotate_all(ctx, accs, [key] * len(accs))
-        accs = [ctx.add(a, r) for a, r in zip(accs, rotated)]
+        accs = ctx.add_batch(accs, rotated)
     return accs
 
 
@@ -315,16 +315,17 @@ def apply_diagonal_linear_transform_batch(ctx: RnsCkksContext, ciphertexts: Sequ
     for k, r in zip(order, rot):
         i, g = where[k]
         inner[i][g] = r
-    out = []
-    for i in range(len(cts)):
-        terms = [t for t in inner[i] if t is not None]
-        if not terms:
-            _panic("diagonal transform must contain at least one non-empty giant-step block")
-        acc = terms[0]
-        for t in terms[1:]:
-            acc = ctx.add(acc, t)
-        out.append(ctx.rescale(acc))
-    return out
+    # the adds of the reference's giant-step order, one batched call per giant step over all ciphertexts
+    terms = [[t for t in inner[i] if t is not None] for i in range(len(cts))]
+    if any(not t for t in terms):
+        _panic("diagonal transform must contain at least one non-empty giant-step block")
+    accs = [t[0] for t in terms]
+    for g in range(1, max(len(t) for t in terms)):
+        idx = [i for i in range(len(cts)) if g < len(terms[i])]
+        summed = ctx.add_batch([accs[i] for i in idx], [terms[i][g] for i in idx])
+        for i, v in zip(idx, summed):
+            accs[i] = v
+    return [ctx.rescale(a) for a in accs]
 
 
 # --------------------------------------------------------------------------------------------------------
@@ -422,16 +423,6 @@ class _Plains:
         return self.memo[key]
 
 
-def _lift_ciphertext_scale(ctx, pl: _Plains, ct: RnsCiphertext, target: int) -> RnsCiphertext:
-    """paterson_stockmeyer.rs:230-254: multiply by an encoded 1.0 at scale target - scale_bits."""
-    if ct.scale_bits > target:
-        _panic("cannot lower ciphertext scale with a plaintext-one lift")
-    if ct.scale_bits == target:
-        return ct
-    lifted = ctx.multiply_plain_rns(ct, pl.constant(1.0, ct.level, target - ct.scale_bits))
-    return RnsCiphertext(lifted.data, target, lifted.level)
-
-
 def _align_ciphertext_to_level(ct: RnsCiphertext, target_level: int) -> RnsCiphertext:
     """paterson_stockmeyer.rs:221-228."""
     if target_level > ct.level:
@@ -510,23 +501,33 @@ def paterson_stockmeyer_eval_batch(ctx: RnsCkksContext, ciphertexts: Sequence[Rn
     coeff_scale = working - in_scale
     if coeff_scale < 0:
         _panic("Paterson-Stockmeyer working scale must dominate the input ciphertext scale")
+    def lift_all(cs: List[RnsCiphertext], target: int) -> List[RnsCiphertext]:
+        """_lift_ciphertext_scale (paterson_stockmeyer.rs:230-254) over a batch that shares level and scale,
+        one batched call."""
+        if cs[0].scale_bits > target:
+            _panic("cannot lower ciphertext scale with a plaintext-one lift")
+        if cs[0].scale_bits == target:
+            return cs
+        one = pl.constant(1.0, cs[0].level, target - cs[0].scale_bits)
+        return [RnsCiphertext(x.data, target, x.level) for x in ctx.multiply_plain_rns_batch(cs, [one] * len(cs))]
+
     # precompute_baby_powers (146-173): note the crate lifts to the INPUT scale here
-    base = [_lift_ciphertext_scale(ctx, pl, ct, in_scale) for ct in cts]
+    base = lift_all(cts, in_scale)
     powers = [base]
     for _ in range(2, b + 1):
         prev = powers[-1]
-        aligned_prev = [_lift_ciphertext_scale(ctx, pl, p, in_scale) for p in prev]
+        aligned_prev = lift_all(prev, in_scale)
         aligned_base = [_align_ciphertext_to_level(x, p.level) for x, p in zip(base, prev)]
         nxt = _mult_relin_all(ctx, aligned_prev, aligned_base, relin_keys)
-        powers.append([_lift_ciphertext_scale(ctx, pl, x, in_scale) for x in nxt])
+        powers.append(lift_all(nxt, in_scale))
     giant = powers[-1]
     if giant[0].level + 1 < blocks:
         _panic("polynomial degree is too large for the available CKKS level budget")
     top = giant[0].level
 
-    def evaluate_block(i: int, block_index: int, target_level: int) -> RnsCiphertext:
-        """paterson_stockmeyer.rs:175-219."""
-        acc = _constant_ciphertext(ctx, pl, target_level, working, 0.0)
+    def evaluate_block(block_index: int, target_level: int) -> List[RnsCiphertext]:
+        """paterson_stockmeyer.rs:175-219, every ciphertext of the batch per step."""
+        accs = [_constant_ciphertext(ctx, pl, target_level, working, 0.0) for _ in cts]
         for offset in range(b):
             k = block_index * b + offset
             if k >= len(coeffs):
@@ -535,25 +536,23 @@ def paterson_stockmeyer_eval_batch(ctx: RnsCkksContext, ciphertexts: Sequence[Rn
             if c == 0.0:
                 continue
             if offset == 0:
-                acc = _add_constant_term(ctx, pl, acc, c)
+                accs = [_add_constant_term(ctx, pl, a, c) for a in accs]
                 continue
-            power = powers[offset - 1][i]
-            aligned = _lift_ciphertext_scale(ctx, pl, _align_ciphertext_to_level(power, target_level),
-                                             power.scale_bits)
-            term = ctx.multiply_plain_rns(aligned, pl.constant(c, aligned.level, coeff_scale))
-            term = RnsCiphertext(term.data, aligned.scale_bits + coeff_scale, term.level)
-            acc = ctx.add(acc, term)
-        return acc
+            power = [p[offset - 1] for p in per_ct_powers]
+            aligned = lift_all([_align_ciphertext_to_level(x, target_level) for x in power], power[0].scale_bits)
+            plain = pl.constant(c, aligned[0].level, coeff_scale)
+            terms = [RnsCiphertext(t.data, aligned[0].scale_bits + coeff_scale, t.level)
+                     for t in ctx.multiply_plain_rns_batch(aligned, [plain] * len(aligned))]
+            accs = ctx.add_batch(accs, terms)
+        return accs
 
-    results = []
-    per_ct_blocks = [[evaluate_block(i, bi, top - (blocks - 1 - bi)) for bi in range(blocks)]
-                     for i in range(len(cts))]
-    result = [bl[-1] for bl in per_ct_blocks]
+    per_ct_powers = [[powers[e][i] for e in range(b)] for i in range(len(cts))]
+    blocks_out = [evaluate_block(bi, top - (blocks - 1 - bi)) for bi in range(blocks)]
+    result = blocks_out[-1]
     for bi in range(blocks - 2, -1, -1):
-        aligned_giant = [_lift_ciphertext_scale(ctx, pl, _align_ciphertext_to_level(gs, r.level), r.scale_bits)
-                         for gs, r in zip(giant, result)]
+        aligned_giant = lift_all([_align_ciphertext_to_level(gs, result[0].level) for gs in giant],
+                                 result[0].scale_bits)
         multiplied = _mult_relin_all(ctx, result, aligned_giant, relin_keys)
-        lifted = [_lift_ciphertext_scale(ctx, pl, m, r.scale_bits) for m, r in zip(multiplied, result)]
-        result = [ctx.add(x, bl[bi]) for x, bl in zip(lifted, per_ct_blocks)]
-    results = result
-    return results
+        lifted = lift_all(multiplied, result[0].scale_bits)
+        result = ctx.add_batch(lifted, blocks_out[bi])
+    return result

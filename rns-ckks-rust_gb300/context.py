@@ -600,6 +600,30 @@ class RnsCkksContext:
         call("rc_mult_plain", self.handle, ctypes.byref(ct.raw()), _ptr(plain.data), ctypes.byref(r), _stream())
         return RnsCiphertext(out, r.scale_bits, r.level)
 
+    def add_batch(self, lhs: Sequence[RnsCiphertext], rhs: Sequence[RnsCiphertext]) -> List[RnsCiphertext]:
+        """`add` of many independent pairs in one call (rc_add_batch)."""
+        n = len(lhs)
+        if n == 0:
+            return []
+        outs = [self._ct_out(2, a.level + 1) for a in lhs]
+        A = (RcCiphertext * n)(*[a.raw() for a in lhs])
+        B = (RcCiphertext * n)(*[b.raw() for b in rhs])
+        O = (RcCiphertext * n)(*[RcCiphertext(o.data_ptr(), 0, 0) for o in outs])
+        call("rc_add_batch", self.handle, n, A, B, O, _stream())
+        return [RnsCiphertext(o, O[i].scale_bits, O[i].level) for i, o in enumerate(outs)]
+
+    def multiply_plain_rns_batch(self, cts: Sequence[RnsCiphertext], plains: Sequence) -> List[RnsCiphertext]:
+        """`multiply_plain_rns` of many independent pairs in one call (rc_multiply_plain_rns_batch)."""
+        n = len(cts)
+        if n == 0:
+            return []
+        outs = [self._ct_out(2, c.level + 1) for c in cts]
+        C = (RcCiphertext * n)(*[c.raw() for c in cts])
+        P = (ctypes.c_void_p * n)(*[(p.data if isinstance(p, RnsPolynomial) else p).data_ptr() for p in plains])
+        O = (RcCiphertext * n)(*[RcCiphertext(o.data_ptr(), 0, 0) for o in outs])
+        call("rc_multiply_plain_rns_batch", self.handle, n, C, P, O, _stream())
+        return [RnsCiphertext(o, O[i].scale_bits, O[i].level) for i, o in enumerate(outs)]
+
     def multiply_plain_rns(self, ct: RnsCiphertext, plain: RnsPolynomial) -> RnsCiphertext:
         """src/rns/ops.rs:54-66 (scale unchanged)."""
         if plain.levels() != ct.level + 1:

@@ -1166,6 +1166,45 @@ extern "C" int rc_add(rc_context* c, const rc_ciphertext* a, const rc_ciphertext
   });
 }
 
+// Batched forms of add and multiply_plain_rns: `count` independent jobs in one call (the Python-side
+// algorithms and the server issue one call per step of a batch instead of one per job).
+extern "C" int rc_add_batch(rc_context* c, uint32_t count, const rc_ciphertext* a, const rc_ciphertext* b,
+                            rc_ciphertext* out, void* stream) {
+  return guarded([&] {
+    require(c && a && b && out, "arguments must not be null");
+    // jobs of one level go out in launches of up to MAXP/2 ciphertexts (two components each)
+    std::map<int, std::vector<uint32_t>> by_level;
+    for (uint32_t i = 0; i < count; ++i) {
+      require(out[i].data != nullptr, "arguments must not be null");
+      check_ct(c, &a[i], "lhs");
+      check_ct(c, &b[i], "rhs");
+      require(a[i].scale_bits == b[i].scale_bits, "ciphertexts must share the same scale to add");
+      require(a[i].level == b[i].level, "ciphertexts must be at the same level to add");
+      by_level[a[i].level].push_back(i);
+    }
+    for (auto& g : by_level) {
+      const int limbs = g.first + 1;
+      const size_t pl = (size_t)limbs * c->N;
+      for (size_t b0 = 0; b0 < g.second.size(); b0 += MAXP / 2) {
+        PtrTab x{}, y{}, o{};
+        int polys = 0;
+        for (size_t k = b0; k < g.second.size() && k < b0 + MAXP / 2; ++k) {
+          const uint32_t i = g.second[k];
+          for (int comp = 0; comp < 2; ++comp, ++polys) {
+            x.p[polys] = a[i].data + comp * pl;
+            y.p[polys] = b[i].data + comp * pl;
+            o.p[polys] = out[i].data + comp * pl;
+          }
+          out[i].level = a[i].level;
+          out[i].scale_bits = a[i].scale_bits;
+        }
+        ew_binary(EwOp::Add, c->d_pc, x, y, 0, o, polys, limbs, qmap(c, limbs), c->N, S(stream));
+        launch_check("add_batch");
+      }
+    }
+  });
+}
+
 static void mult_plain_impl(rc_context* c, const rc_ciphertext* ct, const uint64_t* plain, rc_ciphertext* out,
                             cudaStream_t s) {
   require(c && out && out->data && plain, "arguments must not be null");
@@ -1199,6 +1238,18 @@ extern "C" int rc_mult_plain(rc_context* c, const rc_ciphertext* ct, const uint6
     const int sb = ct ? ct->scale_bits : 0;
     mult_plain_impl(c, ct, plain, out, S(stream));
     out->scale_bits = sb + sb;  // context/ops.rs:24-29
+  });
+}
+
+extern "C" int rc_multiply_plain_rns_batch(rc_context* c, uint32_t count, const rc_ciphertext* ct,
+                                           const uint64_t* const* plains, rc_ciphertext* out, void* stream) {
+  return guarded([&] {
+    require(c && ct && plains && out, "arguments must not be null");
+    for (uint32_t i = 0; i < count; ++i) {
+      const int sb = ct[i].scale_bits;
+      mult_plain_impl(c, &ct[i], plains[i], &out[i], S(stream));
+      out[i].scale_bits = sb;
+    }
   });
 }
 

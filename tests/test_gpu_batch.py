@@ -117,3 +117,23 @@ def test_fused_and_unfused_tensor_agree(env):
     for u, v in zip(got[0][0], got[1][0]):
         assert np.array_equal(u, v)
     assert np.array_equal(got[0][1], got[1][1])
+
+
+def test_add_and_multiply_plain_batches_equal_single_calls(env):
+    C, ctx, params, keys, host_keys, O = env
+    rng = np.random.default_rng(10)
+    q, n = params.q_moduli(), params.poly_degree
+    levels = [3, 6, 3, 7, 1]
+    mk = lambda lv: C.RnsCiphertext(C.to_device(np.stack([np.stack([rng.integers(0, m, n, dtype=np.uint64)
+                                                                      for m in q[: lv + 1]]) for _ in range(2)])), 33)
+    a, b = [mk(lv) for lv in levels], [mk(lv) for lv in levels]
+    pts = [C.RnsPolynomial(C.to_device(np.stack([rng.integers(0, m, n, dtype=np.uint64) for m in q[: lv + 1]])))
+           for lv in levels]
+    for got, x, y in zip(ctx.add_batch(a, b), a, b):
+        ref = ctx.add(x, y)
+        assert np.array_equal(got.numpy(), ref.numpy()) and got.scale_bits == ref.scale_bits
+    for got, x, p in zip(ctx.multiply_plain_rns_batch(a, pts), a, pts):
+        ref = ctx.multiply_plain_rns(x, p)
+        assert np.array_equal(got.numpy(), ref.numpy()) and got.scale_bits == 33
+    with pytest.raises(C.RcError, match="same scale to add"):
+        ctx.add_batch([a[0]], [C.RnsCiphertext(b[0].data, 34)])
