@@ -162,6 +162,8 @@ int rc_add_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* lhs, cons
                  rc_ciphertext* out, void* stream);
 int rc_multiply_plain_rns_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* ct,
                                 const uint64_t* const* plains, rc_ciphertext* out, void* stream);
+/* `count` independent rescales (context/ops.rs:32-37) in one call */
+int rc_rescale_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* ct, rc_ciphertext* out, void* stream);
 /* Sum over k of mult_plain(cts[k], plains[k]), the inner sum of the BSGS linear transform
  * (apply_giant_step_terms, src/ckks/bootstrapping/linear_transform.rs:234-252: mult_plain, context/ops.rs:20-30,
  * folded with RnsCiphertext::add, ciphertexts.rs:60-69).  All cts share level and scale; out gets the level and

@@ -81,6 +81,7 @@ SIGNATURES = [
     ("rc_mult_plain_accumulate", ctypes.c_int, [_vp, _u32, _CT, _i32, _vp, _i32, _CT, _vp]),
     ("rc_add_batch", ctypes.c_int, [_vp, _u32, _CT, _CT, _CT, _vp]),
     ("rc_multiply_plain_rns_batch", ctypes.c_int, [_vp, _u32, _CT, _vp, _CT, _vp]),
+    ("rc_rescale_batch", ctypes.c_int, [_vp, _u32, _CT, _CT, _vp]),
     ("rc_mult", ctypes.c_int, [_vp, _CT, _CT, _CT, _vp]),
     ("rc_rescale", ctypes.c_int, [_vp, _CT, _CT, _vp]),
     ("rc_rescale_quadratic", ctypes.c_int, [_vp, _CT, _CT, _vp]),

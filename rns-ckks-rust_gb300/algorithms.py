@@ -86,7 +86,17 @@ def halevi_shoup_dot_product_batch(ctx: RnsCkksContext, ciphertexts: Sequence[Rn
     """`halevi_shoup_dot_product` for many independent (ciphertext, plaintext) pairs: every fold step rotates
     the whole batch in one call.  Each result equals the single-pair routine's."""
     lengths = {len(np.atleast_1d(p)) for p in plaintext_slots}
-    accs = [ctx.mult_plain_slots_real(ct, _padded(ctx, p)) for ct, p in zip(ciphertexts, plaintext_slots)]
+    # mult_plain_slots_real (context/ops.rs:39-48) for every pair: encode at the ciphertext's level and scale,
+    # mult_plain (scale doubles), rescale -- the products and rescales as batched calls
+    cts = list(ciphertexts)
+    plains = [ctx.encode_at_level_and_scale(_padded(ctx, p).astype(np.complex128), ct.level, ct.scale_bits)
+              for ct, p in zip(cts, plaintext_slots)]
+    for ct, p in zip(cts, plains):
+        if p.levels() != ct.level + 1:
+            _panic("plaintext levels must match the multiplication context")
+    prods = [RnsCiphertext(m.data, ct.scale_bits + ct.scale_bits, m.level)
+             for m, ct in zip(ctx.multiply_plain_rns_batch(cts, plains), cts)]
+    accs = ctx.rescale_batch(prods)
     if len(lengths) != 1:  # different fold widths: run each pair's schedule on its own
         return [_fold(ctx, [a], len(np.atleast_1d(p)), rotation_keys, "missing rotation key for step {}")[0]
                 for a, p in zip(accs, plaintext_slots)]

@@ -624,6 +624,17 @@ class RnsCkksContext:
         call("rc_multiply_plain_rns_batch", self.handle, n, C, P, O, _stream())
         return [RnsCiphertext(o, O[i].scale_bits, O[i].level) for i, o in enumerate(outs)]
 
+    def rescale_batch(self, cts: Sequence[RnsCiphertext]) -> List[RnsCiphertext]:
+        """`rescale` of many ciphertexts in one call (rc_rescale_batch)."""
+        n = len(cts)
+        if n == 0:
+            return []
+        outs = [self._ct_out(2, max(c.level, 1)) for c in cts]
+        C = (RcCiphertext * n)(*[c.raw() for c in cts])
+        O = (RcCiphertext * n)(*[RcCiphertext(o.data_ptr(), 0, 0) for o in outs])
+        call("rc_rescale_batch", self.handle, n, C, O, _stream())
+        return [RnsCiphertext(o, O[i].scale_bits, O[i].level) for i, o in enumerate(outs)]
+
     def multiply_plain_rns(self, ct: RnsCiphertext, plain: RnsPolynomial) -> RnsCiphertext:
         """src/rns/ops.rs:54-66 (scale unchanged)."""
         if plain.levels() != ct.level + 1:

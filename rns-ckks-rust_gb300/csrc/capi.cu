@@ -1363,6 +1363,13 @@ extern "C" int rc_rescale(rc_context* c, const rc_ciphertext* ct, rc_ciphertext*
 extern "C" int rc_rescale_quadratic(rc_context* c, const rc_ciphertext* ct, rc_ciphertext* out, void* stream) {
   return guarded([&] { rescale_impl(c, ct, out, 3, S(stream)); });
 }
+extern "C" int rc_rescale_batch(rc_context* c, uint32_t count, const rc_ciphertext* ct, rc_ciphertext* out,
+                                void* stream) {
+  return guarded([&] {
+    require(c && ct && out, "arguments must not be null");
+    for (uint32_t i = 0; i < count; ++i) rescale_impl(c, &ct[i], &out[i], 2, S(stream));
+  });
+}
 
 extern "C" int rc_keyswitch(rc_context* c, const uint64_t* poly, int32_t level, const rc_ksk* key,
                             rc_ciphertext* out, void* stream) {
