@@ -93,8 +93,11 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
       }
     }
   }
-  // X' = X - k*Q with k = floor(sum y_i / q_i) (exact up to +-1, fixed below)
+  // X' = X - k*Q with k = floor(sum y_i / q_i) (exact up to +-1, fixed below).  `top` follows the
+  // word W-1 as each pass writes it: reading X[W-1] afterwards would index X dynamically and move it to
+  // local memory.
   u64 k = (u64)kf;
+  u64 top = 0;
   {
     u64 borrow = 0, carry = 0;
 #pragma unroll
@@ -109,18 +112,13 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
         u64 d2 = d - borrow;
         u64 b2 = d < borrow ? 1ull : 0ull;
         X[w] = d2;
+        top = d2;
         borrow = b1 + b2;
       }
     }
   }
   // X is now in [-Q, 2Q) as a W-word two's complement value
-  auto top_neg = [&]() -> bool {
-    bool n = false;
-#pragma unroll
-    for (int w = 0; w < WM; ++w)
-      if (w == W - 1) n = (X[w] >> 63) != 0;
-    return n;
-  };
+  auto top_neg = [&]() -> bool { return (top >> 63) != 0; };
   auto add_Q = [&](bool subtract) {
     u64 c = 0;
 #pragma unroll
@@ -133,6 +131,7 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
           u64 s2 = s + c;
           u64 c2 = s2 < c ? 1ull : 0ull;
           X[w] = s2;
+          top = s2;
           c = c1 + c2;
         } else {
           u64 d = X[w] - qw;
@@ -140,6 +139,7 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
           u64 d2 = d - c;
           u64 b2 = d < c ? 1ull : 0ull;
           X[w] = d2;
+          top = d2;
           c = b1 + b2;
         }
       }

@@ -28,6 +28,13 @@ namespace {
 constexpr int W_ROW_WARPS = 4;
 constexpr int W_MAC_WARPS = 8;
 
+// entry 2 * pair + k of a four-entry table in the kernel parameter, picked by a select: a dynamic index
+// would copy the whole parameter struct to local memory
+template <class T>
+__device__ __forceinline__ T pick(const T (&a)[4], int pair, int k) {
+  return pair ? a[2 + k] : a[k];
+}
+
 template <int M>
 struct WColTile {
   static constexpr int COLS = (8 * core::Geo<M>::SUBS) > 16 ? 8 * core::Geo<M>::SUBS : 16;
@@ -51,7 +58,7 @@ __global__ __launch_bounds__(256, 2) void k_w_cols_fwd(WidePrimes w, const void*
   const int c0 = blockIdx.x * COLS;
   const int pair = blockIdx.y;
   const size_t poly = (size_t)p0 + blockIdx.z;
-  const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
+  const uint32_t q0 = pick(w.q, pair, 0), q1 = pick(w.q, pair, 1);
   // tile (digits: the int32 into the element's first word, converted at first use) and twiddles by
   // asynchronous copies, all in flight together
 #pragma unroll 4
@@ -113,7 +120,7 @@ __global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_fwd(WidePrimes w, u
   const int row0 = blockIdx.x * ROWS;
   const int pair = blockIdx.y;
   const size_t poly = (size_t)p0 + blockIdx.z;
-  const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
+  const uint32_t q0 = pick(w.q, pair, 0), q1 = pick(w.q, pair, 1);
   const Tw2* twg = w.tw_fwd + (size_t)pair * N;
   const int rl = warp * G::SUBS + sub, row = row0 + rl;
   uint2* in = data + (poly * 2 + pair) * N + (size_t)row * N2;
@@ -153,7 +160,7 @@ __global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_inv(WidePrimes w, u
   const int row0 = blockIdx.x * ROWS;
   const int pair = blockIdx.y;
   const size_t poly = blockIdx.z;
-  const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
+  const uint32_t q0 = pick(w.q, pair, 0), q1 = pick(w.q, pair, 1);
   const Tw2* twg = w.tw_inv + (size_t)pair * N;
   const int rl = warp * G::SUBS + sub, row = row0 + rl;
   uint2* in = data + (poly * 2 + pair) * N + (size_t)row * N2;
@@ -181,7 +188,7 @@ __global__ __launch_bounds__(256, 2) void k_w_cols_inv(WidePrimes w, uint2* data
   const int c0 = blockIdx.x * COLS;
   const int pair = blockIdx.y;
   const size_t poly = blockIdx.z;
-  const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
+  const uint32_t q0 = pick(w.q, pair, 0), q1 = pick(w.q, pair, 1);
   uint2* io = data + (poly * 2 + pair) * N;
 #pragma unroll 4
   for (int it = 0; it < N1 * COLS / 256; ++it) {
@@ -207,8 +214,8 @@ __global__ __launch_bounds__(256, 2) void k_w_cols_inv(WidePrimes w, uint2* data
     for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::first_idx<M1>(l, k))] = v[k];
   }
   __syncthreads();
-  const uint32_t n0 = w.n_inv[2 * pair], n0s = w.n_inv_s[2 * pair];
-  const uint32_t n1 = w.n_inv[2 * pair + 1], n1s = w.n_inv_s[2 * pair + 1];
+  const uint32_t n0 = pick(w.n_inv, pair, 0), n0s = pick(w.n_inv_s, pair, 0);
+  const uint32_t n1 = pick(w.n_inv, pair, 1), n1s = pick(w.n_inv_s, pair, 1);
 #pragma unroll 4
   for (int it = 0; it < N1 * COLS / 256; ++it) {
     const int idx = it * 256 + threadIdx.x;
@@ -265,8 +272,8 @@ __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC 
   }
   __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const uint32_t q0 = w.q[2 * pair], q1 = w.q[2 * pair + 1];
-  const u64 bar0 = w.bar[2 * pair], bar1 = w.bar[2 * pair + 1];
+  const uint32_t q0 = pick(w.q, pair, 0), q1 = pick(w.q, pair, 1);
+  const u64 bar0 = pick(w.bar, pair, 0), bar1 = pick(w.bar, pair, 1);
   const size_t krun = (size_t)key_digits * 2 * 32;
   // this lane's slots of the warp's key ring: slot u holds (k0, k1) of one digit at ring[u][0|1][lane]
   uint2* ring = dsm + (size_t)BC * run + (size_t)warp * W_PF * 64 + lane;
