@@ -164,6 +164,16 @@ int rc_multiply_plain_rns_batch(rc_context* ctx, uint32_t count, const rc_cipher
                                 const uint64_t* const* plains, rc_ciphertext* out, void* stream);
 /* `count` independent rescales (context/ops.rs:32-37) in one call */
 int rc_rescale_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* ct, rc_ciphertext* out, void* stream);
+/* lift_poly_to_context: src/rns/keyswitching.rs:242-276 (convert_centered_residues_to_target, 365-379).
+ * `polys` polynomials over Q_limbs ([polys][limbs][N]) -> over Q_limbs followed by the aux primes
+ * ([polys][limbs + aux_count][N]): the Q limbs are copied, each aux limb is the centred CRT value (the tie
+ * X == floor(Q/2) stays positive) mod that prime.  Requires an aux basis. */
+int rc_lift_to_aux(rc_context* ctx, const uint64_t* a, uint64_t* out, uint32_t polys, uint32_t limbs,
+                   void* stream);
+/* mod_raise: src/ckks/bootstrapping/mod_raise.rs:29-45.  out->data holds [2][level + 1 + aux_count][N]
+ * (c0 then c1 over the eval-key basis); out->level = ct->level + aux_count (the eval-key context's level),
+ * scale unchanged.  The first level + 1 limbs of each component are the input's. */
+int rc_mod_raise(rc_context* ctx, const rc_ciphertext* ct, rc_ciphertext* out, void* stream);
 /* Sum over k of mult_plain(cts[k], plains[k]), the inner sum of the BSGS linear transform
  * (apply_giant_step_terms, src/ckks/bootstrapping/linear_transform.rs:234-252: mult_plain, context/ops.rs:20-30,
  * folded with RnsCiphertext::add, ciphertexts.rs:60-69).  All cts share level and scale; out gets the level and

@@ -82,6 +82,8 @@ SIGNATURES = [
     ("rc_add_batch", ctypes.c_int, [_vp, _u32, _CT, _CT, _CT, _vp]),
     ("rc_multiply_plain_rns_batch", ctypes.c_int, [_vp, _u32, _CT, _vp, _CT, _vp]),
     ("rc_rescale_batch", ctypes.c_int, [_vp, _u32, _CT, _CT, _vp]),
+    ("rc_lift_to_aux", ctypes.c_int, [_vp, _vp, _vp, _u32, _u32, _vp]),
+    ("rc_mod_raise", ctypes.c_int, [_vp, _CT, _CT, _vp]),
     ("rc_mult", ctypes.c_int, [_vp, _CT, _CT, _CT, _vp]),
     ("rc_rescale", ctypes.c_int, [_vp, _CT, _CT, _vp]),
     ("rc_rescale_quadratic", ctypes.c_int, [_vp, _CT, _CT, _vp]),

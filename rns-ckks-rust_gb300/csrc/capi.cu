@@ -683,6 +683,15 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
       size_t o_hQ = blob.size();
       auto hw = Q.shr1().words(W);
       blob.insert(blob.end(), hw.begin(), hw.end());
+      // lift to the aux primes: 2^(64 w) mod p_k for w = 0..W, then their Shoup companions
+      size_t o_pw = blob.size();
+      for (size_t k = 0; k < pm.size(); ++k) {
+        const uint64_t two64 = mulmod_h(powmod_h(2, 32, pm[k]), powmod_h(2, 32, pm[k]), pm[k]);
+        for (int w = 0; w <= W; ++w) blob.push_back(powmod_h(two64, (uint64_t)w, pm[k]));
+      }
+      size_t o_pws = blob.size();
+      for (size_t k = 0; k < pm.size(); ++k)
+        for (int w = 0; w <= W; ++w) blob.push_back(shoup_h(blob[o_pw + k * (W + 1) + w], pm[k]));
       li.buf.reset(new DevBuf(blob.size() * 8));
       uint64_t* d = (uint64_t*)li.buf->p;
       cuda_check(cudaMemcpy(d, blob.data(), blob.size() * 8, cudaMemcpyHostToDevice), "upload level tables");
@@ -692,6 +701,8 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
       li.dt.inv_q = (const double*)(d + o_invq);
       li.dt.Q = d + o_Q;
       li.dt.halfQ = d + o_hQ;
+      li.dt.lift_pw = pm.empty() ? nullptr : d + o_pw;
+      li.dt.lift_pw_s = pm.empty() ? nullptr : d + o_pws;
       li.dt.W = W;
       li.dt.small_q = li.bits <= 30 ? 1 : 0;
       li.dt.Qsmall = li.bits <= 63 ? Q.words(1)[0] : 0;
@@ -1368,6 +1379,33 @@ extern "C" int rc_rescale_batch(rc_context* c, uint32_t count, const rc_cipherte
   return guarded([&] {
     require(c && ct && out, "arguments must not be null");
     for (uint32_t i = 0; i < count; ++i) rescale_impl(c, &ct[i], &out[i], 2, S(stream));
+  });
+}
+
+// lift_poly_to_context (keyswitching.rs:242-276) from Q_limbs to Q_limbs u P
+static void lift_impl(rc_context* c, const uint64_t* a, uint64_t* out, uint32_t polys, uint32_t limbs,
+                      cudaStream_t s) {
+  require(c && a && out, "arguments must not be null");
+  require(c->K > 0, "lifting requires an auxiliary evaluation basis");
+  require(limbs >= 1 && (int)limbs <= c->L, "limb count out of range for this context");
+  require(a != out, "lift output must not alias its input");
+  lift_to_aux(c->d_pc, c->d_pc + c->L, level_info(c, (int)limbs).dt, a, out, (int)polys, (int)limbs, c->K,
+              c->log_n, s);
+  launch_check("lift");
+}
+
+extern "C" int rc_lift_to_aux(rc_context* c, const uint64_t* a, uint64_t* out, uint32_t polys, uint32_t limbs,
+                              void* stream) {
+  return guarded([&] { lift_impl(c, a, out, polys, limbs, S(stream)); });
+}
+
+extern "C" int rc_mod_raise(rc_context* c, const rc_ciphertext* ct, rc_ciphertext* out, void* stream) {
+  return guarded([&] {
+    require(c && out && out->data, "arguments must not be null");
+    check_ct(c, ct, "ciphertext");
+    lift_impl(c, ct->data, out->data, 2, (uint32_t)ct->level + 1, S(stream));
+    out->level = ct->level + c->K;  // the eval-key context's levels - 1 (mod_raise.rs:40-44)
+    out->scale_bits = ct->scale_bits;
   });
 }
 

@@ -103,6 +103,8 @@ struct DecompTab {
   int W;                 // words for Q (with headroom for the CRT sum)
   int small_q;           // Q <= 2^30: digits need the general centred lift
   u64 Qsmall;            // Q when small_q
+  const u64* lift_pw;    // [K][W+1]: 2^(64 w) mod p_k (the aux primes), w = 0..W
+  const u64* lift_pw_s;  // Shoup companions
 };
 
 struct ModDownTab {
@@ -121,6 +123,10 @@ struct ModDownTab {
 
 // digits[job][d][x] (int32) of the centred CRT value of src (optionally read
 // through the automorphism with inverse element g_inv; 0/1 = none)
+// lift_poly_to_context (keyswitching.rs:242-276): polys polynomials over Q_limbs ([polys][limbs][N]) to
+// Q_limbs u P ([polys][limbs + K][N]); ppc = the aux primes' constants.
+void lift_to_aux(const PrimeConst* pc, const PrimeConst* ppc, const DecompTab& dt, const u64* src, u64* dst,
+                 int polys, int limbs, int K, int log_n, cudaStream_t s);
 void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int jobs, int limbs, int D,
                int32_t* digits, uint64_t g_inv, int log_n, cudaStream_t s);
 

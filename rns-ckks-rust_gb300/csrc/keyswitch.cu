@@ -29,10 +29,15 @@ namespace {
 // ---------------------------------------------------------------------------
 // decomposition
 // ---------------------------------------------------------------------------
-template <int WM>
-__global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int limbs, int D, int32_t* digits,
-                            u64 g_inv, int log_n) {
-  // the tables every thread walks (CRT words of Q/q_l, (Q/q_l)^-1, q_l, Q, floor(Q/2)) staged in shared memory
+// The CRT tables every thread of a decomposition or lift walks (words of Q/q_l, (Q/q_l)^-1, q_l, 1/q_l,
+// Q, floor(Q/2)), staged in shared memory by all threads of the block; the caller synchronises.
+struct CrtSmem {
+  const u64 *qhat, *q, *hinv, *hinv_s;
+  const double* invq;
+  const u64 *Q, *half;
+};
+
+__device__ __forceinline__ CrtSmem stage_crt_tables(const PrimeConst* pc, const DecompTab& dt, int limbs) {
   extern __shared__ u64 dsm_tab[];
   const int W = dt.W;
   u64* s_qhat = dsm_tab;                       // [limbs][W]
@@ -53,32 +58,28 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
     s_Q[e] = dt.Q[e];
     s_half[e] = dt.halfQ[e];
   }
-  __syncthreads();
-  const u64 N = 1ull << log_n;
-  const u64 x = blockIdx.x * (u64)blockDim.x + threadIdx.x;
-  if (x >= N) return;
-  const int job = blockIdx.y;
-  const u64* in = src.p[job];
+  return CrtSmem{s_qhat, s_q, s_hinv, s_hinv_s, s_invq, s_Q, s_half};
+}
 
-  u64 sidx = x;
-  bool neg = false;
-  if (g_inv > 1) {
-    sidx = (x * g_inv) & (2 * N - 1);
-    neg = sidx >= N;
-    if (neg) sidx -= N;
-  }
+size_t crt_smem_bytes(int limbs, int W) { return ((size_t)limbs * W + 4 * (size_t)limbs + 2 * (size_t)W) * 8; }
 
-  u64 X[WM];
+// The centred CRT value of one coefficient: X in (-Q/2, Q/2] as a W-word two's complement number in X[0..W)
+// (keyswitching.rs:397-454 up to the digit split; the tie X == floor(Q/2) stays positive).  `in` points at
+// limb 0 of the coefficient, limbs N apart; neg negates every residue first (a negacyclic automorphism
+// source).  Returns the sign extension word (all ones when X < 0).
+template <int WM>
+__device__ __forceinline__ u64 centred_crt(const CrtSmem& t, int W, int limbs, const u64* in, u64 N, bool neg,
+                                           u64 (&X)[WM]) {
 #pragma unroll
   for (int w = 0; w < WM; ++w) X[w] = 0;
   double kf = 0.0;
   for (int l = 0; l < limbs; ++l) {
-    const u64 q = s_q[l];
-    u64 r = in[(u64)l * N + sidx];
+    const u64 q = t.q[l];
+    u64 r = in[(u64)l * N];
     if (neg && r) r = q - r;
-    const u64 y = mul_shoup(r, s_hinv[l], s_hinv_s[l], q);
-    kf += (double)y * s_invq[l];
-    const u64* qh = s_qhat + (size_t)l * W;
+    const u64 y = mul_shoup(r, t.hinv[l], t.hinv_s[l], q);
+    kf += (double)y * t.invq[l];
+    const u64* qh = t.qhat + (size_t)l * W;
     u64 carry = 0;
 #pragma unroll
     for (int w = 0; w < WM; ++w) {
@@ -103,7 +104,7 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
 #pragma unroll
     for (int w = 0; w < WM; ++w) {
       if (w < W) {
-        U128 p = mul_wide(k, s_Q[w]);
+        U128 p = mul_wide(k, t.Q[w]);
         u64 sub = p.lo + carry;
         carry = p.hi + (sub < carry ? 1ull : 0ull);
         u64 xw = X[w];
@@ -124,7 +125,7 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
 #pragma unroll
     for (int w = 0; w < WM; ++w) {
       if (w < W) {
-        u64 qw = s_Q[w];
+        u64 qw = t.Q[w];
         if (!subtract) {
           u64 s = X[w] + qw;
           u64 c1 = s < qw ? 1ull : 0ull;
@@ -158,10 +159,33 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
     return res > 0 || (or_equal && res == 0);
   };
   if (top_neg()) add_Q(false);
-  else if (greater_than(s_Q, true)) add_Q(true);
+  else if (greater_than(t.Q, true)) add_Q(true);
   // centre: X > floor(Q/2) -> X - Q
-  if (greater_than(s_half, false)) add_Q(true);
-  const u64 ext = top_neg() ? ~0ull : 0ull;
+  if (greater_than(t.half, false)) add_Q(true);
+  return top_neg() ? ~0ull : 0ull;
+}
+
+template <int WM>
+__global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int limbs, int D, int32_t* digits,
+                            u64 g_inv, int log_n) {
+  const CrtSmem tabs = stage_crt_tables(pc, dt, limbs);
+  __syncthreads();
+  const int W = dt.W;
+  const u64 N = 1ull << log_n;
+  const u64 x = blockIdx.x * (u64)blockDim.x + threadIdx.x;
+  if (x >= N) return;
+  const int job = blockIdx.y;
+  const u64* in = src.p[job];
+
+  u64 sidx = x;
+  bool neg = false;
+  if (g_inv > 1) {
+    sidx = (x * g_inv) & (2 * N - 1);
+    neg = sidx >= N;
+    if (neg) sidx -= N;
+  }
+  u64 X[WM];
+  const u64 ext = centred_crt<WM>(tabs, W, limbs, in + sidx, N, neg, X);
 
   // balanced base-2^30 digits of the two's complement value
   int32_t* out = digits + (size_t)job * D * N + x;
@@ -206,6 +230,40 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
       carry = 0;
     }
     out[(size_t)d * N] = (int32_t)dig;
+  }
+}
+
+// lift_poly_to_context (keyswitching.rs:242-276) for polynomial blockIdx.y: the Q limbs are copied and limb
+// limbs + k is the centred CRT value mod p_k (convert_centered_residues_to_target, 365-379):
+// sum_w X[w] * (2^(64 w) mod p_k) minus 2^(64 W) mod p_k when X < 0.
+template <int WM>
+__global__ void k_lift(const PrimeConst* pc, const PrimeConst* ppc, DecompTab dt, const u64* src, u64* dst,
+                       int limbs, int K, int log_n) {
+  const CrtSmem tabs = stage_crt_tables(pc, dt, limbs);
+  __syncthreads();
+  const int W = dt.W;
+  const u64 N = 1ull << log_n;
+  const u64 x = blockIdx.x * (u64)blockDim.x + threadIdx.x;
+  if (x >= N) return;
+  const u64* in = src + (size_t)blockIdx.y * limbs * N + x;
+  u64* out = dst + (size_t)blockIdx.y * (limbs + K) * N + x;
+  for (int l = 0; l < limbs; ++l) out[(size_t)l * N] = in[(size_t)l * N];
+  u64 X[WM];
+  const u64 ext = centred_crt<WM>(tabs, W, limbs, in, N, false, X);
+  for (int k = 0; k < K; ++k) {
+    const u64 p = ppc[k].q, one_s = ppc[k].one_s;
+    const u64* pw = dt.lift_pw + (size_t)k * (W + 1);
+    const u64* pws = dt.lift_pw_s + (size_t)k * (W + 1);
+    u64 acc = 0;
+#pragma unroll
+    for (int w = 0; w < WM; ++w) {
+      if (w < W) {
+        const u64 r = reduce_2q(mul_shoup_lazy(X[w], 1, one_s, p), p);  // X[w] mod p
+        acc = add_mod(acc, mul_shoup(r, pw[w], pws[w], p), p);
+      }
+    }
+    if (ext) acc = sub_mod(acc, pw[W], p);
+    out[(size_t)(limbs + k) * N] = acc;
   }
 }
 
@@ -753,7 +811,7 @@ void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int
   const int W = dt.W;
   ProfScope p("decompose", s);
   // the word count is a template parameter (register-resident value); the closest instance above W runs
-  const size_t smem = ((size_t)limbs * W + 4 * (size_t)limbs + 2 * (size_t)W) * sizeof(u64);
+  const size_t smem = crt_smem_bytes(limbs, W);
   if (W <= 4) k_decompose<4><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
   else if (W <= 8) k_decompose<8><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
   else if (W <= 12) k_decompose<12><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
@@ -762,6 +820,23 @@ void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int
   else if (W <= 24) k_decompose<24><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
   else if (W <= 32) k_decompose<32><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
   else k_decompose<64><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+}
+
+void lift_to_aux(const PrimeConst* pc, const PrimeConst* ppc, const DecompTab& dt, const u64* src, u64* dst,
+                 int polys, int limbs, int K, int log_n, cudaStream_t s) {
+  if (polys <= 0) return;
+  const int N = 1 << log_n;
+  const int threads = N < 128 ? N : 128;
+  dim3 g((N + threads - 1) / threads, polys);
+  const int W = dt.W;
+  ProfScope p("lift", s);
+  const size_t smem = crt_smem_bytes(limbs, W);
+  if (W <= 4) k_lift<4><<<g, threads, smem, s>>>(pc, ppc, dt, src, dst, limbs, K, log_n);
+  else if (W <= 8) k_lift<8><<<g, threads, smem, s>>>(pc, ppc, dt, src, dst, limbs, K, log_n);
+  else if (W <= 16) k_lift<16><<<g, threads, smem, s>>>(pc, ppc, dt, src, dst, limbs, K, log_n);
+  else if (W <= 24) k_lift<24><<<g, threads, smem, s>>>(pc, ppc, dt, src, dst, limbs, K, log_n);
+  else if (W <= 32) k_lift<32><<<g, threads, smem, s>>>(pc, ppc, dt, src, dst, limbs, K, log_n);
+  else k_lift<64><<<g, threads, smem, s>>>(pc, ppc, dt, src, dst, limbs, K, log_n);
 }
 
 void digit_ntt_mac(const KsArgs& a, const int32_t* digits, const u64* const* keys, int jobs, u64* acc,
