@@ -248,6 +248,14 @@ int rc_encode(const rc_context* ctx, const double* slots, int32_t level, uint32_
 /* reconstruct_coefficients + decode_integer_coeffs: polynomial.rs:162-201, encoding.rs:33-66 */
 int rc_decode(const rc_context* ctx, const uint64_t* poly_host, int32_t level, uint32_t scale_bits,
               double* slots_out);
+/* The two slot/coefficient maps the exact bootstrapping transforms are built from, in FP64 with the
+ * reference's operation order; they need no context (n = ring degree).
+ * dense_slots_to_real_coeffs (src/ckks/bootstrapping/exact_transforms.rs:180-200): n/2 complex slots
+ * (interleaved) -> n real coefficients.
+ * dense_complex_coeffs_to_slots (exact_transforms.rs:210-229): n complex coefficients (interleaved) -> n/2
+ * complex slots (interleaved). */
+int rc_slots_to_real_coeffs(uint64_t n, const double* slots, double* coeffs_out);
+int rc_complex_coeffs_to_slots(uint64_t n, const double* coeffs, double* slots_out);
 
 /* ---- instrumentation (no reference counterpart: the reference only has
  * std::time::Instant around whole ops, examples/operations/timings.rs:282-308) ----

@@ -538,12 +538,12 @@ class RnsCkksContext:
         return self._rotation_key(sk, pk, self.galois_element_for_rotation(steps), level, sampler, samples,
                                   return_coeff)
 
-    def generate_conjugation_key(self, sk, pk, sampler=None):
+    def generate_conjugation_key(self, sk, pk, sampler=None, return_coeff=False):
         return self._rotation_key(sk, pk, self.conjugation_galois_element(), self.levels() - 1, sampler, None,
-                                  False)
+                                  return_coeff)
 
-    def generate_conjugation_key_at_level(self, sk, pk, level: int, sampler=None):
-        return self._rotation_key(sk, pk, self.conjugation_galois_element(), level, sampler, None, False)
+    def generate_conjugation_key_at_level(self, sk, pk, level: int, sampler=None, return_coeff=False):
+        return self._rotation_key(sk, pk, self.conjugation_galois_element(), level, sampler, None, return_coeff)
 
     # ---- encryption, src/rns/ops.rs:8-52 ----
     def _encrypt_raw(self, pt, p0, p1, u, e0, e1, moduli):

@@ -204,3 +204,46 @@ extern "C" int rc_decode(const rc_context* c, const uint64_t* poly, int32_t leve
     return RC_ERR_CUDA;
   }
 }
+
+// dense_slots_to_real_coeffs (src/ckks/bootstrapping/exact_transforms.rs:180-200): conjugate-symmetric
+// evaluations at the 5^j exponents, canonical_embedding_backward, times xi^-i, real part.  Needs no context.
+extern "C" int rc_slots_to_real_coeffs(uint64_t n, const double* slots, double* coeffs_out) {
+  try {
+    if (!slots || !coeffs_out || n < 2 || (n & (n - 1))) return RC_ERR_INVALID_ARGUMENT;
+    std::vector<C> evals(n, C{0.0, 0.0});
+    auto ex = slot_exponents(n);
+    for (size_t k = 0; k < n / 2; ++k) {
+      const C v{slots[2 * k], slots[2 * k + 1]};
+      const size_t e = ex[k];
+      evals[(e - 1) / 2] = v;
+      evals[(((2 * n - e) % (2 * n)) - 1) / 2] = C{v.re, -v.im};
+    }
+    fft_in_place(evals, true);
+    const C xi = polar(M_PI / (double)n);
+    for (size_t i = 0; i < n; ++i) coeffs_out[i] = cmul(evals[i], cpowi(xi, -(long)i)).re;
+    return RC_OK;
+  } catch (...) {
+    return RC_ERR_OUT_OF_MEMORY;
+  }
+}
+
+// dense_complex_coeffs_to_slots (exact_transforms.rs:210-229): coefficients times xi^i,
+// canonical_embedding_forward, the evaluations at the 5^j exponents.  Needs no context.
+extern "C" int rc_complex_coeffs_to_slots(uint64_t n, const double* coeffs, double* slots_out) {
+  try {
+    if (!coeffs || !slots_out || n < 2 || (n & (n - 1))) return RC_ERR_INVALID_ARGUMENT;
+    const C xi = polar(M_PI / (double)n);
+    std::vector<C> v(n);
+    for (size_t i = 0; i < n; ++i) v[i] = cmul(C{coeffs[2 * i], coeffs[2 * i + 1]}, cpowi(xi, (long)i));
+    fft_in_place(v, false);
+    auto ex = slot_exponents(n);
+    for (size_t k = 0; k < n / 2; ++k) {
+      const C s = v[(ex[k] - 1) / 2];
+      slots_out[2 * k] = s.re;
+      slots_out[2 * k + 1] = s.im;
+    }
+    return RC_OK;
+  } catch (...) {
+    return RC_ERR_OUT_OF_MEMORY;
+  }
+}
