@@ -444,6 +444,7 @@ def run_gpu(args):
         result["ntt_microbench"] = ntt_microbench(C, ctx, params, peak, args.seed)
         result["mixed_level_relin"] = mixed_level_relin(C, ctx, params, load_oracle(), args.seed)
         result["bsgs_matvec"] = bsgs_matvec_bench(pkg, C, args.seed)
+        result["bootstrap"] = bootstrap_bench(pkg, C, args.seed)
         result["serving"] = serving_bench(pkg, C, args.seed)
     if rank == 0:
         print(json.dumps(result), flush=True)
@@ -607,6 +608,84 @@ def bsgs_matvec_bench(pkg, C, seed, batch=32, dim=128, reps=2):
             "ms_per_batch": round(secs * 1e3, 2), "single_matvec_ms": round(single * 1e3, 2),
             "batched_vs_single": round(single * batch / secs, 2), "batch_equals_single": same,
             "decoded_max_abs_err": err, "key_generation_s": round(t_keys, 2), "diagonal_packing_s": round(t_pack, 2)}
+
+
+def bootstrap_bench(pkg, C, seed, batch=16, reps=3):
+    """The crate's exact sparse EvalMod bootstrapping roundtrip (ModRaise, CoeffToSlot, degree-5 sine EvalMod,
+    SlotToCoeff; roundtrip.rs:26-44,77-99) at `realistic_8_level` (N=2^15, 8 limbs of 50-bit primes, 2 aux
+    primes, scale 2^45) with 8 active slots, the reference test's configuration.  The prepared form packs
+    the diagonals and generates the keys once; the single-ciphertext time and a batch of 16 are reported,
+    with the oracle's time for one roundtrip on the host cores (same keys and input) beside them."""
+    import torch
+    from rnsckks_gb300 import bootstrapping as B
+    P = pkg.params
+    ctx = C.RnsCkksContext(P.RnsCkksParams.realistic_8_level())
+    kp = ctx.keygen(64, C.Sampler(seed + 7))
+    rng = np.random.default_rng(seed + 8)
+    inputs = [rng.uniform(-0.05, 0.05, 8) + 1j * rng.uniform(-0.05, 0.05, 8) for _ in range(batch)]
+    cts = [ctx.encrypt(ctx.encode(np.tile(v, ctx.num_slots() // 8)), kp.public_key, C.Sampler(seed + 90 + i))
+           for i, v in enumerate(inputs)]
+    t0 = time.perf_counter()
+    boot = B.SparseBootstrapper(ctx, kp, cts[0].level, cts[0].scale_bits, 8, 1.0, 5)
+    torch.cuda.synchronize()
+    t_prep = time.perf_counter() - t0
+    one = boot.run(cts[0])  # warm
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        one = boot.run(cts[0])
+    torch.cuda.synchronize()
+    single = (time.perf_counter() - t0) / reps
+    outs = boot.run_batch(cts)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    for _ in range(reps):
+        outs = boot.run_batch(cts)
+    torch.cuda.synchronize()
+    secs = (time.perf_counter() - t0) / reps
+    coeffs = B.sine_taylor_coefficients(5, 1.0)
+    c2s = B.exact_coeff_to_slot_matrix(ctx, 8)
+    s2c = B.exact_slot_to_coeff_matrix(ctx, 8)
+    err = 0.0
+    for i in (0, batch - 1):
+        ev = np.array([sum(c * z ** k for k, c in enumerate(coeffs)) for z in c2s @ inputs[i]])
+        dec = ctx.decode_at_scale(ctx.decrypt(outs[i], kp.secret_key), outs[i].scale_bits)
+        err = max(err, float(np.max(np.abs(dec[:8] - s2c @ ev))))
+    res = {"workload": "exact sparse EvalMod bootstrap roundtrip, realistic_8_level (N=2^15, 8x50-bit + 2 aux), "
+                       "8 active slots, sine degree 5",
+           "bootstraps_per_s": round(batch / secs, 2), "ms_per_batch": round(secs * 1e3, 2), "batch": batch,
+           "single_ms": round(single * 1e3, 2), "batched_vs_single": round(single * batch / secs, 2),
+           "batch_equals_single": bool(np.array_equal(one.numpy(), outs[0].numpy())),
+           "decoded_max_abs_err": err, "prepare_s": round(t_prep, 2)}
+    try:  # the oracle's roundtrip on the host cores, same keys and input
+        O = load_oracle()
+        import algorithms as OA
+        import bootstrapping as OB
+
+        def coeff_keys(steps, level):  # the prepared form's keys again (deterministic samplers), coefficient form
+            return {s: (ctx.galois_element_for_rotation(s), np.ascontiguousarray(
+                ctx.generate_rotation_key_at_level(kp.secret_key, kp.public_key, s, level,
+                                                   return_coeff=True)[1].cpu().numpy().view(np.uint64)))
+                    for s in steps}
+        rk = boot.keys
+        okeys = {"c2s": coeff_keys(rk.coeff_to_slot_rotation_keys, boot.level),
+                 "s2c": coeff_keys(rk.slot_to_coeff_rotation_keys, boot.s2c_level),
+                 "eval_mod": {lv: np.ascontiguousarray(ctx.generate_relinearization_key_at_level(
+                     kp.secret_key, kp.public_key, lv, return_coeff=True)[1].cpu().numpy().view(np.uint64))
+                     for lv in rk.eval_mod_relinearization_keys}}
+        params = P.RnsCkksParams.realistic_8_level()
+        octx = OA.Context(params.poly_degree, params.primes, params.aux_primes)
+        h = cts[0].numpy()
+        t0 = time.perf_counter()
+        ref = OB.sparse_eval_mod_roundtrip(octx, OA.Ct(h[0].copy(), h[1].copy(), cts[0].scale_bits), 8, coeffs,
+                                           okeys)
+        osecs = time.perf_counter() - t0
+        res["bit_exact_vs_cpu"] = bool(np.array_equal(one.numpy()[0], ref.c0) and np.array_equal(one.numpy()[1], ref.c1))
+        res["cpu_oracle_s_per_bootstrap"] = round(osecs, 2)
+        res["cpu_cores"] = os.cpu_count()
+    except Exception as e:  # the GPU numbers stand on their own
+        res["cpu_oracle_error"] = str(e)[:200]
+    return res
 
 
 def serving_bench(pkg, C, seed, jobs_per_phase=240):
