@@ -45,7 +45,7 @@ cudaEvent_t HostPipe::event() {
 
 HostPipe::~HostPipe() {
   for (cudaEvent_t e : events) cudaEventDestroy(e);
-  for (cudaStream_t st : {in[0], in[1], comp, out})
+  for (cudaStream_t st : {in, comp, out})
     if (st) cudaStreamDestroy(st);
 }
 
@@ -1656,6 +1656,19 @@ extern "C" int rc_rotate_batch(rc_context* c, uint32_t count, const rc_ciphertex
 // inputs have landed; one key-product pass covers all jobs; then each chunk's inverse transforms and
 // finalize run and its results are copied out while the next chunk finishes.  Returns false (nothing
 // done) when the batch does not fit this form.
+// Stage boundaries of a pipelined host-buffer batch: the first stage has half the jobs of the others, so the
+// first compute starts once half as many bytes have crossed the host link (the last stage is the remainder).
+static std::vector<uint32_t> stage_bounds(uint32_t count, uint32_t chunk) {
+  std::vector<uint32_t> b{0};
+  uint32_t at = std::min(count, std::max<uint32_t>(1, chunk / 2));
+  b.push_back(at);
+  while (at < count) {
+    at = std::min(count, at + chunk);
+    b.push_back(at);
+  }
+  return b;
+}
+
 static bool mult_relin_host_phased(rc_context* c, HostPipe* hp, uint32_t count, const uint64_t* const* lhs,
                                    const uint64_t* const* rhs, const int32_t* levels, const int32_t* scale_bits,
                                    const rc_ksk* const* keys, uint64_t* const* out, int32_t* out_scale_bits,
@@ -1683,7 +1696,7 @@ static bool mult_relin_host_phased(rc_context* c, HostPipe* hp, uint32_t count, 
   // staging: inputs [J][lhs, rhs][2][limbs][N], outputs [J][2][limbs-1][N]
   const size_t stage = ((size_t)J * 4 * pl + (size_t)J * 2 * po) * 8;
   if (!hp->slot[0] || hp->slot[0]->bytes < stage) {
-    for (cudaStream_t st : {hp->in[0], hp->in[1], hp->comp, hp->out})
+    for (cudaStream_t st : {hp->in, hp->comp, hp->out})
       cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
     hp->slot[0].reset();
     hp->slot[0].reset(new DevBuf(stage));
@@ -1700,22 +1713,21 @@ static bool mult_relin_host_phased(rc_context* c, HostPipe* hp, uint32_t count, 
 
   cudaEvent_t start = hp->event();
   cuda_check(cudaEventRecord(start, s), "cudaEventRecord");
-  for (cudaStream_t st : {hp->in[0], hp->in[1], hp->comp, hp->out})
+  for (cudaStream_t st : {hp->in, hp->comp, hp->out})
     cuda_check(cudaStreamWaitEvent(st, start, 0), "cudaStreamWaitEvent");
-  const int nchunks = (J + chunk - 1) / chunk;
-  std::vector<cudaEvent_t> in_done(2 * nchunks), comp_done(nchunks);
-  for (int k = 0; k < nchunks; ++k) {  // every chunk's inputs, back to back on two copy streams
-    for (int j = k * chunk; j < std::min(J, (k + 1) * chunk); ++j) {
-      cuda_check(cudaMemcpyAsync(in_dev + (size_t)j * 4 * pl, lhs[j], 2 * pl * 8, cudaMemcpyHostToDevice, hp->in[0]),
+  const std::vector<uint32_t> bounds = stage_bounds((uint32_t)J, (uint32_t)chunk);
+  const int nchunks = (int)bounds.size() - 1;
+  std::vector<cudaEvent_t> in_done(nchunks), comp_done(nchunks);
+  for (int k = 0; k < nchunks; ++k) {  // every chunk's inputs, back to back in job order
+    for (int j = (int)bounds[k]; j < (int)bounds[k + 1]; ++j) {
+      cuda_check(cudaMemcpyAsync(in_dev + (size_t)j * 4 * pl, lhs[j], 2 * pl * 8, cudaMemcpyHostToDevice, hp->in),
                  "H2D");
       cuda_check(cudaMemcpyAsync(in_dev + (size_t)j * 4 * pl + 2 * pl, rhs[j], 2 * pl * 8, cudaMemcpyHostToDevice,
-                                 hp->in[1]),
+                                 hp->in),
                  "H2D");
     }
-    for (int q = 0; q < 2; ++q) {
-      in_done[2 * k + q] = hp->event();
-      cuda_check(cudaEventRecord(in_done[2 * k + q], hp->in[q]), "cudaEventRecord");
-    }
+    in_done[k] = hp->event();
+    cuda_check(cudaEventRecord(in_done[k], hp->in), "cudaEventRecord");
   }
   std::vector<KsJob> jobs(J);
   for (int j = 0; j < J; ++j) {
@@ -1723,8 +1735,8 @@ static bool mult_relin_host_phased(rc_context* c, HostPipe* hp, uint32_t count, 
     jobs[j] = KsJob{qd + 2 * pl, keys[j], qd, qd + pl, out_dev + (size_t)j * 2 * po, out_dev + (size_t)j * 2 * po + po};
   }
   for (int k = 0; k < nchunks; ++k) {
-    const int b0 = k * chunk, n = std::min(J, b0 + chunk) - b0;
-    for (int q = 0; q < 2; ++q) cuda_check(cudaStreamWaitEvent(hp->comp, in_done[2 * k + q], 0), "wait");
+    const int b0 = (int)bounds[k], n = (int)bounds[k + 1] - b0;
+    cuda_check(cudaStreamWaitEvent(hp->comp, in_done[k], 0), "wait");
     std::vector<const uint64_t*> Lp(n), Rp(n);
     std::vector<uint64_t*> Q(n);
     for (int j = 0; j < n; ++j) {
@@ -1738,7 +1750,7 @@ static bool mult_relin_host_phased(rc_context* c, HostPipe* hp, uint32_t count, 
   wide_ks_mac(c, w, jobs, hp->comp);
   const int drop = floor_log2(c->mod[limbs - 1]);
   for (int k = 0; k < nchunks; ++k) {
-    const int b0 = k * chunk, n = std::min(J, b0 + chunk) - b0;
+    const int b0 = (int)bounds[k], n = (int)bounds[k + 1] - b0;
     wide_ks_finish(c, w, jobs, b0, n, 0, true, hp->comp);
     comp_done[k] = hp->event();
     cuda_check(cudaEventRecord(comp_done[k], hp->comp), "cudaEventRecord");
@@ -1779,7 +1791,7 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
       auto& p = c->pipes[s];
       if (!p) {
         p.reset(new HostPipe());
-        for (cudaStream_t* st : {&p->in[0], &p->in[1], &p->comp, &p->out})
+        for (cudaStream_t* st : {&p->in, &p->comp, &p->out})
           cuda_check(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking), "cudaStreamCreate");
       }
       hp = p.get();
@@ -1790,19 +1802,20 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
     if (c->host_phased &&
         mult_relin_host_phased(c, hp, count, lhs, rhs, levels, scale_bits, keys, out, out_scale_bits, s, chunk))
       return;
-    const uint32_t nchunks = (count + chunk - 1) / chunk;
+    const std::vector<uint32_t> bounds = stage_bounds(count, (uint32_t)chunk);
+    const uint32_t nchunks = (uint32_t)bounds.size() - 1;
     auto in_elems = [&](uint32_t i) { return (size_t)2 * (levels[i] + 1) * c->N; };
     auto out_elems = [&](uint32_t i) { return (size_t)2 * levels[i] * c->N; };
     size_t need = 0;
     for (uint32_t k = 0; k < nchunks; ++k) {
       size_t b = 0;
-      for (uint32_t i = k * chunk; i < std::min<uint32_t>(count, (k + 1) * chunk); ++i)
+      for (uint32_t i = bounds[k]; i < bounds[k + 1]; ++i)
         b += 2 * in_elems(i) + out_elems(i);
       need = std::max(need, b * 8);
     }
     for (int sl = 0; sl < 2; ++sl) {
       if (!hp->slot[sl] || hp->slot[sl]->bytes < need) {
-        for (cudaStream_t st : {hp->in[0], hp->in[1], hp->comp, hp->out})
+        for (cudaStream_t st : {hp->in, hp->comp, hp->out})
           cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
         hp->slot[sl].reset();
         hp->slot[sl].reset(new DevBuf(need));
@@ -1810,33 +1823,33 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
     }
     cudaEvent_t start = hp->event();
     cuda_check(cudaEventRecord(start, s), "cudaEventRecord");
-    for (cudaStream_t st : {hp->in[0], hp->in[1], hp->comp, hp->out})
+    for (cudaStream_t st : {hp->in, hp->comp, hp->out})
       cuda_check(cudaStreamWaitEvent(st, start, 0), "cudaStreamWaitEvent");
     std::vector<cudaEvent_t> comp_done(nchunks), out_done(nchunks);
     for (uint32_t k = 0; k < nchunks; ++k) {
-      const uint32_t i0 = k * chunk, i1 = std::min<uint32_t>(count, i0 + chunk), n = i1 - i0;
+      const uint32_t i0 = bounds[k], i1 = bounds[k + 1], n = i1 - i0;
       uint64_t* dev = (uint64_t*)hp->slot[k & 1]->p;
       if (k >= 2) {  // the slot's inputs were consumed by chunk k-2's compute
-        for (int q = 0; q < 2; ++q) cuda_check(cudaStreamWaitEvent(hp->in[q], comp_done[k - 2], 0), "wait");
+        cuda_check(cudaStreamWaitEvent(hp->in, comp_done[k - 2], 0), "wait");
       }
       std::vector<rc_ciphertext> L(n), R(n), O(n);
       size_t off = 0;
       for (uint32_t j = 0; j < n; ++j) {
         const uint32_t i = i0 + j;
         L[j] = rc_ciphertext{dev + off, levels[i], scale_bits[i]};
-        cuda_check(cudaMemcpyAsync(dev + off, lhs[i], in_elems(i) * 8, cudaMemcpyHostToDevice, hp->in[0]), "H2D");
+        cuda_check(cudaMemcpyAsync(dev + off, lhs[i], in_elems(i) * 8, cudaMemcpyHostToDevice, hp->in), "H2D");
         off += in_elems(i);
         R[j] = rc_ciphertext{dev + off, levels[i], scale_bits[i]};
-        cuda_check(cudaMemcpyAsync(dev + off, rhs[i], in_elems(i) * 8, cudaMemcpyHostToDevice, hp->in[1]), "H2D");
+        cuda_check(cudaMemcpyAsync(dev + off, rhs[i], in_elems(i) * 8, cudaMemcpyHostToDevice, hp->in), "H2D");
         off += in_elems(i);
       }
       for (uint32_t j = 0; j < n; ++j) {
         O[j] = rc_ciphertext{dev + off, 0, 0};
         off += out_elems(i0 + j);
       }
-      for (int q = 0; q < 2; ++q) {
+      {
         cudaEvent_t e = hp->event();
-        cuda_check(cudaEventRecord(e, hp->in[q]), "cudaEventRecord");
+        cuda_check(cudaEventRecord(e, hp->in), "cudaEventRecord");
         cuda_check(cudaStreamWaitEvent(hp->comp, e, 0), "wait");
       }
       if (k >= 2) cuda_check(cudaStreamWaitEvent(hp->comp, out_done[k - 2], 0), "wait");  // slot outputs read
