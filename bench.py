@@ -445,6 +445,7 @@ def run_gpu(args):
         result["mixed_level_relin"] = mixed_level_relin(C, ctx, params, load_oracle(), args.seed)
         result["bsgs_matvec"] = bsgs_matvec_bench(pkg, C, args.seed)
         result["bootstrap"] = bootstrap_bench(pkg, C, args.seed)
+        result["key_serialization"] = key_serialization_bench(C, ctx, W["kp"], key)
         result["serving"] = serving_bench(pkg, C, args.seed)
     if rank == 0:
         print(json.dumps(result), flush=True)
@@ -686,6 +687,26 @@ def bootstrap_bench(pkg, C, seed, batch=16, reps=3):
     except Exception as e:  # the GPU numbers stand on their own
         res["cpu_oracle_error"] = str(e)[:200]
     return res
+
+
+def key_serialization_bench(C, ctx, kp, key):
+    """Saving and reloading the bench's relinearization key (the device-resident record, csrc/serialize.cu)
+    against generating it again on the GPU (host sampling + GPU arithmetic + transform)."""
+    import torch
+    t0 = time.perf_counter()
+    blob = key.to_bytes()
+    t_save = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    back = ctx.keyswitch_key_from_bytes(blob)
+    torch.cuda.synchronize()
+    t_load = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    again = ctx.generate_relinearization_key(kp.secret_key, kp.public_key, C.Sampler(123))
+    torch.cuda.synchronize()
+    t_gen = time.perf_counter() - t0
+    del again
+    return {"record_bytes": len(blob), "save_s": round(t_save, 3), "load_s": round(t_load, 3),
+            "generate_s": round(t_gen, 3), "reloaded_level": back.level}
 
 
 def serving_bench(pkg, C, seed, jobs_per_phase=240):

@@ -108,6 +108,15 @@ int rc_ksk_upload_device(rc_context* ctx, const uint64_t* device_key, uint32_t d
 int rc_ksk_truncate(rc_context* ctx, const rc_ksk* key, int32_t level, rc_ksk** out);
 int rc_ksk_info(const rc_ksk* key, uint32_t* digits, int32_t* level, uint32_t* aux_count, uint64_t* galois_element);
 void rc_ksk_destroy(rc_ksk* key);
+/* Serialised keys (no counterpart in the reference, which has none): a 96-byte header (magic "RCKSKEY1",
+ * version, form, N, digits, level, aux_count, galois element, payload bytes, fingerprint of the modulus chain,
+ * payload checksum) followed by the key exactly as it is resident (NTT domain, the library's layout), so
+ * reloading is one host->device copy.  A record loads only into a context with the same ring degree and
+ * modulus chain; a truncated Q-only key serialises its prefix of limbs.  rc_ksk_serialize writes into a
+ * caller buffer of at least rc_ksk_serialized_size bytes and returns when the buffer is filled. */
+int rc_ksk_serialized_size(const rc_ksk* key, uint64_t* bytes);
+int rc_ksk_serialize(rc_context* ctx, const rc_ksk* key, void* host_buf, uint64_t buf_bytes, void* stream);
+int rc_ksk_deserialize(rc_context* ctx, const void* host_buf, uint64_t buf_bytes, rc_ksk** out);
 
 /* ---- polynomial-level ops (device pointers, limb-major) ---- */
 /* NttPlan::forward/inverse composed with the negacyclic twist
@@ -164,6 +173,16 @@ int rc_multiply_plain_rns_batch(rc_context* ctx, uint32_t count, const rc_cipher
                                 const uint64_t* const* plains, rc_ciphertext* out, void* stream);
 /* `count` independent rescales (context/ops.rs:32-37) in one call */
 int rc_rescale_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* ct, rc_ciphertext* out, void* stream);
+/* Serialised ciphertexts: a 64-byte header (magic "RCCTXT01", version, components (2 or 3), N, level,
+ * scale_bits, payload bytes, modulus-chain fingerprint, checksum) followed by the [components][level+1][N]
+ * coefficient-form residues.  rc_ct_header reads the header of a record (no context needed) so the caller can
+ * allocate the device buffer rc_ct_deserialize fills; out->level and out->scale_bits are set from the record. */
+int rc_ct_serialized_size(const rc_context* ctx, int32_t level, uint32_t components, uint64_t* bytes);
+int rc_ct_serialize(rc_context* ctx, const rc_ciphertext* ct, uint32_t components, void* host_buf,
+                    uint64_t buf_bytes, void* stream);
+int rc_ct_header(const void* host_buf, uint64_t buf_bytes, uint64_t* poly_degree, int32_t* level,
+                 int32_t* scale_bits, uint32_t* components);
+int rc_ct_deserialize(rc_context* ctx, const void* host_buf, uint64_t buf_bytes, rc_ciphertext* out, void* stream);
 /* lift_poly_to_context: src/rns/keyswitching.rs:242-276 (convert_centered_residues_to_target, 365-379).
  * `polys` polynomials over Q_limbs ([polys][limbs][N]) -> over Q_limbs followed by the aux primes
  * ([polys][limbs + aux_count][N]): the Q limbs are copied, each aux limb is the centred CRT value (the tie

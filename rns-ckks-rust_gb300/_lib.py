@@ -67,6 +67,14 @@ SIGNATURES = [
     ("rc_ksk_info", ctypes.c_int, [_vp, ctypes.POINTER(_u32), ctypes.POINTER(_i32), ctypes.POINTER(_u32),
                                    ctypes.POINTER(_u64)]),
     ("rc_ksk_destroy", None, [_vp]),
+    ("rc_ksk_serialized_size", ctypes.c_int, [_vp, ctypes.POINTER(_u64)]),
+    ("rc_ksk_serialize", ctypes.c_int, [_vp, _vp, _vp, _u64, _vp]),
+    ("rc_ksk_deserialize", ctypes.c_int, [_vp, _vp, _u64, ctypes.POINTER(_vp)]),
+    ("rc_ct_serialized_size", ctypes.c_int, [_vp, _i32, _u32, ctypes.POINTER(_u64)]),
+    ("rc_ct_serialize", ctypes.c_int, [_vp, _CT, _u32, _vp, _u64, _vp]),
+    ("rc_ct_header", ctypes.c_int, [_vp, _u64, ctypes.POINTER(_u64), ctypes.POINTER(_i32), ctypes.POINTER(_i32),
+                                    ctypes.POINTER(_u32)]),
+    ("rc_ct_deserialize", ctypes.c_int, [_vp, _vp, _u64, _CT, _vp]),
     ("rc_ntt_forward", ctypes.c_int, [_vp, _vp, _u32, _u32, _i32, _vp]),
     ("rc_ntt_inverse", ctypes.c_int, [_vp, _vp, _u32, _u32, _i32, _vp]),
     ("rc_poly_multiply", ctypes.c_int, [_vp, _vp, _vp, _vp, _u32, _i32, _vp]),

@@ -218,6 +218,18 @@ class RnsKeySwitchingKey:
         call("rc_ksk_truncate", self.ctx.handle, self.handle, level_count - 1, ctypes.byref(out))
         return RnsKeySwitchingKey(self.ctx, out, owner=self)
 
+    def to_bytes(self) -> bytes:
+        """The resident key as a serialised record (rc_ksk_serialize)."""
+        size = ctypes.c_uint64()
+        call("rc_ksk_serialized_size", self.handle, ctypes.byref(size))
+        buf = torch.empty(size.value, dtype=torch.uint8, pin_memory=torch.cuda.is_available())
+        call("rc_ksk_serialize", self.ctx.handle, self.handle, buf.data_ptr(), size.value, _stream())
+        return buf.numpy().tobytes()
+
+    def save(self, path) -> None:
+        with open(path, "wb") as f:
+            f.write(self.to_bytes())
+
 
 @dataclass
 class RnsRotationKey:
@@ -489,6 +501,43 @@ class RnsCkksContext:
         call("rc_ksk_upload", self.handle, host_key.ctypes.data, host_key.shape[0], level, aux_level_count,
              galois_element, ctypes.byref(handle))
         return RnsKeySwitchingKey(self, handle)
+
+    # ---- serialised keys and ciphertexts (csrc/serialize.cu) ----
+    def keyswitch_key_from_bytes(self, data) -> RnsKeySwitchingKey:
+        """A key saved by `RnsKeySwitchingKey.to_bytes`/`save` on a context with the same modulus chain."""
+        buf = np.frombuffer(data, dtype=np.uint8)
+        out = ctypes.c_void_p()
+        call("rc_ksk_deserialize", self.handle, buf.ctypes.data, buf.size, ctypes.byref(out))
+        return RnsKeySwitchingKey(self, out)
+
+    def load_keyswitch_key(self, path) -> RnsKeySwitchingKey:
+        with open(path, "rb") as f:
+            return self.keyswitch_key_from_bytes(f.read())
+
+    def load_rotation_key(self, path) -> "RnsRotationKey":
+        k = self.load_keyswitch_key(path)
+        return RnsRotationKey(k.galois_element, k)
+
+    def ciphertext_to_bytes(self, ct: "RnsCiphertext") -> bytes:
+        comps = ct.data.shape[0]
+        size = ctypes.c_uint64()
+        call("rc_ct_serialized_size", self.handle, ct.level, comps, ctypes.byref(size))
+        buf = np.empty(size.value, dtype=np.uint8)
+        call("rc_ct_serialize", self.handle, ctypes.byref(ct.raw()), comps, buf.ctypes.data, size.value, _stream())
+        return buf.tobytes()
+
+    def ciphertext_from_bytes(self, data) -> "RnsCiphertext":
+        buf = np.frombuffer(data, dtype=np.uint8)
+        n, lv, sb, comps = ctypes.c_uint64(), ctypes.c_int32(), ctypes.c_int32(), ctypes.c_uint32()
+        call("rc_ct_header", buf.ctypes.data, buf.size, ctypes.byref(n), ctypes.byref(lv), ctypes.byref(sb),
+             ctypes.byref(comps))
+        if n.value != self.params.poly_degree or not (0 <= lv.value < self.levels()) or comps.value not in (2, 3):
+            raise RcError(1, "serialized ciphertext was made for another modulus chain")
+        data_t = torch.empty((comps.value, lv.value + 1, n.value), dtype=torch.int64, device="cuda")
+        o = RcCiphertext(data_t.data_ptr(), 0, 0)
+        call("rc_ct_deserialize", self.handle, buf.ctypes.data, buf.size, ctypes.byref(o), _stream())
+        cls = RnsQuadraticCiphertext if comps.value == 3 else RnsCiphertext
+        return cls(data_t, o.scale_bits, o.level)
 
     def _source_square(self, sk: RnsSecretKey, level: int) -> torch.Tensor:
         s = sk.poly.data[: level + 1].contiguous()

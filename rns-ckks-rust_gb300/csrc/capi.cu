@@ -51,23 +51,6 @@ HostPipe::~HostPipe() {
 
 }  // namespace rc
 
-template <class F>
-static int guarded(F&& f) {
-  try {
-    f();
-    return RC_OK;
-  } catch (const ApiError& e) {
-    g_err = e.what();
-    return e.code;
-  } catch (const std::bad_alloc&) {
-    g_err = "host allocation failed";
-    return RC_ERR_OUT_OF_MEMORY;
-  } catch (const std::exception& e) {
-    g_err = e.what();
-    return RC_ERR_CUDA;
-  }
-}
-
 namespace {
 
 typedef unsigned __int128 u128h;
@@ -535,6 +518,13 @@ void check_mult_pair(const rc_context* c, const rc_ciphertext* a, const rc_ciphe
 }
 
 }  // namespace
+
+namespace rc {
+const LevelInfo& context_level(const rc_context* c, int limbs) { return level_info(c, limbs); }
+bool context_wide_applies(const rc_context* c, int qlimbs, int K, int D) { return wide_applies(c, qlimbs, K, D); }
+void context_check_ct(const rc_context* c, const rc_ciphertext* ct, const char* name) { check_ct(c, ct, name); }
+uint64_t context_galois_inverse(const rc_context* c, uint64_t g) { return galois_inverse(c, g); }
+}  // namespace rc
 
 // =========================================================================
 // context

@@ -29,6 +29,25 @@ inline void require(bool cond, const std::string& msg) {
 void cuda_check(cudaError_t e, const char* what);
 void set_last_error(const std::string& m);
 
+// Runs an entry point's body: an ApiError becomes its status code and rc_last_error message; allocation
+// failures and CUDA errors become RC_ERR_OUT_OF_MEMORY / RC_ERR_CUDA.  Nothing escapes the C ABI.
+template <class F>
+int guarded(F&& f) {
+  try {
+    f();
+    return RC_OK;
+  } catch (const ApiError& e) {
+    set_last_error(e.what());
+    return e.code;
+  } catch (const std::bad_alloc&) {
+    set_last_error("host allocation failed");
+    return RC_ERR_OUT_OF_MEMORY;
+  } catch (const std::exception& e) {
+    set_last_error(e.what());
+    return RC_ERR_CUDA;
+  }
+}
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;
@@ -126,3 +145,11 @@ struct rc_ksk {
   uint64_t galois = 0;
   uint32_t limbs() const { return (uint32_t)level + 1 + aux; }
 };
+
+namespace rc {
+// context queries shared by the C ABI's translation units (defined in capi.cu)
+const LevelInfo& context_level(const rc_context* c, int limbs);
+bool context_wide_applies(const rc_context* c, int qlimbs, int K, int D);
+void context_check_ct(const rc_context* c, const rc_ciphertext* ct, const char* name);
+uint64_t context_galois_inverse(const rc_context* c, uint64_t g);
+}  // namespace rc

@@ -272,3 +272,82 @@ def paterson_stockmeyer_job(ctx, ct, coeffs, keys, plains=None) -> Job:
     return Job("paterson_stockmeyer", ("paterson_stockmeyer", id(ctx), ct.level, ct.scale_bits,
                                        tuple(float(c) for c in coeffs), id(keys)), fp,
                {"ctx": ctx, "ct": ct, "coeffs": list(coeffs), "keys": keys, "plains": plains})
+
+
+class KeyStore:
+    """Device-resident keys kept as serialised records in a directory, so a restarted server reloads them with
+    one host->device copy each instead of generating and transforming them again.
+
+    Keys are stored by name, singly (`put`) or as groups keyed by an integer (`put_group`: rotation keys by
+    step, relinearization keys by level); `index.json` lists names, files and kinds.  `KeyStore.open` on a
+    context with the same modulus chain reloads everything (a record made for another chain is refused by
+    the library)."""
+
+    INDEX = "index.json"
+
+    def __init__(self, ctx, directory):
+        import os
+        self.ctx, self.dir = ctx, str(directory)
+        os.makedirs(self.dir, exist_ok=True)
+        self.index: Dict[str, Dict[str, Any]] = {}
+        self.keys: Dict[str, Any] = {}
+
+    def _path(self, fname: str) -> str:
+        import os
+        return os.path.join(self.dir, fname)
+
+    def _write_index(self) -> None:
+        import json
+        import os
+        tmp = self._path(self.INDEX + ".tmp")
+        with open(tmp, "w") as f:
+            json.dump(self.index, f, indent=1, sort_keys=True)
+        os.replace(tmp, self._path(self.INDEX))
+
+    @staticmethod
+    def _switching_key(key):
+        return getattr(key, "keyswitch_key", key)
+
+    def _save_one(self, fname: str, key) -> None:
+        self._switching_key(key).save(self._path(fname))
+
+    def put(self, name: str, key) -> None:
+        kind = "rotation" if hasattr(key, "keyswitch_key") else "keyswitch"
+        fname = f"{name}.rcksk"
+        self._save_one(fname, key)
+        self.index[name] = {"kind": kind, "file": fname}
+        self.keys[name] = key
+        self._write_index()
+
+    def put_group(self, name: str, keys: Dict[int, Any]) -> None:
+        files, kind = {}, "keyswitch"
+        for k, key in keys.items():
+            kind = "rotation" if hasattr(key, "keyswitch_key") else "keyswitch"
+            fname = f"{name}.{int(k)}.rcksk"
+            self._save_one(fname, key)
+            files[str(int(k))] = fname
+        self.index[name] = {"kind": kind, "group": files}
+        self.keys[name] = dict(keys)
+        self._write_index()
+
+    def get(self, name: str):
+        return self.keys[name]
+
+    def _load(self, kind: str, fname: str):
+        if kind == "rotation":
+            return self.ctx.load_rotation_key(self._path(fname))
+        return self.ctx.load_keyswitch_key(self._path(fname))
+
+    @classmethod
+    def open(cls, ctx, directory) -> "KeyStore":
+        """Reload every key listed in the directory's index onto `ctx`."""
+        import json
+        store = cls(ctx, directory)
+        with open(store._path(cls.INDEX)) as f:
+            store.index = json.load(f)
+        for name, entry in store.index.items():
+            if "group" in entry:
+                store.keys[name] = {int(k): store._load(entry["kind"], fn) for k, fn in entry["group"].items()}
+            else:
+                store.keys[name] = store._load(entry["kind"], entry["file"])
+        return store
