@@ -157,6 +157,22 @@ int rc_poly_mul_scalar(rc_context* ctx, const uint64_t* a, const uint64_t* scala
 int rc_poly_automorphism(rc_context* ctx, const uint64_t* a, uint64_t* out, uint32_t limbs, uint64_t galois_element,
                          void* stream);
 
+/* ---- seeded samplers on the device (key generation and encryption inputs) ----
+ * The distributions of src/rns/keys.rs, written as residues over `limbs` limbs (with_aux as for
+ * rc_poly_multiply) into out[limbs][N]: rc_sample_uniform = 64 random bits mod q_j per residue
+ * (sample_uniform_poly, keys.rs:87-99); rc_sample_error = round(N(0, 3.19)) per coefficient, the same integer
+ * in every limb (sample_gaussian_i64 / sample_error_poly, keys.rs:82-85,101-121); rc_sample_ternary = uniform
+ * {0, 1, -1} per coefficient (sample_ternary_poly, keys.rs:123-147).  Every value is a function of
+ * (seed, stream_id, index) through Philox4x32-10, so a (seed, stream_id) pair names one reproducible sample;
+ * callers use a distinct stream_id for each polynomial they draw.  The reference seeds from the OS, so its
+ * samples are not reproducible and are not compared value for value. */
+int rc_sample_uniform(rc_context* ctx, uint64_t seed, uint64_t stream_id, uint64_t* out, uint32_t limbs,
+                      int32_t with_aux, void* stream);
+int rc_sample_error(rc_context* ctx, uint64_t seed, uint64_t stream_id, uint64_t* out, uint32_t limbs,
+                    int32_t with_aux, void* stream);
+int rc_sample_ternary(rc_context* ctx, uint64_t seed, uint64_t stream_id, uint64_t* out, uint32_t limbs,
+                      int32_t with_aux, void* stream);
+
 /* ---- ciphertext ops (RnsCkksContext, src/rns/context/ops.rs) ---- */
 /* RnsCiphertext::add: src/rns/ciphertexts.rs:60-69 */
 int rc_add(rc_context* ctx, const rc_ciphertext* lhs, const rc_ciphertext* rhs, rc_ciphertext* out, void* stream);

@@ -83,6 +83,9 @@ SIGNATURES = [
     ("rc_poly_mul_scalar", ctypes.c_int, [_vp, _vp, _vp, _vp, _u32, _i32, _vp]),
     ("rc_poly_multiply_noalloc", ctypes.c_int, [_vp, _vp, _vp, _vp, _u32, _i32, _vp]),
     ("rc_poly_automorphism", ctypes.c_int, [_vp, _vp, _vp, _u32, _u64, _vp]),
+    ("rc_sample_uniform", ctypes.c_int, [_vp, _u64, _u64, _vp, _u32, _i32, _vp]),
+    ("rc_sample_error", ctypes.c_int, [_vp, _u64, _u64, _vp, _u32, _i32, _vp]),
+    ("rc_sample_ternary", ctypes.c_int, [_vp, _u64, _u64, _vp, _u32, _i32, _vp]),
     ("rc_add", ctypes.c_int, [_vp, _CT, _CT, _CT, _vp]),
     ("rc_mult_plain", ctypes.c_int, [_vp, _CT, _vp, _CT, _vp]),
     ("rc_multiply_plain_rns", ctypes.c_int, [_vp, _CT, _vp, _CT, _vp]),

@@ -276,6 +276,36 @@ class Sampler:
         return out
 
 
+class DeviceSampler:
+    """The same distributions drawn on the GPU (`rc_sample_uniform/error/ternary`, Philox4x32-10): each draw
+    takes the next stream id, so the seed fixes the whole sequence and a polynomial is one launch with no
+    host-to-device copy.  Draws are residue tensors [limbs][N] over the first `limbs` chain primes, or over
+    Q_(limbs-aux) u P with `with_aux`.  The secret key's fixed-weight ternary draw (a choice of positions)
+    stays on the host generator."""
+
+    def __init__(self, ctx: "RnsCkksContext", seed: int = 0):
+        self.ctx, self.seed, self.next_id = ctx, int(seed) & (2 ** 64 - 1), 0
+        self.host = Sampler(seed)
+
+    def _draw(self, fn: str, limbs: int, with_aux: bool) -> torch.Tensor:
+        out = torch.empty((limbs, self.ctx.params.poly_degree), dtype=torch.int64, device="cuda")
+        call(fn, self.ctx.handle, self.seed, self.next_id, _ptr(out), limbs, int(with_aux), _stream())
+        self.next_id += 1
+        return out
+
+    def uniform_residues(self, limbs: int, with_aux: bool = False) -> torch.Tensor:
+        return self._draw("rc_sample_uniform", limbs, with_aux)
+
+    def error_residues(self, limbs: int, with_aux: bool = False) -> torch.Tensor:
+        return self._draw("rc_sample_error", limbs, with_aux)
+
+    def ternary_residues(self, limbs: int, with_aux: bool = False) -> torch.Tensor:
+        return self._draw("rc_sample_ternary", limbs, with_aux)
+
+    def sparse_ternary(self, n: int, hamming_weight: int) -> np.ndarray:
+        return self.host.sparse_ternary(n, hamming_weight)
+
+
 def signed_to_residues(coeffs: np.ndarray, moduli: Sequence[int]) -> np.ndarray:
     c = np.asarray(coeffs, dtype=np.int64)
     return np.stack([(c % np.int64(q)).astype(np.uint64) for q in moduli])
@@ -414,16 +444,21 @@ class RnsCkksContext:
                samples: Optional[Tuple[np.ndarray, np.ndarray, np.ndarray]] = None) -> RnsKeyPair:
         """`rns_keygen` (keys.rs:153-166): p0 = e - p1*s.  `samples` = (s, p1, e)."""
         n = self.params.poly_degree
-        if samples is None:
-            sampler = sampler or Sampler()
+        if isinstance(sampler, DeviceSampler) and samples is None:
             s = sampler.sparse_ternary(n, hamming_weight)
-            p1 = sampler.uniform(self.q_moduli, n)
-            e = sampler.gaussian(n)
+            p1d = sampler.uniform_residues(len(self.q_moduli))
+            ed = sampler.error_residues(len(self.q_moduli))
         else:
-            s, p1, e = samples
+            if samples is None:
+                sampler = sampler or Sampler()
+                s = sampler.sparse_ternary(n, hamming_weight)
+                p1 = sampler.uniform(self.q_moduli, n)
+                e = sampler.gaussian(n)
+            else:
+                s, p1, e = samples
+            ed = to_device(signed_to_residues(e, self.q_moduli))
+            p1d = to_device(p1)
         sd = to_device(signed_to_residues(s, self.q_moduli))
-        ed = to_device(signed_to_residues(e, self.q_moduli))
-        p1d = to_device(p1)
         p0 = self._poly_sub(ed, self._poly_mul(p1d, sd))
         return RnsKeyPair(RnsSecretKey(np.asarray(s, dtype=np.int64), RnsPolynomial(sd)),
                           RnsPublicKey(RnsPolynomial(p0), RnsPolynomial(p1d)), RnsPolynomial(ed))
@@ -452,11 +487,14 @@ class RnsCkksContext:
             pt = self._poly_scalar(ext, scal, with_aux=True)
             if samples is not None:
                 a1, e = samples[i]
+                a1d = to_device(a1)
+                ed = to_device(signed_to_residues(e, allm) if np.asarray(e).ndim == 1 else e)
+            elif isinstance(sampler, DeviceSampler):
+                a1d = sampler.uniform_residues(len(allm), True)
+                ed = sampler.error_residues(len(allm), True)
             else:
-                a1 = sampler.uniform(allm, n)
-                e = sampler.gaussian(n)
-            a1d = to_device(a1)
-            ed = to_device(signed_to_residues(e, allm) if np.asarray(e).ndim == 1 else e)
+                a1d = to_device(sampler.uniform(allm, n))
+                ed = to_device(signed_to_residues(sampler.gaussian(n), allm))
             a1s = self._poly_mul(a1d, target, with_aux=True)
             key[i, 0] = self._poly_sub(self._poly_add(pt, ed, True), a1s, True)
             key[i, 1] = a1d
@@ -477,6 +515,9 @@ class RnsCkksContext:
             pt = self._poly_scalar(src, [pow(2, DECOMP_BITS * i, m) for m in qm])
             if samples is not None:
                 u, e0, e1 = samples[i]
+            elif isinstance(sampler, DeviceSampler):
+                lq = len(qm)
+                u, e0, e1 = sampler.ternary_residues(lq), sampler.error_residues(lq), sampler.error_residues(lq)
             else:
                 u, e0, e1 = sampler.ternary(n), sampler.gaussian(n), sampler.gaussian(n)
             c0, c1 = self._encrypt_raw(pt, p0, p1, u, e0, e1, qm)
@@ -596,9 +637,11 @@ class RnsCkksContext:
 
     # ---- encryption, src/rns/ops.rs:8-52 ----
     def _encrypt_raw(self, pt, p0, p1, u, e0, e1, moduli):
-        ud = to_device(signed_to_residues(u, moduli)) if np.asarray(u).ndim == 1 else to_device(u)
-        e0d = to_device(signed_to_residues(e0, moduli)) if np.asarray(e0).ndim == 1 else to_device(e0)
-        e1d = to_device(signed_to_residues(e1, moduli)) if np.asarray(e1).ndim == 1 else to_device(e1)
+        def residues(x):
+            if isinstance(x, torch.Tensor):  # already device residues (DeviceSampler)
+                return x
+            return to_device(signed_to_residues(x, moduli)) if np.asarray(x).ndim == 1 else to_device(x)
+        ud, e0d, e1d = residues(u), residues(e0), residues(e1)
         c0 = self._poly_add(self._poly_add(self._poly_mul(p0, ud), e0d), pt)
         c1 = self._poly_add(self._poly_mul(p1, ud), e1d)
         return c0, c1
@@ -609,7 +652,10 @@ class RnsCkksContext:
         if plaintext.levels() != self.levels():
             raise RcError(1, "plaintext levels must match the active RNS context")
         n = self.params.poly_degree
-        if samples is None:
+        if samples is None and isinstance(sampler, DeviceSampler):
+            lq = len(self.q_moduli)
+            samples = (sampler.ternary_residues(lq), sampler.error_residues(lq), sampler.error_residues(lq))
+        elif samples is None:
             sampler = sampler or Sampler()
             samples = (sampler.ternary(n), sampler.gaussian(n), sampler.gaussian(n))
         c0, c1 = self._encrypt_raw(plaintext.data, public_key.p0.data, public_key.p1.data, *samples, self.q_moduli)

@@ -1062,6 +1062,10 @@ static LimbMap basis_map(const rc_context* c, uint32_t limbs, int32_t with_aux) 
   return LimbMap{(int)limbs, c->L};
 }
 
+LimbMap rc::context_basis_map(const rc_context* c, uint32_t limbs, int32_t with_aux) {
+  return basis_map(c, limbs, with_aux);
+}
+
 extern "C" int rc_poly_multiply(rc_context* c, const uint64_t* a, const uint64_t* b, uint64_t* out, uint32_t limbs,
                                 int32_t with_aux, void* stream) {
   return guarded([&] {

@@ -152,4 +152,5 @@ const LevelInfo& context_level(const rc_context* c, int limbs);
 bool context_wide_applies(const rc_context* c, int qlimbs, int K, int D);
 void context_check_ct(const rc_context* c, const rc_ciphertext* ct, const char* name);
 uint64_t context_galois_inverse(const rc_context* c, uint64_t g);
+LimbMap context_basis_map(const rc_context* c, uint32_t limbs, int32_t with_aux);
 }  // namespace rc
