@@ -283,6 +283,14 @@ int rc_encode(const rc_context* ctx, const double* slots, int32_t level, uint32_
 /* reconstruct_coefficients + decode_integer_coeffs: polynomial.rs:162-201, encoding.rs:33-66 */
 int rc_decode(const rc_context* ctx, const uint64_t* poly_host, int32_t level, uint32_t scale_bits,
               double* slots_out);
+/* The same encode and decode on the GPU, bit for bit (same FFT twiddles and order, every product and sum
+ * rounded separately, same rounding and CRT): `count` plaintexts per call, device buffers.  Encode: slots
+ * [count][N/2] complex as interleaved (re, im) doubles -> out [count][level+1][N] residues.  Decode: polys
+ * [count][level+1][N] -> slots [count][N/2] interleaved (count <= 65535). */
+int rc_encode_device(rc_context* ctx, const double* slots, uint32_t count, int32_t level, uint32_t scale_bits,
+                     uint64_t* out, void* stream);
+int rc_decode_device(rc_context* ctx, const uint64_t* polys, uint32_t count, int32_t level, uint32_t scale_bits,
+                     double* slots_out, void* stream);
 /* The two slot/coefficient maps the exact bootstrapping transforms are built from, in FP64 with the
  * reference's operation order; they need no context (n = ring degree).
  * dense_slots_to_real_coeffs (src/ckks/bootstrapping/exact_transforms.rs:180-200): n/2 complex slots

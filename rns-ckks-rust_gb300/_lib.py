@@ -118,6 +118,8 @@ SIGNATURES = [
                                                        ctypes.POINTER(_i32), _vp]),
     ("rc_encode", ctypes.c_int, [_vp, _vp, _i32, _u32, _vp]),
     ("rc_decode", ctypes.c_int, [_vp, _vp, _i32, _u32, _vp]),
+    ("rc_encode_device", ctypes.c_int, [_vp, _vp, _u32, _i32, _u32, _vp, _vp]),
+    ("rc_decode_device", ctypes.c_int, [_vp, _vp, _u32, _i32, _u32, _vp, _vp]),
     ("rc_slots_to_real_coeffs", ctypes.c_int, [_u64, _vp, _vp]),
     ("rc_complex_coeffs_to_slots", ctypes.c_int, [_u64, _vp, _vp]),
     ("rc_profile_enable", ctypes.c_int, [ctypes.c_int]),

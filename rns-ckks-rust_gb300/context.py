@@ -393,6 +393,28 @@ class RnsCkksContext:
     def encode_at_level_and_scale(self, slots, level: int, scale_bits: int) -> RnsPolynomial:
         return RnsPolynomial(to_device(self.encode_host(slots, level, scale_bits)))
 
+    def encode_device_batch(self, slots_list: Sequence, level: int, scale_bits: int) -> List[RnsPolynomial]:
+        """Encode many slot vectors on the GPU (rc_encode_device): the same residues as `encode_host`."""
+        if not len(slots_list):
+            return []
+        s = np.asarray(slots_list, dtype=np.complex128).reshape(len(slots_list), -1)
+        if s.shape[1] != self.num_slots():
+            raise RcError(1, "slot count must be N/2")
+        src = torch.from_numpy(np.ascontiguousarray(np.stack([s.real, s.imag], axis=2))).to("cuda")
+        out = torch.empty((len(slots_list), level + 1, self.params.poly_degree), dtype=torch.int64, device="cuda")
+        call("rc_encode_device", self.handle, _ptr(src), len(slots_list), level, scale_bits, _ptr(out), _stream())
+        return [RnsPolynomial(out[i]) for i in range(out.shape[0])]
+
+    def decode_device_batch(self, polys: Sequence[RnsPolynomial], scale_bits: int) -> np.ndarray:
+        """Decode many polynomials of one level on the GPU (rc_decode_device): the same values as
+        `decode_host`; returns [count][N/2] complex."""
+        data = torch.stack([p.data for p in polys]).contiguous()
+        out = torch.empty((data.shape[0], self.num_slots(), 2), dtype=torch.float64, device="cuda")
+        call("rc_decode_device", self.handle, _ptr(data), data.shape[0], data.shape[1] - 1, scale_bits, _ptr(out),
+             _stream())
+        h = out.cpu().numpy()
+        return h[..., 0] + 1j * h[..., 1]
+
     def decode_host(self, poly: np.ndarray, scale_bits: int) -> np.ndarray:
         poly = np.ascontiguousarray(poly, dtype=np.uint64)
         out = np.empty(self.params.poly_degree, dtype=np.float64)

@@ -1066,6 +1066,8 @@ LimbMap rc::context_basis_map(const rc_context* c, uint32_t limbs, int32_t with_
   return basis_map(c, limbs, with_aux);
 }
 
+void* rc::context_workspace(rc_context* c, cudaStream_t s, size_t bytes) { return ws_device(c, s, bytes); }
+
 extern "C" int rc_poly_multiply(rc_context* c, const uint64_t* a, const uint64_t* b, uint64_t* out, uint32_t limbs,
                                 int32_t with_aux, void* stream) {
   return guarded([&] {

@@ -99,6 +99,7 @@ struct rc_context {
   rc::WidePrimes wp{};    // internal primes, transform constants and twiddle tables (wide_tw)
   rc::WideTab wide{};     // CRT back to the scheme primes (tables in wide_buf)
   std::unique_ptr<rc::DevBuf> wide_buf, wide_tw;
+  std::unique_ptr<rc::DevBuf> fft_buf;  // device encoder tables (built on first use, under mu)
   std::vector<uint64_t> mod, root;  // Q then P
   std::unique_ptr<rc::DevBuf> pc_buf, tw_buf, md_buf, rt_buf;
   rc::PrimeConst* d_pc = nullptr;
@@ -153,4 +154,8 @@ bool context_wide_applies(const rc_context* c, int qlimbs, int K, int D);
 void context_check_ct(const rc_context* c, const rc_ciphertext* ct, const char* name);
 uint64_t context_galois_inverse(const rc_context* c, uint64_t g);
 LimbMap context_basis_map(const rc_context* c, uint32_t limbs, int32_t with_aux);
+void* context_workspace(rc_context* c, cudaStream_t s, size_t bytes);
+// host FFT values for the device encoder (encode.cpp)
+void fft_tables(size_t n, std::vector<double>& tw_inv, std::vector<double>& tw_fwd, std::vector<double>& xi_neg,
+                std::vector<double>& xi_pos);
 }  // namespace rc

@@ -247,3 +247,36 @@ extern "C" int rc_complex_coeffs_to_slots(uint64_t n, const double* coeffs, doub
     return RC_ERR_OUT_OF_MEMORY;
   }
 }
+
+// The values the host FFT uses, for the device encoder/decoder to reproduce it bit for bit: per stage
+// len = 2, 4, ..., n the twiddles w_i (i < len/2) by fft_in_place's recurrence w *= w_len, stored from
+// complex offset len/2 - 1 (n - 1 entries per direction), and the twists xi^-i (encode) and xi^i (decode).
+// Interleaved (re, im).
+void rc::fft_tables(size_t n, std::vector<double>& tw_inv, std::vector<double>& tw_fwd, std::vector<double>& xi_neg,
+                    std::vector<double>& xi_pos) {
+  tw_inv.assign(2 * (n - 1), 0.0);
+  tw_fwd.assign(2 * (n - 1), 0.0);
+  for (int dir = 0; dir < 2; ++dir) {
+    std::vector<double>& t = dir ? tw_inv : tw_fwd;
+    for (size_t len = 2; len <= n; len <<= 1) {
+      const double angle = dir ? -2.0 * M_PI / (double)len : 2.0 * M_PI / (double)len;
+      const C w_len = polar(angle);
+      C w{1.0, 0.0};
+      for (size_t i = 0; i < len / 2; ++i) {
+        t[2 * (len / 2 - 1 + i)] = w.re;
+        t[2 * (len / 2 - 1 + i) + 1] = w.im;
+        w = cmul(w, w_len);
+      }
+    }
+  }
+  const C xi = polar(M_PI / (double)n);
+  xi_neg.resize(2 * n);
+  xi_pos.resize(2 * n);
+  for (size_t i = 0; i < n; ++i) {
+    const C a = cpowi(xi, -(long)i), b = cpowi(xi, (long)i);
+    xi_neg[2 * i] = a.re;
+    xi_neg[2 * i + 1] = a.im;
+    xi_pos[2 * i] = b.re;
+    xi_pos[2 * i + 1] = b.im;
+  }
+}
