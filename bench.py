@@ -453,6 +453,7 @@ def run_gpu(args):
         result["bsgs_matvec"] = bsgs_matvec_bench(pkg, C, args.seed)
         result["bootstrap"] = bootstrap_bench(pkg, C, args.seed)
         result["key_serialization"] = key_serialization_bench(C, ctx, W["kp"], key)
+        result["encode_decode"] = encode_decode_bench(ctx, args.seed)
         result["serving"] = serving_bench(pkg, C, args.seed)
     if rank == 0:
         print(json.dumps(result), flush=True)
@@ -723,6 +724,37 @@ def key_serialization_bench(C, ctx, kp, key):
     return {"record_bytes": len(blob), "save_s": round(t_save, 3), "load_s": round(t_load, 3),
             "generate_host_sampled_s": round(t_gen, 3), "generate_device_sampled_s": round(t_dgen, 3),
             "reloaded_level": back.level}
+
+
+def encode_decode_bench(ctx, seed, batch=32):
+    """FP64 encode and decode at the bench shape (N=2^16, 24 limbs): the host encoder (one plaintext at a time,
+    as the reference) against the GPU encoder on a batch; the GPU results are checked equal to the host's."""
+    import torch
+    rng = np.random.default_rng(seed + 11)
+    h, level, sb = ctx.num_slots(), ctx.levels() - 1, ctx.params.scale_bits
+    slots = [rng.uniform(-1, 1, h) + 1j * rng.uniform(-1, 1, h) for _ in range(batch)]
+    t0 = time.perf_counter()
+    host = [ctx.encode_host(slots[i], level, sb) for i in range(2)]
+    t_henc = (time.perf_counter() - t0) / 2
+    t0 = time.perf_counter()
+    host_dec = [ctx.decode_host(host[i], sb) for i in range(2)]
+    t_hdec = (time.perf_counter() - t0) / 2
+    dev = ctx.encode_device_batch(slots, level, sb)  # warm (tables, workspace)
+    ctx.decode_device_batch(dev, sb)
+    torch.cuda.synchronize()
+    t0 = time.perf_counter()
+    dev = ctx.encode_device_batch(slots, level, sb)
+    torch.cuda.synchronize()
+    t_denc = (time.perf_counter() - t0) / batch
+    t0 = time.perf_counter()
+    dec = ctx.decode_device_batch(dev, sb)
+    t_ddec = (time.perf_counter() - t0) / batch
+    same = all(np.array_equal(dev[i].numpy(), host[i]) for i in range(2)) and \
+        all(np.array_equal(dec[i].view(np.uint64), host_dec[i].view(np.uint64)) for i in range(2))
+    return {"workload": f"encode/decode N=2^16, 24 limbs, batch {batch} on the GPU",
+            "host_encode_ms": round(t_henc * 1e3, 3), "gpu_encode_ms_per_plaintext": round(t_denc * 1e3, 4),
+            "host_decode_ms": round(t_hdec * 1e3, 3), "gpu_decode_ms_per_plaintext": round(t_ddec * 1e3, 4),
+            "bit_exact_vs_host": bool(same)}
 
 
 def serving_bench(pkg, C, seed, jobs_per_phase=240):

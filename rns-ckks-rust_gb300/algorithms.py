@@ -251,17 +251,24 @@ def pack_diagonal_transform_plaintexts(ctx: RnsCkksContext, matrix, level: int,
     d = _validate_square_matrix(matrix, ctx.num_slots())
     m = np.asarray(matrix, dtype=np.complex128)
     b = diagonal_transform_bsgs_baby_step(d)
-    diagonals = [ctx.encode_at_level_and_scale(_packed_diagonal_slots(m, k, ctx.num_slots()), level, scale_bits)
-                 for k in range(d)]
     giants = (d + b - 1) // b
-    gsd: List[List[Optional[RnsPolynomial]]] = []
+    # every diagonal and every pre-rotated BSGS diagonal in one batched GPU encode (each plaintext equals the
+    # single host encode of its slots)
+    slots = [_packed_diagonal_slots(m, k, ctx.num_slots()) for k in range(d)]
+    where = []
     for g in range(giants):
-        row = []
         for j in range(b):
             k = g * b + j
-            row.append(None if k >= d else ctx.encode_at_level_and_scale(
-                _packed_bsgs_diagonal_slots(m, k, g * b, ctx.num_slots()), level, scale_bits))
-        gsd.append(row)
+            if k < d:
+                where.append((g, j))
+                slots.append(_packed_bsgs_diagonal_slots(m, k, g * b, ctx.num_slots()))
+    encoded = []
+    for c0 in range(0, len(slots), 256):
+        encoded += ctx.encode_device_batch(slots[c0:c0 + 256], level, scale_bits)
+    diagonals = encoded[:d]
+    gsd: List[List[Optional[RnsPolynomial]]] = [[None] * b for _ in range(giants)]
+    for (g, j), p in zip(where, encoded[d:]):
+        gsd[g][j] = p
     gsd_ntt = [[None if p is None else ctx.ntt_forward_copy(p.data) for p in row] for row in gsd]
     return DiagonalTransformPlaintexts(diagonals, d, b, gsd, level, scale_bits, gsd_ntt)
 

@@ -391,7 +391,8 @@ class RnsCkksContext:
         return out
 
     def encode_at_level_and_scale(self, slots, level: int, scale_bits: int) -> RnsPolynomial:
-        return RnsPolynomial(to_device(self.encode_host(slots, level, scale_bits)))
+        """context/encoding.rs: encoded on the GPU (the same residues as the host encoder, `encode_host`)."""
+        return self.encode_device_batch([slots], level, scale_bits)[0]
 
     def encode_device_batch(self, slots_list: Sequence, level: int, scale_bits: int) -> List[RnsPolynomial]:
         """Encode many slot vectors on the GPU (rc_encode_device): the same residues as `encode_host`."""
@@ -402,7 +403,8 @@ class RnsCkksContext:
             raise RcError(1, "slot count must be N/2")
         src = torch.from_numpy(np.ascontiguousarray(np.stack([s.real, s.imag], axis=2))).to("cuda")
         out = torch.empty((len(slots_list), level + 1, self.params.poly_degree), dtype=torch.int64, device="cuda")
-        call("rc_encode_device", self.handle, _ptr(src), len(slots_list), level, scale_bits, _ptr(out), _stream())
+        call("rc_encode_device", self.handle, ctypes.c_void_p(src.data_ptr()), len(slots_list), level, scale_bits,
+             _ptr(out), _stream())
         return [RnsPolynomial(out[i]) for i in range(out.shape[0])]
 
     def decode_device_batch(self, polys: Sequence[RnsPolynomial], scale_bits: int) -> np.ndarray:
@@ -410,8 +412,8 @@ class RnsCkksContext:
         `decode_host`; returns [count][N/2] complex."""
         data = torch.stack([p.data for p in polys]).contiguous()
         out = torch.empty((data.shape[0], self.num_slots(), 2), dtype=torch.float64, device="cuda")
-        call("rc_decode_device", self.handle, _ptr(data), data.shape[0], data.shape[1] - 1, scale_bits, _ptr(out),
-             _stream())
+        call("rc_decode_device", self.handle, _ptr(data), data.shape[0], data.shape[1] - 1, scale_bits,
+             ctypes.c_void_p(out.data_ptr()), _stream())
         h = out.cpu().numpy()
         return h[..., 0] + 1j * h[..., 1]
 
@@ -428,7 +430,8 @@ class RnsCkksContext:
         return self.decode(poly).real
 
     def decode_at_scale(self, poly: RnsPolynomial, scale_bits: int) -> np.ndarray:
-        return self.decode_host(poly.numpy(), scale_bits)
+        """context/encoding.rs: decoded on the GPU (the same doubles as the host decoder, `decode_host`)."""
+        return self.decode_device_batch([poly], scale_bits)[0]
 
     def decode_real_at_scale(self, poly: RnsPolynomial, scale_bits: int) -> np.ndarray:
         return self.decode_at_scale(poly, scale_bits).real
