@@ -352,12 +352,12 @@ def run_gpu(args):
     tune_host = T.tune_host_pipeline(ctx, e2e_step, limbs - 1, B, reps=3)
     e2e_step()
     torch.cuda.synchronize()
-    # three timed rounds of e_steps steps each; the host link of a shared machine slows down now and then for
-    # tens of milliseconds (seen as single 2x-slow trials in the tuner), so the median round is reported and
+    # seven timed rounds of e_steps steps each; the host link of a shared machine slows down now and then for
+    # tens of milliseconds (seen as single 2-4x slow trials in the tuner), so the median round is reported and
     # every round is listed
     e_steps = max(1, min(args.steps, 5))
     e_rounds = []
-    for _ in range(3):
+    for _ in range(7):
         barrier(world)
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
@@ -394,7 +394,7 @@ def run_gpu(args):
                                          for k, v in sorted(per_op_prof.items(), key=lambda kv: -kv[1]["ms"])}},
         "batched_vs_per_op": round(value / world / per_op_value, 3),
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "rounds_ms_per_step": [round(r / e_steps, 3) for r in e_rounds], "estimator": "median of 3 rounds"},
+                "rounds_ms_per_step": [round(r / e_steps, 3) for r in e_rounds], "estimator": "median of 7 rounds"},
         "gpu_launches": int(sum(v["launches"] for v in prof.values())),
         "clocks": clk.summary(),
     }
