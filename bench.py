@@ -406,16 +406,18 @@ def run_gpu(args):
         per_launch_ms = st["ms"] / st["launches"]
         ab = algorithmic_bytes(name, B * args.steps, n, limbs, aux, digits, st["launches"])
         achieved = (ab / (per_launch_ms / 1e3) / 1e9) if ab else None
-        traffic = None  # DRAM bytes per launch from the committed ncu summary, when it covers this shape
+        traffic = imad = None  # per launch, from the committed ncu summary when it covers this shape
         tpath = ROOT / "profiles" / "dram_traffic_n16_l24.json"
         if tpath.exists() and n == 65536 and limbs == 24:
             t = json.loads(tpath.read_text()).get(name)
             if t and t["jobs_per_launch"] * st["launches"] == B * args.steps:
-                traffic = t["bytes_per_launch"]
+                traffic, imad = t["bytes_per_launch"], t.get("imad_pipe_pct")
         result["roofline"] = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1) if achieved else None,
                               "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
                               "peak_kind": peak_kind, "traffic": traffic,
-                              "share": round(st["ms"] / sum(v["ms"] for v in prof.values()), 4)}
+                              "share": round(st["ms"] / sum(v["ms"] for v in prof.values()), 4),
+                              # what actually limits it: the integer multiply (FMA-heavy) pipe, % busy under ncu
+                              "imad_pipe_pct": imad}
     share = min(B, JOBS_PER_LAUNCH)
     hm = hmult_algorithmic_bytes(n, limbs, aux, digits, share)
     hm1 = hmult_algorithmic_bytes(n, limbs, aux, digits, 1)
