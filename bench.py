@@ -457,6 +457,7 @@ def run_gpu(args):
         result["bootstrap"] = bootstrap_bench(pkg, C, args.seed)
         result["key_serialization"] = key_serialization_bench(C, ctx, W["kp"], key)
         result["encode_decode"] = encode_decode_bench(ctx, args.seed)
+        result["decoded_error_per_op"] = decoded_error_per_op(C, ctx, W, args.seed)
         result["serving"] = serving_bench(pkg, C, args.seed)
     if rank == 0:
         print(json.dumps(result), flush=True)
@@ -727,6 +728,28 @@ def key_serialization_bench(C, ctx, kp, key):
     return {"record_bytes": len(blob), "save_s": round(t_save, 3), "load_s": round(t_load, 3),
             "generate_host_sampled_s": round(t_gen, 3), "generate_device_sampled_s": round(t_dgen, 3),
             "reloaded_level": back.level}
+
+
+def decoded_error_per_op(C, ctx, W, seed):
+    """Decoded slot error of each operation against the FP64 computation on the slots, at the bench shape
+    (N=2^16, 24 limbs, scale 2^50): max |decoded - expected| over all 2^15 slots."""
+    kp, a, b = W["kp"], W["slots_a"][0], W["slots_b"][0]
+    ca, cb = W["lhs"][0], W["rhs"][0]
+    ds = C.DeviceSampler(ctx, seed + 21)
+    sk, pk = kp.secret_key, kp.public_key
+
+    def err(ct, want):
+        got = ctx.decode_at_scale(ctx.decrypt(ct, sk), ct.scale_bits)
+        return float(np.max(np.abs(got - want)))
+    out = {"encrypt_decrypt": err(ca, a), "add": err(ctx.add(ca, cb), a + b)}
+    plain = np.cos(np.arange(ctx.num_slots()) * 0.001)
+    out["mult_plain_slots_real"] = err(ctx.mult_plain_slots_real(ca, plain), a * plain)  # includes the rescale
+    out["mult_relinearized"] = err(ctx.mult_relinearized(ca, cb, W["key"]), a * b)
+    rot = ctx.generate_rotation_key(sk, pk, 5, ds)
+    out["rotate_5"] = err(ctx.rotate(ca, rot), np.roll(a, -5))
+    conj = ctx.generate_conjugation_key(sk, pk, ds)
+    out["conjugate"] = err(ctx.conjugate(ca, conj), np.conj(a))
+    return {k: float(f"{v:.3e}") for k, v in out.items()}
 
 
 def encode_decode_bench(ctx, seed, batch=32):
