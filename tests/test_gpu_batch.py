@@ -137,3 +137,40 @@ def test_add_and_multiply_plain_batches_equal_single_calls(env):
         assert np.array_equal(got.numpy(), ref.numpy()) and got.scale_bits == 33
     with pytest.raises(C.RcError, match="same scale to add"):
         ctx.add_batch([a[0]], [C.RnsCiphertext(b[0].data, 34)])
+
+
+def test_one_graph_spans_ring_degrees(env, pkg):
+    """Jobs of uneven ring degree and level in one replayable launch: the batched calls of two contexts
+    (N = 2^12 and N = 2^13) captured into one CUDA graph on one stream; the replay equals the direct calls."""
+    C, ctx, params, keys, host_keys, O = env
+    params2 = pkg.params.hybrid_params(13, 6, 2, 50)
+    ctx2 = C.RnsCkksContext(params2)
+    q2, p2 = params2.q_moduli(), params2.p_moduli()
+    rng = np.random.default_rng(8)
+    keys2 = {}
+    for lv in (3, 5):
+        D = math.ceil(math.prod(q2[: lv + 1]).bit_length() / 30)
+        k = np.stack([np.stack([np.stack([rng.integers(0, m, params2.poly_degree, dtype=np.uint64)
+                                          for m in q2[: lv + 1] + p2]) for _ in range(2)]) for _ in range(D)])
+        keys2[lv] = ctx2.upload_keyswitch_key(k, lv, len(p2))
+    lv1, lv2 = [7, 2, 5], [5, 3, 5]
+    cts1 = [_quad(C, rng, params, lv)[0] for lv in lv1]
+    cts2 = [_quad(C, rng, params2, lv)[0] for lv in lv2]
+    side = torch.cuda.Stream()
+    with torch.cuda.stream(side):
+        ctx.reserve(7, 8)
+        ctx2.reserve(5, 8)
+        o1 = [torch.zeros((2, lv, params.poly_degree), dtype=torch.int64, device="cuda") for lv in lv1]
+        o2 = [torch.zeros((2, lv, params2.poly_degree), dtype=torch.int64, device="cuda") for lv in lv2]
+        d1 = [r.data.clone() for r in ctx.relinearize_rescale_batch(cts1, [keys[lv] for lv in lv1])]
+        d2 = [r.data.clone() for r in ctx2.relinearize_rescale_batch(cts2, [keys2[lv] for lv in lv2])]
+
+        def both():
+            ctx.relinearize_rescale_batch(cts1, [keys[lv] for lv in lv1], o1)
+            ctx2.relinearize_rescale_batch(cts2, [keys2[lv] for lv in lv2], o2)
+        graph = ctx.capture_graph(both)
+        graph.launch()
+        side.synchronize()
+        for o, d in zip(o1 + o2, d1 + d2):
+            assert torch.equal(o, d)
+    torch.cuda.synchronize()
