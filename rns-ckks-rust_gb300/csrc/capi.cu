@@ -881,6 +881,9 @@ extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
     } else if (n == "host_chunk") {
       require(value >= 1, "host_chunk must be positive");
       c->host_chunk = value;
+    } else if (n == "host_edge") {
+      require(value >= 1, "host_edge must be positive");
+      c->host_edge = value;
     } else if (n == "fuse_tensor") {
       c->fuse_tensor = value != 0;
     } else if (n == "host_phased") {
@@ -903,6 +906,7 @@ extern "C" int rc_tune_get(const rc_context* c, const char* name, int32_t* value
     if (n == "ks_jobs") *value = c->ks_jobs;
     else if (n == "mac_bc") *value = c->mac_bc;
     else if (n == "host_chunk") *value = c->host_chunk;
+    else if (n == "host_edge") *value = c->host_edge;
     else if (n == "lazy_ntt") *value = c->lazy ? 1 : 0;
     else if (n == "fuse_tensor") *value = c->fuse_tensor ? 1 : 0;
     else if (n == "host_phased") *value = c->host_phased ? 1 : 0;
@@ -1652,16 +1656,23 @@ extern "C" int rc_rotate_batch(rc_context* c, uint32_t count, const rc_ciphertex
 // inputs have landed; one key-product pass covers all jobs; then each chunk's inverse transforms and
 // finalize run and its results are copied out while the next chunk finishes.  Returns false (nothing
 // done) when the batch does not fit this form.
-// Stage boundaries of a pipelined host-buffer batch: the first stage has half the jobs of the others, so the
-// first compute starts once half as many bytes have crossed the host link (the last stage is the remainder).
-static std::vector<uint32_t> stage_bounds(uint32_t count, uint32_t chunk) {
+// Stage boundaries of a pipelined host-buffer batch.  Only the first stage's copy-in and the last stage's
+// copy-out are not overlapped with arithmetic, so those two stages get chunk / edge jobs and the others
+// chunk: [e, c, c, ..., c, rest - e, e].
+static std::vector<uint32_t> stage_bounds(uint32_t count, uint32_t chunk, uint32_t edge) {
+  const uint32_t e = std::max<uint32_t>(1, chunk / std::max<uint32_t>(1, edge));
   std::vector<uint32_t> b{0};
-  uint32_t at = std::min(count, std::max<uint32_t>(1, chunk / 2));
+  uint32_t at = std::min(count, e);
   b.push_back(at);
-  while (at < count) {
-    at = std::min(count, at + chunk);
+  while (count - at > chunk + e) {
+    at += chunk;
     b.push_back(at);
   }
+  if (count - at > e) {
+    at = count - e;
+    b.push_back(at);
+  }
+  if (at < count) b.push_back(count);
   return b;
 }
 
@@ -1711,7 +1722,7 @@ static bool mult_relin_host_phased(rc_context* c, HostPipe* hp, uint32_t count, 
   cuda_check(cudaEventRecord(start, s), "cudaEventRecord");
   for (cudaStream_t st : {hp->in, hp->comp, hp->out})
     cuda_check(cudaStreamWaitEvent(st, start, 0), "cudaStreamWaitEvent");
-  const std::vector<uint32_t> bounds = stage_bounds((uint32_t)J, (uint32_t)chunk);
+  const std::vector<uint32_t> bounds = stage_bounds((uint32_t)J, (uint32_t)chunk, (uint32_t)c->host_edge);
   const int nchunks = (int)bounds.size() - 1;
   std::vector<cudaEvent_t> in_done(nchunks), comp_done(nchunks);
   for (int k = 0; k < nchunks; ++k) {  // every chunk's inputs, back to back in job order
@@ -1798,7 +1809,7 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
     if (c->host_phased &&
         mult_relin_host_phased(c, hp, count, lhs, rhs, levels, scale_bits, keys, out, out_scale_bits, s, chunk))
       return;
-    const std::vector<uint32_t> bounds = stage_bounds(count, (uint32_t)chunk);
+    const std::vector<uint32_t> bounds = stage_bounds(count, (uint32_t)chunk, (uint32_t)c->host_edge);
     const uint32_t nchunks = (uint32_t)bounds.size() - 1;
     auto in_elems = [&](uint32_t i) { return (size_t)2 * (levels[i] + 1) * c->N; };
     auto out_elems = [&](uint32_t i) { return (size_t)2 * levels[i] * c->N; };

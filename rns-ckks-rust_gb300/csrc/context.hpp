@@ -117,6 +117,7 @@ struct rc_context {
   int ks_jobs = 32;     // jobs per key-switch launch (one key read serves them), <= MAXP / 2
   int mac_bc = 8;       // most jobs per CTA of the wide key product (1, 2, 4 or 8)
   int host_chunk = 8;   // jobs per stage of the pipelined host-buffer entry
+  int host_edge = 2;    // its first and last stages have host_chunk / host_edge jobs
   bool fuse_tensor = true;  // forward rows + tensor + inverse rows in one kernel
   bool host_phased = true;  // host-buffer batches: one key read for the batch, transfers overlapped per chunk
 
