@@ -830,12 +830,44 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
           blob[QP + t] = shoup_h(c01, m);
           blob[2 * QP + t] = (uint64_t)(A % m);
         }
+        // the Q primes' constants times P^-1 (ModDown folded into the CRT): c01p[L], c01p_s[L], ap[L],
+        // mkp[L][K], mkp_s[L][K]
+        const size_t o_fold = blob.size();
+        const int L = c->L, K = c->K;
+        if (K > 0) {
+          std::vector<uint64_t> pinv(L), c01p(L), c01ps(L), ap(L), mkp((size_t)L * K), mkps((size_t)L * K);
+          for (int i = 0; i < L; ++i) {
+            const uint64_t m = c->mod[i];
+            uint64_t pm = 1 % m;
+            for (int k = 0; k < K; ++k) pm = mulmod_h(pm, c->mod[L + k] % m, m);
+            pinv[i] = invmod_h(pm, m);
+            c01p[i] = mulmod_h(blob[i], pinv[i], m);
+            c01ps[i] = shoup_h(c01p[i], m);
+            ap[i] = mulmod_h(blob[2 * QP + i], pinv[i], m);
+            uint64_t mk = 1 % m;  // M_k = p_0 ... p_{k-1}
+            for (int k = 0; k < K; ++k) {
+              mkp[(size_t)i * K + k] = mulmod_h(mk, pinv[i], m);
+              mkps[(size_t)i * K + k] = shoup_h(mkp[(size_t)i * K + k], m);
+              mk = mulmod_h(mk, c->mod[L + k] % m, m);
+            }
+          }
+          for (auto* v : {&c01p, &c01ps, &ap, &mkp, &mkps}) blob.insert(blob.end(), v->begin(), v->end());
+        }
         c->wide_buf.reset(new DevBuf(blob.size() * 8));
         uint64_t* d = (uint64_t*)c->wide_buf->p;
         cuda_check(cudaMemcpy(d, blob.data(), blob.size() * 8, cudaMemcpyHostToDevice), "upload wide tables");
         W.c01_mod_t = d;
         W.c01_mod_t_s = d + QP;
         W.A_mod_t = d + 2 * QP;
+        if (K > 0) {
+          W.c01p = d + o_fold;
+          W.c01p_s = W.c01p + L;
+          W.ap = W.c01p_s + L;
+          W.mkp = W.ap + L;
+          W.mkp_s = W.mkp + (size_t)L * K;
+        } else {
+          W.c01p = W.c01p_s = W.ap = W.mkp = W.mkp_s = nullptr;
+        }
       }
     }
     cuda_check(cudaDeviceSynchronize(), "context setup");

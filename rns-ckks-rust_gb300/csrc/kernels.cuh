@@ -121,12 +121,12 @@ struct ModDownTab {
   const u64* mk_s;
 };
 
-// digits[job][d][x] (int32) of the centred CRT value of src (optionally read
-// through the automorphism with inverse element g_inv; 0/1 = none)
 // lift_poly_to_context (keyswitching.rs:242-276): polys polynomials over Q_limbs ([polys][limbs][N]) to
 // Q_limbs u P ([polys][limbs + K][N]); ppc = the aux primes' constants.
 void lift_to_aux(const PrimeConst* pc, const PrimeConst* ppc, const DecompTab& dt, const u64* src, u64* dst,
                  int polys, int limbs, int K, int log_n, cudaStream_t s);
+// digits[job][d][x] (int32) of the centred CRT value of src (optionally read
+// through the automorphism with inverse element g_inv; 0/1 = none)
 void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int jobs, int limbs, int D,
                int32_t* digits, uint64_t g_inv, int log_n, cudaStream_t s);
 
@@ -151,6 +151,14 @@ struct WideTab {
   const u64* c01_mod_t;                      // [Q u P] (w0 w1) mod t and its Shoup companion
   const u64* c01_mod_t_s;
   const u64* A_mod_t;                        // [Q u P] A mod t
+  // with an aux basis P, the same constants times P^-1 mod q_i for the Q primes, so the CRT lands directly on
+  // S * P^-1 and ModDown needs no separate multiply: [L] (w0 w1 P^-1) mod q_i (+ Shoup), (A P^-1) mod q_i,
+  // and [L][K] (M_k P^-1) mod q_i (+ Shoup)
+  const u64* c01p;
+  const u64* c01p_s;
+  const u64* ap;
+  const u64* mkp;
+  const u64* mkp_s;
 };
 
 struct KsArgs {

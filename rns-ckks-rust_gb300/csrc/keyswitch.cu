@@ -498,7 +498,8 @@ constexpr int KMAX = 8;
 
 // Per-limb constants of k_finalize, staged once per CTA in shared memory (every thread of a CTA walks the
 // same limbs): FT fields per limb, then K Montgomery weights and their Shoup companions.
-enum FT { FT_Q, FT_ONE_S, FT_C01, FT_C01_S, FT_AMOD, FT_PINV, FT_PINV_S, FT_PMOD, FT_RINV, FT_RINV_S, FT_N };
+enum FT { FT_Q, FT_ONE_S, FT_LO, FT_LO_S, FT_C01, FT_C01_S, FT_AMOD, FT_PINV, FT_PINV_S, FT_PMOD, FT_RINV,
+          FT_RINV_S, FT_N };
 __host__ __device__ __forceinline__ int ft_stride(int K) { return FT_N + 2 * K; }
 
 __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab out) {
@@ -507,25 +508,33 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
   const int lq = f.qlimbs, K = f.K;
   const LimbMap fmap{lq, f.L};
   const int st = ft_stride(K);
+  // with the wide CRT and an aux basis, a Q limb's constants carry the factor P^-1 (`fold`): the CRT then
+  // yields S * P^-1, the P-part conversion (M_k P^-1) and its sign correction (P P^-1 = 1) match it, and
+  // ModDown's own multiply by P^-1 disappears
+  const bool fold = f.wide && K > 0;
   for (int e = threadIdx.x; e < (lq + K) * st; e += blockDim.x) {
     const int i = e / st, fld = e - i * st;
     const int t = fmap.prime(i);
     const bool q_limb = i < lq;
+    const bool fq = fold && q_limb;
     u64 v = 0;
     switch (fld) {
       case FT_Q: v = f.pc[t].q; break;
       case FT_ONE_S: v = f.pc[t].one_s; break;
-      case FT_C01: v = f.wide ? f.wt.c01_mod_t[t] : 0; break;
-      case FT_C01_S: v = f.wide ? f.wt.c01_mod_t_s[t] : 0; break;
-      case FT_AMOD: v = f.wide ? f.wt.A_mod_t[t] : 0; break;
+      case FT_LO: v = fq ? f.md.pinv[i] : 1; break;
+      case FT_LO_S: v = fq ? f.md.pinv_s[i] : f.pc[t].one_s; break;
+      case FT_C01: v = !f.wide ? 0 : (fq ? f.wt.c01p[i] : f.wt.c01_mod_t[t]); break;
+      case FT_C01_S: v = !f.wide ? 0 : (fq ? f.wt.c01p_s[i] : f.wt.c01_mod_t_s[t]); break;
+      case FT_AMOD: v = !f.wide ? 0 : (fq ? f.wt.ap[i] : f.wt.A_mod_t[t]); break;
       case FT_PINV: v = (K && q_limb) ? f.md.pinv[i] : 0; break;
       case FT_PINV_S: v = (K && q_limb) ? f.md.pinv_s[i] : 0; break;
-      case FT_PMOD: v = (K && q_limb) ? f.md.pmod[i] : 0; break;
+      case FT_PMOD: v = (K && q_limb) ? (fq ? 1 : f.md.pmod[i]) : 0; break;
       case FT_RINV: v = (f.rescale && i < lq - 1) ? f.rt.inv[(size_t)(lq - 1) * f.L + i] : 0; break;
       case FT_RINV_S: v = (f.rescale && i < lq - 1) ? f.rt.inv_s[(size_t)(lq - 1) * f.L + i] : 0; break;
       default: {
         const int k = fld - FT_N;
-        v = !q_limb ? 0 : (k < K ? f.md.mk[(size_t)i * K + k] : f.md.mk_s[(size_t)i * K + (k - K)]);
+        if (q_limb && k < K) v = fq ? f.wt.mkp[(size_t)i * K + k] : f.md.mk[(size_t)i * K + k];
+        else if (q_limb) v = fq ? f.wt.mkp_s[(size_t)i * K + (k - K)] : f.md.mk_s[(size_t)i * K + (k - K)];
       }
     }
     tab[e] = v;
@@ -541,7 +550,7 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
   auto accv = [&](int j) -> u64 {  // value of limb j at x
     if (!f.wide) return a[(size_t)j * N + x];
     return wide_crt_mod_c(a2[(size_t)j * 2 * N + x], a2[((size_t)j * 2 + 1) * N + x], f.wt, T(j, FT_Q),
-                          T(j, FT_ONE_S), T(j, FT_C01), T(j, FT_C01_S), T(j, FT_AMOD));
+                          T(j, FT_LO), T(j, FT_LO_S), T(j, FT_C01), T(j, FT_C01_S), T(j, FT_AMOD));
   };
   const u64* add = addend.p[2 * job + comp];
   u64* dst = out.p[2 * job + comp];
@@ -617,7 +626,7 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
       }
       if (pneg) conv = sub_mod(conv, T(i, FT_PMOD), q);
       val = sub_mod(val, conv, q);
-      val = mul_shoup(val, T(i, FT_PINV), T(i, FT_PINV_S), q);
+      if (!fold) val = mul_shoup(val, T(i, FT_PINV), T(i, FT_PINV_S), q);
     }
     if (add) {
       u64 av = add[(size_t)i * N + addsrc];

@@ -22,9 +22,11 @@ __device__ __forceinline__ uint32_t sub32(uint32_t a, uint32_t b, uint32_t q) { 
 // v < 2q -> v mod q
 __device__ __forceinline__ uint32_t fold32(uint32_t v, uint32_t q) { return v >= q ? v - q : v; }
 
-// wide_crt_mod with the per-prime constants passed in (q, floor(2^64/q), (w0 w1) mod q + Shoup, A mod q)
-__device__ __forceinline__ u64 wide_crt_mod_c(uint2 p01, uint2 p23, const WideTab& W, u64 q, u64 one_s, u64 c01,
-                                              u64 c01_s, u64 a_mod) {
+// wide_crt_mod with the per-prime constants passed in: S * F mod q for a factor F given as
+// (F mod q + Shoup) = (lo_w, lo_ws), (w0 w1 F) mod q + Shoup = (c01, c01_s) and (A F) mod q = a_mod
+// (F = 1: lo_w = 1, lo_ws = floor(2^64 / q))
+__device__ __forceinline__ u64 wide_crt_mod_c(uint2 p01, uint2 p23, const WideTab& W, u64 q, u64 lo_w, u64 lo_ws,
+                                              u64 c01, u64 c01_s, u64 a_mod) {
   const uint32_t w1 = W.w[1], w2 = W.w[2], w3 = W.w[3];
   const uint32_t v0 = p01.x;
   const uint32_t v1 = mul_shoup32(sub32(p01.y, fold32(v0, w1), w1), W.g01, W.g01s, w1);
@@ -35,7 +37,7 @@ __device__ __forceinline__ u64 wide_crt_mod_c(uint2 p01, uint2 p23, const WideTa
   const uint32_t v3 = mul_shoup32(sub32(b, fold32(v2, w3), w3), W.g23, W.g23s, w3);
   const u64 lo = (u64)v0 + (u64)W.w[0] * v1;
   const u64 hi = (u64)v2 + (u64)w2 * v3;
-  u64 r = reduce_4q(mul_shoup_lazy(lo, 1, one_s, q) + mul_shoup_lazy(hi, c01, c01_s, q), q);
+  u64 r = reduce_4q(mul_shoup_lazy(lo, lo_w, lo_ws, q) + mul_shoup_lazy(hi, c01, c01_s, q), q);
   if (v3 >= W.half3) r = sub_mod(r, a_mod, q);
   return r;
 }
