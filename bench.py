@@ -399,6 +399,13 @@ def run_gpu(args):
         "gpu_launches": int(sum(v["launches"] for v in prof.values())),
         "clocks": clk.summary(),
     }
+    # the integer multiply rates that bound the kernels (measured on this GPU, outside the timed region)
+    rates = (ctypes.c_double * 5)()
+    C.call("rc_measure_multiply_rates", rates, s_ptr)
+    result["integer_multiply_rates"] = {
+        "unit": "warp instructions per SM per cycle",
+        "imad_wide_32x32_64": round(rates[0], 3), "imad_32": round(rates[1], 3), "imad_hi_32": round(rates[2], 3),
+        "mul_lo_64": round(rates[3], 3), "umul64hi": round(rates[4], 3)}
     # roofline of the dominant kernel
     peak, peak_kind = peaks()
     dom = max(prof.items(), key=lambda kv: kv[1]["ms"]) if prof else None

@@ -277,6 +277,12 @@ int rc_mult_relinearized_batch_host(rc_context* ctx, uint32_t count, const uint6
                                     const rc_ksk* const* keys, uint64_t* const* out, int32_t* out_scale_bits,
                                     void* stream);
 
+/* ---- measurement (no reference counterpart) ----
+ * Throughput of the integer multiply forms the kernels use, in warp-wide instructions per SM per SM cycle:
+ * rates[0] IMAD.WIDE (32x32->64 with a 64-bit addend), [1] 32-bit IMAD, [2] IMAD.HI, [3] 64-bit low product,
+ * [4] __umul64hi.  Runs five short kernels on `stream` (about 30 ms). */
+int rc_measure_multiply_rates(double* rates, void* stream);
+
 /* ---- host FP64 helpers (src/rns/encoding.rs, src/math/canonical_embedding.rs) ---- */
 /* encode_integer_coeffs + poly_from_bigint_coeffs: encoding.rs:9-31,
  * polynomial.rs:78-85.  slots: N/2 complex values as interleaved (re, im). */

@@ -122,6 +122,7 @@ SIGNATURES = [
     ("rc_decode_device", ctypes.c_int, [_vp, _vp, _u32, _i32, _u32, _vp, _vp]),
     ("rc_slots_to_real_coeffs", ctypes.c_int, [_u64, _vp, _vp]),
     ("rc_complex_coeffs_to_slots", ctypes.c_int, [_u64, _vp, _vp]),
+    ("rc_measure_multiply_rates", ctypes.c_int, [_vp, _vp]),
     ("rc_profile_enable", ctypes.c_int, [ctypes.c_int]),
     ("rc_profile_report", ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
 ]
