@@ -613,6 +613,43 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
     pneg = res > 0;
   }
 
+  // one limb's inputs (wide products and addend) and the value computed from them; the rescale loop below
+  // requests limb i+1's inputs before computing limb i, so each thread has two limbs' loads in flight
+  struct LimbIn {
+    uint2 p01, p23;
+    u64 av;
+  };
+  auto load = [&](int j) -> LimbIn {
+    LimbIn r;
+    r.p01 = a2[(size_t)j * 2 * N + x];
+    r.p23 = a2[((size_t)j * 2 + 1) * N + x];
+    r.av = add ? add[(size_t)j * N + addsrc] : 0;
+    return r;
+  };
+  auto finish_value = [&](int i, u64 val, u64 av) -> u64 {
+    const u64 q = T(i, FT_Q);
+    if (K > 0) {
+      u64 conv = 0;
+#pragma unroll
+      for (int k = 0; k < KMAX; ++k) {
+        if (k < K) conv = add_mod(conv, mul_shoup(v[k], T(i, FT_N + k), T(i, FT_N + K + k), q), q);
+      }
+      if (pneg) conv = sub_mod(conv, T(i, FT_PMOD), q);
+      val = sub_mod(val, conv, q);
+      if (!fold) val = mul_shoup(val, T(i, FT_PINV), T(i, FT_PINV_S), q);
+    }
+    if (add) {
+      if (addneg && av) av = q - av;
+      val = add_mod(val, av, q);
+    }
+    return val;
+  };
+  auto wide_value = [&](int i, const LimbIn& in) -> u64 {
+    const u64 val = wide_crt_mod_c(in.p01, in.p23, f.wt, T(i, FT_Q), T(i, FT_LO), T(i, FT_LO_S), T(i, FT_C01),
+                                   T(i, FT_C01_S), T(i, FT_AMOD));
+    return finish_value(i, val, in.av);
+  };
+
   auto limb_value = [&](int i) -> u64 {
     const u64 q = T(i, FT_Q);
     u64 val = accv(i);
@@ -645,13 +682,25 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
   const u64 ql = T(last, FT_Q), half = ql >> 1;
   const bool pos = vl <= half;
   const u64 dist = pos ? vl : ql - vl;
-  for (int i = 0; i < last; ++i) {
+  auto rescaled = [&](int i, u64 value) {
     const u64 q = T(i, FT_Q);
     const u64 d = dist < q ? dist : mul_shoup(dist, 1, T(i, FT_ONE_S), q);
     const u64 cd = pos ? d : (d == 0 ? 0 : q - d);
-    const u64 num = sub_mod(limb_value(i), cd, q);
+    const u64 num = sub_mod(value, cd, q);
     dst[(size_t)i * N + x] = mul_shoup(num, T(i, FT_RINV), T(i, FT_RINV_S), q);
+  };
+  if (f.wide && last > 0) {
+    LimbIn cur = load(0);
+#pragma unroll 1
+    for (int i = 0; i < last; ++i) {
+      LimbIn nxt;
+      if (i + 1 < last) nxt = load(i + 1);
+      rescaled(i, wide_value(i, cur));
+      cur = nxt;
+    }
+    return;
   }
+  for (int i = 0; i < last; ++i) rescaled(i, limb_value(i));
 }
 
 // key relayout [digits][2][limbs][N] (NTT domain) -> [limbs][digits][2][N] in Montgomery form
