@@ -690,13 +690,15 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
     dst[(size_t)i * N + x] = mul_shoup(num, T(i, FT_RINV), T(i, FT_RINV_S), q);
   };
   if (f.wide && last > 0) {
-    LimbIn cur = load(0);
+    LimbIn cur = load(0), nxt;
+    if (last > 1) nxt = load(1);
 #pragma unroll 1
     for (int i = 0; i < last; ++i) {
-      LimbIn nxt;
-      if (i + 1 < last) nxt = load(i + 1);
+      LimbIn far;
+      if (i + 2 < last) far = load(i + 2);
       rescaled(i, wide_value(i, cur));
       cur = nxt;
+      nxt = far;
     }
     return;
   }
