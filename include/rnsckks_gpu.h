@@ -257,6 +257,25 @@ int rc_rotate_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* ct, co
 int rc_relinearize_rescale_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* quadratic,
                                  const rc_ksk* const* keys, rc_ciphertext* out, void* stream);
 
+/* ---- the crate's src/algorithms routines as whole schedules over a batch (one call, no per-step host
+ * glue; the crate's schedules, scale/level rules and messages, so residues equal the crate's) ----
+ * rc_total_sum_batch: total_sum.rs:45-60 for `count` ciphertexts; step_keys[t] is the rotation key of fold
+ *   step 2^t (t < key_count), out[i] receives the result (level and scale of the input).
+ * rc_halevi_shoup_batch: halevi_shoup.rs:46-71; plain = [count][plain_len] real slot values (zero-padded to
+ *   N/2 and encoded at each ciphertext's level and scale on the GPU), mult_plain_slots_real then the fold
+ *   over next_power_of_two(plain_len); out[i] is one level down.
+ * rc_paterson_stockmeyer_batch: paterson_stockmeyer.rs:28-108 (helpers 146-349) of one polynomial
+ *   (coefficients[terms], lowest degree first) on ciphertexts sharing level and scale; relin_keys[l] is the
+ *   relinearization key at level l (null where absent, key_levels entries). */
+int rc_total_sum_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* cts, uint32_t active_slots,
+                       const rc_ksk* const* step_keys, uint32_t key_count, rc_ciphertext* out, void* stream);
+int rc_halevi_shoup_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* cts, const double* plain,
+                          uint32_t plain_len, const rc_ksk* const* step_keys, uint32_t key_count, rc_ciphertext* out,
+                          void* stream);
+int rc_paterson_stockmeyer_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* cts,
+                                 const double* coefficients, uint32_t terms, const rc_ksk* const* relin_keys,
+                                 uint32_t key_levels, rc_ciphertext* out, void* stream);
+
 /* ---- CUDA graphs of library calls (no reference counterpart: the crate is CPU-only).  Capture every
  * call made on `stream` between begin and end (thread-local capture mode) into an executable graph;
  * rc_reserve the scratch first (capture refuses to grow it).  Pointers and sizes are baked in: replay

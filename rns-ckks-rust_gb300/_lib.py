@@ -107,6 +107,10 @@ SIGNATURES = [
     ("rc_relinearize_batch", ctypes.c_int, [_vp, _u32, _CT, ctypes.POINTER(_vp), _CT, _vp]),
     ("rc_rotate_batch", ctypes.c_int, [_vp, _u32, _CT, ctypes.POINTER(_vp), _CT, _vp]),
     ("rc_relinearize_rescale_batch", ctypes.c_int, [_vp, _u32, _CT, ctypes.POINTER(_vp), _CT, _vp]),
+    ("rc_total_sum_batch", ctypes.c_int, [_vp, _u32, _CT, _u32, ctypes.POINTER(_vp), _u32, _CT, _vp]),
+    ("rc_halevi_shoup_batch", ctypes.c_int, [_vp, _u32, _CT, _vp, _u32, ctypes.POINTER(_vp), _u32, _CT, _vp]),
+    ("rc_paterson_stockmeyer_batch", ctypes.c_int, [_vp, _u32, _CT, _vp, _u32, ctypes.POINTER(_vp), _u32, _CT,
+                                                    _vp]),
     ("rc_graph_begin", ctypes.c_int, [_vp, _vp]),
     ("rc_graph_end", ctypes.c_int, [_vp, _vp, ctypes.POINTER(_vp)]),
     ("rc_graph_launch", ctypes.c_int, [_vp, _vp]),

@@ -573,3 +573,81 @@ def paterson_stockmeyer_eval_batch(ctx: RnsCkksContext, ciphertexts: Sequence[Rn
         lifted = lift_all(multiplied, result[0].scale_bits)
         result = ctx.add_batch(lifted, blocks_out[bi])
     return result
+
+
+# --------------------------------------------------------------------------------------------------------
+# the same schedules run natively (rc_total_sum_batch, rc_halevi_shoup_batch, rc_paterson_stockmeyer_batch):
+# one library call per batch, no per-step host glue; residues equal the routines above
+# --------------------------------------------------------------------------------------------------------
+
+def _raw_in(cts):
+    from ._lib import RcCiphertext
+    n = len(cts)
+    return (RcCiphertext * n)(*[c.raw() for c in cts])
+
+
+def _raw_out(ctx, levels):
+    from ._lib import RcCiphertext
+    outs = [torch.empty((2, lv + 1, ctx.params.poly_degree), dtype=torch.int64, device="cuda") for lv in levels]
+    return outs, (RcCiphertext * len(outs))(*[RcCiphertext(o.data_ptr(), 0, 0) for o in outs])
+
+
+def _step_keys(rotation_keys: Dict[int, RnsRotationKey], active_slots: int):
+    import ctypes
+    steps = _fold_steps(active_slots)
+    return (ctypes.c_void_p * max(1, len(steps)))(
+        *[(rotation_keys[s].keyswitch_key.handle if s in rotation_keys else None) for s in steps]), len(steps)
+
+
+def total_sum_native(ctx: RnsCkksContext, ciphertexts: Sequence[RnsCiphertext], active_slots: int,
+                     rotation_keys: Dict[int, RnsRotationKey]) -> List[RnsCiphertext]:
+    """`total_sum` (total_sum.rs:45-60) of a batch in one call (rc_total_sum_batch)."""
+    from ._lib import call
+    from .context import _stream
+    cts = list(ciphertexts)
+    if not cts:
+        return []
+    keys, nk = _step_keys(rotation_keys, active_slots)
+    outs, O = _raw_out(ctx, [c.level for c in cts])
+    call("rc_total_sum_batch", ctx.handle, len(cts), _raw_in(cts), active_slots, keys, nk, O, _stream())
+    return [RnsCiphertext(o, O[i].scale_bits, O[i].level) for i, o in enumerate(outs)]
+
+
+def halevi_shoup_dot_product_native(ctx: RnsCkksContext, ciphertexts: Sequence[RnsCiphertext], plaintext_slots,
+                                    rotation_keys: Dict[int, RnsRotationKey]) -> List[RnsCiphertext]:
+    """`halevi_shoup_dot_product` (halevi_shoup.rs:46-71) of a batch sharing one plaintext length, in one call
+    (rc_halevi_shoup_batch); plaintext_slots is one real vector per ciphertext."""
+    from ._lib import call
+    from .context import _stream
+    cts = list(ciphertexts)
+    if not cts:
+        return []
+    plain = np.ascontiguousarray(np.asarray(plaintext_slots, dtype=np.float64).reshape(len(cts), -1))
+    keys, nk = _step_keys(rotation_keys, plain.shape[1])
+    outs, O = _raw_out(ctx, [max(c.level - 1, 0) for c in cts])
+    call("rc_halevi_shoup_batch", ctx.handle, len(cts), _raw_in(cts), plain.ctypes.data, plain.shape[1], keys, nk,
+         O, _stream())
+    return [RnsCiphertext(o, O[i].scale_bits, O[i].level) for i, o in enumerate(outs)]
+
+
+def paterson_stockmeyer_eval_native(ctx: RnsCkksContext, ciphertexts: Sequence[RnsCiphertext],
+                                    coefficients: Sequence[float],
+                                    relin_keys: Dict[int, RnsKeySwitchingKey]) -> List[RnsCiphertext]:
+    """`paterson_stockmeyer_eval` (paterson_stockmeyer.rs:28-108) of one polynomial on a batch sharing level
+    and scale, in one call (rc_paterson_stockmeyer_batch)."""
+    import ctypes
+    from ._lib import call
+    from .context import _stream
+    cts = list(ciphertexts)
+    if not cts:
+        return []
+    coeffs = np.ascontiguousarray(np.asarray(coefficients, dtype=np.float64))
+    levels = ctx.levels()
+    keys = (ctypes.c_void_p * levels)(*[(relin_keys[l].handle if l in relin_keys else None) for l in range(levels)])
+    outs, O = _raw_out(ctx, [c.level for c in cts])  # results are at or below the input level
+    call("rc_paterson_stockmeyer_batch", ctx.handle, len(cts), _raw_in(cts), coeffs.ctypes.data, coeffs.size, keys,
+         levels, O, _stream())
+    n = ctx.params.poly_degree
+    # the library wrote [c0][c1] with the result's limb count at the front of each buffer
+    return [RnsCiphertext(o.view(-1)[: 2 * (O[i].level + 1) * n].view(2, O[i].level + 1, n).clone(), O[i].scale_bits,
+                          O[i].level) for i, o in enumerate(outs)]

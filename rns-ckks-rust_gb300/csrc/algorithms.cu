@@ -1,0 +1,350 @@
+// The crate's src/algorithms routines (total sum, Halevi-Shoup dot product, Paterson-Stockmeyer) as C ABI
+// entry points over the library's own batched ops, so a caller runs a whole schedule for a batch of
+// ciphertexts in one call with no per-step host glue.  Each routine keeps the crate's schedule, scale and
+// level bookkeeping and panic messages (returned as RC_ERR_INVALID_ARGUMENT with the message), so the
+// residues equal the crate's for the same keys and inputs:
+//   total_sum.rs:45-60, halevi_shoup.rs:46-71 (with context/ops.rs:39-48), paterson_stockmeyer.rs:28-349.
+// Intermediates live in stream-ordered device allocations (cudaMallocAsync) released at the end of the call.
+#include <cmath>
+#include <map>
+#include <mutex>
+#include <string>
+#include <tuple>
+#include <vector>
+
+#include "context.hpp"
+
+using namespace rc;
+
+namespace {
+
+// N/2 complex slots all equal to (value, 0), interleaved
+__global__ void k_fill_const(double* slots, double value, size_t half) {
+  for (size_t k = blockIdx.x * (size_t)blockDim.x + threadIdx.x; k < half; k += (size_t)gridDim.x * blockDim.x) {
+    slots[2 * k] = value;
+    slots[2 * k + 1] = 0.0;
+  }
+}
+
+void ok(int status) {
+  if (status != RC_OK) fail(status, rc_last_error(nullptr));
+}
+
+// stream-ordered scratch of one call
+struct Pool {
+  cudaStream_t s;
+  std::vector<void*> ptrs;
+  explicit Pool(cudaStream_t st) : s(st) {}
+  ~Pool() {
+    for (void* p : ptrs) cudaFreeAsync(p, s);
+  }
+  uint64_t* take(size_t words) {
+    void* p = nullptr;
+    cuda_check(cudaMallocAsync(&p, words * 8, s), "cudaMallocAsync");
+    ptrs.push_back(p);
+    return (uint64_t*)p;
+  }
+};
+
+struct Algo {
+  rc_context* c;
+  cudaStream_t s;
+  Pool pool;
+  size_t N;
+  std::map<std::tuple<double, int, int>, uint64_t*> consts;  // encoded constants by (value, level, scale)
+
+  Algo(rc_context* ctx, void* stream) : c(ctx), s((cudaStream_t)stream), pool((cudaStream_t)stream), N(ctx->N) {
+    // keep freed blocks in the device's stream-ordered pool between calls (a setting of this process's pool)
+    static std::once_flag once;
+    std::call_once(once, [] {
+      int dev = 0;
+      cudaMemPool_t mp;
+      if (cudaGetDevice(&dev) == cudaSuccess && cudaDeviceGetDefaultMemPool(&mp, dev) == cudaSuccess) {
+        uint64_t keep = ~0ull;
+        cudaMemPoolSetAttribute(mp, cudaMemPoolAttrReleaseThreshold, &keep);
+      }
+    });
+  }
+
+  rc_ciphertext fresh(int level, int scale) { return rc_ciphertext{pool.take(2 * (size_t)(level + 1) * N), level, scale}; }
+
+  // the first `level + 1` limbs of each component (truncate_levels): a copy, components are [2][limbs][N]
+  rc_ciphertext truncate(const rc_ciphertext& ct, int level) {
+    if (level == ct.level) return ct;
+    rc_ciphertext o = fresh(level, ct.scale_bits);
+    const size_t bytes = (size_t)(level + 1) * N * 8;
+    for (int k = 0; k < 2; ++k)
+      cuda_check(cudaMemcpyAsync(o.data + k * (level + 1) * N, ct.data + k * (size_t)(ct.level + 1) * N, bytes,
+                                 cudaMemcpyDeviceToDevice, s),
+                 "truncate");
+    return o;
+  }
+
+  // encode of N/2 slots all equal to `value` at (level, scale), on the GPU, memoised for the call
+  uint64_t* constant(double value, int level, int scale) {
+    auto key = std::make_tuple(value, level, scale);
+    auto it = consts.find(key);
+    if (it != consts.end()) return it->second;
+    uint64_t* out = pool.take((size_t)(level + 1) * N);
+    double* dslots = (double*)pool.take(N);
+    const size_t half = N / 2;
+    k_fill_const<<<(unsigned)std::min<size_t>((half + 255) / 256, 1024), 256, 0, s>>>(dslots, value, half);
+    cuda_check(cudaGetLastError(), "constant slots");
+    ok(rc_encode_device(c, dslots, 1, level, (uint32_t)scale, out, s));
+    consts[key] = out;
+    return out;
+  }
+
+  std::vector<rc_ciphertext> add(const std::vector<rc_ciphertext>& a, const std::vector<rc_ciphertext>& b,
+                                 rc_ciphertext* into = nullptr) {
+    std::vector<rc_ciphertext> o(a.size());
+    for (size_t i = 0; i < a.size(); ++i) o[i] = into ? into[i] : fresh(a[i].level, a[i].scale_bits);
+    ok(rc_add_batch(c, (uint32_t)a.size(), a.data(), b.data(), o.data(), s));
+    return o;
+  }
+
+  std::vector<rc_ciphertext> rotate(const std::vector<rc_ciphertext>& a, const rc_ksk* key) {
+    std::vector<rc_ciphertext> o(a.size());
+    std::vector<const rc_ksk*> ks(a.size(), key);
+    for (size_t i = 0; i < a.size(); ++i) o[i] = fresh(a[i].level, a[i].scale_bits);
+    ok(rc_rotate_batch(c, (uint32_t)a.size(), a.data(), ks.data(), o.data(), s));
+    return o;
+  }
+
+  // multiply_plain_rns of every ciphertext by the same plaintext, then scale_bits set to `scale`
+  std::vector<rc_ciphertext> mul_plain(const std::vector<rc_ciphertext>& a, const uint64_t* plain, int scale) {
+    std::vector<rc_ciphertext> o(a.size());
+    std::vector<const uint64_t*> ps(a.size(), plain);
+    for (size_t i = 0; i < a.size(); ++i) o[i] = fresh(a[i].level, a[i].scale_bits);
+    ok(rc_multiply_plain_rns_batch(c, (uint32_t)a.size(), a.data(), ps.data(), o.data(), s));
+    for (auto& x : o) x.scale_bits = scale;
+    return o;
+  }
+};
+
+// fold steps 1, 2, 4, ... below next_power_of_two(active_slots) (halevi_shoup.rs:15-26, total_sum.rs:14-25)
+std::vector<uint32_t> fold_steps(uint32_t active_slots) {
+  require(active_slots > 0, "active_slots must be positive");
+  uint32_t width = 1;
+  while (width < active_slots) width <<= 1;
+  std::vector<uint32_t> steps;
+  for (uint32_t st = 1; st < width; st <<= 1) steps.push_back(st);
+  return steps;
+}
+
+// rotate-and-add over the fold steps; the last add writes into `out`
+void fold(Algo& A, std::vector<rc_ciphertext> accs, uint32_t active_slots, const rc_ksk* const* keys,
+          uint32_t key_count, const char* missing, rc_ciphertext* out) {
+  const std::vector<uint32_t> steps = fold_steps(active_slots);
+  for (size_t t = 0; t < steps.size(); ++t) {
+    if (t >= key_count || !keys[t]) fail(RC_ERR_INVALID_ARGUMENT, missing + std::to_string(steps[t]));
+    const std::vector<rc_ciphertext> rotated = A.rotate(accs, keys[t]);
+    accs = A.add(accs, rotated, t + 1 == steps.size() ? out : nullptr);
+  }
+  if (steps.empty()) {  // nothing to fold: the input itself
+    for (size_t i = 0; i < accs.size(); ++i) {
+      cuda_check(cudaMemcpyAsync(out[i].data, accs[i].data, 2 * (size_t)(accs[i].level + 1) * A.N * 8,
+                                 cudaMemcpyDeviceToDevice, A.s),
+                 "copy");
+      out[i].level = accs[i].level;
+      out[i].scale_bits = accs[i].scale_bits;
+    }
+  }
+}
+
+// paterson_stockmeyer.rs:18-26 and 110-126
+uint32_t ps_block_size(uint32_t terms) {
+  require(terms > 0, "term_count must be positive");
+  uint32_t b = 1;
+  while (b * b < terms) ++b;
+  return b;
+}
+
+std::vector<int> ps_required_levels(int level, uint32_t terms) {
+  require(terms > 0, "term_count must be positive");
+  if (terms == 1) return {};
+  const int b = (int)ps_block_size(terms), blocks = (int)((terms + b - 1) / b);
+  const int top = level - (b - 1);
+  require(top >= 0, "polynomial degree is too large for the available CKKS level budget");
+  const int fin = top - (blocks - 1);
+  require(fin >= 0, "polynomial degree is too large for the available CKKS level budget");
+  std::vector<int> out;
+  for (int l = level; l > fin; --l) out.push_back(l);
+  return out;
+}
+
+int floor_log2_u64(uint64_t q) { return 63 - __builtin_clzll(q); }
+
+}  // namespace
+
+extern "C" int rc_total_sum_batch(rc_context* c, uint32_t count, const rc_ciphertext* cts, uint32_t active_slots,
+                                  const rc_ksk* const* step_keys, uint32_t key_count, rc_ciphertext* out,
+                                  void* stream) {
+  return guarded([&] {
+    require(c && cts && out, "arguments must not be null");
+    if (count == 0) return;
+    Algo A(c, stream);
+    fold(A, std::vector<rc_ciphertext>(cts, cts + count), active_slots, step_keys, key_count,
+         "missing total-sum rotation key for step ", out);
+  });
+}
+
+extern "C" int rc_halevi_shoup_batch(rc_context* c, uint32_t count, const rc_ciphertext* cts, const double* plain,
+                                     uint32_t plain_len, const rc_ksk* const* step_keys, uint32_t key_count,
+                                     rc_ciphertext* out, void* stream) {
+  return guarded([&] {
+    require(c && cts && plain && out, "arguments must not be null");
+    if (count == 0) return;
+    Algo A(c, stream);
+    const size_t half = A.N / 2;
+    require(plain_len <= half, "plaintext slot vector cannot exceed the CKKS slot count");
+    require(plain_len > 0, "plaintext slot vector cannot be empty");
+    // mult_plain_slots_real (context/ops.rs:39-48): encode at the ciphertext's level and scale, mult_plain
+    // (scale doubles), rescale
+    std::vector<rc_ciphertext> in(cts, cts + count), prods(count), accs(count);
+    std::vector<double> slots((size_t)count * 2 * half, 0.0);
+    for (uint32_t i = 0; i < count; ++i)
+      for (uint32_t k = 0; k < plain_len; ++k) slots[(size_t)i * 2 * half + 2 * k] = plain[(size_t)i * plain_len + k];
+    double* dslots = (double*)A.pool.take(slots.size());
+    // a copy from pageable memory returns once the source has been staged, so `slots` may go at return
+    cuda_check(cudaMemcpyAsync(dslots, slots.data(), slots.size() * 8, cudaMemcpyHostToDevice, A.s), "slots");
+    std::vector<const uint64_t*> plains(count);
+    bool uniform = true;
+    for (uint32_t i = 0; i < count; ++i)
+      uniform = uniform && in[i].level == in[0].level && in[i].scale_bits == in[0].scale_bits;
+    if (uniform) {  // one batched encode
+      const size_t pl = (size_t)(in[0].level + 1) * A.N;
+      uint64_t* p = A.pool.take(pl * count);
+      ok(rc_encode_device(c, dslots, count, in[0].level, (uint32_t)in[0].scale_bits, p, A.s));
+      for (uint32_t i = 0; i < count; ++i) plains[i] = p + i * pl;
+    } else {
+      for (uint32_t i = 0; i < count; ++i) {
+        uint64_t* p = A.pool.take((size_t)(in[i].level + 1) * A.N);
+        ok(rc_encode_device(c, dslots + (size_t)i * 2 * half, 1, in[i].level, (uint32_t)in[i].scale_bits, p, A.s));
+        plains[i] = p;
+      }
+    }
+    for (uint32_t i = 0; i < count; ++i) {
+      prods[i] = A.fresh(in[i].level, in[i].scale_bits);
+      accs[i] = A.fresh(in[i].level > 0 ? in[i].level - 1 : 0, 0);
+    }
+    ok(rc_multiply_plain_rns_batch(c, count, in.data(), plains.data(), prods.data(), A.s));
+    for (uint32_t i = 0; i < count; ++i) prods[i].scale_bits = in[i].scale_bits + in[i].scale_bits;
+    ok(rc_rescale_batch(c, count, prods.data(), accs.data(), A.s));
+    fold(A, accs, plain_len, step_keys, key_count, "missing rotation key for step ", out);
+  });
+}
+
+extern "C" int rc_paterson_stockmeyer_batch(rc_context* c, uint32_t count, const rc_ciphertext* cts,
+                                            const double* coefficients, uint32_t terms,
+                                            const rc_ksk* const* relin_keys, uint32_t key_levels,
+                                            rc_ciphertext* out, void* stream) {
+  return guarded([&] {
+    require(c && cts && out && (terms == 0 || coefficients), "arguments must not be null");
+    require(terms > 0, "polynomial must contain at least one coefficient");
+    if (count == 0) return;
+    Algo A(c, stream);
+    // floor(log2 q_level) of the context's chain (the crate's scale rule)
+    auto qbits = [&](int level) -> int { return floor_log2_u64(c->mod[level]); };
+    std::vector<rc_ciphertext> in(cts, cts + count);
+    const int level = in[0].level, in_scale = in[0].scale_bits;
+    for (const auto& ct : in)
+      require(ct.level == level && ct.scale_bits == in_scale, "a batch must share level and scale");
+
+    auto constant_ct = [&](int lv, int scale, double value) {  // paterson_stockmeyer.rs:311-336
+      rc_ciphertext z = A.fresh(lv, scale);
+      cuda_check(cudaMemsetAsync(z.data, 0, 2 * (size_t)(lv + 1) * A.N * 8, A.s), "zero");
+      if (value != 0.0) ok(rc_poly_add(c, z.data, A.constant(value, lv, scale), z.data, lv + 1, 0, A.s));
+      return z;
+    };
+    auto write_out = [&](const std::vector<rc_ciphertext>& r) {
+      for (uint32_t i = 0; i < count; ++i) {
+        cuda_check(cudaMemcpyAsync(out[i].data, r[i].data, 2 * (size_t)(r[i].level + 1) * A.N * 8,
+                                   cudaMemcpyDeviceToDevice, A.s),
+                   "copy");
+        out[i].level = r[i].level;
+        out[i].scale_bits = r[i].scale_bits;
+      }
+    };
+    if (terms == 1) {
+      std::vector<rc_ciphertext> r(count);
+      for (auto& x : r) x = constant_ct(level, in_scale, coefficients[0]);
+      write_out(r);
+      return;
+    }
+    const int b = (int)ps_block_size(terms), blocks = (int)((terms + b - 1) / b);
+    const std::vector<int> req = ps_required_levels(level, terms);
+    require(!req.empty(), "Paterson-Stockmeyer multiplication levels must be non-empty");
+    int working = 1 << 30;
+    for (int lv : req) working = std::min(working, qbits(lv));
+    const int coeff_scale = working - in_scale;
+    require(coeff_scale >= 0, "Paterson-Stockmeyer working scale must dominate the input ciphertext scale");
+
+    auto lift_all = [&](const std::vector<rc_ciphertext>& cs, int target) {  // paterson_stockmeyer.rs:230-254
+      require(cs[0].scale_bits <= target, "cannot lower ciphertext scale with a plaintext-one lift");
+      if (cs[0].scale_bits == target) return cs;
+      return A.mul_plain(cs, A.constant(1.0, cs[0].level, target - cs[0].scale_bits), target);
+    };
+    auto truncate_all = [&](const std::vector<rc_ciphertext>& cs, int lv) {  // paterson_stockmeyer.rs:221-228
+      require(lv <= cs[0].level, "target level cannot exceed ciphertext level");
+      std::vector<rc_ciphertext> o(cs.size());
+      for (size_t i = 0; i < cs.size(); ++i) o[i] = A.truncate(cs[i], lv);
+      return o;
+    };
+    auto mult_relin = [&](const std::vector<rc_ciphertext>& lhs, const std::vector<rc_ciphertext>& rhs) {
+      const int lv = lhs[0].level;
+      if (lv < 0 || (uint32_t)lv >= key_levels || !relin_keys[lv])
+        fail(RC_ERR_INVALID_ARGUMENT, "missing Paterson-Stockmeyer relinearization key at level " + std::to_string(lv));
+      std::vector<rc_ciphertext> o(lhs.size());
+      std::vector<const rc_ksk*> ks(lhs.size(), relin_keys[lv]);
+      for (size_t i = 0; i < lhs.size(); ++i) o[i] = A.fresh(lv > 0 ? lv - 1 : 0, 0);
+      ok(rc_mult_relinearized_batch(c, (uint32_t)lhs.size(), lhs.data(), rhs.data(), ks.data(), o.data(), A.s));
+      return o;
+    };
+
+    // baby powers x, x^2, ..., x^b (paterson_stockmeyer.rs:146-173; each lifted to the input scale)
+    const std::vector<rc_ciphertext> base = lift_all(in, in_scale);
+    std::vector<std::vector<rc_ciphertext>> powers{base};
+    for (int e = 2; e <= b; ++e) {
+      const std::vector<rc_ciphertext>& prev = powers.back();
+      const std::vector<rc_ciphertext> aligned_prev = lift_all(prev, in_scale);
+      const std::vector<rc_ciphertext> aligned_base = truncate_all(base, prev[0].level);
+      powers.push_back(lift_all(mult_relin(aligned_prev, aligned_base), in_scale));
+    }
+    const std::vector<rc_ciphertext> giant = powers.back();
+    require(giant[0].level + 1 >= blocks, "polynomial degree is too large for the available CKKS level budget");
+    const int top = giant[0].level;
+
+    auto evaluate_block = [&](int bi, int target_level) {  // paterson_stockmeyer.rs:175-219
+      std::vector<rc_ciphertext> accs(count);
+      for (auto& x : accs) x = constant_ct(target_level, working, 0.0);
+      for (int off = 0; off < b; ++off) {
+        const int k = bi * b + off;
+        if (k >= (int)terms) break;
+        const double cf = coefficients[k];
+        if (cf == 0.0) continue;
+        if (off == 0) {
+          for (auto& x : accs)
+            ok(rc_poly_add(c, x.data, A.constant(cf, x.level, x.scale_bits), x.data, x.level + 1, 0, A.s));
+          continue;
+        }
+        const std::vector<rc_ciphertext>& power = powers[off - 1];
+        const std::vector<rc_ciphertext> aligned = lift_all(truncate_all(power, target_level), power[0].scale_bits);
+        const std::vector<rc_ciphertext> t =
+            A.mul_plain(aligned, A.constant(cf, aligned[0].level, coeff_scale), aligned[0].scale_bits + coeff_scale);
+        accs = A.add(accs, t);
+      }
+      return accs;
+    };
+    std::vector<std::vector<rc_ciphertext>> block_out;
+    for (int bi = 0; bi < blocks; ++bi) block_out.push_back(evaluate_block(bi, top - (blocks - 1 - bi)));
+    std::vector<rc_ciphertext> result = block_out.back();
+    for (int bi = blocks - 2; bi >= 0; --bi) {
+      const std::vector<rc_ciphertext> aligned_giant =
+          lift_all(truncate_all(giant, result[0].level), result[0].scale_bits);
+      const std::vector<rc_ciphertext> multiplied = mult_relin(result, aligned_giant);
+      result = A.add(lift_all(multiplied, result[0].scale_bits), block_out[bi]);
+    }
+    write_out(result);
+  });
+}

@@ -338,3 +338,55 @@ def test_gpu_mult_plain_accumulate_equals_sum_of_mult_plain(realistic):
     assert np.array_equal(ctx.mult_plain_accumulate(ntt_c, ntt_p, True, True).numpy(), acc.numpy())
     with pytest.raises(Exception, match="same scale to add"):
         ctx.mult_plain_accumulate([cts[0], C.RnsCiphertext(cts[1].data, 31)], pts[:2])
+
+
+# ---------------------------------------------------------------------------------------------------------
+# the native schedules (one library call per batch) equal the routines above, residue for residue
+# ---------------------------------------------------------------------------------------------------------
+
+@pytest.mark.gpu
+def test_gpu_native_total_sum_and_halevi_shoup(A, realistic):
+    C, ctx, kp, octx, params = realistic
+    rng = np.random.default_rng(31)
+    cts = [_encrypt(C, ctx, kp, rng.uniform(-0.5, 0.5, ctx.num_slots()), 60 + i) for i in range(3)]
+    gk, _ = _rot_keys(ctx, kp, A.total_sum_rotation_steps(8), cts[0].level)
+    got = A.total_sum_native(ctx, cts, 8, gk)
+    want = A.total_sum_batch(ctx, cts, 8, gk)
+    for g, w in zip(got, want):
+        assert (g.level, g.scale_bits) == (w.level, w.scale_bits) and np.array_equal(g.numpy(), w.numpy())
+    with pytest.raises(Exception, match="missing total-sum rotation key for step 4"):
+        A.total_sum_native(ctx, cts, 8, {1: gk[1], 2: gk[2]})
+    # Halevi-Shoup: one plaintext per ciphertext, same length
+    plains = [rng.uniform(-2, 2, 4) for _ in cts]
+    hk, _ = _rot_keys(ctx, kp, A.halevi_shoup_dot_product_rotation_steps(4), cts[0].level - 1)
+    got = A.halevi_shoup_dot_product_native(ctx, cts, plains, hk)
+    want = A.halevi_shoup_dot_product_batch(ctx, cts, plains, hk)
+    for g, w in zip(got, want):
+        assert (g.level, g.scale_bits) == (w.level, w.scale_bits) and np.array_equal(g.numpy(), w.numpy())
+    with pytest.raises(Exception, match="plaintext slot vector cannot exceed the CKKS slot count"):
+        A.halevi_shoup_dot_product_native(ctx, cts[:1], [np.zeros(ctx.num_slots() + 1)], hk)
+
+
+@pytest.mark.gpu
+def test_gpu_native_paterson_stockmeyer(A, realistic):
+    C, ctx, kp, octx, params = realistic
+    slots = np.zeros(ctx.num_slots())
+    slots[:4] = PS_INPUT
+    cts = [_encrypt(C, ctx, kp, slots, 71), _encrypt(C, ctx, kp, slots[::-1].copy(), 72)]
+    gk = {lv: ctx.generate_relinearization_key_at_level(kp.secret_key, kp.public_key, lv)
+          for lv in A.paterson_stockmeyer_required_levels(cts[0].level, len(PS_COEFFS))}
+    got = A.paterson_stockmeyer_eval_native(ctx, cts, PS_COEFFS, gk)
+    want = A.paterson_stockmeyer_eval_batch(ctx, cts, PS_COEFFS, gk)
+    for g, w in zip(got, want):
+        assert (g.level, g.scale_bits) == (w.level, w.scale_bits) and np.array_equal(g.numpy(), w.numpy())
+    dec = ctx.decode_real_at_scale(ctx.decrypt(got[0], kp.secret_key), got[0].scale_bits)
+    expect = [sum(c * x ** i for i, c in enumerate(PS_COEFFS)) for x in PS_INPUT]
+    assert np.max(np.abs(dec[:4] - expect)) <= 2e-2
+    # a constant polynomial, a polynomial with zero terms, and a missing key
+    one = A.paterson_stockmeyer_eval_native(ctx, cts[:1], [0.25], gk)[0]
+    assert np.array_equal(one.numpy(), A.paterson_stockmeyer_eval(ctx, cts[0], [0.25], gk).numpy())
+    sparse = [0.0, 0.5, 0.0, -0.25, 0.0]
+    assert np.array_equal(A.paterson_stockmeyer_eval_native(ctx, cts[:1], sparse, gk)[0].numpy(),
+                          A.paterson_stockmeyer_eval(ctx, cts[0], sparse, gk).numpy())
+    with pytest.raises(Exception, match="missing Paterson-Stockmeyer relinearization key at level"):
+        A.paterson_stockmeyer_eval_native(ctx, cts[:1], PS_COEFFS, {})
