@@ -100,6 +100,8 @@ struct Algo {
     std::vector<rc_ciphertext> o(a.size());
     for (size_t i = 0; i < a.size(); ++i) o[i] = into ? into[i] : fresh(a[i].level, a[i].scale_bits);
     ok(rc_add_batch(c, (uint32_t)a.size(), a.data(), b.data(), o.data(), s));
+    if (into)
+      for (size_t i = 0; i < a.size(); ++i) into[i] = o[i];  // level and scale of the caller's outputs
     return o;
   }
 
