@@ -80,19 +80,35 @@ struct Algo {
     return o;
   }
 
-  // encode of N/2 slots all equal to `value` at (level, scale), on the GPU, memoised for the call
+  // encode of N/2 slots all equal to `value` at (level, scale), on the GPU, kept in the context's cache (the
+  // same constants recur across calls: PS coefficients, plaintext ones of the scale lifts); past the cache's
+  // cap a constant lives in this call's stream-ordered scratch
   uint64_t* constant(double value, int level, int scale) {
     auto key = std::make_tuple(value, level, scale);
     auto it = consts.find(key);
     if (it != consts.end()) return it->second;
-    uint64_t* out = pool.take((size_t)(level + 1) * N);
+    const size_t words = (size_t)(level + 1) * N;
+    std::unique_ptr<DevBuf> buf;
+    {
+      std::lock_guard<std::mutex> lk(c->mu);
+      auto ct = c->const_cache.find(key);
+      if (ct != c->const_cache.end()) return consts[key] = (uint64_t*)ct->second->p;
+      if (c->const_cache.size() < 1024) buf.reset(new DevBuf(words * 8));
+    }
+    uint64_t* out = buf ? (uint64_t*)buf->p : pool.take(words);
     double* dslots = (double*)pool.take(N);
     const size_t half = N / 2;
     k_fill_const<<<(unsigned)std::min<size_t>((half + 255) / 256, 1024), 256, 0, s>>>(dslots, value, half);
     cuda_check(cudaGetLastError(), "constant slots");
     ok(rc_encode_device(c, dslots, 1, level, (uint32_t)scale, out, s));
-    consts[key] = out;
-    return out;
+    if (buf) {
+      cuda_check(cudaStreamSynchronize(s), "constant encode");  // complete before another stream may read it
+      std::lock_guard<std::mutex> lk(c->mu);
+      auto& slot = c->const_cache[key];
+      if (!slot) slot = std::move(buf);  // another thread may have cached the same constant meanwhile
+      out = (uint64_t*)slot->p;
+    }
+    return consts[key] = out;
   }
 
   std::vector<rc_ciphertext> add(const std::vector<rc_ciphertext>& a, const std::vector<rc_ciphertext>& b,

@@ -5,6 +5,7 @@
 #include <cuda_runtime.h>
 
 #include <map>
+#include <tuple>
 #include <memory>
 #include <mutex>
 #include <stdexcept>
@@ -100,6 +101,9 @@ struct rc_context {
   rc::WideTab wide{};     // CRT back to the scheme primes (tables in wide_buf)
   std::unique_ptr<rc::DevBuf> wide_buf, wide_tw;
   std::unique_ptr<rc::DevBuf> fft_buf;  // device encoder tables (built on first use, under mu)
+  // encoded constant plaintexts (all slots = value) by (value, level, scale_bits) for the native schedules;
+  // complete before they are handed out, capped in count (under mu)
+  std::map<std::tuple<double, int, int>, std::unique_ptr<rc::DevBuf>> const_cache;
   std::vector<uint64_t> mod, root;  // Q then P
   std::unique_ptr<rc::DevBuf> pc_buf, tw_buf, md_buf, rt_buf;
   rc::PrimeConst* d_pc = nullptr;

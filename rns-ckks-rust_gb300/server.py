@@ -216,11 +216,13 @@ def keyswitch_scratch_bytes(n: int, limbs: int, aux: int, digits: int) -> int:
 class GpuExecutor:
     """Runs batches of jobs on per-slot CUDA streams through the batched routines of `algorithms` and the
     context.  Jobs carry (kind, ctx, inputs...); see `hadamard_job`, `halevi_shoup_job`,
-    `paterson_stockmeyer_job`."""
+    `paterson_stockmeyer_job`.  With `native` (the default) the Halevi-Shoup and Paterson-Stockmeyer batches
+    run as one library call each (the native schedules, same residues)."""
 
-    def __init__(self, slots: int):
+    def __init__(self, slots: int, native: bool = True):
         import torch
         self.torch = torch
+        self.native = native
         self.streams = [torch.cuda.Stream() for _ in range(slots)]
 
     def __call__(self, slot: int, jobs: List[Job]) -> List[Any]:
@@ -234,11 +236,15 @@ class GpuExecutor:
                 out = ctx.mult_relinearized_batch([j.payload["lhs"] for j in jobs], [j.payload["rhs"] for j in jobs],
                                                   [j.payload["key"] for j in jobs])
             elif kind == "halevi_shoup":
-                out = A.halevi_shoup_dot_product_batch(ctx, [j.payload["ct"] for j in jobs],
-                                                       [j.payload["plain"] for j in jobs], p0["keys"])
+                hs = A.halevi_shoup_dot_product_native if self.native else A.halevi_shoup_dot_product_batch
+                out = hs(ctx, [j.payload["ct"] for j in jobs], [j.payload["plain"] for j in jobs], p0["keys"])
             elif kind == "paterson_stockmeyer":
-                out = A.paterson_stockmeyer_eval_batch(ctx, [j.payload["ct"] for j in jobs], p0["coeffs"], p0["keys"],
-                                                       p0.get("plains"))
+                if self.native:
+                    out = A.paterson_stockmeyer_eval_native(ctx, [j.payload["ct"] for j in jobs], p0["coeffs"],
+                                                            p0["keys"])
+                else:
+                    out = A.paterson_stockmeyer_eval_batch(ctx, [j.payload["ct"] for j in jobs], p0["coeffs"],
+                                                           p0["keys"], p0.get("plains"))
             else:
                 raise ValueError(f"unknown job kind {kind}")
             self.streams[slot].synchronize()
