@@ -606,11 +606,11 @@ def bsgs_matvec_bench(pkg, C, seed, batch=32, dim=128, reps=2):
     diags = A.pack_diagonal_plaintexts(ctx, matrix, cts[0].level, cts[0].scale_bits)
     torch.cuda.synchronize()
     t_pack = time.perf_counter() - t0
-    out = A.apply_diagonal_linear_transform_batch(ctx, cts, diags, keys)  # warm
+    out = A.apply_diagonal_linear_transform_native(ctx, cts, diags, keys)  # warm
     torch.cuda.synchronize()
     t0 = time.perf_counter()
     for _ in range(reps):
-        out = A.apply_diagonal_linear_transform_batch(ctx, cts, diags, keys)
+        out = A.apply_diagonal_linear_transform_native(ctx, cts, diags, keys)
     torch.cuda.synchronize()
     secs = (time.perf_counter() - t0) / reps
     single_t0 = time.perf_counter()

@@ -275,6 +275,15 @@ int rc_halevi_shoup_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* 
 int rc_paterson_stockmeyer_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* cts,
                                  const double* coefficients, uint32_t terms, const rc_ksk* const* relin_keys,
                                  uint32_t key_levels, rc_ciphertext* out, void* stream);
+/* apply_diagonal_linear_transform (src/ckks/bootstrapping/linear_transform.rs:109-150, 213-252) for `count`
+ * ciphertexts at (diag_level, diag_scale_bits) sharing one set of packed BSGS diagonals: diag_ntt[g *
+ * baby_step + j] is diagonal g*b+j pre-rotated by the giant shift g*b, encoded at the ciphertexts' level and
+ * scale and in the NTT domain (rc_ntt_forward), null past the dimension; baby_keys[s-1] rotates by s
+ * (s < min(baby_step, dimension)), giant_keys[g-1] by g*baby_step.  out[i] is one level down. */
+int rc_bsgs_apply_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* cts, uint32_t dimension,
+                        uint32_t baby_step, const uint64_t* const* diag_ntt, uint32_t giants, int32_t diag_level,
+                        int32_t diag_scale_bits, const rc_ksk* const* baby_keys, const rc_ksk* const* giant_keys,
+                        rc_ciphertext* out, void* stream);
 
 /* ---- CUDA graphs of library calls (no reference counterpart: the crate is CPU-only).  Capture every
  * call made on `stream` between begin and end (thread-local capture mode) into an executable graph;

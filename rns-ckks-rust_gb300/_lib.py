@@ -111,6 +111,8 @@ SIGNATURES = [
     ("rc_halevi_shoup_batch", ctypes.c_int, [_vp, _u32, _CT, _vp, _u32, ctypes.POINTER(_vp), _u32, _CT, _vp]),
     ("rc_paterson_stockmeyer_batch", ctypes.c_int, [_vp, _u32, _CT, _vp, _u32, ctypes.POINTER(_vp), _u32, _CT,
                                                     _vp]),
+    ("rc_bsgs_apply_batch", ctypes.c_int, [_vp, _u32, _CT, _u32, _u32, ctypes.POINTER(_vp), _u32, _i32, _i32,
+                                           ctypes.POINTER(_vp), ctypes.POINTER(_vp), _CT, _vp]),
     ("rc_graph_begin", ctypes.c_int, [_vp, _vp]),
     ("rc_graph_end", ctypes.c_int, [_vp, _vp, ctypes.POINTER(_vp)]),
     ("rc_graph_launch", ctypes.c_int, [_vp, _vp]),

@@ -651,3 +651,28 @@ def paterson_stockmeyer_eval_native(ctx: RnsCkksContext, ciphertexts: Sequence[R
     # the library wrote [c0][c1] with the result's limb count at the front of each buffer
     return [RnsCiphertext(o.view(-1)[: 2 * (O[i].level + 1) * n].view(2, O[i].level + 1, n).clone(), O[i].scale_bits,
                           O[i].level) for i, o in enumerate(outs)]
+
+
+def apply_diagonal_linear_transform_native(ctx: RnsCkksContext, ciphertexts: Sequence[RnsCiphertext],
+                                           diagonals: DiagonalTransformPlaintexts,
+                                           rotation_keys: DiagonalTransformRotationKeys) -> List[RnsCiphertext]:
+    """The BSGS transform (linear_transform.rs:109-150) of a batch with one set of diagonals, as one library call
+    (rc_bsgs_apply_batch); the same residues as `apply_diagonal_linear_transform_batch`."""
+    import ctypes
+    from ._lib import call
+    from .context import _stream
+    cts = list(ciphertexts)
+    if not cts:
+        return []
+    b, g = diagonals.baby_step, len(diagonals.giant_step_diagonals_ntt)
+    diag = (ctypes.c_void_p * (g * b))(*[(p.data_ptr() if p is not None else None)
+                                          for row in diagonals.giant_step_diagonals_ntt for p in row])
+    ks = rotation_keys.by_step
+    baby = (ctypes.c_void_p * max(1, b - 1))(
+        *[(ks[s].keyswitch_key.handle if s in ks else None) for s in range(1, b)])
+    giant = (ctypes.c_void_p * max(1, g - 1))(
+        *[(ks[k * b].keyswitch_key.handle if k * b in ks else None) for k in range(1, g)])
+    outs, O = _raw_out(ctx, [max(c.level - 1, 0) for c in cts])
+    call("rc_bsgs_apply_batch", ctx.handle, len(cts), _raw_in(cts), diagonals.dimension, b, diag, g,
+         diagonals.level, diagonals.scale_bits, baby, giant, O, _stream())
+    return [RnsCiphertext(o, O[i].scale_bits, O[i].level) for i, o in enumerate(outs)]

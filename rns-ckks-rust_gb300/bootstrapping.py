@@ -408,7 +408,7 @@ def _transform_batch(ctx, cts: Sequence[RnsCiphertext], pre: _TransformPrecomput
                      rotation_keys: A.DiagonalTransformRotationKeys) -> List[RnsCiphertext]:
     for ct in cts:
         _Runtime.new(pre.plan, ct)
-    return A.apply_diagonal_linear_transform_batch(ctx, list(cts), pre.diagonals, rotation_keys)
+    return A.apply_diagonal_linear_transform_native(ctx, list(cts), pre.diagonals, rotation_keys)
 
 
 def coeff_to_slot(ctx: RnsCkksContext, ciphertext: RnsCiphertext, precomputed: CoeffToSlotPrecomputed,
@@ -445,7 +445,8 @@ def coeff_to_slot_dense(ctx: RnsCkksContext, ciphertext: RnsCiphertext, conjugat
     """coeff_to_slot.rs:262-307 with apply_dense_branch (332-343)."""
     _Runtime.new(precomputed.plan, ciphertext)
     _check_pair(conjugated_ciphertext, ciphertext, "conjugated ciphertext", "CoeffToSlot input")
-    lt = A.apply_diagonal_linear_transform
+    def lt(ctx_, ct, diags, keys):
+        return A.apply_diagonal_linear_transform_native(ctx_, [ct], diags, keys)[0]
 
     def branch(from_slots, from_conj):
         return lt(ctx, ciphertext, from_slots, rotation_keys).add(
@@ -462,7 +463,8 @@ def slot_to_coeff_dense(ctx: RnsCkksContext, upper: RnsCiphertext, lower: RnsCip
     """slot_to_coeff.rs:243-280."""
     _Runtime.new(precomputed.plan, upper)
     _check_pair(lower, upper, "lower dense SlotToCoeff ciphertext", "upper")
-    lt = A.apply_diagonal_linear_transform
+    def lt(ctx_, ct, diags, keys):
+        return A.apply_diagonal_linear_transform_native(ctx_, [ct], diags, keys)[0]
     return lt(ctx, upper, precomputed.slots_from_upper, rotation_keys).add(
         lt(ctx, lower, precomputed.slots_from_lower, rotation_keys))
 

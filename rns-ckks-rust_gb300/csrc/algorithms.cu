@@ -366,3 +366,118 @@ extern "C" int rc_paterson_stockmeyer_batch(rc_context* c, uint32_t count, const
     write_out(result);
   });
 }
+
+// apply_diagonal_linear_transform (src/ckks/bootstrapping/linear_transform.rs:109-150, 213-252) for a batch
+// sharing one set of packed diagonals: baby-step rotations of every ciphertext in one call, all babies to the
+// NTT domain in one call, each inner sum as one NTT-domain multiply-accumulate, the giant-step rotations of all
+// inner sums in one call, the adds in the crate's giant order, one rescale.  diag_ntt[g * baby_step + j] is
+// the NTT-domain diagonal g*b+j pre-rotated by g*b (null past the dimension); baby_keys[s-1] rotates by s,
+// giant_keys[g-1] by g*b.
+extern "C" int rc_bsgs_apply_batch(rc_context* c, uint32_t count, const rc_ciphertext* cts, uint32_t dimension,
+                                   uint32_t baby_step, const uint64_t* const* diag_ntt, uint32_t giants,
+                                   int32_t diag_level, int32_t diag_scale_bits, const rc_ksk* const* baby_keys,
+                                   const rc_ksk* const* giant_keys, rc_ciphertext* out, void* stream) {
+  return guarded([&] {
+    require(c && cts && diag_ntt && out, "arguments must not be null");
+    if (count == 0) return;
+    for (uint32_t i = 0; i < count; ++i) {
+      require(cts[i].level == diag_level, "packed diagonals must match the ciphertext level");
+      require(cts[i].scale_bits == diag_scale_bits, "packed diagonals must match the ciphertext scale");
+    }
+    Algo A(c, stream);
+    const int lv = diag_level, limbs = lv + 1;
+    const uint32_t b = std::min(baby_step, dimension);
+    const size_t ct_words = 2 * (size_t)limbs * A.N;
+    // precompute_baby_rotations (213-232): rotations by 1 .. b-1 of every ciphertext, jobs sharing a key adjacent
+    std::vector<rc_ciphertext> jobs, rot;
+    std::vector<const rc_ksk*> keys;
+    for (uint32_t st = 1; st < b; ++st) {
+      if (!baby_keys || !baby_keys[st - 1])
+        fail(RC_ERR_INVALID_ARGUMENT, "missing input rotation key for BSGS baby step " + std::to_string(st));
+      for (uint32_t i = 0; i < count; ++i) {
+        jobs.push_back(cts[i]);
+        keys.push_back(baby_keys[st - 1]);
+      }
+    }
+    // the babies of ciphertext i in the NTT domain: babies[(i * b + j)] (j = 0 is the ciphertext itself)
+    uint64_t* babies = A.pool.take(ct_words * count * b);
+    if (!jobs.empty()) {
+      rot.resize(jobs.size());
+      for (size_t k = 0; k < jobs.size(); ++k) {
+        const uint32_t st = 1 + (uint32_t)(k / count), i = (uint32_t)(k % count);
+        rot[k] = rc_ciphertext{babies + ((size_t)i * b + st) * ct_words, lv, diag_scale_bits};
+      }
+      ok(rc_rotate_batch(c, (uint32_t)jobs.size(), jobs.data(), keys.data(), rot.data(), A.s));
+    }
+    for (uint32_t i = 0; i < count; ++i)
+      cuda_check(cudaMemcpyAsync(babies + (size_t)i * b * ct_words, cts[i].data, ct_words * 8,
+                                 cudaMemcpyDeviceToDevice, A.s),
+                 "copy");
+    ok(rc_ntt_forward(c, babies, count * b * 2, (uint32_t)limbs, 0, A.s));
+    // apply_giant_step_terms (234-252): inner[i][g] = sum_j mult_plain(baby_j, diag_{g,j})
+    std::vector<std::vector<rc_ciphertext>> inner(count, std::vector<rc_ciphertext>(giants));
+    std::vector<std::vector<bool>> present(count, std::vector<bool>(giants, false));
+    for (uint32_t i = 0; i < count; ++i) {
+      for (uint32_t g = 0; g < giants; ++g) {
+        std::vector<rc_ciphertext> terms;
+        std::vector<const uint64_t*> plains;
+        for (uint32_t j = 0; j < baby_step; ++j) {
+          const uint64_t* d = diag_ntt[(size_t)g * baby_step + j];
+          if (!d) continue;
+          require(j < b, "internal: diagonal beyond the baby steps");
+          terms.push_back(rc_ciphertext{babies + ((size_t)i * b + j) * ct_words, lv, diag_scale_bits});
+          plains.push_back(d);
+        }
+        if (terms.empty()) continue;
+        inner[i][g] = A.fresh(lv, 0);
+        ok(rc_mult_plain_accumulate(c, (uint32_t)terms.size(), terms.data(), 1, plains.data(), 1, &inner[i][g], A.s));
+        present[i][g] = true;
+      }
+    }
+    // giant-step rotations of the unrescaled inner sums, jobs sharing a key adjacent
+    jobs.clear();
+    keys.clear();
+    std::vector<std::pair<uint32_t, uint32_t>> where;
+    for (uint32_t g = 1; g < giants; ++g) {
+      for (uint32_t i = 0; i < count; ++i) {
+        if (!present[i][g]) continue;
+        if (!giant_keys || !giant_keys[g - 1])
+          fail(RC_ERR_INVALID_ARGUMENT,
+               "missing input rotation key for BSGS giant step " + std::to_string(g * baby_step));
+        jobs.push_back(inner[i][g]);
+        keys.push_back(giant_keys[g - 1]);
+        where.emplace_back(i, g);
+      }
+    }
+    if (!jobs.empty()) {
+      rot.assign(jobs.size(), rc_ciphertext{});
+      for (size_t k = 0; k < jobs.size(); ++k) rot[k] = A.fresh(lv, jobs[k].scale_bits);
+      ok(rc_rotate_batch(c, (uint32_t)jobs.size(), jobs.data(), keys.data(), rot.data(), A.s));
+      for (size_t k = 0; k < jobs.size(); ++k) inner[where[k].first][where[k].second] = rot[k];
+    }
+    // the adds in giant order (one batched call per giant step over all ciphertexts), then one rescale
+    std::vector<rc_ciphertext> accs(count);
+    std::vector<uint32_t> next(count, 0);
+    for (uint32_t i = 0; i < count; ++i) {
+      uint32_t g = 0;
+      while (g < giants && !present[i][g]) ++g;
+      require(g < giants, "diagonal transform must contain at least one non-empty giant-step block");
+      accs[i] = inner[i][g];
+      next[i] = g + 1;
+    }
+    for (uint32_t g = 1; g < giants; ++g) {
+      std::vector<rc_ciphertext> lhs, rhs;
+      std::vector<uint32_t> idx;
+      for (uint32_t i = 0; i < count; ++i)
+        if (g >= next[i] && present[i][g]) {
+          lhs.push_back(accs[i]);
+          rhs.push_back(inner[i][g]);
+          idx.push_back(i);
+        }
+      if (lhs.empty()) continue;
+      const std::vector<rc_ciphertext> sum = A.add(lhs, rhs);
+      for (size_t k = 0; k < idx.size(); ++k) accs[idx[k]] = sum[k];
+    }
+    ok(rc_rescale_batch(c, count, accs.data(), out, A.s));
+  });
+}

@@ -390,3 +390,26 @@ def test_gpu_native_paterson_stockmeyer(A, realistic):
                           A.paterson_stockmeyer_eval(ctx, cts[0], sparse, gk).numpy())
     with pytest.raises(Exception, match="missing Paterson-Stockmeyer relinearization key at level"):
         A.paterson_stockmeyer_eval_native(ctx, cts[:1], PS_COEFFS, {})
+
+
+@pytest.mark.gpu
+@pytest.mark.parametrize("dim", [4, 8, 16])
+def test_gpu_native_bsgs_equals_routine(A, realistic, dim):
+    C, ctx, kp, octx, params = realistic
+    rng = np.random.default_rng(100 + dim)
+    matrix = rng.uniform(-1, 1, (dim, dim))
+    cts = [_encrypt(C, ctx, kp, A.repeat_real_vector_blocks(rng.uniform(-1, 1, dim), ctx.num_slots()), 110 + i)
+           for i in range(3)]
+    gk, _ = _rot_keys(ctx, kp, A.diagonal_transform_bsgs_rotation_steps(dim), cts[0].level)
+    keys = A.DiagonalTransformRotationKeys(gk)
+    diags = A.pack_diagonal_plaintexts(ctx, matrix, cts[0].level, cts[0].scale_bits)
+    got = A.apply_diagonal_linear_transform_native(ctx, cts, diags, keys)
+    want = A.apply_diagonal_linear_transform_batch(ctx, cts, diags, keys)
+    for g, w in zip(got, want):
+        assert (g.level, g.scale_bits) == (w.level, w.scale_bits) and np.array_equal(g.numpy(), w.numpy())
+    missing = dict(gk)
+    missing.pop(1)
+    with pytest.raises(Exception, match="missing input rotation key for BSGS baby step 1"):
+        A.apply_diagonal_linear_transform_native(ctx, cts[:1], diags, A.DiagonalTransformRotationKeys(missing))
+    with pytest.raises(Exception, match="packed diagonals must match the ciphertext level"):
+        A.apply_diagonal_linear_transform_native(ctx, [cts[0].drop_last_level()], diags, keys)
