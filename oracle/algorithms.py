@@ -145,12 +145,14 @@ def bsgs_baby_step(dimension: int) -> int:
     return b
 
 
-def pack_bsgs_diagonals(ctx: Context, matrix, level: int, scale_bits: int) -> List[List[Optional[np.ndarray]]]:
+def pack_bsgs_diagonals(ctx: Context, matrix, level: int, scale_bits: int,
+                        baby_step: Optional[int] = None) -> List[List[Optional[np.ndarray]]]:
     """linear_transform.rs:160-211: giant_step_diagonals[g][j] = diagonal g*b+j, pre-rotated by the giant
-    shift g*b and tiled with period `dimension`."""
+    shift g*b and tiled with period `dimension`.  `baby_step` overrides the crate's ceil(sqrt(d)) split (a
+    variant the crate does not offer; the same packing rule with another b)."""
     m = [list(map(complex, row)) for row in matrix]
     d = len(m)
-    b = bsgs_baby_step(d)
+    b = baby_step or bsgs_baby_step(d)
     out = []
     for g in range((d + b - 1) // b):
         shift = (g * b) % d
@@ -171,9 +173,9 @@ def pack_bsgs_diagonals(ctx: Context, matrix, level: int, scale_bits: int) -> Li
 
 
 def apply_diagonal_linear_transform(ctx: Context, ct: Ct, giant_step_diagonals, dimension: int,
-                                    rotation_keys: Dict[int, tuple]) -> Ct:
-    """linear_transform.rs:109-150 with 213-252."""
-    b = bsgs_baby_step(dimension)
+                                    rotation_keys: Dict[int, tuple], baby_step: Optional[int] = None) -> Ct:
+    """linear_transform.rs:109-150 with 213-252 (`baby_step` as in pack_bsgs_diagonals)."""
+    b = baby_step or bsgs_baby_step(dimension)
     babies = [ct] + [ctx.rotate(ct, rotation_keys[s]) for s in range(1, min(b, dimension))]
     acc = None
     for g, diags in enumerate(giant_step_diagonals):

@@ -179,13 +179,23 @@ def diagonal_transform_bsgs_baby_step(dimension: int) -> int:
     return b
 
 
-def diagonal_transform_bsgs_rotation_steps(dimension: int) -> List[int]:
+def _baby_step_for(dimension: int, baby_step: Optional[int]) -> int:
+    """The crate's split (ceil(sqrt(dimension))) unless a baby step is given.  Another split is a variant the
+    crate does not offer: the same rotations and packing rule with another b, not the crate's residues."""
+    if baby_step is None:
+        return diagonal_transform_bsgs_baby_step(dimension)
+    if baby_step <= 0 or baby_step > dimension:
+        _panic("BSGS baby step must be in 1..=dimension")
+    return baby_step
+
+
+def diagonal_transform_bsgs_rotation_steps(dimension: int, baby_step: Optional[int] = None) -> List[int]:
     """linear_transform.rs:27-50: baby steps 1..b-1 and giant steps g*b below dimension."""
     if dimension <= 0:
         _panic("transform dimension must be positive")
     if dimension == 1:
         return []
-    b = diagonal_transform_bsgs_baby_step(dimension)
+    b = _baby_step_for(dimension, baby_step)
     giants = (dimension + b - 1) // b
     steps = set(range(1, min(b, dimension)))
     steps.update(g * b for g in range(1, giants) if g * b < dimension)
@@ -193,11 +203,12 @@ def diagonal_transform_bsgs_rotation_steps(dimension: int) -> List[int]:
 
 
 def generate_diagonal_transform_rotation_keys(ctx: RnsCkksContext, secret_key, public_key, ciphertext_level: int,
-                                              dimension: int) -> DiagonalTransformRotationKeys:
+                                              dimension: int,
+                                              baby_step: Optional[int] = None) -> DiagonalTransformRotationKeys:
     """linear_transform.rs:52-67."""
     return DiagonalTransformRotationKeys({
         step: ctx.generate_rotation_key_at_level(secret_key, public_key, step, ciphertext_level)
-        for step in diagonal_transform_bsgs_rotation_steps(dimension)})
+        for step in diagonal_transform_bsgs_rotation_steps(dimension, baby_step)})
 
 
 def repeat_block_slots(values, slot_count: int) -> np.ndarray:
@@ -245,12 +256,12 @@ def _packed_bsgs_diagonal_slots(m: np.ndarray, diagonal_step: int, giant_shift: 
     return m[src, (diagonal_step + src) % d]
 
 
-def pack_diagonal_transform_plaintexts(ctx: RnsCkksContext, matrix, level: int,
-                                       scale_bits: int) -> DiagonalTransformPlaintexts:
-    """linear_transform.rs:79-107 (+ 160-191)."""
+def pack_diagonal_transform_plaintexts(ctx: RnsCkksContext, matrix, level: int, scale_bits: int,
+                                       baby_step: Optional[int] = None) -> DiagonalTransformPlaintexts:
+    """linear_transform.rs:79-107 (+ 160-191); `baby_step` as in diagonal_transform_bsgs_rotation_steps."""
     d = _validate_square_matrix(matrix, ctx.num_slots())
     m = np.asarray(matrix, dtype=np.complex128)
-    b = diagonal_transform_bsgs_baby_step(d)
+    b = _baby_step_for(d, baby_step)
     giants = (d + b - 1) // b
     # every diagonal and every pre-rotated BSGS diagonal in one batched GPU encode (each plaintext equals the
     # single host encode of its slots)
@@ -359,9 +370,10 @@ def packed_diagonal_rotation_steps(row_count: int) -> List[int]:
 
 
 def generate_packed_diagonal_rotation_keys(ctx, secret_key, public_key, ciphertext_level: int,
-                                           row_count: int) -> PackedDiagonalRotationKeys:
+                                           row_count: int, baby_step: Optional[int] = None) -> PackedDiagonalRotationKeys:
     """packed_diagonal.rs:33-41 (BSGS steps)."""
-    return generate_diagonal_transform_rotation_keys(ctx, secret_key, public_key, ciphertext_level, row_count)
+    return generate_diagonal_transform_rotation_keys(ctx, secret_key, public_key, ciphertext_level, row_count,
+                                                     baby_step)
 
 
 def repeat_real_vector_blocks(values, slot_count: int) -> np.ndarray:
@@ -369,10 +381,11 @@ def repeat_real_vector_blocks(values, slot_count: int) -> np.ndarray:
     return repeat_block_slots(np.asarray(values, dtype=np.float64), slot_count)
 
 
-def pack_diagonal_plaintexts(ctx, matrix, level: int, scale_bits: int) -> PackedDiagonalPlaintexts:
+def pack_diagonal_plaintexts(ctx, matrix, level: int, scale_bits: int,
+                             baby_step: Optional[int] = None) -> PackedDiagonalPlaintexts:
     """packed_diagonal.rs:47-58 (real matrix)."""
     return pack_diagonal_transform_plaintexts(ctx, np.asarray(matrix, dtype=np.float64).astype(np.complex128),
-                                              level, scale_bits)
+                                              level, scale_bits, baby_step)
 
 
 def packed_diagonal_matvec_prepacked(ctx, ciphertext, diagonals, rotation_keys) -> RnsCiphertext:

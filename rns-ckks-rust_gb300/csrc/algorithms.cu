@@ -30,6 +30,117 @@ void ok(int status) {
   if (status != RC_OK) fail(status, rc_last_error(nullptr));
 }
 
+// ---- BSGS inner sums of a batch in one launch (apply_giant_step_terms, linear_transform.rs:234-252) ----
+// inner[i][g][c] = sum_j baby[i][j][c] * diag[g][j] mod q over the NTT domain, for every ciphertext i, giant
+// g and component c.  A thread owns one coefficient of one ciphertext and keeps its b babies in registers
+// across the giants; the warps of a block share coefficients (ciphertexts differ), so each diagonal word is
+// fetched from memory once per block.  On a limb whose prime is below 2^52 a residue x splits as
+// x1 * 2^26 + x0 (both < 2^26) and a product as x0 y0 + ((x0 + x1)(y0 + y1) - x0 y0 - x1 y1) 2^26 + x1 y1 2^52:
+// three 32 x 32 -> 64-bit multiply-adds per term, summed exactly in 64-bit columns (each column below
+// 16 * 2^54) and reduced once per output.  A limb with a larger prime (a 60-bit base prime) takes the
+// per-term Barrett product; a warp's 32 coefficients always share one limb, so the branch is uniform.
+constexpr int BSGS_MAX_TABLE = 256;
+struct DiagTab {
+  const u64* p[BSGS_MAX_TABLE];  // [g * b + j], null past the dimension
+};
+
+__device__ __forceinline__ uint32_t lo26(u64 x) { return (uint32_t)x & ((1u << 26) - 1); }
+__device__ __forceinline__ uint32_t hi26(u64 x) { return (uint32_t)(x >> 26); }
+__device__ __forceinline__ u64 mad_wide(uint32_t a, uint32_t b, u64 acc) { return acc + (u64)a * b; }
+
+template <int BM>
+__global__ void __launch_bounds__(256, 2) k_bsgs_inner(const PrimeConst* pc, const u64* __restrict__ babies,
+                                                    DiagTab diag, u64* __restrict__ out, int count, int b,
+                                                    int giants, int limbs, int log_n) {
+  const size_t pl = (size_t)limbs << log_n;
+  const size_t e = (size_t)blockIdx.x * 32 + threadIdx.x;
+  const int i = blockIdx.y * blockDim.y + threadIdx.y;
+  if (e >= pl || i >= count) return;
+  const PrimeConst& c = pc[(int)(e >> log_n)];
+  const bool split = (c.q >> 52) == 0;
+  // babies: (x0, x1) = the 26-bit halves when split, else the 32-bit words
+  uint32_t x0[2][BM], x1[2][BM];
+#pragma unroll
+  for (int j = 0; j < BM; ++j) {
+    if (j < b) {
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const u64 v = babies[(((size_t)i * b + j) * 2 + k) * pl + e];
+        x0[k][j] = split ? lo26(v) : (uint32_t)v;
+        x1[k][j] = split ? hi26(v) : (uint32_t)(v >> 32);
+      }
+    }
+  }
+  for (int g = 0; g < giants; ++g) {
+    u64* o = out + ((size_t)i * giants + g) * 2 * pl + e;
+    if (split) {
+      u64 p00[2] = {0, 0}, p11[2] = {0, 0}, pk[2] = {0, 0};
+#pragma unroll
+      for (int j = 0; j < BM; ++j) {
+        if (j < b) {
+          const u64* d = diag.p[g * b + j];
+          if (d) {
+            const u64 y = __ldg(d + e);
+            const uint32_t y0 = lo26(y), y1 = hi26(y), ys = y0 + y1;
+#pragma unroll
+            for (int k = 0; k < 2; ++k) {
+              p00[k] = mad_wide(x0[k][j], y0, p00[k]);
+              p11[k] = mad_wide(x1[k][j], y1, p11[k]);
+              pk[k] = mad_wide(x0[k][j] + x1[k][j], ys, pk[k]);
+            }
+          }
+        }
+      }
+#pragma unroll
+      for (int k = 0; k < 2; ++k) {
+        const u64 cross = pk[k] - p00[k] - p11[k];
+        // p00 + cross * 2^26 + p11 * 2^52 as 128 bits (below 16 q^2 < q * 2^64)
+        U128 t;
+        const u64 c_lo = cross << 26, p_lo = p11[k] << 52;
+        t.lo = p00[k] + c_lo;
+        t.hi = (cross >> 38) + (t.lo < c_lo ? 1ull : 0ull);
+        t.lo += p_lo;
+        t.hi += (p11[k] >> 12) + (t.lo < p_lo ? 1ull : 0ull);
+        o[(size_t)k * pl] = barrett_reduce(t, c);
+      }
+    } else {
+      u64 acc[2] = {0, 0};
+#pragma unroll
+      for (int j = 0; j < BM; ++j) {
+        if (j < b) {
+          const u64* d = diag.p[g * b + j];
+          if (d) {
+            const u64 y = __ldg(d + e);
+#pragma unroll
+            for (int k = 0; k < 2; ++k)
+              acc[k] = add_mod(acc[k], mul_mod((u64)x1[k][j] << 32 | x0[k][j], y, c), c.q);
+          }
+        }
+      }
+      o[0] = acc[0];
+      o[pl] = acc[1];
+    }
+  }
+}
+
+// true when the fused kernel applies: baby step within the register budget and the diagonal table within the
+// launch parameter block
+bool bsgs_inner_applies(uint32_t b, uint32_t giants) {
+  return b <= 16 && (size_t)b * giants <= (size_t)BSGS_MAX_TABLE;
+}
+
+void bsgs_inner(const rc_context* c, const u64* babies, const DiagTab& diag, u64* out, int count, int b, int giants,
+                int limbs, cudaStream_t s) {
+  ProfScope p("bsgs_inner", s);
+  const size_t pl = (size_t)limbs * c->N;
+  const dim3 block(32, 8), grid((unsigned)((pl + 31) / 32), (unsigned)((count + 7) / 8));
+  if (b <= 4) k_bsgs_inner<4><<<grid, block, 0, s>>>(c->d_pc, babies, diag, out, count, b, giants, limbs, c->log_n);
+  else if (b <= 8) k_bsgs_inner<8><<<grid, block, 0, s>>>(c->d_pc, babies, diag, out, count, b, giants, limbs, c->log_n);
+  else if (b <= 12) k_bsgs_inner<12><<<grid, block, 0, s>>>(c->d_pc, babies, diag, out, count, b, giants, limbs, c->log_n);
+  else k_bsgs_inner<16><<<grid, block, 0, s>>>(c->d_pc, babies, diag, out, count, b, giants, limbs, c->log_n);
+  cuda_check(cudaGetLastError(), "bsgs inner sums");
+}
+
 // stream-ordered scratch of one call
 struct Pool {
   cudaStream_t s;
@@ -417,7 +528,26 @@ extern "C" int rc_bsgs_apply_batch(rc_context* c, uint32_t count, const rc_ciphe
     // apply_giant_step_terms (234-252): inner[i][g] = sum_j mult_plain(baby_j, diag_{g,j})
     std::vector<std::vector<rc_ciphertext>> inner(count, std::vector<rc_ciphertext>(giants));
     std::vector<std::vector<bool>> present(count, std::vector<bool>(giants, false));
-    for (uint32_t i = 0; i < count; ++i) {
+    const bool fused = b == baby_step && bsgs_inner_applies(b, giants);
+    if (fused) {
+      // every inner sum of the batch in one launch, then one batched inverse NTT
+      DiagTab tab{};
+      std::vector<bool> row(giants, false);
+      for (uint32_t g = 0; g < giants; ++g)
+        for (uint32_t j = 0; j < b; ++j) {
+          tab.p[g * b + j] = diag_ntt[(size_t)g * b + j];
+          if (tab.p[g * b + j]) row[g] = true;
+        }
+      uint64_t* sums = A.pool.take(ct_words * count * giants);
+      bsgs_inner(c, babies, tab, sums, (int)count, (int)b, (int)giants, limbs, A.s);
+      ok(rc_ntt_inverse(c, sums, count * giants * 2, (uint32_t)limbs, 0, A.s));
+      for (uint32_t i = 0; i < count; ++i)
+        for (uint32_t g = 0; g < giants; ++g) {
+          inner[i][g] = rc_ciphertext{sums + ((size_t)i * giants + g) * ct_words, lv, diag_scale_bits + diag_scale_bits};
+          present[i][g] = row[g];
+        }
+    }
+    for (uint32_t i = 0; i < count && !fused; ++i) {
       for (uint32_t g = 0; g < giants; ++g) {
         std::vector<rc_ciphertext> terms;
         std::vector<const uint64_t*> plains;

@@ -393,7 +393,7 @@ def test_gpu_native_paterson_stockmeyer(A, realistic):
 
 
 @pytest.mark.gpu
-@pytest.mark.parametrize("dim", [4, 8, 16])
+@pytest.mark.parametrize("dim", [4, 8, 16, 128])
 def test_gpu_native_bsgs_equals_routine(A, realistic, dim):
     C, ctx, kp, octx, params = realistic
     rng = np.random.default_rng(100 + dim)
@@ -413,3 +413,79 @@ def test_gpu_native_bsgs_equals_routine(A, realistic, dim):
         A.apply_diagonal_linear_transform_native(ctx, cts[:1], diags, A.DiagonalTransformRotationKeys(missing))
     with pytest.raises(Exception, match="packed diagonals must match the ciphertext level"):
         A.apply_diagonal_linear_transform_native(ctx, [cts[0].drop_last_level()], diags, keys)
+
+
+@pytest.mark.gpu
+def test_gpu_bsgs_other_baby_step_matches_oracle(A, realistic):
+    """A baby step other than the crate's ceil(sqrt(d)) (the 16/8 split of a 128-wide transform, here 8/2 at
+    d = 16): the same packing rule and schedule with another b, against the oracle run with that b."""
+    C, ctx, kp, octx, params = realistic
+    dim, baby = 16, 8
+    rng = np.random.default_rng(77)
+    matrix = rng.uniform(-1, 1, (dim, dim))
+    vector = rng.uniform(-1, 1, dim)
+    ct = _encrypt(C, ctx, kp, A.repeat_real_vector_blocks(vector, ctx.num_slots()), 78)
+    steps = A.diagonal_transform_bsgs_rotation_steps(dim, baby)
+    assert steps == [1, 2, 3, 4, 5, 6, 7, 8]
+    gk, ok = _rot_keys(ctx, kp, steps, ct.level)
+    keys = A.DiagonalTransformRotationKeys(gk)
+    diags = A.pack_diagonal_plaintexts(ctx, matrix, ct.level, ct.scale_bits, baby)
+    assert (diags.baby_step, len(diags.giant_step_diagonals)) == (8, 2)
+    odiags = OA.pack_bsgs_diagonals(octx, matrix, ct.level, ct.scale_bits, baby)
+    ref = OA.apply_diagonal_linear_transform(octx, _oct(C, ct), odiags, dim, ok, baby)
+    native = A.apply_diagonal_linear_transform_native(ctx, [ct], diags, keys)[0]
+    assert _same(C, native, ref)
+    assert np.array_equal(A.apply_diagonal_linear_transform(ctx, ct, diags, keys).numpy(), native.numpy())
+    dec = ctx.decode_real_at_scale(ctx.decrypt(native, kp.secret_key), native.scale_bits)
+    assert np.max(np.abs(dec[:dim] - matrix @ vector)) <= 2e-2
+
+
+def test_bsgs_baby_step_override_validation(A):
+    assert A.diagonal_transform_bsgs_rotation_steps(128) == list(range(1, 12)) + [12 * g for g in range(1, 11)]
+    assert A.diagonal_transform_bsgs_rotation_steps(128, 16) == list(range(1, 16)) + [16 * g for g in range(1, 8)]
+    for bad in (0, 129):
+        with pytest.raises(Exception, match="BSGS baby step must be in"):
+            A.diagonal_transform_bsgs_rotation_steps(128, bad)
+
+
+@pytest.mark.gpu
+def test_gpu_native_bsgs_16_8_split_equals_routine(A, realistic):
+    """The 16/8 split of a 128-wide transform: the fused inner-sum kernel at its largest register tile against
+    the routine's per-giant multiply-accumulate (an independent code path)."""
+    C, ctx, kp, octx, params = realistic
+    rng = np.random.default_rng(128)
+    matrix = rng.standard_normal((128, 128))
+    cts = [_encrypt(C, ctx, kp, A.repeat_real_vector_blocks(rng.uniform(-1, 1, 128), ctx.num_slots()), 130 + i)
+           for i in range(2)]
+    gk, _ = _rot_keys(ctx, kp, A.diagonal_transform_bsgs_rotation_steps(128, 16), cts[0].level)
+    keys = A.DiagonalTransformRotationKeys(gk)
+    diags = A.pack_diagonal_plaintexts(ctx, matrix, cts[0].level, cts[0].scale_bits, 16)
+    got = A.apply_diagonal_linear_transform_native(ctx, cts, diags, keys)
+    want = A.apply_diagonal_linear_transform_batch(ctx, cts, diags, keys)
+    for g, w in zip(got, want):
+        assert np.array_equal(g.numpy(), w.numpy())
+
+
+@pytest.mark.gpu
+def test_gpu_native_bsgs_with_60_bit_base_prime_matches_oracle(pkg, oracle, A):
+    """A chain with a 60-bit base prime (the inner sums' per-term Barrett branch on that limb, the split
+    branch on the 41-bit scaling limbs) against the oracle."""
+    _gpu()
+    from rnsckks_gb300 import context as C
+    params = pkg.params.scheme_params(13, 4, 2, 40)
+    ctx = C.RnsCkksContext(params)
+    kp = ctx.keygen(64, C.Sampler(21))
+    octx = OA.Context(params.poly_degree, params.primes, params.aux_primes)
+    dim = 16
+    rng = np.random.default_rng(16)
+    matrix = rng.uniform(-1, 1, (dim, dim))
+    vector = rng.uniform(-1, 1, dim)
+    ct = _encrypt(C, ctx, kp, A.repeat_real_vector_blocks(vector, ctx.num_slots()), 22)
+    gk, ok = _rot_keys(ctx, kp, A.diagonal_transform_bsgs_rotation_steps(dim), ct.level)
+    diags = A.pack_diagonal_plaintexts(ctx, matrix, ct.level, ct.scale_bits)
+    out = A.apply_diagonal_linear_transform_native(ctx, [ct], diags, A.DiagonalTransformRotationKeys(gk))[0]
+    ref = OA.apply_diagonal_linear_transform(octx, _oct(C, ct), OA.pack_bsgs_diagonals(octx, matrix, ct.level,
+                                                                                      ct.scale_bits), dim, ok)
+    assert _same(C, out, ref)
+    dec = ctx.decode_real_at_scale(ctx.decrypt(out, kp.secret_key), out.scale_bits)
+    assert np.max(np.abs(dec[:dim] - matrix @ vector)) <= 1e-3
