@@ -37,8 +37,9 @@ void ok(int status) {
 // fetched from memory once per block.  On a limb whose prime is below 2^52 a residue x splits as
 // x1 * 2^26 + x0 (both < 2^26) and a product as x0 y0 + ((x0 + x1)(y0 + y1) - x0 y0 - x1 y1) 2^26 + x1 y1 2^52:
 // three 32 x 32 -> 64-bit multiply-adds per term, summed exactly in 64-bit columns (each column below
-// 16 * 2^54) and reduced once per output.  A limb with a larger prime (a 60-bit base prime) takes the
-// per-term Barrett product; a warp's 32 coefficients always share one limb, so the branch is uniform.
+// 16 * 2^54) and reduced once per output.  A limb with a larger prime (a 60-bit base prime) sums full
+// 128-bit products (one Barrett reduction per output; per term above 2^60); a block's 32 coefficients always
+// share one limb, so the branch is uniform.
 constexpr int BSGS_MAX_TABLE = 256;
 struct DiagTab {
   const u64* p[BSGS_MAX_TABLE];  // [g * b + j], null past the dimension
@@ -50,45 +51,52 @@ __device__ __forceinline__ u64 mad_wide(uint32_t a, uint32_t b, u64 acc) { retur
 
 template <int BM>
 __global__ void __launch_bounds__(256, 2) k_bsgs_inner(const PrimeConst* pc, const u64* __restrict__ babies,
-                                                    DiagTab diag, u64* __restrict__ out, int count, int b,
-                                                    int giants, int limbs, int log_n) {
+                                                       DiagTab diag, u64* __restrict__ out, int count, int b,
+                                                       int giants, int limbs, int log_n) {
+  extern __shared__ u64 dsm[];  // [giants * BM][32]: this block's 32 words of every diagonal
   const size_t pl = (size_t)limbs << log_n;
-  const size_t e = (size_t)blockIdx.x * 32 + threadIdx.x;
+  const size_t e0 = (size_t)blockIdx.x * 32, e = e0 + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
-  if (e >= pl || i >= count) return;
-  const PrimeConst& c = pc[(int)(e >> log_n)];
+  const int tid = threadIdx.y * 32 + threadIdx.x, slots = giants * BM;
+  // the block's 32 coefficients lie in one limb (N is a multiple of 32)
+  const PrimeConst& c = pc[(int)(e0 >> log_n)];
   const bool split = (c.q >> 52) == 0;
-  // babies: (x0, x1) = the 26-bit halves when split, else the 32-bit words
+  // every diagonal word of the block in flight at once (one 256-byte row per diagonal), stored as the two
+  // 26-bit halves (low word, high word) when split
+  for (int k = tid; k < slots * 32; k += 256) {
+    const int slot = k >> 5, lane = k & 31;
+    const u64 y = e0 + lane < pl ? __ldg(diag.p[slot] + e0 + lane) : 0;
+    dsm[k] = split ? ((u64)hi26(y) << 32 | lo26(y)) : y;
+  }
+  const bool active = e < pl && i < count;
+  // babies: (x0, x1) = the 26-bit halves when split, else the 32-bit words; zero past the baby step (their
+  // diagonals are the zero polynomial)
   uint32_t x0[2][BM], x1[2][BM];
 #pragma unroll
   for (int j = 0; j < BM; ++j) {
-    if (j < b) {
 #pragma unroll
-      for (int k = 0; k < 2; ++k) {
-        const u64 v = babies[(((size_t)i * b + j) * 2 + k) * pl + e];
-        x0[k][j] = split ? lo26(v) : (uint32_t)v;
-        x1[k][j] = split ? hi26(v) : (uint32_t)(v >> 32);
-      }
+    for (int k = 0; k < 2; ++k) {
+      const u64 v = active && j < b ? babies[(((size_t)i * b + j) * 2 + k) * pl + e] : 0;
+      x0[k][j] = split ? lo26(v) : (uint32_t)v;
+      x1[k][j] = split ? hi26(v) : (uint32_t)(v >> 32);
     }
   }
+  __syncthreads();
+  if (!active) return;
   for (int g = 0; g < giants; ++g) {
+    const u64* y = dsm + (size_t)g * BM * 32 + threadIdx.x;
     u64* o = out + ((size_t)i * giants + g) * 2 * pl + e;
     if (split) {
       u64 p00[2] = {0, 0}, p11[2] = {0, 0}, pk[2] = {0, 0};
 #pragma unroll
       for (int j = 0; j < BM; ++j) {
-        if (j < b) {
-          const u64* d = diag.p[g * b + j];
-          if (d) {
-            const u64 y = __ldg(d + e);
-            const uint32_t y0 = lo26(y), y1 = hi26(y), ys = y0 + y1;
+        const u64 yj = y[j * 32];
+        const uint32_t y0 = (uint32_t)yj, y1 = (uint32_t)(yj >> 32), ys = y0 + y1;
 #pragma unroll
-            for (int k = 0; k < 2; ++k) {
-              p00[k] = mad_wide(x0[k][j], y0, p00[k]);
-              p11[k] = mad_wide(x1[k][j], y1, p11[k]);
-              pk[k] = mad_wide(x0[k][j] + x1[k][j], ys, pk[k]);
-            }
-          }
+        for (int k = 0; k < 2; ++k) {
+          p00[k] = mad_wide(x0[k][j], y0, p00[k]);
+          p11[k] = mad_wide(x1[k][j], y1, p11[k]);
+          pk[k] = mad_wide(x0[k][j] + x1[k][j], ys, pk[k]);
         }
       }
 #pragma unroll
@@ -103,19 +111,25 @@ __global__ void __launch_bounds__(256, 2) k_bsgs_inner(const PrimeConst* pc, con
         t.hi += (p11[k] >> 12) + (t.lo < p_lo ? 1ull : 0ull);
         o[(size_t)k * pl] = barrett_reduce(t, c);
       }
+    } else if ((c.q >> 60) == 0) {
+      // 128-bit sums of at most 16 products, below 16 q^2 < q * 2^64: one reduction per output
+      U128 acc[2] = {{0, 0}, {0, 0}};
+#pragma unroll
+      for (int j = 0; j < BM; ++j) {
+        const u64 yj = y[j * 32];
+#pragma unroll
+        for (int k = 0; k < 2; ++k) add_to(acc[k], mul_wide((u64)x1[k][j] << 32 | x0[k][j], yj));
+      }
+      o[0] = barrett_reduce(acc[0], c);
+      o[pl] = barrett_reduce(acc[1], c);
     } else {
       u64 acc[2] = {0, 0};
 #pragma unroll
       for (int j = 0; j < BM; ++j) {
-        if (j < b) {
-          const u64* d = diag.p[g * b + j];
-          if (d) {
-            const u64 y = __ldg(d + e);
+        const u64 yj = y[j * 32];
 #pragma unroll
-            for (int k = 0; k < 2; ++k)
-              acc[k] = add_mod(acc[k], mul_mod((u64)x1[k][j] << 32 | x0[k][j], y, c), c.q);
-          }
-        }
+        for (int k = 0; k < 2; ++k)
+          acc[k] = add_mod(acc[k], mul_mod((u64)x1[k][j] << 32 | x0[k][j], yj, c), c.q);
       }
       o[0] = acc[0];
       o[pl] = acc[1];
@@ -123,21 +137,38 @@ __global__ void __launch_bounds__(256, 2) k_bsgs_inner(const PrimeConst* pc, con
   }
 }
 
-// true when the fused kernel applies: baby step within the register budget and the diagonal table within the
-// launch parameter block
-bool bsgs_inner_applies(uint32_t b, uint32_t giants) {
-  return b <= 16 && (size_t)b * giants <= (size_t)BSGS_MAX_TABLE;
+template <int BM>
+void launch_bsgs_inner(const rc_context* c, dim3 grid, dim3 block, const u64* babies, const DiagTab& diag, u64* out,
+                       int count, int b, int giants, int limbs, cudaStream_t s) {
+  const size_t smem = (size_t)giants * BM * 32 * 8;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    cudaFuncSetAttribute(k_bsgs_inner<BM>, cudaFuncAttributeMaxDynamicSharedMemorySize, BSGS_MAX_TABLE * 32 * 8);
+  });
+  k_bsgs_inner<BM><<<grid, block, smem, s>>>(c->d_pc, babies, diag, out, count, b, giants, limbs, c->log_n);
 }
 
+// register tile (babies per thread) for a baby step b <= 16
+int bsgs_tile(uint32_t b) { return b <= 4 ? 4 : b <= 8 ? 8 : b <= 12 ? 12 : 16; }
+
+// true when the fused kernel applies: baby step within the register budget and the padded diagonal table
+// within the launch parameter block
+bool bsgs_inner_applies(uint32_t b, uint32_t giants) {
+  return b <= 16 && (size_t)bsgs_tile(b) * giants <= (size_t)BSGS_MAX_TABLE;
+}
+
+// diag: [giants][bsgs_tile(b)] NTT-domain diagonals, the zero polynomial where the transform has none
 void bsgs_inner(const rc_context* c, const u64* babies, const DiagTab& diag, u64* out, int count, int b, int giants,
                 int limbs, cudaStream_t s) {
   ProfScope p("bsgs_inner", s);
   const size_t pl = (size_t)limbs * c->N;
   const dim3 block(32, 8), grid((unsigned)((pl + 31) / 32), (unsigned)((count + 7) / 8));
-  if (b <= 4) k_bsgs_inner<4><<<grid, block, 0, s>>>(c->d_pc, babies, diag, out, count, b, giants, limbs, c->log_n);
-  else if (b <= 8) k_bsgs_inner<8><<<grid, block, 0, s>>>(c->d_pc, babies, diag, out, count, b, giants, limbs, c->log_n);
-  else if (b <= 12) k_bsgs_inner<12><<<grid, block, 0, s>>>(c->d_pc, babies, diag, out, count, b, giants, limbs, c->log_n);
-  else k_bsgs_inner<16><<<grid, block, 0, s>>>(c->d_pc, babies, diag, out, count, b, giants, limbs, c->log_n);
+  switch (bsgs_tile((uint32_t)b)) {
+    case 4: launch_bsgs_inner<4>(c, grid, block, babies, diag, out, count, b, giants, limbs, s); break;
+    case 8: launch_bsgs_inner<8>(c, grid, block, babies, diag, out, count, b, giants, limbs, s); break;
+    case 12: launch_bsgs_inner<12>(c, grid, block, babies, diag, out, count, b, giants, limbs, s); break;
+    default: launch_bsgs_inner<16>(c, grid, block, babies, diag, out, count, b, giants, limbs, s);
+  }
   cuda_check(cudaGetLastError(), "bsgs inner sums");
 }
 
@@ -531,12 +562,17 @@ extern "C" int rc_bsgs_apply_batch(rc_context* c, uint32_t count, const rc_ciphe
     const bool fused = b == baby_step && bsgs_inner_applies(b, giants);
     if (fused) {
       // every inner sum of the batch in one launch, then one batched inverse NTT
+      const uint32_t tile = (uint32_t)bsgs_tile(b);
+      const size_t pl = (size_t)limbs * A.N;
+      uint64_t* zero = A.pool.take(pl);
+      cuda_check(cudaMemsetAsync(zero, 0, pl * 8, A.s), "zero diagonal");
       DiagTab tab{};
       std::vector<bool> row(giants, false);
       for (uint32_t g = 0; g < giants; ++g)
-        for (uint32_t j = 0; j < b; ++j) {
-          tab.p[g * b + j] = diag_ntt[(size_t)g * b + j];
-          if (tab.p[g * b + j]) row[g] = true;
+        for (uint32_t j = 0; j < tile; ++j) {
+          const uint64_t* d = j < b ? diag_ntt[(size_t)g * b + j] : nullptr;
+          tab.p[g * tile + j] = d ? d : zero;
+          if (d) row[g] = true;
         }
       uint64_t* sums = A.pool.take(ct_words * count * giants);
       bsgs_inner(c, babies, tab, sums, (int)count, (int)b, (int)giants, limbs, A.s);

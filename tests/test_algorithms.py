@@ -489,3 +489,25 @@ def test_gpu_native_bsgs_with_60_bit_base_prime_matches_oracle(pkg, oracle, A):
     assert _same(C, out, ref)
     dec = ctx.decode_real_at_scale(ctx.decrypt(out, kp.secret_key), out.scale_bits)
     assert np.max(np.abs(dec[:dim] - matrix @ vector)) <= 1e-3
+
+
+@pytest.mark.gpu
+def test_gpu_native_bsgs_with_61_bit_primes_equals_routine(pkg, A):
+    """Primes in [2^60, 2^61): the inner sums' per-term reduction branch, against the routine's multiply-
+    accumulate."""
+    _gpu()
+    from rnsckks_gb300 import context as C
+    params = pkg.params.hybrid_params(13, 3, 2, 61, 40)
+    assert all(p.modulus >> 60 == 1 for p in params.primes)
+    ctx = C.RnsCkksContext(params)
+    kp = ctx.keygen(64, C.Sampler(31))
+    dim = 8
+    rng = np.random.default_rng(8)
+    matrix = rng.uniform(-1, 1, (dim, dim))
+    ct = _encrypt(C, ctx, kp, A.repeat_real_vector_blocks(rng.uniform(-1, 1, dim), ctx.num_slots()), 32)
+    gk, _ = _rot_keys(ctx, kp, A.diagonal_transform_bsgs_rotation_steps(dim), ct.level)
+    keys = A.DiagonalTransformRotationKeys(gk)
+    diags = A.pack_diagonal_plaintexts(ctx, matrix, ct.level, ct.scale_bits)
+    got = A.apply_diagonal_linear_transform_native(ctx, [ct], diags, keys)[0]
+    want = A.apply_diagonal_linear_transform(ctx, ct, diags, keys)
+    assert np.array_equal(got.numpy(), want.numpy())
