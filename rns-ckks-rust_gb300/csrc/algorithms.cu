@@ -38,8 +38,8 @@ void ok(int status) {
 // x1 * 2^26 + x0 (both < 2^26) and a product as x0 y0 + ((x0 + x1)(y0 + y1) - x0 y0 - x1 y1) 2^26 + x1 y1 2^52:
 // three 32 x 32 -> 64-bit multiply-adds per term, summed exactly in 64-bit columns (each column below
 // 16 * 2^54) and reduced once per output.  A limb with a larger prime (a 60-bit base prime) sums full
-// 128-bit products (one Barrett reduction per output; per term above 2^60); a block's 32 coefficients always
-// share one limb, so the branch is uniform.
+// 128-bit products (one Barrett reduction per output; per term above 2^60); a block's 32 coefficients
+// share one limb for N >= 32, so the branch is uniform there.
 constexpr int BSGS_MAX_TABLE = 256;
 struct DiagTab {
   const u64* p[BSGS_MAX_TABLE];  // [g * b + j], null past the dimension
@@ -58,17 +58,19 @@ __global__ void __launch_bounds__(256, 2) k_bsgs_inner(const PrimeConst* pc, con
   const size_t e0 = (size_t)blockIdx.x * 32, e = e0 + threadIdx.x;
   const int i = blockIdx.y * blockDim.y + threadIdx.y;
   const int tid = threadIdx.y * 32 + threadIdx.x, slots = giants * BM;
-  // the block's 32 coefficients lie in one limb (N is a multiple of 32)
-  const PrimeConst& c = pc[(int)(e0 >> log_n)];
-  const bool split = (c.q >> 52) == 0;
   // every diagonal word of the block in flight at once (one 256-byte row per diagonal), stored as the two
-  // 26-bit halves (low word, high word) when split
+  // 26-bit halves (low word, high word) when the word's prime is split (a block's 32 coefficients share one
+  // limb unless N < 32)
   for (int k = tid; k < slots * 32; k += 256) {
     const int slot = k >> 5, lane = k & 31;
-    const u64 y = e0 + lane < pl ? __ldg(diag.p[slot] + e0 + lane) : 0;
-    dsm[k] = split ? ((u64)hi26(y) << 32 | lo26(y)) : y;
+    const size_t ek = e0 + lane;
+    const u64 y = ek < pl ? __ldg(diag.p[slot] + ek) : 0;
+    const bool sk = ek < pl && (pc[(int)(ek >> log_n)].q >> 52) == 0;
+    dsm[k] = sk ? ((u64)hi26(y) << 32 | lo26(y)) : y;
   }
   const bool active = e < pl && i < count;
+  const PrimeConst& c = pc[(int)((active ? e : e0) >> log_n)];
+  const bool split = (c.q >> 52) == 0;
   // babies: (x0, x1) = the 26-bit halves when split, else the 32-bit words; zero past the baby step (their
   // diagonals are the zero polynomial)
   uint32_t x0[2][BM], x1[2][BM];
