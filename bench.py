@@ -965,7 +965,17 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the NTT microbenchmark and the mixed-level relinearization batch")
+    ap.add_argument("--extra-only", choices=["bsgs_matvec", "bootstrap"],
+                    help="run one of the extra workloads alone (a profiling case) and print its JSON object")
+    ap.add_argument("--extra-batch", type=int, default=None, help="batch of --extra-only (default: its own)")
     args = ap.parse_args()
+    if args.extra_only:
+        pkg = load_package()
+        from rnsckks_gb300 import context as C
+        fn = {"bsgs_matvec": bsgs_matvec_bench, "bootstrap": bootstrap_bench}[args.extra_only]
+        kw = {} if args.extra_batch is None else {"batch": args.extra_batch}
+        print(json.dumps({args.extra_only: fn(pkg, C, args.seed, **kw)}), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args)
     else:
