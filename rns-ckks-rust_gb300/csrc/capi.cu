@@ -288,6 +288,7 @@ void wide_ks_finish(rc_context* c, const WideKs& w, const std::vector<KsJob>& jo
   f.add_g_inv = g_inv;
   f.wide = 1;
   f.wt = c->wide;
+  f.lazy = c->lazy ? 1 : 0;
   PtrTab add{}, out{};
   for (int j = 0; j < n; ++j) {
     add.p[2 * j] = const_cast<uint64_t*>(jobs[b0 + j].add0);
@@ -347,6 +348,7 @@ void keyswitch_core(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, u
   f.add_g_inv = g_inv;
   f.wide = 0;
   f.wt = c->wide;
+  f.lazy = 0;
   PtrTab add{}, out{};
   for (int j = 0; j < J; ++j) {
     add.p[2 * j] = const_cast<uint64_t*>(jobs[j].add0);

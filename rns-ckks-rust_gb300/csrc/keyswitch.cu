@@ -512,6 +512,10 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
   // yields S * P^-1, the P-part conversion (M_k P^-1) and its sign correction (P P^-1 = 1) match it, and
   // ModDown's own multiply by P^-1 disappears
   const bool fold = f.wide && K > 0;
+  // lazy wide path: each Q limb's terms are summed unreduced and reduced once, so its subtracted constants
+  // are staged negated: q - A F (added when S < 0) and q - M_k F with Shoup companion ~(M_k F)_s (for
+  // 0 < w < q, floor((q - w) 2^64 / q) = 2^64 - 1 - floor(w 2^64 / q))
+  const bool fast = f.wide && f.lazy;
   for (int e = threadIdx.x; e < (lq + K) * st; e += blockDim.x) {
     const int i = e / st, fld = e - i * st;
     const int t = fmap.prime(i);
@@ -535,6 +539,20 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
         const int k = fld - FT_N;
         if (q_limb && k < K) v = fq ? f.wt.mkp[(size_t)i * K + k] : f.md.mk[(size_t)i * K + k];
         else if (q_limb) v = fq ? f.wt.mkp_s[(size_t)i * K + (k - K)] : f.md.mk_s[(size_t)i * K + (k - K)];
+      }
+    }
+    if (fast) {
+      const u64 q = f.pc[t].q;
+      if (q_limb && fld == FT_AMOD) v = v ? q - v : 0;  // the aux limbs' Garner keeps A F
+      if (q_limb && fld >= FT_N && fld < FT_N + K) {
+        const int k = fld - FT_N;
+        const u64 w = fq ? f.wt.mkp[(size_t)i * K + k] : f.md.mk[(size_t)i * K + k];
+        v = w ? q - w : 0;
+      }
+      if (q_limb && fld >= FT_N + K) {
+        const int k = fld - FT_N - K;
+        const u64 w = fq ? f.wt.mkp[(size_t)i * K + k] : f.md.mk[(size_t)i * K + k];
+        v = w ? ~v : 0;
       }
     }
     tab[e] = v;
@@ -613,8 +631,8 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
     pneg = res > 0;
   }
 
-  // one limb's inputs (wide products and addend) and the value computed from them; the rescale loop below
-  // requests limb i+1's inputs before computing limb i, so each thread has two limbs' loads in flight
+  // one limb's inputs (wide products and addend) and the value computed from them; the limb loops below
+  // request limb i+2's inputs before computing limb i, so each thread has several limbs' loads in flight
   struct LimbIn {
     uint2 p01, p23;
     u64 av;
@@ -626,6 +644,57 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
     r.av = add ? add[(size_t)j * N + addsrc] : 0;
     return r;
   };
+
+  if (fast) {
+    // S F + [S < 0] (q - A F) + sum_k v_k (q - M_k F) + [X_P > P/2] P F + addend (+ the rescale term), each
+    // below 2q or q: at most (8 + 2K) q < 2^63, reduced once by the final Shoup product
+    auto lazy_value = [&](int i, const LimbIn& in) -> u64 {
+      const u64 q = T(i, FT_Q);
+      u64 s = wide_crt_lazy(in.p01, in.p23, f.wt, q, T(i, FT_LO), T(i, FT_LO_S), T(i, FT_C01), T(i, FT_C01_S),
+                            T(i, FT_AMOD));
+#pragma unroll
+      for (int k = 0; k < KMAX; ++k)
+        if (k < K) s += mul_shoup_lazy(v[k], T(i, FT_N + k), T(i, FT_N + K + k), q);
+      if (pneg) s += T(i, FT_PMOD);
+      if (add) s += (addneg && in.av) ? q - in.av : in.av;
+      return s;
+    };
+    if (!f.rescale) {
+      LimbIn cur = load(0), nxt;
+      if (lq > 1) nxt = load(1);
+#pragma unroll 1
+      for (int i = 0; i < lq; ++i) {
+        LimbIn far;
+        if (i + 2 < lq) far = load(i + 2);
+        const u64 q = T(i, FT_Q);
+        dst[(size_t)i * N + x] = reduce_2q(mul_shoup_lazy(lazy_value(i, cur), 1, T(i, FT_ONE_S), q), q);
+        cur = nxt;
+        nxt = far;
+      }
+      return;
+    }
+    const int last = lq - 1;
+    const u64 ql = T(last, FT_Q), half = ql >> 1;
+    const u64 vl = reduce_2q(mul_shoup_lazy(lazy_value(last, load(last)), 1, T(last, FT_ONE_S), ql), ql);
+    const bool pos = vl <= half;
+    const u64 dist = pos ? vl : ql - vl;
+    if (last == 0) return;
+    LimbIn cur = load(0), nxt;
+    if (last > 1) nxt = load(1);
+#pragma unroll 1
+    for (int i = 0; i < last; ++i) {
+      LimbIn far;
+      if (i + 2 < last) far = load(i + 2);
+      const u64 q = T(i, FT_Q);
+      // (value - centred last limb) * q_last^-1: the centred value's negation enters the sum lazily
+      const u64 d = dist < q ? dist : mul_shoup(dist, 1, T(i, FT_ONE_S), q);
+      const u64 s = lazy_value(i, cur) + (pos ? q - d : d);
+      dst[(size_t)i * N + x] = reduce_2q(mul_shoup_lazy(s, T(i, FT_RINV), T(i, FT_RINV_S), q), q);
+      cur = nxt;
+      nxt = far;
+    }
+    return;
+  }
   auto finish_value = [&](int i, u64 val, u64 av) -> u64 {
     const u64 q = T(i, FT_Q);
     if (K > 0) {

@@ -42,6 +42,24 @@ __device__ __forceinline__ u64 wide_crt_mod_c(uint2 p01, uint2 p23, const WideTa
   return r;
 }
 
+// wide_crt_mod_c before its reduction, for a caller that sums further lazy terms: a value below 5q congruent
+// to S * F mod q, where namod = (q - (A F mod q)) mod q is what a negative S adds
+__device__ __forceinline__ u64 wide_crt_lazy(uint2 p01, uint2 p23, const WideTab& W, u64 q, u64 lo_w, u64 lo_ws,
+                                            u64 c01, u64 c01_s, u64 namod) {
+  const uint32_t w1 = W.w[1], w2 = W.w[2], w3 = W.w[3];
+  const uint32_t v0 = p01.x;
+  const uint32_t v1 = mul_shoup32(sub32(p01.y, fold32(v0, w1), w1), W.g01, W.g01s, w1);
+  uint32_t a = mul_shoup32(sub32(p23.x, fold32(v0, w2), w2), W.g02, W.g02s, w2);
+  const uint32_t v2 = mul_shoup32(sub32(a, fold32(v1, w2), w2), W.g12, W.g12s, w2);
+  uint32_t b = mul_shoup32(sub32(p23.y, fold32(v0, w3), w3), W.g03, W.g03s, w3);
+  b = mul_shoup32(sub32(b, fold32(v1, w3), w3), W.g13, W.g13s, w3);
+  const uint32_t v3 = mul_shoup32(sub32(b, fold32(v2, w3), w3), W.g23, W.g23s, w3);
+  const u64 lo = (u64)v0 + (u64)W.w[0] * v1;
+  const u64 hi = (u64)v2 + (u64)w2 * v3;
+  u64 r = mul_shoup_lazy(lo, lo_w, lo_ws, q) + mul_shoup_lazy(hi, c01, c01_s, q);
+  return v3 >= W.half3 ? r + namod : r;
+}
+
 // Centred S from (S mod w0, S mod w1) = p01 and (S mod w2, S mod w3) = p23,
 // reduced mod the scheme prime t.  Garner: S = v0 + w0 v1 + w0 w1 v2 + w0 w1 w2 v3
 // with v_i < w_i; with |S| < A/4 the sign of the centred value is v3 >= (w3+1)/2.
