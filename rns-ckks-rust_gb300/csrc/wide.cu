@@ -105,12 +105,17 @@ __global__ __launch_bounds__(256, 2) void k_w_cols_fwd(WidePrimes w, const void*
   }
 }
 
-// Forward row phase of data[poly][pair][N] (poly = p0 + blockIdx.z), outputs
-// reduced to [0, q).  TILED: written as dtt[job][pair][x/32][digit][32] with
-// poly = job * D + digit; otherwise in place.
+// Row kernels: a block transforms the same ROWS rows of W_ROW_POLYS consecutive polynomials, so each row's
+// twiddles (as many bytes as two rows of data) are staged once for all of them; the next polynomial's rows
+// are loaded while the current one is transformed.
+constexpr int W_ROW_POLYS = 4;
+
+// Forward row phase of data[poly][pair][N] (polys p0 + blockIdx.z * W_ROW_POLYS .. below p0 + cnt), outputs
+// reduced to [0, q).  TILED: written as dtt[job][pair][x/32][digit][32] with poly = job * D + digit;
+// otherwise in place.
 template <int M1, int M2, bool TILED>
 __global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_fwd(WidePrimes w, uint2* data, uint2* dtt, int p0,
-                                                                 int D) {
+                                                                 int cnt, int D) {
   using G = core::Geo<M2>;
   constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = W_ROW_WARPS * G::SUBS;
   __shared__ uint2 bufs[ROWS * G::STRIDE];
@@ -119,38 +124,55 @@ __global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_fwd(WidePrimes w, u
   const int sub = lane / G::LANES, l = lane % G::LANES;
   const int row0 = blockIdx.x * ROWS;
   const int pair = blockIdx.y;
-  const size_t poly = (size_t)p0 + blockIdx.z;
+  const int first = blockIdx.z * W_ROW_POLYS, count = min(W_ROW_POLYS, cnt - first);
   const uint32_t q0 = pick(w.q, pair, 0), q1 = pick(w.q, pair, 1);
   const Tw2* twg = w.tw_fwd + (size_t)pair * N;
   const int rl = warp * G::SUBS + sub, row = row0 + rl;
-  uint2* in = data + (poly * 2 + pair) * N + (size_t)row * N2;
+  auto row_ptr = [&](int t) { return data + (((size_t)p0 + first + t) * 2 + pair) * N + (size_t)row * N2; };
   uint2* buf = bufs + rl * G::STRIDE;
-  uint2 v[8];  // requested before the twiddle tables, so both latencies overlap
+  uint2 v[8], vn[8];  // requested before the twiddle tables, so both latencies overlap
+  {
+    const uint2* in = row_ptr(0);
 #pragma unroll
-  for (int k = 0; k < 8; ++k) v[k] = in[core::first_idx<M2>(l, k)];
+    for (int k = 0; k < 8; ++k) v[k] = in[core::first_idx<M2>(l, k)];
+  }
 #pragma unroll 1
   for (int rr = 0; rr < ROWS; ++rr)
     core::stage_twiddles_async<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * W_ROW_WARPS);
   core::cp_async_wait_all();
   __syncthreads();
-  core::fwd_sub2<M2>(v, buf, l, twl[rl], q0, q1);
-  if (TILED) {
-    const size_t job = poly / D, digit = poly % D;
-    uint2* o = dtt + (job * 2 + pair) * (N / 32) * (size_t)(D * 32) + digit * 32;
+#pragma unroll 1
+  for (int t = 0; t < count; ++t) {
+    if (t + 1 < count) {
+      const uint2* in = row_ptr(t + 1);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      const int x = row * N2 + core::last_idx<M2>(l, k);
-      o[(size_t)(x >> 5) * (D * 32) + (x & 31)] = reduce4(v[k], q0, q1);
+      for (int k = 0; k < 8; ++k) vn[k] = in[core::first_idx<M2>(l, k)];
     }
-  } else {
+    core::fwd_sub2<M2>(v, buf, l, twl[rl], q0, q1);
+    const size_t poly = (size_t)p0 + first + t;
+    if (TILED) {
+      const size_t job = poly / D, digit = poly % D;
+      uint2* o = dtt + (job * 2 + pair) * (N / 32) * (size_t)(D * 32) + digit * 32;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) in[core::last_idx<M2>(l, k)] = reduce4(v[k], q0, q1);
+      for (int k = 0; k < 8; ++k) {
+        const int x = row * N2 + core::last_idx<M2>(l, k);
+        o[(size_t)(x >> 5) * (D * 32) + (x & 31)] = reduce4(v[k], q0, q1);
+      }
+    } else {
+      uint2* out = row_ptr(t);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) out[core::last_idx<M2>(l, k)] = reduce4(v[k], q0, q1);
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = vn[k];
+    __syncwarp();  // the warp's buffer is reused by the next polynomial
   }
 }
 
-// Inverse row phase, in place on data[poly][pair][N]; inputs in [0, 2q).
+// Inverse row phase, in place on data[poly][pair][N] (polys blockIdx.z * W_ROW_POLYS .. below cnt); inputs in
+// [0, 2q).
 template <int M1, int M2>
-__global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_inv(WidePrimes w, uint2* data) {
+__global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_inv(WidePrimes w, uint2* data, int cnt) {
   using G = core::Geo<M2>;
   constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = W_ROW_WARPS * G::SUBS;
   __shared__ uint2 bufs[ROWS * G::STRIDE];
@@ -159,23 +181,38 @@ __global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_inv(WidePrimes w, u
   const int sub = lane / G::LANES, l = lane % G::LANES;
   const int row0 = blockIdx.x * ROWS;
   const int pair = blockIdx.y;
-  const size_t poly = blockIdx.z;
+  const int first = blockIdx.z * W_ROW_POLYS, count = min(W_ROW_POLYS, cnt - first);
   const uint32_t q0 = pick(w.q, pair, 0), q1 = pick(w.q, pair, 1);
   const Tw2* twg = w.tw_inv + (size_t)pair * N;
   const int rl = warp * G::SUBS + sub, row = row0 + rl;
-  uint2* in = data + (poly * 2 + pair) * N + (size_t)row * N2;
+  auto row_ptr = [&](int t) { return data + (((size_t)first + t) * 2 + pair) * N + (size_t)row * N2; };
   uint2* buf = bufs + rl * G::STRIDE;
-  uint2 v[8];  // requested before the twiddle tables, so both latencies overlap
+  uint2 v[8], vn[8];  // requested before the twiddle tables, so both latencies overlap
+  {
+    const uint2* in = row_ptr(0);
 #pragma unroll
-  for (int k = 0; k < 8; ++k) v[k] = in[core::last_idx<M2>(l, k)];
+    for (int k = 0; k < 8; ++k) v[k] = in[core::last_idx<M2>(l, k)];
+  }
 #pragma unroll 1
   for (int rr = 0; rr < ROWS; ++rr)
     core::stage_twiddles_async<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * W_ROW_WARPS);
   core::cp_async_wait_all();
   __syncthreads();
-  core::inv_sub2<M2>(v, buf, l, twl[rl], q0, q1);
+#pragma unroll 1
+  for (int t = 0; t < count; ++t) {
+    if (t + 1 < count) {
+      const uint2* in = row_ptr(t + 1);
 #pragma unroll
-  for (int k = 0; k < 8; ++k) in[core::first_idx<M2>(l, k)] = v[k];
+      for (int k = 0; k < 8; ++k) vn[k] = in[core::last_idx<M2>(l, k)];
+    }
+    core::inv_sub2<M2>(v, buf, l, twl[rl], q0, q1);
+    uint2* out = row_ptr(t);
+#pragma unroll
+    for (int k = 0; k < 8; ++k) out[core::first_idx<M2>(l, k)] = v[k];
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = vn[k];
+    __syncwarp();  // the warp's buffer is reused by the next polynomial
+  }
 }
 
 // Inverse column phase, in place, times N^-1: outputs in [0, q).
@@ -407,8 +444,9 @@ void w_forward(const WidePrimes& w, const void* src, uint2* work, uint2* dtt, in
   for (int p0 = 0; p0 < polys; p0 += 65535) {
     const int cnt = polys - p0 < 65535 ? polys - p0 : 65535;
     k_w_cols_fwd<M1, M2, SRC><<<dim3(N2 / WColTile<M1>::COLS, 2, cnt), 256, 0, s>>>(w, src, work, p0);
-    k_w_rows_fwd<M1, M2, TILED>
-        <<<dim3(N1 / (W_ROW_WARPS * core::Geo<M2>::SUBS), 2, cnt), 32 * W_ROW_WARPS, 0, s>>>(w, work, dtt, p0, D);
+    k_w_rows_fwd<M1, M2, TILED><<<dim3(N1 / (W_ROW_WARPS * core::Geo<M2>::SUBS), 2,
+                                       (cnt + W_ROW_POLYS - 1) / W_ROW_POLYS),
+                                  32 * W_ROW_WARPS, 0, s>>>(w, work, dtt, p0, cnt, D);
   }
 }
 
@@ -433,8 +471,9 @@ void w_inverse(const WidePrimes& w, uint2* data, int polys, cudaStream_t s) {
     uint2* d = data + (size_t)p0 * 2 * (N1 * N2);
     {
       ProfScope p("wide_inv_rows", s);
-      k_w_rows_inv<M1, M2>
-          <<<dim3(N1 / (W_ROW_WARPS * core::Geo<M2>::SUBS), 2, cnt), 32 * W_ROW_WARPS, 0, s>>>(w, d);
+      k_w_rows_inv<M1, M2><<<dim3(N1 / (W_ROW_WARPS * core::Geo<M2>::SUBS), 2,
+                                  (cnt + W_ROW_POLYS - 1) / W_ROW_POLYS),
+                             32 * W_ROW_WARPS, 0, s>>>(w, d, cnt);
     }
     {
       ProfScope p("wide_inv_cols", s);
