@@ -256,11 +256,16 @@ __global__ __launch_bounds__(256, 2) void k_cols_f(NttArgs a, PtrTab src, PtrTab
 }
 
 constexpr int ROW_WARPS = 4;
+// polynomials per row block: the same rows (and limb) of ROW_POLYS polynomials share one staging of the rows'
+// twiddles, which take as many bytes as two rows of data
+constexpr int ROW_POLYS = 4;
 
-// Row phase: each warp transforms SUBS rows of 2^M2 contiguous residues; the
-// CTA stages the rows' twiddle tables in shared memory.
+// Row phase: each warp transforms SUBS rows of 2^M2 contiguous residues of polynomials
+// blockIdx.z * ROW_POLYS .. below `polys`, loading the next polynomial's rows while transforming the current
+// one; the CTA stages the rows' twiddle tables in shared memory once.
 template <int M1, int M2, bool LAZY, bool FWD>
-__global__ __launch_bounds__(32 * ROW_WARPS) void k_rows_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
+__global__ __launch_bounds__(32 * ROW_WARPS) void k_rows_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map,
+                                                           int polys) {
   using G = core::Geo<M2>;
   constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = ROW_WARPS * G::SUBS;
   __shared__ u64 bufs[ROWS * G::STRIDE];
@@ -268,31 +273,45 @@ __global__ __launch_bounds__(32 * ROW_WARPS) void k_rows_f(NttArgs a, PtrTab src
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sub = lane / G::LANES, l = lane % G::LANES;
   const int row0 = blockIdx.x * ROWS;
-  const int limb = blockIdx.y, poly = blockIdx.z;
+  const int limb = blockIdx.y, first = blockIdx.z * ROW_POLYS, count = min(ROW_POLYS, polys - first);
   const int prime = map.prime(limb);
   const PrimeConst& pc = a.pc[prime];
   const Twiddle* twg = (FWD ? a.tw_fwd : a.tw_inv) + (size_t)prime * N;
   const int rl = warp * G::SUBS + sub, row = row0 + rl;
-  const u64* in = src.p[poly] + (size_t)limb * N + (size_t)row * N2;
-  u64* out = dst.p[poly] + (size_t)limb * N + (size_t)row * N2;
+  const size_t off = (size_t)limb * N + (size_t)row * N2;
   u64* buf = bufs + rl * G::STRIDE;
-  // the row's values are requested before the twiddle tables, so both latencies overlap
-  u64 v[8];
+  // the first polynomial's values are requested before the twiddle tables, so both latencies overlap
+  u64 v[8], vn[8];
+  {
+    const u64* in = src.p[first] + off;
 #pragma unroll
-  for (int k = 0; k < 8; ++k) v[k] = in[FWD ? core::first_idx<M2>(l, k) : core::last_idx<M2>(l, k)];
+    for (int k = 0; k < 8; ++k) v[k] = in[FWD ? core::first_idx<M2>(l, k) : core::last_idx<M2>(l, k)];
+  }
 #pragma unroll 1
   for (int rr = 0; rr < ROWS; ++rr)
     core::stage_twiddles_async<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * ROW_WARPS);
   core::cp_async_wait_all();
   __syncthreads();
-  if (FWD) {
-    core::fwd_sub<M2, LAZY>(v, buf, l, twl[rl], pc.q);
+#pragma unroll 1
+  for (int t = 0; t < count; ++t) {
+    if (t + 1 < count) {
+      const u64* in = src.p[first + t + 1] + off;
 #pragma unroll
-    for (int k = 0; k < 8; ++k) out[core::last_idx<M2>(l, k)] = reduce_out<LAZY>(v[k], pc);
-  } else {
-    core::inv_sub<M2>(v, buf, l, twl[rl], pc.q);
+      for (int k = 0; k < 8; ++k) vn[k] = in[FWD ? core::first_idx<M2>(l, k) : core::last_idx<M2>(l, k)];
+    }
+    u64* out = dst.p[first + t] + off;
+    if (FWD) {
+      core::fwd_sub<M2, LAZY>(v, buf, l, twl[rl], pc.q);
 #pragma unroll
-    for (int k = 0; k < 8; ++k) out[core::first_idx<M2>(l, k)] = v[k];
+      for (int k = 0; k < 8; ++k) out[core::last_idx<M2>(l, k)] = reduce_out<LAZY>(v[k], pc);
+    } else {
+      core::inv_sub<M2>(v, buf, l, twl[rl], pc.q);
+#pragma unroll
+      for (int k = 0; k < 8; ++k) out[core::first_idx<M2>(l, k)] = v[k];
+    }
+#pragma unroll
+    for (int k = 0; k < 8; ++k) v[k] = vn[k];
+    __syncwarp();  // the warp's buffer is reused by the next polynomial
   }
 }
 
@@ -300,14 +319,15 @@ template <int M1, int M2, bool LAZY>
 void fwd_fast(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
               cudaStream_t s) {
   constexpr int N2 = 1 << M2, N1 = 1 << M1;
-  dim3 g1(N2 / ColTile<M1>::COLS, limbs, polys), g2(N1 / (ROW_WARPS * core::Geo<M2>::SUBS), limbs, polys);
+  dim3 g1(N2 / ColTile<M1>::COLS, limbs, polys),
+      g2(N1 / (ROW_WARPS * core::Geo<M2>::SUBS), limbs, (polys + ROW_POLYS - 1) / ROW_POLYS);
   {
     ProfScope p("ntt_fwd_cols", s);
     k_cols_f<M1, M2, LAZY, true><<<g1, 256, 0, s>>>(a, src, dst, map);
   }
   {
     ProfScope p("ntt_fwd_rows", s);
-    k_rows_f<M1, M2, LAZY, true><<<g2, 32 * ROW_WARPS, 0, s>>>(a, dst, dst, map);
+    k_rows_f<M1, M2, LAZY, true><<<g2, 32 * ROW_WARPS, 0, s>>>(a, dst, dst, map, polys);
   }
 }
 
@@ -315,10 +335,11 @@ template <int M1, int M2>
 void inv_fast(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
               cudaStream_t s) {
   constexpr int N2 = 1 << M2, N1 = 1 << M1;
-  dim3 g1(N2 / ColTile<M1>::COLS, limbs, polys), g2(N1 / (ROW_WARPS * core::Geo<M2>::SUBS), limbs, polys);
+  dim3 g1(N2 / ColTile<M1>::COLS, limbs, polys),
+      g2(N1 / (ROW_WARPS * core::Geo<M2>::SUBS), limbs, (polys + ROW_POLYS - 1) / ROW_POLYS);
   {
     ProfScope p("ntt_inv_rows", s);
-    k_rows_f<M1, M2, false, false><<<g2, 32 * ROW_WARPS, 0, s>>>(a, src, dst, map);
+    k_rows_f<M1, M2, false, false><<<g2, 32 * ROW_WARPS, 0, s>>>(a, src, dst, map, polys);
   }
   {
     ProfScope p("ntt_inv_cols", s);
