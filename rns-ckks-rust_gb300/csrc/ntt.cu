@@ -200,7 +200,7 @@ __device__ __forceinline__ u64 reduce_out(u64 x, const PrimeConst& c) {
 // column twiddle table in shared memory; each warp transforms SUBS columns at
 // a time in registers.
 template <int M1, int M2, bool LAZY, bool FWD>
-__global__ __launch_bounds__(256, 2) void k_cols_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
+__global__ __launch_bounds__(256, 3) void k_cols_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
   using G = core::Geo<M1>;
   constexpr int COLS = ColTile<M1>::COLS, N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2;
   __shared__ u64 tile[COLS * G::STRIDE];

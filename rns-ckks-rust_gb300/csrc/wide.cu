@@ -217,7 +217,7 @@ __global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_inv(WidePrimes w, u
 
 // Inverse column phase, in place, times N^-1: outputs in [0, q).
 template <int M1, int M2>
-__global__ __launch_bounds__(256, 2) void k_w_cols_inv(WidePrimes w, uint2* data) {
+__global__ __launch_bounds__(256, 3) void k_w_cols_inv(WidePrimes w, uint2* data) {
   using G = core::Geo<M1>;
   constexpr int COLS = WColTile<M1>::COLS, N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2;
   __shared__ uint2 tile[COLS * G::STRIDE];
