@@ -664,10 +664,12 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
       for (int i = 0; i < l; ++i) blob.push_back(shoup_h(blob[o_qinv + i], qm[i]));
       size_t o_invq = blob.size();
       for (int i = 0; i < l; ++i) {
-        double d = 1.0 / (double)qm[i];
-        uint64_t bits;
-        memcpy(&bits, &d, 8);
-        blob.push_back(bits);
+        int bits = 0;
+        while (bits < 64 && (qm[i] >> bits)) ++bits;
+        const uint32_t n = (uint32_t)(64 - bits);
+        const unsigned __int128 qn = (unsigned __int128)(qm[i] << n);
+        const uint64_t r = (uint64_t)((((unsigned __int128)1) << 95) / qn);  // < 2^32: qn > 2^63
+        blob.push_back(((uint64_t)n << 32) | r);
       }
       size_t o_Q = blob.size();
       auto qw = Q.words(W);
@@ -690,7 +692,7 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
       li.dt.qhat = d;
       li.dt.qhat_inv = d + o_qinv;
       li.dt.qhat_inv_s = d + o_qinv_s;
-      li.dt.inv_q = (const double*)(d + o_invq);
+      li.dt.inv_q = d + o_invq;
       li.dt.Q = d + o_Q;
       li.dt.halfQ = d + o_hQ;
       li.dt.lift_pw = pm.empty() ? nullptr : d + o_pw;

@@ -11,7 +11,7 @@ namespace rc {
 // Q, floor(Q/2)), staged in shared memory by all threads of the block; the caller synchronises.
 struct CrtSmem {
   const u64 *qhat, *q, *hinv, *hinv_s;
-  const double* invq;
+  const u64* invq;  // fixed-point 1/q_l (DecompTab::inv_q)
   const u64 *Q, *half;
 };
 
@@ -22,8 +22,8 @@ __device__ __forceinline__ CrtSmem stage_crt_tables(const PrimeConst* pc, const 
   u64* s_q = s_qhat + (size_t)limbs * W;       // [limbs]
   u64* s_hinv = s_q + limbs;                   // [limbs]
   u64* s_hinv_s = s_hinv + limbs;              // [limbs]
-  double* s_invq = reinterpret_cast<double*>(s_hinv_s + limbs);  // [limbs]
-  u64* s_Q = reinterpret_cast<u64*>(s_invq + limbs);  // [W]
+  u64* s_invq = s_hinv_s + limbs;              // [limbs]
+  u64* s_Q = s_invq + limbs;                   // [W]
   u64* s_half = s_Q + W;                       // [W]
   for (int e = threadIdx.x; e < limbs * W; e += blockDim.x) s_qhat[e] = dt.qhat[e];
   for (int e = threadIdx.x; e < limbs; e += blockDim.x) {
@@ -50,13 +50,14 @@ __device__ __forceinline__ u64 centred_crt(const CrtSmem& t, int W, int limbs, c
                                            u64 (&X)[WM]) {
 #pragma unroll
   for (int w = 0; w < WM; ++w) X[w] = 0;
-  double kf = 0.0;
+  u64 fsum = 0;  // sum of y_l / q_l in units of 2^-31 (each term within 3 units below its value)
   for (int l = 0; l < limbs; ++l) {
     const u64 q = t.q[l];
     u64 r = in[(u64)l * N];
     if (neg && r) r = q - r;
     const u64 y = mul_shoup(r, t.hinv[l], t.hinv_s[l], q);
-    kf += (double)y * t.invq[l];
+    const u64 fx = t.invq[l];
+    fsum += __umulhi((uint32_t)((y << (uint32_t)(fx >> 32)) >> 32), (uint32_t)fx);
     const u64* qh = t.qhat + (size_t)l * W;
     u64 carry = 0;
 #pragma unroll
@@ -75,7 +76,7 @@ __device__ __forceinline__ u64 centred_crt(const CrtSmem& t, int W, int limbs, c
   // X' = X - k*Q with k = floor(sum y_i / q_i) (exact up to +-1, fixed below).  `top` follows the
   // word W-1 as each pass writes it: reading X[W-1] afterwards would index X dynamically and move it to
   // local memory.
-  u64 k = (u64)kf;
+  u64 k = fsum >> 31;
   u64 top = 0;
   {
     u64 borrow = 0, carry = 0;

@@ -97,7 +97,7 @@ struct DecompTab {
   const u64* qhat;       // [limbs][W] words of Q/q_i
   const u64* qhat_inv;   // [limbs] (Q/q_i)^-1 mod q_i
   const u64* qhat_inv_s; // Shoup companions
-  const double* inv_q;   // [limbs] 1/q_i
+  const u64* inv_q;      // [limbs] 1/q_i in fixed point: (n << 32) | floor(2^95 / (q_i << n)), n = 64 - bits(q_i)
   const u64* Q;          // [W]
   const u64* halfQ;      // [W]
   int W;                 // words for Q (with headroom for the CRT sum)
