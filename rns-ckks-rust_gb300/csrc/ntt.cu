@@ -258,7 +258,7 @@ __global__ __launch_bounds__(256, 3) void k_cols_f(NttArgs a, PtrTab src, PtrTab
 constexpr int ROW_WARPS = 4;
 // polynomials per row block: the same rows (and limb) of ROW_POLYS polynomials share one staging of the rows'
 // twiddles, which take as many bytes as two rows of data
-constexpr int ROW_POLYS = 4;
+constexpr int ROW_POLYS = 8;
 
 // Row phase: each warp transforms SUBS rows of 2^M2 contiguous residues of polynomials
 // blockIdx.z * ROW_POLYS .. below `polys`, loading the next polynomial's rows while transforming the current
