@@ -430,7 +430,10 @@ void tensor_core(rc_context* c, const std::vector<const uint64_t*>& lhs, const s
   launch_check("ntt_forward(tensor)");
   tensor_ntt(c->d_pc, dst, o3, J, limbs, c->N, s);
   launch_check("tensor");
-  ntt_inverse(c->ntt(), o3, o3, 3 * J, limbs, qmap(c, limbs), s);
+  // the tensor's Montgomery products carry a factor 2^-64, taken out by the inverse transform's scale
+  NttArgs inv = c->ntt();
+  inv.mont_out = 1;
+  ntt_inverse(inv, o3, o3, 3 * J, limbs, qmap(c, limbs), s);
   launch_check("ntt_inverse(tensor)");
 }
 
@@ -611,6 +614,8 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
       k.n_inv = invmod_h(N % q, q);
       k.n_inv_s = shoup_h(k.n_inv, q);
       k.r2 = (uint64_t)((((u128h)1 << 64) % q) * (((u128h)1 << 64) % q) % q);
+      k.n_inv_r = (uint64_t)((u128h)k.n_inv * (uint64_t)(((u128h)1 << 64) % q) % q);
+      k.n_inv_r_s = shoup_h(k.n_inv_r, q);
       k.one_s = shoup_h(1, q);
       // key words are < q: sum of chunk products stays below q * 2^64
       k.mac_chunk = (uint64_t)((~0ull) / (out_bound * q));

@@ -44,6 +44,7 @@ struct NttArgs {
   int log_n;
   int n1;    // column-phase size 2^n1; row-phase size 2^(log_n - n1)
   int lazy;  // all primes < 2^58: forward butterflies skip the [0,4q) correction
+  int mont_out = 0;  // inverse: scale by N^-1 2^64 instead of N^-1 (inputs are Montgomery products)
 };
 
 // Negacyclic NTT over `polys` x `limbs` limbs, src -> dst (may alias).
@@ -77,7 +78,8 @@ struct ScalarTab {
 };
 void mul_scalar(const PrimeConst* pc, const u64* a, const ScalarTab& v, u64* out, int limbs, LimbMap map, int n,
                 cudaStream_t s);
-// NTT-domain tensor: for each job j, in = [a0,a1,b0,b1] (4 polys) -> out = [d0,d1,d2]
+// NTT-domain tensor: for each job j, in = [a0,a1,b0,b1] (4 polys) -> out = [d0,d1,d2] * 2^-64 (Montgomery
+// products; an inverse transform with NttArgs::mont_out takes the factor out)
 void tensor_ntt(const PrimeConst* pc, const PtrTab& in4, const PtrTab& out3, int jobs, int limbs, int n,
                 cudaStream_t s);
 // coefficient-domain Galois automorphism X -> X^g (signed permutation), g given by its inverse mod 2N

@@ -40,7 +40,8 @@ struct PrimeConst {
   u64 mac_chunk;      // products of a lazy NTT output and a key word that sum below q * 2^64
   u64 one_s;          // floor(2^64 / q): Shoup companion of 1 (reduces x < 2^64 to [0, 2q))
   u64 mac_chunk64;    // per-term Montgomery values (< 2q each) that sum below 2^64
-  u64 pad[5];
+  u64 n_inv_r, n_inv_r_s;  // N^-1 2^64 mod q (+ Shoup): the inverse transform's scale after Montgomery products
+  u64 pad[3];
 };
 
 #ifdef __CUDACC__

@@ -174,7 +174,8 @@ __global__ void k_inv_cols(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
   }
   for (int idx = threadIdx.x; idx < N1 * COLS; idx += blockDim.x) {
     int r = idx / COLS, c = idx % COLS;
-    out[(size_t)r * N2 + c0 + c] = mul_shoup(sm[idx], pc.n_inv, pc.n_inv_s, q);
+    out[(size_t)r * N2 + c0 + c] =
+        a.mont_out ? mul_shoup(sm[idx], pc.n_inv_r, pc.n_inv_r_s, q) : mul_shoup(sm[idx], pc.n_inv, pc.n_inv_s, q);
   }
 }
 
@@ -210,6 +211,7 @@ __global__ __launch_bounds__(256, 3) void k_cols_f(NttArgs a, PtrTab src, PtrTab
   const int prime = map.prime(limb);
   const PrimeConst& pc = a.pc[prime];
   const u64 q = pc.q;
+  const u64 ninv = a.mont_out ? pc.n_inv_r : pc.n_inv, ninv_s = a.mont_out ? pc.n_inv_r_s : pc.n_inv_s;
   const u64* in = src.p[poly] + (size_t)limb * N;
   u64* out = dst.p[poly] + (size_t)limb * N;
   // tile and twiddles by asynchronous copies, all in flight together
@@ -251,7 +253,7 @@ __global__ __launch_bounds__(256, 3) void k_cols_f(NttArgs a, PtrTab src, PtrTab
     const int idx = it * 256 + threadIdx.x;
     const int r = idx / COLS, c = idx % COLS;
     const u64 x = tile[c * G::STRIDE + core::swz<M1>(r)];
-    out[(size_t)r * N2 + c0 + c] = FWD ? x : mul_shoup(x, pc.n_inv, pc.n_inv_s, q);
+    out[(size_t)r * N2 + c0 + c] = FWD ? x : mul_shoup(x, ninv, ninv_s, q);
   }
 }
 

@@ -63,11 +63,13 @@ __global__ void k_tensor(const PrimeConst* pc, PtrTab in4, PtrTab out3, int limb
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
     const PrimeConst& c = pc[(int)(e >> log_n)];
     u64 x0 = a0[e], x1 = a1[e], y0 = b0[e], y1 = b1[e];
-    d0[e] = mul_mod(x0, y0, c);
+    // Montgomery products (x y 2^-64 mod q; the sum of two stays below q 2^64): one low and one high
+    // 64-bit product per reduction against Barrett's five
+    d0[e] = mont_reduce(mul_wide(x0, y0), c);
     U128 m = mul_wide(x0, y1);
     add_to(m, mul_wide(x1, y0));
-    d1[e] = barrett_reduce(m, c);
-    d2[e] = mul_mod(x1, y1, c);
+    d1[e] = mont_reduce(m, c);
+    d2[e] = mont_reduce(mul_wide(x1, y1), c);
   }
 }
 
