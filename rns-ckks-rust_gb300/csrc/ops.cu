@@ -40,10 +40,22 @@ __global__ void k_plain_mac(const PrimeConst* pc, PtrTab ct, PtrTab pt, int coun
   for (size_t e = blockIdx.x * (size_t)blockDim.x + threadIdx.x; e < total; e += (size_t)gridDim.x * blockDim.x) {
     const PrimeConst& c = pc[map.prime((int)(e >> log_n))];
     u64 s0 = accumulate ? acc[e] : 0, s1 = accumulate ? acc[total + e] : 0;
-    for (int k = 0; k < count; ++k) {
-      const u64 p = pt.p[k][e];
-      s0 = add_mod(s0, mul_mod(ct.p[k][e], p, c), c.q);
-      s1 = add_mod(s1, mul_mod(ct.p[k][total + e], p, c), c.q);
+    if ((c.q >> 59) == 0 && count <= 16) {
+      // 128-bit sums (below (count + 1) q^2 < q 2^64), one Barrett reduction per output
+      U128 t0{s0, 0}, t1{s1, 0};
+      for (int k = 0; k < count; ++k) {
+        const u64 p = pt.p[k][e];
+        add_to(t0, mul_wide(ct.p[k][e], p));
+        add_to(t1, mul_wide(ct.p[k][total + e], p));
+      }
+      s0 = barrett_reduce(t0, c);
+      s1 = barrett_reduce(t1, c);
+    } else {
+      for (int k = 0; k < count; ++k) {
+        const u64 p = pt.p[k][e];
+        s0 = add_mod(s0, mul_mod(ct.p[k][e], p, c), c.q);
+        s1 = add_mod(s1, mul_mod(ct.p[k][total + e], p, c), c.q);
+      }
     }
     acc[e] = s0;
     acc[total + e] = s1;
