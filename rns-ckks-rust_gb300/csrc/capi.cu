@@ -45,7 +45,7 @@ cudaEvent_t HostPipe::event() {
 
 HostPipe::~HostPipe() {
   for (cudaEvent_t e : events) cudaEventDestroy(e);
-  for (cudaStream_t st : {in, comp, out})
+  for (cudaStream_t st : {in, comp, out, comp2})
     if (st) cudaStreamDestroy(st);
 }
 
@@ -1744,7 +1744,7 @@ static bool mult_relin_host_phased(rc_context* c, HostPipe* hp, uint32_t count, 
   // staging: inputs [J][lhs, rhs][2][limbs][N], outputs [J][2][limbs-1][N]
   const size_t stage = ((size_t)J * 4 * pl + (size_t)J * 2 * po) * 8;
   if (!hp->slot[0] || hp->slot[0]->bytes < stage) {
-    for (cudaStream_t st : {hp->in, hp->comp, hp->out})
+    for (cudaStream_t st : {hp->in, hp->comp, hp->out, hp->comp2})
       cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
     hp->slot[0].reset();
     hp->slot[0].reset(new DevBuf(stage));
@@ -1839,7 +1839,7 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
       auto& p = c->pipes[s];
       if (!p) {
         p.reset(new HostPipe());
-        for (cudaStream_t* st : {&p->in, &p->comp, &p->out})
+        for (cudaStream_t* st : {&p->in, &p->comp, &p->out, &p->comp2})
           cuda_check(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking), "cudaStreamCreate");
       }
       hp = p.get();
@@ -1863,7 +1863,7 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
     }
     for (int sl = 0; sl < 2; ++sl) {
       if (!hp->slot[sl] || hp->slot[sl]->bytes < need) {
-        for (cudaStream_t st : {hp->in, hp->comp, hp->out})
+        for (cudaStream_t st : {hp->in, hp->comp, hp->out, hp->comp2})
           cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
         hp->slot[sl].reset();
         hp->slot[sl].reset(new DevBuf(need));
@@ -1871,7 +1871,7 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
     }
     cudaEvent_t start = hp->event();
     cuda_check(cudaEventRecord(start, s), "cudaEventRecord");
-    for (cudaStream_t st : {hp->in, hp->comp, hp->out})
+    for (cudaStream_t st : {hp->in, hp->comp, hp->out, hp->comp2})
       cuda_check(cudaStreamWaitEvent(st, start, 0), "cudaStreamWaitEvent");
     std::vector<cudaEvent_t> comp_done(nchunks), out_done(nchunks);
     for (uint32_t k = 0; k < nchunks; ++k) {
@@ -1895,16 +1895,17 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
         O[j] = rc_ciphertext{dev + off, 0, 0};
         off += out_elems(i0 + j);
       }
+      cudaStream_t cs = (k & 1) ? hp->comp2 : hp->comp;
       {
         cudaEvent_t e = hp->event();
         cuda_check(cudaEventRecord(e, hp->in), "cudaEventRecord");
-        cuda_check(cudaStreamWaitEvent(hp->comp, e, 0), "wait");
+        cuda_check(cudaStreamWaitEvent(cs, e, 0), "wait");
       }
-      if (k >= 2) cuda_check(cudaStreamWaitEvent(hp->comp, out_done[k - 2], 0), "wait");  // slot outputs read
-      int rc = rc_mult_relinearized_batch(c, n, L.data(), R.data(), keys + i0, O.data(), hp->comp);
+      if (k >= 2) cuda_check(cudaStreamWaitEvent(cs, out_done[k - 2], 0), "wait");  // slot outputs read
+      int rc = rc_mult_relinearized_batch(c, n, L.data(), R.data(), keys + i0, O.data(), cs);
       if (rc != RC_OK) fail(rc, g_err);
       comp_done[k] = hp->event();
-      cuda_check(cudaEventRecord(comp_done[k], hp->comp), "cudaEventRecord");
+      cuda_check(cudaEventRecord(comp_done[k], cs), "cudaEventRecord");
       cuda_check(cudaStreamWaitEvent(hp->out, comp_done[k], 0), "wait");
       for (uint32_t j = 0; j < n; ++j) {
         const uint32_t i = i0 + j;

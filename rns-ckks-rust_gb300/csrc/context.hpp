@@ -77,9 +77,10 @@ struct Workspace {
 // Streams, events and two device staging slots of the pipelined host-buffer entry points: chunk k's
 // inputs are copied in while chunk k-1 computes and chunk k-2's results are copied out.  All inputs go
 // through one copy stream in job order: the host link serves one copy at a time, so a second input stream
-// would only delay the first chunk's other operand.
+// would only delay the first chunk's other operand.  Consecutive chunks compute on alternating streams
+// (comp, comp2), so one chunk's kernels fill the SMs the other's leave idle.
 struct HostPipe {
-  cudaStream_t in = nullptr, comp = nullptr, out = nullptr;
+  cudaStream_t in = nullptr, comp = nullptr, out = nullptr, comp2 = nullptr;
   std::unique_ptr<DevBuf> slot[2];
   std::vector<cudaEvent_t> events;
   cudaEvent_t event();  // from the pool, created on first use
