@@ -20,9 +20,10 @@ from ._lib import RcCiphertext, call
 
 DEVICE_CANDIDATES: Dict[str, Sequence[int]] = {"ks_jobs": (8, 16, 32), "mac_bc": (4, 8), "lazy_ntt": (0, 1),
                                                "fuse_tensor": (0, 1)}
-# host_edge (edge stages of chunk / host_edge jobs) is left at 2: smaller edge stages measured slower at every
-# chunk size (the per-stage overhead outweighs the shorter fill and drain)
-HOST_CANDIDATES: Dict[str, Sequence[int]] = {"host_chunk": (2, 4, 8, 16), "host_phased": (0, 1)}
+# host_edge: the first and last stages have chunk / host_edge jobs (a shorter fill and drain against one more
+# stage's overhead)
+HOST_CANDIDATES: Dict[str, Sequence[int]] = {"host_chunk": (2, 4, 8, 16), "host_phased": (0, 1),
+                                             "host_edge": (2, 4)}
 
 
 def default_cache_path() -> Path:
