@@ -1,0 +1,111 @@
+"""Edge cases of the batch entry points: empty batches, batches larger than one launch, the lowest level,
+and plaintext sums past one pass of the multiply-accumulate."""
+import ctypes
+
+import numpy as np
+import pytest
+
+pytestmark = pytest.mark.gpu
+
+torch = pytest.importorskip("torch")
+if not torch.cuda.is_available():  # collected on CPU-only machines, never run there
+    pytest.skip("needs a CUDA GPU", allow_module_level=True)
+
+from test_gpu_parity import _random_key, rand_ct  # noqa: E402
+
+
+@pytest.fixture(scope="module")
+def C(pkg):
+    pkg.lib()
+    from rnsckks_gb300 import context as C
+    return C
+
+
+@pytest.fixture(scope="module")
+def small(pkg, C):
+    params = pkg.params.hybrid_params(12, 4, 2, 50)
+    return params, C.RnsCkksContext(params)
+
+
+def test_empty_batches_are_no_ops(C, small):
+    params, ctx = small
+    one = (C.RcCiphertext * 1)()
+    ptrs = (ctypes.c_void_p * 1)()
+    i32 = (ctypes.c_int32 * 1)()
+    s = C._stream()
+    h = ctx.handle
+    C.call("rc_mult_relinearized_batch", h, 0, one, one, ptrs, one, s)
+    C.call("rc_relinearize_batch", h, 0, one, ptrs, one, s)
+    C.call("rc_rotate_batch", h, 0, one, ptrs, one, s)
+    C.call("rc_relinearize_rescale_batch", h, 0, one, ptrs, one, s)
+    C.call("rc_add_batch", h, 0, one, one, one, s)
+    C.call("rc_rescale_batch", h, 0, one, one, s)
+    C.call("rc_multiply_plain_rns_batch", h, 0, one, ptrs, one, s)
+    C.call("rc_mult_relinearized_batch_host", h, 0, ptrs, ptrs, i32, i32, ptrs, ptrs, i32, s)
+    coeffs = np.zeros(4)
+    C.call("rc_total_sum_batch", h, 0, one, 4, ptrs, 1, one, s)
+    C.call("rc_halevi_shoup_batch", h, 0, one, coeffs.ctypes.data, 4, ptrs, 1, one, s)
+    C.call("rc_paterson_stockmeyer_batch", h, 0, one, coeffs.ctypes.data, 4, ptrs, 1, one, s)
+    C.call("rc_bsgs_apply_batch", h, 0, one, 4, 2, ptrs, 2, 3, 40, ptrs, ptrs, one, s)
+    torch.cuda.synchronize()
+    assert ctx.mult_relinearized_batch([], [], []) == []
+    from rnsckks_gb300 import algorithms as A
+    assert A.total_sum_native(ctx, [], 4, {}) == []
+    assert A.apply_diagonal_linear_transform_native(ctx, [], None, None) == []
+
+
+def test_batch_beyond_one_launch_equals_per_op(C, small):
+    """70 jobs: more than one key-product launch (32 jobs) and more than one tensor chunk (16 jobs)."""
+    params, ctx = small
+    n, q = params.poly_degree, params.q_moduli()
+    rng = np.random.default_rng(70)
+    key = ctx.upload_keyswitch_key(_random_key(rng, params, len(q), True)[0], len(q) - 1, 2)
+    lhs = [C.RnsCiphertext(C.to_device(rand_ct(rng, q, n)), 40) for _ in range(70)]
+    rhs = [C.RnsCiphertext(C.to_device(rand_ct(rng, q, n)), 40) for _ in range(70)]
+    batch = ctx.mult_relinearized_batch(lhs, rhs, [key] * 70)
+    for i in (0, 31, 32, 47, 63, 64, 69):
+        single = ctx.mult_relinearized(lhs[i], rhs[i], key)
+        assert np.array_equal(single.numpy(), batch[i].numpy())
+
+
+def test_lowest_level_matches_oracle(C, small, oracle):
+    """mult_relinearized from two limbs down to one, and a keyswitch at one limb, against the oracle."""
+    params, ctx = small
+    n = params.poly_degree
+    rng = np.random.default_rng(2)
+    qpl = oracle.Plans(n, params.primes).prefix(2)
+    ppl = oracle.Plans(n, params.aux_primes)
+    q = params.q_moduli()[:2]
+    key, D = _random_key(rng, params, 2, True)
+    ksk = ctx.upload_keyswitch_key(key, 1, 2)
+    a, b = rand_ct(rng, q, n), rand_ct(rng, q, n)
+    out = ctx.mult_relinearized(C.RnsCiphertext(C.to_device(a), 35), C.RnsCiphertext(C.to_device(b), 35), ksk)
+    m0, m1 = oracle.mult_relinearized(qpl, ppl, a[0], a[1], b[0], b[1], key, D)
+    assert out.level == 0
+    assert np.array_equal(out.numpy()[0], m0) and np.array_equal(out.numpy()[1], m1)
+    qpl1 = oracle.Plans(n, params.primes).prefix(1)
+    key1, D1 = _random_key(rng, params, 1, True)
+    ksk1 = ctx.upload_keyswitch_key(key1, 0, 2)
+    x = rand_ct(rng, params.q_moduli()[:1], n, 1)[0]
+    ks = ctx.keyswitch(C.RnsPolynomial(C.to_device(x)), ksk1)
+    r0, r1 = oracle.keyswitch(qpl1, ppl, x, key1, D1)
+    assert np.array_equal(ks.numpy()[0], r0) and np.array_equal(ks.numpy()[1], r1)
+
+
+def test_plain_accumulate_past_one_pass_equals_sum_of_products(C, small):
+    """40 terms: three passes of the 16-term multiply-accumulate, against mult_plain + add term by term."""
+    params, ctx = small
+    n, q = params.poly_degree, params.q_moduli()
+    rng = np.random.default_rng(40)
+    cts = [C.RnsCiphertext(C.to_device(rand_ct(rng, q, n)), 40) for _ in range(40)]
+    plains = [C.to_device(np.stack([rng.integers(0, m, n, dtype=np.uint64) for m in q])) for _ in range(40)]
+    out = torch.zeros((2, len(q), n), dtype=torch.int64, device="cuda")
+    CT = (C.RcCiphertext * 40)(*[c.raw() for c in cts])
+    PT = (ctypes.c_void_p * 40)(*[p.data_ptr() for p in plains])
+    O = C.RcCiphertext(out.data_ptr(), 0, 0)
+    C.call("rc_mult_plain_accumulate", ctx.handle, 40, CT, 0, PT, 0, ctypes.byref(O), C._stream())
+    want = None
+    for c, p in zip(cts, plains):
+        term = ctx.multiply_plain_rns(c, C.RnsPolynomial(p))
+        want = term if want is None else want.add(term)
+    assert np.array_equal(C.to_host(out), want.numpy())
