@@ -288,7 +288,10 @@ void wide_ks_finish(rc_context* c, const WideKs& w, const std::vector<KsJob>& jo
   f.add_g_inv = g_inv;
   f.wide = 1;
   f.wt = c->wide;
-  f.lazy = c->lazy ? 1 : 0;
+  // the lazy finalize sums at most (8 + 2K) terms below q per limb: every prime below 2^64 / (8 + 2K)
+  f.lazy = 1;
+  for (uint64_t m : c->mod)
+    if (m >= UINT64_MAX / (uint64_t)(8 + 2 * w.K)) f.lazy = 0;
   PtrTab add{}, out{};
   for (int j = 0; j < n; ++j) {
     add.p[2 * j] = const_cast<uint64_t*>(jobs[b0 + j].add0);

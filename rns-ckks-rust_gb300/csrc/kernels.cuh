@@ -195,7 +195,7 @@ struct FinalizeArgs {
   uint64_t add_g_inv;  // automorphism applied to the addend (0/1 = none)
   int wide;            // acc holds [job][2][limbs][2 pairs][N] uint2 residues mod w0..w3 to CRT-combine
   WideTab wt;
-  int lazy;            // every prime below 2^58: a limb's terms are summed unreduced (below 24 q)
+  int lazy;            // every prime below 2^64 / (8 + 2K): a limb's terms are summed unreduced
 };
 void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const PtrTab& out, int jobs,
               cudaStream_t s);

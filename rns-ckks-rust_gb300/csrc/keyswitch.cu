@@ -647,7 +647,7 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
 
   if (fast) {
     // S F + [S < 0] (q - A F) + sum_k v_k (q - M_k F) + [X_P > P/2] P F + addend (+ the rescale term), each
-    // below 2q or q: at most (8 + 2K) q < 2^63, reduced once by the final Shoup product
+    // below 2q or q: at most (8 + 2K) q < 2^64, reduced once by the final Shoup product
     auto lazy_value = [&](int i, const LimbIn& in) -> u64 {
       const u64 q = T(i, FT_Q);
       u64 s = wide_crt_lazy(in.p01, in.p23, f.wt, q, T(i, FT_LO), T(i, FT_LO_S), T(i, FT_C01), T(i, FT_C01_S),
