@@ -1135,10 +1135,12 @@ extern "C" int rc_poly_multiply(rc_context* c, const uint64_t* a, const uint64_t
     PtrTab x{}, y{};
     x.p[0] = ta;
     y.p[0] = tb;
-    ew_binary(EwOp::Mul, c->d_pc, x, y, 0, x, 1, (int)limbs, map, c->N, s);
+    ew_binary(EwOp::MulMont, c->d_pc, x, y, 0, x, 1, (int)limbs, map, c->N, s);
     PtrTab o{};
     o.p[0] = out;
-    ntt_inverse(c->ntt(), x, o, 1, (int)limbs, map, s);
+    NttArgs inv = c->ntt();
+    inv.mont_out = 1;  // takes out the Montgomery products' 2^-64
+    ntt_inverse(inv, x, o, 1, (int)limbs, map, s);
     launch_check("poly_multiply");
   });
 }
@@ -1278,11 +1280,13 @@ static void mult_plain_impl(rc_context* c, const rc_ciphertext* ct, const uint64
   a.p[0] = f;
   a.p[1] = f + pl;
   b.p[0] = f + 2 * pl;
-  ew_binary(EwOp::Mul, c->d_pc, a, b, 1, a, 2, limbs, qmap(c, limbs), c->N, s);
+  ew_binary(EwOp::MulMont, c->d_pc, a, b, 1, a, 2, limbs, qmap(c, limbs), c->N, s);
   PtrTab o{};
   o.p[0] = out->data;
   o.p[1] = out->data + pl;
-  ntt_inverse(c->ntt(), a, o, 2, limbs, qmap(c, limbs), s);
+  NttArgs inv = c->ntt();
+  inv.mont_out = 1;  // takes out the Montgomery products' 2^-64
+  ntt_inverse(inv, a, o, 2, limbs, qmap(c, limbs), s);
   launch_check("mult_plain");
   out->level = ct->level;
 }

@@ -63,7 +63,8 @@ bool tensor_fused(const NttArgs& a, const PrimeConst* pc, const PtrTab& in4, con
                   const PtrTab& out3, int jobs, int limbs, LimbMap map, cudaStream_t s);
 
 // ---- elementwise / scheme kernels (ops.cu) ----
-enum class EwOp { Add, Sub, Mul };
+// MulMont: x y 2^-64 mod q (Montgomery), for products an inverse transform with NttArgs::mont_out follows
+enum class EwOp { Add, Sub, Mul, MulMont };
 // out[k] = a[k] (op) b[k] over `polys` polys of `limbs` limbs; b may be shared
 // across polys (b_shared != 0 uses b.p[0] for every poly).
 void ew_binary(EwOp op, const PrimeConst* pc, const PtrTab& a, const PtrTab& b, int b_shared, const PtrTab& out,

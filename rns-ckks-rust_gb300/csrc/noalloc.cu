@@ -82,9 +82,11 @@ extern "C" int rc_poly_multiply_noalloc(rc_context* c, const uint64_t* a, const 
     PtrTab x{}, y{}, o{};
     x.p[0] = scratch;
     y.p[0] = scratch + pl;
-    ew_binary(EwOp::Mul, c->d_pc, x, y, 0, x, 1, (int)limbs, map, c->N, s);
+    ew_binary(EwOp::MulMont, c->d_pc, x, y, 0, x, 1, (int)limbs, map, c->N, s);
     o.p[0] = out;
-    ntt_inverse(c->ntt(), x, o, 1, (int)limbs, map, s);
+    NttArgs inv = c->ntt();
+    inv.mont_out = 1;  // takes out the Montgomery products' 2^-64
+    ntt_inverse(inv, x, o, 1, (int)limbs, map, s);
     cuda_check(cudaGetLastError(), "rc_poly_multiply_noalloc");
     return RC_OK;
   } catch (const ApiError& e) {

@@ -29,7 +29,8 @@ __global__ void k_ew_binary(int op, const PrimeConst* pc, PtrTab a, PtrTab b, in
     u64 r;
     if (op == 0) r = add_mod(x, y, c.q);
     else if (op == 1) r = sub_mod(x, y, c.q);
-    else r = mul_mod(x, y, c);
+    else if (op == 2) r = mul_mod(x, y, c);
+    else r = mont_reduce(mul_wide(x, y), c);
     po[e] = r;
   }
 }
@@ -155,8 +156,8 @@ void ew_binary(EwOp op, const PrimeConst* pc, const PtrTab& a, const PtrTab& b, 
   int log_n = __builtin_ctz(n);
   dim3 g(grid_for((size_t)limbs * n, 256), polys);
   ProfScope p("elementwise", s);
-  k_ew_binary<<<g, 256, 0, s>>>(op == EwOp::Add ? 0 : op == EwOp::Sub ? 1 : 2, pc, a, b, b_shared, out, limbs, map,
-                                log_n);
+  k_ew_binary<<<g, 256, 0, s>>>(op == EwOp::Add ? 0 : op == EwOp::Sub ? 1 : op == EwOp::Mul ? 2 : 3, pc, a, b,
+                                b_shared, out, limbs, map, log_n);
 }
 
 void plain_mac(const PrimeConst* pc, const PtrTab& ct, const PtrTab& pt, int count, u64* acc, int accumulate,

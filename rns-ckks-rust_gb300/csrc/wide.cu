@@ -18,6 +18,8 @@
 //   digit transforms, tiled:  dtt[job][pair][x/32][digit][32]
 //   key, tiled:               kwt[limb][pair][x/32][digit][c][32]
 //   products:                 acc[job][c][limb][pair][N]
+#include <mutex>
+
 #include "kernels.cuh"
 #include "nttcore.cuh"
 #include "wide.cuh"
@@ -384,11 +386,14 @@ template <int BC, bool FOLD>
 void launch_w_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt,
                   uint2* acc, int b0, int nb, cudaStream_t s) {
   const size_t smem = ((size_t)BC * D * 32 + (size_t)W_MAC_WARPS * W_PF * 64) * sizeof(uint2);
-  static size_t configured = 0;
-  if (smem > 48 * 1024 && smem > configured) {
-    cudaFuncSetAttribute(k_w_mac<BC, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-    configured = smem;
-  }
+  // the opt-in limit is set once per instance, before any launch of it (callers on several host threads)
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0, optin = 48 * 1024;
+    if (cudaGetDevice(&dev) == cudaSuccess)
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+    cudaFuncSetAttribute(k_w_mac<BC, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+  });
   dim3 g((nb + BC - 1) / BC, 2, (1 << w.log_n) / 32);
   k_w_mac<BC, FOLD><<<g, 32 * W_MAC_WARPS, smem, s>>>(w, D, key_digits, total, kwt, dtt, acc, b0, nb);
 }
