@@ -250,6 +250,14 @@ int rc_relinearize_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* q
                          rc_ciphertext* out, void* stream);
 int rc_rotate_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* ct, const rc_ksk* const* keys,
                     rc_ciphertext* out, void* stream);
+/* rotate (context/rotation.rs:104-127) of each of `count` same-level ciphertexts by each of `nrot` rotation
+ * keys, out[i * nrot + r] = rotate(ct[i], keys[r]), with one decomposition of each c1 shared by its rotations
+ * ("hoisted"; the baby steps of linear_transform.rs:213-232 rotate one input by 1..b-1).  Results equal
+ * rc_rotate's residue for residue: an input whose decomposition holds a digit at -2^29 (where the digits of a
+ * negated coefficient are not the negated digits) is rotated the ordinary way.  Mixed levels or key shapes
+ * run as rc_rotate_batch. */
+int rc_rotate_hoisted(rc_context* ctx, uint32_t count, const rc_ciphertext* ct, uint32_t nrot,
+                      const rc_ksk* const* keys, rc_ciphertext* out, void* stream);
 /* relinearize then rescale (context/ops.rs:111-122 followed by context/ops.rs:32-37) for `count`
  * quadratic ciphertexts of any mix of levels; the rescale is fused into the keyswitch's last pass.  out[i]
  * gets level - 1 and the rescaled scale.  After rc_reserve(ctx, top level, 32, stream) the call allocates

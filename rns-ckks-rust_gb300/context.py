@@ -928,6 +928,20 @@ class RnsCkksContext:
         call("rc_rotate_batch", self.handle, n, C, K, O, _stream())
         return [RnsCiphertext(o, O[i].scale_bits, O[i].level) for i, o in enumerate(outs)]
 
+    def rotate_hoisted(self, cts: Sequence[RnsCiphertext], keys: Sequence[RnsRotationKey]) -> List[List[RnsCiphertext]]:
+        """out[i][r] = rotate(cts[i], keys[r]) with one decomposition of each ciphertext shared by its rotations
+        (rc_rotate_hoisted); the same residues as `rotate`."""
+        n, m = len(cts), len(keys)
+        if n == 0 or m == 0:
+            return [[] for _ in range(n)]
+        outs = [self._ct_out(2, c.level + 1) for c in cts for _ in range(m)]
+        C = (RcCiphertext * n)(*[c.raw() for c in cts])
+        O = (RcCiphertext * (n * m))(*[RcCiphertext(o.data_ptr(), 0, 0) for o in outs])
+        K = (ctypes.c_void_p * m)(*[k.keyswitch_key.handle for k in keys])
+        call("rc_rotate_hoisted", self.handle, n, C, m, K, O, _stream())
+        return [[RnsCiphertext(outs[i * m + r], O[i * m + r].scale_bits, O[i * m + r].level) for r in range(m)]
+                for i in range(n)]
+
 
 class CudaGraph:
     """An executable CUDA graph of library calls (rc_graph_*): replays on the captured buffers."""

@@ -532,26 +532,23 @@ extern "C" int rc_bsgs_apply_batch(rc_context* c, uint32_t count, const rc_ciphe
     const int lv = diag_level, limbs = lv + 1;
     const uint32_t b = std::min(baby_step, dimension);
     const size_t ct_words = 2 * (size_t)limbs * A.N;
-    // precompute_baby_rotations (213-232): rotations by 1 .. b-1 of every ciphertext, jobs sharing a key adjacent
+    // precompute_baby_rotations (213-232): rotations by 1 .. b-1 of every ciphertext, hoisted (one
+    // decomposition of each ciphertext serves its b-1 rotations)
     std::vector<rc_ciphertext> jobs, rot;
     std::vector<const rc_ksk*> keys;
     for (uint32_t st = 1; st < b; ++st) {
       if (!baby_keys || !baby_keys[st - 1])
         fail(RC_ERR_INVALID_ARGUMENT, "missing input rotation key for BSGS baby step " + std::to_string(st));
-      for (uint32_t i = 0; i < count; ++i) {
-        jobs.push_back(cts[i]);
-        keys.push_back(baby_keys[st - 1]);
-      }
+      keys.push_back(baby_keys[st - 1]);
     }
     // the babies of ciphertext i in the NTT domain: babies[(i * b + j)] (j = 0 is the ciphertext itself)
     uint64_t* babies = A.pool.take(ct_words * count * b);
-    if (!jobs.empty()) {
-      rot.resize(jobs.size());
-      for (size_t k = 0; k < jobs.size(); ++k) {
-        const uint32_t st = 1 + (uint32_t)(k / count), i = (uint32_t)(k % count);
-        rot[k] = rc_ciphertext{babies + ((size_t)i * b + st) * ct_words, lv, diag_scale_bits};
-      }
-      ok(rc_rotate_batch(c, (uint32_t)jobs.size(), jobs.data(), keys.data(), rot.data(), A.s));
+    if (b > 1) {
+      rot.resize((size_t)count * (b - 1));
+      for (uint32_t i = 0; i < count; ++i)
+        for (uint32_t st = 1; st < b; ++st)
+          rot[(size_t)i * (b - 1) + st - 1] = rc_ciphertext{babies + ((size_t)i * b + st) * ct_words, lv, diag_scale_bits};
+      ok(rc_rotate_hoisted(c, count, cts, b - 1, keys.data(), rot.data(), A.s));
     }
     for (uint32_t i = 0; i < count; ++i)
       cuda_check(cudaMemcpyAsync(babies + (size_t)i * b * ct_words, cts[i].data, ct_words * 8,

@@ -1695,6 +1695,99 @@ extern "C" int rc_rotate_batch(rc_context* c, uint32_t count, const rc_ciphertex
   });
 }
 
+// Rotations of every ciphertext by each of several keys from one decomposition ("hoisted"): c1 is decomposed
+// and its digits transformed once, and each rotation's key product reads those transforms through the
+// automorphism's NTT-domain permutation; the addend is sigma(c0) as in rc_rotate.  The digits of sigma(c1)
+// are sigma of the digits of c1 -- the automorphism moves coefficients and flips signs, and the balanced
+// digits of -X are the negated digits of X -- except where a digit of X is -2^29 (the balanced rule sends
+// both +2^29 and -2^29 there).  A ciphertext with such a digit is rotated again the ordinary way, so every
+// result equals rc_rotate's for the same (ciphertext, key).  Mixed levels, keys of different shapes or a
+// chain outside the wide key product run as rc_rotate_batch.
+extern "C" int rc_rotate_hoisted(rc_context* c, uint32_t count, const rc_ciphertext* cts, uint32_t nrot,
+                                 const rc_ksk* const* keys, rc_ciphertext* out, void* stream) {
+  return guarded([&] {
+    require(c && cts && keys && out, "arguments must not be null");
+    if (count == 0 || nrot == 0) return;
+    cudaStream_t s = S(stream);
+    const int level = cts[0].level;
+    bool hoist = true;
+    for (uint32_t i = 0; i < count; ++i) {
+      check_ct(c, &cts[i], "ciphertext");
+      hoist = hoist && cts[i].level == level;
+      for (uint32_t r = 0; r < nrot; ++r)
+        require(out[(size_t)i * nrot + r].data != nullptr && out[(size_t)i * nrot + r].data != cts[i].data,
+                "rotate output must not alias its input");
+    }
+    for (uint32_t r = 0; r < nrot; ++r) {
+      require(keys[r] != nullptr, "rotation key must not be null");
+      hoist = hoist && keys[r]->aux == keys[0]->aux && keys[r]->digits == keys[0]->digits && keys[r]->wdata &&
+              keys[r]->galois > 1 && keys[r]->level == level;
+    }
+    auto ordinary = [&](const std::vector<std::pair<uint32_t, uint32_t>>& pairs) {
+      std::vector<rc_ciphertext> in, o;
+      std::vector<const rc_ksk*> ks;
+      for (auto& p : pairs) {
+        in.push_back(cts[p.first]);
+        ks.push_back(keys[p.second]);
+        o.push_back(out[(size_t)p.first * nrot + p.second]);
+      }
+      const int rc = rc_rotate_batch(c, (uint32_t)in.size(), in.data(), ks.data(), o.data(), stream);
+      if (rc != RC_OK) fail(rc, g_err);
+      for (size_t k = 0; k < pairs.size(); ++k) out[(size_t)pairs[k].first * nrot + pairs[k].second] = o[k];
+    };
+    const int limbs = level + 1;
+    const int K = keys[0]->aux ? c->K : 0;
+    const int D = ks_digits(c, keys[0], limbs);
+    if (hoist) {
+      for (uint32_t r = 0; r < nrot; ++r) check_key_for(c, keys[r], limbs);
+      hoist = wide_applies(c, limbs, K, D) && c->log_n >= 5;
+    }
+    if (!hoist) {
+      std::vector<std::pair<uint32_t, uint32_t>> all;
+      for (uint32_t i = 0; i < count; ++i)
+        for (uint32_t r = 0; r < nrot; ++r) all.emplace_back(i, r);
+      ordinary(all);
+      return;
+    }
+    const size_t N = c->N, pl = (size_t)limbs * N;
+    for (uint32_t b0 = 0; b0 < count; b0 += (uint32_t)c->ks_jobs) {
+      const int n = (int)std::min<uint32_t>((uint32_t)c->ks_jobs, count - b0);
+      Arena ar(ws_device(c, s, wide_ks_bytes(c, n, n, limbs, K, D) + 2048));
+      const WideKs w = wide_ks_layout(c, ar, n, n, limbs, K, D);
+      int* flags = ar.take<int>((size_t)n);
+      cuda_check(cudaMemsetAsync(flags, 0, (size_t)n * sizeof(int), s), "cudaMemsetAsync");
+      PtrTab src{};
+      for (int j = 0; j < n; ++j) src.p[j] = cts[b0 + j].data + pl;
+      decompose(c->d_pc, level_info(c, limbs).dt, src, n, limbs, D, w.digits, 1, c->log_n, s, flags);
+      launch_check("decompose");
+      require(wide_digit_transforms(c->wp, D, n, w.digits, w.work, w.dt, s), "internal: wide transforms unsupported");
+      launch_check("wide digit transforms");
+      std::vector<int> tie((size_t)n);
+      cuda_check(cudaMemcpyAsync(tie.data(), flags, (size_t)n * sizeof(int), cudaMemcpyDeviceToHost, s), "D2H");
+      for (uint32_t r = 0; r < nrot; ++r) {
+        const rc_ksk* k = keys[r];
+        wide_mac(c->wp, D, (int)k->digits, w.total, (const uint2*)k->wdata, w.dt, w.acc, 0, n, c->mac_bc, s,
+                 (uint32_t)k->galois);
+        launch_check("wide mac");
+        std::vector<KsJob> fin((size_t)n);
+        for (int j = 0; j < n; ++j) {
+          rc_ciphertext& o = out[(size_t)(b0 + j) * nrot + r];
+          fin[(size_t)j] = KsJob{nullptr, k, cts[b0 + j].data, nullptr, o.data, o.data + pl};
+          o.level = level;
+          o.scale_bits = cts[b0 + j].scale_bits;
+        }
+        wide_ks_finish(c, w, fin, 0, n, galois_inverse(c, k->galois), false, s);
+      }
+      cuda_check(cudaStreamSynchronize(s), "cudaStreamSynchronize");  // the tie flags
+      std::vector<std::pair<uint32_t, uint32_t>> redo;
+      for (int j = 0; j < n; ++j)
+        if (tie[(size_t)j])
+          for (uint32_t r = 0; r < nrot; ++r) redo.emplace_back(b0 + (uint32_t)j, r);
+      if (!redo.empty()) ordinary(redo);
+    }
+  });
+}
+
 // =========================================================================
 // host-buffer entry points
 // =========================================================================

@@ -129,9 +129,11 @@ struct ModDownTab {
 void lift_to_aux(const PrimeConst* pc, const PrimeConst* ppc, const DecompTab& dt, const u64* src, u64* dst,
                  int polys, int limbs, int K, int log_n, cudaStream_t s);
 // digits[job][d][x] (int32) of the centred CRT value of src (optionally read
-// through the automorphism with inverse element g_inv; 0/1 = none)
+// through the automorphism with inverse element g_inv; 0/1 = none).  tie_flags (optional, [jobs], zeroed by
+// the caller) get 1 where a digit equals -2^29: only then can the digits of -X differ from the negated
+// digits of X (the balanced rule sends both +2^29 and -2^29 to -2^29)
 void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int jobs, int limbs, int D,
-               int32_t* digits, uint64_t g_inv, int log_n, cudaStream_t s);
+               int32_t* digits, uint64_t g_inv, int log_n, cudaStream_t s, int* tie_flags = nullptr);
 
 // Exact integer key product ("wide-CRT"): S = sum_i d_i * k_i is carried under
 // four internal primes w0..w3 < 2^29 (product A), handled as two pairs
@@ -208,9 +210,10 @@ void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const
 bool wide_digit_transforms(const WidePrimes& w, int D, int jobs, const int32_t* digits, uint2* work, uint2* dtt,
                            cudaStream_t s);
 // acc[b][c][j][pair][N] (NTT domain, reduced) for jobs b0..b0+nb-1 sharing the
-// tiled key kwt[j][pair][x/32][digit][c][32]
+// tiled key kwt[j][pair][x/32][digit][c][32]; gal > 1 reads the digit transforms through the automorphism
+// X -> X^gal (their NTT-domain permutation: hoisted rotations of one decomposition)
 void wide_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt, uint2* acc,
-              int b0, int nb, int bc_max, cudaStream_t s);
+              int b0, int nb, int bc_max, cudaStream_t s, uint32_t gal = 0);
 // inverse transforms of `polys` consecutive [pair][N] polynomials, in place
 bool wide_inverse(const WidePrimes& w, uint2* data, int polys, cudaStream_t s);
 // coefficient-form key [digits][2][limbs][N] (residues mod the scheme primes) ->

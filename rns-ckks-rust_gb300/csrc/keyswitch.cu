@@ -32,7 +32,7 @@ namespace {
 // ---------------------------------------------------------------------------
 template <int WM>
 __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int limbs, int D, int32_t* digits,
-                            u64 g_inv, int log_n) {
+                            u64 g_inv, int log_n, int* tie_flags) {
   const CrtSmem tabs = stage_crt_tables(pc, dt, limbs);
   __syncthreads();
   const int W = dt.W;
@@ -55,6 +55,7 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
   // balanced base-2^30 digits of the two's complement value
   int32_t* out = digits + (size_t)job * D * N + x;
   u64 carry = 0;
+  bool tie = false;  // a digit at -2^29
   constexpr int DMAX = (64 * WM) / 30 + 2;
 #pragma unroll
   for (int d = 0; d < DMAX; ++d) {
@@ -78,6 +79,7 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
         dig = (int64_t)v;
         carry = 0;
       }
+      tie |= dig == -(1ll << 29);
       out[(size_t)d * N] = (int32_t)dig;
     }
   }
@@ -94,8 +96,10 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
       dig = (int64_t)v;
       carry = 0;
     }
+    tie |= dig == -(1ll << 29);
     out[(size_t)d * N] = (int32_t)dig;
   }
+  if (tie && tie_flags) atomicOr(&tie_flags[job], 1);
 }
 
 // lift_poly_to_context (keyswitching.rs:242-276) for polynomial blockIdx.y: the Q limbs are copied and limb
@@ -797,7 +801,7 @@ __global__ void k_key_relayout(const PrimeConst* pc, const u64* src, u64* dst, i
 }  // namespace
 
 void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int jobs, int limbs, int D,
-               int32_t* digits, uint64_t g_inv, int log_n, cudaStream_t s) {
+               int32_t* digits, uint64_t g_inv, int log_n, cudaStream_t s, int* tie_flags) {
   if (jobs <= 0) return;
   const int N = 1 << log_n;
   const int threads = N < 128 ? N : 128;
@@ -806,14 +810,14 @@ void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int
   ProfScope p("decompose", s);
   // the word count is a template parameter (register-resident value); the closest instance above W runs
   const size_t smem = crt_smem_bytes(limbs, W);
-  if (W <= 4) k_decompose<4><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
-  else if (W <= 8) k_decompose<8><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
-  else if (W <= 12) k_decompose<12><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
-  else if (W <= 16) k_decompose<16><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
-  else if (W <= 20) k_decompose<20><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
-  else if (W <= 24) k_decompose<24><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
-  else if (W <= 32) k_decompose<32><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
-  else k_decompose<64><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n);
+  if (W <= 4) k_decompose<4><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else if (W <= 8) k_decompose<8><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else if (W <= 12) k_decompose<12><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else if (W <= 16) k_decompose<16><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else if (W <= 20) k_decompose<20><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else if (W <= 24) k_decompose<24><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else if (W <= 32) k_decompose<32><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else k_decompose<64><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
 }
 
 void lift_to_aux(const PrimeConst* pc, const PrimeConst* ppc, const DecompTab& dt, const u64* src, u64* dst,

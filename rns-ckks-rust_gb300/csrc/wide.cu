@@ -282,10 +282,21 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// Hoisted rotations: the digit transforms of sigma_g(d) are those of d permuted, NTT(sigma_g d) at evaluation
+// index k = NTT(d) at k' with 2k'+1 = g (2k+1) mod 2N.  In the bit-reversed storage order the 32 positions of
+// one tile all come from one source tile, permuted among its lanes (the top five bits of k' depend on the
+// lane, the rest on the tile only): src(x) = bitrev(k'(bitrev(x))).
+__device__ __forceinline__ uint32_t galois_source(uint32_t x, uint32_t g, int log_n) {
+  const uint32_t k = __brev(x) >> (32 - log_n);
+  const uint32_t mask2 = (2u << log_n) - 1;  // mod 2N
+  const uint32_t kk = (((g * (2 * k + 1)) & mask2) - 1) >> 1;
+  return __brev(kk) >> (32 - log_n);
+}
+
 template <int BC, bool FOLD>
 __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC >= 2 ? 4 : 5))) void k_w_mac(
     WidePrimes w, int D, int key_digits, int total, const uint2* __restrict__ kwt, const uint2* __restrict__ dtt,
-    uint2* acc, int b0, int nb) {
+    uint2* acc, int b0, int nb, uint32_t gal) {
   extern __shared__ uint2 dsm[];  // [BC][D][32] digit transforms, then [warps][W_PF][2][32] key ring
   const int N = 1 << w.log_n, tiles = N >> 5;
   // job groups vary fastest, so the CTAs that stream the same key tile run together and share it in L2
@@ -293,6 +304,11 @@ __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC 
   const int bstart = b0 + blockIdx.x * BC;
   const int nloc = min(BC, b0 + nb - bstart);
   const int run = D * 32;
+  // gal > 1: the digits are those of sigma_gal of the decomposed polynomial (one source tile, lanes permuted)
+  const uint32_t src0 = gal > 1 ? galois_source((uint32_t)xb * 32, gal, w.log_n) : (uint32_t)xb * 32;
+  const int stile = (int)(src0 >> 5);
+  const int slane = gal > 1 ? (int)(galois_source((uint32_t)xb * 32 + (threadIdx.x & 31), gal, w.log_n) & 31)
+                            : (int)(threadIdx.x & 31);
   // the jobs' digit-transform runs (D * 256 bytes each, contiguous) go to shared memory by asynchronous
   // 16-byte copies, all in flight at once; jobs past nloc read as zero
   {
@@ -301,7 +317,7 @@ __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC 
     for (int e = threadIdx.x; e < BC * run16; e += 32 * W_MAC_WARPS) {
       const int b = e / run16, r = e - b * run16;
       if (b < nloc) {
-        const uint2* g = dtt + (((size_t)(bstart + b) * 2 + pair) * tiles + xb) * run + 2 * r;
+        const uint2* g = dtt + (((size_t)(bstart + b) * 2 + pair) * tiles + stile) * run + 2 * r;
         asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sbase + 16u * e), "l"(g) : "memory");
       } else {
         reinterpret_cast<uint4*>(dsm)[e] = make_uint4(0, 0, 0, 0);
@@ -349,7 +365,7 @@ __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC 
         if (i < D) {
           cp_async_wait<W_PF - 1>();  // digit i's group has landed
           const uint2 k0 = ring[64 * u], k1 = ring[64 * u + 32];
-          const uint2* dp = dsm + i * 32 + lane;
+          const uint2* dp = dsm + i * 32 + slane;
 #pragma unroll
           for (int b = 0; b < BC; ++b) {
             const uint2 d = dp[b * run];
@@ -384,7 +400,7 @@ __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC 
 
 template <int BC, bool FOLD>
 void launch_w_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt,
-                  uint2* acc, int b0, int nb, cudaStream_t s) {
+                  uint2* acc, int b0, int nb, uint32_t gal, cudaStream_t s) {
   const size_t smem = ((size_t)BC * D * 32 + (size_t)W_MAC_WARPS * W_PF * 64) * sizeof(uint2);
   // the opt-in limit is set once per instance, before any launch of it (callers on several host threads)
   static std::once_flag once;
@@ -395,7 +411,7 @@ void launch_w_mac(const WidePrimes& w, int D, int key_digits, int total, const u
     cudaFuncSetAttribute(k_w_mac<BC, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
   });
   dim3 g((nb + BC - 1) / BC, 2, (1 << w.log_n) / 32);
-  k_w_mac<BC, FOLD><<<g, 32 * W_MAC_WARPS, smem, s>>>(w, D, key_digits, total, kwt, dtt, acc, b0, nb);
+  k_w_mac<BC, FOLD><<<g, 32 * W_MAC_WARPS, smem, s>>>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal);
 }
 
 // coefficient-form key [digits][2][limbs][N] -> kw[((j * digits + i) * 2 + c)][pair][N]
@@ -496,19 +512,19 @@ bool wide_digit_transforms(const WidePrimes& w, int D, int jobs, const int32_t* 
 }
 
 void wide_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt, uint2* acc,
-              int b0, int nb, int bc_max, cudaStream_t s) {
+              int b0, int nb, int bc_max, cudaStream_t s, uint32_t gal) {
   ProfScope p("wide_mac", s);
   const int want = nb < bc_max ? nb : bc_max;  // jobs per CTA: the group size, at most bc_max
   if (D > 64) {  // folded sums; at most 4 jobs per CTA keep the fold within the register budget
-    if (want <= 1) launch_w_mac<1, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
-    else if (want <= 2) launch_w_mac<2, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
-    else launch_w_mac<4, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
+    if (want <= 1) launch_w_mac<1, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
+    else if (want <= 2) launch_w_mac<2, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
+    else launch_w_mac<4, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
     return;
   }
-  if (want <= 1) launch_w_mac<1, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
-  else if (want <= 2) launch_w_mac<2, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
-  else if (want <= 4) launch_w_mac<4, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
-  else launch_w_mac<8, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, s);
+  if (want <= 1) launch_w_mac<1, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
+  else if (want <= 2) launch_w_mac<2, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
+  else if (want <= 4) launch_w_mac<4, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
+  else launch_w_mac<8, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
 }
 
 bool wide_inverse(const WidePrimes& w, uint2* data, int polys, cudaStream_t s) {

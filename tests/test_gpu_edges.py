@@ -109,3 +109,45 @@ def test_plain_accumulate_past_one_pass_equals_sum_of_products(C, small):
         term = ctx.multiply_plain_rns(c, C.RnsPolynomial(p))
         want = term if want is None else want.add(term)
     assert np.array_equal(C.to_host(out), want.numpy())
+
+
+def _rot_keys(C, ctx, params, rng, gals):
+    q = params.q_moduli()
+    key = _random_key(rng, params, len(q), True)[0]
+    return [C.RnsRotationKey(g, ctx.upload_keyswitch_key(key, len(q) - 1, 2, g)) for g in gals]
+
+
+def test_hoisted_rotations_equal_ordinary_rotations(C, small):
+    """rc_rotate_hoisted (one decomposition per ciphertext, the automorphism applied to its digit transforms)
+    against rc_rotate for steps 1, 2, 5, -1, -7 and the conjugation, three ciphertexts."""
+    params, ctx = small
+    n, q = params.poly_degree, params.q_moduli()
+    rng = np.random.default_rng(5)
+    gals = [ctx.galois_element_for_rotation(st) for st in (1, 2, 5, -1, -7)] + [ctx.conjugation_galois_element()]
+    keys = _rot_keys(C, ctx, params, rng, gals)
+    cts = [C.RnsCiphertext(C.to_device(rand_ct(rng, q, n)), 40) for _ in range(3)]
+    got = ctx.rotate_hoisted(cts, keys)
+    for i, ct in enumerate(cts):
+        for r, k in enumerate(keys):
+            want = ctx.rotate(ct, k)
+            assert (got[i][r].level, got[i][r].scale_bits) == (want.level, want.scale_bits)
+            assert np.array_equal(got[i][r].numpy(), want.numpy()), (i, r)
+
+
+def test_hoisted_rotation_of_a_balanced_digit_tie(C, small):
+    """Coefficients whose centred value has a base-2^30 digit at exactly 2^29 (the balanced rule's tie, where
+    the digits of -X are not the negated digits of X) moved with a sign flip by the conjugation: the hoisted
+    call must still equal the ordinary rotation."""
+    params, ctx = small
+    n, q = params.poly_degree, params.q_moduli()
+    rng = np.random.default_rng(6)
+    keys = _rot_keys(C, ctx, params, rng, [ctx.conjugation_galois_element(), ctx.galois_element_for_rotation(3)])
+    a = rand_ct(rng, q, n)
+    for j, X in ((1, 1 << 29), (2, (1 << 29) + (5 << 30)), (3, -(1 << 29)), (7, 3 << 59)):
+        for limb, m in enumerate(q):
+            a[1][limb][j] = X % m
+    cts = [C.RnsCiphertext(C.to_device(a), 40), C.RnsCiphertext(C.to_device(rand_ct(rng, q, n)), 40)]
+    got = ctx.rotate_hoisted(cts, keys)
+    for i, ct in enumerate(cts):
+        for r, k in enumerate(keys):
+            assert np.array_equal(got[i][r].numpy(), ctx.rotate(ct, k).numpy()), (i, r)
