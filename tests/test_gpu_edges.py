@@ -151,3 +151,25 @@ def test_hoisted_rotation_of_a_balanced_digit_tie(C, small):
     for i, ct in enumerate(cts):
         for r, k in enumerate(keys):
             assert np.array_equal(got[i][r].numpy(), ctx.rotate(ct, k).numpy()), (i, r)
+
+
+def test_hoisted_rotations_fall_back_where_they_cannot_hoist(C, pkg):
+    """A ring below the wide key product's sizes (N=2^11) and a batch of mixed levels run as ordinary
+    rotations with the same results."""
+    params = pkg.params.hybrid_params(11, 3, 2, 50)
+    ctx = C.RnsCkksContext(params)
+    n, q = params.poly_degree, params.q_moduli()
+    rng = np.random.default_rng(11)
+    keys = _rot_keys(C, ctx, params, rng, [ctx.galois_element_for_rotation(1), ctx.conjugation_galois_element()])
+    cts = [C.RnsCiphertext(C.to_device(rand_ct(rng, q, n)), 40) for _ in range(2)]
+    got = ctx.rotate_hoisted(cts, keys)
+    for i, ct in enumerate(cts):
+        for r, k in enumerate(keys):
+            assert np.array_equal(got[i][r].numpy(), ctx.rotate(ct, k).numpy())
+    params2 = pkg.params.hybrid_params(12, 4, 2, 50)
+    ctx2 = C.RnsCkksContext(params2)
+    q2 = params2.q_moduli()
+    low = C.RnsCiphertext(C.to_device(rand_ct(rng, q2[:3], params2.poly_degree)), 40)
+    top = C.RnsCiphertext(C.to_device(rand_ct(rng, q2, params2.poly_degree)), 40)
+    with pytest.raises(Exception, match="rotation key level must match the ciphertext level"):
+        ctx2.rotate_hoisted([top, low], _rot_keys(C, ctx2, params2, rng, [ctx2.galois_element_for_rotation(1)]))
