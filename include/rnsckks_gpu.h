@@ -73,6 +73,10 @@ typedef struct {
 int rc_context_create(const rc_params* params, rc_context** out);
 void rc_context_destroy(rc_context* ctx);
 const char* rc_last_error(const rc_context* ctx);
+/* Device-side error flags of the library's kernels (no reference counterpart): nonzero when a key-product
+ * launch gave up waiting for its bulk copies (its results are then invalid).  Synchronises the device; clear
+ * != 0 resets the flags. */
+int rc_kernel_errors(int32_t* flags, int32_t clear);
 /* levels(), num_slots(), poly_degree, aux count: context.rs:57-95 */
 int rc_context_info(const rc_context* ctx, uint64_t* poly_degree, uint32_t* levels, uint32_t* aux_count,
                     uint32_t* scale_bits);

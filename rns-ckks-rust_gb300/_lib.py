@@ -107,6 +107,7 @@ SIGNATURES = [
     ("rc_relinearize_batch", ctypes.c_int, [_vp, _u32, _CT, ctypes.POINTER(_vp), _CT, _vp]),
     ("rc_rotate_batch", ctypes.c_int, [_vp, _u32, _CT, ctypes.POINTER(_vp), _CT, _vp]),
     ("rc_rotate_hoisted", ctypes.c_int, [_vp, _u32, _CT, _u32, ctypes.POINTER(_vp), _CT, _vp]),
+    ("rc_kernel_errors", ctypes.c_int, [ctypes.POINTER(_i32), _i32]),
     ("rc_relinearize_rescale_batch", ctypes.c_int, [_vp, _u32, _CT, ctypes.POINTER(_vp), _CT, _vp]),
     ("rc_total_sum_batch", ctypes.c_int, [_vp, _u32, _CT, _u32, ctypes.POINTER(_vp), _u32, _CT, _vp]),
     ("rc_halevi_shoup_batch", ctypes.c_int, [_vp, _u32, _CT, _vp, _u32, ctypes.POINTER(_vp), _u32, _CT, _vp]),

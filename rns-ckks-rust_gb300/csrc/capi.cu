@@ -895,6 +895,13 @@ extern "C" void rc_context_destroy(rc_context* ctx) {
 
 extern "C" const char* rc_last_error(const rc_context*) { return g_err.c_str(); }
 
+extern "C" int rc_kernel_errors(int32_t* flags, int32_t clear) {
+  return guarded([&] {
+    require(flags != nullptr, "arguments must not be null");
+    *flags = wide_kernel_errors(clear != 0);
+  });
+}
+
 extern "C" int rc_context_info(const rc_context* c, uint64_t* n, uint32_t* levels, uint32_t* aux, uint32_t* sb) {
   return guarded([&] {
     require(c != nullptr, "context must not be null");

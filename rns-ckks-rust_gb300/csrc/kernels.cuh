@@ -214,6 +214,9 @@ bool wide_digit_transforms(const WidePrimes& w, int D, int jobs, const int32_t* 
 // X -> X^gal (their NTT-domain permutation: hoisted rotations of one decomposition)
 void wide_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt, uint2* acc,
               int b0, int nb, int bc_max, cudaStream_t s, uint32_t gal = 0);
+// nonzero if a key-product launch timed out waiting for its bulk copies (then its outputs are not valid);
+// reads the device flag (synchronising) and optionally clears it
+int wide_kernel_errors(bool clear);
 // inverse transforms of `polys` consecutive [pair][N] polynomials, in place
 bool wide_inverse(const WidePrimes& w, uint2* data, int polys, cudaStream_t s);
 // coefficient-form key [digits][2][limbs][N] (residues mod the scheme primes) ->

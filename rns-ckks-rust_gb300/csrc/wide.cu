@@ -282,6 +282,24 @@ __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
 }
 
+// Set by a key-product CTA whose bulk copies did not complete within the wait limit (read and cleared by
+// rc_kernel_errors); no such CTA computes.
+__device__ int g_wide_errors = 0;
+
+// Waits for phase `parity` of the mbarrier at shared address bar, at most ~2^22 polls; false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
+  for (uint32_t it = 0; it < (1u << 22); ++it) {
+    uint32_t done;
+    asm volatile(
+        "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
+        : "=r"(done)
+        : "r"(bar), "r"(parity)
+        : "memory");
+    if (done) return true;
+  }
+  return false;
+}
+
 // Hoisted rotations: the digit transforms of sigma_g(d) are those of d permuted, NTT(sigma_g d) at evaluation
 // index k = NTT(d) at k' with 2k'+1 = g (2k+1) mod 2N.  In the bit-reversed storage order the 32 positions of
 // one tile all come from one source tile, permuted among its lanes (the top five bits of k' depend on the
@@ -297,7 +315,7 @@ template <int BC, bool FOLD>
 __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC >= 2 ? 4 : 5))) void k_w_mac(
     WidePrimes w, int D, int key_digits, int total, const uint2* __restrict__ kwt, const uint2* __restrict__ dtt,
     uint2* acc, int b0, int nb, uint32_t gal) {
-  extern __shared__ uint2 dsm[];  // [BC][D][32] digit transforms, then [warps][W_PF][2][32] key ring
+  extern __shared__ __align__(128) uint2 dsm[];  // [BC][D][32] digit transforms, then [warps][W_PF][2][32] key ring
   const int N = 1 << w.log_n, tiles = N >> 5;
   // job groups vary fastest, so the CTAs that stream the same key tile run together and share it in L2
   const int pair = blockIdx.y, xb = blockIdx.z;
@@ -309,23 +327,38 @@ __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC 
   const int stile = (int)(src0 >> 5);
   const int slane = gal > 1 ? (int)(galois_source((uint32_t)xb * 32 + (threadIdx.x & 31), gal, w.log_n) & 31)
                             : (int)(threadIdx.x & 31);
-  // the jobs' digit-transform runs (D * 256 bytes each, contiguous) go to shared memory by asynchronous
-  // 16-byte copies, all in flight at once; jobs past nloc read as zero
+  // the jobs' digit-transform runs (D * 256 bytes each, contiguous, 256-byte aligned) go to shared memory as
+  // one bulk copy per job through the tensor memory accelerator, completing on an mbarrier; jobs past nloc
+  // read as zero.  The wait is bounded: on timeout the kernel records it in g_wide_errors and returns.
   {
-    const int run16 = run / 2;  // 16-byte units per job
+    __shared__ __align__(8) uint64_t mbar;
+    const uint32_t bar = (uint32_t)__cvta_generic_to_shared(&mbar);
     const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(dsm);
-    for (int e = threadIdx.x; e < BC * run16; e += 32 * W_MAC_WARPS) {
-      const int b = e / run16, r = e - b * run16;
-      if (b < nloc) {
-        const uint2* g = dtt + (((size_t)(bstart + b) * 2 + pair) * tiles + stile) * run + 2 * r;
-        asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(sbase + 16u * e), "l"(g) : "memory");
-      } else {
-        reinterpret_cast<uint4*>(dsm)[e] = make_uint4(0, 0, 0, 0);
+    const uint32_t run_bytes = (uint32_t)run * 8u;
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
+      asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    }
+    for (int e = nloc * run + threadIdx.x; e < BC * run; e += 32 * W_MAC_WARPS) dsm[e] = make_uint2(0, 0);
+    __syncthreads();
+    if (threadIdx.x == 0) {
+      asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(run_bytes * (uint32_t)nloc)
+                   : "memory");
+      for (int b = 0; b < nloc; ++b) {
+        const uint2* src = dtt + (((size_t)(bstart + b) * 2 + pair) * tiles + stile) * run;
+        asm volatile(
+            "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+                sbase + (uint32_t)b * run_bytes),
+            "l"(src), "r"(run_bytes), "r"(bar)
+            : "memory");
       }
     }
-    asm volatile("cp.async.wait_all;" ::: "memory");
+    if (!mbar_wait_bounded(bar, 0)) {
+      atomicOr(&g_wide_errors, 1);
+      mbar_wait_bounded(bar, 0);  // the copies in flight, once more with a limit
+      return;
+    }
   }
-  __syncthreads();
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t q0 = pick(w.q, pair, 0), q1 = pick(w.q, pair, 1);
   const u64 bar0 = pick(w.bar, pair, 0), bar1 = pick(w.bar, pair, 1);
@@ -525,6 +558,16 @@ void wide_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2
   else if (want <= 2) launch_w_mac<2, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
   else if (want <= 4) launch_w_mac<4, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
   else launch_w_mac<8, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
+}
+
+int wide_kernel_errors(bool clear) {
+  int v = 0;
+  cudaMemcpyFromSymbol(&v, g_wide_errors, sizeof(int));
+  if (clear && v) {
+    const int zero = 0;
+    cudaMemcpyToSymbol(g_wide_errors, &zero, sizeof(int));
+  }
+  return v;
 }
 
 bool wide_inverse(const WidePrimes& w, uint2* data, int polys, cudaStream_t s) {

@@ -173,3 +173,16 @@ def test_hoisted_rotations_fall_back_where_they_cannot_hoist(C, pkg):
     top = C.RnsCiphertext(C.to_device(rand_ct(rng, q2, params2.poly_degree)), 40)
     with pytest.raises(Exception, match="rotation key level must match the ciphertext level"):
         ctx2.rotate_hoisted([top, low], _rot_keys(C, ctx2, params2, rng, [ctx2.galois_element_for_rotation(1)]))
+
+
+def test_key_products_report_no_copy_timeouts(C, small):
+    """The key product's bulk copies complete within the kernel's bounded wait (the device flag stays 0)."""
+    params, ctx = small
+    n, q = params.poly_degree, params.q_moduli()
+    rng = np.random.default_rng(9)
+    key = ctx.upload_keyswitch_key(_random_key(rng, params, len(q), True)[0], len(q) - 1, 2)
+    cts = [C.RnsCiphertext(C.to_device(rand_ct(rng, q, n)), 40) for _ in range(9)]
+    ctx.mult_relinearized_batch(cts, cts[::-1], [key] * 9)
+    flags = ctypes.c_int32(-1)
+    C.call("rc_kernel_errors", ctypes.byref(flags), 1)
+    assert flags.value == 0
