@@ -441,7 +441,10 @@ void launch_w_mac(const WidePrimes& w, int D, int key_digits, int total, const u
     int dev = 0, optin = 48 * 1024;
     if (cudaGetDevice(&dev) == cudaSuccess)
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
-    cudaFuncSetAttribute(k_w_mac<BC, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize, optin);
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, k_w_mac<BC, FOLD>);  // the static part (the mbarrier) counts against the limit
+    cudaFuncSetAttribute(k_w_mac<BC, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         optin - (int)fa.sharedSizeBytes);
   });
   dim3 g((nb + BC - 1) / BC, 2, (1 << w.log_n) / 32);
   k_w_mac<BC, FOLD><<<g, 32 * W_MAC_WARPS, smem, s>>>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal);
