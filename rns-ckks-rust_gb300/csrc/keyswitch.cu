@@ -30,7 +30,7 @@ namespace {
 // ---------------------------------------------------------------------------
 // decomposition
 // ---------------------------------------------------------------------------
-template <int WM>
+template <int WM, bool TIES>
 __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int limbs, int D, int32_t* digits,
                             u64 g_inv, int log_n, int* tie_flags) {
   const CrtSmem tabs = stage_crt_tables(pc, dt, limbs);
@@ -79,7 +79,7 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
         dig = (int64_t)v;
         carry = 0;
       }
-      tie |= dig == -(1ll << 29);
+      if (TIES) tie |= dig == -(1ll << 29);
       out[(size_t)d * N] = (int32_t)dig;
     }
   }
@@ -96,10 +96,10 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
       dig = (int64_t)v;
       carry = 0;
     }
-    tie |= dig == -(1ll << 29);
+    if (TIES) tie |= dig == -(1ll << 29);
     out[(size_t)d * N] = (int32_t)dig;
   }
-  if (tie && tie_flags) atomicOr(&tie_flags[job], 1);
+  if (TIES && tie) atomicOr(&tie_flags[job], 1);
 }
 
 // lift_poly_to_context (keyswitching.rs:242-276) for polynomial blockIdx.y: the Q limbs are copied and limb
@@ -800,6 +800,14 @@ __global__ void k_key_relayout(const PrimeConst* pc, const u64* src, u64* dst, i
 
 }  // namespace
 
+template <int WM>
+void launch_decompose(dim3 g, int threads, size_t smem, cudaStream_t s, const PrimeConst* pc, const DecompTab& dt,
+                      const PtrTab& src, int limbs, int D, int32_t* digits, uint64_t g_inv, int log_n,
+                      int* tie_flags) {
+  if (tie_flags) k_decompose<WM, true><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else k_decompose<WM, false><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, nullptr);
+}
+
 void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int jobs, int limbs, int D,
                int32_t* digits, uint64_t g_inv, int log_n, cudaStream_t s, int* tie_flags) {
   if (jobs <= 0) return;
@@ -810,14 +818,14 @@ void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int
   ProfScope p("decompose", s);
   // the word count is a template parameter (register-resident value); the closest instance above W runs
   const size_t smem = crt_smem_bytes(limbs, W);
-  if (W <= 4) k_decompose<4><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else if (W <= 8) k_decompose<8><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else if (W <= 12) k_decompose<12><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else if (W <= 16) k_decompose<16><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else if (W <= 20) k_decompose<20><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else if (W <= 24) k_decompose<24><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else if (W <= 32) k_decompose<32><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else k_decompose<64><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  if (W <= 4) launch_decompose<4>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else if (W <= 8) launch_decompose<8>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else if (W <= 12) launch_decompose<12>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else if (W <= 16) launch_decompose<16>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else if (W <= 20) launch_decompose<20>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else if (W <= 24) launch_decompose<24>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else if (W <= 32) launch_decompose<32>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  else launch_decompose<64>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
 }
 
 void lift_to_aux(const PrimeConst* pc, const PrimeConst* ppc, const DecompTab& dt, const u64* src, u64* dst,
