@@ -259,7 +259,8 @@ int rc_rotate_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* ct, co
  * ("hoisted"; the baby steps of linear_transform.rs:213-232 rotate one input by 1..b-1).  Results equal
  * rc_rotate's residue for residue: an input whose decomposition holds a digit at -2^29 (where the digits of a
  * negated coefficient are not the negated digits) is rotated the ordinary way.  Mixed levels or key shapes
- * run as rc_rotate_batch. */
+ * run as rc_rotate_batch.  Reading those flags synchronises the stream once per 32 inputs, so the call is not
+ * capturable in a CUDA graph (neither is rc_bsgs_apply_batch, which uses it for its baby steps). */
 int rc_rotate_hoisted(rc_context* ctx, uint32_t count, const rc_ciphertext* ct, uint32_t nrot,
                       const rc_ksk* const* keys, rc_ciphertext* out, void* stream);
 /* relinearize then rescale (context/ops.rs:111-122 followed by context/ops.rs:32-37) for `count`
