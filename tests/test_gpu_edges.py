@@ -186,3 +186,16 @@ def test_key_products_report_no_copy_timeouts(C, small):
     flags = ctypes.c_int32(-1)
     C.call("rc_kernel_errors", ctypes.byref(flags), 1)
     assert flags.value == 0
+
+
+def test_hoisted_rotations_past_one_launch(C, small):
+    """34 ciphertexts: two chunks of the hoisted path (32 jobs per key-product launch)."""
+    params, ctx = small
+    n, q = params.poly_degree, params.q_moduli()
+    rng = np.random.default_rng(34)
+    keys = _rot_keys(C, ctx, params, rng, [ctx.galois_element_for_rotation(s) for s in (1, -3)])
+    cts = [C.RnsCiphertext(C.to_device(rand_ct(rng, q, n)), 40) for _ in range(34)]
+    got = ctx.rotate_hoisted(cts, keys)
+    for i in (0, 31, 32, 33):
+        for r, k in enumerate(keys):
+            assert np.array_equal(got[i][r].numpy(), ctx.rotate(cts[i], k).numpy()), (i, r)
