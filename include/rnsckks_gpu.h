@@ -87,7 +87,7 @@ int rc_decomp_digits(const rc_context* ctx, int32_t level, uint32_t* digits);
 int rc_reserve(rc_context* ctx, int32_t max_level, uint32_t max_batch, void* stream);
 
 /* Tunables (no reference counterpart; results never depend on them): "ks_jobs" (jobs per key-switch
- * launch, 1..32, default 32), "mac_bc" (most jobs per CTA of the key product: 1, 2, 4, 8), "host_chunk" (jobs
+ * launch, 1..64, default 32), "mac_bc" (most jobs per CTA of the key product: 1, 2, 4, 8), "host_chunk" (jobs
  * per stage of the pipelined host-buffer entry, default 8), "host_edge" (its first and last stages have
  * host_chunk / host_edge jobs, default 2), "lazy_ntt" (unreduced forward butterflies, only
  * when every prime is below 2^58), "fuse_tensor" (forward row phase + tensor + inverse row phase of a

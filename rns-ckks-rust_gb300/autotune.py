@@ -18,7 +18,7 @@ from typing import Callable, Dict, Iterable, List, Optional, Sequence
 
 from ._lib import RcCiphertext, call
 
-DEVICE_CANDIDATES: Dict[str, Sequence[int]] = {"ks_jobs": (8, 16, 32), "mac_bc": (4, 8), "lazy_ntt": (0, 1),
+DEVICE_CANDIDATES: Dict[str, Sequence[int]] = {"ks_jobs": (8, 16, 32, 64), "mac_bc": (4, 8), "lazy_ntt": (0, 1),
                                                "fuse_tensor": (0, 1)}
 # host_edge: the first and last stages have chunk / host_edge jobs (a shorter fill and drain against one more
 # stage's overhead)

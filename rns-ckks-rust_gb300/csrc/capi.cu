@@ -924,7 +924,7 @@ extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
     require(c && name, "arguments must not be null");
     const std::string n(name);
     if (n == "ks_jobs") {
-      require(value >= 1 && value <= MAXP / 2, "ks_jobs must be in 1..32");
+      require(value >= 1 && value <= MAXP / 2, "ks_jobs must be in 1.." + std::to_string(MAXP / 2));
       c->ks_jobs = value;
     } else if (n == "mac_bc") {
       require(value == 1 || value == 2 || value == 4 || value == 8, "mac_bc must be 1, 2, 4 or 8");

@@ -23,7 +23,7 @@ struct ProfScope {
 // Up to MAXP polynomials per launch, addressed through a by-value pointer table
 // (kernel parameters, so launches need no extra upload and can be captured in
 // CUDA graphs).  Limb j of polynomial k lives at p[k] + j * N.
-constexpr int MAXP = 64;
+constexpr int MAXP = 128;
 struct PtrTab {
   u64* p[MAXP];
 };
