@@ -54,7 +54,7 @@ def test_tuning_keeps_results_and_applies_choice(pkg, T, tmp_path):
     outs = [torch.empty((2, len(q) - 1, n), dtype=torch.int64, device="cuda") for _ in range(12)]
     rep = T.tune_mult_relinearized(ctx, lhs, rhs, [key] * 12, outs, reps=1, cache=tmp_path / "t.json")
     assert not rep["cached"] and T.current(ctx, rep["choice"]) == rep["choice"]
-    assert len(rep["trials"]) == 24  # 3 x 2 x 2 x 2 candidates, all primes below 2^58
+    assert len(rep["trials"]) == 32  # 4 x 2 x 2 x 2 candidates, all primes below 2^58
     for o, r in zip(ctx.mult_relinearized_batch(lhs, rhs, [key] * 12), ref):
         assert np.array_equal(o.numpy(), r)
     again = T.tune_mult_relinearized(ctx, lhs, rhs, [key] * 12, outs, reps=1, cache=tmp_path / "t.json")
@@ -62,4 +62,4 @@ def test_tuning_keeps_results_and_applies_choice(pkg, T, tmp_path):
     with pytest.raises(C.RcError, match="unknown tunable"):
         T.apply(ctx, {"nope": 1})
     with pytest.raises(C.RcError, match="ks_jobs must be"):
-        T.apply(ctx, {"ks_jobs": 33})
+        T.apply(ctx, {"ks_jobs": 65})
