@@ -889,7 +889,9 @@ void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const
               cudaStream_t s) {
   if (jobs <= 0) return;
   const int N = f.n;
-  const int threads = N < 128 ? N : 128;
+  // batches: one staging of the limb constants per 256 coefficients; a few jobs: smaller blocks fill the SMs
+  const int tpb = jobs >= 8 ? 256 : 128;
+  const int threads = N < tpb ? N : tpb;
   dim3 g((N + threads - 1) / threads, 2 * jobs);
   ProfScope p("finalize", s);
   const size_t smem = (size_t)(f.qlimbs + f.K) * ft_stride(f.K) * sizeof(u64);
