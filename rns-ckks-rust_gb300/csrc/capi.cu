@@ -431,11 +431,17 @@ void tensor_core(rc_context* c, const std::vector<const uint64_t*>& lhs, const s
   }
   ntt_forward(c->ntt(), src, dst, 4 * J, limbs, qmap(c, limbs), s);
   launch_check("ntt_forward(tensor)");
-  tensor_ntt(c->d_pc, dst, o3, J, limbs, c->N, s);
-  launch_check("tensor");
   // the tensor's Montgomery products carry a factor 2^-64, taken out by the inverse transform's scale
   NttArgs inv = c->ntt();
   inv.mont_out = 1;
+  if (tensor_inverse_rows(inv, dst, o3, J, limbs, qmap(c, limbs), s)) {
+    launch_check("tensor + inverse rows");
+    require(ntt_inverse_cols(inv, o3, 3 * J, limbs, qmap(c, limbs), s), "internal: inverse columns unsupported");
+    launch_check("ntt_inverse(tensor) columns");
+    return;
+  }
+  tensor_ntt(c->d_pc, dst, o3, J, limbs, c->N, s);
+  launch_check("tensor");
   ntt_inverse(inv, o3, o3, 3 * J, limbs, qmap(c, limbs), s);
   launch_check("ntt_inverse(tensor)");
 }

@@ -55,6 +55,14 @@ void ntt_forward(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int pol
 void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
                  cudaStream_t s);
 
+// NTT-domain (a0, a1, b0, b1) = in4.p[4j..4j+3] -> out3.p[3j..3j+2] = the inverse row phase of (a0 b0,
+// a0 b1 + a1 b0, a1 b1) as Montgomery products; ntt_inverse_cols with NttArgs::mont_out then completes the
+// inverse transform.  False (nothing launched) if N is not supported (log N outside 12..16).
+bool tensor_inverse_rows(const NttArgs& a, const PtrTab& in4, const PtrTab& out3, int jobs, int limbs, LimbMap map,
+                         cudaStream_t s);
+// the inverse transform's column phase alone (in place, times N^-1), after a row phase done elsewhere
+bool ntt_inverse_cols(const NttArgs& a, const PtrTab& data, int polys, int limbs, LimbMap map, cudaStream_t s);
+
 // Coefficient-form ciphertext pairs in4.p[4j..4j+3] = (a0, a1, b0, b1) -> coefficient-form
 // out3.p[3j..3j+2] = (a0 b0, a0 b1 + a1 b0, a1 b1): forward column phase into work4, one fused kernel for the
 // forward row phase, the NTT-domain tensor and the inverse row phase, then the inverse column phase in place.

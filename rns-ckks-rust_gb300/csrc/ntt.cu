@@ -349,6 +349,84 @@ void inv_fast(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys,
   }
 }
 
+// The tensor and the inverse row phase in one pass: for each job of the block, d0 = a0 b0, d1 = a0 b1 + a1 b0
+// and d2 = a1 b1 (Montgomery products of the forward transforms in4[4j..4j+3]; the inverse column pass's scale
+// takes out their 2^-64) go straight into the inverse row transform, so the quadratic NTT-domain values never
+// reach HBM.  A block transforms the same rows of TENSOR_ROW_JOBS jobs (three outputs each) with one twiddle
+// staging.
+constexpr int TENSOR_ROW_JOBS = 2;
+
+template <int M1, int M2>
+__global__ __launch_bounds__(32 * ROW_WARPS) void k_tensor_inv_rows(NttArgs a, PtrTab in4, PtrTab out3, LimbMap map,
+                                                                    int jobs) {
+  using G = core::Geo<M2>;
+  constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = ROW_WARPS * G::SUBS;
+  __shared__ u64 bufs[ROWS * G::STRIDE];
+  __shared__ __align__(16) Twiddle twl[ROWS][N2];
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int sub = lane / G::LANES, l = lane % G::LANES;
+  const int row0 = blockIdx.x * ROWS;
+  const int limb = blockIdx.y, first = blockIdx.z * TENSOR_ROW_JOBS, count = min(TENSOR_ROW_JOBS, jobs - first);
+  const int prime = map.prime(limb);
+  const PrimeConst& pc = a.pc[prime];
+  const Twiddle* twg = a.tw_inv + (size_t)prime * N;
+  const int rl = warp * G::SUBS + sub, row = row0 + rl;
+  const size_t off = (size_t)limb * N + (size_t)row * N2;
+  u64* buf = bufs + rl * G::STRIDE;
+  // the first job's products are formed before the twiddle tables land, so both latencies overlap
+  u64 d[3][8];
+  auto products = [&](int j) {
+    const u64 *x0 = in4.p[4 * j] + off, *x1 = in4.p[4 * j + 1] + off;
+    const u64 *y0 = in4.p[4 * j + 2] + off, *y1 = in4.p[4 * j + 3] + off;
+#pragma unroll
+    for (int k = 0; k < 8; ++k) {
+      const int x = core::last_idx<M2>(l, k);
+      const u64 a0 = x0[x], a1 = x1[x], b0 = y0[x], b1 = y1[x];
+      d[0][k] = mont_reduce(mul_wide(a0, b0), pc);
+      U128 m = mul_wide(a0, b1);
+      add_to(m, mul_wide(a1, b0));
+      d[1][k] = mont_reduce(m, pc);
+      d[2][k] = mont_reduce(mul_wide(a1, b1), pc);
+    }
+  };
+  products(first);
+#pragma unroll 1
+  for (int rr = 0; rr < ROWS; ++rr)
+    core::stage_twiddles_async<M2>(twl[rr], twg, (u64)(N1 + row0 + rr), threadIdx.x, 32 * ROW_WARPS);
+  core::cp_async_wait_all();
+  __syncthreads();
+#pragma unroll 1
+  for (int t = 0; t < count; ++t) {
+    const int j = first + t;
+    if (t > 0) products(j);
+#pragma unroll
+    for (int o = 0; o < 3; ++o) {
+      core::inv_sub<M2>(d[o], buf, l, twl[rl], pc.q);
+      u64* out = out3.p[3 * j + o] + off;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) out[core::first_idx<M2>(l, k)] = d[o][k];
+      __syncwarp();  // the warp's buffer is reused by the next transform
+    }
+  }
+}
+
+template <int M1, int M2>
+void tensor_inv_rows_fast(const NttArgs& a, const PtrTab& in4, const PtrTab& out3, int jobs, int limbs, LimbMap map,
+                          cudaStream_t s) {
+  constexpr int N1 = 1 << M1;
+  dim3 g(N1 / (ROW_WARPS * core::Geo<M2>::SUBS), limbs, (jobs + TENSOR_ROW_JOBS - 1) / TENSOR_ROW_JOBS);
+  ProfScope p("tensor_inv_rows", s);
+  k_tensor_inv_rows<M1, M2><<<g, 32 * ROW_WARPS, 0, s>>>(a, in4, out3, map, jobs);
+}
+
+template <int M1, int M2>
+void inv_cols_fast(const NttArgs& a, const PtrTab& data, int polys, int limbs, LimbMap map, cudaStream_t s) {
+  constexpr int N2 = 1 << M2;
+  dim3 g1(N2 / ColTile<M1>::COLS, limbs, polys);
+  ProfScope p("ntt_inv_cols", s);
+  k_cols_f<M1, M2, false, false><<<g1, 256, 0, s>>>(a, data, data, map);
+}
+
 template <bool LAZY>
 bool fwd_dispatch(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
                   cudaStream_t s) {
@@ -536,6 +614,29 @@ void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int pol
   {
     ProfScope p("ntt_inv_cols", s);
     k_inv_cols<<<g1, threads_for(N1 * COLS / 2), N1 * COLS * sizeof(u64), s>>>(a, dst, dst, map);
+  }
+}
+
+bool tensor_inverse_rows(const NttArgs& a, const PtrTab& in4, const PtrTab& out3, int jobs, int limbs, LimbMap map,
+                         cudaStream_t s) {
+  switch (a.log_n) {
+    case 12: tensor_inv_rows_fast<6, 6>(a, in4, out3, jobs, limbs, map, s); return true;
+    case 13: tensor_inv_rows_fast<6, 7>(a, in4, out3, jobs, limbs, map, s); return true;
+    case 14: tensor_inv_rows_fast<7, 7>(a, in4, out3, jobs, limbs, map, s); return true;
+    case 15: tensor_inv_rows_fast<7, 8>(a, in4, out3, jobs, limbs, map, s); return true;
+    case 16: tensor_inv_rows_fast<8, 8>(a, in4, out3, jobs, limbs, map, s); return true;
+    default: return false;
+  }
+}
+
+bool ntt_inverse_cols(const NttArgs& a, const PtrTab& data, int polys, int limbs, LimbMap map, cudaStream_t s) {
+  switch (a.log_n) {
+    case 12: inv_cols_fast<6, 6>(a, data, polys, limbs, map, s); return true;
+    case 13: inv_cols_fast<6, 7>(a, data, polys, limbs, map, s); return true;
+    case 14: inv_cols_fast<7, 7>(a, data, polys, limbs, map, s); return true;
+    case 15: inv_cols_fast<7, 8>(a, data, polys, limbs, map, s); return true;
+    case 16: inv_cols_fast<8, 8>(a, data, polys, limbs, map, s); return true;
+    default: return false;
   }
 }
 
