@@ -1,0 +1,101 @@
+"""Python models of integer tricks the CUDA kernels rely on, checked exhaustively or on random inputs against
+exact arithmetic (CPU only).
+
+* the centred CRT's quotient estimate: each term y/q in 32-bit fixed point, truncated, at most 3 units of
+  2^-31 below its value, so floor(sum) is exact or one low (the kernel's correction handles one);
+* the BSGS inner sums' split products: x = x1 2^26 + x0, three 32x32->64 products per term summed in 64-bit
+  columns, recombined and reduced once, equal sum(x y) mod q for primes below 2^52 and up to 16 terms;
+* the lazy finalize's negated-constant Shoup companions: floor((q - w) 2^64 / q) = 2^64 - 1 - floor(w 2^64 / q).
+"""
+import random
+
+import pytest
+
+M64 = (1 << 64) - 1
+
+
+def _primes(bits, count, n=1 << 16):
+    import importlib.util
+    import sys
+    from pathlib import Path
+    root = Path(__file__).resolve().parent.parent
+    if "rnsckks_gb300" not in sys.modules:
+        spec = importlib.util.spec_from_file_location("rnsckks_gb300", root / "rns-ckks-rust_gb300" / "__init__.py",
+                                                      submodule_search_locations=[str(root / "rns-ckks-rust_gb300")])
+        mod = importlib.util.module_from_spec(spec)
+        sys.modules["rnsckks_gb300"] = mod
+        spec.loader.exec_module(mod)
+    from rnsckks_gb300 import params
+    return [q for q, _ in params.find_ntt_primes(n, bits, count)]
+
+
+def _fx(q):
+    """(n << 32) | floor(2^95 / (q << n)), n = 64 - bits(q): the table entry the library stores per prime."""
+    n = 64 - q.bit_length()
+    return n, (1 << 95) // (q << n)
+
+
+def _term(y, n, r):
+    """umulhi32((y << n) >> 32, r): the kernel's fixed-point y / q * 2^31."""
+    yh = ((y << n) & M64) >> 32
+    return (yh * r) >> 32
+
+
+@pytest.mark.parametrize("bits", [30, 41, 50, 60, 61])
+def test_fixed_point_quotient_terms_are_at_most_three_units_low(bits):
+    rng = random.Random(bits)
+    for q in _primes(bits, 3):
+        n, r = _fx(q)
+        assert r < 1 << 32
+        for y in [0, 1, q - 1, q // 2, q // 2 + 1] + [rng.randrange(q) for _ in range(2000)]:
+            exact_units = (y << 31) / q  # the value in units of 2^-31
+            f = _term(y, n, r)
+            assert f <= exact_units and exact_units - f < 3, (q, y)
+
+
+def test_fixed_point_quotient_floor_is_exact_or_one_low():
+    rng = random.Random(7)
+    qs = _primes(50, 24)
+    for _ in range(3000):
+        ys = [rng.randrange(q) for q in qs]
+        fsum = sum(_term(y, *_fx(q)) for y, q in zip(ys, qs))
+        k = fsum >> 31
+        exact = sum(__import__("fractions").Fraction(y, q) for y, q in zip(ys, qs))
+        assert k in (int(exact), int(exact) - 1)
+
+
+def _split_sum(xs, ys, q):
+    """The k_bsgs_inner split-26 path: three 32x32 products per term in 64-bit columns, then one reduction."""
+    mask = (1 << 26) - 1
+    p00 = p11 = pk = 0
+    for x, y in zip(xs, ys):
+        x0, x1, y0, y1 = x & mask, x >> 26, y & mask, y >> 26
+        p00 = (p00 + x0 * y0) & M64
+        p11 = (p11 + x1 * y1) & M64
+        pk = (pk + (x0 + x1) * (y0 + y1)) & M64
+    cross = (pk - p00 - p11) & M64
+    t = p00 + (cross << 26) + (p11 << 52)  # the 128-bit value the kernel assembles
+    assert t < q << 64  # Barrett's precondition
+    return t % q
+
+
+@pytest.mark.parametrize("bits", [30, 41, 50, 52])
+def test_bsgs_split_products_equal_the_modular_sum(bits):
+    rng = random.Random(bits + 100)
+    for q in _primes(bits, 2):
+        assert q < 1 << 52
+        for terms in (1, 2, 12, 16):
+            for _ in range(200):
+                xs = [rng.randrange(q) for _ in range(terms)]
+                ys = [rng.randrange(q) for _ in range(terms)]
+                assert _split_sum(xs, ys, q) == sum(x * y for x, y in zip(xs, ys)) % q
+            worst = [q - 1] * terms
+            assert _split_sum(worst, worst, q) == (terms * (q - 1) ** 2) % q
+
+
+def test_negated_shoup_companion():
+    rng = random.Random(3)
+    for q in _primes(50, 2) + _primes(60, 2):
+        for w in [1, 2, q - 1, q // 2] + [rng.randrange(1, q) for _ in range(500)]:
+            ws = (w << 64) // q
+            assert ((q - w) << 64) // q == M64 - ws
