@@ -28,7 +28,12 @@ namespace rc {
 namespace {
 
 constexpr int W_ROW_WARPS = 4;
-constexpr int W_MAC_WARPS = 8;
+// warps per key-product CTA: 8 for job groups (two CTAs per SM); one job per CTA (the per-op path, bound by the
+// key stream) takes 13, more loads in flight per SM
+template <int BC>
+__host__ __device__ constexpr int w_mac_warps() {
+  return BC == 1 ? 13 : 8;
+}
 
 // entry 2 * pair + k of a four-entry table in the kernel parameter, picked by a select: a dynamic index
 // would copy the whole parameter struct to local memory
@@ -312,7 +317,7 @@ __device__ __forceinline__ uint32_t galois_source(uint32_t x, uint32_t g, int lo
 }
 
 template <int BC, bool FOLD>
-__global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC >= 2 ? 4 : 5))) void k_w_mac(
+__global__ __launch_bounds__(32 * w_mac_warps<BC>(), BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC >= 2 ? 4 : 3))) void k_w_mac(
     WidePrimes w, int D, int key_digits, int total, const uint2* __restrict__ kwt, const uint2* __restrict__ dtt,
     uint2* acc, int b0, int nb, uint32_t gal) {
   extern __shared__ __align__(128) uint2 dsm[];  // [BC][D][32] digit transforms, then [warps][W_PF][2][32] key ring
@@ -339,7 +344,7 @@ __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC 
       asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(bar) : "memory");
       asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
     }
-    for (int e = nloc * run + threadIdx.x; e < BC * run; e += 32 * W_MAC_WARPS) dsm[e] = make_uint2(0, 0);
+    for (int e = nloc * run + threadIdx.x; e < BC * run; e += 32 * w_mac_warps<BC>()) dsm[e] = make_uint2(0, 0);
     __syncthreads();
     if (threadIdx.x == 0) {
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(run_bytes * (uint32_t)nloc)
@@ -367,7 +372,7 @@ __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC 
   uint2* ring = dsm + (size_t)BC * run + (size_t)warp * W_PF * 64 + lane;
   const uint32_t rs = (uint32_t)__cvta_generic_to_shared(ring);
 #pragma unroll 1
-  for (int j = warp; j < total; j += W_MAC_WARPS) {
+  for (int j = warp; j < total; j += w_mac_warps<BC>()) {
     const uint2* kp = kwt + (((size_t)j * 2 + pair) * tiles + xb) * krun + lane;
     u64 a0[BC], a1[BC], c0[BC], c1[BC];
 #pragma unroll
@@ -434,7 +439,7 @@ __global__ __launch_bounds__(32 * W_MAC_WARPS, BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC 
 template <int BC, bool FOLD>
 void launch_w_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt,
                   uint2* acc, int b0, int nb, uint32_t gal, cudaStream_t s) {
-  const size_t smem = ((size_t)BC * D * 32 + (size_t)W_MAC_WARPS * W_PF * 64) * sizeof(uint2);
+  const size_t smem = ((size_t)BC * D * 32 + (size_t)w_mac_warps<BC>() * W_PF * 64) * sizeof(uint2);
   // the opt-in limit is set once per instance, before any launch of it (callers on several host threads)
   static std::once_flag once;
   std::call_once(once, [] {
@@ -447,7 +452,7 @@ void launch_w_mac(const WidePrimes& w, int D, int key_digits, int total, const u
                          optin - (int)fa.sharedSizeBytes);
   });
   dim3 g((nb + BC - 1) / BC, 2, (1 << w.log_n) / 32);
-  k_w_mac<BC, FOLD><<<g, 32 * W_MAC_WARPS, smem, s>>>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal);
+  k_w_mac<BC, FOLD><<<g, 32 * w_mac_warps<BC>(), smem, s>>>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal);
 }
 
 // coefficient-form key [digits][2][limbs][N] -> kw[((j * digits + i) * 2 + c)][pair][N]
