@@ -15,6 +15,8 @@ A step is one batched call over the B pairs (rc_mult_relinearized_batch).
 `--impl reference` times the CPU restatement of the reference path (the
 oracle, faithful mode: per-call NTT round trips, u128 % arithmetic, Garner
 gadget) on the host's cores on the same workload.
+`--extra-only bsgs_matvec|bootstrap [--extra-batch B]` runs one of the extra
+workloads alone and prints its JSON object (the profiling cases of profiles/).
 Multi-GPU: replicas only (each rank runs its own batch; no collective on the
 data path), launched by torchrun.
 """
