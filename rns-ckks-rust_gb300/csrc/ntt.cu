@@ -260,7 +260,7 @@ __global__ __launch_bounds__(256, 3) void k_cols_f(NttArgs a, PtrTab src, PtrTab
 constexpr int ROW_WARPS = 4;
 // polynomials per row block: the same rows (and limb) of ROW_POLYS polynomials share one staging of the rows'
 // twiddles, which take as many bytes as two rows of data
-constexpr int ROW_POLYS = 8;
+constexpr int ROW_POLYS = 16;
 
 // Row phase: each warp transforms SUBS rows of 2^M2 contiguous residues of polynomials
 // blockIdx.z * ROW_POLYS .. below `polys`, loading the next polynomial's rows while transforming the current
@@ -354,7 +354,7 @@ void inv_fast(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys,
 // takes out their 2^-64) go straight into the inverse row transform, so the quadratic NTT-domain values never
 // reach HBM.  A block transforms the same rows of TENSOR_ROW_JOBS jobs (three outputs each) with one twiddle
 // staging.
-constexpr int TENSOR_ROW_JOBS = 2;
+constexpr int TENSOR_ROW_JOBS = 4;
 
 template <int M1, int M2>
 __global__ __launch_bounds__(32 * ROW_WARPS) void k_tensor_inv_rows(NttArgs a, PtrTab in4, PtrTab out3, LimbMap map,

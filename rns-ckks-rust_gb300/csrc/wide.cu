@@ -115,7 +115,7 @@ __global__ __launch_bounds__(256, 2) void k_w_cols_fwd(WidePrimes w, const void*
 // Row kernels: a block transforms the same ROWS rows of W_ROW_POLYS consecutive polynomials, so each row's
 // twiddles (as many bytes as two rows of data) are staged once for all of them; the next polynomial's rows
 // are loaded while the current one is transformed.
-constexpr int W_ROW_POLYS = 8;
+constexpr int W_ROW_POLYS = 16;
 
 // Forward row phase of data[poly][pair][N] (polys p0 + blockIdx.z * W_ROW_POLYS .. below p0 + cnt), outputs
 // reduced to [0, q).  TILED: written as dtt[job][pair][x/32][digit][32] with poly = job * D + digit;
