@@ -204,39 +204,43 @@ def cpu_oracle_op(O, params, lhs_np, rhs_np, key_np, threads: int):
 JOBS_PER_LAUNCH = 32
 
 
-# algorithmic bytes per launch for the kernels the roofline may name
-def algorithmic_bytes(kernel: str, batch: int, n: int, limbs: int, aux: int, digits: int, launches: int):
+def hmult_algorithmic_bytes(n, limbs, aux, digits, sharing=1):
+    """Algorithmic bytes of one HMult+relin (mult_relinearized): the two input ciphertexts read once
+    (4 limbs*N*8), the output ciphertext written once (2 (limbs-1) N*8) and the relinearization key in the
+    reference's form (digits x 2 components x (limbs + aux) limbs of u64 residues) read once per `sharing`
+    ops that use it in one launch.  Intermediates (NTT-domain copies, digits, products) are not counted."""
+    return 4 * limbs * n * 8 + 2 * (limbs - 1) * n * 8 + digits * 2 * (limbs + aux) * n * 8 / sharing
+
+
+def kernel_algorithmic_bytes(batch: int, n: int, limbs: int, aux: int, digits: int, launches: int):
+    """Algorithmic bytes per launch of a kernel of the HMult+relin step: the per-op figure above times the
+    ops one launch processes (every kernel of the step covers all jobs of its launch), with the key counted
+    once per launch."""
+    if launches == 0:
+        return None
+    jobs = batch / launches
+    return hmult_algorithmic_bytes(n, limbs, aux, digits, jobs) * jobs
+
+
+def kernel_traffic_breakdown(kernel: str, jobs: int, n: int, limbs: int, aux: int, digits: int):
+    """Bytes the kernel moves by its design (what ncu's DRAM counters should show), itemised: the wide key
+    (four 29-bit residues per coefficient, twice the reference form) and the intermediates the step keeps in
+    HBM between kernels."""
     ext = limbs + aux
     if kernel == "wide_mac":
-        # key product under the two 55-bit internal primes: the NTT-domain key (ext limbs x 2 primes x
-        # digits x 2 components) once per launch, the digit transforms (digits x 2 primes) of every job in,
-        # the exact products (ext limbs x 2 components x 2 primes) of every job out
-        key = ext * 2 * digits * 2 * n * 8
-        per_job = digits * 2 * n * 8 + ext * 2 * 2 * n * 8
-        return key + per_job * batch / launches
-    per_job = {
-        # digit column pass of the wide product: int32 digits in, residues under 2 primes out
-        "wide_digit_cols": digits * n * 4 + digits * 2 * n * 8,
-        # digit NTT row pass + key product: key (2 comps, all digits, extended basis) in, accumulators out
-        "digit_rows_mac": digits * 2 * ext * n * 8 + 2 * ext * n * 8,
-        # digit column pass: int32 digits in, per (digit, limb) residues out (counted as the
-        # algorithmic half of each digit transform: N*8 per digit per limb)
-        "digit_cols": digits * n * 4 + digits * ext * n * 8,
-        "decompose": limbs * n * 8 + digits * n * 4,
-        "finalize": 2 * ext * n * 8 + 2 * limbs * n * 8 + 2 * (limbs - 1) * n * 8,
-        "tensor": 4 * limbs * n * 8 + 3 * limbs * n * 8,
-        # one phase of a transform reads and writes the limb once: half of 2*N*8 per transform
-        "ntt_fwd_cols": 4 * limbs * n * 8, "ntt_fwd_rows": 4 * limbs * n * 8,
-        "ntt_inv_rows": (3 * limbs + 2 * ext) * n * 8, "ntt_inv_cols": (3 * limbs + 2 * ext) * n * 8,
-    }.get(kernel)
-    if per_job is None or launches == 0:
-        return None
-    return per_job * batch / launches
+        return {"wide_key": ext * 2 * digits * 2 * n * 8, "digit_transforms_in": jobs * digits * 2 * n * 8,
+                "products_out": jobs * 2 * ext * 2 * n * 8}
+    return None
 
 
-def hmult_algorithmic_bytes(n, limbs, aux, digits, sharing=1):
-    """HMult+relin: 2 input ciphertexts, 1 output ciphertext, the key read once per `sharing` ops."""
-    return 4 * limbs * n * 8 + 2 * (limbs - 1) * n * 8 + digits * 2 * (limbs + aux) * n * 8 / sharing
+def workload_config(n, limbs, aux, digits, batch, world):
+    """The workload both arms report (the reference arm samples one op of this batch per step)."""
+    return {"workload": "mult_relinearized (tensor+relinearize+rescale), hybrid keyswitch",
+            "poly_degree": n, "limbs": limbs, "aux_limbs": aux, "prime_bits": 50,
+            "gadget": "balanced base-2^30", "digits": digits, "batch": batch,
+            "parallelism": f"replicas x{world}",
+            "l2": "no flush: each step reads ~%.1f GB of inputs and key (L2 129 MB)"
+                  % ((batch * 4 * limbs + digits * 2 * (limbs + aux)) * n * 8 / 1e9)}
 
 
 def peaks():
@@ -355,9 +359,19 @@ def run_gpu(args):
     tune_host = T.tune_host_pipeline(ctx, e2e_step, limbs - 1, B, reps=3)
     e2e_step()
     torch.cuda.synchronize()
-    # seven timed rounds of e_steps steps each; the host link of a shared machine slows down now and then for
-    # tens of milliseconds (seen as single 2-4x slow trials in the tuner), so the median round is reported and
-    # every round is listed
+    # the headline e2e: exactly `steps` consecutive steps, the same protocol as `value`
+    barrier(world)
+    torch.cuda.synchronize()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(stream)
+    for _ in range(args.steps):
+        e2e_step()
+    e1.record(stream)
+    torch.cuda.synchronize()
+    e_all_ms = max_over_ranks(e0.elapsed_time(e1), world)
+    e2e_value = world * B * args.steps / (e_all_ms / 1e3)
+    # beside it, seven rounds of e_steps steps each: the host link of a shared machine slows down now and then
+    # for tens of milliseconds (seen as single 2-4x slow trials in the tuner), so the median round is listed too
     e_steps = max(1, min(args.steps, 5))
     e_rounds = []
     for _ in range(7):
@@ -370,7 +384,7 @@ def run_gpu(args):
         torch.cuda.synchronize()
         e_rounds.append(max_over_ranks(e0.elapsed_time(e1), world))
     e_ms = statistics.median(e_rounds)
-    e2e_value = world * B * e_steps / (e_ms / 1e3)
+    e2e_median_round_value = world * B * e_steps / (e_ms / 1e3)
     h2d = B * 2 * 2 * limbs * n * 8
     d2h = B * 2 * (limbs - 1) * n * 8
 
@@ -380,16 +394,10 @@ def run_gpu(args):
         "warmup": max(args.warmup, 3), "ms_per_step": round(ms_per_step, 4), "higher_is_better": True,
         "scaling": "weak", "vs_baseline": None, "dtype": "u64 (exact modular integer)",
         "data": "synthetic: seeded encryptions of uniform [-1,1] complex slots; seeded keys",
-        "config": {"workload": "mult_relinearized (tensor+relinearize+rescale), hybrid keyswitch",
-                   "poly_degree": n, "limbs": limbs, "aux_limbs": aux, "prime_bits": 50,
-                   "gadget": "balanced base-2^30", "digits": digits, "batch": B,
-                   "parallelism": f"replicas x{world}",
-                   "autotune": {"device": tune_dev["choice"], "host": tune_host["choice"],
-                                "cached": bool(tune_dev["cached"]),
-                                "host_trials_ms": {"/".join(f"{k}={v}" for k, v in sorted(t["config"].items())): t["ms"]
-                                                   for t in tune_host.get("trials", [])}},
-                   "l2": "no flush: each step reads ~%.1f GB of inputs and key (L2 129 MB)"
-                         % ((B * 4 * limbs + digits * 2 * (limbs + aux)) * n * 8 / 1e9)},
+        "config": workload_config(n, limbs, aux, digits, B, world),
+        "autotune": {"device": tune_dev["choice"], "host": tune_host["choice"], "cached": bool(tune_dev["cached"]),
+                     "host_trials_ms": {"/".join(f"{k}={v}" for k, v in sorted(t["config"].items())): t["ms"]
+                                        for t in tune_host.get("trials", [])}},
         "per_op": {"value": round(per_op_value, 3), "unit": UNIT,
                    "p50_ms": round(float(np.percentile(per_op_ms, 50)), 4),
                    "p99_ms": round(float(np.percentile(per_op_ms, 99)), 4),
@@ -397,43 +405,58 @@ def run_gpu(args):
                                          for k, v in sorted(per_op_prof.items(), key=lambda kv: -kv[1]["ms"])}},
         "batched_vs_per_op": round(value / world / per_op_value, 3),
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "rounds_ms_per_step": [round(r / e_steps, 3) for r in e_rounds], "estimator": "median of 7 rounds"},
+                "ms_per_step": round(e_all_ms / args.steps, 4),
+                "estimator": f"{args.steps} consecutive steps (the protocol of value)",
+                "median_round_value": round(e2e_median_round_value, 3),
+                "rounds_ms_per_step": [round(r / e_steps, 3) for r in e_rounds]},
         "gpu_launches": int(sum(v["launches"] for v in prof.values())),
         "clocks": clk.summary(),
     }
     # the integer multiply rates that bound the kernels (measured on this GPU, outside the timed region)
     rates = (ctypes.c_double * 5)()
-    C.call("rc_measure_multiply_rates", rates, s_ptr)
+    from rnsckks_gb300._lib import probe_lib
+    rc = probe_lib().rc_measure_multiply_rates(rates, s_ptr)
+    if rc != 0:
+        raise RuntimeError(f"multiply-rate probe failed: CUDA error {rc}")
     result["integer_multiply_rates"] = {
         "unit": "warp instructions per SM per cycle",
         "imad_wide_32x32_64": round(rates[0], 3), "imad_32": round(rates[1], 3), "imad_hi_32": round(rates[2], 3),
         "mul_lo_64": round(rates[3], 3), "umul64hi": round(rates[4], 3)}
-    # roofline of the dominant kernel
+    # roofline of the dominant kernel: the algorithmic bytes of the HMult+relin ops one launch processes
     peak, peak_kind = peaks()
+    share = min(B, JOBS_PER_LAUNCH)
+    hm = hmult_algorithmic_bytes(n, limbs, aux, digits, share)
+    hm1 = hmult_algorithmic_bytes(n, limbs, aux, digits, 1)
+    step_frac = round(hm * value / world / 1e9 / peak, 4)
     dom = max(prof.items(), key=lambda kv: kv[1]["ms"]) if prof else None
     if dom:
         name, st = dom
         per_launch_ms = st["ms"] / st["launches"]
-        ab = algorithmic_bytes(name, B * args.steps, n, limbs, aux, digits, st["launches"])
+        ab = kernel_algorithmic_bytes(B * args.steps, n, limbs, aux, digits, st["launches"])
         achieved = (ab / (per_launch_ms / 1e3) / 1e9) if ab else None
+        jobs_per_launch = B * args.steps // st["launches"]
         traffic = imad = None  # per launch, from the committed ncu summary when it covers this shape
         tpath = ROOT / "profiles" / "dram_traffic_n16_l24.json"
         if tpath.exists() and n == 65536 and limbs == 24:
             t = json.loads(tpath.read_text()).get(name)
-            if t and t["jobs_per_launch"] * st["launches"] == B * args.steps:
+            if t and t["jobs_per_launch"] == jobs_per_launch:
                 traffic, imad = t["bytes_per_launch"], t.get("imad_pipe_pct")
+        design = kernel_traffic_breakdown(name, jobs_per_launch, n, limbs, aux, digits)
         result["roofline"] = {"bound": "hbm", "kernel": name, "achieved": round(achieved, 1) if achieved else None,
                               "peak": peak, "unit": "GB/s", "frac": round(achieved / peak, 4) if achieved else None,
                               "peak_kind": peak_kind, "traffic": traffic,
+                              "algorithmic_bytes_per_launch": int(ab) if ab else None,
+                              "jobs_per_launch": jobs_per_launch,
+                              "traffic_over_algorithmic": round(traffic / ab, 3) if traffic and ab else None,
+                              "design_traffic_per_launch": design,
                               "share": round(st["ms"] / sum(v["ms"] for v in prof.values()), 4),
+                              # the whole step against the same peak (all kernels, the same algorithmic bytes)
+                              "step_frac": step_frac,
                               # what actually limits it: the integer multiply (FMA-heavy) pipe, % busy under ncu
                               "imad_pipe_pct": imad}
-    share = min(B, JOBS_PER_LAUNCH)
-    hm = hmult_algorithmic_bytes(n, limbs, aux, digits, share)
-    hm1 = hmult_algorithmic_bytes(n, limbs, aux, digits, 1)
     result["hmult_roofline"] = {"algorithmic_bytes_per_op": int(hm), "key_shared_by": share,
                                 "achieved_GBs": round(hm * value / world / 1e9, 1),
-                                "frac": round(hm * value / world / 1e9 / peak, 4),
+                                "frac": step_frac,
                                 "per_op_algorithmic_bytes": int(hm1),
                                 "per_op_achieved_GBs": round(hm1 * per_op_value / 1e9, 1),
                                 "per_op_frac": round(hm1 * per_op_value / 1e9 / peak, 4)}
@@ -953,10 +976,11 @@ def run_reference(args):
     lhs, rhs = np.stack([rp(q), rp(q)]), np.stack([rp(q), rp(q)])
     key = np.stack([np.stack([rp(allm), rp(allm)]) for _ in range(D)])
     threads = os.cpu_count() or 1
-    for _ in range(min(args.warmup, 1)):
+    # a step is a bounded sample of the GPU arm's step: one of its B HMult+relin ops (about 10 s on 16 cores;
+    # the oracle parallelises inside the op, so the per-op rate is the batch's rate)
+    for _ in range(max(args.warmup, 0)):
         cpu_oracle_op(O, params, lhs, rhs, key, threads)
-    # one HMult+relin takes ~10 s on the oracle: at most 8 timed steps keep the arm within a few minutes
-    steps = max(1, min(args.steps, 8))
+    steps = max(1, args.steps)
     t0 = time.perf_counter()
     for _ in range(steps):
         cpu_oracle_op(O, params, lhs, rhs, key, threads)
@@ -964,17 +988,16 @@ def run_reference(args):
     value = steps / secs
     print(json.dumps({
         "impl": "reference", "metric": METRIC, "value": round(value, 5), "unit": UNIT, "n_gpus": world,
-        "steps": steps, "requested_steps": args.steps, "warmup": min(args.warmup, 1),
+        "steps": steps, "warmup": max(args.warmup, 0),
         "ms_per_step": round(secs / steps * 1e3, 1),
         "higher_is_better": True, "scaling": "weak", "vs_baseline": None, "dtype": "u64 (exact modular integer)",
         "data": "synthetic: seeded uniform residues and key",
-        "config": {"workload": "mult_relinearized (tensor+relinearize+rescale), hybrid keyswitch", "poly_degree": n,
-                   "limbs": len(q), "aux_limbs": len(params.aux_primes), "prime_bits": 50,
-                   "gadget": "balanced base-2^30", "digits": D, "batch": 1, "parallelism": "host threads"},
+        "config": workload_config(n, len(q), len(params.aux_primes), D, args.batch, world),
         "cpu_baseline": {"value": round(value, 5), "unit": UNIT, "cores": threads, "kind": "port",
-                         "sample": "one faithful HMult+relin per step on the oracle (C restatement of the "
-                                   "reference CPU path: per-call NTT round trips, u128 %, Garner gadget); "
-                                   "the Rust crate itself cannot be built here (no Rust toolchain)"},
+                         "sample": f"one faithful HMult+relin of the {args.batch}-pair batch per step on the oracle "
+                                   "(C restatement of the reference CPU path: per-call NTT round trips, u128 %, "
+                                   "Garner gadget, all host threads inside the op); the Rust crate itself cannot "
+                                   "be built here (no Rust toolchain)"},
         "e2e": {"value": round(value, 5), "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0},
     }), flush=True)
 

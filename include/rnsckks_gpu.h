@@ -74,8 +74,9 @@ int rc_context_create(const rc_params* params, rc_context** out);
 void rc_context_destroy(rc_context* ctx);
 const char* rc_last_error(const rc_context* ctx);
 /* Device-side error flags of the library's kernels (no reference counterpart): nonzero when a key-product
- * launch gave up waiting for its bulk copies (its results are then invalid).  Synchronises the device; clear
- * != 0 resets the flags. */
+ * launch gave up waiting for its bulk copies.  Such a CTA drains its copies and writes nothing, so the
+ * results of every operation issued since the flag was last clear are invalid and must be discarded.
+ * Synchronises the device; clear != 0 resets the flags.  A failed read of the flag returns RC_ERR_CUDA. */
 int rc_kernel_errors(int32_t* flags, int32_t clear);
 /* levels(), num_slots(), poly_degree, aux count: context.rs:57-95 */
 int rc_context_info(const rc_context* ctx, uint64_t* poly_degree, uint32_t* levels, uint32_t* aux_count,
@@ -92,7 +93,10 @@ int rc_reserve(rc_context* ctx, int32_t max_level, uint32_t max_batch, void* str
  * host_chunk / host_edge jobs, default 2), "lazy_ntt" (unreduced forward butterflies, only
  * when every prime is below 2^58), "fuse_tensor" (forward row phase + tensor + inverse row phase of a
  * ciphertext product in one kernel, default 1), "host_phased" (host-buffer batches of up to ks_jobs same-level
- * jobs: one key read for the batch, copies overlapped chunk by chunk; default 1).  Set them between calls, not while calls on the context are in flight. */
+ * jobs: one key read for the batch, copies overlapped chunk by chunk; default 1), "mac_wait_polls" (polls of
+ * the key product's first wait for its staged digit transforms, 0..2^22, default 2^22; 0 makes every CTA
+ * time out and raise the rc_kernel_errors flag, for testing that path).  Set them between calls, not while
+ * calls on the context are in flight. */
 int rc_tune_set(rc_context* ctx, const char* name, int32_t value);
 int rc_tune_get(const rc_context* ctx, const char* name, int32_t* value);
 
@@ -197,13 +201,15 @@ int rc_rescale_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* ct, r
 /* Serialised ciphertexts: a 64-byte header (magic "RCCTXT01", version, components (2 or 3), N, level,
  * scale_bits, payload bytes, modulus-chain fingerprint, checksum) followed by the [components][level+1][N]
  * coefficient-form residues.  rc_ct_header reads the header of a record (no context needed) so the caller can
- * allocate the device buffer rc_ct_deserialize fills; out->level and out->scale_bits are set from the record. */
+ * allocate the device buffer rc_ct_deserialize fills; out->level and out->scale_bits are set from the record.
+ * out_bytes is the capacity of out->data: a record whose payload is larger is refused, nothing is written. */
 int rc_ct_serialized_size(const rc_context* ctx, int32_t level, uint32_t components, uint64_t* bytes);
 int rc_ct_serialize(rc_context* ctx, const rc_ciphertext* ct, uint32_t components, void* host_buf,
                     uint64_t buf_bytes, void* stream);
 int rc_ct_header(const void* host_buf, uint64_t buf_bytes, uint64_t* poly_degree, int32_t* level,
                  int32_t* scale_bits, uint32_t* components);
-int rc_ct_deserialize(rc_context* ctx, const void* host_buf, uint64_t buf_bytes, rc_ciphertext* out, void* stream);
+int rc_ct_deserialize(rc_context* ctx, const void* host_buf, uint64_t buf_bytes, rc_ciphertext* out,
+                      uint64_t out_bytes, void* stream);
 /* lift_poly_to_context: src/rns/keyswitching.rs:242-276 (convert_centered_residues_to_target, 365-379).
  * `polys` polynomials over Q_limbs ([polys][limbs][N]) -> over Q_limbs followed by the aux primes
  * ([polys][limbs + aux_count][N]): the Q limbs are copied, each aux limb is the centred CRT value (the tie
@@ -317,12 +323,6 @@ int rc_mult_relinearized_batch_host(rc_context* ctx, uint32_t count, const uint6
                                     const uint64_t* const* rhs, const int32_t* levels, const int32_t* scale_bits,
                                     const rc_ksk* const* keys, uint64_t* const* out, int32_t* out_scale_bits,
                                     void* stream);
-
-/* ---- measurement (no reference counterpart) ----
- * Throughput of the integer multiply forms the kernels use, in warp-wide instructions per SM per SM cycle:
- * rates[0] IMAD.WIDE (32x32->64 with a 64-bit addend), [1] 32-bit IMAD, [2] IMAD.HI, [3] 64-bit low product,
- * [4] __umul64hi.  Runs five short kernels on `stream` (about 30 ms). */
-int rc_measure_multiply_rates(double* rates, void* stream);
 
 /* ---- host FP64 helpers (src/rns/encoding.rs, src/math/canonical_embedding.rs) ---- */
 /* encode_integer_coeffs + poly_from_bigint_coeffs: encoding.rs:9-31,

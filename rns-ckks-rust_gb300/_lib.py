@@ -74,7 +74,7 @@ SIGNATURES = [
     ("rc_ct_serialize", ctypes.c_int, [_vp, _CT, _u32, _vp, _u64, _vp]),
     ("rc_ct_header", ctypes.c_int, [_vp, _u64, ctypes.POINTER(_u64), ctypes.POINTER(_i32), ctypes.POINTER(_i32),
                                     ctypes.POINTER(_u32)]),
-    ("rc_ct_deserialize", ctypes.c_int, [_vp, _vp, _u64, _CT, _vp]),
+    ("rc_ct_deserialize", ctypes.c_int, [_vp, _vp, _u64, _CT, _u64, _vp]),
     ("rc_ntt_forward", ctypes.c_int, [_vp, _vp, _u32, _u32, _i32, _vp]),
     ("rc_ntt_inverse", ctypes.c_int, [_vp, _vp, _u32, _u32, _i32, _vp]),
     ("rc_poly_multiply", ctypes.c_int, [_vp, _vp, _vp, _vp, _u32, _i32, _vp]),
@@ -130,7 +130,6 @@ SIGNATURES = [
     ("rc_decode_device", ctypes.c_int, [_vp, _vp, _u32, _i32, _u32, _vp, _vp]),
     ("rc_slots_to_real_coeffs", ctypes.c_int, [_u64, _vp, _vp]),
     ("rc_complex_coeffs_to_slots", ctypes.c_int, [_u64, _vp, _vp]),
-    ("rc_measure_multiply_rates", ctypes.c_int, [_vp, _vp]),
     ("rc_profile_enable", ctypes.c_int, [ctypes.c_int]),
     ("rc_profile_report", ctypes.c_int, [ctypes.c_char_p, ctypes.c_size_t]),
 ]
@@ -159,6 +158,23 @@ def lib():
             f.argtypes = args
         _lib = L
     return _lib
+
+
+_probe = None
+
+
+def probe_lib():
+    """Load librnsckks_probe.so, the measurement probes of the benchmark (not part of the library's ABI)."""
+    global _probe
+    if _probe is None:
+        path = BUILD_DIR / "librnsckks_probe.so"
+        if not path.exists():
+            raise RuntimeError(f"{path} is missing: build it first (make -C {PKG_DIR})")
+        P = ctypes.CDLL(str(path))
+        P.rc_measure_multiply_rates.restype = ctypes.c_int
+        P.rc_measure_multiply_rates.argtypes = [_vp, _vp]
+        _probe = P
+    return _probe
 
 
 def check(status: int) -> None:

@@ -601,7 +601,8 @@ class RnsCkksContext:
             raise RcError(1, "serialized ciphertext was made for another modulus chain")
         data_t = torch.empty((comps.value, lv.value + 1, n.value), dtype=torch.int64, device="cuda")
         o = RcCiphertext(data_t.data_ptr(), 0, 0)
-        call("rc_ct_deserialize", self.handle, buf.ctypes.data, buf.size, ctypes.byref(o), _stream())
+        call("rc_ct_deserialize", self.handle, buf.ctypes.data, buf.size, ctypes.byref(o),
+             data_t.numel() * 8, _stream())
         cls = RnsQuadraticCiphertext if comps.value == 3 else RnsCiphertext
         return cls(data_t, o.scale_bits, o.level)
 

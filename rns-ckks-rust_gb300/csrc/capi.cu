@@ -945,6 +945,9 @@ extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
       c->fuse_tensor = value != 0;
     } else if (n == "host_phased") {
       c->host_phased = value != 0;
+    } else if (n == "mac_wait_polls") {
+      require(value >= 0 && value <= (1 << 22), "mac_wait_polls must be in 0..4194304");
+      c->wp.first_wait_polls = (uint32_t)value;
     } else if (n == "lazy_ntt") {
       bool ok = true;
       for (uint64_t q : c->mod) ok = ok && q < (1ull << 58);
@@ -967,6 +970,7 @@ extern "C" int rc_tune_get(const rc_context* c, const char* name, int32_t* value
     else if (n == "lazy_ntt") *value = c->lazy ? 1 : 0;
     else if (n == "fuse_tensor") *value = c->fuse_tensor ? 1 : 0;
     else if (n == "host_phased") *value = c->host_phased ? 1 : 0;
+    else if (n == "mac_wait_polls") *value = (int32_t)c->wp.first_wait_polls;
     else fail(RC_ERR_INVALID_ARGUMENT, "unknown tunable " + n);
   });
 }

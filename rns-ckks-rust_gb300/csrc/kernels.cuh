@@ -9,6 +9,9 @@
 
 namespace rc {
 
+// throws (RC_ERR_CUDA) on a CUDA error; defined with the C ABI
+void cuda_check(cudaError_t e, const char* what);
+
 // per-kernel event timing (profile.cu); no-ops unless rc_profile_enable(1)
 bool prof_enabled();
 void prof_begin(const char* name, cudaStream_t s);
@@ -153,6 +156,9 @@ struct WidePrimes {
   const Tw2* tw_fwd;              // [2 pairs][N]: psi^bitrev(k)
   const Tw2* tw_inv;              // [2 pairs][N]: psi^-bitrev(k)
   int log_n;
+  // polls of the key product's first wait for its staged digit transforms (tunable "mac_wait_polls"; a
+  // limit of 0 makes every CTA time out, which tests the error path without a fault)
+  uint32_t first_wait_polls = 1u << 22;
 };
 // Garner CRT of (S mod w0..w3) to the centred integer S (|S| < A/4), reduced mod
 // each scheme prime t.

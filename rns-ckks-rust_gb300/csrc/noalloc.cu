@@ -52,17 +52,10 @@ using namespace rc;
 
 extern "C" int rc_poly_multiply_noalloc(rc_context* c, const uint64_t* a, const uint64_t* b, uint64_t* out,
                                         uint32_t limbs, int32_t with_aux, void* stream) {
-  try {
-    if (!c || !a || !b || !out) fail(RC_ERR_INVALID_ARGUMENT, "arguments must not be null");
-    LimbMap map{(int)limbs, c->L};
-    if (with_aux) {
-      if (c->K == 0) fail(RC_ERR_INVALID_ARGUMENT, "eval-key level context requires an auxiliary basis");
-      if ((int)limbs <= c->K || (int)limbs - c->K > c->L)
-        fail(RC_ERR_INVALID_ARGUMENT, "limb count out of range for the extended basis");
-      map.qcount = (int)limbs - c->K;
-    } else if (limbs < 1 || (int)limbs > c->L) {
-      fail(RC_ERR_INVALID_ARGUMENT, "context level count must match polynomial levels");
-    }
+  return guarded([&] {
+    require(c && a && b && out, "arguments must not be null");
+    // the same limb and basis checks (and messages) as rc_poly_multiply
+    const LimbMap map = context_basis_map(c, limbs, with_aux);
     const size_t pl = (size_t)limbs * c->N;
     if (2 * pl > NOALLOC_SCRATCH_ELEMS)
       fail(RC_ERR_INVALID_ARGUMENT, "rc_poly_multiply_noalloc: limbs * N = " + std::to_string(pl) +
@@ -88,12 +81,5 @@ extern "C" int rc_poly_multiply_noalloc(rc_context* c, const uint64_t* a, const 
     inv.mont_out = 1;  // takes out the Montgomery products' 2^-64
     ntt_inverse(inv, x, o, 1, (int)limbs, map, s);
     cuda_check(cudaGetLastError(), "rc_poly_multiply_noalloc");
-    return RC_OK;
-  } catch (const ApiError& e) {
-    set_last_error(e.what());
-    return e.code;
-  } catch (const std::exception& e) {
-    set_last_error(e.what());
-    return RC_ERR_CUDA;
-  }
+  });
 }

@@ -212,7 +212,7 @@ extern "C" int rc_ct_header(const void* host_buf, uint64_t buf_bytes, uint64_t* 
 }
 
 extern "C" int rc_ct_deserialize(rc_context* c, const void* host_buf, uint64_t buf_bytes, rc_ciphertext* out,
-                                 void* stream) {
+                                 uint64_t out_bytes, void* stream) {
   return guarded([&] {
     require(c && host_buf && out && out->data, "arguments must not be null");
     require(buf_bytes >= sizeof(CtHeader), "serialized ciphertext is truncated");
@@ -227,6 +227,8 @@ extern "C" int rc_ct_deserialize(rc_context* c, const void* host_buf, uint64_t b
     const size_t payload = (size_t)h.components * (h.level + 1) * c->N * 8;
     require(h.payload_bytes == payload && buf_bytes >= sizeof(CtHeader) + payload,
             "serialized ciphertext is truncated");
+    // the record decides the size; a destination sized for a lower level must not be overrun
+    require(out_bytes >= payload, "serialized ciphertext does not fit the destination buffer");
     const uint64_t* words = (const uint64_t*)((const char*)host_buf + sizeof(CtHeader));
     require(payload_checksum(words, payload / 8) == h.checksum, "serialized ciphertext checksum mismatch");
     cuda_check(cudaMemcpyAsync(out->data, words, payload, cudaMemcpyHostToDevice, (cudaStream_t)stream), "ciphertext upload");

@@ -288,12 +288,16 @@ __device__ __forceinline__ void cp_async_wait() {
 }
 
 // Set by a key-product CTA whose bulk copies did not complete within the wait limit (read and cleared by
-// rc_kernel_errors); no such CTA computes.
+// rc_kernel_errors).  The decision is taken for the whole CTA at once: no thread of such a CTA computes or
+// writes its outputs, so every result of the launch (and of whatever consumed it) must be discarded.
 __device__ int g_wide_errors = 0;
 
-// Waits for phase `parity` of the mbarrier at shared address bar, at most ~2^22 polls; false on timeout.
-__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity) {
-  for (uint32_t it = 0; it < (1u << 22); ++it) {
+// polls of the drain wait after a timed-out first wait: long enough for any copy to land
+constexpr uint32_t W_DRAIN_POLLS = 1u << 22;
+
+// Waits for phase `parity` of the mbarrier at shared address bar, at most `polls` polls; false on timeout.
+__device__ __forceinline__ bool mbar_wait_bounded(uint32_t bar, uint32_t parity, uint32_t polls) {
+  for (uint32_t it = 0; it < polls; ++it) {
     uint32_t done;
     asm volatile(
         "{\n\t.reg .pred p;\n\tmbarrier.try_wait.parity.shared::cta.b64 p, [%1], %2;\n\tselp.u32 %0, 1, 0, p;\n\t}"
@@ -358,9 +362,12 @@ __global__ __launch_bounds__(32 * w_mac_warps<BC>(), BC >= 8 ? 2 : (BC >= 4 ? 3 
             : "memory");
       }
     }
-    if (!mbar_wait_bounded(bar, 0)) {
-      atomicOr(&g_wide_errors, 1);
-      mbar_wait_bounded(bar, 0);  // the copies in flight, once more with a limit
+    // one decision for the whole CTA: either every thread saw the copies land, or none computes
+    if (!__syncthreads_and(mbar_wait_bounded(bar, 0, w.first_wait_polls))) {
+      if (threadIdx.x == 0) atomicOr(&g_wide_errors, 1);
+      // drain: the bulk copies still in flight target this CTA's shared memory, so wait for them (again
+      // bounded) before the CTA exits and the shared memory passes to another CTA
+      __syncthreads_and(mbar_wait_bounded(bar, 0, W_DRAIN_POLLS));
       return;
     }
   }
@@ -570,10 +577,11 @@ void wide_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2
 
 int wide_kernel_errors(bool clear) {
   int v = 0;
-  cudaMemcpyFromSymbol(&v, g_wide_errors, sizeof(int));
+  // a failed read (e.g. a sticky error after a fault) is an error, never a clean flag
+  cuda_check(cudaMemcpyFromSymbol(&v, g_wide_errors, sizeof(int)), "reading the key-product error flag");
   if (clear && v) {
     const int zero = 0;
-    cudaMemcpyToSymbol(g_wide_errors, &zero, sizeof(int));
+    cuda_check(cudaMemcpyToSymbol(g_wide_errors, &zero, sizeof(int)), "clearing the key-product error flag");
   }
   return v;
 }

@@ -188,6 +188,44 @@ def test_key_products_report_no_copy_timeouts(C, small):
     assert flags.value == 0
 
 
+def test_key_product_wait_that_runs_out_raises_the_flag_and_recovers(C, small):
+    """The key product's first wait for its staged digit transforms is bounded.  A poll limit of 0 makes every
+    CTA give up at once: the CTA drains its copies (the second wait keeps its full bound, so nothing is left in
+    flight), raises the device flag and writes nothing.  rc_kernel_errors reports the flag, clearing it works,
+    and with the limit restored the same batch is bit-exact again."""
+    params, ctx = small
+    n, q = params.poly_degree, params.q_moduli()
+    rng = np.random.default_rng(77)
+    key = ctx.upload_keyswitch_key(_random_key(rng, params, len(q), True)[0], len(q) - 1, 2)
+    cts = [C.RnsCiphertext(C.to_device(rand_ct(rng, q, n)), 40) for _ in range(3)]
+    flags = ctypes.c_int32(-1)
+    C.call("rc_kernel_errors", ctypes.byref(flags), 1)
+    assert flags.value == 0
+    ref = [o.numpy() for o in ctx.mult_relinearized_batch(cts, cts[::-1], [key] * 3)]
+    default = ctypes.c_int32(0)
+    C.call("rc_tune_get", ctx.handle, b"mac_wait_polls", ctypes.byref(default))
+    assert default.value == 1 << 22
+    C.call("rc_tune_set", ctx.handle, b"mac_wait_polls", 0)
+    try:
+        ctx.mult_relinearized_batch(cts, cts[::-1], [key] * 3)
+        torch.cuda.synchronize()
+    finally:
+        C.call("rc_tune_set", ctx.handle, b"mac_wait_polls", default.value)
+    C.call("rc_kernel_errors", ctypes.byref(flags), 0)
+    assert flags.value == 1
+    C.call("rc_kernel_errors", ctypes.byref(flags), 1)  # read and clear
+    assert flags.value == 1
+    C.call("rc_kernel_errors", ctypes.byref(flags), 0)
+    assert flags.value == 0
+    got = [o.numpy() for o in ctx.mult_relinearized_batch(cts, cts[::-1], [key] * 3)]
+    C.call("rc_kernel_errors", ctypes.byref(flags), 1)
+    assert flags.value == 0
+    for g, r in zip(got, ref):
+        assert np.array_equal(g, r)
+    with pytest.raises(C.RcError, match="mac_wait_polls must be in"):
+        C.call("rc_tune_set", ctx.handle, b"mac_wait_polls", -1)
+
+
 def test_hoisted_rotations_past_one_launch(C, small):
     """34 ciphertexts: two chunks of the hoisted path (32 jobs per key-product launch)."""
     params, ctx = small

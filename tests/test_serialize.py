@@ -129,6 +129,16 @@ def test_damaged_records_are_refused(setup, pkg):
         ctx.ciphertext_from_bytes(bytes(crec))
     with pytest.raises(RcError, match="another modulus chain"):
         other.ciphertext_from_bytes(ctx.ciphertext_to_bytes(cts[0]))
+    # a destination sized for a lower level than the record's is refused and left untouched
+    import torch
+    rec = np.frombuffer(ctx.ciphertext_to_bytes(cts[0]), dtype=np.uint8)
+    small = torch.full((2, cts[0].level, params.poly_degree), 7, dtype=torch.int64, device="cuda")
+    o = C.RcCiphertext(small.data_ptr(), 0, 0)
+    with pytest.raises(RcError, match="does not fit the destination buffer"):
+        C.call("rc_ct_deserialize", ctx.handle, rec.ctypes.data, rec.size, ctypes.byref(o), small.numel() * 8,
+               C._stream())
+    torch.cuda.synchronize()
+    assert bool((small == 7).all())
 
 
 @pytest.mark.gpu
