@@ -284,7 +284,8 @@ def run_gpu(args):
     torch.cuda.synchronize()
 
     # ---- batched, device-resident (inputs 50 MB per pair: far larger than L2 in total) ----
-    lib.rc_profile_enable(1)
+    # kernel timing by CUDA events, plus NVTX ranges per entry point and kernel launch (for timeline tools)
+    lib.rc_profile_enable(3)
     buf = ctypes.create_string_buffer(1 << 16)
     lib.rc_profile_report(buf, len(buf))  # reset
     barrier(world)

@@ -350,10 +350,17 @@ int rc_complex_coeffs_to_slots(uint64_t n, const double* coeffs, double* slots_o
 
 /* ---- instrumentation (no reference counterpart: the reference only has
  * std::time::Instant around whole ops, examples/operations/timings.rs:282-308) ----
- * When enabled, every kernel launch is bracketed by CUDA events on its stream;
- * rc_profile_report synchronizes the device and writes a JSON object
- * {"kernel": {"launches": n, "ms": total}, ...} into buf, then resets. */
-int rc_profile_enable(int on);
+ * rc_profile_enable(flags), flags a combination of:
+ *   RC_PROFILE_EVENTS: every kernel launch is bracketed by CUDA events on its stream (not for launches
+ *     recorded into a CUDA graph); rc_profile_report synchronizes the device and writes a JSON object
+ *     {"kernel": {"launches": n, "ms": total}, ...} into buf, then resets;
+ *   RC_PROFILE_NVTX: NVTX ranges on the calling host thread, one per public entry point (named after it,
+ *     e.g. "rc_mult_relinearized_batch") and one per kernel launch inside it (the names the event report
+ *     uses), for a timeline tool; no cost when no tool is attached.
+ * 0 turns both off (the default). */
+#define RC_PROFILE_EVENTS 1
+#define RC_PROFILE_NVTX 2
+int rc_profile_enable(int flags);
 int rc_profile_report(char* buf, size_t len);
 
 #ifdef __cplusplus

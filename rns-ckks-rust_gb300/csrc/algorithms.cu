@@ -342,7 +342,7 @@ int floor_log2_u64(uint64_t q) { return 63 - __builtin_clzll(q); }
 extern "C" int rc_total_sum_batch(rc_context* c, uint32_t count, const rc_ciphertext* cts, uint32_t active_slots,
                                   const rc_ksk* const* step_keys, uint32_t key_count, rc_ciphertext* out,
                                   void* stream) {
-  return guarded([&] {
+  return guarded("rc_total_sum_batch", [&] {
     require(c && cts && out, "arguments must not be null");
     if (count == 0) return;
     Algo A(c, stream);
@@ -354,7 +354,7 @@ extern "C" int rc_total_sum_batch(rc_context* c, uint32_t count, const rc_cipher
 extern "C" int rc_halevi_shoup_batch(rc_context* c, uint32_t count, const rc_ciphertext* cts, const double* plain,
                                      uint32_t plain_len, const rc_ksk* const* step_keys, uint32_t key_count,
                                      rc_ciphertext* out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_halevi_shoup_batch", [&] {
     require(c && cts && plain && out, "arguments must not be null");
     if (count == 0) return;
     Algo A(c, stream);
@@ -401,7 +401,7 @@ extern "C" int rc_paterson_stockmeyer_batch(rc_context* c, uint32_t count, const
                                             const double* coefficients, uint32_t terms,
                                             const rc_ksk* const* relin_keys, uint32_t key_levels,
                                             rc_ciphertext* out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_paterson_stockmeyer_batch", [&] {
     require(c && cts && out && (terms == 0 || coefficients), "arguments must not be null");
     require(terms > 0, "polynomial must contain at least one coefficient");
     if (count == 0) return;
@@ -521,7 +521,7 @@ extern "C" int rc_bsgs_apply_batch(rc_context* c, uint32_t count, const rc_ciphe
                                    uint32_t baby_step, const uint64_t* const* diag_ntt, uint32_t giants,
                                    int32_t diag_level, int32_t diag_scale_bits, const rc_ksk* const* baby_keys,
                                    const rc_ksk* const* giant_keys, rc_ciphertext* out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_bsgs_apply_batch", [&] {
     require(c && cts && diag_ntt && out, "arguments must not be null");
     if (count == 0) return;
     for (uint32_t i = 0; i < count; ++i) {

@@ -544,7 +544,7 @@ uint64_t context_galois_inverse(const rc_context* c, uint64_t g) { return galois
 // context
 // =========================================================================
 extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
-  return guarded([&] {
+  return guarded("rc_context_create", [&] {
     require(p != nullptr && out != nullptr, "params and out must not be null");
     *out = nullptr;
     // RnsCkksParams::validate, src/rns/context/params.rs:48-73
@@ -902,14 +902,14 @@ extern "C" void rc_context_destroy(rc_context* ctx) {
 extern "C" const char* rc_last_error(const rc_context*) { return g_err.c_str(); }
 
 extern "C" int rc_kernel_errors(int32_t* flags, int32_t clear) {
-  return guarded([&] {
+  return guarded("rc_kernel_errors", [&] {
     require(flags != nullptr, "arguments must not be null");
     *flags = wide_kernel_errors(clear != 0);
   });
 }
 
 extern "C" int rc_context_info(const rc_context* c, uint64_t* n, uint32_t* levels, uint32_t* aux, uint32_t* sb) {
-  return guarded([&] {
+  return guarded("rc_context_info", [&] {
     require(c != nullptr, "context must not be null");
     if (n) *n = (uint64_t)c->N;
     if (levels) *levels = (uint32_t)c->L;
@@ -919,14 +919,14 @@ extern "C" int rc_context_info(const rc_context* c, uint64_t* n, uint32_t* level
 }
 
 extern "C" int rc_decomp_digits(const rc_context* c, int32_t level, uint32_t* digits) {
-  return guarded([&] {
+  return guarded("rc_decomp_digits", [&] {
     require(c != nullptr && digits != nullptr, "arguments must not be null");
     *digits = (uint32_t)level_info(c, level + 1).digits;
   });
 }
 
 extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
-  return guarded([&] {
+  return guarded("rc_tune_set", [&] {
     require(c && name, "arguments must not be null");
     const std::string n(name);
     if (n == "ks_jobs") {
@@ -960,7 +960,7 @@ extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
 }
 
 extern "C" int rc_tune_get(const rc_context* c, const char* name, int32_t* value) {
-  return guarded([&] {
+  return guarded("rc_tune_get", [&] {
     require(c && name && value, "arguments must not be null");
     const std::string n(name);
     if (n == "ks_jobs") *value = c->ks_jobs;
@@ -976,7 +976,7 @@ extern "C" int rc_tune_get(const rc_context* c, const char* name, int32_t* value
 }
 
 extern "C" int rc_reserve(rc_context* c, int32_t max_level, uint32_t max_batch, void* stream) {
-  return guarded([&] {
+  return guarded("rc_reserve", [&] {
     require(c != nullptr, "context must not be null");
     const int limbs = max_level + 1;
     const LevelInfo& li = level_info(c, limbs);
@@ -1053,16 +1053,18 @@ static int ksk_upload_impl(rc_context* c, const uint64_t* key, bool on_device, u
 
 extern "C" int rc_ksk_upload(rc_context* c, const uint64_t* host_key, uint32_t digits, int32_t level,
                              uint32_t aux_count, uint64_t galois_element, rc_ksk** out) {
+  OpRange op_range("rc_ksk_upload");
   return ksk_upload_impl(c, host_key, false, digits, level, aux_count, galois_element, out);
 }
 
 extern "C" int rc_ksk_upload_device(rc_context* c, const uint64_t* dev_key, uint32_t digits, int32_t level,
                                     uint32_t aux_count, uint64_t galois_element, rc_ksk** out) {
+  OpRange op_range("rc_ksk_upload_device");
   return ksk_upload_impl(c, dev_key, true, digits, level, aux_count, galois_element, out);
 }
 
 extern "C" int rc_ksk_truncate(rc_context* c, const rc_ksk* key, int32_t level, rc_ksk** out) {
-  return guarded([&] {
+  return guarded("rc_ksk_truncate", [&] {
     require(c && key && out, "arguments must not be null");
     // RnsKeySwitchingKey::truncate_levels / drop_last_level, keyswitching.rs:21-41
     require(level + 1 > 0, "level_count must be positive");
@@ -1111,9 +1113,11 @@ static int ntt_entry(rc_context* c, uint64_t* data, uint32_t polys, uint32_t lim
 }
 
 extern "C" int rc_ntt_forward(rc_context* c, uint64_t* d, uint32_t polys, uint32_t limbs, int32_t aux, void* s) {
+  OpRange op_range("rc_ntt_forward");
   return ntt_entry(c, d, polys, limbs, aux, s, true);
 }
 extern "C" int rc_ntt_inverse(rc_context* c, uint64_t* d, uint32_t polys, uint32_t limbs, int32_t aux, void* s) {
+  OpRange op_range("rc_ntt_inverse");
   return ntt_entry(c, d, polys, limbs, aux, s, false);
 }
 
@@ -1135,7 +1139,7 @@ void* rc::context_workspace(rc_context* c, cudaStream_t s, size_t bytes) { retur
 
 extern "C" int rc_poly_multiply(rc_context* c, const uint64_t* a, const uint64_t* b, uint64_t* out, uint32_t limbs,
                                 int32_t with_aux, void* stream) {
-  return guarded([&] {
+  return guarded("rc_poly_multiply", [&] {
     require(c && a && b && out, "arguments must not be null");
     const LimbMap map = basis_map(c, limbs, with_aux);
     cudaStream_t s = S(stream);
@@ -1177,16 +1181,18 @@ static int poly_binary(rc_context* c, const uint64_t* a, const uint64_t* b, uint
 }
 extern "C" int rc_poly_add(rc_context* c, const uint64_t* a, const uint64_t* b, uint64_t* o, uint32_t l,
                            int32_t aux, void* s) {
+  OpRange op_range("rc_poly_add");
   return poly_binary(c, a, b, o, l, aux, s, EwOp::Add);
 }
 extern "C" int rc_poly_sub(rc_context* c, const uint64_t* a, const uint64_t* b, uint64_t* o, uint32_t l,
                            int32_t aux, void* s) {
+  OpRange op_range("rc_poly_sub");
   return poly_binary(c, a, b, o, l, aux, s, EwOp::Sub);
 }
 
 extern "C" int rc_poly_mul_scalar(rc_context* c, const uint64_t* a, const uint64_t* scalars, uint64_t* out,
                                   uint32_t limbs, int32_t with_aux, void* stream) {
-  return guarded([&] {
+  return guarded("rc_poly_mul_scalar", [&] {
     require(c && a && scalars && out, "arguments must not be null");
     const LimbMap map = basis_map(c, limbs, with_aux);
     ScalarTab st{};
@@ -1199,7 +1205,7 @@ extern "C" int rc_poly_mul_scalar(rc_context* c, const uint64_t* a, const uint64
 
 extern "C" int rc_poly_automorphism(rc_context* c, const uint64_t* a, uint64_t* out, uint32_t limbs, uint64_t g,
                                     void* stream) {
-  return guarded([&] {
+  return guarded("rc_poly_automorphism", [&] {
     require(c && a && out, "arguments must not be null");
     require(limbs >= 1 && (int)limbs <= c->L, "limb count out of range for this context");
     require(a != out, "automorphism output must not alias its input");
@@ -1218,7 +1224,7 @@ extern "C" int rc_poly_automorphism(rc_context* c, const uint64_t* a, uint64_t* 
 // =========================================================================
 extern "C" int rc_add(rc_context* c, const rc_ciphertext* a, const rc_ciphertext* b, rc_ciphertext* out,
                       void* stream) {
-  return guarded([&] {
+  return guarded("rc_add", [&] {
     require(c && out && out->data, "arguments must not be null");
     check_ct(c, a, "lhs");
     check_ct(c, b, "rhs");
@@ -1244,7 +1250,7 @@ extern "C" int rc_add(rc_context* c, const rc_ciphertext* a, const rc_ciphertext
 // algorithms and the server issue one call per step of a batch instead of one per job).
 extern "C" int rc_add_batch(rc_context* c, uint32_t count, const rc_ciphertext* a, const rc_ciphertext* b,
                             rc_ciphertext* out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_add_batch", [&] {
     require(c && a && b && out, "arguments must not be null");
     // jobs of one level go out in launches of up to MAXP/2 ciphertexts (two components each)
     std::map<int, std::vector<uint32_t>> by_level;
@@ -1310,7 +1316,7 @@ static void mult_plain_impl(rc_context* c, const rc_ciphertext* ct, const uint64
 
 extern "C" int rc_mult_plain(rc_context* c, const rc_ciphertext* ct, const uint64_t* plain, rc_ciphertext* out,
                              void* stream) {
-  return guarded([&] {
+  return guarded("rc_mult_plain", [&] {
     const int sb = ct ? ct->scale_bits : 0;
     mult_plain_impl(c, ct, plain, out, S(stream));
     out->scale_bits = sb + sb;  // context/ops.rs:24-29
@@ -1319,7 +1325,7 @@ extern "C" int rc_mult_plain(rc_context* c, const rc_ciphertext* ct, const uint6
 
 extern "C" int rc_multiply_plain_rns_batch(rc_context* c, uint32_t count, const rc_ciphertext* ct,
                                            const uint64_t* const* plains, rc_ciphertext* out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_multiply_plain_rns_batch", [&] {
     require(c && ct && plains && out, "arguments must not be null");
     for (uint32_t i = 0; i < count; ++i) {
       const int sb = ct[i].scale_bits;
@@ -1331,7 +1337,7 @@ extern "C" int rc_multiply_plain_rns_batch(rc_context* c, uint32_t count, const 
 
 extern "C" int rc_multiply_plain_rns(rc_context* c, const rc_ciphertext* ct, const uint64_t* plain,
                                      rc_ciphertext* out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_multiply_plain_rns", [&] {
     const int sb = ct ? ct->scale_bits : 0;
     mult_plain_impl(c, ct, plain, out, S(stream));
     out->scale_bits = sb;
@@ -1341,7 +1347,7 @@ extern "C" int rc_multiply_plain_rns(rc_context* c, const rc_ciphertext* ct, con
 extern "C" int rc_mult_plain_accumulate(rc_context* c, uint32_t count, const rc_ciphertext* cts, int32_t cts_ntt,
                                         const uint64_t* const* plains, int32_t plains_ntt, rc_ciphertext* out,
                                         void* stream) {
-  return guarded([&] {
+  return guarded("rc_mult_plain_accumulate", [&] {
     require(c && cts && plains && out && out->data, "arguments must not be null");
     require(count >= 1, "the inner sum needs at least one term");
     for (uint32_t k = 0; k < count; ++k) {
@@ -1402,7 +1408,7 @@ extern "C" int rc_mult_plain_accumulate(rc_context* c, uint32_t count, const rc_
 
 extern "C" int rc_mult(rc_context* c, const rc_ciphertext* a, const rc_ciphertext* b, rc_ciphertext* out,
                        void* stream) {
-  return guarded([&] {
+  return guarded("rc_mult", [&] {
     require(c && out && out->data, "arguments must not be null");
     check_mult_pair(c, a, b);
     const int limbs = a->level + 1;
@@ -1434,14 +1440,14 @@ static void rescale_impl(rc_context* c, const rc_ciphertext* ct, rc_ciphertext* 
 }
 
 extern "C" int rc_rescale(rc_context* c, const rc_ciphertext* ct, rc_ciphertext* out, void* stream) {
-  return guarded([&] { rescale_impl(c, ct, out, 2, S(stream)); });
+  return guarded("rc_rescale", [&] { rescale_impl(c, ct, out, 2, S(stream)); });
 }
 extern "C" int rc_rescale_quadratic(rc_context* c, const rc_ciphertext* ct, rc_ciphertext* out, void* stream) {
-  return guarded([&] { rescale_impl(c, ct, out, 3, S(stream)); });
+  return guarded("rc_rescale_quadratic", [&] { rescale_impl(c, ct, out, 3, S(stream)); });
 }
 extern "C" int rc_rescale_batch(rc_context* c, uint32_t count, const rc_ciphertext* ct, rc_ciphertext* out,
                                 void* stream) {
-  return guarded([&] {
+  return guarded("rc_rescale_batch", [&] {
     require(c && ct && out, "arguments must not be null");
     for (uint32_t i = 0; i < count; ++i) rescale_impl(c, &ct[i], &out[i], 2, S(stream));
   });
@@ -1461,11 +1467,11 @@ static void lift_impl(rc_context* c, const uint64_t* a, uint64_t* out, uint32_t 
 
 extern "C" int rc_lift_to_aux(rc_context* c, const uint64_t* a, uint64_t* out, uint32_t polys, uint32_t limbs,
                               void* stream) {
-  return guarded([&] { lift_impl(c, a, out, polys, limbs, S(stream)); });
+  return guarded("rc_lift_to_aux", [&] { lift_impl(c, a, out, polys, limbs, S(stream)); });
 }
 
 extern "C" int rc_mod_raise(rc_context* c, const rc_ciphertext* ct, rc_ciphertext* out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_mod_raise", [&] {
     require(c && out && out->data, "arguments must not be null");
     check_ct(c, ct, "ciphertext");
     lift_impl(c, ct->data, out->data, 2, (uint32_t)ct->level + 1, S(stream));
@@ -1476,7 +1482,7 @@ extern "C" int rc_mod_raise(rc_context* c, const rc_ciphertext* ct, rc_ciphertex
 
 extern "C" int rc_keyswitch(rc_context* c, const uint64_t* poly, int32_t level, const rc_ksk* key,
                             rc_ciphertext* out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_keyswitch", [&] {
     require(c && poly && out && out->data, "arguments must not be null");
     require(level >= 0 && level < c->L, "keyswitch level context must exist");
     const int limbs = level + 1;
@@ -1489,7 +1495,7 @@ extern "C" int rc_keyswitch(rc_context* c, const uint64_t* poly, int32_t level, 
 
 extern "C" int rc_relinearize(rc_context* c, const rc_ciphertext* qct, const rc_ksk* key, rc_ciphertext* out,
                               void* stream) {
-  return guarded([&] {
+  return guarded("rc_relinearize", [&] {
     require(c && out && out->data, "arguments must not be null");
     check_ct(c, qct, "quadratic ciphertext");
     const int limbs = qct->level + 1;
@@ -1503,7 +1509,7 @@ extern "C" int rc_relinearize(rc_context* c, const rc_ciphertext* qct, const rc_
 
 extern "C" int rc_mult_relinearized(rc_context* c, const rc_ciphertext* a, const rc_ciphertext* b,
                                     const rc_ksk* key, rc_ciphertext* out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_mult_relinearized", [&] {
     require(c && out && out->data, "arguments must not be null");
     check_mult_pair(c, a, b);
     std::vector<int> idx{0};
@@ -1513,7 +1519,7 @@ extern "C" int rc_mult_relinearized(rc_context* c, const rc_ciphertext* a, const
 
 extern "C" int rc_rotate(rc_context* c, const rc_ciphertext* ct, const rc_ksk* key, rc_ciphertext* out,
                          void* stream) {
-  return guarded([&] {
+  return guarded("rc_rotate", [&] {
     require(c && out && out->data && key, "arguments must not be null");
     check_ct(c, ct, "ciphertext");
     // context/rotation.rs:106
@@ -1532,7 +1538,7 @@ extern "C" int rc_rotate(rc_context* c, const rc_ciphertext* ct, const rc_ksk* k
 
 extern "C" int rc_automorphism(rc_context* c, const rc_ciphertext* ct, uint64_t g, rc_ciphertext* out,
                                void* stream) {
-  return guarded([&] {
+  return guarded("rc_automorphism", [&] {
     require(c && out && out->data, "arguments must not be null");
     check_ct(c, ct, "ciphertext");
     require(out->data != ct->data, "automorphism output must not alias its input");
@@ -1557,7 +1563,7 @@ extern "C" int rc_automorphism(rc_context* c, const rc_ciphertext* ct, uint64_t 
 extern "C" int rc_mult_relinearized_batch(rc_context* c, uint32_t count, const rc_ciphertext* lhs,
                                           const rc_ciphertext* rhs, const rc_ksk* const* keys, rc_ciphertext* out,
                                           void* stream) {
-  return guarded([&] {
+  return guarded("rc_mult_relinearized_batch", [&] {
     require(c && lhs && rhs && keys && out, "arguments must not be null");
     std::map<std::pair<int, std::pair<int, int>>, std::vector<int>> groups;
     for (uint32_t i = 0; i < count; ++i) {
@@ -1573,7 +1579,7 @@ extern "C" int rc_mult_relinearized_batch(rc_context* c, uint32_t count, const r
 
 extern "C" int rc_relinearize_batch(rc_context* c, uint32_t count, const rc_ciphertext* qct,
                                     const rc_ksk* const* keys, rc_ciphertext* out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_relinearize_batch", [&] {
     require(c && qct && keys && out, "arguments must not be null");
     std::map<std::pair<int, std::pair<int, int>>, std::vector<int>> groups;
     for (uint32_t i = 0; i < count; ++i) {
@@ -1601,7 +1607,7 @@ extern "C" int rc_relinearize_batch(rc_context* c, uint32_t count, const rc_ciph
 
 extern "C" int rc_relinearize_rescale_batch(rc_context* c, uint32_t count, const rc_ciphertext* qct,
                                             const rc_ksk* const* keys, rc_ciphertext* out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_relinearize_rescale_batch", [&] {
     require(c && qct && keys && out, "arguments must not be null");
     std::map<std::pair<int, std::pair<int, int>>, std::vector<int>> groups;
     for (uint32_t i = 0; i < count; ++i) {
@@ -1641,7 +1647,7 @@ struct rc_graph {
 };
 
 extern "C" int rc_graph_begin(rc_context* c, void* stream) {
-  return guarded([&] {
+  return guarded("rc_graph_begin", [&] {
     require(c != nullptr, "context must not be null");
     require(stream != nullptr, "CUDA graph capture needs a non-default stream");
     cuda_check(cudaStreamBeginCapture(S(stream), cudaStreamCaptureModeThreadLocal), "cudaStreamBeginCapture");
@@ -1649,7 +1655,7 @@ extern "C" int rc_graph_begin(rc_context* c, void* stream) {
 }
 
 extern "C" int rc_graph_end(rc_context* c, void* stream, rc_graph** out) {
-  return guarded([&] {
+  return guarded("rc_graph_end", [&] {
     require(c && out && stream, "arguments must not be null");
     *out = nullptr;
     std::unique_ptr<rc_graph> g(new rc_graph());
@@ -1660,6 +1666,7 @@ extern "C" int rc_graph_end(rc_context* c, void* stream, rc_graph** out) {
 }
 
 extern "C" int rc_graph_launch(rc_graph* g, void* stream) {
+  OpRange op_range("rc_graph_launch");
   if (!g || !g->exec) {
     set_last_error("graph must not be null");
     return RC_ERR_INVALID_ARGUMENT;
@@ -1681,7 +1688,7 @@ extern "C" void rc_graph_destroy(rc_graph* g) {
 
 extern "C" int rc_rotate_batch(rc_context* c, uint32_t count, const rc_ciphertext* ct, const rc_ksk* const* keys,
                                rc_ciphertext* out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_rotate_batch", [&] {
     require(c && ct && keys && out, "arguments must not be null");
     // group by (level, key kind, galois element): the gather is per launch
     std::map<std::pair<std::pair<int, uint64_t>, std::pair<int, int>>, std::vector<int>> groups;
@@ -1722,7 +1729,7 @@ extern "C" int rc_rotate_batch(rc_context* c, uint32_t count, const rc_ciphertex
 // chain outside the wide key product run as rc_rotate_batch.
 extern "C" int rc_rotate_hoisted(rc_context* c, uint32_t count, const rc_ciphertext* cts, uint32_t nrot,
                                  const rc_ksk* const* keys, rc_ciphertext* out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_rotate_hoisted", [&] {
     require(c && cts && keys && out, "arguments must not be null");
     if (count == 0 || nrot == 0) return;
     cudaStream_t s = S(stream);
@@ -1944,7 +1951,7 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
                                                const uint64_t* const* rhs, const int32_t* levels,
                                                const int32_t* scale_bits, const rc_ksk* const* keys,
                                                uint64_t* const* out, int32_t* out_scale_bits, void* stream) {
-  return guarded([&] {
+  return guarded("rc_mult_relinearized_batch_host", [&] {
     require(c && lhs && rhs && levels && scale_bits && keys && out, "arguments must not be null");
     cudaStream_t s = S(stream);
     for (uint32_t i = 0; i < count; ++i)
@@ -2041,6 +2048,7 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
 extern "C" int rc_mult_relinearized_host(rc_context* c, const uint64_t* lhs, const uint64_t* rhs, int32_t level,
                                          int32_t scale_bits, const rc_ksk* key, uint64_t* out,
                                          int32_t* out_scale_bits, void* stream) {
+  OpRange op_range("rc_mult_relinearized_host");
   const uint64_t* l[1] = {lhs};
   const uint64_t* r[1] = {rhs};
   uint64_t* o[1] = {out};

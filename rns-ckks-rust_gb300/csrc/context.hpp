@@ -49,6 +49,22 @@ int guarded(F&& f) {
   }
 }
 
+// A public entry point's body inside an NVTX range named after it (when rc_profile_enable turned NVTX on).
+struct OpRange {
+  bool on;
+  explicit OpRange(const char* name) : on(nvtx_enabled()) {
+    if (on) nvtx_push(name);
+  }
+  ~OpRange() {
+    if (on) nvtx_pop();
+  }
+};
+template <class F>
+int guarded(const char* op, F&& f) {
+  OpRange r(op);
+  return guarded(std::forward<F>(f));
+}
+
 struct DevBuf {
   void* p = nullptr;
   size_t bytes = 0;

@@ -273,7 +273,7 @@ void fft(Cd* work, const Cd* tw, int log_n, uint32_t count, cudaStream_t s) {
 
 extern "C" int rc_encode_device(rc_context* c, const double* slots, uint32_t count, int32_t level,
                                 uint32_t scale_bits, uint64_t* out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_encode_device", [&] {
     require(c && slots && out, "arguments must not be null");
     require(level >= 0 && level < c->L, "level out of range for this context");
     if (count == 0) return;
@@ -292,7 +292,7 @@ extern "C" int rc_encode_device(rc_context* c, const double* slots, uint32_t cou
 
 extern "C" int rc_decode_device(rc_context* c, const uint64_t* polys, uint32_t count, int32_t level,
                                 uint32_t scale_bits, double* slots_out, void* stream) {
-  return guarded([&] {
+  return guarded("rc_decode_device", [&] {
     require(c && polys && slots_out, "arguments must not be null");
     require(level >= 0 && level < c->L, "level out of range for this context");
     if (count == 0) return;

@@ -12,8 +12,11 @@ namespace rc {
 // throws (RC_ERR_CUDA) on a CUDA error; defined with the C ABI
 void cuda_check(cudaError_t e, const char* what);
 
-// per-kernel event timing (profile.cu); no-ops unless rc_profile_enable(1)
+// per-kernel event timing and NVTX ranges (profile.cu); no-ops unless rc_profile_enable turned them on
 bool prof_enabled();
+bool nvtx_enabled();
+void nvtx_push(const char* name);
+void nvtx_pop();
 void prof_begin(const char* name, cudaStream_t s);
 void prof_end(const char* name, cudaStream_t s);
 struct ProfScope {

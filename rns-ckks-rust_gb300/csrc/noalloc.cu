@@ -52,7 +52,7 @@ using namespace rc;
 
 extern "C" int rc_poly_multiply_noalloc(rc_context* c, const uint64_t* a, const uint64_t* b, uint64_t* out,
                                         uint32_t limbs, int32_t with_aux, void* stream) {
-  return guarded([&] {
+  return guarded("rc_poly_multiply_noalloc", [&] {
     require(c && a && b && out, "arguments must not be null");
     // the same limb and basis checks (and messages) as rc_poly_multiply
     const LimbMap map = context_basis_map(c, limbs, with_aux);

@@ -1,6 +1,13 @@
-// Optional per-kernel timing with CUDA events recorded on the launching stream
-// (off by default).  Each launch site brackets its kernel with prof_begin /
-// prof_end; rc_profile_report sums the event intervals per kernel name.
+// Optional per-kernel timing with CUDA events recorded on the launching stream,
+// and optional NVTX ranges per public entry point and per kernel launch (both
+// off by default; rc_profile_enable picks them).  Each launch site brackets its
+// kernel with prof_begin / prof_end; rc_profile_report sums the event intervals
+// per kernel name.  The NVTX ranges are host-side markers for a timeline tool
+// (they cost nothing when no tool is attached) and are also emitted for launches
+// recorded into a CUDA graph.
+#include <nvtx3/nvToolsExt.h>
+
+#include <atomic>
 #include <cstdio>
 #include <map>
 #include <mutex>
@@ -38,7 +45,12 @@ cudaEvent_t take_event() {
 }
 }  // namespace
 
+std::atomic<bool> g_nvtx{false};
+
 bool prof_enabled() { return g_on; }
+bool nvtx_enabled() { return g_nvtx.load(std::memory_order_relaxed); }
+void nvtx_push(const char* name) { nvtxRangePushA(name); }
+void nvtx_pop() { nvtxRangePop(); }
 
 // launches recorded into a CUDA graph are not timed (an event record would become a graph node)
 static bool capturing(cudaStream_t s) {
@@ -47,6 +59,7 @@ static bool capturing(cudaStream_t s) {
 }
 
 void prof_begin(const char* name, cudaStream_t s) {
+  if (nvtx_enabled()) nvtx_push(name);
   if (!g_on || capturing(s)) return;
   std::lock_guard<std::mutex> lk(g_mu);
   cudaEvent_t e = take_event();
@@ -55,6 +68,7 @@ void prof_begin(const char* name, cudaStream_t s) {
 }
 
 void prof_end(const char* name, cudaStream_t s) {
+  if (nvtx_enabled()) nvtx_pop();
   if (!g_on || capturing(s)) return;
   std::lock_guard<std::mutex> lk(g_mu);
   auto& v = g_open[s];
@@ -70,9 +84,10 @@ void prof_end(const char* name, cudaStream_t s) {
 
 using namespace rc;
 
-extern "C" int rc_profile_enable(int on) {
+extern "C" int rc_profile_enable(int flags) {
   std::lock_guard<std::mutex> lk(g_mu);
-  g_on = on != 0;
+  g_on = (flags & RC_PROFILE_EVENTS) != 0;
+  g_nvtx.store((flags & RC_PROFILE_NVTX) != 0, std::memory_order_relaxed);
   return RC_OK;
 }
 

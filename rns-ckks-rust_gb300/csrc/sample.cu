@@ -120,15 +120,18 @@ int sample_entry(rc_context* c, Dist d, uint64_t seed, uint64_t stream_id, uint6
 
 extern "C" int rc_sample_uniform(rc_context* c, uint64_t seed, uint64_t stream_id, uint64_t* out, uint32_t limbs,
                                  int32_t with_aux, void* stream) {
+  OpRange op_range("rc_sample_uniform");
   return sample_entry(c, Dist::uniform, seed, stream_id, out, limbs, with_aux, stream);
 }
 
 extern "C" int rc_sample_error(rc_context* c, uint64_t seed, uint64_t stream_id, uint64_t* out, uint32_t limbs,
                                int32_t with_aux, void* stream) {
+  OpRange op_range("rc_sample_error");
   return sample_entry(c, Dist::error, seed, stream_id, out, limbs, with_aux, stream);
 }
 
 extern "C" int rc_sample_ternary(rc_context* c, uint64_t seed, uint64_t stream_id, uint64_t* out, uint32_t limbs,
                                  int32_t with_aux, void* stream) {
+  OpRange op_range("rc_sample_ternary");
   return sample_entry(c, Dist::ternary, seed, stream_id, out, limbs, with_aux, stream);
 }

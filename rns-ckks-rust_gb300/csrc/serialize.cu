@@ -84,14 +84,14 @@ size_t ksk_payload_bytes(const rc_ksk* k) {
 }  // namespace
 
 extern "C" int rc_ksk_serialized_size(const rc_ksk* k, uint64_t* bytes) {
-  return guarded([&] {
+  return guarded("rc_ksk_serialized_size", [&] {
     require(k && bytes, "arguments must not be null");
     *bytes = sizeof(KskHeader) + ksk_payload_bytes(k);
   });
 }
 
 extern "C" int rc_ksk_serialize(rc_context* c, const rc_ksk* k, void* host_buf, uint64_t buf_bytes, void* stream) {
-  return guarded([&] {
+  return guarded("rc_ksk_serialize", [&] {
     require(c && k && host_buf, "arguments must not be null");
     require(k->ctx == c, "keyswitch key belongs to another context");
     const size_t payload = ksk_payload_bytes(k);
@@ -119,7 +119,7 @@ extern "C" int rc_ksk_serialize(rc_context* c, const rc_ksk* k, void* host_buf, 
 }
 
 extern "C" int rc_ksk_deserialize(rc_context* c, const void* host_buf, uint64_t buf_bytes, rc_ksk** out) {
-  return guarded([&] {
+  return guarded("rc_ksk_deserialize", [&] {
     require(c && host_buf && out, "arguments must not be null");
     *out = nullptr;
     require(buf_bytes >= sizeof(KskHeader), "serialized key is truncated");
@@ -161,7 +161,7 @@ extern "C" int rc_ksk_deserialize(rc_context* c, const void* host_buf, uint64_t 
 }
 
 extern "C" int rc_ct_serialized_size(const rc_context* c, int32_t level, uint32_t components, uint64_t* bytes) {
-  return guarded([&] {
+  return guarded("rc_ct_serialized_size", [&] {
     require(c && bytes, "arguments must not be null");
     require(level >= 0 && level < c->L, "ciphertext level out of range for this context");
     require(components == 2 || components == 3, "a ciphertext has 2 or 3 components");
@@ -171,7 +171,7 @@ extern "C" int rc_ct_serialized_size(const rc_context* c, int32_t level, uint32_
 
 extern "C" int rc_ct_serialize(rc_context* c, const rc_ciphertext* ct, uint32_t components, void* host_buf,
                                uint64_t buf_bytes, void* stream) {
-  return guarded([&] {
+  return guarded("rc_ct_serialize", [&] {
     require(c && host_buf, "arguments must not be null");
     context_check_ct(c, ct, "ciphertext");
     require(components == 2 || components == 3, "a ciphertext has 2 or 3 components");
@@ -197,7 +197,7 @@ extern "C" int rc_ct_serialize(rc_context* c, const rc_ciphertext* ct, uint32_t 
 
 extern "C" int rc_ct_header(const void* host_buf, uint64_t buf_bytes, uint64_t* poly_degree, int32_t* level,
                             int32_t* scale_bits, uint32_t* components) {
-  return guarded([&] {
+  return guarded("rc_ct_header", [&] {
     require(host_buf, "arguments must not be null");
     require(buf_bytes >= sizeof(CtHeader), "serialized ciphertext is truncated");
     CtHeader h;
@@ -213,7 +213,7 @@ extern "C" int rc_ct_header(const void* host_buf, uint64_t buf_bytes, uint64_t* 
 
 extern "C" int rc_ct_deserialize(rc_context* c, const void* host_buf, uint64_t buf_bytes, rc_ciphertext* out,
                                  uint64_t out_bytes, void* stream) {
-  return guarded([&] {
+  return guarded("rc_ct_deserialize", [&] {
     require(c && host_buf && out && out->data, "arguments must not be null");
     require(buf_bytes >= sizeof(CtHeader), "serialized ciphertext is truncated");
     CtHeader h;

@@ -31,6 +31,15 @@ def test_library_exports_every_declared_symbol(pkg):
         assert hasattr(lib, name), name
 
 
+def test_profile_flags_switch_without_a_device(pkg):
+    """rc_profile_enable takes RC_PROFILE_EVENTS (1) and RC_PROFILE_NVTX (2); switching is host-only."""
+    text = HEADER.read_text()
+    assert "#define RC_PROFILE_EVENTS 1" in text and "#define RC_PROFILE_NVTX 2" in text
+    lib = pkg.lib()
+    for flags in (2, 3, 1, 0):
+        assert lib.rc_profile_enable(flags) == 0
+
+
 def test_binding_table_covers_header(pkg):
     from rnsckks_gb300 import _lib
     bound = {s[0] for s in _lib.SIGNATURES}

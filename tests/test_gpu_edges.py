@@ -226,6 +226,38 @@ def test_key_product_wait_that_runs_out_raises_the_flag_and_recovers(C, small):
         C.call("rc_tune_set", ctx.handle, b"mac_wait_polls", -1)
 
 
+def test_nvtx_ranges_leave_results_unchanged(C, small):
+    """With NVTX ranges on (per entry point and per kernel launch), also inside a captured graph, the residues
+    are the same as with instrumentation off."""
+    params, ctx = small
+    n, q = params.poly_degree, params.q_moduli()
+    rng = np.random.default_rng(78)
+    key = ctx.upload_keyswitch_key(_random_key(rng, params, len(q), True)[0], len(q) - 1, 2)
+    cts = [C.RnsCiphertext(C.to_device(rand_ct(rng, q, n)), 40) for _ in range(2)]
+    lib = C.lib()
+    ref = [o.numpy() for o in ctx.mult_relinearized_batch(cts, cts[::-1], [key] * 2)]
+    try:
+        assert lib.rc_profile_enable(2) == 0
+        got = [o.numpy() for o in ctx.mult_relinearized_batch(cts, cts[::-1], [key] * 2)]
+        side = torch.cuda.Stream()
+        with torch.cuda.stream(side):
+            ctx.reserve(len(q) - 1, 2)
+            outs = [torch.zeros((2, len(q) - 1, n), dtype=torch.int64, device="cuda") for _ in range(2)]
+            quads = [ctx.mult(a, b) for a, b in zip(cts, cts[::-1])]
+            graph = ctx.capture_graph(lambda: ctx.relinearize_rescale_batch(quads, [key] * 2, outs))
+            graph.launch()
+            side.synchronize()
+            direct = ctx.relinearize_rescale_batch(quads, [key] * 2)
+            side.synchronize()
+    finally:
+        lib.rc_profile_enable(0)
+    torch.cuda.synchronize()
+    for g, r in zip(got, ref):
+        assert np.array_equal(g, r)
+    for o, d in zip(outs, direct):
+        assert torch.equal(o, d.data)
+
+
 def test_hoisted_rotations_past_one_launch(C, small):
     """34 ciphertexts: two chunks of the hoisted path (32 jobs per key-product launch)."""
     params, ctx = small
