@@ -34,6 +34,20 @@ struct PtrTab {
   u64* p[MAXP];
 };
 
+// Mixed-level batches: up to ML_MAXJ jobs of different levels in one launch per pass.  Job j has
+// limbs[j] Q limbs; its digit polynomials are [dig[j], dig[j+1]) of the batch's digit array and its key
+// products the limb polynomials [acc[j], acc[j+1]) (2 (limbs[j] + K) of them) of the product array.
+constexpr int ML_MAXJ = 128;
+struct MlTab {
+  int J;
+  int limbs[ML_MAXJ];
+  int dig[ML_MAXJ + 1];
+  int acc[ML_MAXJ + 1];
+};
+struct MlPtrTab {
+  u64* p[2 * ML_MAXJ];
+};
+
 // Limb j of a polynomial uses prime prime(j) of the context's Q u P list:
 // the first `qcount` limbs are Q primes 0..qcount-1, the rest are the aux
 // primes L, L+1, ...
@@ -219,6 +233,32 @@ struct FinalizeArgs {
 };
 void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const PtrTab& out, int jobs,
               cudaStream_t s);
+
+// ---- mixed-level forms (one launch per pass; f.qlimbs unused) ----
+// digits of job j (src.p[j], limbs[j] Q limbs) from polynomial dig[j] of `digits`; d_dts[limbs] are the
+// per-level tables, max_limbs / max_W the largest job's
+void decompose_ml(const PrimeConst* pc, const DecompTab* d_dts, const MlTab& t, const MlPtrTab& src, int max_limbs,
+                  int max_W, int32_t* digits, int log_n, cudaStream_t s);
+// finalize of wide products acc (job j's 2 (limbs[j] + K) limb polynomials from acc[j] on)
+void finalize_ml(const FinalizeArgs& f, const MlTab& t, const u64* acc, const MlPtrTab& addend, const MlPtrTab& out,
+                 cudaStream_t s);
+// the jobs of one key in a mixed-level key product: jobs [first, first + count) (consecutive), the key's
+// tiled wide form, its digits used (D) and stored (key_digits), limbs + K of the level
+struct MlKey {
+  const uint2* kwt;
+  int D, key_digits, total, first, count;
+};
+constexpr int ML_MAXK = 64;
+struct MlKeys {
+  int n;
+  MlKey k[ML_MAXK];
+};
+// digit transforms of every job (dig[J] digit polynomials), tiled per job: job j's tiles from 2 N dig[j]
+bool wide_digit_transforms_ml(const WidePrimes& w, const MlTab& t, const int32_t* digits, uint2* work, uint2* dtt,
+                              cudaStream_t s);
+// key products of every job into acc (job j's [c][limb][pair][N] from 2 N acc[j]), one launch
+void wide_mac_ml(const WidePrimes& w, const MlTab& t, const MlKeys& keys, const uint2* dtt, uint2* acc, int bc_max,
+                 cudaStream_t s);
 
 // ---- wide-CRT key product (wide.cu) ----
 // digits [job][digit][N] -> transforms under w0..w3, written tiled:

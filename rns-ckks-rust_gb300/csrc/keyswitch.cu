@@ -30,17 +30,42 @@ namespace {
 // ---------------------------------------------------------------------------
 // decomposition
 // ---------------------------------------------------------------------------
-template <int WM, bool TIES>
-__global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int limbs, int D, int32_t* digits,
-                            u64 g_inv, int log_n, int* tie_flags) {
+// Job tables of the decomposition: where job j's input, tables and digits are.  UniDecomp: one level for
+// every job (digits [job][D][N]); MlDecomp: each job at its own level (tables from the per-level array,
+// digits of job j from polynomial dig[j] on).
+struct UniDecomp {
+  DecompTab dt;
+  PtrTab src;
+  int limbs, D;
+  __device__ __forceinline__ const DecompTab& tab(int) const { return dt; }
+  __device__ __forceinline__ int nlimbs(int) const { return limbs; }
+  __device__ __forceinline__ int digits(int) const { return D; }
+  __device__ __forceinline__ size_t first_digit(int job) const { return (size_t)job * D; }
+  __device__ __forceinline__ const u64* in(int job) const { return src.p[job]; }
+};
+struct MlDecomp {
+  const DecompTab* dts;  // [limbs] (device)
+  MlTab t;
+  MlPtrTab src;
+  __device__ __forceinline__ const DecompTab& tab(int job) const { return dts[t.limbs[job]]; }
+  __device__ __forceinline__ int nlimbs(int job) const { return t.limbs[job]; }
+  __device__ __forceinline__ int digits(int job) const { return t.dig[job + 1] - t.dig[job]; }
+  __device__ __forceinline__ size_t first_digit(int job) const { return (size_t)t.dig[job]; }
+  __device__ __forceinline__ const u64* in(int job) const { return src.p[job]; }
+};
+
+template <int WM, bool TIES, class JT>
+__global__ void k_decompose(const PrimeConst* pc, JT jt, int32_t* digits, u64 g_inv, int log_n, int* tie_flags) {
+  const int job = blockIdx.y;
+  const DecompTab& dt = jt.tab(job);
+  const int limbs = jt.nlimbs(job), D = jt.digits(job);
   const CrtSmem tabs = stage_crt_tables(pc, dt, limbs);
   __syncthreads();
   const int W = dt.W;
   const u64 N = 1ull << log_n;
   const u64 x = blockIdx.x * (u64)blockDim.x + threadIdx.x;
   if (x >= N) return;
-  const int job = blockIdx.y;
-  const u64* in = src.p[job];
+  const u64* in = jt.in(job);
 
   u64 sidx = x;
   bool neg = false;
@@ -53,7 +78,7 @@ __global__ void k_decompose(const PrimeConst* pc, DecompTab dt, PtrTab src, int 
   const u64 ext = centred_crt<WM>(tabs, W, limbs, in + sidx, N, neg, X);
 
   // balanced base-2^30 digits of the two's complement value
-  int32_t* out = digits + (size_t)job * D * N + x;
+  int32_t* out = digits + jt.first_digit(job) * N + x;
   u64 carry = 0;
   bool tie = false;  // a digit at -2^29
   constexpr int DMAX = (64 * WM) / 30 + 2;
@@ -506,10 +531,32 @@ enum FT { FT_Q, FT_ONE_S, FT_LO, FT_LO_S, FT_C01, FT_C01_S, FT_AMOD, FT_PINV, FT
           FT_RINV_S, FT_N };
 __host__ __device__ __forceinline__ int ft_stride(int K) { return FT_N + 2 * K; }
 
-__global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab out) {
+// Job tables of the finalize pass: job j's Q limb count, where its products start in acc (in limb
+// polynomials of N words), its addends and outputs.  UniFin: every job at f.qlimbs, acc [job][2][lq + K];
+// MlFin: each job at its own level, products from limb polynomial 2 acc[j] on.
+struct UniFin {
+  PtrTab addend, out;
+  int lq, K;
+  __device__ __forceinline__ int limbs(int) const { return lq; }
+  __device__ __forceinline__ size_t first_poly(int job) const { return (size_t)job * 2 * (lq + K); }
+  __device__ __forceinline__ const u64* add(int job, int comp) const { return addend.p[2 * job + comp]; }
+  __device__ __forceinline__ u64* dst(int job, int comp) const { return out.p[2 * job + comp]; }
+};
+struct MlFin {
+  MlTab t;
+  MlPtrTab addend, out;
+  __device__ __forceinline__ int limbs(int job) const { return t.limbs[job]; }
+  __device__ __forceinline__ size_t first_poly(int job) const { return (size_t)t.acc[job]; }
+  __device__ __forceinline__ const u64* add(int job, int comp) const { return addend.p[2 * job + comp]; }
+  __device__ __forceinline__ u64* dst(int job, int comp) const { return out.p[2 * job + comp]; }
+};
+
+template <class JT>
+__global__ void k_finalize(FinalizeArgs f, const u64* acc, JT jt) {
   extern __shared__ u64 tab[];  // [lq + K][FT_N + 2K]
   const u64 N = 1ull << f.log_n;
-  const int lq = f.qlimbs, K = f.K;
+  const int comp = blockIdx.y & 1, job = blockIdx.y >> 1;
+  const int lq = jt.limbs(job), K = f.K;
   const LimbMap fmap{lq, f.L};
   const int st = ft_stride(K);
   // with the wide CRT and an aux basis, a Q limb's constants carry the factor P^-1 (`fold`): the CRT then
@@ -564,9 +611,8 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
   __syncthreads();
   const u64 x = blockIdx.x * (u64)blockDim.x + threadIdx.x;
   if (x >= N) return;
-  const int comp = blockIdx.y & 1, job = blockIdx.y >> 1;
   const int wf = f.wide ? 2 : 1;  // 8-byte words per limb and coefficient in acc
-  const u64* a = acc + ((size_t)job * 2 + comp) * (size_t)(lq + K) * N * wf;
+  const u64* a = acc + (jt.first_poly(job) + (size_t)comp * (lq + K)) * N * wf;
   const uint2* a2 = reinterpret_cast<const uint2*>(a);
   auto T = [&](int i, int fld) -> u64 { return tab[i * st + fld]; };
   auto accv = [&](int j) -> u64 {  // value of limb j at x
@@ -574,8 +620,8 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, PtrTab addend, PtrTab
     return wide_crt_mod_c(a2[(size_t)j * 2 * N + x], a2[((size_t)j * 2 + 1) * N + x], f.wt, T(j, FT_Q),
                           T(j, FT_LO), T(j, FT_LO_S), T(j, FT_C01), T(j, FT_C01_S), T(j, FT_AMOD));
   };
-  const u64* add = addend.p[2 * job + comp];
-  u64* dst = out.p[2 * job + comp];
+  const u64* add = jt.add(job, comp);
+  u64* dst = jt.dst(job, comp);
 
   u64 addsrc = x;
   bool addneg = false;
@@ -800,12 +846,25 @@ __global__ void k_key_relayout(const PrimeConst* pc, const u64* src, u64* dst, i
 
 }  // namespace
 
-template <int WM>
-void launch_decompose(dim3 g, int threads, size_t smem, cudaStream_t s, const PrimeConst* pc, const DecompTab& dt,
-                      const PtrTab& src, int limbs, int D, int32_t* digits, uint64_t g_inv, int log_n,
-                      int* tie_flags) {
-  if (tie_flags) k_decompose<WM, true><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else k_decompose<WM, false><<<g, threads, smem, s>>>(pc, dt, src, limbs, D, digits, g_inv, log_n, nullptr);
+template <int WM, class JT>
+void launch_decompose(dim3 g, int threads, size_t smem, cudaStream_t s, const PrimeConst* pc, const JT& jt,
+                      int32_t* digits, uint64_t g_inv, int log_n, int* tie_flags) {
+  if (tie_flags) k_decompose<WM, true, JT><<<g, threads, smem, s>>>(pc, jt, digits, g_inv, log_n, tie_flags);
+  else k_decompose<WM, false, JT><<<g, threads, smem, s>>>(pc, jt, digits, g_inv, log_n, nullptr);
+}
+
+// the word count is a template parameter (register-resident value); the closest instance at or above W runs
+template <class JT>
+void decompose_dispatch(int W, dim3 g, int threads, size_t smem, cudaStream_t s, const PrimeConst* pc, const JT& jt,
+                        int32_t* digits, uint64_t g_inv, int log_n, int* tie_flags) {
+  if (W <= 4) launch_decompose<4>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
+  else if (W <= 8) launch_decompose<8>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
+  else if (W <= 12) launch_decompose<12>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
+  else if (W <= 16) launch_decompose<16>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
+  else if (W <= 20) launch_decompose<20>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
+  else if (W <= 24) launch_decompose<24>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
+  else if (W <= 32) launch_decompose<32>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
+  else launch_decompose<64>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
 }
 
 void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int jobs, int limbs, int D,
@@ -814,18 +873,20 @@ void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int
   const int N = 1 << log_n;
   const int threads = N < 128 ? N : 128;
   dim3 g((N + threads - 1) / threads, jobs);
-  const int W = dt.W;
   ProfScope p("decompose", s);
-  // the word count is a template parameter (register-resident value); the closest instance above W runs
-  const size_t smem = crt_smem_bytes(limbs, W);
-  if (W <= 4) launch_decompose<4>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else if (W <= 8) launch_decompose<8>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else if (W <= 12) launch_decompose<12>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else if (W <= 16) launch_decompose<16>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else if (W <= 20) launch_decompose<20>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else if (W <= 24) launch_decompose<24>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else if (W <= 32) launch_decompose<32>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
-  else launch_decompose<64>(g, threads, smem, s, pc, dt, src, limbs, D, digits, g_inv, log_n, tie_flags);
+  const UniDecomp jt{dt, src, limbs, D};
+  decompose_dispatch(dt.W, g, threads, crt_smem_bytes(limbs, dt.W), s, pc, jt, digits, g_inv, log_n, tie_flags);
+}
+
+void decompose_ml(const PrimeConst* pc, const DecompTab* d_dts, const MlTab& t, const MlPtrTab& src, int max_limbs,
+                  int max_W, int32_t* digits, int log_n, cudaStream_t s) {
+  if (t.J <= 0) return;
+  const int N = 1 << log_n;
+  const int threads = N < 128 ? N : 128;
+  dim3 g((N + threads - 1) / threads, t.J);
+  ProfScope p("decompose", s);
+  const MlDecomp jt{d_dts, t, src};
+  decompose_dispatch(max_W, g, threads, crt_smem_bytes(max_limbs, max_W), s, pc, jt, digits, 0, log_n, nullptr);
 }
 
 void lift_to_aux(const PrimeConst* pc, const PrimeConst* ppc, const DecompTab& dt, const u64* src, u64* dst,
@@ -895,7 +956,23 @@ void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const
   dim3 g((N + threads - 1) / threads, 2 * jobs);
   ProfScope p("finalize", s);
   const size_t smem = (size_t)(f.qlimbs + f.K) * ft_stride(f.K) * sizeof(u64);
-  k_finalize<<<g, threads, smem, s>>>(f, acc, addend, out);
+  const UniFin jt{addend, out, f.qlimbs, f.K};
+  k_finalize<UniFin><<<g, threads, smem, s>>>(f, acc, jt);
+}
+
+void finalize_ml(const FinalizeArgs& f, const MlTab& t, const u64* acc, const MlPtrTab& addend, const MlPtrTab& out,
+                 cudaStream_t s) {
+  if (t.J <= 0) return;
+  const int N = f.n;
+  const int tpb = t.J >= 8 ? 256 : 128;
+  const int threads = N < tpb ? N : tpb;
+  dim3 g((N + threads - 1) / threads, 2 * t.J);
+  int max_lq = 0;
+  for (int j = 0; j < t.J; ++j) max_lq = t.limbs[j] > max_lq ? t.limbs[j] : max_lq;
+  ProfScope p("finalize", s);
+  const size_t smem = (size_t)(max_lq + f.K) * ft_stride(f.K) * sizeof(u64);
+  const MlFin jt{t, addend, out};
+  k_finalize<MlFin><<<g, threads, smem, s>>>(f, acc, jt);
 }
 
 void key_to_device_form(const NttArgs& a, const PrimeConst* pc, const u64* src, u64* dst, int digits, int limbs,

@@ -117,12 +117,45 @@ __global__ __launch_bounds__(256, 2) void k_w_cols_fwd(WidePrimes w, const void*
 // are loaded while the current one is transformed.
 constexpr int W_ROW_POLYS = 16;
 
+// Where digit polynomial `poly` of a batch goes in the tiled layout: its job's first digit polynomial, its
+// digit index and its job's digit count.  UniDig: D digits per job (poly = job * D + digit); MlDig: job j's
+// digits are polynomials [dig[j], dig[j+1]), found by a binary search for a block's first polynomial and
+// then followed forward (`job` carries the position between calls).
+struct UniDig {
+  int D;
+  __device__ __forceinline__ void locate(int poly, int& job, int& first, int& digit, int& d) const {
+    job = poly / D;
+    first = job * D;
+    digit = poly - first;
+    d = D;
+  }
+};
+struct MlDig {
+  int J;
+  int dig[ML_MAXJ + 1];
+  __device__ __forceinline__ void locate(int poly, int& job, int& first, int& digit, int& d) const {
+    if (job < 0) {  // first call: the last job whose first digit is at or below poly
+      int lo = 0, hi = J - 1;
+      while (lo < hi) {
+        const int mid = (lo + hi + 1) >> 1;
+        if (dig[mid] <= poly) lo = mid;
+        else hi = mid - 1;
+      }
+      job = lo;
+    }
+    while (poly >= dig[job + 1]) ++job;
+    first = dig[job];
+    digit = poly - first;
+    d = dig[job + 1] - first;
+  }
+};
+
 // Forward row phase of data[poly][pair][N] (polys p0 + blockIdx.z * W_ROW_POLYS .. below p0 + cnt), outputs
-// reduced to [0, q).  TILED: written as dtt[job][pair][x/32][digit][32] with poly = job * D + digit;
-// otherwise in place.
-template <int M1, int M2, bool TILED>
+// reduced to [0, q).  TILED: written as dtt[job][pair][x/32][digit][32] (job j's tiles from 2 N first(j),
+// DM maps a polynomial to its job); otherwise in place.
+template <int M1, int M2, bool TILED, class DM>
 __global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_fwd(WidePrimes w, uint2* data, uint2* dtt, int p0,
-                                                                 int cnt, int D) {
+                                                                 int cnt, DM dm) {
   using G = core::Geo<M2>;
   constexpr int N1 = 1 << M1, N2 = 1 << M2, N = N1 * N2, ROWS = W_ROW_WARPS * G::SUBS;
   __shared__ uint2 bufs[ROWS * G::STRIDE];
@@ -137,6 +170,7 @@ __global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_fwd(WidePrimes w, u
   const int rl = warp * G::SUBS + sub, row = row0 + rl;
   auto row_ptr = [&](int t) { return data + (((size_t)p0 + first + t) * 2 + pair) * N + (size_t)row * N2; };
   uint2* buf = bufs + rl * G::STRIDE;
+  int job = -1;  // the digit map's position (TILED)
   uint2 v[8], vn[8];  // requested before the twiddle tables, so both latencies overlap
   {
     const uint2* in = row_ptr(0);
@@ -156,10 +190,10 @@ __global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_fwd(WidePrimes w, u
       for (int k = 0; k < 8; ++k) vn[k] = in[core::first_idx<M2>(l, k)];
     }
     core::fwd_sub2<M2>(v, buf, l, twl[rl], q0, q1);
-    const size_t poly = (size_t)p0 + first + t;
     if (TILED) {
-      const size_t job = poly / D, digit = poly % D;
-      uint2* o = dtt + (job * 2 + pair) * (N / 32) * (size_t)(D * 32) + digit * 32;
+      int jfirst, digit, D;
+      dm.locate(p0 + first + t, job, jfirst, digit, D);
+      uint2* o = dtt + (size_t)jfirst * 2 * N + (size_t)pair * N * D + (size_t)digit * 32;
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
         const int x = row * N2 + core::last_idx<M2>(l, k);
@@ -320,16 +354,52 @@ __device__ __forceinline__ uint32_t galois_source(uint32_t x, uint32_t g, int lo
   return __brev(kk) >> (32 - log_n);
 }
 
-template <int BC, bool FOLD>
+// Job tables of the key product.  A CTA (blockIdx.x) covers up to BC consecutive jobs that share one key;
+// cta() gives that key (tiled wide form, digits used and stored, limbs + K) and the jobs; dt_first(job) is
+// where the job's digit transforms start (in uint2 words), acc_first(job, total) where its products start
+// (in [pair][N] limb polynomials).  UniMac: nb jobs from b0 sharing one key, D digits each; MlMac: CTA x
+// covers jobs [ch_first[x], + ch_n[x]) of key ch_key[x], jobs laid out by the mixed-level table.
+struct UniMac {
+  const uint2* kwt;
+  int D, key_digits, total, b0, nb;
+  template <int BC>
+  __device__ __forceinline__ void cta(int x, const uint2*& k, int& d, int& kd, int& tot, int& bstart,
+                                      int& nloc) const {
+    k = kwt, d = D, kd = key_digits, tot = total;
+    bstart = b0 + x * BC;
+    nloc = min(BC, b0 + nb - bstart);
+  }
+  __device__ __forceinline__ size_t dt_first(int job, int N) const { return (size_t)job * 2 * N * D; }
+  __device__ __forceinline__ size_t acc_first(int job, int tot) const { return (size_t)job * 2 * tot; }
+};
+struct MlMac {
+  MlKeys keys;
+  int dig[ML_MAXJ + 1], acc[ML_MAXJ + 1];
+  unsigned char ch_key[ML_MAXJ], ch_n[ML_MAXJ];
+  short ch_first[ML_MAXJ];
+  template <int BC>
+  __device__ __forceinline__ void cta(int x, const uint2*& k, int& d, int& kd, int& tot, int& bstart,
+                                      int& nloc) const {
+    const MlKey& key = keys.k[ch_key[x]];
+    k = key.kwt, d = key.D, kd = key.key_digits, tot = key.total;
+    bstart = ch_first[x];
+    nloc = ch_n[x];
+  }
+  __device__ __forceinline__ size_t dt_first(int job, int N) const { return (size_t)dig[job] * 2 * N; }
+  __device__ __forceinline__ size_t acc_first(int job, int) const { return (size_t)acc[job]; }
+};
+
+template <int BC, bool FOLD, class KT>
 __global__ __launch_bounds__(32 * w_mac_warps<BC>(), BC >= 8 ? 2 : (BC >= 4 ? 3 : (BC >= 2 ? 4 : 3))) void k_w_mac(
-    WidePrimes w, int D, int key_digits, int total, const uint2* __restrict__ kwt, const uint2* __restrict__ dtt,
-    uint2* acc, int b0, int nb, uint32_t gal) {
+    WidePrimes w, KT kt, const uint2* __restrict__ dtt, uint2* acc, uint32_t gal) {
   extern __shared__ __align__(128) uint2 dsm[];  // [BC][D][32] digit transforms, then [warps][W_PF][2][32] key ring
   const int N = 1 << w.log_n, tiles = N >> 5;
   // job groups vary fastest, so the CTAs that stream the same key tile run together and share it in L2
   const int pair = blockIdx.y, xb = blockIdx.z;
-  const int bstart = b0 + blockIdx.x * BC;
-  const int nloc = min(BC, b0 + nb - bstart);
+  const uint2* key;
+  int D, key_digits, total, bstart, nloc;
+  kt.template cta<BC>(blockIdx.x, key, D, key_digits, total, bstart, nloc);
+  const uint2* __restrict__ kwt = key;
   const int run = D * 32;
   // gal > 1: the digits are those of sigma_gal of the decomposed polynomial (one source tile, lanes permuted)
   const uint32_t src0 = gal > 1 ? galois_source((uint32_t)xb * 32, gal, w.log_n) : (uint32_t)xb * 32;
@@ -354,7 +424,7 @@ __global__ __launch_bounds__(32 * w_mac_warps<BC>(), BC >= 8 ? 2 : (BC >= 4 ? 3 
       asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(run_bytes * (uint32_t)nloc)
                    : "memory");
       for (int b = 0; b < nloc; ++b) {
-        const uint2* src = dtt + (((size_t)(bstart + b) * 2 + pair) * tiles + stile) * run;
+        const uint2* src = dtt + kt.dt_first(bstart + b, N) + ((size_t)pair * tiles + stile) * run;
         asm volatile(
             "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
                 sbase + (uint32_t)b * run_bytes),
@@ -433,19 +503,19 @@ __global__ __launch_bounds__(32 * w_mac_warps<BC>(), BC >= 8 ? 2 : (BC >= 4 ? 3 
 #pragma unroll
     for (int b = 0; b < BC; ++b) {
       if (b < nloc) {
-        const size_t jb = (size_t)(bstart + b);
-        acc[(((jb * 2 + 0) * total + j) * 2 + pair) * N + x] =
-            make_uint2(reduce64_32(a0[b], q0, bar0), reduce64_32(a1[b], q1, bar1));
-        acc[(((jb * 2 + 1) * total + j) * 2 + pair) * N + x] =
+        const size_t ab = kt.acc_first(bstart + b, total);
+        acc[((ab + j) * 2 + pair) * N + x] = make_uint2(reduce64_32(a0[b], q0, bar0), reduce64_32(a1[b], q1, bar1));
+        acc[((ab + total + j) * 2 + pair) * N + x] =
             make_uint2(reduce64_32(c0[b], q0, bar0), reduce64_32(c1[b], q1, bar1));
       }
     }
   }
 }
 
-template <int BC, bool FOLD>
-void launch_w_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt,
-                  uint2* acc, int b0, int nb, uint32_t gal, cudaStream_t s) {
+// D: the largest digit count of the launch (sizes the shared memory); ctas: grid.x
+template <int BC, bool FOLD, class KT>
+void launch_w_mac(const WidePrimes& w, const KT& kt, int D, int ctas, const uint2* dtt, uint2* acc, uint32_t gal,
+                  cudaStream_t s) {
   const size_t smem = ((size_t)BC * D * 32 + (size_t)w_mac_warps<BC>() * W_PF * 64) * sizeof(uint2);
   // the opt-in limit is set once per instance, before any launch of it (callers on several host threads)
   static std::once_flag once;
@@ -454,12 +524,19 @@ void launch_w_mac(const WidePrimes& w, int D, int key_digits, int total, const u
     if (cudaGetDevice(&dev) == cudaSuccess)
       cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
     cudaFuncAttributes fa{};
-    cudaFuncGetAttributes(&fa, k_w_mac<BC, FOLD>);  // the static part (the mbarrier) counts against the limit
-    cudaFuncSetAttribute(k_w_mac<BC, FOLD>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+    cudaFuncGetAttributes(&fa, k_w_mac<BC, FOLD, KT>);  // the static part (the mbarrier) counts against the limit
+    cudaFuncSetAttribute(k_w_mac<BC, FOLD, KT>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          optin - (int)fa.sharedSizeBytes);
   });
-  dim3 g((nb + BC - 1) / BC, 2, (1 << w.log_n) / 32);
-  k_w_mac<BC, FOLD><<<g, 32 * w_mac_warps<BC>(), smem, s>>>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal);
+  dim3 g(ctas, 2, (1 << w.log_n) / 32);
+  k_w_mac<BC, FOLD, KT><<<g, 32 * w_mac_warps<BC>(), smem, s>>>(w, kt, dtt, acc, gal);
+}
+
+template <int BC, bool FOLD>
+void launch_w_mac_uni(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt,
+                      uint2* acc, int b0, int nb, uint32_t gal, cudaStream_t s) {
+  const UniMac kt{kwt, D, key_digits, total, b0, nb};
+  launch_w_mac<BC, FOLD>(w, kt, D, (nb + BC - 1) / BC, dtt, acc, gal, s);
 }
 
 // coefficient-form key [digits][2][limbs][N] -> kw[((j * digits + i) * 2 + c)][pair][N]
@@ -506,28 +583,30 @@ int grid_for_elems(size_t total) {
   return (int)(g > 65535 * 8 ? 65535 * 8 : g);
 }
 
-// forward transforms of polys [p0, p0 + count) of data[poly][pair][N]; SRC as in k_w_cols_fwd
-template <int M1, int M2, int SRC, bool TILED>
-void w_forward(const WidePrimes& w, const void* src, uint2* work, uint2* dtt, int polys, int D, cudaStream_t s) {
+// forward transforms of polys [p0, p0 + count) of data[poly][pair][N]; SRC as in k_w_cols_fwd, DM as in
+// k_w_rows_fwd
+template <int M1, int M2, int SRC, bool TILED, class DM>
+void w_forward(const WidePrimes& w, const void* src, uint2* work, uint2* dtt, int polys, const DM& dm,
+               cudaStream_t s) {
   constexpr int N1 = 1 << M1, N2 = 1 << M2;
   for (int p0 = 0; p0 < polys; p0 += 65535) {
     const int cnt = polys - p0 < 65535 ? polys - p0 : 65535;
     k_w_cols_fwd<M1, M2, SRC><<<dim3(N2 / WColTile<M1>::COLS, 2, cnt), 256, 0, s>>>(w, src, work, p0);
-    k_w_rows_fwd<M1, M2, TILED><<<dim3(N1 / (W_ROW_WARPS * core::Geo<M2>::SUBS), 2,
-                                       (cnt + W_ROW_POLYS - 1) / W_ROW_POLYS),
-                                  32 * W_ROW_WARPS, 0, s>>>(w, work, dtt, p0, cnt, D);
+    k_w_rows_fwd<M1, M2, TILED, DM><<<dim3(N1 / (W_ROW_WARPS * core::Geo<M2>::SUBS), 2,
+                                           (cnt + W_ROW_POLYS - 1) / W_ROW_POLYS),
+                                      32 * W_ROW_WARPS, 0, s>>>(w, work, dtt, p0, cnt, dm);
   }
 }
 
-template <int SRC, bool TILED>
-bool w_forward_dispatch(const WidePrimes& w, const void* src, uint2* work, uint2* dtt, int polys, int D,
+template <int SRC, bool TILED, class DM>
+bool w_forward_dispatch(const WidePrimes& w, const void* src, uint2* work, uint2* dtt, int polys, const DM& dm,
                         cudaStream_t s) {
   switch (w.log_n) {
-    case 12: w_forward<6, 6, SRC, TILED>(w, src, work, dtt, polys, D, s); return true;
-    case 13: w_forward<6, 7, SRC, TILED>(w, src, work, dtt, polys, D, s); return true;
-    case 14: w_forward<7, 7, SRC, TILED>(w, src, work, dtt, polys, D, s); return true;
-    case 15: w_forward<7, 8, SRC, TILED>(w, src, work, dtt, polys, D, s); return true;
-    case 16: w_forward<8, 8, SRC, TILED>(w, src, work, dtt, polys, D, s); return true;
+    case 12: w_forward<6, 6, SRC, TILED>(w, src, work, dtt, polys, dm, s); return true;
+    case 13: w_forward<6, 7, SRC, TILED>(w, src, work, dtt, polys, dm, s); return true;
+    case 14: w_forward<7, 7, SRC, TILED>(w, src, work, dtt, polys, dm, s); return true;
+    case 15: w_forward<7, 8, SRC, TILED>(w, src, work, dtt, polys, dm, s); return true;
+    case 16: w_forward<8, 8, SRC, TILED>(w, src, work, dtt, polys, dm, s); return true;
     default: return false;
   }
 }
@@ -556,7 +635,17 @@ void w_inverse(const WidePrimes& w, uint2* data, int polys, cudaStream_t s) {
 bool wide_digit_transforms(const WidePrimes& w, int D, int jobs, const int32_t* digits, uint2* work, uint2* dtt,
                            cudaStream_t s) {
   ProfScope p("wide_digit_ntt", s);
-  return w_forward_dispatch<0, true>(w, digits, work, dtt, jobs * D, D, s);
+  return w_forward_dispatch<0, true>(w, digits, work, dtt, jobs * D, UniDig{D}, s);
+}
+
+bool wide_digit_transforms_ml(const WidePrimes& w, const MlTab& t, const int32_t* digits, uint2* work, uint2* dtt,
+                              cudaStream_t s) {
+  if (t.J <= 0) return true;
+  ProfScope p("wide_digit_ntt", s);
+  MlDig dm;
+  dm.J = t.J;
+  for (int j = 0; j <= t.J; ++j) dm.dig[j] = t.dig[j];
+  return w_forward_dispatch<0, true>(w, digits, work, dtt, t.dig[t.J], dm, s);
 }
 
 void wide_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt, const uint2* dtt, uint2* acc,
@@ -564,15 +653,59 @@ void wide_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2
   ProfScope p("wide_mac", s);
   const int want = nb < bc_max ? nb : bc_max;  // jobs per CTA: the group size, at most bc_max
   if (D > 64) {  // folded sums; at most 4 jobs per CTA keep the fold within the register budget
-    if (want <= 1) launch_w_mac<1, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
-    else if (want <= 2) launch_w_mac<2, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
-    else launch_w_mac<4, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
+    if (want <= 1) launch_w_mac_uni<1, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
+    else if (want <= 2) launch_w_mac_uni<2, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
+    else launch_w_mac_uni<4, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
     return;
   }
-  if (want <= 1) launch_w_mac<1, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
-  else if (want <= 2) launch_w_mac<2, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
-  else if (want <= 4) launch_w_mac<4, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
-  else launch_w_mac<8, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
+  if (want <= 1) launch_w_mac_uni<1, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
+  else if (want <= 2) launch_w_mac_uni<2, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
+  else if (want <= 4) launch_w_mac_uni<4, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
+  else launch_w_mac_uni<8, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
+}
+
+namespace {
+// CTAs of BC jobs, each within one key's consecutive jobs
+template <int BC, bool FOLD>
+void launch_w_mac_ml(const WidePrimes& w, const MlTab& t, const MlKeys& keys, const uint2* dtt, uint2* acc,
+                     cudaStream_t s) {
+  MlMac kt;
+  kt.keys = keys;
+  for (int j = 0; j <= t.J; ++j) kt.dig[j] = t.dig[j], kt.acc[j] = t.acc[j];
+  int ctas = 0, D = 0;
+  for (int k = 0; k < keys.n; ++k) {
+    D = keys.k[k].D > D ? keys.k[k].D : D;
+    for (int b = 0; b < keys.k[k].count; b += BC) {
+      kt.ch_key[ctas] = (unsigned char)k;
+      kt.ch_first[ctas] = (short)(keys.k[k].first + b);
+      kt.ch_n[ctas] = (unsigned char)(keys.k[k].count - b < BC ? keys.k[k].count - b : BC);
+      ++ctas;
+    }
+  }
+  launch_w_mac<BC, FOLD>(w, kt, D, ctas, dtt, acc, 0, s);
+}
+}  // namespace
+
+void wide_mac_ml(const WidePrimes& w, const MlTab& t, const MlKeys& keys, const uint2* dtt, uint2* acc, int bc_max,
+                 cudaStream_t s) {
+  if (t.J <= 0 || keys.n <= 0) return;
+  ProfScope p("wide_mac", s);
+  int most = 0, D = 0;
+  for (int k = 0; k < keys.n; ++k) {
+    most = keys.k[k].count > most ? keys.k[k].count : most;
+    D = keys.k[k].D > D ? keys.k[k].D : D;
+  }
+  const int want = most < bc_max ? most : bc_max;
+  if (D > 64) {
+    if (want <= 1) launch_w_mac_ml<1, true>(w, t, keys, dtt, acc, s);
+    else if (want <= 2) launch_w_mac_ml<2, true>(w, t, keys, dtt, acc, s);
+    else launch_w_mac_ml<4, true>(w, t, keys, dtt, acc, s);
+    return;
+  }
+  if (want <= 1) launch_w_mac_ml<1, false>(w, t, keys, dtt, acc, s);
+  else if (want <= 2) launch_w_mac_ml<2, false>(w, t, keys, dtt, acc, s);
+  else if (want <= 4) launch_w_mac_ml<4, false>(w, t, keys, dtt, acc, s);
+  else launch_w_mac_ml<8, false>(w, t, keys, dtt, acc, s);
 }
 
 int wide_kernel_errors(bool clear) {
@@ -603,7 +736,7 @@ bool wide_key_build(const WidePrimes& w, const u64* key, int digits, int limbs, 
   const int polys = digits * 2 * limbs;
   k_w_key_prep<<<grid_for_elems((size_t)polys * N), 256, 0, s>>>(w, key, tmp, digits, limbs);
   // forward transforms in place (the column phase reads tmp and writes tmp)
-  if (!w_forward_dispatch<1, false>(w, tmp, tmp, nullptr, polys, 1, s)) return false;
+  if (!w_forward_dispatch<1, false>(w, tmp, tmp, nullptr, polys, UniDig{1}, s)) return false;
   k_w_key_tile<<<grid_for_elems((size_t)polys * 2 * N), 256, 0, s>>>(tmp, kwt, digits, limbs, w.log_n);
   return true;
 }
