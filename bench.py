@@ -599,14 +599,13 @@ def mixed_level_relin(C, ctx, params, O, seed, count=128, reps=3):
     side = torch.cuda.Stream()
     res = {"jobs": count, "limbs": "uniform 8..24", "levels_distinct": len(keys),
            "key_bytes_standard_form": int(sum(ctx.decomp_digits(lv) * 2 * (lv + 1 + len(p)) * n * 8 for lv in keys))}
+    lib = C.lib()
     with torch.cuda.stream(side):
-        ctx.reserve(max(levels), 32)
+        ctx.reserve(max(levels), count)
         outs = [torch.empty((2, lv, n), dtype=torch.int64, device="cuda") for lv in levels]
-        ctx.relinearize_rescale_batch(quads, ks, outs)  # warm
-        graph = ctx.capture_graph(lambda: ctx.relinearize_rescale_batch(quads, ks, outs))
         st = torch.cuda.current_stream()
-        for name, fn in (("direct", lambda: ctx.relinearize_rescale_batch(quads, ks, outs)),
-                         ("graph", graph.launch)):
+
+        def timed(fn):
             fn()
             st.synchronize()
             e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -615,9 +614,31 @@ def mixed_level_relin(C, ctx, params, O, seed, count=128, reps=3):
                 fn()
             e1.record(st)
             st.synchronize()
-            ms = e0.elapsed_time(e1) / reps
-            res[f"{name}_ms"] = round(ms, 3)
-            res[f"{name}_relin_per_s"] = round(count / (ms / 1e3), 1)
+            return e0.elapsed_time(e1) / reps
+
+        # level by level (one launch per level and pass), then all levels in one launch per pass
+        for mode, tag in ((0, "by_level_"), (1, "")):
+            C.call("rc_tune_set", ctx.handle, b"mixed_levels", mode)
+            ctx.relinearize_rescale_batch(quads, ks, outs)  # warm
+            graph = ctx.capture_graph(lambda: ctx.relinearize_rescale_batch(quads, ks, outs))
+            for name, fn in (("direct", lambda: ctx.relinearize_rescale_batch(quads, ks, outs)),
+                             ("graph", graph.launch)):
+                ms = timed(fn)
+                res[f"{tag}{name}_ms"] = round(ms, 3)
+                res[f"{tag}{name}_relin_per_s"] = round(count / (ms / 1e3), 1)
+            if mode == 1:  # launches per pass of the mixed-level form
+                buf = ctypes.create_string_buffer(1 << 16)
+                st.synchronize()
+                lib.rc_profile_enable(1)
+                lib.rc_profile_report(buf, len(buf))
+                ctx.relinearize_rescale_batch(quads, ks, outs)
+                lib.rc_profile_report(buf, len(buf))
+                lib.rc_profile_enable(0)
+                prof = json.loads(buf.value.decode())
+                res["launches_per_pass"] = {k: v["launches"] for k, v in sorted(prof.items())}
+                res["kernels_ms"] = {k: round(v["ms"], 3) for k, v in sorted(prof.items(), key=lambda kv: -kv[1]["ms"])}
+            del graph
+        C.call("rc_tune_set", ctx.handle, b"mixed_levels", 1)
         i = levels.index(low)
         qpl = O.Plans(n, params.primes[: low + 1])
         ppl = O.Plans(n, params.aux_primes)
@@ -1014,14 +1035,24 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the NTT microbenchmark and the mixed-level relinearization batch")
-    ap.add_argument("--extra-only", choices=["bsgs_matvec", "bootstrap"],
+    ap.add_argument("--extra-only", choices=["bsgs_matvec", "bootstrap", "mixed_level_relin", "ntt_microbench"],
                     help="run one of the extra workloads alone (a profiling case) and print its JSON object")
     ap.add_argument("--extra-batch", type=int, default=None, help="batch of --extra-only (default: its own)")
     args = ap.parse_args()
     if args.extra_only:
         pkg = load_package()
         from rnsckks_gb300 import context as C
-        fn = {"bsgs_matvec": bsgs_matvec_bench, "bootstrap": bootstrap_bench}[args.extra_only]
+        def on_bench_context(f):
+            def run(pkg, C, seed, **kw):
+                params = pkg.params.bench_params()
+                ctx = C.RnsCkksContext(params)
+                if f is mixed_level_relin:
+                    return f(C, ctx, params, load_oracle(), seed, **({"count": kw["batch"]} if kw else {}))
+                return f(C, ctx, params, peaks()[0], seed)
+            return run
+        fn = {"bsgs_matvec": bsgs_matvec_bench, "bootstrap": bootstrap_bench,
+              "mixed_level_relin": on_bench_context(mixed_level_relin),
+              "ntt_microbench": on_bench_context(ntt_microbench)}[args.extra_only]
         kw = {} if args.extra_batch is None else {"batch": args.extra_batch}
         print(json.dumps({args.extra_only: fn(pkg, C, args.seed, **kw)}), flush=True)
         return

@@ -93,7 +93,9 @@ int rc_reserve(rc_context* ctx, int32_t max_level, uint32_t max_batch, void* str
  * host_chunk / host_edge jobs, default 2), "lazy_ntt" (unreduced forward butterflies, only
  * when every prime is below 2^58), "fuse_tensor" (forward row phase + tensor + inverse row phase of a
  * ciphertext product in one kernel, default 1), "host_phased" (host-buffer batches of up to ks_jobs same-level
- * jobs: one key read for the batch, copies overlapped chunk by chunk; default 1), "mac_wait_polls" (polls of
+ * jobs: one key read for the batch, copies overlapped chunk by chunk; default 1), "mixed_levels" (relinearize batches
+ * whose jobs are at different levels: one launch per pass over all levels instead of one per level, default
+ * 1), "ml_jobs" (jobs per such launch, 1..128, default 128), "mac_wait_polls" (polls of
  * the key product's first wait for its staged digit transforms, 0..2^22, default 2^22; 0 makes every CTA
  * time out and raise the rc_kernel_errors flag, for testing that path).  Set them between calls, not while
  * calls on the context are in flight. */
@@ -271,8 +273,11 @@ int rc_rotate_hoisted(rc_context* ctx, uint32_t count, const rc_ciphertext* ct, 
                       const rc_ksk* const* keys, rc_ciphertext* out, void* stream);
 /* relinearize then rescale (context/ops.rs:111-122 followed by context/ops.rs:32-37) for `count`
  * quadratic ciphertexts of any mix of levels; the rescale is fused into the keyswitch's last pass.  out[i]
- * gets level - 1 and the rescaled scale.  After rc_reserve(ctx, top level, 32, stream) the call allocates
- * nothing and can be captured in a CUDA graph. */
+ * gets level - 1 and the rescaled scale.  A batch of several levels whose keys all take the wide key product
+ * runs as one launch per pass (decompose, digit transforms, key product, inverse transforms, finalize) over
+ * all its levels, in chunks of up to 128 jobs (tunable "ml_jobs"); other batches run level by level.  Both
+ * rc_relinearize_batch and this call do so.  After rc_reserve(ctx, top level, batch size, stream) the call
+ * allocates nothing and can be captured in a CUDA graph. */
 int rc_relinearize_rescale_batch(rc_context* ctx, uint32_t count, const rc_ciphertext* quadratic,
                                  const rc_ksk* const* keys, rc_ciphertext* out, void* stream);
 

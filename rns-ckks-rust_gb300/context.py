@@ -859,6 +859,17 @@ class RnsCkksContext:
         call("rc_mult_relinearized_batch", self.handle, n, L, R, K, O, _stream())
         return [RnsCiphertext(o, O[i].scale_bits, O[i].level) for i, o in enumerate(outs)]
 
+    def relinearize_batch(self, cts: Sequence[RnsQuadraticCiphertext],
+                          keys: Sequence[RnsKeySwitchingKey]) -> List[RnsCiphertext]:
+        """relinearize (context/ops.rs:111-122) of many quadratic ciphertexts (mixed levels) in one call."""
+        n = len(cts)
+        outs = [self._ct_out(2, c.level + 1) for c in cts]
+        Q = (RcCiphertext * n)(*[c.raw() for c in cts])
+        O = (RcCiphertext * n)(*[RcCiphertext(o.data_ptr(), 0, 0) for o in outs])
+        K = (ctypes.c_void_p * n)(*[k.handle for k in keys])
+        call("rc_relinearize_batch", self.handle, n, Q, K, O, _stream())
+        return [RnsCiphertext(o, O[i].scale_bits, O[i].level) for i, o in enumerate(outs)]
+
     def relinearize_rescale_batch(self, cts: Sequence[RnsQuadraticCiphertext],
                                   keys: Sequence[RnsKeySwitchingKey], outs: Optional[Sequence[torch.Tensor]] = None
                                   ) -> List[RnsCiphertext]:

@@ -303,6 +303,134 @@ void wide_ks_finish(rc_context* c, const WideKs& w, const std::vector<KsJob>& jo
   launch_check("finalize");
 }
 
+// ---- mixed-level wide key switch: every pass is one launch over jobs of different levels ----
+// Job j is at qlimbs[j] Q limbs; jobs sharing a key are consecutive.  Buffers: int32 digits [sum D][N],
+// column-phase work and tiled digit transforms [sum D][2][N], products [sum 2 (limbs + K)][2][N] (uint2).
+size_t ml_ks_bytes(const rc_context* c, const std::vector<KsJob>& jobs, const std::vector<int>& qlimbs, int K) {
+  size_t dig = 0, acc = 0;
+  for (size_t j = 0; j < jobs.size(); ++j) {
+    dig += (size_t)ks_digits(c, jobs[j].key, qlimbs[j]);
+    acc += (size_t)2 * (qlimbs[j] + K);
+  }
+  const size_t N = c->N;
+  return align_up(dig * N * 4, 256) + 2 * arena_size_u64(dig * 2 * N) + arena_size_u64(acc * 2 * N) + 1024;
+}
+
+// a job fits the mixed-level path: a wide key of the batch's kind whose level passes the wide product's bound
+bool ml_job_ok(const rc_context* c, const rc_ksk* key, int qlimbs, int K) {
+  if (!key || !key->wdata || (key->aux ? c->K : 0) != K) return false;
+  return wide_applies(c, qlimbs, K, ks_digits(c, key, qlimbs));
+}
+
+void keyswitch_ml(rc_context* c, const std::vector<KsJob>& jobs, const std::vector<int>& qlimbs, bool rescale,
+                  void* ws, cudaStream_t s) {
+  const int J = (int)jobs.size();
+  if (!J) return;
+  require(J <= ML_MAXJ, "internal: mixed-level chunk too large");
+  const int K = jobs[0].key->aux ? c->K : 0;
+  const size_t N = c->N;
+  MlTab t{};
+  MlPtrTab src{}, add{}, out{};
+  MlKeys keys{};
+  t.J = J;
+  int max_limbs = 0, max_W = 0;
+  for (int j = 0; j < J; ++j) {
+    check_key_for(c, jobs[j].key, qlimbs[j]);
+    require(ml_job_ok(c, jobs[j].key, qlimbs[j], K), "internal: job outside the mixed-level key switch");
+    const int D = ks_digits(c, jobs[j].key, qlimbs[j]);
+    t.limbs[j] = qlimbs[j];
+    t.dig[j + 1] = t.dig[j] + D;
+    t.acc[j + 1] = t.acc[j] + 2 * (qlimbs[j] + K);
+    src.p[j] = const_cast<uint64_t*>(jobs[j].poly);
+    add.p[2 * j] = const_cast<uint64_t*>(jobs[j].add0);
+    add.p[2 * j + 1] = const_cast<uint64_t*>(jobs[j].add1);
+    out.p[2 * j] = jobs[j].out0;
+    out.p[2 * j + 1] = jobs[j].out1;
+    max_limbs = std::max(max_limbs, qlimbs[j]);
+    max_W = std::max(max_W, level_info(c, qlimbs[j]).dt.W);
+    if (j == 0 || jobs[j].key->wdata != jobs[j - 1].key->wdata) {
+      require(keys.n < ML_MAXK, "internal: too many keys in a mixed-level chunk");
+      keys.k[keys.n++] = MlKey{(const uint2*)jobs[j].key->wdata, D, (int)jobs[j].key->digits, qlimbs[j] + K, j, 0};
+    }
+    require(keys.k[keys.n - 1].total == qlimbs[j] + K, "internal: one key at two levels");
+    keys.k[keys.n - 1].count++;
+  }
+  Arena ar(ws);
+  int32_t* digits = ar.take<int32_t>((size_t)t.dig[J] * N);
+  uint2* work = ar.take<uint2>((size_t)t.dig[J] * 2 * N);
+  uint2* dt = ar.take<uint2>((size_t)t.dig[J] * 2 * N);
+  uint2* acc = ar.take<uint2>((size_t)t.acc[J] * 2 * N);
+  decompose_ml(c->d_pc, c->d_dts, t, src, max_limbs, max_W, digits, c->log_n, s);
+  launch_check("decompose (mixed levels)");
+  require(wide_digit_transforms_ml(c->wp, t, digits, work, dt, s), "internal: wide transforms unsupported");
+  launch_check("wide digit transforms (mixed levels)");
+  wide_mac_ml(c->wp, t, keys, dt, acc, c->mac_bc, s);
+  launch_check("wide mac (mixed levels)");
+  require(wide_inverse(c->wp, acc, t.acc[J], s), "internal: wide transforms unsupported");
+  launch_check("wide inverse transforms (mixed levels)");
+  FinalizeArgs f;
+  f.pc = c->d_pc;
+  f.md = c->md;
+  f.rt = c->rt;
+  f.L = c->L;
+  f.n = c->N;
+  f.log_n = c->log_n;
+  f.qlimbs = max_limbs;
+  f.K = K;
+  f.rescale = rescale ? 1 : 0;
+  f.add_g_inv = 0;
+  f.wide = 1;
+  f.wt = c->wide;
+  f.lazy = 1;
+  for (uint64_t m : c->mod)
+    if (m >= UINT64_MAX / (uint64_t)(8 + 2 * K)) f.lazy = 0;
+  finalize_ml(f, t, (const uint64_t*)acc, add, out, s);
+  launch_check("finalize (mixed levels)");
+}
+
+// Key switch + add (+ rescale) of a batch of any levels: when every job fits the mixed-level path, the jobs
+// (highest level first, jobs of one key together) run in chunks of up to ml_jobs jobs, each chunk one
+// launch per pass; otherwise false (the caller groups by level).
+bool keyswitch_mixed_batch(rc_context* c, const rc_ciphertext* qct, const rc_ksk* const* keys, rc_ciphertext* out,
+                           uint32_t count, bool rescale, cudaStream_t s) {
+  if (!c->mixed_levels || !c->wide_ok || count < 2) return false;
+  const int K = keys[0]->aux ? c->K : 0;
+  bool mixed = false;
+  for (uint32_t i = 0; i < count; ++i) {
+    if (!ml_job_ok(c, keys[i], qct[i].level + 1, K)) return false;
+    mixed = mixed || qct[i].level != qct[0].level;
+  }
+  if (!mixed) return false;  // one level: the uniform path
+  std::vector<int> order(count);
+  for (uint32_t i = 0; i < count; ++i) order[i] = (int)i;
+  std::stable_sort(order.begin(), order.end(), [&](int a, int b) {
+    if (qct[a].level != qct[b].level) return qct[a].level > qct[b].level;
+    return keys[a]->wdata < keys[b]->wdata;
+  });
+  size_t b = 0;
+  while (b < order.size()) {
+    std::vector<KsJob> jobs;
+    std::vector<int> ql;
+    int nkeys = 0;
+    for (size_t k = b; k < order.size() && (int)jobs.size() < c->ml_jobs; ++k) {
+      const int i = order[k];
+      const bool new_key = jobs.empty() || keys[i]->wdata != jobs.back().key->wdata;
+      if (new_key && nkeys == ML_MAXK) break;
+      nkeys += new_key ? 1 : 0;
+      const int limbs = qct[i].level + 1;
+      const size_t pl = (size_t)limbs * c->N;
+      const size_t po = (size_t)(rescale ? limbs - 1 : limbs) * c->N;
+      jobs.push_back(KsJob{qct[i].data + 2 * pl, keys[i], qct[i].data, qct[i].data + pl, out[i].data,
+                           out[i].data + po});
+      ql.push_back(limbs);
+    }
+    void* ws = ws_device(c, s, ml_ks_bytes(c, jobs, ql, K));
+    keyswitch_ml(c, jobs, ql, rescale, ws, s);
+    b += jobs.size();
+  }
+  return true;
+}
+
 // Runs keyswitch for `jobs` jobs at `qlimbs` limbs (all keys of the same kind);
 // the result is finalized with addends, optional automorphism on the addend and
 // optional rescale.  g_inv: automorphism applied to the keyswitched polynomial
@@ -715,6 +843,15 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
       li.dt.small_q = li.bits <= 30 ? 1 : 0;
       li.dt.Qsmall = li.bits <= 63 ? Q.words(1)[0] : 0;
     }
+    // the same tables as one device array indexed by limb count, for launches that mix levels
+    {
+      std::vector<DecompTab> dts(c->L + 1);
+      for (int l = 1; l <= c->L; ++l) dts[l] = c->levels[l].dt;
+      c->dt_buf.reset(new DevBuf(dts.size() * sizeof(DecompTab)));
+      c->d_dts = (DecompTab*)c->dt_buf->p;
+      cuda_check(cudaMemcpy(c->d_dts, dts.data(), dts.size() * sizeof(DecompTab), cudaMemcpyHostToDevice),
+                 "upload level tables");
+    }
 
     // ---- ModDown tables (aux basis)
     {
@@ -945,6 +1082,11 @@ extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
       c->fuse_tensor = value != 0;
     } else if (n == "host_phased") {
       c->host_phased = value != 0;
+    } else if (n == "mixed_levels") {
+      c->mixed_levels = value != 0;
+    } else if (n == "ml_jobs") {
+      require(value >= 1 && value <= ML_MAXJ, "ml_jobs must be in 1.." + std::to_string(ML_MAXJ));
+      c->ml_jobs = value;
     } else if (n == "mac_wait_polls") {
       require(value >= 0 && value <= (1 << 22), "mac_wait_polls must be in 0..4194304");
       c->wp.first_wait_polls = (uint32_t)value;
@@ -971,6 +1113,8 @@ extern "C" int rc_tune_get(const rc_context* c, const char* name, int32_t* value
     else if (n == "fuse_tensor") *value = c->fuse_tensor ? 1 : 0;
     else if (n == "host_phased") *value = c->host_phased ? 1 : 0;
     else if (n == "mac_wait_polls") *value = (int32_t)c->wp.first_wait_polls;
+    else if (n == "mixed_levels") *value = c->mixed_levels ? 1 : 0;
+    else if (n == "ml_jobs") *value = c->ml_jobs;
     else fail(RC_ERR_INVALID_ARGUMENT, "unknown tunable " + n);
   });
 }
@@ -986,6 +1130,14 @@ extern "C" int rc_reserve(rc_context* c, int32_t max_level, uint32_t max_batch, 
     size_t need = align_up(std::max(ks_ws_bytes(c, J, limbs, c->K, D), tensor_ws_bytes(c, std::min(J, MAXP / 4), limbs)),
                            256) +
                   arena_size_u64((size_t)3 * J * pl) + 256;
+    // a mixed-level chunk of up to ml_jobs jobs, each at most at max_level (digits with the same headroom)
+    if (c->wide_ok) {
+      const int JM = (int)std::min<uint32_t>(max_batch ? max_batch : 1, (uint32_t)c->ml_jobs);
+      const size_t N = c->N;
+      const size_t dig = (size_t)JM * D, acc = (size_t)JM * 2 * (limbs + c->K);
+      need = std::max(need, align_up(dig * N * 4, 256) + 2 * arena_size_u64(dig * 2 * N) +
+                                arena_size_u64(acc * 2 * N) + 1024);
+    }
     ws_device(c, S(stream), need);
   });
 }
@@ -1585,7 +1737,15 @@ extern "C" int rc_relinearize_batch(rc_context* c, uint32_t count, const rc_ciph
     for (uint32_t i = 0; i < count; ++i) {
       check_ct(c, &qct[i], "quadratic ciphertext");
       require(keys[i] != nullptr, "keyswitch key must not be null");
+      check_key_for(c, keys[i], qct[i].level + 1);
       groups[{qct[i].level, {(int)keys[i]->aux, (int)keys[i]->digits}}].push_back((int)i);
+    }
+    if (keyswitch_mixed_batch(c, qct, keys, out, count, false, S(stream))) {
+      for (uint32_t i = 0; i < count; ++i) {
+        out[i].level = qct[i].level;
+        out[i].scale_bits = qct[i].scale_bits;
+      }
+      return;
     }
     for (auto& g : groups) {
       const int limbs = g.first.first + 1;
@@ -1616,7 +1776,16 @@ extern "C" int rc_relinearize_rescale_batch(rc_context* c, uint32_t count, const
       require(out[i].data != qct[i].data, "rescale output must not alias its input");
       require(qct[i].level >= 1, "rescale requires at least two levels");
       require(keys[i] != nullptr, "keyswitch key must not be null");
+      check_key_for(c, keys[i], qct[i].level + 1);
       groups[{qct[i].level, {(int)keys[i]->aux, (int)keys[i]->digits}}].push_back((int)i);
+    }
+    if (keyswitch_mixed_batch(c, qct, keys, out, count, true, S(stream))) {
+      for (uint32_t i = 0; i < count; ++i) {
+        out[i].level = qct[i].level - 1;
+        const int sb = qct[i].scale_bits - floor_log2(c->mod[qct[i].level]);  // rescale_ciphertext_rns
+        out[i].scale_bits = sb < 0 ? 0 : sb;
+      }
+      return;
     }
     // groups run from the highest level down, each in chunks of at most MAXP/2 jobs (the size rc_reserve
     // provisions), so one reserve of the top level covers a whole mixed-level batch under graph capture

@@ -127,6 +127,8 @@ struct rc_context {
   rc::Twiddle* d_twf = nullptr;
   rc::Twiddle* d_twi = nullptr;
   std::vector<rc::LevelInfo> levels;  // index = limb count (1..L)
+  std::unique_ptr<rc::DevBuf> dt_buf;
+  rc::DecompTab* d_dts = nullptr;     // levels[l].dt for l = 0..L on the device (entry 0 unused)
   rc::ModDownTab md{};
   rc::RescaleTab rt{};
   std::vector<uint64_t> host_halfP;
@@ -141,6 +143,8 @@ struct rc_context {
   int host_edge = 2;    // its first and last stages have host_chunk / host_edge jobs
   bool fuse_tensor = true;  // forward rows + tensor + inverse rows in one kernel
   bool host_phased = true;  // host-buffer batches: one key read for the batch, transfers overlapped per chunk
+  bool mixed_levels = true;  // mixed-level key-switch batches: one launch per pass over all levels
+  int ml_jobs = rc::ML_MAXJ;  // jobs per mixed-level chunk (each chunk one launch per pass)
 
   rc::NttArgs ntt() const {
     rc::NttArgs a;

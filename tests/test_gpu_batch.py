@@ -174,3 +174,45 @@ def test_one_graph_spans_ring_degrees(env, pkg):
         for o, d in zip(o1 + o2, d1 + d2):
             assert torch.equal(o, d)
     torch.cuda.synchronize()
+
+
+def test_mixed_levels_run_one_launch_per_pass(env):
+    """A batch of seven levels runs each pass of the key switch (decompose, digit transforms, key product,
+    inverse transforms, finalize) as one launch over all levels; its residues equal the level-by-level path
+    (mixed_levels off) and the per-op path, also when the batch is cut into chunks of 5 jobs."""
+    import ctypes
+    import json
+    C, ctx, params, keys, host_keys, O = env
+    rng = np.random.default_rng(55)
+    levels = [int(x) for x in rng.integers(1, 8, 23)]
+    assert len(set(levels)) >= 5
+    cts = [_quad(C, rng, params, lv)[0] for lv in levels]
+    ks = [keys[lv] for lv in levels]
+    lib = C.lib()
+    buf = ctypes.create_string_buffer(1 << 16)
+    torch.cuda.synchronize()
+    lib.rc_profile_enable(1)
+    lib.rc_profile_report(buf, len(buf))  # reset
+    mixed = [o.numpy() for o in ctx.relinearize_rescale_batch(cts, ks)]
+    lib.rc_profile_report(buf, len(buf))
+    lib.rc_profile_enable(0)
+    prof = json.loads(buf.value.decode())
+    for name in ("decompose", "wide_digit_ntt", "wide_mac", "wide_inv_rows", "wide_inv_cols", "finalize"):
+        assert prof[name]["launches"] == 1, (name, prof)
+    plain = [o.numpy() for o in ctx.relinearize_batch(cts, ks)]
+    try:
+        C.call("rc_tune_set", ctx.handle, b"mixed_levels", 0)
+        by_level = [o.numpy() for o in ctx.relinearize_rescale_batch(cts, ks)]
+        plain_by_level = [o.numpy() for o in ctx.relinearize_batch(cts, ks)]
+        C.call("rc_tune_set", ctx.handle, b"mixed_levels", 1)
+        C.call("rc_tune_set", ctx.handle, b"ml_jobs", 5)
+        chunked = [o.numpy() for o in ctx.relinearize_rescale_batch(cts, ks)]
+    finally:
+        C.call("rc_tune_set", ctx.handle, b"mixed_levels", 1)
+        C.call("rc_tune_set", ctx.handle, b"ml_jobs", 128)
+    for i, lv in enumerate(levels):
+        assert np.array_equal(mixed[i], by_level[i]), i
+        assert np.array_equal(mixed[i], chunked[i]), i
+        assert np.array_equal(plain[i], plain_by_level[i]), i
+    for i in (0, int(np.argmin(levels))):
+        assert np.array_equal(mixed[i], ctx.rescale(ctx.relinearize(cts[i], ks[i])).numpy())
