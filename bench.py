@@ -648,7 +648,7 @@ def mixed_level_relin(C, ctx, params, O, seed, count=128, reps=3):
         res["bit_exact_vs_cpu"] = bool(np.array_equal(got[0], O.rescale_poly(qpl, r0))
                                        and np.array_equal(got[1], O.rescale_poly(qpl, r1)))
         res["checked_job_limbs"] = low + 1
-    del graph, quads, outs, keys
+    del quads, outs, keys
     torch.cuda.synchronize()
     return res
 
