@@ -499,6 +499,48 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def hmult_profile(C, ctx, params, seed, batch=8, reps=3):
+    """A small fixed case for profilers: `batch` pairs of uniform-residue ciphertexts at the top of the
+    benchmark chain and a uniform-residue relinearization key (no key generation launches), `reps` calls of
+    rc_mult_relinearized_batch with NVTX ranges on, so a profiler can select the kernels of those calls by
+    the range "rc_mult_relinearized_batch".  Returns the mean ms per call (CUDA events)."""
+    import torch
+    n, q, p = params.poly_degree, params.q_moduli(), params.p_moduli()
+    limbs = len(q)
+    rng = np.random.default_rng(seed)
+    D = ctx.decomp_digits(limbs - 1)
+    key = np.empty((D, 2, limbs + len(p), n), dtype=np.uint64)
+    for j, m in enumerate(q + p):
+        key[:, :, j, :] = rng.integers(0, m, (D, 2, n), dtype=np.uint64)
+    ksk = ctx.upload_keyswitch_key(key, limbs - 1, len(p))
+    del key
+    mod = torch.tensor(q, dtype=torch.int64, device="cuda").view(1, limbs, 1)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    lhs = [C.RnsCiphertext(torch.randint(0, 1 << 62, (2, limbs, n), device="cuda", generator=gen) % mod, 40)
+           for _ in range(batch)]
+    rhs = [C.RnsCiphertext(torch.randint(0, 1 << 62, (2, limbs, n), device="cuda", generator=gen) % mod, 40)
+           for _ in range(batch)]
+    # the launch shapes the benchmark's tuner picks on this GPU at the benchmark batch
+    for name, v in ((b"fuse_tensor", 0), (b"lazy_ntt", 1), (b"mac_bc", 8), (b"ks_jobs", 32)):
+        C.call("rc_tune_set", ctx.handle, name, v)
+    ctx.reserve(limbs - 1, batch)
+    ctx.mult_relinearized_batch(lhs, rhs, [ksk] * batch)  # warm: workspace, kernel loading
+    torch.cuda.synchronize()
+    lib = C.lib()
+    lib.rc_profile_enable(2)
+    st = torch.cuda.current_stream()
+    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    e0.record(st)
+    for _ in range(reps):
+        ctx.mult_relinearized_batch(lhs, rhs, [ksk] * batch)
+    e1.record(st)
+    torch.cuda.synchronize()
+    lib.rc_profile_enable(0)
+    return {"batch": batch, "reps": reps, "ms_per_call": round(e0.elapsed_time(e1) / reps, 4),
+            "nvtx_range": "rc_mult_relinearized_batch"}
+
+
 def ntt_microbench(C, ctx, params, peak, seed, reps=5):
     """Batched NTT/INTT microbenchmark: 64 polynomials x 24 limbs at N=2^16 (uniform residues), forward then
     inverse as one batched call each, against one call per polynomial, and the batched pair replayed as one
@@ -1035,7 +1077,8 @@ def main():
     ap.add_argument("--no-cpu", action="store_true", help="skip the CPU baseline leg")
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the NTT microbenchmark and the mixed-level relinearization batch")
-    ap.add_argument("--extra-only", choices=["bsgs_matvec", "bootstrap", "mixed_level_relin", "ntt_microbench"],
+    ap.add_argument("--extra-only", choices=["bsgs_matvec", "bootstrap", "mixed_level_relin", "ntt_microbench",
+                                             "hmult_profile"],
                     help="run one of the extra workloads alone (a profiling case) and print its JSON object")
     ap.add_argument("--extra-batch", type=int, default=None, help="batch of --extra-only (default: its own)")
     args = ap.parse_args()
@@ -1048,11 +1091,14 @@ def main():
                 ctx = C.RnsCkksContext(params)
                 if f is mixed_level_relin:
                     return f(C, ctx, params, load_oracle(), seed, **({"count": kw["batch"]} if kw else {}))
+                if f is hmult_profile:
+                    return f(C, ctx, params, seed, **kw)
                 return f(C, ctx, params, peaks()[0], seed)
             return run
         fn = {"bsgs_matvec": bsgs_matvec_bench, "bootstrap": bootstrap_bench,
               "mixed_level_relin": on_bench_context(mixed_level_relin),
-              "ntt_microbench": on_bench_context(ntt_microbench)}[args.extra_only]
+              "ntt_microbench": on_bench_context(ntt_microbench),
+              "hmult_profile": on_bench_context(hmult_profile)}[args.extra_only]
         kw = {} if args.extra_batch is None else {"batch": args.extra_batch}
         print(json.dumps({args.extra_only: fn(pkg, C, args.seed, **kw)}), flush=True)
         return
