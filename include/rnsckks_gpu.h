@@ -93,7 +93,9 @@ int rc_reserve(rc_context* ctx, int32_t max_level, uint32_t max_batch, void* str
  * host_chunk / host_edge jobs, default 2), "lazy_ntt" (unreduced forward butterflies, only
  * when every prime is below 2^58), "fuse_tensor" (forward row phase + tensor + inverse row phase of a
  * ciphertext product in one kernel, default 1), "host_phased" (host-buffer batches of up to ks_jobs same-level
- * jobs: one key read for the batch, copies overlapped chunk by chunk; default 1), "mixed_levels" (relinearize batches
+ * jobs: 1 = one key read for the batch, copies overlapped chunk by chunk; 2 = two such groups on two compute
+ * streams, the second's copy-in and preparation overlapping the first's key product; 0 = independent
+ * stages; default 1), "mixed_levels" (relinearize batches
  * whose jobs are at different levels: one launch per pass over all levels instead of one per level, default
  * 1), "ml_jobs" (jobs per such launch, 1..128, default 128), "mac_wait_polls" (polls of
  * the key product's first wait for its staged digit transforms, 0..2^22, default 2^22; 0 makes every CTA

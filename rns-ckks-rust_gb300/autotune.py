@@ -22,7 +22,8 @@ DEVICE_CANDIDATES: Dict[str, Sequence[int]] = {"ks_jobs": (8, 16, 32, 64), "mac_
                                                "fuse_tensor": (0, 1)}
 # host_edge: the first and last stages have chunk / host_edge jobs (a shorter fill and drain against one more
 # stage's overhead)
-HOST_CANDIDATES: Dict[str, Sequence[int]] = {"host_chunk": (2, 4, 8, 16), "host_phased": (0, 1),
+# host_phased: 0 independent stages, 1 one key-product group, 2 two groups on two compute streams
+HOST_CANDIDATES: Dict[str, Sequence[int]] = {"host_chunk": (2, 4, 8, 16), "host_phased": (0, 1, 2),
                                              "host_edge": (2, 4)}
 
 

@@ -726,6 +726,8 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
     c->lazy = true;
     if (const char* e = getenv("RNSCKKS_LAZY_NTT")) c->lazy = atoi(e) != 0;
     for (uint64_t q : c->mod) c->lazy = c->lazy && q < (1ull << 58);
+    c->lazy_inv = true;
+    for (uint64_t q : c->mod) c->lazy_inv = c->lazy_inv && q < (1ull << 55);
     if (const char* e = getenv("RNSCKKS_MAC64")) c->mac64 = atoi(e) != 0;
 
     // ---- per-prime constants and twiddles
@@ -1081,7 +1083,8 @@ extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
     } else if (n == "fuse_tensor") {
       c->fuse_tensor = value != 0;
     } else if (n == "host_phased") {
-      c->host_phased = value != 0;
+      require(value >= 0 && value <= 2, "host_phased must be 0, 1 or 2");
+      c->host_phased = value;
     } else if (n == "mixed_levels") {
       c->mixed_levels = value != 0;
     } else if (n == "ml_jobs") {
@@ -1111,7 +1114,7 @@ extern "C" int rc_tune_get(const rc_context* c, const char* name, int32_t* value
     else if (n == "host_edge") *value = c->host_edge;
     else if (n == "lazy_ntt") *value = c->lazy ? 1 : 0;
     else if (n == "fuse_tensor") *value = c->fuse_tensor ? 1 : 0;
-    else if (n == "host_phased") *value = c->host_phased ? 1 : 0;
+    else if (n == "host_phased") *value = c->host_phased;
     else if (n == "mac_wait_polls") *value = (int32_t)c->wp.first_wait_polls;
     else if (n == "mixed_levels") *value = c->mixed_levels ? 1 : 0;
     else if (n == "ml_jobs") *value = c->ml_jobs;
@@ -1984,12 +1987,6 @@ extern "C" int rc_rotate_hoisted(rc_context* c, uint32_t count, const rc_ciphert
 // =========================================================================
 // host-buffer entry points
 // =========================================================================
-// Host-buffer batch of up to ks_jobs same-level jobs on the wide key-switch path, in phases so that one key
-// read serves the whole batch while transfers still overlap the arithmetic: the inputs of all chunks are
-// copied in back to back; each chunk's tensor, decomposition and digit transforms start as soon as its
-// inputs have landed; one key-product pass covers all jobs; then each chunk's inverse transforms and
-// finalize run and its results are copied out while the next chunk finishes.  Returns false (nothing
-// done) when the batch does not fit this form.
 // Stage boundaries of a pipelined host-buffer batch.  Only the first stage's copy-in and the last stage's
 // copy-out are not overlapped with arithmetic, so those two stages get chunk / edge jobs and the others
 // chunk: [e, c, c, ..., c, rest - e, e].
@@ -2010,10 +2007,103 @@ static std::vector<uint32_t> stage_bounds(uint32_t count, uint32_t chunk, uint32
   return b;
 }
 
+// One key-product group of a phased host-buffer batch: jobs [j0, j1) of the call, computed on `cs` with
+// staging slot `sl`; inputs go through hp->in in job order, outputs through hp->out.  Returns the event of
+// its last copy out.
+static cudaEvent_t host_phased_group(rc_context* c, HostPipe* hp, uint32_t j0, uint32_t j1,
+                                     const uint64_t* const* lhs, const uint64_t* const* rhs, const int32_t* levels,
+                                     const int32_t* scale_bits, const rc_ksk* const* keys, uint64_t* const* out,
+                                     int32_t* out_scale_bits, cudaStream_t cs, int sl, int chunk, int K, int D) {
+  const int limbs = levels[j0] + 1;
+  const int J = (int)(j1 - j0);
+  const size_t N = c->N, pl = (size_t)limbs * N, po = (size_t)(limbs - 1) * N;
+  // staging: inputs [J][lhs, rhs][2][limbs][N], outputs [J][2][limbs-1][N]
+  const size_t stage = ((size_t)J * 4 * pl + (size_t)J * 2 * po) * 8;
+  if (!hp->slot[sl] || hp->slot[sl]->bytes < stage) {
+    for (cudaStream_t st : {hp->in, hp->comp, hp->out, hp->comp2})
+      cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
+    hp->slot[sl].reset();
+    hp->slot[sl].reset(new DevBuf(stage));
+  }
+  uint64_t* in_dev = (uint64_t*)hp->slot[sl]->p;
+  uint64_t* out_dev = in_dev + (size_t)J * 4 * pl;
+  const size_t tbytes = tensor_ws_bytes(c, chunk, limbs);
+  char* ws = (char*)ws_device(c, cs, arena_size_u64((size_t)3 * J * pl) + align_up(tbytes, 256) +
+                                         wide_ks_bytes(c, J, chunk, limbs, K, D) + 1024);
+  Arena ar(ws);
+  uint64_t* quads = ar.take<uint64_t>((size_t)3 * J * pl);
+  char* tscr = ar.take<char>(tbytes);
+  const WideKs w = wide_ks_layout(c, ar, J, chunk, limbs, K, D);
+
+  const std::vector<uint32_t> bounds = stage_bounds((uint32_t)J, (uint32_t)chunk, (uint32_t)c->host_edge);
+  const int nchunks = (int)bounds.size() - 1;
+  std::vector<cudaEvent_t> in_done(nchunks), comp_done(nchunks);
+  for (int k = 0; k < nchunks; ++k) {  // every chunk's inputs, back to back in job order
+    for (int j = (int)bounds[k]; j < (int)bounds[k + 1]; ++j) {
+      cuda_check(cudaMemcpyAsync(in_dev + (size_t)j * 4 * pl, lhs[j0 + j], 2 * pl * 8, cudaMemcpyHostToDevice,
+                                 hp->in),
+                 "H2D");
+      cuda_check(cudaMemcpyAsync(in_dev + (size_t)j * 4 * pl + 2 * pl, rhs[j0 + j], 2 * pl * 8,
+                                 cudaMemcpyHostToDevice, hp->in),
+                 "H2D");
+    }
+    in_done[k] = hp->event();
+    cuda_check(cudaEventRecord(in_done[k], hp->in), "cudaEventRecord");
+  }
+  std::vector<KsJob> jobs(J);
+  for (int j = 0; j < J; ++j) {
+    uint64_t* qd = quads + (size_t)j * 3 * pl;
+    jobs[j] = KsJob{qd + 2 * pl, keys[j0 + j], qd, qd + pl, out_dev + (size_t)j * 2 * po,
+                    out_dev + (size_t)j * 2 * po + po};
+  }
+  for (int k = 0; k < nchunks; ++k) {
+    const int b0 = (int)bounds[k], n = (int)bounds[k + 1] - b0;
+    cuda_check(cudaStreamWaitEvent(cs, in_done[k], 0), "wait");
+    std::vector<const uint64_t*> Lp(n), Rp(n);
+    std::vector<uint64_t*> Q(n);
+    for (int j = 0; j < n; ++j) {
+      Lp[j] = in_dev + (size_t)(b0 + j) * 4 * pl;
+      Rp[j] = Lp[j] + 2 * pl;
+      Q[j] = quads + (size_t)(b0 + j) * 3 * pl;
+    }
+    tensor_core(c, Lp, Rp, Q, limbs, tscr, cs);
+    wide_ks_prepare(c, w, jobs, b0, n, 0, cs);
+  }
+  wide_ks_mac(c, w, jobs, cs);
+  const int drop = floor_log2(c->mod[limbs - 1]);
+  for (int k = 0; k < nchunks; ++k) {
+    const int b0 = (int)bounds[k], n = (int)bounds[k + 1] - b0;
+    wide_ks_finish(c, w, jobs, b0, n, 0, true, cs);
+    comp_done[k] = hp->event();
+    cuda_check(cudaEventRecord(comp_done[k], cs), "cudaEventRecord");
+    cuda_check(cudaStreamWaitEvent(hp->out, comp_done[k], 0), "wait");
+    for (int j = b0; j < b0 + n; ++j) {
+      cuda_check(cudaMemcpyAsync(out[j0 + j], out_dev + (size_t)j * 2 * po, 2 * po * 8, cudaMemcpyDeviceToHost,
+                                 hp->out),
+                 "D2H");
+      if (out_scale_bits) {
+        const int sb = scale_bits[j0 + j] + scale_bits[j0 + j] - drop;  // mult_relinearized, context/ops.rs:124-133
+        out_scale_bits[j0 + j] = sb < 0 ? 0 : sb;
+      }
+    }
+  }
+  cudaEvent_t fin = hp->event();
+  cuda_check(cudaEventRecord(fin, hp->out), "cudaEventRecord");
+  return fin;
+}
+
+// Host-buffer batch of up to ks_jobs same-level jobs on the wide key-switch path in `groups` key-product
+// groups (1 or 2).  Each group is phased: its inputs are copied in back to back, each chunk's tensor,
+// decomposition and digit transforms start as soon as the chunk's inputs have landed, one key-product pass
+// covers the group, then each chunk's inverse transforms and finalize run and its results are copied out
+// while the next chunk finishes.  With two groups the second computes on its own stream and staging slot,
+// so its copy-in and preparation overlap the first group's key product and the first group's copy-out
+// overlaps the second's arithmetic (one more key read).  Returns false (nothing done) when the batch does
+// not fit this form.
 static bool mult_relin_host_phased(rc_context* c, HostPipe* hp, uint32_t count, const uint64_t* const* lhs,
                                    const uint64_t* const* rhs, const int32_t* levels, const int32_t* scale_bits,
                                    const rc_ksk* const* keys, uint64_t* const* out, int32_t* out_scale_bits,
-                                   cudaStream_t s, int chunk) {
+                                   cudaStream_t s, int chunk, int groups) {
   const int level = levels[0];
   if (count > (uint32_t)c->ks_jobs) return false;
   for (uint32_t i = 0; i < count; ++i)
@@ -2031,83 +2121,20 @@ static bool mult_relin_host_phased(rc_context* c, HostPipe* hp, uint32_t count, 
   for (uint32_t i = 0; i < count; ++i)
     if (!K && (int)keys[i]->digits != D) return false;
   if (!wide_applies(c, limbs, K, D)) return false;
-  const int J = (int)count;
   chunk = std::max(1, std::min(chunk, MAXP / 4));
-  const size_t N = c->N, pl = (size_t)limbs * N, po = (size_t)(limbs - 1) * N;
-  // staging: inputs [J][lhs, rhs][2][limbs][N], outputs [J][2][limbs-1][N]
-  const size_t stage = ((size_t)J * 4 * pl + (size_t)J * 2 * po) * 8;
-  if (!hp->slot[0] || hp->slot[0]->bytes < stage) {
-    for (cudaStream_t st : {hp->in, hp->comp, hp->out, hp->comp2})
-      cuda_check(cudaStreamSynchronize(st), "cudaStreamSynchronize");
-    hp->slot[0].reset();
-    hp->slot[0].reset(new DevBuf(stage));
-  }
-  uint64_t* in_dev = (uint64_t*)hp->slot[0]->p;
-  uint64_t* out_dev = in_dev + (size_t)J * 4 * pl;
-  const size_t tbytes = tensor_ws_bytes(c, chunk, limbs);
-  char* ws = (char*)ws_device(c, hp->comp, arena_size_u64((size_t)3 * J * pl) + align_up(tbytes, 256) +
-                                               wide_ks_bytes(c, J, chunk, limbs, K, D) + 1024);
-  Arena ar(ws);
-  uint64_t* quads = ar.take<uint64_t>((size_t)3 * J * pl);
-  char* tscr = ar.take<char>(tbytes);
-  const WideKs w = wide_ks_layout(c, ar, J, chunk, limbs, K, D);
-
+  groups = std::max(1, std::min(groups, 2));
+  if (count < 2) groups = 1;
   cudaEvent_t start = hp->event();
   cuda_check(cudaEventRecord(start, s), "cudaEventRecord");
-  for (cudaStream_t st : {hp->in, hp->comp, hp->out})
+  for (cudaStream_t st : {hp->in, hp->comp, hp->out, hp->comp2})
     cuda_check(cudaStreamWaitEvent(st, start, 0), "cudaStreamWaitEvent");
-  const std::vector<uint32_t> bounds = stage_bounds((uint32_t)J, (uint32_t)chunk, (uint32_t)c->host_edge);
-  const int nchunks = (int)bounds.size() - 1;
-  std::vector<cudaEvent_t> in_done(nchunks), comp_done(nchunks);
-  for (int k = 0; k < nchunks; ++k) {  // every chunk's inputs, back to back in job order
-    for (int j = (int)bounds[k]; j < (int)bounds[k + 1]; ++j) {
-      cuda_check(cudaMemcpyAsync(in_dev + (size_t)j * 4 * pl, lhs[j], 2 * pl * 8, cudaMemcpyHostToDevice, hp->in),
-                 "H2D");
-      cuda_check(cudaMemcpyAsync(in_dev + (size_t)j * 4 * pl + 2 * pl, rhs[j], 2 * pl * 8, cudaMemcpyHostToDevice,
-                                 hp->in),
-                 "H2D");
-    }
-    in_done[k] = hp->event();
-    cuda_check(cudaEventRecord(in_done[k], hp->in), "cudaEventRecord");
-  }
-  std::vector<KsJob> jobs(J);
-  for (int j = 0; j < J; ++j) {
-    uint64_t* qd = quads + (size_t)j * 3 * pl;
-    jobs[j] = KsJob{qd + 2 * pl, keys[j], qd, qd + pl, out_dev + (size_t)j * 2 * po, out_dev + (size_t)j * 2 * po + po};
-  }
-  for (int k = 0; k < nchunks; ++k) {
-    const int b0 = (int)bounds[k], n = (int)bounds[k + 1] - b0;
-    cuda_check(cudaStreamWaitEvent(hp->comp, in_done[k], 0), "wait");
-    std::vector<const uint64_t*> Lp(n), Rp(n);
-    std::vector<uint64_t*> Q(n);
-    for (int j = 0; j < n; ++j) {
-      Lp[j] = in_dev + (size_t)(b0 + j) * 4 * pl;
-      Rp[j] = Lp[j] + 2 * pl;
-      Q[j] = quads + (size_t)(b0 + j) * 3 * pl;
-    }
-    tensor_core(c, Lp, Rp, Q, limbs, tscr, hp->comp);
-    wide_ks_prepare(c, w, jobs, b0, n, 0, hp->comp);
-  }
-  wide_ks_mac(c, w, jobs, hp->comp);
-  const int drop = floor_log2(c->mod[limbs - 1]);
-  for (int k = 0; k < nchunks; ++k) {
-    const int b0 = (int)bounds[k], n = (int)bounds[k + 1] - b0;
-    wide_ks_finish(c, w, jobs, b0, n, 0, true, hp->comp);
-    comp_done[k] = hp->event();
-    cuda_check(cudaEventRecord(comp_done[k], hp->comp), "cudaEventRecord");
-    cuda_check(cudaStreamWaitEvent(hp->out, comp_done[k], 0), "wait");
-    for (int j = b0; j < b0 + n; ++j) {
-      cuda_check(cudaMemcpyAsync(out[j], out_dev + (size_t)j * 2 * po, 2 * po * 8, cudaMemcpyDeviceToHost, hp->out),
-                 "D2H");
-      if (out_scale_bits) {
-        const int sb = scale_bits[j] + scale_bits[j] - drop;  // mult_relinearized, context/ops.rs:124-133
-        out_scale_bits[j] = sb < 0 ? 0 : sb;
-      }
-    }
-  }
-  cudaEvent_t fin = hp->event();
-  cuda_check(cudaEventRecord(fin, hp->out), "cudaEventRecord");
-  cuda_check(cudaStreamWaitEvent(s, fin, 0), "wait");
+  const uint32_t split = groups == 2 ? (count + 1) / 2 : count;
+  cudaEvent_t fin = host_phased_group(c, hp, 0, split, lhs, rhs, levels, scale_bits, keys, out, out_scale_bits,
+                                      hp->comp, 0, chunk, K, D);
+  if (split < count)
+    fin = host_phased_group(c, hp, split, count, lhs, rhs, levels, scale_bits, keys, out, out_scale_bits, hp->comp2,
+                            1, chunk, K, D);
+  cuda_check(cudaStreamWaitEvent(s, fin, 0), "wait");  // the copies out are in order on hp->out
   cuda_check(cudaStreamSynchronize(hp->out), "cudaStreamSynchronize");
   return true;
 }
@@ -2140,8 +2167,8 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
     hp->next = 0;
     int chunk = c->host_chunk;  // jobs per pipeline stage
     if (const char* e = getenv("RNSCKKS_HOST_CHUNK")) chunk = std::max(1, atoi(e));
-    if (c->host_phased &&
-        mult_relin_host_phased(c, hp, count, lhs, rhs, levels, scale_bits, keys, out, out_scale_bits, s, chunk))
+    if (c->host_phased && mult_relin_host_phased(c, hp, count, lhs, rhs, levels, scale_bits, keys, out,
+                                                 out_scale_bits, s, chunk, c->host_phased))
       return;
     const std::vector<uint32_t> bounds = stage_bounds(count, (uint32_t)chunk, (uint32_t)c->host_edge);
     const uint32_t nchunks = (uint32_t)bounds.size() - 1;

@@ -112,6 +112,7 @@ struct rc_context {
   int scale_bits = 0;
   int device = 0;
   bool lazy = false;   // every prime < 2^58
+  bool lazy_inv = false;  // every prime < 2^55 (2^9 q < 2^64: an unreduced 8-stage inverse pass)
   bool mac64 = false;  // 64-bit per-term Montgomery accumulation in the key product
   bool wide_ok = false;  // exact integer key product under the four internal primes available
   rc::WidePrimes wp{};    // internal primes, transform constants and twiddle tables (wide_tw)
@@ -142,7 +143,7 @@ struct rc_context {
   int host_chunk = 8;   // jobs per stage of the pipelined host-buffer entry
   int host_edge = 2;    // its first and last stages have host_chunk / host_edge jobs
   bool fuse_tensor = true;  // forward rows + tensor + inverse rows in one kernel
-  bool host_phased = true;  // host-buffer batches: one key read for the batch, transfers overlapped per chunk
+  int host_phased = 1;  // host-buffer batches: key-product groups (0 = staged, 1 or 2 phased groups)
   bool mixed_levels = true;  // mixed-level key-switch batches: one launch per pass over all levels
   int ml_jobs = rc::ML_MAXJ;  // jobs per mixed-level chunk (each chunk one launch per pass)
 
@@ -154,6 +155,7 @@ struct rc_context {
     a.log_n = log_n;
     a.n1 = n1;
     a.lazy = lazy ? 1 : 0;
+    a.lazy_inv = lazy_inv ? 1 : 0;
     return a;
   }
 };

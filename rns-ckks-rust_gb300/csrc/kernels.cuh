@@ -65,6 +65,7 @@ struct NttArgs {
   int n1;    // column-phase size 2^n1; row-phase size 2^(log_n - n1)
   int lazy;  // all primes < 2^58: forward butterflies skip the [0,4q) correction
   int mont_out = 0;  // inverse: scale by N^-1 2^64 instead of N^-1 (inputs are Montgomery products)
+  int lazy_inv = 0;  // all primes < 2^55: the inverse column pass runs without reductions
 };
 
 // Negacyclic NTT over `polys` x `limbs` limbs, src -> dst (may alias).

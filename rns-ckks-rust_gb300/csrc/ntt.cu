@@ -199,7 +199,8 @@ __device__ __forceinline__ u64 reduce_out(u64 x, const PrimeConst& c) {
 
 // Column phase: the CTA stages a tile of COLS columns (2^M1 rows each) and the
 // column twiddle table in shared memory; each warp transforms SUBS columns at
-// a time in registers.
+// a time in registers.  LAZY: forward, unreduced butterflies; inverse, butterflies without reductions
+// (inputs below 2q, primes below 2^55), the final N^-1 product reducing every output.
 template <int M1, int M2, bool LAZY, bool FWD>
 __global__ __launch_bounds__(256, 3) void k_cols_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
   using G = core::Geo<M1>;
@@ -242,7 +243,7 @@ __global__ __launch_bounds__(256, 3) void k_cols_f(NttArgs a, PtrTab src, PtrTab
 #pragma unroll
       for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::last_idx<M1>(l, k))];
       __syncwarp();
-      core::inv_sub<M1>(v, buf, l, twl, q);
+      core::inv_sub<M1, LAZY>(v, buf, l, twl, q);
 #pragma unroll
       for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::first_idx<M1>(l, k))] = v[k];
     }
@@ -345,7 +346,8 @@ void inv_fast(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys,
   }
   {
     ProfScope p("ntt_inv_cols", s);
-    k_cols_f<M1, M2, false, false><<<g1, 256, 0, s>>>(a, dst, dst, map);
+    if (a.lazy_inv) k_cols_f<M1, M2, true, false><<<g1, 256, 0, s>>>(a, dst, dst, map);
+    else k_cols_f<M1, M2, false, false><<<g1, 256, 0, s>>>(a, dst, dst, map);
   }
 }
 
@@ -424,7 +426,8 @@ void inv_cols_fast(const NttArgs& a, const PtrTab& data, int polys, int limbs, L
   constexpr int N2 = 1 << M2;
   dim3 g1(N2 / ColTile<M1>::COLS, limbs, polys);
   ProfScope p("ntt_inv_cols", s);
-  k_cols_f<M1, M2, false, false><<<g1, 256, 0, s>>>(a, data, data, map);
+  if (a.lazy_inv) k_cols_f<M1, M2, true, false><<<g1, 256, 0, s>>>(a, data, data, map);
+  else k_cols_f<M1, M2, false, false><<<g1, 256, 0, s>>>(a, data, data, map);
 }
 
 template <bool LAZY>

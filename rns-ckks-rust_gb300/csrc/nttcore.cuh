@@ -176,26 +176,53 @@ __device__ __forceinline__ void fwd_group(u64 (&v)[8], int l, const Twiddle* __r
   }
 }
 
-// Gentleman-Sande butterflies of one group, stages in decreasing order; values
-// stay in [0, 2q).
+// stages of the inverse sub-transform done before group GI starts (groups run from the last down)
 template <int M, int GI>
+__host__ __device__ constexpr int inv_done() {
+  if constexpr (GI + 1 < NGroups<M>::value) return Grp<M, GI + 1>::G + inv_done<M, GI + 1>();
+  else return 0;
+}
+
+// Gentleman-Sande butterflies of one group, stages in decreasing order; values
+// stay in [0, 2q).  LAZYI (inputs of the sub-transform below 2q): no reductions; after c stages of the
+// sub-transform values are below 2^(c+1) q, so the difference path adds that bound as its offset and its
+// Shoup product restarts below 2q; valid while 2^(M+1) q < 2^64, and the caller reduces the outputs.
+template <int M, int GI, bool LAZYI = false>
 __device__ __forceinline__ void inv_group(u64 (&v)[8], int l, const Twiddle* __restrict__ tw, u64 q) {
   constexpr int S0 = Grp<M, GI>::S0, G = Grp<M, GI>::G;
   const u64 two_q = q << 1;
+  if constexpr (LAZYI) {
 #pragma unroll
-  for (int j = G - 1; j >= 0; --j) {
-    const int s = S0 + j;
-    const int b = G - 1 - j;
+    for (int j = G - 1; j >= 0; --j) {
+      const int s = S0 + j;
+      const int b = G - 1 - j;
+      const int c = inv_done<M, GI>() + (G - 1 - j);  // stages done before this one
 #pragma unroll
-    for (int k = 0; k < 8; ++k) {
-      if (k & (1 << b)) continue;
-      const int r = gidx<M, S0, G>(l, k);
-      const Twiddle w = tw[(1 << s) + (r >> (M - s))];
-      const u64 x = v[k], y = v[k | (1 << b)];
-      u64 u = x + y;
-      u = u >= two_q ? u - two_q : u;
-      v[k] = u;
-      v[k | (1 << b)] = mul_shoup_lazy(x - y + two_q, w.w, w.ws, q);
+      for (int k = 0; k < 8; ++k) {
+        if (k & (1 << b)) continue;
+        const int r = gidx<M, S0, G>(l, k);
+        const Twiddle w = tw[(1 << s) + (r >> (M - s))];
+        const u64 x = v[k], y = v[k | (1 << b)];
+        v[k] = x + y;
+        v[k | (1 << b)] = mul_shoup_lazy(x - y + (q << (c + 1)), w.w, w.ws, q);
+      }
+    }
+  } else {
+#pragma unroll
+    for (int j = G - 1; j >= 0; --j) {
+      const int s = S0 + j;
+      const int b = G - 1 - j;
+#pragma unroll
+      for (int k = 0; k < 8; ++k) {
+        if (k & (1 << b)) continue;
+        const int r = gidx<M, S0, G>(l, k);
+        const Twiddle w = tw[(1 << s) + (r >> (M - s))];
+        const u64 x = v[k], y = v[k | (1 << b)];
+        u64 u = x + y;
+        u = u >= two_q ? u - two_q : u;
+        v[k] = u;
+        v[k | (1 << b)] = mul_shoup_lazy(x - y + two_q, w.w, w.ws, q);
+      }
     }
   }
 }
@@ -225,15 +252,15 @@ __device__ __forceinline__ void fwd_sub(u64 (&v)[8], u64* buf, int l, const Twid
 }
 
 // full inverse sub-transform: v holds the last group's layout on entry, group 0's on exit
-template <int M>
+template <int M, bool LAZYI = false>
 __device__ __forceinline__ void inv_sub(u64 (&v)[8], u64* buf, int l, const Twiddle* tw, u64 q) {
   if constexpr (NGroups<M>::value == 3) {
-    inv_group<M, 2>(v, l, tw, q);
+    inv_group<M, 2, LAZYI>(v, l, tw, q);
     exchange<M, 2, 1>(v, buf, l);
   }
-  inv_group<M, 1>(v, l, tw, q);
+  inv_group<M, 1, LAZYI>(v, l, tw, q);
   exchange<M, 1, 0>(v, buf, l);
-  inv_group<M, 0>(v, l, tw, q);
+  inv_group<M, 0, LAZYI>(v, l, tw, q);
 }
 
 template <int M>
@@ -288,8 +315,8 @@ __device__ __forceinline__ void fwd_group2(uint2 (&v)[8], int l, const Tw2* __re
       const Tw2 w = tw[(1 << s) + (r >> (M - s))];
       uint2 x = v[k];
       const uint2 y = v[k | (1 << b)];
-      x.x = x.x >= t0 ? x.x - t0 : x.x;
-      x.y = x.y >= t1 ? x.y - t1 : x.y;
+      x.x = min(x.x, x.x - t0);  // x - t0 wraps above x when x < t0
+      x.y = min(x.y, x.y - t1);
       const uint32_t u0 = mul_shoup32_lazy(y.x, w.w0, w.s0, q0);
       const uint32_t u1 = mul_shoup32_lazy(y.y, w.w1, w.s1, q1);
       v[k] = make_uint2(x.x + u0, x.y + u1);

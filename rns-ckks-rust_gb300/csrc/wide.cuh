@@ -7,7 +7,7 @@ namespace rc {
 
 __device__ __forceinline__ uint32_t mul_shoup32(uint32_t x, uint32_t w, uint32_t ws, uint32_t q) {
   const uint32_t r = x * w - __umulhi(x, ws) * q;
-  return r >= q ? r - q : r;
+  return min(r, r - q);  // r - q wraps above r when r < q
 }
 
 // x mod q for any 64-bit x (bar = floor(2^64 / q))
@@ -20,7 +20,7 @@ __device__ __forceinline__ uint32_t reduce64_32(u64 x, uint32_t q, u64 bar) {
 __device__ __forceinline__ uint32_t sub32(uint32_t a, uint32_t b, uint32_t q) { return a >= b ? a - b : a + q - b; }
 
 // v < 2q -> v mod q
-__device__ __forceinline__ uint32_t fold32(uint32_t v, uint32_t q) { return v >= q ? v - q : v; }
+__device__ __forceinline__ uint32_t fold32(uint32_t v, uint32_t q) { return min(v, v - q); }
 
 // wide_crt_mod with the per-prime constants passed in: S * F mod q for a factor F given as
 // (F mod q + Shoup) = (lo_w, lo_ws), (w0 w1 F) mod q + Shoup = (c01, c01_s) and (A F) mod q = a_mod

@@ -99,3 +99,39 @@ def test_negated_shoup_companion():
         for w in [1, 2, q - 1, q // 2] + [rng.randrange(1, q) for _ in range(500)]:
             ws = (w << 64) // q
             assert ((q - w) << 64) // q == M64 - ws
+
+
+def _shoup_lazy(x, w, q):
+    """The kernels' mul_shoup_lazy: x w - floor(x floor(w 2^64 / q) / 2^64) q, mod 2^64."""
+    ws = (w << 64) // q
+    return (x * w - ((x * ws) >> 64) * q) & M64
+
+
+@pytest.mark.parametrize("bits", [50, 54])
+def test_lazy_inverse_pass_stays_below_2_64_and_matches_the_reduced_pass(bits):
+    """The unreduced Gentleman-Sande pass of the inverse column phase (primes below 2^55, M = 8 stages,
+    inputs below 2q): the sum path's bound doubles per stage, the difference path adds 2^(c+1) q before its
+    Shoup product; every intermediate stays below 2^64 and every output is congruent to the reduced pass's,
+    here on a 256-point sub-transform with random twiddles and adversarial (all 2q - 1) inputs."""
+    rng = random.Random(bits)
+    q = _primes(bits, 1)[0]
+    assert q < 1 << 55
+    M = 8
+    tw = {(s, j): rng.randrange(1, q) for s in range(M) for j in range(1 << s)}
+    for inputs in ([2 * q - 1] * (1 << M), [rng.randrange(2 * q) for _ in range(1 << M)]):
+        lazy, ref = list(inputs), [x % q for x in inputs]
+        for c, s in enumerate(reversed(range(M))):  # stage s = M-1 .. 0; c stages done before it
+            t = 1 << (M - 1 - s)
+            for blk in range(0, 1 << M, 2 * t):
+                for i in range(blk, blk + t):
+                    w = tw[(s, i >> (M - s))] if (i >> (M - s)) < (1 << s) else tw[(s, 0)]
+                    x, y = lazy[i], lazy[i + t]
+                    assert x < (2 << c) * q and y < (2 << c) * q
+                    d = x - y + (q << (c + 1))
+                    assert 0 <= d < 1 << 64 and x + y < 1 << 64
+                    lazy[i], lazy[i + t] = x + y, _shoup_lazy(d, w, q)
+                    assert lazy[i + t] < 2 * q
+                    rx, ry = ref[i], ref[i + t]
+                    ref[i], ref[i + t] = (rx + ry) % q, (rx - ry) * w % q
+        assert all(v < (2 << M) * q for v in lazy)
+        assert [v % q for v in lazy] == ref
