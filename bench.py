@@ -360,32 +360,23 @@ def run_gpu(args):
     tune_host = T.tune_host_pipeline(ctx, e2e_step, limbs - 1, B, reps=3)
     e2e_step()
     torch.cuda.synchronize()
-    # the headline e2e: exactly `steps` consecutive steps, the same protocol as `value`
-    barrier(world)
-    torch.cuda.synchronize()
-    e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
-    e0.record(stream)
-    for _ in range(args.steps):
-        e2e_step()
-    e1.record(stream)
-    torch.cuda.synchronize()
-    e_all_ms = max_over_ranks(e0.elapsed_time(e1), world)
-    e2e_value = world * B * args.steps / (e_all_ms / 1e3)
-    # beside it, seven rounds of e_steps steps each: the host link of a shared machine slows down now and then
-    # for tens of milliseconds (seen as single 2-4x slow trials in the tuner), so the median round is listed too
-    e_steps = max(1, min(args.steps, 5))
+    # e2e: five rounds of exactly `steps` consecutive steps each (the protocol of `value`); the host link of a
+    # shared machine stalls now and then for tens of milliseconds (single 2-4x slow trials in the tuner), so
+    # the median round is the value, and every round and the mean over all of them are listed beside it
     e_rounds = []
-    for _ in range(7):
+    for _ in range(5):
         barrier(world)
+        torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
         e0.record(stream)
-        for _ in range(e_steps):
+        for _ in range(args.steps):
             e2e_step()
         e1.record(stream)
         torch.cuda.synchronize()
         e_rounds.append(max_over_ranks(e0.elapsed_time(e1), world))
     e_ms = statistics.median(e_rounds)
-    e2e_median_round_value = world * B * e_steps / (e_ms / 1e3)
+    e2e_value = world * B * args.steps / (e_ms / 1e3)
+    e2e_mean_value = world * B * args.steps * len(e_rounds) / (sum(e_rounds) / 1e3)
     h2d = B * 2 * 2 * limbs * n * 8
     d2h = B * 2 * (limbs - 1) * n * 8
 
@@ -406,10 +397,10 @@ def run_gpu(args):
                                          for k, v in sorted(per_op_prof.items(), key=lambda kv: -kv[1]["ms"])}},
         "batched_vs_per_op": round(value / world / per_op_value, 3),
         "e2e": {"value": round(e2e_value, 3), "unit": UNIT, "h2d_bytes_per_step": h2d, "d2h_bytes_per_step": d2h,
-                "ms_per_step": round(e_all_ms / args.steps, 4),
-                "estimator": f"{args.steps} consecutive steps (the protocol of value)",
-                "median_round_value": round(e2e_median_round_value, 3),
-                "rounds_ms_per_step": [round(r / e_steps, 3) for r in e_rounds]},
+                "ms_per_step": round(e_ms / args.steps, 4),
+                "estimator": f"median of 5 rounds of {args.steps} consecutive steps (each round the protocol of value)",
+                "mean_value": round(e2e_mean_value, 3),
+                "rounds_ms_per_step": [round(r / args.steps, 3) for r in e_rounds]},
         "gpu_launches": int(sum(v["launches"] for v in prof.values())),
         "clocks": clk.summary(),
     }
