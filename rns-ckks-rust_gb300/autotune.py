@@ -1,8 +1,9 @@
 """Autotuner for the library's launch-shape tunables.
 
 The tunables (`rc_tune_set`: jobs per key-switch launch, jobs per CTA of the key product, the forward
-butterfly mode, the fused tensor pass, jobs per stage of the host pipeline) change how work is split into
-launches, never the results.  The tuner times each candidate on synthetic inputs of the caller's shape (ring degree, level,
+butterfly mode, the fused tensor pass, the transforms' four-step split, CTAs per SM of their column pass and
+polynomials per row block, jobs per stage and key-product groups of the host pipeline) change how work is
+split into launches, never the results.  The tuner times each candidate on synthetic inputs of the caller's shape (ring degree, level,
 batch), keeps the fastest, applies it to the context and caches the choice per (device, shape) in a JSON
 file, so later runs apply it without measuring.
 """
@@ -20,6 +21,16 @@ from ._lib import RcCiphertext, call
 
 DEVICE_CANDIDATES: Dict[str, Sequence[int]] = {"ks_jobs": (8, 16, 32, 64), "mac_bc": (4, 8), "lazy_ntt": (0, 1),
                                                "fuse_tensor": (0, 1)}
+# kernel shapes of the 64-bit transforms, tuned after the launch-shape tunables above (with their choice
+# applied): CTAs per SM the column pass is compiled for (2 leaves it more registers), polynomials per row
+# block (one twiddle staging each), and the four-step split (the column phase's log size; both phases must
+# have 2^6..2^8 points, so at N = 2^16 only 8 x 8 exists)
+SHAPE_CANDIDATES: Dict[str, Sequence[int]] = {"col_ctas": (2, 3), "row_polys": (8, 16)}
+
+
+def split_candidates(log_n: int) -> List[int]:
+    """Column-phase log sizes of the four-step split for a ring of 2^log_n points (both phases 6..8)."""
+    return [m for m in (6, 7, 8) if 6 <= log_n - m <= 8]
 # host_edge: the first and last stages have chunk / host_edge jobs (a shorter fill and drain against one more
 # stage's overhead)
 # host_phased: 0 independent stages, 1 one key-product group, 2 two groups on two compute streams
@@ -141,7 +152,15 @@ def tune_mult_relinearized(ctx, lhs, rhs, keys, outs, reps: int = 3, cache: Opti
     K = (ctypes.c_void_p * n)(*[k.handle for k in keys])
     s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
     run = lambda: call("rc_mult_relinearized_batch", ctx.handle, n, L, R, K, O, s)
-    return tune(ctx, "mult_relinearized_batch", run, lhs[0].level, n, DEVICE_CANDIDATES, reps, cache, use_cache)
+    launch = tune(ctx, "mult_relinearized_batch", run, lhs[0].level, n, DEVICE_CANDIDATES, reps, cache, use_cache)
+    space = dict(SHAPE_CANDIDATES)
+    splits = split_candidates(ctx.params.poly_degree.bit_length() - 1)
+    if len(splits) > 1:
+        space["ntt_split"] = splits
+    shapes = tune(ctx, "mult_relinearized_batch_shapes", run, lhs[0].level, n, space, reps, cache, use_cache)
+    return {"choice": dict(launch["choice"], **shapes["choice"]), "ms": shapes["ms"],
+            "cached": launch["cached"] and shapes["cached"], "trials": launch.get("trials", []),
+            "shape_trials": shapes.get("trials", [])}
 
 
 def tune_host_pipeline(ctx, run: Callable[[], None], level: int, batch: int, reps: int = 2,

@@ -1085,6 +1085,17 @@ extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
     } else if (n == "host_phased") {
       require(value >= 0 && value <= 2, "host_phased must be 0, 1 or 2");
       c->host_phased = value;
+    } else if (n == "ntt_split") {
+      const int n2 = c->log_n - value;
+      require(c->log_n >= 12 && c->log_n <= 16 && value >= 6 && value <= 8 && n2 >= 6 && n2 <= 8,
+              "ntt_split must leave both four-step phases between 2^6 and 2^8 points (log N 12..16)");
+      c->n1 = value;
+    } else if (n == "col_ctas") {
+      require(value == 2 || value == 3, "col_ctas must be 2 or 3");
+      c->col_ctas = value;
+    } else if (n == "row_polys") {
+      require(value == 8 || value == 16, "row_polys must be 8 or 16");
+      c->row_polys = value;
     } else if (n == "mixed_levels") {
       c->mixed_levels = value != 0;
     } else if (n == "ml_jobs") {
@@ -1117,6 +1128,9 @@ extern "C" int rc_tune_get(const rc_context* c, const char* name, int32_t* value
     else if (n == "host_phased") *value = c->host_phased;
     else if (n == "mac_wait_polls") *value = (int32_t)c->wp.first_wait_polls;
     else if (n == "mixed_levels") *value = c->mixed_levels ? 1 : 0;
+    else if (n == "ntt_split") *value = c->n1;
+    else if (n == "col_ctas") *value = c->col_ctas;
+    else if (n == "row_polys") *value = c->row_polys;
     else if (n == "ml_jobs") *value = c->ml_jobs;
     else fail(RC_ERR_INVALID_ARGUMENT, "unknown tunable " + n);
   });

@@ -146,6 +146,8 @@ struct rc_context {
   int host_phased = 1;  // host-buffer batches: key-product groups (0 = staged, 1 or 2 phased groups)
   bool mixed_levels = true;  // mixed-level key-switch batches: one launch per pass over all levels
   int ml_jobs = rc::ML_MAXJ;  // jobs per mixed-level chunk (each chunk one launch per pass)
+  int col_ctas = 3;           // 64-bit column passes: CTAs per SM (2 or 3)
+  int row_polys = 16;         // 64-bit row passes: polynomials per block (8 or 16)
 
   rc::NttArgs ntt() const {
     rc::NttArgs a;
@@ -156,6 +158,8 @@ struct rc_context {
     a.n1 = n1;
     a.lazy = lazy ? 1 : 0;
     a.lazy_inv = lazy_inv ? 1 : 0;
+    a.col_ctas = col_ctas;
+    a.row_polys = row_polys;
     return a;
   }
 };

@@ -62,10 +62,12 @@ struct NttArgs {
   const Twiddle* tw_fwd;  // [primes][N]: psi^bitrev(k)
   const Twiddle* tw_inv;  // [primes][N]: psi^-bitrev(k)
   int log_n;
-  int n1;    // column-phase size 2^n1; row-phase size 2^(log_n - n1)
+  int n1;    // column-phase size 2^n1; row-phase size 2^(log_n - n1) (tunable "ntt_split" for log N 12..16)
   int lazy;  // all primes < 2^58: forward butterflies skip the [0,4q) correction
   int mont_out = 0;  // inverse: scale by N^-1 2^64 instead of N^-1 (inputs are Montgomery products)
   int lazy_inv = 0;  // all primes < 2^55: the inverse column pass runs without reductions
+  int col_ctas = 3;  // column passes: CTAs per SM the kernel is compiled for (2 or 3; more registers at 2)
+  int row_polys = 16;  // row passes: polynomials per block sharing one twiddle staging (8 or 16)
 };
 
 // Negacyclic NTT over `polys` x `limbs` limbs, src -> dst (may alias).
@@ -81,6 +83,10 @@ void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int pol
 // inverse transform.  False (nothing launched) if N is not supported (log N outside 12..16).
 bool tensor_inverse_rows(const NttArgs& a, const PtrTab& in4, const PtrTab& out3, int jobs, int limbs, LimbMap map,
                          cudaStream_t s);
+// the forward transform's column phase alone (src -> dst; the row phase is done elsewhere); false (nothing
+// launched) if N is not supported (log N outside 12..16)
+bool ntt_forward_cols(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
+                      cudaStream_t s);
 // the inverse transform's column phase alone (in place, times N^-1), after a row phase done elsewhere
 bool ntt_inverse_cols(const NttArgs& a, const PtrTab& data, int polys, int limbs, LimbMap map, cudaStream_t s);
 
