@@ -216,3 +216,52 @@ def test_mixed_levels_run_one_launch_per_pass(env):
         assert np.array_equal(plain[i], plain_by_level[i]), i
     for i in (0, int(np.argmin(levels))):
         assert np.array_equal(mixed[i], ctx.rescale(ctx.relinearize(cts[i], ks[i])).numpy())
+
+
+def test_mixed_levels_with_q_only_keys(pkg, oracle):
+    """The one-launch-per-pass form with Q-only keys (no aux basis; the digit count is the key's) on the plain
+    small chain (N=2^13, 60 + 41 + 41 bits): equal to the level-by-level form, to the per-op path and, for one
+    job, to the oracle's relinearize then rescale."""
+    import ctypes
+    import json
+    from rnsckks_gb300 import context as C
+    params = pkg.params.plain_small_params()
+    ctx = C.RnsCkksContext(params)
+    n, q = params.poly_degree, params.q_moduli()
+    rng = np.random.default_rng(91)
+    keys, host = {}, {}
+    for lv in (1, 2):
+        qm = q[: lv + 1]
+        D = math.ceil(math.prod(qm).bit_length() / 30)
+        k = np.stack([np.stack([np.stack([rng.integers(0, m, n, dtype=np.uint64) for m in qm])
+                                for _ in range(2)]) for _ in range(D)])
+        host[lv] = k
+        keys[lv] = ctx.upload_keyswitch_key(k, lv, 0)
+    levels = [2, 1, 2, 1, 1, 2]
+    raw = [np.stack([np.stack([rng.integers(0, m, n, dtype=np.uint64) for m in q[: lv + 1]]) for _ in range(3)])
+           for lv in levels]
+    cts = [C.RnsQuadraticCiphertext(C.to_device(r), 80) for r in raw]
+    ks = [keys[lv] for lv in levels]
+    lib = C.lib()
+    buf = ctypes.create_string_buffer(1 << 16)
+    torch.cuda.synchronize()
+    lib.rc_profile_enable(1)
+    lib.rc_profile_report(buf, len(buf))
+    mixed = [o.numpy() for o in ctx.relinearize_rescale_batch(cts, ks)]
+    lib.rc_profile_report(buf, len(buf))
+    lib.rc_profile_enable(0)
+    assert json.loads(buf.value.decode())["wide_mac"]["launches"] == 1
+    try:
+        C.call("rc_tune_set", ctx.handle, b"mixed_levels", 0)
+        by_level = [o.numpy() for o in ctx.relinearize_rescale_batch(cts, ks)]
+    finally:
+        C.call("rc_tune_set", ctx.handle, b"mixed_levels", 1)
+    for i in range(len(levels)):
+        assert np.array_equal(mixed[i], by_level[i]), i
+        assert np.array_equal(mixed[i], ctx.rescale(ctx.relinearize(cts[i], ks[i])).numpy()), i
+    lv = levels[0]
+    qpl = oracle.Plans(n, params.primes[: lv + 1])
+    d = raw[0]
+    r0, r1 = oracle.relinearize(qpl, None, d[0], d[1], d[2], host[lv], host[lv].shape[0])
+    assert np.array_equal(mixed[0][0], oracle.rescale_poly(qpl, r0))
+    assert np.array_equal(mixed[0][1], oracle.rescale_poly(qpl, r1))
