@@ -150,20 +150,6 @@ __global__ void k_decompose_s(const PrimeConst* pc, JT jt, int32_t* digits, u64 
   uint32_t* s_qhs = s_qh + limbs * C;                              // [limbs][C]
   uint32_t* s_Q = s_qhs + limbs * C;                               // [C]
   uint32_t* s_hQ = s_Q + C;                                        // [C]
-  // [limbs][threads]: this thread's residues, all requested at once (one memory latency per coefficient)
-  u64* s_r = reinterpret_cast<u64*>(s_hQ + C);  // 2 limbs C + 2 C words before it: 8-byte aligned
-  const u64 N = 1ull << log_n;
-  const u64 x = blockIdx.x * (u64)blockDim.x + threadIdx.x;
-  const u64* in = jt.in(job);
-  u64 sidx = x;
-  bool neg = false;
-  if (g_inv > 1) {
-    sidx = (x * g_inv) & (2 * N - 1);
-    neg = sidx >= N;
-    if (neg) sidx -= N;
-  }
-  if (x < N)
-    for (int l = 0; l < limbs; ++l) core::cp_async8(s_r + (size_t)l * blockDim.x + threadIdx.x, in + (u64)l * N + sidx);
   for (int e = threadIdx.x; e < limbs; e += blockDim.x) {
     s_q[e] = pc[e].q;
     s_hinv[e] = dt.qhat_inv[e];
@@ -175,16 +161,25 @@ __global__ void k_decompose_s(const PrimeConst* pc, JT jt, int32_t* digits, u64 
     s_Q[e] = dt.q32[e];
     s_hQ[e] = dt.hq32[e];
   }
-  core::cp_async_wait_all();
   __syncthreads();
+  const u64 N = 1ull << log_n;
+  const u64 x = blockIdx.x * (u64)blockDim.x + threadIdx.x;
   if (x >= N) return;
+  const u64* in = jt.in(job);
+  u64 sidx = x;
+  bool neg = false;
+  if (g_inv > 1) {
+    sidx = (x * g_inv) & (2 * N - 1);
+    neg = sidx >= N;
+    if (neg) sidx -= N;
+  }
   u64 A[CM];
 #pragma unroll
   for (int c = 0; c < CM; ++c) A[c] = 0;
   u64 fsum = 0;  // sum of y_i / q_i in units of 2^-31
   for (int l = 0; l < limbs; ++l) {
     const u64 q = s_q[l];
-    u64 r = s_r[(size_t)l * blockDim.x + threadIdx.x];
+    u64 r = in[(u64)l * N + sidx];
     if (neg && r) r = q - r;
     const u64 y = mul_shoup(r, s_hinv[l], s_hinv_s[l], q);
     const u64 fx = s_invq[l];
@@ -272,10 +267,7 @@ __global__ void k_decompose_s(const PrimeConst* pc, JT jt, int32_t* digits, u64 
   if (TIES && tie) atomicOr(&tie_flags[job], 1);
 }
 
-// tables, then this block's residues ([limbs][threads] words; the block size is at most 128)
-inline size_t split_smem_bytes(int limbs, int C) {
-  return (size_t)limbs * 4 * 8 + ((size_t)2 * limbs * C + 2 * C + 2) * 4 + (size_t)limbs * 128 * 8;
-}
+inline size_t split_smem_bytes(int limbs, int C) { return (size_t)limbs * 4 * 8 + ((size_t)2 * limbs * C + 2 * C) * 4; }
 
 // lift_poly_to_context (keyswitching.rs:242-276) for polynomial blockIdx.y: the Q limbs are copied and limb
 // limbs + k is the centred CRT value mod p_k (convert_centered_residues_to_target, 365-379):
@@ -1028,7 +1020,6 @@ void launch_decompose_s(dim3 g, int threads, size_t smem, cudaStream_t s, const 
 template <class JT>
 bool decompose_split_dispatch(int C, dim3 g, int threads, size_t smem, cudaStream_t s, const PrimeConst* pc,
                               const JT& jt, int32_t* digits, uint64_t g_inv, int log_n, int* tie_flags) {
-  if (smem > 48 * 1024 || threads > 128) return false;  // the static limit of dynamic shared memory
   if (C <= 16) launch_decompose_s<16>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
   else if (C <= 24) launch_decompose_s<24>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
   else if (C <= 32) launch_decompose_s<32>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
