@@ -131,14 +131,6 @@ struct Arena {
 
 size_t arena_size_u64(size_t count) { return align_up(count * 8, 256); }
 
-const LevelInfo& level_info(const rc_context* c, int limbs);
-// the level's decomposition tables with the context's choice of CRT-sum form
-DecompTab decomp_tab(const rc_context* c, int limbs) {
-  DecompTab d = level_info(c, limbs).dt;
-  d.split = c->decomp_form != 0 && d.split_ok ? 1 : 0;
-  return d;
-}
-
 const LevelInfo& level_info(const rc_context* c, int limbs) {
   require(limbs >= 1 && limbs <= c->L, "level out of range for this context");
   return c->levels[limbs];
@@ -254,7 +246,7 @@ void wide_ks_prepare(rc_context* c, const WideKs& w, const std::vector<KsJob>& j
   const size_t N = c->N;
   PtrTab src{};
   for (int j = 0; j < n; ++j) src.p[j] = const_cast<uint64_t*>(jobs[b0 + j].poly);
-  decompose(c->d_pc, decomp_tab(c, w.qlimbs), src, n, w.qlimbs, w.D, w.digits + (size_t)b0 * w.D * N, g_inv,
+  decompose(c->d_pc, level_info(c, w.qlimbs).dt, src, n, w.qlimbs, w.D, w.digits + (size_t)b0 * w.D * N, g_inv,
             c->log_n, s);
   launch_check("decompose");
   require(wide_digit_transforms(c->wp, w.D, n, w.digits + (size_t)b0 * w.D * N, w.work,
@@ -368,12 +360,7 @@ void keyswitch_ml(rc_context* c, const std::vector<KsJob>& jobs, const std::vect
   uint2* work = ar.take<uint2>((size_t)t.dig[J] * 2 * N);
   uint2* dt = ar.take<uint2>((size_t)t.dig[J] * 2 * N);
   uint2* acc = ar.take<uint2>((size_t)t.acc[J] * 2 * N);
-  int split = c->decomp_form != 0, max_C = 0;
-  for (int j = 0; j < J; ++j) {
-    split = split && level_info(c, qlimbs[j]).dt.split_ok;
-    max_C = std::max(max_C, level_info(c, qlimbs[j]).dt.C);
-  }
-  decompose_ml(c->d_pc, c->d_dts, t, src, max_limbs, max_W, digits, c->log_n, s, split, max_C);
+  decompose_ml(c->d_pc, c->d_dts, t, src, max_limbs, max_W, digits, c->log_n, s);
   launch_check("decompose (mixed levels)");
   require(wide_digit_transforms_ml(c->wp, t, digits, work, dt, s), "internal: wide transforms unsupported");
   launch_check("wide digit transforms (mixed levels)");
@@ -476,7 +463,7 @@ void keyswitch_core(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, u
   int32_t* digits = ar.take<int32_t>((size_t)J * D * N);
   PtrTab src{};
   for (int j = 0; j < J; ++j) src.p[j] = const_cast<uint64_t*>(jobs[j].poly);
-  decompose(c->d_pc, decomp_tab(c, qlimbs), src, J, qlimbs, D, digits, g_inv, c->log_n, s);
+  decompose(c->d_pc, li.dt, src, J, qlimbs, D, digits, g_inv, c->log_n, s);
   launch_check("decompose");
 
   FinalizeArgs f;
@@ -857,31 +844,6 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
       li.dt.W = W;
       li.dt.small_q = li.bits <= 30 ? 1 : 0;
       li.dt.Qsmall = li.bits <= 63 ? Q.words(1)[0] : 0;
-      // split form: Q/q_i and (Q/q_i) 2^25 in 32-bit words, Q and floor(Q/2) likewise
-      {
-        const int C = (int)((li.bits + 25 + 31) / 32) + 1;
-        bool ok = l <= 31 && C <= 64 && !li.dt.small_q;
-        for (int i = 0; i < l; ++i) ok = ok && qm[i] < (1ull << 50);
-        std::vector<uint32_t> b32;
-        auto push_words = [&](const BigU& v) {
-          const auto w = v.words((size_t)(C + 1) / 2);
-          for (int c = 0; c < C; ++c) b32.push_back((uint32_t)(w[(size_t)c / 2] >> (32 * (c & 1))));
-        };
-        for (int i = 0; i < l; ++i) push_words(Q.div_u64(qm[i]));
-        for (int i = 0; i < l; ++i) push_words(Q.div_u64(qm[i]).mul_u64(1ull << 25));
-        push_words(Q);
-        push_words(Q.shr1());
-        li.buf32.reset(new DevBuf(b32.size() * 4));
-        uint32_t* d32 = (uint32_t*)li.buf32->p;
-        cuda_check(cudaMemcpy(d32, b32.data(), b32.size() * 4, cudaMemcpyHostToDevice), "upload level tables");
-        li.dt.qh32 = d32;
-        li.dt.qhs32 = d32 + (size_t)l * C;
-        li.dt.q32 = d32 + (size_t)2 * l * C;
-        li.dt.hq32 = d32 + (size_t)2 * l * C + C;
-        li.dt.C = C;
-        li.dt.split_ok = ok ? 1 : 0;
-        li.dt.split = 0;
-      }
     }
     // the same tables as one device array indexed by limb count, for launches that mix levels
     {
@@ -1123,9 +1085,6 @@ extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
     } else if (n == "host_phased") {
       require(value >= 0 && value <= 2, "host_phased must be 0, 1 or 2");
       c->host_phased = value;
-    } else if (n == "decomp_form") {
-      require(value == 0 || value == 1, "decomp_form must be 0 or 1");
-      c->decomp_form = value;
     } else if (n == "ntt_split") {
       const int n2 = c->log_n - value;
       require(c->log_n >= 12 && c->log_n <= 16 && value >= 6 && value <= 8 && n2 >= 6 && n2 <= 8,
@@ -1170,7 +1129,6 @@ extern "C" int rc_tune_get(const rc_context* c, const char* name, int32_t* value
     else if (n == "mac_wait_polls") *value = (int32_t)c->wp.first_wait_polls;
     else if (n == "mixed_levels") *value = c->mixed_levels ? 1 : 0;
     else if (n == "ntt_split") *value = c->n1;
-    else if (n == "decomp_form") *value = c->decomp_form;
     else if (n == "col_ctas") *value = c->col_ctas;
     else if (n == "row_polys") *value = c->row_polys;
     else if (n == "ml_jobs") *value = c->ml_jobs;
@@ -2010,7 +1968,7 @@ extern "C" int rc_rotate_hoisted(rc_context* c, uint32_t count, const rc_ciphert
       cuda_check(cudaMemsetAsync(flags, 0, (size_t)n * sizeof(int), s), "cudaMemsetAsync");
       PtrTab src{};
       for (int j = 0; j < n; ++j) src.p[j] = cts[b0 + j].data + pl;
-      decompose(c->d_pc, decomp_tab(c, limbs), src, n, limbs, D, w.digits, 1, c->log_n, s, flags);
+      decompose(c->d_pc, level_info(c, limbs).dt, src, n, limbs, D, w.digits, 1, c->log_n, s, flags);
       launch_check("decompose");
       require(wide_digit_transforms(c->wp, D, n, w.digits, w.work, w.dt, s), "internal: wide transforms unsupported");
       launch_check("wide digit transforms");

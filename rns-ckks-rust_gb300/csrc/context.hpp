@@ -80,7 +80,7 @@ struct LevelInfo {
   size_t bits = 0;     // bits of Q_limbs
   int digits = 0;      // num_decomp_digits(bits, 30)
   DecompTab dt{};
-  std::shared_ptr<DevBuf> buf, buf32;
+  std::shared_ptr<DevBuf> buf;
 };
 
 struct Workspace {
@@ -148,7 +148,6 @@ struct rc_context {
   int ml_jobs = rc::ML_MAXJ;  // jobs per mixed-level chunk (each chunk one launch per pass)
   int col_ctas = 3;           // 64-bit column passes: CTAs per SM (2 or 3)
   int row_polys = 16;         // 64-bit row passes: polynomials per block (8 or 16)
-  int decomp_form = 1;        // decomposition's CRT sum: 0 = 64-bit words, 1 = 32-bit words x 25-bit halves
 
   rc::NttArgs ntt() const {
     rc::NttArgs a;

@@ -143,14 +143,6 @@ struct DecompTab {
   u64 Qsmall;            // Q when small_q
   const u64* lift_pw;    // [K][W+1]: 2^(64 w) mod p_k (the aux primes), w = 0..W
   const u64* lift_pw_s;  // Shoup companions
-  // the split form of the CRT sum (every prime of the level below 2^50, at most 31 limbs): 32-bit words
-  const uint32_t* qh32;   // [limbs][C] words of Q/q_i
-  const uint32_t* qhs32;  // [limbs][C] words of (Q/q_i) 2^25
-  const uint32_t* q32;    // [C] words of Q
-  const uint32_t* hq32;   // [C] words of floor(Q/2)
-  int C;                  // 32-bit columns: ceil((bits(Q) + 25) / 32) + 1
-  int split_ok;           // the level's tables and bounds allow the split form
-  int split;              // use it (set per call from the context's tunable "decomp_form")
 };
 
 struct ModDownTab {
@@ -253,7 +245,7 @@ void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const
 // digits of job j (src.p[j], limbs[j] Q limbs) from polynomial dig[j] of `digits`; d_dts[limbs] are the
 // per-level tables, max_limbs / max_W the largest job's
 void decompose_ml(const PrimeConst* pc, const DecompTab* d_dts, const MlTab& t, const MlPtrTab& src, int max_limbs,
-                  int max_W, int32_t* digits, int log_n, cudaStream_t s, int split = 0, int max_C = 0);
+                  int max_W, int32_t* digits, int log_n, cudaStream_t s);
 // finalize of wide products acc (job j's 2 (limbs[j] + K) limb polynomials from acc[j] on)
 void finalize_ml(const FinalizeArgs& f, const MlTab& t, const u64* acc, const MlPtrTab& addend, const MlPtrTab& out,
                  cudaStream_t s);

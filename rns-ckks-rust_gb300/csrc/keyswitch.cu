@@ -127,148 +127,6 @@ __global__ void k_decompose(const PrimeConst* pc, JT jt, int32_t* digits, u64 g_
   if (TIES && tie) atomicOr(&tie_flags[job], 1);
 }
 
-// The decomposition with the CRT sum in split form (every prime of the level below 2^50, at most 31 limbs):
-// each y_i = c_i (Q/q_i)^-1 mod q_i is split into 25-bit halves, and T = sum_i y_i (Q/q_i) is accumulated as
-// sum_i (y_lo Q/q_i + y_hi (Q/q_i) 2^25) over 32-bit words of the two tables: two 32x32->64 multiply-adds per
-// word, each product below 2^57, so 64-bit columns take the 62 products of 31 limbs without a carry.  The
-// rounding quotient k = floor(sum y_i / q_i + 1/2) comes from the fixed-point sum (each term at most 3 units
-// of 2^-31 low, so k is exact or one low); one carry pass gives X' = T - k Q as 32-bit words with its sign,
-// and X' is the centred value or the centred value plus Q (Q odd: centred means in [-(Q-1)/2, (Q-1)/2]), so one
-// comparison with floor(Q/2) and one conditional subtraction of Q finish it.  The digits are then read off
-// the two's complement words as in k_decompose: the same digits, with fewer multiplies and no carry chains.
-template <int CM, bool TIES, class JT>
-__global__ void k_decompose_s(const PrimeConst* pc, JT jt, int32_t* digits, u64 g_inv, int log_n, int* tie_flags) {
-  const int job = blockIdx.y;
-  const DecompTab& dt = jt.tab(job);
-  const int limbs = jt.nlimbs(job), D = jt.digits(job), C = dt.C;
-  extern __shared__ u64 dsm_tab[];
-  u64* s_q = dsm_tab;                 // [limbs]
-  u64* s_hinv = s_q + limbs;          // [limbs]
-  u64* s_hinv_s = s_hinv + limbs;     // [limbs]
-  u64* s_invq = s_hinv_s + limbs;     // [limbs]
-  uint32_t* s_qh = reinterpret_cast<uint32_t*>(s_invq + limbs);  // [limbs][C]
-  uint32_t* s_qhs = s_qh + limbs * C;                              // [limbs][C]
-  uint32_t* s_Q = s_qhs + limbs * C;                               // [C]
-  uint32_t* s_hQ = s_Q + C;                                        // [C]
-  for (int e = threadIdx.x; e < limbs; e += blockDim.x) {
-    s_q[e] = pc[e].q;
-    s_hinv[e] = dt.qhat_inv[e];
-    s_hinv_s[e] = dt.qhat_inv_s[e];
-    s_invq[e] = dt.inv_q[e];
-  }
-  for (int e = threadIdx.x; e < 2 * limbs * C; e += blockDim.x) s_qh[e] = dt.qh32[e];  // qh32 and qhs32 adjoin
-  for (int e = threadIdx.x; e < C; e += blockDim.x) {
-    s_Q[e] = dt.q32[e];
-    s_hQ[e] = dt.hq32[e];
-  }
-  __syncthreads();
-  const u64 N = 1ull << log_n;
-  const u64 x = blockIdx.x * (u64)blockDim.x + threadIdx.x;
-  if (x >= N) return;
-  const u64* in = jt.in(job);
-  u64 sidx = x;
-  bool neg = false;
-  if (g_inv > 1) {
-    sidx = (x * g_inv) & (2 * N - 1);
-    neg = sidx >= N;
-    if (neg) sidx -= N;
-  }
-  u64 A[CM];
-#pragma unroll
-  for (int c = 0; c < CM; ++c) A[c] = 0;
-  u64 fsum = 0;  // sum of y_i / q_i in units of 2^-31
-  for (int l = 0; l < limbs; ++l) {
-    const u64 q = s_q[l];
-    u64 r = in[(u64)l * N + sidx];
-    if (neg && r) r = q - r;
-    const u64 y = mul_shoup(r, s_hinv[l], s_hinv_s[l], q);
-    const u64 fx = s_invq[l];
-    fsum += __umulhi((uint32_t)((y << (uint32_t)(fx >> 32)) >> 32), (uint32_t)fx);
-    const uint32_t y0 = (uint32_t)y & ((1u << 25) - 1), y1 = (uint32_t)(y >> 25);
-    const uint32_t* qh = s_qh + l * C;
-    const uint32_t* qhs = s_qhs + l * C;
-#pragma unroll
-    for (int c = 0; c < CM; ++c)
-      if (c < C) A[c] += (u64)y0 * qh[c] + (u64)y1 * qhs[c];
-  }
-  const u64 k = (fsum + (1ull << 30)) >> 31;
-  uint32_t X[CM];
-  int64_t carry = 0;
-#pragma unroll
-  for (int c = 0; c < CM; ++c) {
-    if (c < C) {
-      const int64_t v = (int64_t)A[c] - (int64_t)(k * s_Q[c]) + carry;
-      X[c] = (uint32_t)v;
-      carry = v >> 32;
-    }
-  }
-  bool negv = carry < 0;
-  if (!negv) {  // X' > floor(Q/2): X' is the centred value plus Q
-    int res = 0;
-#pragma unroll
-    for (int c = CM - 1; c >= 0; --c) {
-      if (c < C && res == 0) {
-        if (X[c] > s_hQ[c]) res = 1;
-        else if (X[c] < s_hQ[c]) res = -1;
-      }
-    }
-    if (res > 0) {
-      u64 borrow = 0;
-#pragma unroll
-      for (int c = 0; c < CM; ++c) {
-        if (c < C) {
-          const u64 t = (u64)X[c] - s_Q[c] - borrow;
-          X[c] = (uint32_t)t;
-          borrow = (t >> 32) ? 1ull : 0ull;
-        }
-      }
-      negv = true;
-    }
-  }
-  const uint32_t ext = negv ? 0xFFFFFFFFu : 0u;
-  int32_t* out = digits + jt.first_digit(job) * N + x;
-  u64 dcarry = 0;
-  bool tie = false;
-  constexpr int DMAX = (32 * CM) / 30 + 2;
-#pragma unroll
-  for (int d = 0; d < DMAX; ++d) {
-    if (d < D) {
-      const int bit = 30 * d;
-      const int w = bit >> 5, sh = bit & 31;
-      const uint32_t lo = (w < CM && w < C) ? X[w < CM ? w : 0] : ext;
-      const uint32_t hi = (w + 1 < CM && w + 1 < C) ? X[w + 1 < CM ? w + 1 : 0] : ext;
-      const u64 chunk = ((((u64)hi << 32) | lo) >> sh) & ((1ull << 30) - 1);
-      const u64 v = chunk + dcarry;
-      int64_t dig;
-      if (v >= (1ull << 29)) {
-        dig = (int64_t)v - (1ll << 30);
-        dcarry = 1;
-      } else {
-        dig = (int64_t)v;
-        dcarry = 0;
-      }
-      if (TIES) tie |= dig == -(1ll << 29);
-      out[(size_t)d * N] = (int32_t)dig;
-    }
-  }
-  for (int d = DMAX; d < D; ++d) {  // digits past every word: sign extension
-    const u64 v = (u64)(ext & ((1u << 30) - 1)) + dcarry;
-    int64_t dig;
-    if (v >= (1ull << 29)) {
-      dig = (int64_t)v - (1ll << 30);
-      dcarry = 1;
-    } else {
-      dig = (int64_t)v;
-      dcarry = 0;
-    }
-    if (TIES) tie |= dig == -(1ll << 29);
-    out[(size_t)d * N] = (int32_t)dig;
-  }
-  if (TIES && tie) atomicOr(&tie_flags[job], 1);
-}
-
-inline size_t split_smem_bytes(int limbs, int C) { return (size_t)limbs * 4 * 8 + ((size_t)2 * limbs * C + 2 * C) * 4; }
-
 // lift_poly_to_context (keyswitching.rs:242-276) for polynomial blockIdx.y: the Q limbs are copied and limb
 // limbs + k is the centred CRT value mod p_k (convert_centered_residues_to_target, 365-379):
 // sum_w X[w] * (2^(64 w) mod p_k) minus 2^(64 W) mod p_k when X < 0.
@@ -1009,27 +867,6 @@ void decompose_dispatch(int W, dim3 g, int threads, size_t smem, cudaStream_t s,
   else launch_decompose<64>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
 }
 
-template <int CM, class JT>
-void launch_decompose_s(dim3 g, int threads, size_t smem, cudaStream_t s, const PrimeConst* pc, const JT& jt,
-                        int32_t* digits, uint64_t g_inv, int log_n, int* tie_flags) {
-  if (tie_flags) k_decompose_s<CM, true, JT><<<g, threads, smem, s>>>(pc, jt, digits, g_inv, log_n, tie_flags);
-  else k_decompose_s<CM, false, JT><<<g, threads, smem, s>>>(pc, jt, digits, g_inv, log_n, nullptr);
-}
-
-// the split form's column count is a template parameter (register-resident columns); false above 64
-template <class JT>
-bool decompose_split_dispatch(int C, dim3 g, int threads, size_t smem, cudaStream_t s, const PrimeConst* pc,
-                              const JT& jt, int32_t* digits, uint64_t g_inv, int log_n, int* tie_flags) {
-  if (C <= 16) launch_decompose_s<16>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
-  else if (C <= 24) launch_decompose_s<24>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
-  else if (C <= 32) launch_decompose_s<32>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
-  else if (C <= 40) launch_decompose_s<40>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
-  else if (C <= 48) launch_decompose_s<48>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
-  else if (C <= 64) launch_decompose_s<64>(g, threads, smem, s, pc, jt, digits, g_inv, log_n, tie_flags);
-  else return false;
-  return true;
-}
-
 void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int jobs, int limbs, int D,
                int32_t* digits, uint64_t g_inv, int log_n, cudaStream_t s, int* tie_flags) {
   if (jobs <= 0) return;
@@ -1038,24 +875,17 @@ void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int
   dim3 g((N + threads - 1) / threads, jobs);
   ProfScope p("decompose", s);
   const UniDecomp jt{dt, src, limbs, D};
-  if (dt.split && dt.split_ok &&
-      decompose_split_dispatch(dt.C, g, threads, split_smem_bytes(limbs, dt.C), s, pc, jt, digits, g_inv, log_n,
-                               tie_flags))
-    return;
   decompose_dispatch(dt.W, g, threads, crt_smem_bytes(limbs, dt.W), s, pc, jt, digits, g_inv, log_n, tie_flags);
 }
 
 void decompose_ml(const PrimeConst* pc, const DecompTab* d_dts, const MlTab& t, const MlPtrTab& src, int max_limbs,
-                  int max_W, int32_t* digits, int log_n, cudaStream_t s, int split, int max_C) {
+                  int max_W, int32_t* digits, int log_n, cudaStream_t s) {
   if (t.J <= 0) return;
   const int N = 1 << log_n;
   const int threads = N < 128 ? N : 128;
   dim3 g((N + threads - 1) / threads, t.J);
   ProfScope p("decompose", s);
   const MlDecomp jt{d_dts, t, src};
-  if (split && decompose_split_dispatch(max_C, g, threads, split_smem_bytes(max_limbs, max_C), s, pc, jt, digits, 0,
-                                        log_n, nullptr))
-    return;
   decompose_dispatch(max_W, g, threads, crt_smem_bytes(max_limbs, max_W), s, pc, jt, digits, 0, log_n, nullptr);
 }
 

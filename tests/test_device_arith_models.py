@@ -135,53 +135,3 @@ def test_lazy_inverse_pass_stays_below_2_64_and_matches_the_reduced_pass(bits):
                     ref[i], ref[i + t] = (rx + ry) % q, (rx - ry) * w % q
         assert all(v < (2 << M) * q for v in lazy)
         assert [v % q for v in lazy] == ref
-
-
-def _split_decomp_model(res, primes):
-    """k_decompose_s's arithmetic on one coefficient: y_i = c_i (Q/q_i)^-1 mod q_i split into 25-bit halves,
-    carry-free 64-bit columns of 32-bit words, k = floor(F + 1/2) from the fixed-point quotient, one carry
-    pass and at most one subtraction of Q.  Returns (centred value, every column stayed below 2^63)."""
-    import math
-    Q = math.prod(primes)
-    C = (Q.bit_length() + 25 + 31) // 32 + 1
-    words = lambda v: [(v >> (32 * c)) & 0xFFFFFFFF for c in range(C)]
-    A = [0] * C
-    fsum = 0
-    for c_i, q in zip(res, primes):
-        qh = Q // q
-        y = c_i * pow(qh % q, -1, q) % q
-        n, r = _fx(q)
-        fsum += _term(y, n, r)
-        y0, y1 = y & ((1 << 25) - 1), y >> 25
-        for c, (w, ws) in enumerate(zip(words(qh), words(qh << 25))):
-            A[c] += y0 * w + y1 * ws
-    ok = all(a < 1 << 63 for a in A)
-    k = (fsum + (1 << 30)) >> 31
-    X, carry = [], 0
-    for c in range(C):
-        v = A[c] - k * words(Q)[c] + carry
-        X.append(v & 0xFFFFFFFF)
-        carry = v >> 32
-    val = sum(x << (32 * c) for c, x in enumerate(X)) - (1 << (32 * C) if carry < 0 else 0)
-    if val >= 0 and val > Q // 2:
-        val -= Q
-    return val, ok
-
-
-def test_split_form_decomposition_centres_exactly():
-    """The split CRT sum at 24 limbs of 50-bit primes (the benchmark chain) and 31 limbs (the form's limit):
-    random coefficients and coefficients at and around 0, +-floor(Q/2) and Q-1 give exactly the centred value
-    in [-(Q-1)/2, (Q-1)/2], and no column passes 2^63."""
-    import math
-    rng = random.Random(31)
-    for count in (24, 31):
-        primes = _primes(50, count)
-        assert all(q < 1 << 50 for q in primes)
-        Q = math.prod(primes)
-        h = Q // 2
-        vals = [0, 1, Q - 1, h, h + 1, h - 1, Q - h, 2] + [rng.randrange(Q) for _ in range(300)]
-        for x in vals:
-            res = [x % q for q in primes]
-            got, ok = _split_decomp_model(res, primes)
-            want = x if x <= h else x - Q
-            assert ok and got == want, (count, x)

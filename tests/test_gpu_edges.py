@@ -269,39 +269,3 @@ def test_hoisted_rotations_past_one_launch(C, small):
     for i in (0, 31, 32, 33):
         for r, k in enumerate(keys):
             assert np.array_equal(got[i][r].numpy(), ctx.rotate(cts[i], k).numpy()), (i, r)
-
-
-def test_both_forms_of_the_decomposition_agree(C, pkg):
-    """The CRT sum of the decomposition in 64-bit words (decomp_form 0) and in split form (32-bit words times
-    25-bit halves, 1): identical results for products, hoisted rotations (the automorphism read and the
-    tie flags) and a mixed-level relinearize batch, at 24 limbs of 50-bit primes (40 digits)."""
-    params = pkg.params.hybrid_params(12, 24, 2, 50)
-    ctx = C.RnsCkksContext(params)
-    n, q = params.poly_degree, params.q_moduli()
-    rng = np.random.default_rng(2525)
-    key = ctx.upload_keyswitch_key(_random_key(rng, params, len(q), True)[0], len(q) - 1, 2)
-    low = ctx.upload_keyswitch_key(_random_key(rng, params, 9, True)[0], 8, 2)
-    rot = _rot_keys(C, ctx, params, rng, [ctx.galois_element_for_rotation(s) for s in (1, -5)])
-    cts = [C.RnsCiphertext(C.to_device(rand_ct(rng, q, n)), 40) for _ in range(4)]
-    quads = [C.RnsQuadraticCiphertext(C.to_device(rand_ct(rng, q[:lv], n, 3)), 80) for lv in (24, 9, 24)]
-
-    def run():
-        prod = [o.numpy() for o in ctx.mult_relinearized_batch(cts, cts[::-1], [key] * 4)]
-        hoisted = [[r.numpy() for r in row] for row in ctx.rotate_hoisted(cts[:2], rot)]
-        mixed = [o.numpy() for o in ctx.relinearize_rescale_batch(quads, [key, low, key])]
-        return prod, hoisted, mixed
-
-    form = ctypes.c_int32(-1)
-    C.call("rc_tune_get", ctx.handle, b"decomp_form", ctypes.byref(form))
-    assert form.value == 1
-    split = run()
-    try:
-        C.call("rc_tune_set", ctx.handle, b"decomp_form", 0)
-        words = run()
-    finally:
-        C.call("rc_tune_set", ctx.handle, b"decomp_form", 1)
-    for a, b in zip(split[0] + split[2], words[0] + words[2]):
-        assert np.array_equal(a, b)
-    for ra, rb in zip(split[1], words[1]):
-        for a, b in zip(ra, rb):
-            assert np.array_equal(a, b)
