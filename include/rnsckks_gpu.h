@@ -117,6 +117,16 @@ int rc_ksk_upload(rc_context* ctx, const uint64_t* host_key, uint32_t digits, in
  * (e.g. generated on the GPU); the source buffer is not modified. */
 int rc_ksk_upload_device(rc_context* ctx, const uint64_t* device_key, uint32_t digits, int32_t level,
                          uint32_t aux_count, uint64_t galois_element, rc_ksk** out);
+/* RNS-hybrid ("dnum") relinearization key at `level` (no reference counterpart: the reference's only gadget
+ * is balanced base-2^30 digits, keyswitching.rs:238-240).  The active chain is cut into dnum = ceil((level+1)
+ * / alpha) groups of alpha consecutive limbs (1 <= alpha <= aux count, at most 8; every prime below 2^60);
+ * key = [dnum][2][level + 1 + aux][N] coefficient-form residues over Q_level u P (host memory, or device memory
+ * with key_on_device != 0), group b's pair encrypting [i in group b] (P mod q_i) s^2 as (e - a s + that, a).
+ * Relinearization and mult_relinearized with such a key extend each group of c2 to Q u P by a fast basis
+ * conversion, multiply by the key in the NTT domain and ModDown by P: the results decrypt to the same values
+ * as with the reference's gadget but are not its residues.  Relinearization only; not serialisable. */
+int rc_ksk_upload_dnum(rc_context* ctx, const uint64_t* key, int32_t key_on_device, uint32_t alpha, int32_t level,
+                       rc_ksk** out);
 /* RnsKeySwitchingKey::truncate_levels (Q-only keys): keyswitching.rs:32-41 */
 int rc_ksk_truncate(rc_context* ctx, const rc_ksk* key, int32_t level, rc_ksk** out);
 int rc_ksk_info(const rc_ksk* key, uint32_t* digits, int32_t* level, uint32_t* aux_count, uint64_t* galois_element);

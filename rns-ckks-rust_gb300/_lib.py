@@ -63,6 +63,7 @@ SIGNATURES = [
     ("rc_tune_get", ctypes.c_int, [_vp, ctypes.c_char_p, ctypes.POINTER(_i32)]),
     ("rc_ksk_upload", ctypes.c_int, [_vp, _vp, _u32, _i32, _u32, _u64, ctypes.POINTER(_vp)]),
     ("rc_ksk_upload_device", ctypes.c_int, [_vp, _vp, _u32, _i32, _u32, _u64, ctypes.POINTER(_vp)]),
+    ("rc_ksk_upload_dnum", ctypes.c_int, [_vp, _vp, _i32, _u32, _i32, ctypes.POINTER(_vp)]),
     ("rc_ksk_truncate", ctypes.c_int, [_vp, _vp, _i32, ctypes.POINTER(_vp)]),
     ("rc_ksk_info", ctypes.c_int, [_vp, ctypes.POINTER(_u32), ctypes.POINTER(_i32), ctypes.POINTER(_u32),
                                    ctypes.POINTER(_u64)]),

@@ -625,6 +625,43 @@ class RnsCkksContext:
             return self._keyswitch_key_hybrid(src, sk, level, 0, sampler, samples, return_coeff)
         return self._keyswitch_key_q(src, pk, level, 0, sampler, samples, return_coeff)
 
+    def generate_relinearization_key_dnum(self, sk: RnsSecretKey, alpha: int, level: Optional[int] = None,
+                                          sampler: Optional[Sampler] = None, return_coeff: bool = False):
+        """An RNS-hybrid ("dnum") relinearization key (no counterpart in the reference, whose gadget is balanced
+        base-2^30 digits): the level's chain cut into groups of `alpha` limbs (alpha <= the aux prime count),
+        group b's pair (e_b - a_b s + g_b s^2, a_b) over Q_level u P with g_b = P mod q_i on the group's limbs
+        and 0 elsewhere.  Relinearizing with it decrypts to the same values as with the reference's gadget,
+        not to the same residues."""
+        if not self.has_aux_basis():
+            raise RcError(1, "RNS-hybrid keys need an auxiliary basis")
+        level = self.levels() - 1 if level is None else level
+        qm = self.level_moduli(level)
+        allm = qm + self.p_moduli
+        n = self.params.poly_degree
+        dnum = -(-len(qm) // alpha)
+        P = math.prod(self.p_moduli)
+        sampler = sampler or Sampler(level + 4000)
+        s_all = self._secret_over(sk, allm)
+        s2 = self._poly_mul(s_all, s_all, with_aux=True)
+        key = torch.empty((dnum, 2, len(allm), n), dtype=torch.int64, device="cuda")
+        for b in range(dnum):
+            lo, hi = b * alpha, min((b + 1) * alpha, len(qm))
+            gs2 = self._poly_scalar(s2, [P % m if lo <= i < hi else 0 for i, m in enumerate(qm)]
+                                    + [0] * len(self.p_moduli), with_aux=True)
+            if isinstance(sampler, DeviceSampler):
+                a = sampler.uniform_residues(len(allm), True)
+                e = sampler.error_residues(len(allm), True)
+            else:
+                a = to_device(sampler.uniform(allm, n))
+                e = to_device(signed_to_residues(sampler.gaussian(n), allm))
+            key[b, 0] = self._poly_add(self._poly_sub(e, self._poly_mul(a, s_all, True), True), gs2, True)
+            key[b, 1] = a
+        torch.cuda.synchronize()
+        handle = ctypes.c_void_p()
+        call("rc_ksk_upload_dnum", self.handle, _ptr(key), 1, alpha, level, ctypes.byref(handle))
+        k = RnsKeySwitchingKey(self, handle)
+        return (k, key) if return_coeff else k
+
     def galois_element_for_rotation(self, steps: int) -> int:
         return galois_element_for_rotation(self.params.poly_degree, steps)
 

@@ -150,10 +150,19 @@ struct KsJob {
   uint64_t* out1;
 };
 
+// batches group their jobs by (level, key kind, digits); the kind separates Q-only, gadget hybrid and
+// RNS-hybrid keys
+int key_kind(const rc_ksk* k) { return (int)(k->aux | (k->alpha << 16)); }
+
 void check_key_for(const rc_context* c, const rc_ksk* key, int qlimbs) {
   require(key != nullptr, "keyswitch key must not be null");
   require(key->ctx == c, "keyswitch key belongs to another context");
   const LevelInfo& li = level_info(c, qlimbs);
+  if (key->alpha) {  // RNS-hybrid key: one per level, over the active chain and P
+    require(key->level == qlimbs - 1, "keyswitch key level must match the active Q chain");
+    require((int)key->aux == c->K, "eval-key context must match the keyswitch key auxiliary basis");
+    return;
+  }
   if (key->aux == 0) {
     // keyswitch_rns, keyswitching.rs:135-137
     require(key->level == qlimbs - 1, "keyswitch key level must match the active modulus chain");
@@ -171,6 +180,7 @@ int ks_digits(const rc_context* c, const rc_ksk* k0, int qlimbs) {
   // Q-only: the reference decomposes into ksk.ksk.len() digits (keyswitching.rs:138);
   // hybrid: into the active digit count (167-170)
   const LevelInfo& li = level_info(c, qlimbs);
+  if (k0 && k0->alpha) return (int)k0->digits;  // RNS-hybrid: the key's groups
   return (k0 && k0->aux) ? li.digits : (k0 ? std::max((int)k0->digits, 1) : li.digits);
 }
 
@@ -189,6 +199,19 @@ size_t ks_ws_bytes(const rc_context* c, int J, int qlimbs, int K, int D) {
   const size_t wide = align_up((size_t)J * D * c->N * 4, 256) + 2 * arena_size_u64((size_t)J * D * 2 * c->N) +
                       arena_size_u64((size_t)J * 2 * total * 2 * c->N) + 1024;
   return std::max(standard, c->wide_ok ? wide : 0);
+}
+
+// scratch of the RNS-hybrid key switch: ModUp outputs [J][dnum][total][N] and products [J][2][total][N]
+size_t dnum_ws_bytes(const rc_context* c, int J, int qlimbs, int dnum) {
+  const size_t total = (size_t)qlimbs + c->K;
+  return arena_size_u64((size_t)J * dnum * total * c->N) + arena_size_u64((size_t)J * 2 * total * c->N) + 1024;
+}
+
+// scratch of a key switch of J jobs at qlimbs with keys like k0
+size_t ks_bytes_for(const rc_context* c, int J, int qlimbs, const rc_ksk* k0) {
+  if (k0 && k0->alpha) return dnum_ws_bytes(c, J, qlimbs, (int)k0->digits);
+  const int K = k0 && k0->aux ? c->K : 0;
+  return ks_ws_bytes(c, J, qlimbs, K, ks_digits(c, k0, qlimbs));
 }
 
 // The exact integer key product applies when the internal primes' product A
@@ -431,6 +454,75 @@ bool keyswitch_mixed_batch(rc_context* c, const rc_ciphertext* qct, const rc_ksk
   return true;
 }
 
+// The RNS-hybrid key switch of `jobs` (keys from rc_ksk_upload_dnum at this level): ModUp of each job's
+// polynomial group by group, forward transforms over Q_l u P, the key product, inverse transforms, and the
+// exact ModDown with addends and optional rescale of k_finalize.  Relinearization only (no automorphism).
+void keyswitch_dnum(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, uint64_t g_inv, bool rescale,
+                    void* ws, cudaStream_t s) {
+  require(g_inv <= 1, "RNS-hybrid keys serve relinearization only");
+  const int J = (int)jobs.size();
+  const rc_ksk* k0 = jobs[0].key;
+  const int dnum = (int)k0->digits, alpha = (int)k0->alpha, K = c->K, total = qlimbs + K;
+  for (auto& j : jobs) require((int)j.key->digits == dnum, "internal: mixed key shapes in one keyswitch batch");
+  const size_t N = c->N, per = (size_t)total * N;
+  const LimbMap map{qlimbs, c->L};
+  Arena ar(ws);
+  uint64_t* D = ar.take<uint64_t>((size_t)J * dnum * per);
+  uint64_t* acc = ar.take<uint64_t>((size_t)J * 2 * per);
+  int b = 0;
+  while (b < J) {  // runs of jobs sharing a key
+    int e = b + 1;
+    while (e < J && jobs[e].key == jobs[b].key) ++e;
+    PtrTab src{};
+    for (int j = b; j < e; ++j) src.p[j - b] = const_cast<uint64_t*>(jobs[j].poly);
+    dnum_modup(c->d_pc, src, e - b, (const uint64_t*)jobs[b].key->mbuf->p, D + (size_t)b * dnum * per, qlimbs, total,
+               alpha, dnum, map, c->log_n, s);
+    launch_check("dnum modup");
+    const int polys = (e - b) * dnum;
+    for (int p0 = 0; p0 < polys; p0 += MAXP) {
+      PtrTab t{};
+      const int cnt = std::min(MAXP, polys - p0);
+      for (int k = 0; k < cnt; ++k) t.p[k] = D + ((size_t)b * dnum + p0 + k) * per;
+      ntt_forward(c->ntt(), t, t, cnt, total, map, s);
+      launch_check("dnum ntt");
+    }
+    dnum_mac(c->d_pc, D + (size_t)b * dnum * per, jobs[b].key->data, acc + (size_t)b * 2 * per, e - b, total, dnum,
+             map, c->log_n, s);
+    launch_check("dnum mac");
+    b = e;
+  }
+  for (int p0 = 0; p0 < 2 * J; p0 += MAXP) {
+    PtrTab t{};
+    const int cnt = std::min(MAXP, 2 * J - p0);
+    for (int k = 0; k < cnt; ++k) t.p[k] = acc + (size_t)(p0 + k) * per;
+    ntt_inverse(c->ntt(), t, t, cnt, total, map, s);
+    launch_check("dnum inverse ntt");
+  }
+  FinalizeArgs f;
+  f.pc = c->d_pc;
+  f.md = c->md;
+  f.rt = c->rt;
+  f.L = c->L;
+  f.n = c->N;
+  f.log_n = c->log_n;
+  f.qlimbs = qlimbs;
+  f.K = K;
+  f.rescale = rescale ? 1 : 0;
+  f.add_g_inv = 0;
+  f.wide = 0;
+  f.wt = c->wide;
+  f.lazy = 0;
+  PtrTab add{}, out{};
+  for (int j = 0; j < J; ++j) {
+    add.p[2 * j] = const_cast<uint64_t*>(jobs[j].add0);
+    add.p[2 * j + 1] = const_cast<uint64_t*>(jobs[j].add1);
+    out.p[2 * j] = jobs[j].out0;
+    out.p[2 * j + 1] = jobs[j].out1;
+  }
+  finalize(f, acc, add, out, J, s);
+  launch_check("finalize");
+}
+
 // Runs keyswitch for `jobs` jobs at `qlimbs` limbs (all keys of the same kind);
 // the result is finalized with addends, optional automorphism on the addend and
 // optional rescale.  g_inv: automorphism applied to the keyswitched polynomial
@@ -442,6 +534,11 @@ void keyswitch_core(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, u
   require(J <= MAXP / 2, "internal: keyswitch chunk too large");
   const rc_ksk* k0 = jobs[0].key;
   for (auto& j : jobs) check_key_for(c, j.key, qlimbs);
+  for (auto& j : jobs) require(j.key->alpha == k0->alpha, "internal: mixed key kinds in one keyswitch batch");
+  if (k0->alpha) {
+    keyswitch_dnum(c, jobs, qlimbs, g_inv, rescale, ws, s);
+    return;
+  }
   const int K = k0->aux ? c->K : 0;
   const LevelInfo& li = level_info(c, qlimbs);
   const int D = ks_digits(c, k0, qlimbs);
@@ -524,7 +621,8 @@ void keyswitch_run(rc_context* c, const std::vector<KsJob>& jobs, int qlimbs, ui
   const rc_ksk* k0 = jobs[0].key;
   check_key_for(c, k0, qlimbs);
   const int K = k0->aux ? c->K : 0;
-  void* ws = ws_device(c, s, ks_ws_bytes(c, (int)jobs.size(), qlimbs, K, ks_digits(c, k0, qlimbs)));
+  (void)K;
+  void* ws = ws_device(c, s, ks_bytes_for(c, (int)jobs.size(), qlimbs, k0));
   keyswitch_core(c, jobs, qlimbs, g_inv, rescale, ws, s);
 }
 
@@ -588,9 +686,8 @@ uint64_t galois_inverse(const rc_context* c, uint64_t g) {
 // mult_relinearized on J jobs: the tensor runs in chunks of MAXP/4 jobs (four pointer-table entries each),
 // the keyswitch on all J <= MAXP/2 jobs at once so that one key read serves them all
 size_t mult_relin_ws_bytes(const rc_context* c, int J, int limbs, const rc_ksk* k0) {
-  const int K = k0 && k0->aux ? c->K : 0;
   const size_t pl = (size_t)limbs * c->N;
-  return align_up(std::max(ks_ws_bytes(c, J, limbs, K, ks_digits(c, k0, limbs)),
+  return align_up(std::max(ks_bytes_for(c, J, limbs, k0),
                            tensor_ws_bytes(c, std::min(J, MAXP / 4), limbs)),
                   256) +
          arena_size_u64((size_t)3 * J * pl) + 256;
@@ -613,8 +710,7 @@ void mult_relin_group(rc_context* c, const std::vector<int>& idx, const rc_ciphe
       check_key_for(c, keys[idx[b + j]], limbs);
     }
     const rc_ksk* k0 = keys[idx[b]];
-    const int K = k0->aux ? c->K : 0;
-    const size_t head = align_up(std::max(ks_ws_bytes(c, J, limbs, K, ks_digits(c, k0, limbs)),
+    const size_t head = align_up(std::max(ks_bytes_for(c, J, limbs, k0),
                                           tensor_ws_bytes(c, std::min(J, MAXP / 4), limbs)),
                                  256);
     char* ws = (char*)ws_device(c, s, mult_relin_ws_bytes(c, J, limbs, k0));
@@ -1232,6 +1328,66 @@ extern "C" int rc_ksk_upload_device(rc_context* c, const uint64_t* dev_key, uint
   return ksk_upload_impl(c, dev_key, true, digits, level, aux_count, galois_element, out);
 }
 
+// RNS-hybrid ("dnum") relinearization key: no counterpart in the reference (its gadget is base 2^30 digits).
+extern "C" int rc_ksk_upload_dnum(rc_context* c, const uint64_t* key, int32_t key_on_device, uint32_t alpha,
+                                  int32_t level, rc_ksk** out) {
+  return guarded("rc_ksk_upload_dnum", [&] {
+    require(c && key && out, "arguments must not be null");
+    *out = nullptr;
+    require(c->K > 0, "RNS-hybrid keys need an auxiliary basis");
+    require(level >= 0 && level < c->L, "keyswitch key level out of range for this context");
+    require(alpha >= 1 && (int)alpha <= std::min(c->K, 8),
+            "alpha must be between 1 and the number of aux primes (at most 8)");
+    for (uint64_t m : c->mod) require(m < (1ull << 60), "RNS-hybrid keys need every prime below 2^60");
+    const int qlimbs = level + 1, K = c->K, total = qlimbs + K;
+    const int dnum = (qlimbs + (int)alpha - 1) / (int)alpha;
+    require(dnum <= 16, "RNS-hybrid keys take at most 16 groups");
+    const size_t N = c->N, per = (size_t)total * N;
+    std::shared_ptr<DevBuf> kb(new DevBuf((size_t)dnum * 2 * per * 8));
+    uint64_t* kd = (uint64_t*)kb->p;
+    cuda_check(cudaMemcpy(kd, key, (size_t)dnum * 2 * per * 8,
+                          key_on_device ? cudaMemcpyDeviceToDevice : cudaMemcpyHostToDevice),
+               "key upload");
+    const LimbMap map{qlimbs, c->L};
+    for (int p0 = 0; p0 < 2 * dnum; p0 += MAXP) {
+      PtrTab t{};
+      const int cnt = std::min(MAXP, 2 * dnum - p0);
+      for (int k = 0; k < cnt; ++k) t.p[k] = kd + (size_t)(p0 + k) * per;
+      ntt_forward(c->ntt(), t, t, cnt, total, map, 0);
+      launch_check("key ntt");
+    }
+    // ModUp tables per group b: (Q_b/q_i)^-1 mod q_i (+ Shoup), then (Q_b/q_i) mod every target prime
+    const int row = 2 + total;
+    std::vector<uint64_t> tab((size_t)dnum * alpha * row, 0);
+    for (int b = 0; b < dnum; ++b) {
+      const int i0 = b * (int)alpha, i1 = std::min(i0 + (int)alpha, qlimbs);
+      const BigU Qb = product(c->mod, (size_t)i0, (size_t)i1);
+      for (int i = i0; i < i1; ++i) {
+        const uint64_t q = c->mod[i];
+        const BigU hat = Qb.div_u64(q);
+        uint64_t* r = tab.data() + ((size_t)b * alpha + (i - i0)) * row;
+        r[0] = invmod_h(hat.mod_u64(q), q);
+        r[1] = shoup_h(r[0], q);
+        for (int t = 0; t < total; ++t) r[2 + t] = hat.mod_u64(c->mod[map.prime(t)]);
+      }
+    }
+    std::shared_ptr<DevBuf> mb(new DevBuf(tab.size() * 8));
+    cuda_check(cudaMemcpy(mb->p, tab.data(), tab.size() * 8, cudaMemcpyHostToDevice), "key tables");
+    cuda_check(cudaDeviceSynchronize(), "key upload");
+    rc_ksk* k = new rc_ksk();
+    k->ctx = c;
+    k->buf = kb;
+    k->data = kd;
+    k->digits = (uint32_t)dnum;
+    k->level = level;
+    k->aux = (uint32_t)K;
+    k->galois = 0;
+    k->alpha = alpha;
+    k->mbuf = mb;
+    *out = k;
+  });
+}
+
 extern "C" int rc_ksk_truncate(rc_context* c, const rc_ksk* key, int32_t level, rc_ksk** out) {
   return guarded("rc_ksk_truncate", [&] {
     require(c && key && out, "arguments must not be null");
@@ -1740,7 +1896,7 @@ extern "C" int rc_mult_relinearized_batch(rc_context* c, uint32_t count, const r
       require(out[i].data != nullptr, "output must not be null");
       const rc_ksk* k = keys[i];
       require(k != nullptr, "keyswitch key must not be null");
-      groups[{lhs[i].level, {(int)k->aux, (int)k->digits}}].push_back((int)i);
+      groups[{lhs[i].level, {key_kind(k), (int)k->digits}}].push_back((int)i);
     }
     for (auto& g : groups) mult_relin_group(c, g.second, lhs, rhs, keys, out, S(stream));
   });
@@ -1755,7 +1911,7 @@ extern "C" int rc_relinearize_batch(rc_context* c, uint32_t count, const rc_ciph
       check_ct(c, &qct[i], "quadratic ciphertext");
       require(keys[i] != nullptr, "keyswitch key must not be null");
       check_key_for(c, keys[i], qct[i].level + 1);
-      groups[{qct[i].level, {(int)keys[i]->aux, (int)keys[i]->digits}}].push_back((int)i);
+      groups[{qct[i].level, {key_kind(keys[i]), (int)keys[i]->digits}}].push_back((int)i);
     }
     if (keyswitch_mixed_batch(c, qct, keys, out, count, false, S(stream))) {
       for (uint32_t i = 0; i < count; ++i) {
@@ -1794,7 +1950,7 @@ extern "C" int rc_relinearize_rescale_batch(rc_context* c, uint32_t count, const
       require(qct[i].level >= 1, "rescale requires at least two levels");
       require(keys[i] != nullptr, "keyswitch key must not be null");
       check_key_for(c, keys[i], qct[i].level + 1);
-      groups[{qct[i].level, {(int)keys[i]->aux, (int)keys[i]->digits}}].push_back((int)i);
+      groups[{qct[i].level, {key_kind(keys[i]), (int)keys[i]->digits}}].push_back((int)i);
     }
     if (keyswitch_mixed_batch(c, qct, keys, out, count, true, S(stream))) {
       for (uint32_t i = 0; i < count; ++i) {

@@ -176,6 +176,10 @@ struct rc_ksk {
   int32_t level = 0;
   uint32_t aux = 0;
   uint64_t galois = 0;
+  // RNS-hybrid key (rc_ksk_upload_dnum): alpha limbs per group, digits = dnum groups; `data` then holds the
+  // key [dnum][2][level + 1 + aux][N] in the NTT domain and mbuf the ModUp tables (0 for gadget keys)
+  uint32_t alpha = 0;
+  std::shared_ptr<rc::DevBuf> mbuf;
   uint32_t limbs() const { return (uint32_t)level + 1 + aux; }
 };
 

@@ -267,6 +267,16 @@ bool wide_digit_transforms_ml(const WidePrimes& w, const MlTab& t, const int32_t
 void wide_mac_ml(const WidePrimes& w, const MlTab& t, const MlKeys& keys, const uint2* dtt, uint2* acc, int bc_max,
                  cudaStream_t s);
 
+// ---- RNS-hybrid ("dnum") key switching (dnum.cu) ----
+// ModUp of each job's coefficient-form polynomial src.p[job] ([qlimbs][N]) group by group:
+// D[job][b][limb][N] over the qlimbs Q limbs and the aux limbs (total), tab = [dnum][alpha][2 + total]
+// ((Q_b/q_i)^-1 mod q_i, its Shoup companion, then (Q_b/q_i) mod every target prime); alpha <= 8
+void dnum_modup(const PrimeConst* pc, const PtrTab& src, int jobs, const u64* tab, u64* D, int qlimbs, int total,
+                int alpha, int dnum, LimbMap map, int log_n, cudaStream_t s);
+// acc[job][c][limb][N] = sum_b D[job][b] * key[b][c] (NTT domain; key [dnum][2][total][N]; dnum <= 16)
+void dnum_mac(const PrimeConst* pc, const u64* D, const u64* key, u64* acc, int jobs, int total, int dnum,
+              LimbMap map, int log_n, cudaStream_t s);
+
 // ---- wide-CRT key product (wide.cu) ----
 // digits [job][digit][N] -> transforms under w0..w3, written tiled:
 // dtt[job][pair][x/32][digit][32].  `work` holds jobs*D*2*N uint2.  False if N

@@ -85,6 +85,7 @@ size_t ksk_payload_bytes(const rc_ksk* k) {
 
 extern "C" int rc_ksk_serialized_size(const rc_ksk* k, uint64_t* bytes) {
   return guarded("rc_ksk_serialized_size", [&] {
+    require(!k || !k->alpha, "RNS-hybrid keys are not serialisable");
     require(k && bytes, "arguments must not be null");
     *bytes = sizeof(KskHeader) + ksk_payload_bytes(k);
   });
@@ -92,6 +93,7 @@ extern "C" int rc_ksk_serialized_size(const rc_ksk* k, uint64_t* bytes) {
 
 extern "C" int rc_ksk_serialize(rc_context* c, const rc_ksk* k, void* host_buf, uint64_t buf_bytes, void* stream) {
   return guarded("rc_ksk_serialize", [&] {
+    require(!k || !k->alpha, "RNS-hybrid keys are not serialisable");
     require(c && k && host_buf, "arguments must not be null");
     require(k->ctx == c, "keyswitch key belongs to another context");
     const size_t payload = ksk_payload_bytes(k);
