@@ -482,6 +482,7 @@ def run_gpu(args):
         result["key_serialization"] = key_serialization_bench(C, ctx, W["kp"], key)
         result["encode_decode"] = encode_decode_bench(ctx, args.seed)
         result["decoded_error_per_op"] = decoded_error_per_op(C, ctx, W, args.seed)
+        result["dnum_relin"] = dnum_relin_bench(pkg, C, args.seed)
         result["serving"] = serving_bench(pkg, C, args.seed)
     if rank == 0:
         print(json.dumps(result), flush=True)
@@ -859,6 +860,59 @@ def key_serialization_bench(C, ctx, kp, key):
             "reloaded_level": back.level}
 
 
+def dnum_relin_bench(pkg, C, seed, batch=32, reps=5):
+    """Config C's "dnum=3" as the optional RNS-hybrid key switch (not the reference's gadget, so not its
+    residues; reported separately and checked by decryption): N=2^16, 24 limbs of 50-bit primes and 8 aux
+    primes, the chain cut into 3 groups of 8 limbs, against the reference's 40-digit gadget on the same
+    context.  HMult+relin/s batched (32 pairs) and per op, and the decoded error of pair 0 against FP64."""
+    import torch
+    params = pkg.params.hybrid_params(16, 24, 8, 50)
+    ctx = C.RnsCkksContext(params)
+    n = params.poly_degree
+    ds = C.DeviceSampler(ctx, seed + 30)
+    kp = ctx.keygen(64, ds)
+    rng = np.random.default_rng(seed + 31)
+    xs = [rng.uniform(-1, 1, n // 2) for _ in range(2 * batch)]
+    cts = [ctx.encrypt(ctx.encode_real(x), kp.public_key, ds) for x in xs]
+    lhs, rhs = cts[:batch], cts[batch:]
+    t0 = time.perf_counter()
+    dkey = ctx.generate_relinearization_key_dnum(kp.secret_key, 8, sampler=ds)
+    torch.cuda.synchronize()
+    dkey_s = time.perf_counter() - t0
+    gkey = ctx.generate_relinearization_key(kp.secret_key, kp.public_key, ds)
+    st = torch.cuda.current_stream()
+    res = {"workload": "mult_relinearized, N=2^16, 24 x 50-bit limbs, 8 aux primes, batch 32",
+           "groups": dkey.digits, "alpha": 8, "key_bytes_dnum": dkey.digits * 2 * 32 * n * 8,
+           "key_generation_s": round(dkey_s, 3)}
+    for name, key in (("dnum3", dkey), ("gadget40", gkey)):
+        ctx.reserve(23, batch)
+        outs = ctx.mult_relinearized_batch(lhs, rhs, [key] * batch)  # warm
+        torch.cuda.synchronize()
+        e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+        e0.record(st)
+        for _ in range(reps):
+            outs = ctx.mult_relinearized_batch(lhs, rhs, [key] * batch)
+        e1.record(st)
+        torch.cuda.synchronize()
+        ms = e0.elapsed_time(e1) / reps
+        ctx.mult_relinearized(lhs[0], rhs[0], key)
+        torch.cuda.synchronize()
+        e0.record(st)
+        for i in range(8):
+            ctx.mult_relinearized(lhs[i], rhs[i], key)
+        e1.record(st)
+        torch.cuda.synchronize()
+        per_op_ms = e0.elapsed_time(e1) / 8
+        dec = ctx.decode_real_at_scale(ctx.decrypt(outs[0], kp.secret_key), outs[0].scale_bits)
+        res[name] = {"batched_per_s": round(batch / (ms / 1e3), 1), "ms_per_batch": round(ms, 3),
+                     "per_op_per_s": round(1e3 / per_op_ms, 1), "per_op_ms": round(per_op_ms, 4),
+                     "batched_vs_per_op": round(per_op_ms * batch / ms, 3),
+                     "decoded_max_abs_err": float(np.max(np.abs(dec - xs[0] * xs[batch])))}
+    del dkey, gkey, cts, lhs, rhs, outs
+    torch.cuda.synchronize()
+    return res
+
+
 def decoded_error_per_op(C, ctx, W, seed):
     """Decoded slot error of each operation against the FP64 computation on the slots, at the bench shape
     (N=2^16, 24 limbs, scale 2^50): max |decoded - expected| over all 2^15 slots."""
@@ -1069,7 +1123,7 @@ def main():
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the NTT microbenchmark and the mixed-level relinearization batch")
     ap.add_argument("--extra-only", choices=["bsgs_matvec", "bootstrap", "mixed_level_relin", "ntt_microbench",
-                                             "hmult_profile"],
+                                             "hmult_profile", "dnum_relin"],
                     help="run one of the extra workloads alone (a profiling case) and print its JSON object")
     ap.add_argument("--extra-batch", type=int, default=None, help="batch of --extra-only (default: its own)")
     args = ap.parse_args()
@@ -1086,7 +1140,7 @@ def main():
                     return f(C, ctx, params, seed, **kw)
                 return f(C, ctx, params, peaks()[0], seed)
             return run
-        fn = {"bsgs_matvec": bsgs_matvec_bench, "bootstrap": bootstrap_bench,
+        fn = {"bsgs_matvec": bsgs_matvec_bench, "bootstrap": bootstrap_bench, "dnum_relin": dnum_relin_bench,
               "mixed_level_relin": on_bench_context(mixed_level_relin),
               "ntt_microbench": on_bench_context(ntt_microbench),
               "hmult_profile": on_bench_context(hmult_profile)}[args.extra_only]
