@@ -884,8 +884,12 @@ def dnum_relin_bench(pkg, C, seed, batch=32, reps=5):
     res = {"workload": "mult_relinearized, N=2^16, 24 x 50-bit limbs, 8 aux primes, batch 32",
            "groups": dkey.digits, "alpha": 8, "key_bytes_dnum": dkey.digits * 2 * 32 * n * 8,
            "key_generation_s": round(dkey_s, 3)}
+    from rnsckks_gb300 import autotune as T
+    touts = [torch.empty((2, 23, n), dtype=torch.int64, device="cuda") for _ in range(batch)]
     for name, key in (("dnum3", dkey), ("gadget40", gkey)):
         ctx.reserve(23, batch)
+        # launch and kernel shapes tuned for this key kind on this batch (not cached: both kinds share a shape)
+        tuned = T.tune_mult_relinearized(ctx, lhs, rhs, [key] * batch, touts, reps=2, use_cache=False)
         outs = ctx.mult_relinearized_batch(lhs, rhs, [key] * batch)  # warm
         torch.cuda.synchronize()
         e0, e1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
@@ -907,8 +911,9 @@ def dnum_relin_bench(pkg, C, seed, batch=32, reps=5):
         res[name] = {"batched_per_s": round(batch / (ms / 1e3), 1), "ms_per_batch": round(ms, 3),
                      "per_op_per_s": round(1e3 / per_op_ms, 1), "per_op_ms": round(per_op_ms, 4),
                      "batched_vs_per_op": round(per_op_ms * batch / ms, 3),
-                     "decoded_max_abs_err": float(np.max(np.abs(dec - xs[0] * xs[batch])))}
-    del dkey, gkey, cts, lhs, rhs, outs
+                     "decoded_max_abs_err": float(np.max(np.abs(dec - xs[0] * xs[batch]))),
+                     "tuned": tuned["choice"]}
+    del dkey, gkey, cts, lhs, rhs, outs, touts
     torch.cuda.synchronize()
     return res
 
