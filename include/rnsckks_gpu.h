@@ -99,8 +99,12 @@ int rc_reserve(rc_context* ctx, int32_t max_level, uint32_t max_batch, void* str
  * whose jobs are at different levels: one launch per pass over all levels instead of one per level, default
  * 1), "ml_jobs" (jobs per such launch, 1..128, default 128), "mac_wait_polls" (polls of
  * the key product's first wait for its staged digit transforms, 0..2^22, default 2^22; 0 makes every CTA
- * time out and raise the rc_kernel_errors flag, for testing that path).  Set them between calls, not while
- * calls on the context are in flight. */
+ * time out and raise the rc_kernel_errors flag, for testing that path), "mac_persistent" (key products of
+ * more than two jobs per CTA in one persistent CTA per SM taking (tile, limb) units, the next tile's digit
+ * transforms copied while the current one is used; default 1), "ntt_split" (log size of the four-step
+ * column phase, both phases 2^6..2^8 points), "col_ctas" (CTAs per SM of the column pass: 2 or 3),
+ * "row_polys" (polynomials per row block: 8 or 16).  Set them between calls, not while calls on the context
+ * are in flight. */
 int rc_tune_set(rc_context* ctx, const char* name, int32_t value);
 int rc_tune_get(const rc_context* ctx, const char* name, int32_t* value);
 

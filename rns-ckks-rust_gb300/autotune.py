@@ -24,8 +24,9 @@ DEVICE_CANDIDATES: Dict[str, Sequence[int]] = {"ks_jobs": (8, 16, 32, 64), "mac_
 # kernel shapes of the 64-bit transforms, tuned after the launch-shape tunables above (with their choice
 # applied): CTAs per SM the column pass is compiled for (2 leaves it more registers), polynomials per row
 # block (one twiddle staging each), and the four-step split (the column phase's log size; both phases must
-# have 2^6..2^8 points, so at N = 2^16 only 8 x 8 exists)
-SHAPE_CANDIDATES: Dict[str, Sequence[int]] = {"col_ctas": (2, 3), "row_polys": (8, 16)}
+# have 2^6..2^8 points, so at N = 2^16 only 8 x 8 exists); and the key product's form for job groups (one CTA
+# per tile, or persistent CTAs taking (tile, limb) units with double-buffered digit tiles)
+SHAPE_CANDIDATES: Dict[str, Sequence[int]] = {"col_ctas": (2, 3), "row_polys": (8, 16), "mac_persistent": (0, 1)}
 
 
 def split_candidates(log_n: int) -> List[int]:

@@ -1200,6 +1200,8 @@ extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
     } else if (n == "mac_wait_polls") {
       require(value >= 0 && value <= (1 << 22), "mac_wait_polls must be in 0..4194304");
       c->wp.first_wait_polls = (uint32_t)value;
+    } else if (n == "mac_persistent") {
+      c->wp.persistent = value != 0;
     } else if (n == "lazy_ntt") {
       bool ok = true;
       for (uint64_t q : c->mod) ok = ok && q < (1ull << 58);
@@ -1223,6 +1225,7 @@ extern "C" int rc_tune_get(const rc_context* c, const char* name, int32_t* value
     else if (n == "fuse_tensor") *value = c->fuse_tensor ? 1 : 0;
     else if (n == "host_phased") *value = c->host_phased;
     else if (n == "mac_wait_polls") *value = (int32_t)c->wp.first_wait_polls;
+    else if (n == "mac_persistent") *value = c->wp.persistent ? 1 : 0;
     else if (n == "mixed_levels") *value = c->mixed_levels ? 1 : 0;
     else if (n == "ntt_split") *value = c->n1;
     else if (n == "col_ctas") *value = c->col_ctas;

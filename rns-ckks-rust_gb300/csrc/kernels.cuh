@@ -183,6 +183,8 @@ struct WidePrimes {
   // polls of the key product's first wait for its staged digit transforms (tunable "mac_wait_polls"; a
   // limit of 0 makes every CTA time out, which tests the error path without a fault)
   uint32_t first_wait_polls = 1u << 22;
+  // uniform batches of more than two jobs per CTA take the persistent key product (tunable "mac_persistent")
+  int persistent = 1;
 };
 // Garner CRT of (S mod w0..w3) to the centred integer S (|S| < A/4), reduced mod
 // each scheme prime t.

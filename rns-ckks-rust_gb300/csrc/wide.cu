@@ -354,6 +354,78 @@ __device__ __forceinline__ uint32_t galois_source(uint32_t x, uint32_t g, int lo
   return __brev(kk) >> (32 - log_n);
 }
 
+// One limb j of the key product for up to BC jobs whose digit transforms sit in shared memory at dsm
+// ([BC][D][32], job b at b * run): the warp streams limb j's key words of tile xb under pair `pair` through its
+// ring (this lane's slots at ring / shared address rs) and writes the nloc jobs' sums, job b's products from
+// limb polynomial acc_first(bstart + b) on.
+template <int BC, bool FOLD, class KT>
+__device__ __forceinline__ void w_mac_unit(const KT& kt, const uint2* __restrict__ kwt, const uint2* dsm, int run,
+                                           uint2* ring, uint32_t rs, int D, int key_digits, int total, int j,
+                                           int pair, int xb, int log_n, int slane, int bstart, int nloc,
+                                           uint32_t q0, uint32_t q1, u64 bar0, u64 bar1, uint2* acc) {
+  const int lane = threadIdx.x & 31, N = 1 << log_n, tiles = N >> 5;
+  const size_t krun = (size_t)key_digits * 2 * 32;
+  const uint2* kp = kwt + (((size_t)j * 2 + pair) * tiles + xb) * krun + lane;
+  u64 a0[BC], a1[BC], c0[BC], c1[BC];
+#pragma unroll
+  for (int b = 0; b < BC; ++b) a0[b] = a1[b] = c0[b] = c1[b] = 0;
+  // each lane copies and later reads only its own words, so the waits need no warp barrier
+#pragma unroll
+  for (int u = 0; u < W_PF; ++u) {
+    if (u < D) {
+      cp_async8(rs + 8u * (64 * u), kp + (size_t)u * 64);
+      cp_async8(rs + 8u * (64 * u + 32), kp + (size_t)u * 64 + 32);
+    }
+    cp_async_commit();
+  }
+#pragma unroll 1
+  for (int i0 = 0; i0 < D; i0 += W_PF) {
+    if (FOLD && i0 > 0 && (i0 & 63) == 0) {  // fold: the next 64 terms then stay below 2^64
+#pragma unroll
+      for (int b = 0; b < BC; ++b) {
+        a0[b] = reduce64_32(a0[b], q0, bar0);
+        a1[b] = reduce64_32(a1[b], q1, bar1);
+        c0[b] = reduce64_32(c0[b], q0, bar0);
+        c1[b] = reduce64_32(c1[b], q1, bar1);
+      }
+    }
+#pragma unroll
+    for (int u = 0; u < W_PF; ++u) {
+      const int i = i0 + u;
+      if (i < D) {
+        cp_async_wait<W_PF - 1>();  // digit i's group has landed
+        const uint2 k0 = ring[64 * u], k1 = ring[64 * u + 32];
+        const uint2* dp = dsm + i * 32 + slane;
+#pragma unroll
+        for (int b = 0; b < BC; ++b) {
+          const uint2 d = dp[b * run];
+          a0[b] += (u64)d.x * k0.x;
+          a1[b] += (u64)d.y * k0.y;
+          c0[b] += (u64)d.x * k1.x;
+          c1[b] += (u64)d.y * k1.y;
+        }
+        // refill the slot with digit i + W_PF once its words have been used
+        if (i + W_PF < D) {
+          cp_async8(rs + 8u * (64 * u), kp + (size_t)(i + W_PF) * 64);
+          cp_async8(rs + 8u * (64 * u + 32), kp + (size_t)(i + W_PF) * 64 + 32);
+        }
+        cp_async_commit();
+      }
+    }
+  }
+  cp_async_wait<0>();
+  const int x = xb * 32 + lane;
+#pragma unroll
+  for (int b = 0; b < BC; ++b) {
+    if (b < nloc) {
+      const size_t ab = kt.acc_first(bstart + b, total);
+      acc[((ab + j) * 2 + pair) * N + x] = make_uint2(reduce64_32(a0[b], q0, bar0), reduce64_32(a1[b], q1, bar1));
+      acc[((ab + total + j) * 2 + pair) * N + x] =
+          make_uint2(reduce64_32(c0[b], q0, bar0), reduce64_32(c1[b], q1, bar1));
+    }
+  }
+}
+
 // Job tables of the key product.  A CTA (blockIdx.x) covers up to BC consecutive jobs that share one key;
 // cta() gives that key (tiled wide form, digits used and stored, limbs + K) and the jobs; dt_first(job) is
 // where the job's digit transforms start (in uint2 words), acc_first(job, total) where its products start
@@ -444,72 +516,13 @@ __global__ __launch_bounds__(32 * w_mac_warps<BC>(), BC >= 8 ? 2 : (BC >= 4 ? 3 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t q0 = pick(w.q, pair, 0), q1 = pick(w.q, pair, 1);
   const u64 bar0 = pick(w.bar, pair, 0), bar1 = pick(w.bar, pair, 1);
-  const size_t krun = (size_t)key_digits * 2 * 32;
   // this lane's slots of the warp's key ring: slot u holds (k0, k1) of one digit at ring[u][0|1][lane]
   uint2* ring = dsm + (size_t)BC * run + (size_t)warp * W_PF * 64 + lane;
   const uint32_t rs = (uint32_t)__cvta_generic_to_shared(ring);
 #pragma unroll 1
-  for (int j = warp; j < total; j += w_mac_warps<BC>()) {
-    const uint2* kp = kwt + (((size_t)j * 2 + pair) * tiles + xb) * krun + lane;
-    u64 a0[BC], a1[BC], c0[BC], c1[BC];
-#pragma unroll
-    for (int b = 0; b < BC; ++b) a0[b] = a1[b] = c0[b] = c1[b] = 0;
-    // each lane copies and later reads only its own words, so the waits need no warp barrier
-#pragma unroll
-    for (int u = 0; u < W_PF; ++u) {
-      if (u < D) {
-        cp_async8(rs + 8u * (64 * u), kp + (size_t)u * 64);
-        cp_async8(rs + 8u * (64 * u + 32), kp + (size_t)u * 64 + 32);
-      }
-      cp_async_commit();
-    }
-#pragma unroll 1
-    for (int i0 = 0; i0 < D; i0 += W_PF) {
-      if (FOLD && i0 > 0 && (i0 & 63) == 0) {  // fold: the next 64 terms then stay below 2^64
-#pragma unroll
-        for (int b = 0; b < BC; ++b) {
-          a0[b] = reduce64_32(a0[b], q0, bar0);
-          a1[b] = reduce64_32(a1[b], q1, bar1);
-          c0[b] = reduce64_32(c0[b], q0, bar0);
-          c1[b] = reduce64_32(c1[b], q1, bar1);
-        }
-      }
-#pragma unroll
-      for (int u = 0; u < W_PF; ++u) {
-        const int i = i0 + u;
-        if (i < D) {
-          cp_async_wait<W_PF - 1>();  // digit i's group has landed
-          const uint2 k0 = ring[64 * u], k1 = ring[64 * u + 32];
-          const uint2* dp = dsm + i * 32 + slane;
-#pragma unroll
-          for (int b = 0; b < BC; ++b) {
-            const uint2 d = dp[b * run];
-            a0[b] += (u64)d.x * k0.x;
-            a1[b] += (u64)d.y * k0.y;
-            c0[b] += (u64)d.x * k1.x;
-            c1[b] += (u64)d.y * k1.y;
-          }
-          // refill the slot with digit i + W_PF once its words have been used
-          if (i + W_PF < D) {
-            cp_async8(rs + 8u * (64 * u), kp + (size_t)(i + W_PF) * 64);
-            cp_async8(rs + 8u * (64 * u + 32), kp + (size_t)(i + W_PF) * 64 + 32);
-          }
-          cp_async_commit();
-        }
-      }
-    }
-    cp_async_wait<0>();
-    const int x = xb * 32 + lane;
-#pragma unroll
-    for (int b = 0; b < BC; ++b) {
-      if (b < nloc) {
-        const size_t ab = kt.acc_first(bstart + b, total);
-        acc[((ab + j) * 2 + pair) * N + x] = make_uint2(reduce64_32(a0[b], q0, bar0), reduce64_32(a1[b], q1, bar1));
-        acc[((ab + total + j) * 2 + pair) * N + x] =
-            make_uint2(reduce64_32(c0[b], q0, bar0), reduce64_32(c1[b], q1, bar1));
-      }
-    }
-  }
+  for (int j = warp; j < total; j += w_mac_warps<BC>())
+    w_mac_unit<BC, FOLD>(kt, kwt, dsm, run, ring, rs, D, key_digits, total, j, pair, xb, w.log_n, slane, bstart,
+                         nloc, q0, q1, bar0, bar1, acc);
 }
 
 // D: the largest digit count of the launch (sizes the shared memory); ctas: grid.x
@@ -537,6 +550,167 @@ void launch_w_mac_uni(const WidePrimes& w, int D, int key_digits, int total, con
                       uint2* acc, int b0, int nb, uint32_t gal, cudaStream_t s) {
   const UniMac kt{kwt, D, key_digits, total, b0, nb};
   launch_w_mac<BC, FOLD>(w, kt, D, (nb + BC - 1) / BC, dtt, acc, gal, s);
+}
+
+// Persistent form of the key product for a uniform batch (BC jobs per tile, sums of at most 64 terms): one
+// CTA of WP_WARPS warps per SM walks the tiles blockIdx.x, + gridDim.x, ... (a tile = one job group x one pair
+// x 32 positions; job groups vary fastest, so the CTAs streaming the same key tile run side by side and share
+// it in L2).  The (tile, limb) units of the CTA's tiles are taken in order from a shared counter, so no warp
+// waits at a tile's end for another warp's last limb; the digit tiles are double-buffered: the last unit of
+// tile i to finish starts the bulk copy of tile i + 2 into the buffer tile i used.  Every wait is bounded; a
+// wait that runs out records g_wide_errors and stops the CTA, which still waits (bounded) for its copies in
+// flight before it exits.
+constexpr int WP_WARPS = 16;
+
+struct WPersist {
+  uint64_t full[2];  // per buffer: completes when a tile's bulk copies have landed
+  int next;          // next unit to take
+  int done[2];       // units of the buffer's current tile finished
+  int tile_in[2];    // local tile whose copies were last issued into the buffer (-1: none)
+  int abort;
+};
+
+template <int BC>
+__global__ __launch_bounds__(32 * WP_WARPS, 1) void k_w_mac_p(WidePrimes w, UniMac kt, const uint2* __restrict__ dtt,
+                                                              uint2* acc, uint32_t gal, int groups) {
+  extern __shared__ __align__(128) uint2 dsm[];  // [2][BC][D][32] digit tiles, then [warps][W_PF][2][32] key ring
+  __shared__ WPersist st;
+  const int N = 1 << w.log_n, tiles = N >> 5;
+  const int D = kt.D, total = kt.total, run = D * 32;
+  const int ntiles = groups * 2 * tiles;
+  const int count = (int)blockIdx.x < ntiles ? (ntiles - 1 - (int)blockIdx.x) / (int)gridDim.x + 1 : 0;
+  const int units = count * total;
+  const uint32_t full0 = (uint32_t)__cvta_generic_to_shared(&st.full[0]);
+  const uint32_t sbase = (uint32_t)__cvta_generic_to_shared(dsm);
+  const uint32_t run_bytes = (uint32_t)run * 8u, tile_bytes = (uint32_t)BC * run_bytes;
+  auto tile_of = [&](int i, int& g, int& pair, int& xb) {
+    int t = (int)blockIdx.x + i * (int)gridDim.x;
+    g = t % groups;
+    t /= groups;
+    pair = t & 1;
+    xb = t >> 1;
+  };
+  // one thread: the bulk copies of local tile i's digit transforms into buffer i & 1
+  auto issue = [&](int i) {
+    int g, pair, xb;
+    tile_of(i, g, pair, xb);
+    const int bstart = kt.b0 + g * BC, nloc = min(BC, kt.b0 + kt.nb - bstart);
+    const uint32_t src0 = gal > 1 ? galois_source((uint32_t)xb * 32, gal, w.log_n) : (uint32_t)xb * 32;
+    const int stile = (int)(src0 >> 5);
+    const uint32_t bar = full0 + 8u * (uint32_t)(i & 1);
+    asm volatile("mbarrier.arrive.expect_tx.shared::cta.b64 _, [%0], %1;" ::"r"(bar), "r"(run_bytes * (uint32_t)nloc)
+                 : "memory");
+    for (int b = 0; b < nloc; ++b) {
+      const uint2* src = dtt + kt.dt_first(bstart + b, N) + ((size_t)pair * tiles + stile) * run;
+      asm volatile(
+          "cp.async.bulk.shared::cluster.global.mbarrier::complete_tx::bytes [%0], [%1], %2, [%3];" ::"r"(
+              sbase + (uint32_t)(i & 1) * tile_bytes + (uint32_t)b * run_bytes),
+          "l"(src), "r"(run_bytes), "r"(bar)
+          : "memory");
+    }
+    atomicExch(&st.tile_in[i & 1], i);
+  };
+  if (threadIdx.x == 0) {
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0) : "memory");
+    asm volatile("mbarrier.init.shared::cta.b64 [%0], 1;" ::"r"(full0 + 8u) : "memory");
+    asm volatile("fence.mbarrier_init.release.cluster;" ::: "memory");
+    st.next = 0;
+    st.done[0] = st.done[1] = 0;
+    st.tile_in[0] = st.tile_in[1] = -1;
+    st.abort = 0;
+  }
+  __syncthreads();
+  if (threadIdx.x == 0)
+    for (int i = 0; i < 2 && i < count; ++i) issue(i);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  uint2* ring = dsm + 2 * (size_t)BC * run + (size_t)warp * W_PF * 64 + lane;
+  const uint32_t rs = (uint32_t)__cvta_generic_to_shared(ring);
+  volatile int* vst = &st.abort;
+  volatile int* vtile = st.tile_in;
+#pragma unroll 1
+  for (;;) {
+    int u = 0;
+    if (lane == 0) u = atomicAdd(&st.next, 1);
+    u = __shfl_sync(0xffffffffu, u, 0);
+    if (u >= units || *vst) break;
+    const int i = u / total, j = u - i * total, buf = i & 1;
+    // the buffer's mbarrier phase parity names tile i only once tile i's copies have been issued into it
+    bool ok = true;
+    for (uint32_t it = 0; vtile[buf] != i; ++it)
+      if (*vst || it >= w.first_wait_polls) {
+        ok = false;
+        break;
+      }
+    ok = __all_sync(0xffffffffu, ok && mbar_wait_bounded(full0 + 8u * (uint32_t)buf, (uint32_t)(i >> 1) & 1u,
+                                                         w.first_wait_polls));
+    if (!ok) {
+      if (lane == 0) {
+        atomicOr(&g_wide_errors, 1);
+        atomicExch(&st.abort, 1);
+      }
+      break;
+    }
+    int g, pair, xb;
+    tile_of(i, g, pair, xb);
+    const int bstart = kt.b0 + g * BC, nloc = min(BC, kt.b0 + kt.nb - bstart);
+    const int slane = gal > 1 ? (int)(galois_source((uint32_t)xb * 32 + (uint32_t)lane, gal, w.log_n) & 31) : lane;
+    w_mac_unit<BC, false>(kt, kt.kwt, dsm + (size_t)buf * BC * run, run, ring, rs, D, kt.key_digits, total, j, pair,
+                          xb, w.log_n, slane, bstart, nloc, pick(w.q, pair, 0), pick(w.q, pair, 1),
+                          pick(w.bar, pair, 0), pick(w.bar, pair, 1), acc);
+    // every lane's reads of the buffer are done (ordered by the warp barrier and the fence) before the unit
+    // counts; the tile's last unit hands the buffer to the bulk copies of tile i + 2
+    __syncwarp();
+    if (lane == 0) {
+      __threadfence_block();
+      if (atomicAdd(&st.done[buf], 1) == total - 1) {
+        __threadfence_block();
+        atomicExch(&st.done[buf], 0);
+        if (i + 2 < count && !*vst) {
+          asm volatile("fence.proxy.async.shared::cta;" ::: "memory");
+          issue(i + 2);
+        }
+      }
+    }
+  }
+  __syncthreads();
+  // drain: the copies last issued into each buffer have landed before the shared memory is released
+  if (threadIdx.x == 0)
+    for (int b = 0; b < 2; ++b)
+      if (st.tile_in[b] >= 0 &&
+          !mbar_wait_bounded(full0 + 8u * (uint32_t)b, (uint32_t)(st.tile_in[b] >> 1) & 1u, W_DRAIN_POLLS))
+        atomicOr(&g_wide_errors, 1);
+}
+
+// Launches the persistent key product when its two digit tiles and the rings fit the shared memory of one
+// CTA; false (nothing launched) otherwise.
+template <int BC>
+bool launch_w_mac_persistent(const WidePrimes& w, int D, int key_digits, int total, const uint2* kwt,
+                             const uint2* dtt, uint2* acc, int b0, int nb, uint32_t gal, cudaStream_t s) {
+  struct Limits {
+    int smem = 0, sms = 0;
+  };
+  static Limits lim;
+  static std::once_flag once;
+  std::call_once(once, [] {
+    int dev = 0, optin = 48 * 1024, sms = 1;
+    if (cudaGetDevice(&dev) == cudaSuccess) {
+      cudaDeviceGetAttribute(&optin, cudaDevAttrMaxSharedMemoryPerBlockOptin, dev);
+      cudaDeviceGetAttribute(&sms, cudaDevAttrMultiProcessorCount, dev);
+    }
+    cudaFuncAttributes fa{};
+    cudaFuncGetAttributes(&fa, k_w_mac_p<BC>);
+    lim.smem = optin - (int)fa.sharedSizeBytes;
+    lim.sms = sms;
+    cudaFuncSetAttribute(k_w_mac_p<BC>, cudaFuncAttributeMaxDynamicSharedMemorySize, lim.smem);
+  });
+  const size_t smem = (2 * (size_t)BC * D * 32 + (size_t)WP_WARPS * W_PF * 64) * sizeof(uint2);
+  if (D > 64 || smem > (size_t)lim.smem) return false;
+  const int groups = (nb + BC - 1) / BC;
+  const int ntiles = groups * 2 * ((1 << w.log_n) / 32);
+  const int grid = ntiles < lim.sms ? ntiles : lim.sms;
+  const UniMac kt{kwt, D, key_digits, total, b0, nb};
+  k_w_mac_p<BC><<<grid, 32 * WP_WARPS, smem, s>>>(w, kt, dtt, acc, gal, groups);
+  return true;
 }
 
 // coefficient-form key [digits][2][limbs][N] -> kw[((j * digits + i) * 2 + c)][pair][N]
@@ -658,6 +832,11 @@ void wide_mac(const WidePrimes& w, int D, int key_digits, int total, const uint2
     else launch_w_mac_uni<4, true>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
     return;
   }
+  if (w.persistent && want > 4 && launch_w_mac_persistent<8>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s))
+    return;
+  if (w.persistent && want > 2 && want <= 4 &&
+      launch_w_mac_persistent<4>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s))
+    return;
   if (want <= 1) launch_w_mac_uni<1, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
   else if (want <= 2) launch_w_mac_uni<2, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);
   else if (want <= 4) launch_w_mac_uni<4, false>(w, D, key_digits, total, kwt, dtt, acc, b0, nb, gal, s);

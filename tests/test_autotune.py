@@ -55,8 +55,9 @@ def test_tuning_keeps_results_and_applies_choice(pkg, T, tmp_path):
     rep = T.tune_mult_relinearized(ctx, lhs, rhs, [key] * 12, outs, reps=1, cache=tmp_path / "t.json")
     assert not rep["cached"] and T.current(ctx, rep["choice"]) == rep["choice"]
     assert len(rep["trials"]) == 32  # 4 x 2 x 2 x 2 candidates, all primes below 2^58
-    # kernel shapes after that: 2 x 2, times the splits 6x6 only at N = 2^12
-    assert len(rep["shape_trials"]) == 4 and set(rep["choice"]) >= {"col_ctas", "row_polys"}
+    # kernel shapes after that: 2 x 2 x 2 (column CTAs, row polynomials, persistent key product), times the
+    # splits 6x6 only at N = 2^12
+    assert len(rep["shape_trials"]) == 8 and set(rep["choice"]) >= {"col_ctas", "row_polys", "mac_persistent"}
     for o, r in zip(ctx.mult_relinearized_batch(lhs, rhs, [key] * 12), ref):
         assert np.array_equal(o.numpy(), r)
     again = T.tune_mult_relinearized(ctx, lhs, rhs, [key] * 12, outs, reps=1, cache=tmp_path / "t.json")

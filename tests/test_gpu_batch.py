@@ -1,5 +1,6 @@
 """Mixed-level batched relinearize+rescale and CUDA-graph capture of library calls, bit-exact against the
 per-op path and the oracle (relinearize: context/ops.rs:111-122, rescale: context/ops.rs:32-37)."""
+import ctypes
 import math
 
 import numpy as np
@@ -265,3 +266,60 @@ def test_mixed_levels_with_q_only_keys(pkg, oracle):
     r0, r1 = oracle.relinearize(qpl, None, d[0], d[1], d[2], host[lv], host[lv].shape[0])
     assert np.array_equal(mixed[0][0], oracle.rescale_poly(qpl, r0))
     assert np.array_equal(mixed[0][1], oracle.rescale_poly(qpl, r1))
+
+
+def test_persistent_key_product_matches_the_per_tile_form(env):
+    """The persistent key product (one CTA per SM taking (tile, limb) units, the next tile's digit transforms
+    copied while the current one is used) gives the residues of the one-CTA-per-tile form: ragged job groups
+    (11 jobs in groups of 8 and of 4), fewer limbs than the CTA has warps (6 limbs at level 3), and the hoisted
+    rotation's permuted digit tiles; the batch also equals the per-op calls."""
+    C, ctx, params, keys, host_keys, O = env
+    n, q, p = params.poly_degree, params.q_moduli(), params.p_moduli()
+    rng = np.random.default_rng(91)
+
+    def lin(lv):
+        return C.RnsCiphertext(C.to_device(np.stack([np.stack([rng.integers(0, m, n, dtype=np.uint64)
+                                                               for m in q[: lv + 1]]) for _ in range(2)])), 40)
+
+    g = 5  # rotation by one slot
+    rk = {}
+    for lv in (7, 3):
+        k = np.stack([np.stack([np.stack([rng.integers(0, m, n, dtype=np.uint64) for m in q[: lv + 1] + p])
+                                for _ in range(2)]) for _ in range(host_keys[lv].shape[0])])
+        rk[lv] = C.RnsRotationKey(g, ctx.upload_keyswitch_key(k, lv, len(p), g))
+    cases = {lv: ([lin(lv) for _ in range(11)], [lin(lv) for _ in range(11)]) for lv in (7, 3)}
+
+    def run():
+        out = {}
+        for lv, (a, b) in cases.items():
+            out[("mult", lv)] = [o.numpy() for o in ctx.mult_relinearized_batch(a, b, [keys[lv]] * len(a))]
+            out[("rot", lv)] = [o.numpy() for row in ctx.rotate_hoisted(a, [rk[lv]]) for o in row]
+        return out
+
+    old = {}
+    for name in ("mac_persistent", "mac_bc"):
+        v = ctypes.c_int32()
+        C.call("rc_tune_get", ctx.handle, name.encode(), ctypes.byref(v))
+        old[name] = v.value
+    try:
+        results = {}
+        for bc in (8, 4):
+            for pers in (1, 0):
+                C.call("rc_tune_set", ctx.handle, b"mac_bc", bc)
+                C.call("rc_tune_set", ctx.handle, b"mac_persistent", pers)
+                results[(bc, pers)] = run()
+    finally:
+        for name, v in old.items():
+            C.call("rc_tune_set", ctx.handle, name.encode(), v)
+    flags = ctypes.c_int32(-1)
+    C.call("rc_kernel_errors", ctypes.byref(flags), 1)
+    assert flags.value == 0
+    ref = results[(8, 0)]
+    for cfg, res in results.items():
+        for k in ref:
+            for x, y in zip(res[k], ref[k]):
+                assert np.array_equal(x, y), (cfg, k)
+    for lv, (a, b) in cases.items():
+        for i in (0, 10):
+            assert np.array_equal(ctx.mult_relinearized(a[i], b[i], keys[lv]).numpy(), ref[("mult", lv)][i])
+            assert np.array_equal(ctx.rotate(a[i], rk[lv]).numpy(), ref[("rot", lv)][i])
