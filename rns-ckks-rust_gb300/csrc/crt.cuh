@@ -41,6 +41,64 @@ __device__ __forceinline__ CrtSmem stage_crt_tables(const PrimeConst* pc, const 
 
 inline size_t crt_smem_bytes(int limbs, int W) { return ((size_t)limbs * W + 4 * (size_t)limbs + 2 * (size_t)W) * 8; }
 
+// x[0..8) += lo (HI = false) or hi (HI = true) of a * b[j] at word j, a carry chain of 32-bit multiply-adds with
+// carry in cin (0 or 1); returns the carry out of x[7]
+template <bool HI>
+__device__ __forceinline__ uint32_t mac_chain8(uint32_t* x, uint32_t a, const uint32_t* b, uint32_t cin) {
+  uint32_t cout;
+  if (HI)
+    asm("{\n\t.reg .u32 t;\n\t"
+        "add.cc.u32 t, %9, 0xffffffff;\n\t"  // carry flag = (cin != 0)
+        "madc.hi.cc.u32 %0, %10, %11, %0;\n\tmadc.hi.cc.u32 %1, %10, %12, %1;\n\t"
+        "madc.hi.cc.u32 %2, %10, %13, %2;\n\tmadc.hi.cc.u32 %3, %10, %14, %3;\n\t"
+        "madc.hi.cc.u32 %4, %10, %15, %4;\n\tmadc.hi.cc.u32 %5, %10, %16, %5;\n\t"
+        "madc.hi.cc.u32 %6, %10, %17, %6;\n\tmadc.hi.cc.u32 %7, %10, %18, %7;\n\t"
+        "addc.u32 %8, 0, 0;\n\t}"
+        : "+r"(x[0]), "+r"(x[1]), "+r"(x[2]), "+r"(x[3]), "+r"(x[4]), "+r"(x[5]), "+r"(x[6]), "+r"(x[7]),
+          "=r"(cout)
+        : "r"(cin), "r"(a), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]),
+          "r"(b[7]));
+  else
+    asm("{\n\t.reg .u32 t;\n\t"
+        "add.cc.u32 t, %9, 0xffffffff;\n\t"
+        "madc.lo.cc.u32 %0, %10, %11, %0;\n\tmadc.lo.cc.u32 %1, %10, %12, %1;\n\t"
+        "madc.lo.cc.u32 %2, %10, %13, %2;\n\tmadc.lo.cc.u32 %3, %10, %14, %3;\n\t"
+        "madc.lo.cc.u32 %4, %10, %15, %4;\n\tmadc.lo.cc.u32 %5, %10, %16, %5;\n\t"
+        "madc.lo.cc.u32 %6, %10, %17, %6;\n\tmadc.lo.cc.u32 %7, %10, %18, %7;\n\t"
+        "addc.u32 %8, 0, 0;\n\t}"
+        : "+r"(x[0]), "+r"(x[1]), "+r"(x[2]), "+r"(x[3]), "+r"(x[4]), "+r"(x[5]), "+r"(x[6]), "+r"(x[7]),
+          "=r"(cout)
+        : "r"(cin), "r"(a), "r"(b[0]), "r"(b[1]), "r"(b[2]), "r"(b[3]), "r"(b[4]), "r"(b[5]), "r"(b[6]),
+          "r"(b[7]));
+  return cout;
+}
+
+// X (32-bit words x[0..2WM+2)) += y * (W 64-bit words qh): four carry chains of 32-bit multiply-adds (lo and hi
+// halves of y_lo * qh and y_hi * qh) over blocks of eight words, each block's words loaded once for the four
+// chains.  Every partial sum stays below 2^(64 W) (W has 8 bits of headroom over Q and the sum is below
+// limbs * Q), so no chain carries out of word 2W - 1 and the carries out of the last block are zero.
+template <int WM>
+__device__ __forceinline__ void crt_mac32(uint32_t (&x)[2 * WM + 2], u64 y, const u64* qh, int W) {
+  const uint32_t y0 = (uint32_t)y, y1 = (uint32_t)(y >> 32);
+  uint32_t ca = 0, cb = 0, cc = 0, cd = 0;
+#pragma unroll
+  for (int k = 0; k < WM / 4; ++k) {
+    if (4 * k < W) {
+      uint32_t b[8];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const u64 v = 4 * k + i < W ? qh[4 * k + i] : 0ull;
+        b[2 * i] = (uint32_t)v;
+        b[2 * i + 1] = (uint32_t)(v >> 32);
+      }
+      ca = mac_chain8<false>(x + 8 * k, y0, b, ca);
+      cb = mac_chain8<true>(x + 8 * k + 1, y0, b, cb);
+      cc = mac_chain8<false>(x + 8 * k + 1, y1, b, cc);
+      cd = mac_chain8<true>(x + 8 * k + 2, y1, b, cd);
+    }
+  }
+}
+
 // The centred CRT value of one coefficient: X in (-Q/2, Q/2] as a W-word two's complement number in X[0..W)
 // (keyswitching.rs:397-454 up to the digit split; the tie X == floor(Q/2) stays positive).  `in` points at
 // limb 0 of the coefficient, limbs N apart; neg negates every residue first (a negacyclic automorphism
@@ -48,8 +106,9 @@ inline size_t crt_smem_bytes(int limbs, int W) { return ((size_t)limbs * W + 4 *
 template <int WM>
 __device__ __forceinline__ u64 centred_crt(const CrtSmem& t, int W, int limbs, const u64* in, u64 N, bool neg,
                                            u64 (&X)[WM]) {
+  uint32_t X32[2 * WM + 2];
 #pragma unroll
-  for (int w = 0; w < WM; ++w) X[w] = 0;
+  for (int w = 0; w < 2 * WM + 2; ++w) X32[w] = 0;
   u64 fsum = 0;  // sum of y_l / q_l in units of 2^-31 (each term within 3 units below its value)
   for (int l = 0; l < limbs; ++l) {
     const u64 q = t.q[l];
@@ -58,21 +117,10 @@ __device__ __forceinline__ u64 centred_crt(const CrtSmem& t, int W, int limbs, c
     const u64 y = mul_shoup(r, t.hinv[l], t.hinv_s[l], q);
     const u64 fx = t.invq[l];
     fsum += __umulhi((uint32_t)((y << (uint32_t)(fx >> 32)) >> 32), (uint32_t)fx);
-    const u64* qh = t.qhat + (size_t)l * W;
-    u64 carry = 0;
-#pragma unroll
-    for (int w = 0; w < WM; ++w) {
-      if (w < W) {
-        U128 p = mul_wide(y, qh[w]);
-        u64 lo = p.lo + X[w];
-        u64 c1 = lo < X[w] ? 1ull : 0ull;
-        u64 lo2 = lo + carry;
-        u64 c2 = lo2 < carry ? 1ull : 0ull;
-        X[w] = lo2;
-        carry = p.hi + c1 + c2;
-      }
-    }
+    crt_mac32<WM>(X32, y, t.qhat + (size_t)l * W, W);  // X += y * (Q / q_l)
   }
+#pragma unroll
+  for (int w = 0; w < WM; ++w) X[w] = (u64)X32[2 * w] | ((u64)X32[2 * w + 1] << 32);
   // X' = X - k*Q with k = floor(sum y_i / q_i) (exact up to +-1, fixed below).  `top` follows the
   // word W-1 as each pass writes it: reading X[W-1] afterwards would index X dynamically and move it to
   // local memory.
