@@ -99,6 +99,29 @@ __device__ __forceinline__ void crt_mac32(uint32_t (&x)[2 * WM + 2], u64 y, cons
   }
 }
 
+// X (32-bit words) += k * (2^(64 W) - Q) = X - k Q mod 2^(64 W): two carry chains (lo and hi halves) of k times
+// the words of 2^(64 W) - Q = ~Q + 1 (Q is odd, so the +1 never carries out of word 0).  Words at 2W and
+// above take the carries past 2^(64 W) and are not read.
+template <int WM>
+__device__ __forceinline__ void crt_sub_kq32(uint32_t (&x)[2 * WM + 2], uint32_t k, const u64* Q, int W) {
+  uint32_t ca = 0, cb = 0;
+#pragma unroll
+  for (int blk = 0; blk < WM / 4; ++blk) {
+    if (4 * blk < W) {
+      uint32_t b[8];
+#pragma unroll
+      for (int i = 0; i < 4; ++i) {
+        const int w = 4 * blk + i;
+        const u64 v = w < W ? (w == 0 ? ~Q[0] + 1 : ~Q[w]) : 0ull;
+        b[2 * i] = (uint32_t)v;
+        b[2 * i + 1] = (uint32_t)(v >> 32);
+      }
+      ca = mac_chain8<false>(x + 8 * blk, k, b, ca);
+      cb = mac_chain8<true>(x + 8 * blk + 1, k, b, cb);
+    }
+  }
+}
+
 // The centred CRT value of one coefficient: X in (-Q/2, Q/2] as a W-word two's complement number in X[0..W)
 // (keyswitching.rs:397-454 up to the digit split; the tie X == floor(Q/2) stays positive).  `in` points at
 // limb 0 of the coefficient, limbs N apart; neg negates every residue first (a negacyclic automorphism
@@ -119,32 +142,13 @@ __device__ __forceinline__ u64 centred_crt(const CrtSmem& t, int W, int limbs, c
     fsum += __umulhi((uint32_t)((y << (uint32_t)(fx >> 32)) >> 32), (uint32_t)fx);
     crt_mac32<WM>(X32, y, t.qhat + (size_t)l * W, W);  // X += y * (Q / q_l)
   }
+  crt_sub_kq32<WM>(X32, (uint32_t)(fsum >> 31), t.Q, W);
 #pragma unroll
   for (int w = 0; w < WM; ++w) X[w] = (u64)X32[2 * w] | ((u64)X32[2 * w + 1] << 32);
-  // X' = X - k*Q with k = floor(sum y_i / q_i) (exact up to +-1, fixed below).  `top` follows the
-  // word W-1 as each pass writes it: reading X[W-1] afterwards would index X dynamically and move it to
-  // local memory.
-  u64 k = fsum >> 31;
   u64 top = 0;
-  {
-    u64 borrow = 0, carry = 0;
 #pragma unroll
-    for (int w = 0; w < WM; ++w) {
-      if (w < W) {
-        U128 p = mul_wide(k, t.Q[w]);
-        u64 sub = p.lo + carry;
-        carry = p.hi + (sub < carry ? 1ull : 0ull);
-        u64 xw = X[w];
-        u64 d = xw - sub;
-        u64 b1 = xw < sub ? 1ull : 0ull;
-        u64 d2 = d - borrow;
-        u64 b2 = d < borrow ? 1ull : 0ull;
-        X[w] = d2;
-        top = d2;
-        borrow = b1 + b2;
-      }
-    }
-  }
+  for (int w = 0; w < WM; ++w)
+    if (w < W) top = X[w];
   // X is now in [-Q, 2Q) as a W-word two's complement value
   auto top_neg = [&]() -> bool { return (top >> 63) != 0; };
   auto add_Q = [&](bool subtract) {
