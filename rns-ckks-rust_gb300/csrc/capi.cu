@@ -311,10 +311,10 @@ void wide_ks_finish(rc_context* c, const WideKs& w, const std::vector<KsJob>& jo
   f.add_g_inv = g_inv;
   f.wide = 1;
   f.wt = c->wide;
-  // the lazy finalize sums at most (8 + 2K) terms below q per limb: every prime below 2^64 / (8 + 2K)
+  // the lazy finalize sums per limb terms below (12 + 4K) q in all: every prime below 2^64 / (12 + 4K)
   f.lazy = 1;
   for (uint64_t m : c->mod)
-    if (m >= UINT64_MAX / (uint64_t)(8 + 2 * w.K)) f.lazy = 0;
+    if (m >= UINT64_MAX / (uint64_t)(12 + 4 * w.K)) f.lazy = 0;
   PtrTab add{}, out{};
   for (int j = 0; j < n; ++j) {
     add.p[2 * j] = const_cast<uint64_t*>(jobs[b0 + j].add0);
@@ -404,9 +404,9 @@ void keyswitch_ml(rc_context* c, const std::vector<KsJob>& jobs, const std::vect
   f.add_g_inv = 0;
   f.wide = 1;
   f.wt = c->wide;
-  f.lazy = 1;
+  f.lazy = 1;  // as in keyswitch_wide: per-limb terms below (12 + 4K) q in all
   for (uint64_t m : c->mod)
-    if (m >= UINT64_MAX / (uint64_t)(8 + 2 * K)) f.lazy = 0;
+    if (m >= UINT64_MAX / (uint64_t)(12 + 4 * K)) f.lazy = 0;
   finalize_ml(f, t, (const uint64_t*)acc, add, out, s);
   launch_check("finalize (mixed levels)");
 }
@@ -818,21 +818,21 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
     c->root = qg;
     c->root.insert(c->root.end(), pg.begin(), pg.end());
     const int P = (int)c->mod.size();
-    // Lazy (unreduced) forward butterflies need every prime < 2^58
+    // Lazy (unreduced) forward butterflies with approximate Shoup products need every prime < 2^57
+    // ((4 log N + 1) q < 2^64)
     c->lazy = true;
     if (const char* e = getenv("RNSCKKS_LAZY_NTT")) c->lazy = atoi(e) != 0;
-    for (uint64_t q : c->mod) c->lazy = c->lazy && q < (1ull << 58);
+    for (uint64_t q : c->mod) c->lazy = c->lazy && q < (1ull << 57);
     c->lazy_inv = true;
     for (uint64_t q : c->mod) c->lazy_inv = c->lazy_inv && q < (1ull << 55);
     if (const char* e = getenv("RNSCKKS_MAC64")) c->mac64 = atoi(e) != 0;
 
     // ---- per-prime constants and twiddles
     std::vector<PrimeConst> pcs(P);
-    // bound (in multiples of q) of a forward-NTT output fed to the key product:
-    // 2q per stage above q when lazy, 4q otherwise
-    // bound of a forward-transform output in units of q for either butterfly mode (the mode can be changed
-    // later with rc_tune_set), so the key-product chunk below stays valid
-    const uint64_t out_bound = std::max<uint64_t>(2 * c->log_n + 1, 4);
+    // bound (in multiples of q) of a forward-NTT output fed to the key product: 4q per stage above q when lazy
+    // (approximate Shoup products), 4q otherwise; for either butterfly mode (the mode can be changed later with
+    // rc_tune_set), so the key-product chunk below stays valid
+    const uint64_t out_bound = std::max<uint64_t>(4 * c->log_n + 1, 4);
     std::vector<Twiddle> twf((size_t)P * N), twi((size_t)P * N);
     for (int i = 0; i < P; ++i) {
       const uint64_t q = c->mod[i];
@@ -1202,10 +1202,14 @@ extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
       c->wp.first_wait_polls = (uint32_t)value;
     } else if (n == "mac_persistent") {
       c->wp.persistent = value != 0;
+    } else if (n == "ntt_r16") {
+      require(value >= 0 && value <= r16::R16_ALL, "ntt_r16 must be a set of pass bits in 0..63");
+      c->r16 = value;
+      c->wp.r16 = value;
     } else if (n == "lazy_ntt") {
       bool ok = true;
-      for (uint64_t q : c->mod) ok = ok && q < (1ull << 58);
-      require(!value || ok, "lazy_ntt needs every prime below 2^58");
+      for (uint64_t q : c->mod) ok = ok && q < (1ull << 57);
+      require(!value || ok, "lazy_ntt needs every prime below 2^57");
       c->lazy = value != 0;
     } else {
       fail(RC_ERR_INVALID_ARGUMENT, "unknown tunable " + n);
@@ -1230,6 +1234,7 @@ extern "C" int rc_tune_get(const rc_context* c, const char* name, int32_t* value
     else if (n == "ntt_split") *value = c->n1;
     else if (n == "col_ctas") *value = c->col_ctas;
     else if (n == "row_polys") *value = c->row_polys;
+    else if (n == "ntt_r16") *value = c->r16;
     else if (n == "ml_jobs") *value = c->ml_jobs;
     else fail(RC_ERR_INVALID_ARGUMENT, "unknown tunable " + n);
   });

@@ -57,17 +57,26 @@ struct LimbMap {
   __host__ __device__ __forceinline__ int prime(int j) const { return j < qcount ? j : L + (j - qcount); }
 };
 
+namespace r16 {
+// passes of the N = 2^16 transforms that take the 16-residues-per-lane form of nttr16.cuh (bits of NttArgs::r16
+// and WidePrimes::r16, tunable "ntt_r16"): 64-bit forward column passes, 64-bit row passes, the tensor's inverse
+// rows, the wide key product's column and row passes, 64-bit inverse column passes
+enum : int { R16_COLS = 1, R16_ROWS = 2, R16_TENSOR = 4, R16_WCOLS = 8, R16_WROWS = 16, R16_ICOLS = 32, R16_ALL = 63 };
+constexpr int R16_DEFAULT = R16_COLS | R16_WCOLS;
+}  // namespace r16
+
 struct NttArgs {
   const PrimeConst* pc;
   const Twiddle* tw_fwd;  // [primes][N]: psi^bitrev(k)
   const Twiddle* tw_inv;  // [primes][N]: psi^-bitrev(k)
   int log_n;
   int n1;    // column-phase size 2^n1; row-phase size 2^(log_n - n1) (tunable "ntt_split" for log N 12..16)
-  int lazy;  // all primes < 2^58: forward butterflies skip the [0,4q) correction
+  int lazy;  // all primes < 2^57: forward butterflies skip the [0,4q) correction (approximate Shoup products)
   int mont_out = 0;  // inverse: scale by N^-1 2^64 instead of N^-1 (inputs are Montgomery products)
   int lazy_inv = 0;  // all primes < 2^55: the inverse column pass runs without reductions
   int col_ctas = 3;  // column passes: CTAs per SM the kernel is compiled for (2 or 3; more registers at 2)
   int row_polys = 16;  // row passes: polynomials per block sharing one twiddle staging (8 or 16)
+  int r16 = r16::R16_DEFAULT;  // N = 2^16 split 2^8 x 2^8: passes in the 16-residues-per-lane form (bits above)
 };
 
 // Negacyclic NTT over `polys` x `limbs` limbs, src -> dst (may alias).
@@ -185,6 +194,8 @@ struct WidePrimes {
   uint32_t first_wait_polls = 1u << 22;
   // uniform batches of more than two jobs per CTA take the persistent key product (tunable "mac_persistent")
   int persistent = 1;
+  // N = 2^16: transform passes in the 16-residues-per-lane form (bits of r16::R16_*)
+  int r16 = r16::R16_DEFAULT;
 };
 // Garner CRT of (S mod w0..w3) to the centred integer S (|S| < A/4), reduced mod
 // each scheme prime t.

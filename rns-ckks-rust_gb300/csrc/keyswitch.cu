@@ -696,15 +696,16 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, JT jt) {
   };
 
   if (fast) {
-    // S F + [S < 0] (q - A F) + sum_k v_k (q - M_k F) + [X_P > P/2] P F + addend (+ the rescale term), each
-    // below 2q or q: at most (8 + 2K) q < 2^64, reduced once by the final Shoup product
+    // S F + [S < 0] (q - A F) + sum_k v_k (q - M_k F) + [X_P > P/2] P F + addend (+ the rescale term): the
+    // CRT's two products and the K conversion terms are approximate Shoup products below 4q, the rest below q:
+    // at most (12 + 4K) q < 2^64, reduced once by the final (exact) Shoup product
     auto lazy_value = [&](int i, const LimbIn& in) -> u64 {
       const u64 q = T(i, FT_Q);
       u64 s = wide_crt_lazy(in.p01, in.p23, f.wt, q, T(i, FT_LO), T(i, FT_LO_S), T(i, FT_C01), T(i, FT_C01_S),
                             T(i, FT_AMOD));
 #pragma unroll
       for (int k = 0; k < KMAX; ++k)
-        if (k < K) s += mul_shoup_lazy(v[k], T(i, FT_N + k), T(i, FT_N + K + k), q);
+        if (k < K) s += mul_shoup_apx(v[k], T(i, FT_N + k), T(i, FT_N + K + k), q);
       if (pneg) s += T(i, FT_PMOD);
       if (add) s += (addneg && in.av) ? q - in.av : in.av;
       return s;

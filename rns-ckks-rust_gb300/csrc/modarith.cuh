@@ -46,14 +46,26 @@ struct PrimeConst {
 
 #ifdef __CUDACC__
 __device__ __forceinline__ u64 mulhi(u64 a, u64 b) { return __umul64hi(a, b); }
+__device__ __forceinline__ uint32_t mulhi32(uint32_t a, uint32_t b) { return __umulhi(a, b); }
 #else
 inline u64 mulhi(u64 a, u64 b) { return (u64)(((unsigned __int128)a * b) >> 64); }
+inline uint32_t mulhi32(uint32_t a, uint32_t b) { return (uint32_t)(((u64)a * b) >> 32); }
 #endif
 
 // a * w mod q lazily: result in [0, 2q) for any a < 2^64 (requires q < 2^63).
 __device__ __forceinline__ u64 mul_shoup_lazy(u64 a, u64 w, u64 ws, u64 q) {
   u64 hi = mulhi(a, ws);
   return a * w - hi * q;
+}
+// a * w mod q in [0, 4q) for any a < 2^64 (q < 2^62).  Shoup's quotient estimated from three of the four
+// 32 x 32-bit partial products of a * ws: a1 s1 whole and the high halves of a1 s0 and a0 s1 (their low halves and
+// a0 s0 dropped).  The estimate is an integer at most P / 2^64 and above P / 2^64 - 3 (P = a ws), so it is at
+// most 2 below the exact floor(P / 2^64) and the remainder is below 2q + 2q.  One 32 x 32 -> 64-bit product and
+// two high halves instead of the exact quotient's three and one.
+__device__ __forceinline__ u64 mul_shoup_apx(u64 a, u64 w, u64 ws, u64 q) {
+  const uint32_t a0 = (uint32_t)a, a1 = (uint32_t)(a >> 32), s0 = (uint32_t)ws, s1 = (uint32_t)(ws >> 32);
+  const u64 qh = (u64)a1 * s1 + mulhi32(a1, s0) + mulhi32(a0, s1);
+  return a * w - qh * q;
 }
 __device__ __forceinline__ u64 reduce_2q(u64 x, u64 q) { return x >= q ? x - q : x; }
 __device__ __forceinline__ u64 reduce_4q(u64 x, u64 q) {

@@ -1,5 +1,6 @@
 // Forward negacyclic NTT over RNS limbs (the kernels are in ntt_kernels.cuh) and the fused tensor pass.
 #include "ntt_kernels.cuh"
+#include "nttr16.cuh"
 
 namespace rc {
 
@@ -100,6 +101,49 @@ void fwd_fast(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys,
 
 // the inverse column pass, in place (lazy for primes below 2^55)
 
+// N = 2^16: the 16-residue passes (nttr16.cuh), each pass taken when its bit of NttArgs::r16 is set and its
+// polynomials are 16-byte aligned (the passes read and write natural order, so they mix with the others)
+template <bool LAZY>
+bool r16_fwd_cols(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
+                  cudaStream_t s) {
+  if (!r16::applies(a, r16::R16_COLS) || !r16::aligned(src, polys) || !r16::aligned(dst, polys)) return false;
+  const int nt = 16 * limbs * polys;
+  r16::smem_optin<k16_cols<LAZY, true>, r16::COL_SMEM>();
+  ProfScope p("ntt_fwd_cols", s);
+  k16_cols<LAZY, true><<<r16::col_grid(nt), 256, r16::COL_SMEM, s>>>(a, src, dst, map, limbs, nt);
+  return true;
+}
+template <bool LAZY>
+bool r16_fwd_rows(const NttArgs& a, const PtrTab& data, int polys, int limbs, LimbMap map, cudaStream_t s) {
+  if (!r16::applies(a, r16::R16_ROWS) || !r16::aligned(data, polys)) return false;
+  ProfScope p("ntt_fwd_rows", s);
+  with_rp(a.row_polys, [&](auto rp) {
+    k16_rows<LAZY, true, rp.value>
+        <<<dim3(256 / (2 * r16::RW), limbs, (polys + rp.value - 1) / rp.value), 32 * r16::RW, 0, s>>>(a, data, data, map,
+                                                                                                   polys);
+  });
+  return true;
+}
+template <bool LAZY>
+bool r16_forward(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
+                 cudaStream_t s) {
+  if (a.log_n != 16 || a.n1 != 8) return false;
+  if (!r16_fwd_cols<LAZY>(a, src, dst, polys, limbs, map, s)) {
+    ProfScope p("ntt_fwd_cols", s);
+    with_cc(a.col_ctas, [&](auto cc) {
+      k_cols_f<8, 8, LAZY, true, cc.value><<<dim3(256 / ColTile<8>::COLS, limbs, polys), 256, 0, s>>>(a, src, dst, map);
+    });
+  }
+  if (!r16_fwd_rows<LAZY>(a, dst, polys, limbs, map, s)) {
+    ProfScope p("ntt_fwd_rows", s);
+    with_rp(a.row_polys, [&](auto rp) {
+      dim3 g2(256 / (ROW_WARPS * core::Geo<8>::SUBS), limbs, (polys + rp.value - 1) / rp.value);
+      k_rows_f<8, 8, LAZY, true, rp.value><<<g2, 32 * ROW_WARPS, 0, s>>>(a, dst, dst, map, polys);
+    });
+  }
+  return true;
+}
+
 template <bool LAZY>
 bool fwd_dispatch(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
                   cudaStream_t s) {
@@ -114,6 +158,9 @@ bool fwd_dispatch(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int po
 
 bool ntt_forward_cols(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
                       cudaStream_t s) {
+  if (a.lazy ? r16_fwd_cols<true>(a, src, dst, polys, limbs, map, s)
+             : r16_fwd_cols<false>(a, src, dst, polys, limbs, map, s))
+    return true;
   return with_split(a.log_n, a.n1, [&](auto m1, auto m2) {
     constexpr int A = m1.value, B = m2.value;
     dim3 g1((1 << B) / ColTile<A>::COLS, limbs, polys);
@@ -128,6 +175,9 @@ bool ntt_forward_cols(const NttArgs& a, const PtrTab& src, const PtrTab& dst, in
 void ntt_forward(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
                  cudaStream_t s) {
   if (polys <= 0 || limbs <= 0) return;
+  if (a.r16 && (a.lazy ? r16_forward<true>(a, src, dst, polys, limbs, map, s)
+                       : r16_forward<false>(a, src, dst, polys, limbs, map, s)))
+    return;
   if (a.lazy ? fwd_dispatch<true>(a, src, dst, polys, limbs, map, s)
              : fwd_dispatch<false>(a, src, dst, polys, limbs, map, s))
     return;

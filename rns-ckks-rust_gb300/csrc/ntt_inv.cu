@@ -1,6 +1,7 @@
 // Inverse negacyclic NTT over RNS limbs (the kernels are in ntt_kernels.cuh), the tensor products fused into
 // the inverse row pass, and the inverse column pass alone.
 #include "ntt_kernels.cuh"
+#include "nttr16.cuh"
 
 namespace rc {
 
@@ -186,6 +187,42 @@ void tensor_inv_rows_fast(const NttArgs& a, const PtrTab& in4, const PtrTab& out
 }
 
 
+// N = 2^16: the 16-residue passes (nttr16.cuh), each pass taken when its bit of NttArgs::r16 is set and its
+// polynomials are 16-byte aligned
+bool r16_inv_cols(const NttArgs& a, const PtrTab& data, int polys, int limbs, LimbMap map, cudaStream_t s) {
+  if (!r16::applies(a, r16::R16_ICOLS) || !r16::aligned(data, polys)) return false;
+  const int nt = 16 * limbs * polys;
+  ProfScope p("ntt_inv_cols", s);
+  if (a.lazy_inv) {
+    r16::smem_optin<k16_cols<true, false>, r16::COL_SMEM>();
+    k16_cols<true, false><<<r16::col_grid(nt), 256, r16::COL_SMEM, s>>>(a, data, data, map, limbs, nt);
+  } else {
+    r16::smem_optin<k16_cols<false, false>, r16::COL_SMEM>();
+    k16_cols<false, false><<<r16::col_grid(nt), 256, r16::COL_SMEM, s>>>(a, data, data, map, limbs, nt);
+  }
+  return true;
+}
+bool r16_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
+                 cudaStream_t s) {
+  if (!a.r16 || a.log_n != 16 || a.n1 != 8) return false;
+  if (r16::applies(a, r16::R16_ROWS) && r16::aligned(src, polys) && r16::aligned(dst, polys)) {
+    ProfScope p("ntt_inv_rows", s);
+    with_rp(a.row_polys, [&](auto rp) {
+      k16_rows<false, false, rp.value>
+          <<<dim3(256 / (2 * r16::RW), limbs, (polys + rp.value - 1) / rp.value), 32 * r16::RW, 0, s>>>(a, src, dst, map,
+                                                                                                     polys);
+    });
+  } else {
+    ProfScope p("ntt_inv_rows", s);
+    with_rp(a.row_polys, [&](auto rp) {
+      dim3 g2(256 / (ROW_WARPS * core::Geo<8>::SUBS), limbs, (polys + rp.value - 1) / rp.value);
+      k_rows_f<8, 8, false, false, rp.value><<<g2, 32 * ROW_WARPS, 0, s>>>(a, src, dst, map, polys);
+    });
+  }
+  if (!r16_inv_cols(a, dst, polys, limbs, map, s)) inv_cols_fast<8, 8>(a, dst, polys, limbs, map, s);
+  return true;
+}
+
 // calls f(integral_constant<M1>, integral_constant<M2>) for the fast path's four-step split of 2^log_n
 // points with a column phase of 2^n1 (both phases 2^6..2^8); false when there is none
 
@@ -201,6 +238,7 @@ bool inv_dispatch(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int po
 void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys, int limbs, LimbMap map,
                  cudaStream_t s) {
   if (polys <= 0 || limbs <= 0) return;
+  if (r16_inverse(a, src, dst, polys, limbs, map, s)) return;
   if (inv_dispatch(a, src, dst, polys, limbs, map, s)) return;
   const int N = 1 << a.log_n, N1 = 1 << a.n1, N2 = N >> a.n1;
   const int COLS = cols_per_cta(N2), ROWS = rows_per_cta(N1, N2);
@@ -218,6 +256,13 @@ void ntt_inverse(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int pol
 
 bool tensor_inverse_rows(const NttArgs& a, const PtrTab& in4, const PtrTab& out3, int jobs, int limbs, LimbMap map,
                          cudaStream_t s) {
+  if (r16::applies(a, r16::R16_TENSOR) && r16::aligned(in4, 4 * jobs) && r16::aligned(out3, 3 * jobs)) {
+    ProfScope p("tensor_inv_rows", s);
+    k16_tensor_inv_rows<TENSOR_ROW_JOBS>
+        <<<dim3(256 / (2 * r16::RW), limbs, (jobs + TENSOR_ROW_JOBS - 1) / TENSOR_ROW_JOBS), 32 * r16::RW, 0, s>>>(a, in4, out3, map,
+                                                                                                jobs);
+    return true;
+  }
   return with_split(a.log_n, a.n1, [&](auto m1, auto m2) {
     tensor_inv_rows_fast<m1.value, m2.value>(a, in4, out3, jobs, limbs, map, s);
   });
@@ -225,6 +270,7 @@ bool tensor_inverse_rows(const NttArgs& a, const PtrTab& in4, const PtrTab& out3
 
 
 bool ntt_inverse_cols(const NttArgs& a, const PtrTab& data, int polys, int limbs, LimbMap map, cudaStream_t s) {
+  if (r16_inv_cols(a, data, polys, limbs, map, s)) return true;
   return with_split(a.log_n, a.n1, [&](auto m1, auto m2) {
     inv_cols_fast<m1.value, m2.value>(a, data, polys, limbs, map, s);
   });

@@ -45,7 +45,7 @@ struct ColTile {
   static constexpr int COLS = (8 * core::Geo<M>::SUBS) > 16 ? 8 * core::Geo<M>::SUBS : 16;
 };
 
-// x < 33q (lazy) or < 4q -> [0, q)
+// x < 65q (lazy) or < 4q -> [0, q)
 template <bool LAZY>
 __device__ __forceinline__ u64 reduce_out(u64 x, const PrimeConst& c) {
   if (LAZY) {

@@ -151,13 +151,13 @@ __device__ __forceinline__ int swz(int r) {
   return r ^ h;
 }
 
-// Cooley-Tukey butterflies of one group.  LAZY: inputs are not reduced (values
-// grow by < 2q per stage; valid while they stay below 2^64), otherwise Harvey's
-// [0, 4q) invariant.
+// Cooley-Tukey butterflies of one group.  LAZY: inputs are not reduced and the twiddle products take the
+// approximate Shoup quotient (values grow by < 4q per stage; valid while they stay below 2^64: (4 log N + 1) q,
+// primes below 2^57), otherwise Harvey's [0, 4q) invariant with exact Shoup products.
 template <int M, int GI, bool LAZY>
 __device__ __forceinline__ void fwd_group(u64 (&v)[8], int l, const Twiddle* __restrict__ tw, u64 q) {
   constexpr int S0 = Grp<M, GI>::S0, G = Grp<M, GI>::G;
-  const u64 two_q = q << 1;
+  const u64 two_q = q << 1, off = LAZY ? q << 2 : two_q;
 #pragma unroll
   for (int j = 0; j < G; ++j) {
     const int s = S0 + j;
@@ -169,9 +169,9 @@ __device__ __forceinline__ void fwd_group(u64 (&v)[8], int l, const Twiddle* __r
       const Twiddle w = tw[(1 << s) + (r >> (M - s))];
       u64 x = v[k];
       if (!LAZY) x = x >= two_q ? x - two_q : x;
-      const u64 t = mul_shoup_lazy(v[k | (1 << b)], w.w, w.ws, q);
+      const u64 t = LAZY ? mul_shoup_apx(v[k | (1 << b)], w.w, w.ws, q) : mul_shoup_lazy(v[k | (1 << b)], w.w, w.ws, q);
       v[k] = x + t;
-      v[k | (1 << b)] = x - t + two_q;
+      v[k | (1 << b)] = x - t + off;
     }
   }
 }
@@ -183,10 +183,12 @@ __host__ __device__ constexpr int inv_done() {
   else return 0;
 }
 
-// Gentleman-Sande butterflies of one group, stages in decreasing order; values
-// stay in [0, 2q).  LAZYI (inputs of the sub-transform below 2q): no reductions; after c stages of the
-// sub-transform values are below 2^(c+1) q, so the difference path adds that bound as its offset and its
-// Shoup product restarts below 2q; valid while 2^(M+1) q < 2^64, and the caller reduces the outputs.
+// Gentleman-Sande butterflies of one group, stages in decreasing order; values stay in [0, 2q) (exact Shoup
+// products: an approximate one would need a conditional subtraction more, which measured slower).  LAZYI
+// (inputs of the sub-transform below 2q): no reductions, approximate Shoup products (below 4q); after c stages
+// of the sub-transform values are below 2^(c+1) q (a product, below 4q, stays within that from c = 1 on), so
+// the difference path adds that bound as its offset; valid while 2^(M+1) q < 2^64, and the caller reduces the
+// outputs.
 template <int M, int GI, bool LAZYI = false>
 __device__ __forceinline__ void inv_group(u64 (&v)[8], int l, const Twiddle* __restrict__ tw, u64 q) {
   constexpr int S0 = Grp<M, GI>::S0, G = Grp<M, GI>::G;
@@ -204,7 +206,7 @@ __device__ __forceinline__ void inv_group(u64 (&v)[8], int l, const Twiddle* __r
         const Twiddle w = tw[(1 << s) + (r >> (M - s))];
         const u64 x = v[k], y = v[k | (1 << b)];
         v[k] = x + y;
-        v[k | (1 << b)] = mul_shoup_lazy(x - y + (q << (c + 1)), w.w, w.ws, q);
+        v[k | (1 << b)] = mul_shoup_apx(x - y + (q << (c + 1)), w.w, w.ws, q);
       }
     }
   } else {

@@ -23,6 +23,7 @@
 #include "kernels.cuh"
 #include "nttcore.cuh"
 #include "wide.cuh"
+#include "nttr16.cuh"
 
 namespace rc {
 namespace {
@@ -763,12 +764,27 @@ template <int M1, int M2, int SRC, bool TILED, class DM>
 void w_forward(const WidePrimes& w, const void* src, uint2* work, uint2* dtt, int polys, const DM& dm,
                cudaStream_t s) {
   constexpr int N1 = 1 << M1, N2 = 1 << M2;
+  // N = 2^16: the 16-residue passes (nttr16.cuh) on 16-byte aligned buffers
+  const bool n16 = M1 == 8 && M2 == 8 && r16::aligned(src) && r16::aligned(work) && (!TILED || r16::aligned(dtt));
+  const bool cols16 = n16 && (w.r16 & r16::R16_WCOLS), rows16 = n16 && (w.r16 & r16::R16_WROWS);
   for (int p0 = 0; p0 < polys; p0 += 65535) {
     const int cnt = polys - p0 < 65535 ? polys - p0 : 65535;
-    k_w_cols_fwd<M1, M2, SRC><<<dim3(N2 / WColTile<M1>::COLS, 2, cnt), 256, 0, s>>>(w, src, work, p0);
-    k_w_rows_fwd<M1, M2, TILED, DM><<<dim3(N1 / (W_ROW_WARPS * core::Geo<M2>::SUBS), 2,
-                                           (cnt + W_ROW_POLYS - 1) / W_ROW_POLYS),
-                                      32 * W_ROW_WARPS, 0, s>>>(w, work, dtt, p0, cnt, dm);
+    if (cols16) {
+      const int nt = 16 * 2 * cnt;
+      r16::smem_optin<k16_w_cols_fwd<SRC>, r16::COL_SMEM>();
+      k16_w_cols_fwd<SRC><<<r16::col_grid(nt), 256, r16::COL_SMEM, s>>>(w, src, work, p0, nt);
+    } else {
+      k_w_cols_fwd<M1, M2, SRC><<<dim3(N2 / WColTile<M1>::COLS, 2, cnt), 256, 0, s>>>(w, src, work, p0);
+    }
+    if (rows16) {
+      k16_w_rows_fwd<TILED, DM, W_ROW_POLYS>
+          <<<dim3(256 / (2 * r16::RW), 2, (cnt + W_ROW_POLYS - 1) / W_ROW_POLYS), 32 * r16::RW, 0, s>>>(w, work, dtt, p0,
+                                                                                                     cnt, dm);
+    } else {
+      k_w_rows_fwd<M1, M2, TILED, DM><<<dim3(N1 / (W_ROW_WARPS * core::Geo<M2>::SUBS), 2,
+                                             (cnt + W_ROW_POLYS - 1) / W_ROW_POLYS),
+                                        32 * W_ROW_WARPS, 0, s>>>(w, work, dtt, p0, cnt, dm);
+    }
   }
 }
 
@@ -791,13 +807,24 @@ void w_inverse(const WidePrimes& w, uint2* data, int polys, cudaStream_t s) {
   for (int p0 = 0; p0 < polys; p0 += 65535) {
     const int cnt = polys - p0 < 65535 ? polys - p0 : 65535;
     uint2* d = data + (size_t)p0 * 2 * (N1 * N2);
-    {
+    // N = 2^16: the 16-residue passes (nttr16.cuh) where their bits of WidePrimes::r16 are set
+    const bool n16 = M1 == 8 && M2 == 8 && r16::aligned(d);
+    if (n16 && (w.r16 & r16::R16_WROWS)) {
+      ProfScope p("wide_inv_rows", s);
+      k16_w_rows_inv<W_ROW_POLYS>
+          <<<dim3(256 / (2 * r16::RW), 2, (cnt + W_ROW_POLYS - 1) / W_ROW_POLYS), 32 * r16::RW, 0, s>>>(w, d, cnt);
+    } else {
       ProfScope p("wide_inv_rows", s);
       k_w_rows_inv<M1, M2><<<dim3(N1 / (W_ROW_WARPS * core::Geo<M2>::SUBS), 2,
                                   (cnt + W_ROW_POLYS - 1) / W_ROW_POLYS),
                              32 * W_ROW_WARPS, 0, s>>>(w, d, cnt);
     }
-    {
+    if (n16 && (w.r16 & r16::R16_WCOLS)) {
+      const int nt = 16 * 2 * cnt;
+      r16::smem_optin<k16_w_cols_inv<>, r16::COL_SMEM>();
+      ProfScope p("wide_inv_cols", s);
+      k16_w_cols_inv<><<<r16::col_grid(nt), 256, r16::COL_SMEM, s>>>(w, d, nt);
+    } else {
       ProfScope p("wide_inv_cols", s);
       k_w_cols_inv<M1, M2><<<dim3(N2 / WColTile<M1>::COLS, 2, cnt), 256, 0, s>>>(w, d);
     }

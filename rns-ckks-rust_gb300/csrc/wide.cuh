@@ -42,8 +42,9 @@ __device__ __forceinline__ u64 wide_crt_mod_c(uint2 p01, uint2 p23, const WideTa
   return r;
 }
 
-// wide_crt_mod_c before its reduction, for a caller that sums further lazy terms: a value below 5q congruent
-// to S * F mod q, where namod = (q - (A F mod q)) mod q is what a negative S adds
+// wide_crt_mod_c before its reduction, for a caller that sums further lazy terms: a value below 9q congruent
+// to S * F mod q (its two 64-bit products are approximate Shoup products, below 4q each), where
+// namod = (q - (A F mod q)) mod q is what a negative S adds
 __device__ __forceinline__ u64 wide_crt_lazy(uint2 p01, uint2 p23, const WideTab& W, u64 q, u64 lo_w, u64 lo_ws,
                                             u64 c01, u64 c01_s, u64 namod) {
   const uint32_t w1 = W.w[1], w2 = W.w[2], w3 = W.w[3];
@@ -56,7 +57,7 @@ __device__ __forceinline__ u64 wide_crt_lazy(uint2 p01, uint2 p23, const WideTab
   const uint32_t v3 = mul_shoup32(sub32(b, fold32(v2, w3), w3), W.g23, W.g23s, w3);
   const u64 lo = (u64)v0 + (u64)W.w[0] * v1;
   const u64 hi = (u64)v2 + (u64)w2 * v3;
-  u64 r = mul_shoup_lazy(lo, lo_w, lo_ws, q) + mul_shoup_lazy(hi, c01, c01_s, q);
+  u64 r = mul_shoup_apx(lo, lo_w, lo_ws, q) + mul_shoup_apx(hi, c01, c01_s, q);
   return v3 >= W.half3 ? r + namod : r;
 }
 

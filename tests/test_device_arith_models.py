@@ -5,7 +5,10 @@ exact arithmetic (CPU only).
   2^-31 below its value, so floor(sum) is exact or one low (the kernel's correction handles one);
 * the BSGS inner sums' split products: x = x1 2^26 + x0, three 32x32->64 products per term summed in 64-bit
   columns, recombined and reduced once, equal sum(x y) mod q for primes below 2^52 and up to 16 terms;
-* the lazy finalize's negated-constant Shoup companions: floor((q - w) 2^64 / q) = 2^64 - 1 - floor(w 2^64 / q).
+* the lazy finalize's negated-constant Shoup companions: floor((q - w) 2^64 / q) = 2^64 - 1 - floor(w 2^64 / q);
+* the transforms' approximate Shoup product (mul_shoup_apx): the quotient from three of the four 32-bit partial
+  products, remainder in [0, 4q); the unreduced forward pass it feeds stays below (4 log N + 1) q < 2^64 for
+  primes below 2^57, and the unreduced inverse column pass keeps its 2^(c+1) q bounds.
 """
 import random
 
@@ -107,12 +110,66 @@ def _shoup_lazy(x, w, q):
     return (x * w - ((x * ws) >> 64) * q) & M64
 
 
+def _shoup_apx(x, w, q):
+    """The kernels' mul_shoup_apx: x w - qh q mod 2^64 with qh = a1 s1 + hi32(a1 s0) + hi32(a0 s1), where
+    (a1, a0) and (s1, s0) are the 32-bit halves of x and floor(w 2^64 / q)."""
+    ws = (w << 64) // q
+    a0, a1, s0, s1 = x & 0xFFFFFFFF, x >> 32, ws & 0xFFFFFFFF, ws >> 32
+    qh = (a1 * s1 + ((a1 * s0) >> 32) + ((a0 * s1) >> 32)) & M64
+    return (x * w - qh * q) & M64
+
+
+@pytest.mark.parametrize("bits", [30, 41, 50, 56, 61])
+def test_approximate_shoup_product_is_below_4q_and_congruent(bits):
+    rng = random.Random(bits * 3)
+    for q in _primes(bits, 2):
+        for _ in range(3000):
+            w = rng.randrange(q)
+            for x in (rng.randrange(1 << 64), M64, rng.randrange(q), (1 << 64) - rng.randrange(1, 1 << 32)):
+                r = _shoup_apx(x, w, q)
+                assert r < 4 * q and r % q == x * w % q, (q, w, x)
+
+
+@pytest.mark.parametrize("bits", [50, 56])
+def test_lazy_forward_transform_with_approximate_products_stays_below_2_64(bits):
+    """The unreduced Cooley-Tukey forward transform (both four-step passes of N = 2^16, 16 stages) with
+    approximate Shoup products: x' = x + t, y' = x - t + 4q, t < 4q, so values grow by < 4q per stage from
+    inputs below q; modelled on one butterfly chain per stage with adversarial x and t, and on a 2^8-point
+    sub-transform for the congruence."""
+    q = _primes(bits, 1)[0]
+    assert q < 1 << 57
+    bound = q  # worst case per stage: x at its bound, t = 4q - 1
+    for _ in range(16):
+        bound = bound + 4 * q
+        assert bound < 1 << 64
+    assert bound == 65 * q
+    rng = random.Random(bits)
+    M = 8
+    tw = {(s, j): rng.randrange(1, q) for s in range(M) for j in range(1 << s)}
+    vals = [q - 1 if i % 3 else rng.randrange(q) for i in range(1 << M)]
+    ref = list(vals)
+    for s in range(M):
+        t = (1 << M) >> (s + 1)
+        for blk in range(0, 1 << M, 2 * t):
+            for i in range(blk, blk + t):
+                w = tw[(s, i >> (M - s))]
+                x, y = vals[i], vals[i + t]
+                p = _shoup_apx(y, w, q)
+                assert p < 4 * q
+                vals[i], vals[i + t] = x + p, x - p + 4 * q
+                assert vals[i] < (1 + 4 * (s + 1)) * q and vals[i + t] < (1 + 4 * (s + 1)) * q
+                rx, ry = ref[i], ref[i + t]
+                ref[i], ref[i + t] = (rx + ry * w) % q, (rx - ry * w) % q
+    assert [v % q for v in vals] == ref
+
+
 @pytest.mark.parametrize("bits", [50, 54])
 def test_lazy_inverse_pass_stays_below_2_64_and_matches_the_reduced_pass(bits):
     """The unreduced Gentleman-Sande pass of the inverse column phase (primes below 2^55, M = 8 stages,
     inputs below 2q): the sum path's bound doubles per stage, the difference path adds 2^(c+1) q before its
-    Shoup product; every intermediate stays below 2^64 and every output is congruent to the reduced pass's,
-    here on a 256-point sub-transform with random twiddles and adversarial (all 2q - 1) inputs."""
+    approximate Shoup product (below 4q, within the 2^(c+1) q bound from the second stage on); every
+    intermediate stays below 2^64 and every output is congruent to the reduced pass's, here on a 256-point
+    sub-transform with random twiddles and adversarial (all 2q - 1) inputs."""
     rng = random.Random(bits)
     q = _primes(bits, 1)[0]
     assert q < 1 << 55
@@ -129,8 +186,8 @@ def test_lazy_inverse_pass_stays_below_2_64_and_matches_the_reduced_pass(bits):
                     assert x < (2 << c) * q and y < (2 << c) * q
                     d = x - y + (q << (c + 1))
                     assert 0 <= d < 1 << 64 and x + y < 1 << 64
-                    lazy[i], lazy[i + t] = x + y, _shoup_lazy(d, w, q)
-                    assert lazy[i + t] < 2 * q
+                    lazy[i], lazy[i + t] = x + y, _shoup_apx(d, w, q)
+                    assert lazy[i + t] < 4 * q
                     rx, ry = ref[i], ref[i + t]
                     ref[i], ref[i + t] = (rx + ry) % q, (rx - ry) * w % q
         assert all(v < (2 << M) * q for v in lazy)
