@@ -344,6 +344,18 @@ int rc_mult_relinearized_batch_host(rc_context* ctx, uint32_t count, const uint6
                                     const uint64_t* const* rhs, const int32_t* levels, const int32_t* scale_bits,
                                     const rc_ksk* const* keys, uint64_t* const* out, int32_t* out_scale_bits,
                                     void* stream);
+/* The same batch without waiting for it (context/ops.rs:124-133 per job, as above): returns once the copies
+ * and kernels are enqueued, so a caller streaming batches overlaps one batch's copies with the previous one's
+ * arithmetic.  out_scale_bits is filled before the call returns; the residues reach `out` later: after
+ * rc_host_join(ctx, stream) and a synchronisation of `stream` (e.g. cudaStreamSynchronize) every earlier
+ * asynchronous batch of that stream has its results in `out`, and only then may the caller change or free
+ * the `lhs`/`rhs` host buffers or read `out`.  Host buffers should be pinned (page-locked) memory. */
+int rc_mult_relinearized_batch_host_async(rc_context* ctx, uint32_t count, const uint64_t* const* lhs,
+                                          const uint64_t* const* rhs, const int32_t* levels,
+                                          const int32_t* scale_bits, const rc_ksk* const* keys,
+                                          uint64_t* const* out, int32_t* out_scale_bits, void* stream);
+/* Orders later work on `stream` after every asynchronous host-buffer batch issued on it (no host wait). */
+int rc_host_join(rc_context* ctx, void* stream);
 
 /* ---- host FP64 helpers (src/rns/encoding.rs, src/math/canonical_embedding.rs) ---- */
 /* encode_integer_coeffs + poly_from_bigint_coeffs: encoding.rs:9-31,

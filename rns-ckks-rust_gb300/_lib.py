@@ -125,6 +125,11 @@ SIGNATURES = [
                                                        ctypes.POINTER(_i32), ctypes.POINTER(_i32),
                                                        ctypes.POINTER(_vp), ctypes.POINTER(_vp),
                                                        ctypes.POINTER(_i32), _vp]),
+    ("rc_mult_relinearized_batch_host_async", ctypes.c_int, [_vp, _u32, ctypes.POINTER(_vp), ctypes.POINTER(_vp),
+                                                             ctypes.POINTER(_i32), ctypes.POINTER(_i32),
+                                                             ctypes.POINTER(_vp), ctypes.POINTER(_vp),
+                                                             ctypes.POINTER(_i32), _vp]),
+    ("rc_host_join", ctypes.c_int, [_vp, _vp]),
     ("rc_encode", ctypes.c_int, [_vp, _vp, _i32, _u32, _vp]),
     ("rc_decode", ctypes.c_int, [_vp, _vp, _i32, _u32, _vp]),
     ("rc_encode_device", ctypes.c_int, [_vp, _vp, _u32, _i32, _u32, _vp, _vp]),

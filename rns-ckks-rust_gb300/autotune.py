@@ -27,6 +27,9 @@ DEVICE_CANDIDATES: Dict[str, Sequence[int]] = {"ks_jobs": (8, 16, 32, 64), "mac_
 # have 2^6..2^8 points, so at N = 2^16 only 8 x 8 exists); and the key product's form for job groups (one CTA
 # per tile, or persistent CTAs taking (tile, limb) units with double-buffered digit tiles)
 SHAPE_CANDIDATES: Dict[str, Sequence[int]] = {"col_ctas": (2, 3), "row_polys": (8, 16), "mac_persistent": (0, 1)}
+# N = 2^16 only: the passes in the 16-residues-per-lane form (bits of "ntt_r16": 1 forward 64-bit columns, 8 the
+# key product's dual-prime columns; 0 none)
+R16_CANDIDATES: Sequence[int] = (9, 0)
 
 
 def split_candidates(log_n: int) -> List[int]:
@@ -86,7 +89,7 @@ def choose(trials: Iterable[dict]) -> dict:
 
 def _valid(ctx, name: str, value: int) -> bool:
     if name == "lazy_ntt" and value:
-        return all(q < (1 << 58) for q in ctx.q_moduli + ctx.p_moduli)
+        return all(q < (1 << 57) for q in ctx.q_moduli + ctx.p_moduli)
     return True
 
 
@@ -158,6 +161,8 @@ def tune_mult_relinearized(ctx, lhs, rhs, keys, outs, reps: int = 3, cache: Opti
     splits = split_candidates(ctx.params.poly_degree.bit_length() - 1)
     if len(splits) > 1:
         space["ntt_split"] = splits
+    if ctx.params.poly_degree == 1 << 16:  # which passes take the 16-residues-per-lane form (default, none)
+        space["ntt_r16"] = R16_CANDIDATES
     shapes = tune(ctx, "mult_relinearized_batch_shapes", run, lhs[0].level, n, space, reps, cache, use_cache)
     return {"choice": dict(launch["choice"], **shapes["choice"]), "ms": shapes["ms"],
             "cached": launch["cached"] and shapes["cached"], "trials": launch.get("trials", []),

@@ -45,6 +45,11 @@ cudaEvent_t HostPipe::event() {
 
 HostPipe::~HostPipe() {
   for (cudaEvent_t e : events) cudaEventDestroy(e);
+  for (int i = 0; i < 4; ++i) {
+    if (consumed[i]) cudaEventDestroy(consumed[i]);
+    if (drained[i]) cudaEventDestroy(drained[i]);
+  }
+  if (last) cudaEventDestroy(last);
   for (cudaStream_t st : {in, comp, out, comp2})
     if (st) cudaStreamDestroy(st);
 }
@@ -2203,6 +2208,17 @@ static cudaEvent_t host_phased_group(rc_context* c, HostPipe* hp, uint32_t j0, u
     hp->slot[sl].reset();
     hp->slot[sl].reset(new DevBuf(stage));
   }
+  if (!hp->consumed[sl]) {
+    cuda_check(cudaEventCreateWithFlags(&hp->consumed[sl], cudaEventDisableTiming), "cudaEventCreate");
+    cuda_check(cudaEventCreateWithFlags(&hp->drained[sl], cudaEventDisableTiming), "cudaEventCreate");
+  }
+  // an earlier call's work on this slot: its inputs read before new copies in, its outputs copied out before
+  // new results
+  if (hp->used[sl]) {
+    cuda_check(cudaStreamWaitEvent(hp->in, hp->consumed[sl], 0), "wait");
+    cuda_check(cudaStreamWaitEvent(cs, hp->drained[sl], 0), "wait");
+  }
+  hp->used[sl] = true;
   uint64_t* in_dev = (uint64_t*)hp->slot[sl]->p;
   uint64_t* out_dev = in_dev + (size_t)J * 4 * pl;
   const size_t tbytes = tensor_ws_bytes(c, chunk, limbs);
@@ -2247,6 +2263,7 @@ static cudaEvent_t host_phased_group(rc_context* c, HostPipe* hp, uint32_t j0, u
     tensor_core(c, Lp, Rp, Q, limbs, tscr, cs);
     wide_ks_prepare(c, w, jobs, b0, n, 0, cs);
   }
+  cuda_check(cudaEventRecord(hp->consumed[sl], cs), "cudaEventRecord");  // the slot's inputs are read
   wide_ks_mac(c, w, jobs, cs);
   const int drop = floor_log2(c->mod[limbs - 1]);
   for (int k = 0; k < nchunks; ++k) {
@@ -2265,6 +2282,7 @@ static cudaEvent_t host_phased_group(rc_context* c, HostPipe* hp, uint32_t j0, u
       }
     }
   }
+  cuda_check(cudaEventRecord(hp->drained[sl], hp->out), "cudaEventRecord");
   cudaEvent_t fin = hp->event();
   cuda_check(cudaEventRecord(fin, hp->out), "cudaEventRecord");
   return fin;
@@ -2281,7 +2299,7 @@ static cudaEvent_t host_phased_group(rc_context* c, HostPipe* hp, uint32_t j0, u
 static bool mult_relin_host_phased(rc_context* c, HostPipe* hp, uint32_t count, const uint64_t* const* lhs,
                                    const uint64_t* const* rhs, const int32_t* levels, const int32_t* scale_bits,
                                    const rc_ksk* const* keys, uint64_t* const* out, int32_t* out_scale_bits,
-                                   cudaStream_t s, int chunk, int groups) {
+                                   cudaStream_t s, int chunk, int groups, bool async) {
   const int level = levels[0];
   if (count > (uint32_t)c->ks_jobs) return false;
   for (uint32_t i = 0; i < count; ++i)
@@ -2307,13 +2325,21 @@ static bool mult_relin_host_phased(rc_context* c, HostPipe* hp, uint32_t count, 
   for (cudaStream_t st : {hp->in, hp->comp, hp->out, hp->comp2})
     cuda_check(cudaStreamWaitEvent(st, start, 0), "cudaStreamWaitEvent");
   const uint32_t split = groups == 2 ? (count + 1) / 2 : count;
+  const int set = 2 * hp->ring;  // staging slots of this call (alternating sets, see HostPipe)
+  hp->ring ^= 1;
   cudaEvent_t fin = host_phased_group(c, hp, 0, split, lhs, rhs, levels, scale_bits, keys, out, out_scale_bits,
-                                      hp->comp, 0, chunk, K, D);
+                                      hp->comp, set, chunk, K, D);
   if (split < count)
     fin = host_phased_group(c, hp, split, count, lhs, rhs, levels, scale_bits, keys, out, out_scale_bits, hp->comp2,
-                            1, chunk, K, D);
-  cuda_check(cudaStreamWaitEvent(s, fin, 0), "wait");  // the copies out are in order on hp->out
+                            set + 1, chunk, K, D);
+  cuda_check(cudaEventRecord(hp->last, hp->out), "cudaEventRecord");  // the copies out are in order on hp->out
+  if (async) {
+    hp->pending = true;
+    return true;
+  }
+  cuda_check(cudaStreamWaitEvent(s, fin, 0), "wait");
   cuda_check(cudaStreamSynchronize(hp->out), "cudaStreamSynchronize");
+  hp->pending = false;  // the copies out of earlier asynchronous calls precede these on hp->out
   return true;
 }
 
@@ -2321,33 +2347,40 @@ static bool mult_relin_host_phased(rc_context* c, HostPipe* hp, uint32_t count, 
 // on two streams, compute, copy out) with two device staging slots, so that transfers overlap the
 // arithmetic.  The whole call is ordered after earlier work on `stream` and returns when the results are
 // in host memory.
-extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, const uint64_t* const* lhs,
-                                               const uint64_t* const* rhs, const int32_t* levels,
-                                               const int32_t* scale_bits, const rc_ksk* const* keys,
-                                               uint64_t* const* out, int32_t* out_scale_bits, void* stream) {
-  return guarded("rc_mult_relinearized_batch_host", [&] {
+// the host pipeline of caller stream s (created on first use)
+static HostPipe* host_pipe(rc_context* c, cudaStream_t s) {
+  std::lock_guard<std::mutex> lk(c->mu);
+  auto& p = c->pipes[s];
+  if (!p) {
+    p.reset(new HostPipe());
+    for (cudaStream_t* st : {&p->in, &p->comp, &p->out, &p->comp2})
+      cuda_check(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking), "cudaStreamCreate");
+    cuda_check(cudaEventCreateWithFlags(&p->last, cudaEventDisableTiming), "cudaEventCreate");
+  }
+  return p.get();
+}
+
+// The host-buffer batch (see rc_mult_relinearized_batch_host); async: return once enqueued (phased form).
+static void mult_relin_batch_host(rc_context* c, uint32_t count, const uint64_t* const* lhs,
+                                  const uint64_t* const* rhs, const int32_t* levels, const int32_t* scale_bits,
+                                  const rc_ksk* const* keys, uint64_t* const* out, int32_t* out_scale_bits,
+                                  cudaStream_t s, bool async) {
     require(c && lhs && rhs && levels && scale_bits && keys && out, "arguments must not be null");
-    cudaStream_t s = S(stream);
     for (uint32_t i = 0; i < count; ++i)
       require(levels[i] >= 1 && levels[i] < c->L, "ciphertext level context must exist");
     if (count == 0) return;
-    HostPipe* hp;
-    {
-      std::lock_guard<std::mutex> lk(c->mu);
-      auto& p = c->pipes[s];
-      if (!p) {
-        p.reset(new HostPipe());
-        for (cudaStream_t* st : {&p->in, &p->comp, &p->out, &p->comp2})
-          cuda_check(cudaStreamCreateWithFlags(st, cudaStreamNonBlocking), "cudaStreamCreate");
-      }
-      hp = p.get();
-    }
+    HostPipe* hp = host_pipe(c, s);
     hp->next = 0;
     int chunk = c->host_chunk;  // jobs per pipeline stage
     if (const char* e = getenv("RNSCKKS_HOST_CHUNK")) chunk = std::max(1, atoi(e));
     if (c->host_phased && mult_relin_host_phased(c, hp, count, lhs, rhs, levels, scale_bits, keys, out,
-                                                 out_scale_bits, s, chunk, c->host_phased))
+                                                 out_scale_bits, s, chunk, c->host_phased, async))
       return;
+    // the staged form below is synchronous: earlier asynchronous calls finish first
+    if (hp->pending) {
+      cuda_check(cudaStreamSynchronize(hp->out), "cudaStreamSynchronize");
+      hp->pending = false;
+    }
     const std::vector<uint32_t> bounds = stage_bounds(count, (uint32_t)chunk, (uint32_t)c->host_edge);
     const uint32_t nchunks = (uint32_t)bounds.size() - 1;
     auto in_elems = [&](uint32_t i) { return (size_t)2 * (levels[i] + 1) * c->N; };
@@ -2414,10 +2447,46 @@ extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, co
       cuda_check(cudaEventRecord(out_done[k], hp->out), "cudaEventRecord");
     }
     // later work on the caller's stream is ordered after the whole call
+    cuda_check(cudaEventRecord(hp->last, hp->out), "cudaEventRecord");
     cuda_check(cudaStreamWaitEvent(s, out_done[nchunks - 1], 0), "wait");
     cuda_check(cudaStreamSynchronize(hp->out), "cudaStreamSynchronize");
+}
+
+extern "C" int rc_mult_relinearized_batch_host(rc_context* c, uint32_t count, const uint64_t* const* lhs,
+                                               const uint64_t* const* rhs, const int32_t* levels,
+                                               const int32_t* scale_bits, const rc_ksk* const* keys,
+                                               uint64_t* const* out, int32_t* out_scale_bits, void* stream) {
+  return guarded("rc_mult_relinearized_batch_host", [&] {
+    mult_relin_batch_host(c, count, lhs, rhs, levels, scale_bits, keys, out, out_scale_bits, S(stream), false);
   });
 }
+
+extern "C" int rc_mult_relinearized_batch_host_async(rc_context* c, uint32_t count, const uint64_t* const* lhs,
+                                                     const uint64_t* const* rhs, const int32_t* levels,
+                                                     const int32_t* scale_bits, const rc_ksk* const* keys,
+                                                     uint64_t* const* out, int32_t* out_scale_bits, void* stream) {
+  OpRange op_range("rc_mult_relinearized_batch_host_async");
+  return guarded("rc_mult_relinearized_batch_host_async", [&] {
+    mult_relin_batch_host(c, count, lhs, rhs, levels, scale_bits, keys, out, out_scale_bits, S(stream), true);
+  });
+}
+
+extern "C" int rc_host_join(rc_context* c, void* stream) {
+  return guarded("rc_host_join", [&] {
+    require(c != nullptr, "context must not be null");
+    const cudaStream_t s = S(stream);
+    HostPipe* hp = nullptr;
+    {
+      std::lock_guard<std::mutex> lk(c->mu);
+      auto it = c->pipes.find(s);
+      if (it != c->pipes.end()) hp = it->second.get();
+    }
+    if (!hp) return;
+    cuda_check(cudaStreamWaitEvent(s, hp->last, 0), "wait");
+    hp->pending = false;
+  });
+}
+
 
 extern "C" int rc_mult_relinearized_host(rc_context* c, const uint64_t* lhs, const uint64_t* rhs, int32_t level,
                                          int32_t scale_bits, const rc_ksk* key, uint64_t* out,

@@ -95,9 +95,20 @@ struct Workspace {
 // through one copy stream in job order: the host link serves one copy at a time, so a second input stream
 // would only delay the first chunk's other operand.  Consecutive chunks compute on alternating streams
 // (comp, comp2), so one chunk's kernels fill the SMs the other's leave idle.
+//
+// Asynchronous calls (rc_mult_relinearized_batch_host_async) return once their work is enqueued, so the next
+// call's copies in run while the previous call computes.  The phased form then takes its staging slots from
+// alternating sets (`ring`), each slot guarded by two persistent events: `consumed` (its inputs were read by
+// the last call that used it) before new copies in, `drained` (its outputs were copied out) before new
+// results; `last` marks the end of the latest call's copies out (rc_host_join).
 struct HostPipe {
   cudaStream_t in = nullptr, comp = nullptr, out = nullptr, comp2 = nullptr;
-  std::unique_ptr<DevBuf> slot[2];
+  std::unique_ptr<DevBuf> slot[4];
+  cudaEvent_t consumed[4] = {}, drained[4] = {};
+  bool used[4] = {};
+  cudaEvent_t last = nullptr;
+  bool pending = false;  // asynchronous work issued since the last join
+  int ring = 0;
   std::vector<cudaEvent_t> events;
   cudaEvent_t event();  // from the pool, created on first use
   size_t next = 0;      // events handed out in the current call

@@ -305,6 +305,52 @@ def test_pipelined_host_batch_equals_device_path(C, pkg):
             assert np.array_equal(outs[i], dev.numpy()) and OSB[i] == dev.scale_bits
 
 
+@pytest.mark.parametrize("phased", [2, 1, 0])
+def test_async_host_batches_back_to_back_equal_device_path(C, pkg, phased):
+    # several asynchronous batches in a row (their copies and kernels overlap; the staging slots alternate),
+    # then one join and a synchronisation: every batch's results equal the device path's; the last batch
+    # reuses the first batch's output buffers after the join.  phased 0 (the staged form) runs synchronously.
+    import ctypes
+    params = pkg.params.hybrid_params(12, 5, 2, 50)
+    ctx = C.RnsCkksContext(params)
+    C.call("rc_tune_set", ctx.handle, b"host_phased", phased)
+    C.call("rc_tune_set", ctx.handle, b"host_chunk", 2)
+    n, q = params.poly_degree, params.q_moduli()
+    rng = np.random.default_rng(46 + phased)
+    lv, count = 4, 7
+    key = ctx.upload_keyswitch_key(_random_key(rng, params, lv + 1, True)[0], lv, 2)
+    P = lambda arrs: (ctypes.c_void_p * count)(*[x.ctypes.data for x in arrs])
+    LV = (ctypes.c_int32 * count)(*([lv] * count))
+    SB = (ctypes.c_int32 * count)(*([40] * count))
+    K = (ctypes.c_void_p * count)(*([key.handle] * count))
+    def pinned(a):  # page-locked host memory, as the entry point expects (numpy view of a pinned tensor)
+        return torch.from_numpy(np.ascontiguousarray(a).view(np.int64)).pin_memory().numpy().view(np.uint64)
+
+    batches = []
+    for _ in range(4):
+        A = [pinned(rand_ct(rng, q, n)) for _ in range(count)]
+        B = [pinned(rand_ct(rng, q, n)) for _ in range(count)]
+        outs = [pinned(np.zeros((2, lv, n), dtype=np.uint64)) for _ in range(count)]
+        batches.append((A, B, outs, (ctypes.c_int32 * count)()))
+    s = C._stream()
+    for A, B, outs, OSB in batches[:3]:
+        C.call("rc_mult_relinearized_batch_host_async", ctx.handle, count, P(A), P(B), LV, SB, K, P(outs), OSB, s)
+    C.call("rc_host_join", ctx.handle, s)
+    torch.cuda.synchronize()
+    A3, B3, _, OSB3 = batches[3]
+    first = [o.copy() for o in batches[0][2]]
+    C.call("rc_mult_relinearized_batch_host_async", ctx.handle, count, P(A3), P(B3), LV, SB, K, P(batches[0][2]),
+           OSB3, s)
+    C.call("rc_host_join", ctx.handle, s)
+    torch.cuda.synchronize()
+    results = [(batches[0][0], batches[0][1], first, batches[0][3])] + batches[1:3] + [(A3, B3, batches[0][2], OSB3)]
+    for A, B, outs, OSB in results:
+        for i in range(count):
+            dev = ctx.mult_relinearized(C.RnsCiphertext(C.to_device(A[i]), 40), C.RnsCiphertext(C.to_device(B[i]), 40),
+                                        key)
+            assert np.array_equal(outs[i], dev.numpy()) and OSB[i] == dev.scale_bits
+
+
 def test_precondition_errors_carry_reference_messages(C, pkg):
     params = pkg.params.hybrid_params(11, 4, 2, 50)
     ctx = C.RnsCkksContext(params)
