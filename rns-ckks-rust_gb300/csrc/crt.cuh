@@ -133,9 +133,12 @@ __device__ __forceinline__ u64 centred_crt(const CrtSmem& t, int W, int limbs, c
 #pragma unroll
   for (int w = 0; w < 2 * WM + 2; ++w) X32[w] = 0;
   u64 fsum = 0;  // sum of y_l / q_l in units of 2^-31 (each term within 3 units below its value)
+  // limb l + 1's residue is requested before limb l's multiply-add chains, so its latency is covered
+  u64 rnext = limbs > 0 ? in[0] : 0;
   for (int l = 0; l < limbs; ++l) {
     const u64 q = t.q[l];
-    u64 r = in[(u64)l * N];
+    u64 r = rnext;
+    if (l + 1 < limbs) rnext = in[(u64)(l + 1) * N];
     if (neg && r) r = q - r;
     const u64 y = mul_shoup(r, t.hinv[l], t.hinv_s[l], q);
     const u64 fx = t.invq[l];

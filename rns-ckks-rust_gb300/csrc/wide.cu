@@ -370,6 +370,11 @@ __device__ __forceinline__ void w_mac_unit(const KT& kt, const uint2* __restrict
   u64 a0[BC], a1[BC], c0[BC], c1[BC];
 #pragma unroll
   for (int b = 0; b < BC; ++b) a0[b] = a1[b] = c0[b] = c1[b] = 0;
+  // this lane's digit word of job b at the current group's first digit, advanced once per group of W_PF digits,
+  // so that the loads inside a group take compile-time offsets (no per-job address arithmetic per digit)
+  const uint2* dj[BC];
+#pragma unroll
+  for (int b = 0; b < BC; ++b) dj[b] = dsm + (size_t)b * run + slane;
   // each lane copies and later reads only its own words, so the waits need no warp barrier
 #pragma unroll
   for (int u = 0; u < W_PF; ++u) {
@@ -379,6 +384,7 @@ __device__ __forceinline__ void w_mac_unit(const KT& kt, const uint2* __restrict
     }
     cp_async_commit();
   }
+  const uint2* kn = kp + (size_t)W_PF * 64;  // the key words of the digit W_PF past the group's first
 #pragma unroll 1
   for (int i0 = 0; i0 < D; i0 += W_PF) {
     if (FOLD && i0 > 0 && (i0 & 63) == 0) {  // fold: the next 64 terms then stay below 2^64
@@ -396,10 +402,9 @@ __device__ __forceinline__ void w_mac_unit(const KT& kt, const uint2* __restrict
       if (i < D) {
         cp_async_wait<W_PF - 1>();  // digit i's group has landed
         const uint2 k0 = ring[64 * u], k1 = ring[64 * u + 32];
-        const uint2* dp = dsm + i * 32 + slane;
 #pragma unroll
         for (int b = 0; b < BC; ++b) {
-          const uint2 d = dp[b * run];
+          const uint2 d = dj[b][32 * u];
           a0[b] += (u64)d.x * k0.x;
           a1[b] += (u64)d.y * k0.y;
           c0[b] += (u64)d.x * k1.x;
@@ -407,12 +412,15 @@ __device__ __forceinline__ void w_mac_unit(const KT& kt, const uint2* __restrict
         }
         // refill the slot with digit i + W_PF once its words have been used
         if (i + W_PF < D) {
-          cp_async8(rs + 8u * (64 * u), kp + (size_t)(i + W_PF) * 64);
-          cp_async8(rs + 8u * (64 * u + 32), kp + (size_t)(i + W_PF) * 64 + 32);
+          cp_async8(rs + 8u * (64 * u), kn + 64 * u);
+          cp_async8(rs + 8u * (64 * u + 32), kn + 64 * u + 32);
         }
         cp_async_commit();
       }
     }
+#pragma unroll
+    for (int b = 0; b < BC; ++b) dj[b] += 32 * W_PF;
+    kn += (size_t)W_PF * 64;
   }
   cp_async_wait<0>();
   const int x = xb * 32 + lane;
