@@ -551,12 +551,15 @@ struct MlFin {
   __device__ __forceinline__ u64* dst(int job, int comp) const { return out.p[2 * job + comp]; }
 };
 
-template <class JT>
+// KC: the aux limb count K when it is a compile-time constant (0, 1, 2), -1 for any K up to KMAX (loops over the
+// aux limbs then run to KMAX under predicates)
+template <class JT, int KC>
 __global__ void k_finalize(FinalizeArgs f, const u64* acc, JT jt) {
+  constexpr int KB = KC > 0 ? KC : (KC == 0 ? 1 : KMAX);  // bound of the loops over aux limbs and words of P
   extern __shared__ u64 tab[];  // [lq + K][FT_N + 2K]
   const u64 N = 1ull << f.log_n;
   const int comp = blockIdx.y & 1, job = blockIdx.y >> 1;
-  const int lq = jt.limbs(job), K = f.K;
+  const int lq = jt.limbs(job), K = KC >= 0 ? KC : f.K;
   const LimbMap fmap{lq, f.L};
   const int st = ft_stride(K);
   // with the wide CRT and an aux basis, a Q limb's constants carry the factor P^-1 (`fold`): the CRT then
@@ -632,16 +635,16 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, JT jt) {
   }
 
   // Garner over the aux primes: mixed-radix digits v_k of [x]_P
-  u64 v[KMAX];
+  u64 v[KB];
   bool pneg = false;
   if (K > 0) {
 #pragma unroll
-    for (int k = 0; k < KMAX; ++k) {
+    for (int k = 0; k < KB; ++k) {
       if (k < K) {
         const u64 pq = T(lq + k, FT_Q), pone = T(lq + k, FT_ONE_S);
         u64 val = accv(lq + k);
 #pragma unroll
-        for (int t = 0; t < KMAX; ++t) {
+        for (int t = 0; t < KB; ++t) {
           if (t < k) {
             const u64 vr = v[t] < pq ? v[t] : mul_shoup(v[t], 1, pone, pq);
             val = sub_mod(val, vr, pq);
@@ -652,16 +655,16 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, JT jt) {
       }
     }
     // X_P = sum v_k M_k by Horner (K words max); compare with floor(P/2)
-    u64 X[KMAX];
+    u64 X[KB];
 #pragma unroll
-    for (int w = 0; w < KMAX; ++w) X[w] = 0;
+    for (int w = 0; w < KB; ++w) X[w] = 0;
 #pragma unroll
-    for (int k = KMAX - 1; k >= 0; --k) {
+    for (int k = KB - 1; k >= 0; --k) {
       if (k < K) {
         const u64 pk = T(lq + k, FT_Q);
         u64 carry = v[k];
 #pragma unroll
-        for (int w = 0; w < KMAX; ++w) {
+        for (int w = 0; w < KB; ++w) {
           U128 p = mul_wide(X[w], pk);
           u64 lo = p.lo + carry;
           carry = p.hi + (lo < carry ? 1ull : 0ull);
@@ -671,9 +674,9 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, JT jt) {
     }
     int res = 0;
 #pragma unroll
-    for (int w = KMAX - 1; w >= 0; --w) {
+    for (int w = KB - 1; w >= 0; --w) {
       if (res == 0) {
-        u64 h = w < f.md.KW ? f.md.halfP[w < KMAX ? w : 0] : 0ull;
+        u64 h = w < f.md.KW ? f.md.halfP[w < KB ? w : 0] : 0ull;
         if (X[w] > h) res = 1;
         else if (X[w] < h) res = -1;
       }
@@ -704,7 +707,7 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, JT jt) {
       u64 s = wide_crt_lazy(in.p01, in.p23, f.wt, q, T(i, FT_LO), T(i, FT_LO_S), T(i, FT_C01), T(i, FT_C01_S),
                             T(i, FT_AMOD));
 #pragma unroll
-      for (int k = 0; k < KMAX; ++k)
+      for (int k = 0; k < KB; ++k)
         if (k < K) s += mul_shoup_apx(v[k], T(i, FT_N + k), T(i, FT_N + K + k), q);
       if (pneg) s += T(i, FT_PMOD);
       if (add) s += (addneg && in.av) ? q - in.av : in.av;
@@ -751,7 +754,7 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, JT jt) {
     if (K > 0) {
       u64 conv = 0;
 #pragma unroll
-      for (int k = 0; k < KMAX; ++k) {
+      for (int k = 0; k < KB; ++k) {
         if (k < K) conv = add_mod(conv, mul_shoup(v[k], T(i, FT_N + k), T(i, FT_N + K + k), q), q);
       }
       if (pneg) conv = sub_mod(conv, T(i, FT_PMOD), q);
@@ -778,7 +781,7 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, JT jt) {
       // no reduction mod q_i
       u64 conv = 0;
 #pragma unroll
-      for (int k = 0; k < KMAX; ++k) {
+      for (int k = 0; k < KB; ++k) {
         if (k < K) conv = add_mod(conv, mul_shoup(v[k], T(i, FT_N + k), T(i, FT_N + K + k), q), q);
       }
       if (pneg) conv = sub_mod(conv, T(i, FT_PMOD), q);
@@ -958,7 +961,12 @@ void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const
   ProfScope p("finalize", s);
   const size_t smem = (size_t)(f.qlimbs + f.K) * ft_stride(f.K) * sizeof(u64);
   const UniFin jt{addend, out, f.qlimbs, f.K};
-  k_finalize<UniFin><<<g, threads, smem, s>>>(f, acc, jt);
+  switch (f.K) {
+    case 0: k_finalize<UniFin, 0><<<g, threads, smem, s>>>(f, acc, jt); break;
+    case 1: k_finalize<UniFin, 1><<<g, threads, smem, s>>>(f, acc, jt); break;
+    case 2: k_finalize<UniFin, 2><<<g, threads, smem, s>>>(f, acc, jt); break;
+    default: k_finalize<UniFin, -1><<<g, threads, smem, s>>>(f, acc, jt);
+  }
 }
 
 void finalize_ml(const FinalizeArgs& f, const MlTab& t, const u64* acc, const MlPtrTab& addend, const MlPtrTab& out,
@@ -973,7 +981,12 @@ void finalize_ml(const FinalizeArgs& f, const MlTab& t, const u64* acc, const Ml
   ProfScope p("finalize", s);
   const size_t smem = (size_t)(max_lq + f.K) * ft_stride(f.K) * sizeof(u64);
   const MlFin jt{t, addend, out};
-  k_finalize<MlFin><<<g, threads, smem, s>>>(f, acc, jt);
+  switch (f.K) {
+    case 0: k_finalize<MlFin, 0><<<g, threads, smem, s>>>(f, acc, jt); break;
+    case 1: k_finalize<MlFin, 1><<<g, threads, smem, s>>>(f, acc, jt); break;
+    case 2: k_finalize<MlFin, 2><<<g, threads, smem, s>>>(f, acc, jt); break;
+    default: k_finalize<MlFin, -1><<<g, threads, smem, s>>>(f, acc, jt);
+  }
 }
 
 void key_to_device_form(const NttArgs& a, const PrimeConst* pc, const u64* src, u64* dst, int digits, int limbs,
