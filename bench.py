@@ -515,6 +515,31 @@ def run_gpu(args):
         dist.destroy_process_group()
 
 
+def ntt_profile(C, ctx, params, seed, batch=16):
+    """A small fixed case for profilers of the transform passes: one forward + inverse round trip of `batch`
+    polynomials x 24 limbs (uniform residues, 201 MB at batch 16: above L2) with the N = 2^16 passes in the
+    16-residues-per-lane form (tunable ntt_r16 = 63) and one with the eight-residue passes (0), NVTX ranges on
+    (range names "rc_ntt_forward" / "rc_ntt_inverse").  Returns whether both round trips restored the input."""
+    import torch
+    n, q = params.poly_degree, params.q_moduli()
+    limbs = len(q)
+    gen = torch.Generator(device="cuda")
+    gen.manual_seed(seed)
+    mod = torch.tensor(q, dtype=torch.int64, device="cuda").view(1, limbs, 1)
+    data = torch.randint(0, 1 << 62, (batch, limbs, n), device="cuda", generator=gen) % mod
+    orig = data.clone()
+    s = ctypes.c_void_p(torch.cuda.current_stream().cuda_stream)
+    lib = C.lib()
+    lib.rc_profile_enable(2)  # NVTX ranges
+    for r16 in (63, 0):
+        C.call("rc_tune_set", ctx.handle, b"ntt_r16", r16)
+        C.call("rc_ntt_forward", ctx.handle, ctypes.c_void_p(data.data_ptr()), batch, limbs, 0, s)
+        C.call("rc_ntt_inverse", ctx.handle, ctypes.c_void_p(data.data_ptr()), batch, limbs, 0, s)
+    torch.cuda.synchronize()
+    lib.rc_profile_enable(0)
+    return {"batch": batch, "limbs": limbs, "round_trips_exact": bool(torch.equal(data, orig))}
+
+
 def hmult_profile(C, ctx, params, seed, batch=8, reps=3):
     """A small fixed case for profilers: `batch` pairs of uniform-residue ciphertexts at the top of the
     benchmark chain and a uniform-residue relinearization key (no key generation launches), `reps` calls of
@@ -1152,7 +1177,7 @@ def main():
     ap.add_argument("--no-extra", action="store_true",
                     help="skip the NTT microbenchmark and the mixed-level relinearization batch")
     ap.add_argument("--extra-only", choices=["bsgs_matvec", "bootstrap", "mixed_level_relin", "ntt_microbench",
-                                             "hmult_profile", "dnum_relin"],
+                                             "hmult_profile", "ntt_profile", "dnum_relin"],
                     help="run one of the extra workloads alone (a profiling case) and print its JSON object")
     ap.add_argument("--extra-batch", type=int, default=None, help="batch of --extra-only (default: its own)")
     args = ap.parse_args()
@@ -1165,14 +1190,15 @@ def main():
                 ctx = C.RnsCkksContext(params)
                 if f is mixed_level_relin:
                     return f(C, ctx, params, load_oracle(), seed, **({"count": kw["batch"]} if kw else {}))
-                if f is hmult_profile:
+                if f in (hmult_profile, ntt_profile):
                     return f(C, ctx, params, seed, **kw)
                 return f(C, ctx, params, peaks()[0], seed)
             return run
         fn = {"bsgs_matvec": bsgs_matvec_bench, "bootstrap": bootstrap_bench, "dnum_relin": dnum_relin_bench,
               "mixed_level_relin": on_bench_context(mixed_level_relin),
               "ntt_microbench": on_bench_context(ntt_microbench),
-              "hmult_profile": on_bench_context(hmult_profile)}[args.extra_only]
+              "hmult_profile": on_bench_context(hmult_profile),
+              "ntt_profile": on_bench_context(ntt_profile)}[args.extra_only]
         kw = {} if args.extra_batch is None else {"batch": args.extra_batch}
         print(json.dumps({args.extra_only: fn(pkg, C, args.seed, **kw)}), flush=True)
         return
