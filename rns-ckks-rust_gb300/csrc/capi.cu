@@ -1194,6 +1194,9 @@ extern "C" int rc_tune_set(rc_context* c, const char* name, int32_t value) {
     } else if (n == "col_ctas") {
       require(value == 2 || value == 3, "col_ctas must be 2 or 3");
       c->col_ctas = value;
+    } else if (n == "tensor_jobs") {
+      require(value >= 1 && value <= 16, "tensor_jobs must be in 1..16");
+      c->tensor_jobs = value;
     } else if (n == "row_polys") {
       require(value == 8 || value == 16, "row_polys must be 8 or 16");
       c->row_polys = value;
@@ -1239,6 +1242,7 @@ extern "C" int rc_tune_get(const rc_context* c, const char* name, int32_t* value
     else if (n == "ntt_split") *value = c->n1;
     else if (n == "col_ctas") *value = c->col_ctas;
     else if (n == "row_polys") *value = c->row_polys;
+    else if (n == "tensor_jobs") *value = c->tensor_jobs;
     else if (n == "ntt_r16") *value = c->r16;
     else if (n == "ml_jobs") *value = c->ml_jobs;
     else fail(RC_ERR_INVALID_ARGUMENT, "unknown tunable " + n);

@@ -159,6 +159,7 @@ struct rc_context {
   int ml_jobs = rc::ML_MAXJ;  // jobs per mixed-level chunk (each chunk one launch per pass)
   int col_ctas = 3;           // 64-bit column passes: CTAs per SM (2 or 3)
   int row_polys = 16;         // 64-bit row passes: polynomials per block (8 or 16)
+  int tensor_jobs = 4;        // tensor + inverse row pass: jobs per block (1..16)
   int r16 = rc::r16::R16_DEFAULT;  // N = 2^16: passes in the 16-residues-per-lane form (bits; also wp.r16)
 
   rc::NttArgs ntt() const {
@@ -172,6 +173,7 @@ struct rc_context {
     a.lazy_inv = lazy_inv ? 1 : 0;
     a.col_ctas = col_ctas;
     a.row_polys = row_polys;
+    a.tensor_jobs = tensor_jobs;
     a.r16 = r16;
     return a;
   }

@@ -76,6 +76,7 @@ struct NttArgs {
   int lazy_inv = 0;  // all primes < 2^55: the inverse column pass runs without reductions
   int col_ctas = 3;  // column passes: CTAs per SM the kernel is compiled for (2 or 3; more registers at 2)
   int row_polys = 16;  // row passes: polynomials per block sharing one twiddle staging (8 or 16)
+  int tensor_jobs = 4;  // tensor + inverse row pass: jobs per block sharing one twiddle staging (tunable)
   int r16 = r16::R16_DEFAULT;  // N = 2^16 split 2^8 x 2^8: passes in the 16-residues-per-lane form (bits above)
 };
 

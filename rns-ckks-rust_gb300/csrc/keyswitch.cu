@@ -552,8 +552,9 @@ struct MlFin {
 };
 
 // KC: the aux limb count K when it is a compile-time constant (0, 1, 2), -1 for any K up to KMAX (loops over the
-// aux limbs then run to KMAX under predicates)
-template <class JT, int KC>
+// aux limbs then run to KMAX under predicates).  FAST: the lazy wide path (f.wide && f.lazy), so each instance
+// carries only its own path's code
+template <class JT, int KC, bool FAST>
 __global__ void k_finalize(FinalizeArgs f, const u64* acc, JT jt) {
   constexpr int KB = KC > 0 ? KC : (KC == 0 ? 1 : KMAX);  // bound of the loops over aux limbs and words of P
   extern __shared__ u64 tab[];  // [lq + K][FT_N + 2K]
@@ -569,7 +570,7 @@ __global__ void k_finalize(FinalizeArgs f, const u64* acc, JT jt) {
   // lazy wide path: each Q limb's terms are summed unreduced and reduced once, so its subtracted constants
   // are staged negated: q - A F (added when S < 0) and q - M_k F with Shoup companion ~(M_k F)_s (for
   // 0 < w < q, floor((q - w) 2^64 / q) = 2^64 - 1 - floor(w 2^64 / q))
-  const bool fast = f.wide && f.lazy;
+  const bool fast = FAST;  // = f.wide && f.lazy (the launch picks the instance)
   for (int e = threadIdx.x; e < (lq + K) * st; e += blockDim.x) {
     const int i = e / st, fld = e - i * st;
     const int t = fmap.prime(i);
@@ -961,12 +962,16 @@ void finalize(const FinalizeArgs& f, const u64* acc, const PtrTab& addend, const
   ProfScope p("finalize", s);
   const size_t smem = (size_t)(f.qlimbs + f.K) * ft_stride(f.K) * sizeof(u64);
   const UniFin jt{addend, out, f.qlimbs, f.K};
-  switch (f.K) {
-    case 0: k_finalize<UniFin, 0><<<g, threads, smem, s>>>(f, acc, jt); break;
-    case 1: k_finalize<UniFin, 1><<<g, threads, smem, s>>>(f, acc, jt); break;
-    case 2: k_finalize<UniFin, 2><<<g, threads, smem, s>>>(f, acc, jt); break;
-    default: k_finalize<UniFin, -1><<<g, threads, smem, s>>>(f, acc, jt);
-  }
+  auto launch = [&](auto fast) {
+    switch (f.K) {
+      case 0: k_finalize<UniFin, 0, fast.value><<<g, threads, smem, s>>>(f, acc, jt); break;
+      case 1: k_finalize<UniFin, 1, fast.value><<<g, threads, smem, s>>>(f, acc, jt); break;
+      case 2: k_finalize<UniFin, 2, fast.value><<<g, threads, smem, s>>>(f, acc, jt); break;
+      default: k_finalize<UniFin, -1, fast.value><<<g, threads, smem, s>>>(f, acc, jt);
+    }
+  };
+  if (f.wide && f.lazy) launch(std::true_type{});
+  else launch(std::false_type{});
 }
 
 void finalize_ml(const FinalizeArgs& f, const MlTab& t, const u64* acc, const MlPtrTab& addend, const MlPtrTab& out,
@@ -981,12 +986,16 @@ void finalize_ml(const FinalizeArgs& f, const MlTab& t, const u64* acc, const Ml
   ProfScope p("finalize", s);
   const size_t smem = (size_t)(max_lq + f.K) * ft_stride(f.K) * sizeof(u64);
   const MlFin jt{t, addend, out};
-  switch (f.K) {
-    case 0: k_finalize<MlFin, 0><<<g, threads, smem, s>>>(f, acc, jt); break;
-    case 1: k_finalize<MlFin, 1><<<g, threads, smem, s>>>(f, acc, jt); break;
-    case 2: k_finalize<MlFin, 2><<<g, threads, smem, s>>>(f, acc, jt); break;
-    default: k_finalize<MlFin, -1><<<g, threads, smem, s>>>(f, acc, jt);
-  }
+  auto launch = [&](auto fast) {
+    switch (f.K) {
+      case 0: k_finalize<MlFin, 0, fast.value><<<g, threads, smem, s>>>(f, acc, jt); break;
+      case 1: k_finalize<MlFin, 1, fast.value><<<g, threads, smem, s>>>(f, acc, jt); break;
+      case 2: k_finalize<MlFin, 2, fast.value><<<g, threads, smem, s>>>(f, acc, jt); break;
+      default: k_finalize<MlFin, -1, fast.value><<<g, threads, smem, s>>>(f, acc, jt);
+    }
+  };
+  if (f.wide && f.lazy) launch(std::true_type{});
+  else launch(std::false_type{});
 }
 
 void key_to_device_form(const NttArgs& a, const PrimeConst* pc, const u64* src, u64* dst, int digits, int limbs,

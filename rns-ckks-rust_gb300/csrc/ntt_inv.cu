@@ -113,10 +113,9 @@ void inv_fast(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys,
 // The tensor and the inverse row phase in one pass: for each job of the block, d0 = a0 b0, d1 = a0 b1 + a1 b0
 // and d2 = a1 b1 (Montgomery products of the forward transforms in4[4j..4j+3]; the inverse column pass's scale
 // takes out their 2^-64) go straight into the inverse row transform, so the quadratic NTT-domain values never
-// reach HBM.  A block transforms the same rows of TENSOR_ROW_JOBS jobs (three outputs each) with one twiddle
+// reach HBM.  A block transforms the same rows of NttArgs::tensor_jobs jobs (three outputs each) with one twiddle
 // staging.
 
-constexpr int TENSOR_ROW_JOBS = 4;
 
 template <int M1, int M2>
 __global__ __launch_bounds__(32 * ROW_WARPS) void k_tensor_inv_rows(NttArgs a, PtrTab in4, PtrTab out3, LimbMap map,
@@ -128,7 +127,8 @@ __global__ __launch_bounds__(32 * ROW_WARPS) void k_tensor_inv_rows(NttArgs a, P
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int sub = lane / G::LANES, l = lane % G::LANES;
   const int row0 = blockIdx.x * ROWS;
-  const int limb = blockIdx.y, first = blockIdx.z * TENSOR_ROW_JOBS, count = min(TENSOR_ROW_JOBS, jobs - first);
+  const int tj = a.tensor_jobs;
+  const int limb = blockIdx.y, first = blockIdx.z * tj, count = min(tj, jobs - first);
   const int prime = map.prime(limb);
   const PrimeConst& pc = a.pc[prime];
   const Twiddle* twg = a.tw_inv + (size_t)prime * N;
@@ -181,7 +181,7 @@ template <int M1, int M2>
 void tensor_inv_rows_fast(const NttArgs& a, const PtrTab& in4, const PtrTab& out3, int jobs, int limbs, LimbMap map,
                           cudaStream_t s) {
   constexpr int N1 = 1 << M1;
-  dim3 g(N1 / (ROW_WARPS * core::Geo<M2>::SUBS), limbs, (jobs + TENSOR_ROW_JOBS - 1) / TENSOR_ROW_JOBS);
+  dim3 g(N1 / (ROW_WARPS * core::Geo<M2>::SUBS), limbs, (jobs + a.tensor_jobs - 1) / a.tensor_jobs);
   ProfScope p("tensor_inv_rows", s);
   k_tensor_inv_rows<M1, M2><<<g, 32 * ROW_WARPS, 0, s>>>(a, in4, out3, map, jobs);
 }
@@ -258,8 +258,8 @@ bool tensor_inverse_rows(const NttArgs& a, const PtrTab& in4, const PtrTab& out3
                          cudaStream_t s) {
   if (r16::applies(a, r16::R16_TENSOR) && r16::aligned(in4, 4 * jobs) && r16::aligned(out3, 3 * jobs)) {
     ProfScope p("tensor_inv_rows", s);
-    k16_tensor_inv_rows<TENSOR_ROW_JOBS>
-        <<<dim3(256 / (2 * r16::RW), limbs, (jobs + TENSOR_ROW_JOBS - 1) / TENSOR_ROW_JOBS), 32 * r16::RW, 0, s>>>(a, in4, out3, map,
+    k16_tensor_inv_rows<4>
+        <<<dim3(256 / (2 * r16::RW), limbs, (jobs + 4 - 1) / 4), 32 * r16::RW, 0, s>>>(a, in4, out3, map,
                                                                                                 jobs);
     return true;
   }
