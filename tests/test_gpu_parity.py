@@ -388,7 +388,7 @@ def test_encode_decode_matches_oracle(C, pkg, oracle):
     assert np.max(np.abs(back - slots)) <= 1e-6
 
 
-@pytest.mark.parametrize("log_n,limbs,aux", [(12, 5, 2), (13, 4, 0), (14, 6, 2)])
+@pytest.mark.parametrize("log_n,limbs,aux", [(12, 5, 2), (13, 4, 0), (14, 6, 2), (12, 4, 1), (12, 4, 3)])
 def test_wide_and_standard_key_products_agree(C, pkg, oracle, monkeypatch, log_n, limbs, aux):
     """The exact integer key product (two internal primes) and the per-limb
     product give the same residues, equal to the oracle's."""
