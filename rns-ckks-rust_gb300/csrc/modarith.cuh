@@ -116,6 +116,12 @@ __device__ __forceinline__ u64 barrett_reduce(U128 t, const PrimeConst& c) {
 }
 __device__ __forceinline__ u64 mul_mod(u64 a, u64 b, const PrimeConst& c) { return barrett_reduce(mul_wide(a, b), c); }
 
+// Montgomery: t * 2^-64 mod q for t < q * 2^64, before its final conditional subtraction: in [0, 2q)
+__device__ __forceinline__ u64 mont_reduce_lazy(U128 t, const PrimeConst& c) {
+  u64 m = t.lo * c.qinv_neg;
+  U128 mq = mul_wide(m, c.q);
+  return t.hi + mq.hi + (t.lo != 0 ? 1ull : 0ull);
+}
 // Montgomery: t * 2^-64 mod q for t < q * 2^64; result in [0, q).
 __device__ __forceinline__ u64 mont_reduce(U128 t, const PrimeConst& c) {
   u64 m = t.lo * c.qinv_neg;

@@ -111,8 +111,9 @@ void inv_fast(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys,
 }
 
 // The tensor and the inverse row phase in one pass: for each job of the block, d0 = a0 b0, d1 = a0 b1 + a1 b0
-// and d2 = a1 b1 (Montgomery products of the forward transforms in4[4j..4j+3]; the inverse column pass's scale
-// takes out their 2^-64) go straight into the inverse row transform, so the quadratic NTT-domain values never
+// and d2 = a1 b1 (Montgomery products of the forward transforms in4[4j..4j+3], left in [0, 2q) as the inverse
+// butterflies accept; the inverse column pass's scale takes out their 2^-64) go straight into the inverse row
+// transform, so the quadratic NTT-domain values never
 // reach HBM.  A block transforms the same rows of NttArgs::tensor_jobs jobs (three outputs each) with one twiddle
 // staging.
 
@@ -144,11 +145,11 @@ __global__ __launch_bounds__(32 * ROW_WARPS) void k_tensor_inv_rows(NttArgs a, P
     for (int k = 0; k < 8; ++k) {
       const int x = core::last_idx<M2>(l, k);
       const u64 a0 = x0[x], a1 = x1[x], b0 = y0[x], b1 = y1[x];
-      d[0][k] = mont_reduce(mul_wide(a0, b0), pc);
+      d[0][k] = mont_reduce_lazy(mul_wide(a0, b0), pc);
       U128 m = mul_wide(a0, b1);
       add_to(m, mul_wide(a1, b0));
-      d[1][k] = mont_reduce(m, pc);
-      d[2][k] = mont_reduce(mul_wide(a1, b1), pc);
+      d[1][k] = mont_reduce_lazy(m, pc);
+      d[2][k] = mont_reduce_lazy(mul_wide(a1, b1), pc);
     }
   };
   products(first);

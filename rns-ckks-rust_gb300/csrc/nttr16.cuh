@@ -434,8 +434,8 @@ __global__ __launch_bounds__(32 * r16::RW) void k16_rows(NttArgs a, PtrTab src, 
 }
 
 // The tensor and the inverse row phase (as k_tensor_inv_rows): for each job of the block, d0 = a0 b0,
-// d1 = a0 b1 + a1 b0, d2 = a1 b1 (Montgomery products of the forward transforms in4[4j..4j+3]) go straight
-// into the inverse row transform; the inverse column pass with NttArgs::mont_out completes it.
+// d1 = a0 b1 + a1 b0, d2 = a1 b1 (Montgomery products of the forward transforms in4[4j..4j+3], left in [0, 2q))
+// go straight into the inverse row transform; the inverse column pass with NttArgs::mont_out completes it.
 template <int TJ>
 __global__ __launch_bounds__(32 * r16::RW) void k16_tensor_inv_rows(NttArgs a, PtrTab in4, PtrTab out3,
                                                                           LimbMap map, int jobs) {
@@ -476,18 +476,18 @@ __global__ __launch_bounds__(32 * r16::RW) void k16_tensor_inv_rows(NttArgs a, P
           const ulonglong2 y1 = *reinterpret_cast<const ulonglong2*>(y2 + 2 * h);
           U128 m = mul_wide(x.x, y.x);
           add_to(m, mul_wide(x1.x, y1.x));
-          v[2 * h] = mont_reduce(m, pc);
+          v[2 * h] = mont_reduce_lazy(m, pc);
           m = mul_wide(x.y, y.y);
           add_to(m, mul_wide(x1.y, y1.y));
-          v[2 * h + 1] = mont_reduce(m, pc);
+          v[2 * h + 1] = mont_reduce_lazy(m, pc);
         }
       } else {
 #pragma unroll
         for (int h = 0; h < 8; ++h) {
           const ulonglong2 x = *reinterpret_cast<const ulonglong2*>(xp + 2 * h);
           const ulonglong2 y = *reinterpret_cast<const ulonglong2*>(yp + 2 * h);
-          v[2 * h] = mont_reduce(mul_wide(x.x, y.x), pc);
-          v[2 * h + 1] = mont_reduce(mul_wide(x.y, y.y), pc);
+          v[2 * h] = mont_reduce_lazy(mul_wide(x.x, y.x), pc);
+          v[2 * h + 1] = mont_reduce_lazy(mul_wide(x.y, y.y), pc);
         }
       }
       inv_b<false>(v, tw + lam, q);
