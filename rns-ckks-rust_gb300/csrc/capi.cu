@@ -878,6 +878,12 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
         g.w = pwi[e];
         g.ws = shoup_h(g.w, q);
       }
+      // the inverse transform's last stage (its one twiddle, index 1 of the table) times the scale (InvScale)
+      const uint64_t w1 = N > 1 ? twi[(size_t)i * N + 1].w : 1;
+      k.w1n = mulmod_h(w1, k.n_inv, q);
+      k.w1n_s = shoup_h(k.w1n, q);
+      k.w1nr = mulmod_h(w1, k.n_inv_r, q);
+      k.w1nr_s = shoup_h(k.w1nr, q);
     }
     c->pc_buf.reset(new DevBuf(sizeof(PrimeConst) * P));
     c->d_pc = (PrimeConst*)c->pc_buf->p;
@@ -1048,6 +1054,9 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
             pwi[e] = mulmod_h(pwi[e - 1], psi_inv, q);
           }
           const int pair = i >> 1, half = i & 1;
+          // the inverse transform's last stage (its one twiddle, psi^-bitrev(1)) times N^-1 (InvScale2)
+          wp.w1n[i] = (uint32_t)mulmod_h(pwi[bitrev(1, c->log_n)], wp.n_inv[i], q);
+          wp.w1n_s[i] = shoup32(wp.w1n[i], q);
           for (uint64_t kk = 0; kk < N; ++kk) {
             const int e = bitrev((int)kk, c->log_n);
             Tw2& f = tf[(size_t)pair * N + kk];

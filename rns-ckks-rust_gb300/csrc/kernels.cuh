@@ -186,6 +186,7 @@ void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int
 struct WidePrimes {
   uint32_t q[4];
   uint32_t n_inv[4], n_inv_s[4];  // N^-1 mod q and its Shoup companion
+  uint32_t w1n[4], w1n_s[4];      // the inverse transform's stage-0 twiddle times N^-1 (+ Shoup), see InvScale2
   u64 bar[4];                     // floor(2^64 / q): 64-bit -> residue reduction
   const Tw2* tw_fwd;              // [2 pairs][N]: psi^bitrev(k)
   const Tw2* tw_inv;              // [2 pairs][N]: psi^-bitrev(k)

@@ -41,7 +41,21 @@ struct PrimeConst {
   u64 one_s;          // floor(2^64 / q): Shoup companion of 1 (reduces x < 2^64 to [0, 2q))
   u64 mac_chunk64;    // per-term Montgomery values (< 2q each) that sum below 2^64
   u64 n_inv_r, n_inv_r_s;  // N^-1 2^64 mod q (+ Shoup): the inverse transform's scale after Montgomery products
+  // the inverse transform's last stage (global stage 0, one twiddle w1 = psi^-bitrev(1)) times the scale:
+  // w1 N^-1 and w1 N^-1 2^64 mod q (+ Shoup)
+  u64 w1n, w1n_s, w1nr, w1nr_s;
   u64 pad[3];
+};
+
+// The inverse transform's scale folded into its last stage: every butterfly of global stage 0 shares the
+// twiddle w1, so its outputs are (x + y) n and (x - y) (w1 n), canonical, and no separate pass multiplies every
+// output by n (N^-1 or N^-1 2^64): one Shoup product fewer per stage-0 butterfly
+struct InvScale {
+  u64 n, n_s, wn, wn_s;
+};
+// the same for two 29-bit primes (the wide key product's internal primes), 32-bit Shoup companions
+struct InvScale2 {
+  uint32_t n0, n0s, wn0, wn0s, n1, n1s, wn1, wn1s;
 };
 
 #ifdef __CUDACC__

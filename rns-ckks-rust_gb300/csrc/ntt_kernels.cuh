@@ -58,7 +58,8 @@ __device__ __forceinline__ u64 reduce_out(u64 x, const PrimeConst& c) {
 // Column phase: the CTA stages a tile of COLS columns (2^M1 rows each) and the
 // column twiddle table in shared memory; each warp transforms SUBS columns at
 // a time in registers.  LAZY: forward, unreduced butterflies; inverse, butterflies without reductions
-// (inputs below 2q, primes below 2^55), the final N^-1 product reducing every output.
+// (inputs below 2q, primes below 2^55).  Inverse: the N^-1 (or N^-1 2^64) scale is folded into the last stage
+// (InvScale), whose products leave canonical outputs.
 template <int M1, int M2, bool LAZY, bool FWD, int CC>
 __global__ __launch_bounds__(256, CC) void k_cols_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map) {
   using G = core::Geo<M1>;
@@ -70,7 +71,8 @@ __global__ __launch_bounds__(256, CC) void k_cols_f(NttArgs a, PtrTab src, PtrTa
   const int prime = map.prime(limb);
   const PrimeConst& pc = a.pc[prime];
   const u64 q = pc.q;
-  const u64 ninv = a.mont_out ? pc.n_inv_r : pc.n_inv, ninv_s = a.mont_out ? pc.n_inv_r_s : pc.n_inv_s;
+  const InvScale sc = a.mont_out ? InvScale{pc.n_inv_r, pc.n_inv_r_s, pc.w1nr, pc.w1nr_s}
+                                  : InvScale{pc.n_inv, pc.n_inv_s, pc.w1n, pc.w1n_s};
   const u64* in = src.p[poly] + (size_t)limb * N;
   u64* out = dst.p[poly] + (size_t)limb * N;
   // tile and twiddles by asynchronous copies, all in flight together
@@ -101,7 +103,7 @@ __global__ __launch_bounds__(256, CC) void k_cols_f(NttArgs a, PtrTab src, PtrTa
 #pragma unroll
       for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::last_idx<M1>(l, k))];
       __syncwarp();
-      core::inv_sub<M1, LAZY>(v, buf, l, twl, q);
+      core::inv_sub<M1, LAZY, true>(v, buf, l, twl, q, sc);
 #pragma unroll
       for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::first_idx<M1>(l, k))] = v[k];
     }
@@ -112,7 +114,7 @@ __global__ __launch_bounds__(256, CC) void k_cols_f(NttArgs a, PtrTab src, PtrTa
     const int idx = it * 256 + threadIdx.x;
     const int r = idx / COLS, c = idx % COLS;
     const u64 x = tile[c * G::STRIDE + core::swz<M1>(r)];
-    out[(size_t)r * N2 + c0 + c] = FWD ? x : mul_shoup(x, ninv, ninv_s, q);
+    out[(size_t)r * N2 + c0 + c] = x;
   }
 }
 

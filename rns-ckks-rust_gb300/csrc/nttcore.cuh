@@ -189,8 +189,11 @@ __host__ __device__ constexpr int inv_done() {
 // of the sub-transform values are below 2^(c+1) q (a product, below 4q, stays within that from c = 1 on), so
 // the difference path adds that bound as its offset; valid while 2^(M+1) q < 2^64, and the caller reduces the
 // outputs.
-template <int M, int GI, bool LAZYI = false>
-__device__ __forceinline__ void inv_group(u64 (&v)[8], int l, const Twiddle* __restrict__ tw, u64 q) {
+// SC (the column phase of the inverse transform, whose stage 0 is the transform's last): that stage takes the
+// scale (InvScale) and leaves canonical outputs.
+template <int M, int GI, bool LAZYI = false, bool SC = false>
+__device__ __forceinline__ void inv_group(u64 (&v)[8], int l, const Twiddle* __restrict__ tw, u64 q,
+                                          const InvScale& sc = InvScale{}) {
   constexpr int S0 = Grp<M, GI>::S0, G = Grp<M, GI>::G;
   const u64 two_q = q << 1;
   if constexpr (LAZYI) {
@@ -202,9 +205,14 @@ __device__ __forceinline__ void inv_group(u64 (&v)[8], int l, const Twiddle* __r
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
         if (k & (1 << b)) continue;
+        const u64 x = v[k], y = v[k | (1 << b)];
+        if (SC && s == 0) {
+          v[k] = mul_shoup(x + y, sc.n, sc.n_s, q);
+          v[k | (1 << b)] = mul_shoup(x - y + (q << (c + 1)), sc.wn, sc.wn_s, q);
+          continue;
+        }
         const int r = gidx<M, S0, G>(l, k);
         const Twiddle w = tw[(1 << s) + (r >> (M - s))];
-        const u64 x = v[k], y = v[k | (1 << b)];
         v[k] = x + y;
         v[k | (1 << b)] = mul_shoup_apx(x - y + (q << (c + 1)), w.w, w.ws, q);
       }
@@ -217,9 +225,14 @@ __device__ __forceinline__ void inv_group(u64 (&v)[8], int l, const Twiddle* __r
 #pragma unroll
       for (int k = 0; k < 8; ++k) {
         if (k & (1 << b)) continue;
+        const u64 x = v[k], y = v[k | (1 << b)];
+        if (SC && s == 0) {
+          v[k] = mul_shoup(x + y, sc.n, sc.n_s, q);
+          v[k | (1 << b)] = mul_shoup(x - y + two_q, sc.wn, sc.wn_s, q);
+          continue;
+        }
         const int r = gidx<M, S0, G>(l, k);
         const Twiddle w = tw[(1 << s) + (r >> (M - s))];
-        const u64 x = v[k], y = v[k | (1 << b)];
         u64 u = x + y;
         u = u >= two_q ? u - two_q : u;
         v[k] = u;
@@ -253,16 +266,18 @@ __device__ __forceinline__ void fwd_sub(u64 (&v)[8], u64* buf, int l, const Twid
   }
 }
 
-// full inverse sub-transform: v holds the last group's layout on entry, group 0's on exit
-template <int M, bool LAZYI = false>
-__device__ __forceinline__ void inv_sub(u64 (&v)[8], u64* buf, int l, const Twiddle* tw, u64 q) {
+// full inverse sub-transform: v holds the last group's layout on entry, group 0's on exit; SC: the scale folded
+// into stage 0 (column phase)
+template <int M, bool LAZYI = false, bool SC = false>
+__device__ __forceinline__ void inv_sub(u64 (&v)[8], u64* buf, int l, const Twiddle* tw, u64 q,
+                                        const InvScale& sc = InvScale{}) {
   if constexpr (NGroups<M>::value == 3) {
     inv_group<M, 2, LAZYI>(v, l, tw, q);
     exchange<M, 2, 1>(v, buf, l);
   }
   inv_group<M, 1, LAZYI>(v, l, tw, q);
   exchange<M, 1, 0>(v, buf, l);
-  inv_group<M, 0, LAZYI>(v, l, tw, q);
+  inv_group<M, 0, LAZYI, SC>(v, l, tw, q, sc);
 }
 
 template <int M>
@@ -290,6 +305,11 @@ __device__ __forceinline__ int last_idx(int l, int k) {
 // x * w mod q in [0, 2q) for any 32-bit x
 __device__ __forceinline__ uint32_t mul_shoup32_lazy(uint32_t x, uint32_t w, uint32_t ws, uint32_t q) {
   return x * w - __umulhi(x, ws) * q;
+}
+// x * w mod q in [0, q) for any 32-bit x
+__device__ __forceinline__ uint32_t mul_shoup32c(uint32_t x, uint32_t w, uint32_t ws, uint32_t q) {
+  const uint32_t r = mul_shoup32_lazy(x, w, ws, q);
+  return min(r, r - q);  // r - q wraps above r when r < q
 }
 
 template <int M>
@@ -327,9 +347,9 @@ __device__ __forceinline__ void fwd_group2(uint2 (&v)[8], int l, const Tw2* __re
   }
 }
 
-template <int M, int GI>
+template <int M, int GI, bool SC = false>
 __device__ __forceinline__ void inv_group2(uint2 (&v)[8], int l, const Tw2* __restrict__ tw, uint32_t q0,
-                                           uint32_t q1) {
+                                           uint32_t q1, const InvScale2& sc = InvScale2{}) {
   constexpr int S0 = Grp<M, GI>::S0, G = Grp<M, GI>::G;
   const uint32_t t0 = q0 << 1, t1 = q1 << 1;
 #pragma unroll
@@ -339,9 +359,15 @@ __device__ __forceinline__ void inv_group2(uint2 (&v)[8], int l, const Tw2* __re
 #pragma unroll
     for (int k = 0; k < 8; ++k) {
       if (k & (1 << b)) continue;
+      const uint2 x = v[k], y = v[k | (1 << b)];
+      if (SC && s == 0) {  // the scale folded into the last stage, canonical outputs (see InvScale)
+        v[k] = make_uint2(mul_shoup32c(x.x + y.x, sc.n0, sc.n0s, q0), mul_shoup32c(x.y + y.y, sc.n1, sc.n1s, q1));
+        v[k | (1 << b)] = make_uint2(mul_shoup32c(x.x - y.x + t0, sc.wn0, sc.wn0s, q0),
+                                     mul_shoup32c(x.y - y.y + t1, sc.wn1, sc.wn1s, q1));
+        continue;
+      }
       const int r = gidx<M, S0, G>(l, k);
       const Tw2 w = tw[(1 << s) + (r >> (M - s))];
-      const uint2 x = v[k], y = v[k | (1 << b)];
       uint32_t a0 = x.x + y.x, a1 = x.y + y.y;
       a0 = a0 >= t0 ? a0 - t0 : a0;
       a1 = a1 >= t1 ? a1 - t1 : a1;
@@ -373,15 +399,16 @@ __device__ __forceinline__ void fwd_sub2(uint2 (&v)[8], uint2* buf, int l, const
   }
 }
 
-template <int M>
-__device__ __forceinline__ void inv_sub2(uint2 (&v)[8], uint2* buf, int l, const Tw2* tw, uint32_t q0, uint32_t q1) {
+template <int M, bool SC = false>
+__device__ __forceinline__ void inv_sub2(uint2 (&v)[8], uint2* buf, int l, const Tw2* tw, uint32_t q0, uint32_t q1,
+                                         const InvScale2& sc = InvScale2{}) {
   if constexpr (NGroups<M>::value == 3) {
     inv_group2<M, 2>(v, l, tw, q0, q1);
     exchange2<M, 2, 1>(v, buf, l);
   }
   inv_group2<M, 1>(v, l, tw, q0, q1);
   exchange2<M, 1, 0>(v, buf, l);
-  inv_group2<M, 0>(v, l, tw, q0, q1);
+  inv_group2<M, 0, SC>(v, l, tw, q0, q1, sc);
 }
 
 }  // namespace core

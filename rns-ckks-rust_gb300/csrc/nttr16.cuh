@@ -175,15 +175,23 @@ __device__ __forceinline__ void inv_b(u64 (&v)[16], const Twiddle* __restrict__ 
     }
   }
 }
-// inverse stages 3..0 (layout A)
-template <bool LAZYI>
-__device__ __forceinline__ void inv_a(u64 (&v)[16], const Twiddle* __restrict__ tw, u64 q) {
+// inverse stages 3..0 (layout A); SC: the scale folded into stage 0 (the column phase: global stage 0 is the
+// transform's last, InvScale), canonical outputs
+template <bool LAZYI, bool SC = false>
+__device__ __forceinline__ void inv_a(u64 (&v)[16], const Twiddle* __restrict__ tw, u64 q,
+                                      const InvScale& sc = InvScale{}) {
 #pragma unroll
   for (int s = 3; s >= 0; --s) {
     const int b = 3 - s;
 #pragma unroll
     for (int k = 0; k < 16; ++k) {
       if (k & (1 << b)) continue;
+      if (SC && s == 0) {
+        const u64 x = v[k], y = v[k | (1 << b)];
+        v[k] = mul_shoup(x + y, sc.n, sc.n_s, q);
+        v[k | (1 << b)] = mul_shoup(x - y + (LAZYI ? q << 8 : q << 1), sc.wn, sc.wn_s, q);
+        continue;
+      }
       gs<LAZYI>(v[k], v[k | (1 << b)], tw[(1 << s) + (k >> (4 - s))], q, s);
     }
   }
@@ -239,13 +247,25 @@ __device__ __forceinline__ void inv_b2(uint2 (&v)[16], const Tw2* __restrict__ t
       if (!(k & (1 << b))) gs2(v[k], v[k | (1 << b)], twl[(1 << s) + 16 * (k >> (8 - s))], q0, q1);
   }
 }
-__device__ __forceinline__ void inv_a2(uint2 (&v)[16], const Tw2* __restrict__ tw, uint32_t q0, uint32_t q1) {
+template <bool SC = false>
+__device__ __forceinline__ void inv_a2(uint2 (&v)[16], const Tw2* __restrict__ tw, uint32_t q0, uint32_t q1,
+                                       const InvScale2& sc = InvScale2{}) {
 #pragma unroll
   for (int s = 3; s >= 0; --s) {
     const int b = 3 - s;
 #pragma unroll
-    for (int k = 0; k < 16; ++k)
-      if (!(k & (1 << b))) gs2(v[k], v[k | (1 << b)], tw[(1 << s) + (k >> (4 - s))], q0, q1);
+    for (int k = 0; k < 16; ++k) {
+      if (k & (1 << b)) continue;
+      if (SC && s == 0) {  // the scale folded into the last stage (InvScale2), canonical outputs
+        const uint2 x = v[k], y = v[k | (1 << b)];
+        v[k] = make_uint2(core::mul_shoup32c(x.x + y.x, sc.n0, sc.n0s, q0),
+                          core::mul_shoup32c(x.y + y.y, sc.n1, sc.n1s, q1));
+        v[k | (1 << b)] = make_uint2(core::mul_shoup32c(x.x - y.x + (q0 << 1), sc.wn0, sc.wn0s, q0),
+                                     core::mul_shoup32c(x.y - y.y + (q1 << 1), sc.wn1, sc.wn1s, q1));
+        continue;
+      }
+      gs2(v[k], v[k | (1 << b)], tw[(1 << s) + (k >> (4 - s))], q0, q1);
+    }
   }
 }
 
@@ -318,7 +338,8 @@ namespace {
 // Column phase, persistent: block b takes the tiles (16 columns of one limb of one polynomial) b, b + grid, ...;
 // the next tile's copies are in flight while the current one is transformed (two tile buffers).  Forward: LAZY
 // as in k_cols_f.  Inverse (in place allowed): LAZY = unreduced butterflies (inputs below 2q, primes below
-// 2^55), then the N^-1 (or N^-1 2^64) Shoup product reduces every output to [0, q).
+// 2^55); the N^-1 (or N^-1 2^64) scale is folded into the last stage (InvScale), whose Shoup products reduce
+// every output to [0, q).
 template <bool LAZY, bool FWD>
 __global__ __launch_bounds__(256, 2) void k16_cols(NttArgs a, PtrTab src, PtrTab dst, LimbMap map, int limbs,
                                                    int ntiles) {
@@ -364,10 +385,11 @@ __global__ __launch_bounds__(256, 2) void k16_cols(NttArgs a, PtrTab src, PtrTab
       for (int k = 0; k < 16; ++k) v[k] = pB[TROW * k];
       inv_b<LAZY>(v, tw + lam, q);
       exchange<TROW, TBLK>(v, pB, pA);
-      inv_a<LAZY>(v, tw, q);
-      const u64 ninv = a.mont_out ? pc.n_inv_r : pc.n_inv, ninv_s = a.mont_out ? pc.n_inv_r_s : pc.n_inv_s;
+      const InvScale sc = a.mont_out ? InvScale{pc.n_inv_r, pc.n_inv_r_s, pc.w1nr, pc.w1nr_s}
+                                     : InvScale{pc.n_inv, pc.n_inv_s, pc.w1n, pc.w1n_s};
+      inv_a<LAZY, true>(v, tw, q, sc);
 #pragma unroll
-      for (int k = 0; k < 16; ++k) pA[TBLK * k] = mul_shoup(v[k], ninv, ninv_s, q);
+      for (int k = 0; k < 16; ++k) pA[TBLK * k] = v[k];
     }
     __syncthreads();
     tile_store(dst.p[poly] + (size_t)limb * N + c0, tl, t);
@@ -666,8 +688,8 @@ __global__ __launch_bounds__(32 * r16::RW) void k16_w_rows_inv(WidePrimes w, uin
   }
 }
 
-// Inverse column phase, persistent (as k16_cols), in place on data[poly][pair][N], times N^-1: outputs in
-// [0, q).  (A template so that translation units that do not launch it do not compile it.)
+// Inverse column phase, persistent (as k16_cols), in place on data[poly][pair][N], times N^-1 (folded into the
+// last stage, InvScale2): outputs in [0, q).  (A template so that translation units that do not launch it do not compile it.)
 template <int = 0>
 __global__ __launch_bounds__(256, 2) void k16_w_cols_inv(WidePrimes w, uint2* data, int ntiles) {
   using namespace r16;
@@ -701,12 +723,12 @@ __global__ __launch_bounds__(256, 2) void k16_w_cols_inv(WidePrimes w, uint2* da
     for (int k = 0; k < 16; ++k) v[k] = pB[TROW * k];
     inv_b2(v, tw + lam, q0, q1);
     exchange<TROW, TBLK>(v, pB, pA);
-    inv_a2(v, tw, q0, q1);
-    const uint32_t n0 = pair ? w.n_inv[2] : w.n_inv[0], n0s = pair ? w.n_inv_s[2] : w.n_inv_s[0];
-    const uint32_t n1 = pair ? w.n_inv[3] : w.n_inv[1], n1s = pair ? w.n_inv_s[3] : w.n_inv_s[1];
+    const int e0 = pair ? 2 : 0, e1 = e0 + 1;
+    const InvScale2 sc{w.n_inv[e0], w.n_inv_s[e0], w.w1n[e0], w.w1n_s[e0],
+                       w.n_inv[e1], w.n_inv_s[e1], w.w1n[e1], w.w1n_s[e1]};
+    inv_a2<true>(v, tw, q0, q1, sc);
 #pragma unroll
-    for (int k = 0; k < 16; ++k)
-      pA[TBLK * k] = make_uint2(mul_shoup32(v[k].x, n0, n0s, q0), mul_shoup32(v[k].y, n1, n1s, q1));
+    for (int k = 0; k < 16; ++k) pA[TBLK * k] = v[k];
     __syncthreads();
     tile_store(data + ((size_t)poly * 2 + pair) * N + c0, tl, t);
   }

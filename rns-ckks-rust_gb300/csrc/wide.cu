@@ -257,7 +257,7 @@ __global__ __launch_bounds__(32 * W_ROW_WARPS) void k_w_rows_inv(WidePrimes w, u
   }
 }
 
-// Inverse column phase, in place, times N^-1: outputs in [0, q).
+// Inverse column phase, in place, times N^-1 (folded into the last stage, InvScale2): outputs in [0, q).
 template <int M1, int M2>
 __global__ __launch_bounds__(256, 3) void k_w_cols_inv(WidePrimes w, uint2* data) {
   using G = core::Geo<M1>;
@@ -268,6 +268,8 @@ __global__ __launch_bounds__(256, 3) void k_w_cols_inv(WidePrimes w, uint2* data
   const int pair = blockIdx.y;
   const size_t poly = blockIdx.z;
   const uint32_t q0 = pick(w.q, pair, 0), q1 = pick(w.q, pair, 1);
+  const InvScale2 sc{pick(w.n_inv, pair, 0), pick(w.n_inv_s, pair, 0), pick(w.w1n, pair, 0), pick(w.w1n_s, pair, 0),
+                     pick(w.n_inv, pair, 1), pick(w.n_inv_s, pair, 1), pick(w.w1n, pair, 1), pick(w.w1n_s, pair, 1)};
   uint2* io = data + (poly * 2 + pair) * N;
 #pragma unroll 4
   for (int it = 0; it < N1 * COLS / 256; ++it) {
@@ -288,19 +290,16 @@ __global__ __launch_bounds__(256, 3) void k_w_cols_inv(WidePrimes w, uint2* data
 #pragma unroll
     for (int k = 0; k < 8; ++k) v[k] = buf[core::swz<M1>(core::last_idx<M1>(l, k))];
     __syncwarp();
-    core::inv_sub2<M1>(v, buf, l, twl, q0, q1);
+    core::inv_sub2<M1, true>(v, buf, l, twl, q0, q1, sc);
 #pragma unroll
     for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::first_idx<M1>(l, k))] = v[k];
   }
   __syncthreads();
-  const uint32_t n0 = pick(w.n_inv, pair, 0), n0s = pick(w.n_inv_s, pair, 0);
-  const uint32_t n1 = pick(w.n_inv, pair, 1), n1s = pick(w.n_inv_s, pair, 1);
 #pragma unroll 4
   for (int it = 0; it < N1 * COLS / 256; ++it) {
     const int idx = it * 256 + threadIdx.x;
     const int r = idx / COLS, c = idx % COLS;
-    const uint2 x = tile[c * G::STRIDE + core::swz<M1>(r)];
-    io[(size_t)r * N2 + c0 + c] = make_uint2(mul_shoup32(x.x, n0, n0s, q0), mul_shoup32(x.y, n1, n1s, q1));
+    io[(size_t)r * N2 + c0 + c] = tile[c * G::STRIDE + core::swz<M1>(r)];
   }
 }
 
