@@ -111,6 +111,12 @@ __device__ __forceinline__ void add_to(U128& acc, const U128& x) {
   acc.hi += x.hi + (lo < x.lo ? 1ull : 0ull);
   acc.lo = lo;
 }
+// acc -= x (x <= acc)
+__device__ __forceinline__ void sub_from(U128& acc, const U128& x) {
+  const u64 borrow = acc.lo < x.lo ? 1ull : 0ull;
+  acc.lo -= x.lo;
+  acc.hi -= x.hi + borrow;
+}
 
 // Barrett: t mod q for t < q * 2^64, q < 2^61.  The quotient estimate keeps the
 // middle-word carries, so it is at most 2 below the true quotient.

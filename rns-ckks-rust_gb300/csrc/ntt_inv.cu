@@ -145,11 +145,15 @@ __global__ __launch_bounds__(32 * ROW_WARPS) void k_tensor_inv_rows(NttArgs a, P
     for (int k = 0; k < 8; ++k) {
       const int x = core::last_idx<M2>(l, k);
       const u64 a0 = x0[x], a1 = x1[x], b0 = y0[x], b1 = y1[x];
-      d[0][k] = mont_reduce_lazy(mul_wide(a0, b0), pc);
-      U128 m = mul_wide(a0, b1);
-      add_to(m, mul_wide(a1, b0));
+      // a0 b1 + a1 b0 = (a0 + a1)(b0 + b1) - a0 b0 - a1 b1 exactly (inputs below q < 2^61): three 128-bit
+      // products instead of four, the same integer into the same Montgomery reduction
+      const U128 p0 = mul_wide(a0, b0), p2 = mul_wide(a1, b1);
+      U128 m = mul_wide(a0 + a1, b0 + b1);
+      sub_from(m, p0);
+      sub_from(m, p2);
+      d[0][k] = mont_reduce_lazy(p0, pc);
       d[1][k] = mont_reduce_lazy(m, pc);
-      d[2][k] = mont_reduce_lazy(mul_wide(a1, b1), pc);
+      d[2][k] = mont_reduce_lazy(p2, pc);
     }
   };
   products(first);

@@ -8,7 +8,11 @@ exact arithmetic (CPU only).
 * the lazy finalize's negated-constant Shoup companions: floor((q - w) 2^64 / q) = 2^64 - 1 - floor(w 2^64 / q);
 * the transforms' approximate Shoup product (mul_shoup_apx): the quotient from three of the four 32-bit partial
   products, remainder in [0, 4q); the unreduced forward pass it feeds stays below (4 log N + 1) q < 2^64 for
-  primes below 2^57, and the unreduced inverse column pass keeps its 2^(c+1) q bounds.
+  primes below 2^57, and the unreduced inverse column pass keeps its 2^(c+1) q bounds;
+* the tensor pass's middle term by Karatsuba: (a0 + a1)(b0 + b1) - a0 b0 - a1 b1 in two 64-bit words with
+  borrows equals the 128-bit a0 b1 + a1 b0 for inputs below 4q, q < 2^61;
+* the inverse transforms' scale folded into their last stage: (x + y) n and (x - y + off)(w1 n) equal the
+  unfolded stage followed by the product by n.
 """
 import random
 
@@ -192,3 +196,42 @@ def test_lazy_inverse_pass_stays_below_2_64_and_matches_the_reduced_pass(bits):
                     ref[i], ref[i + t] = (rx + ry) % q, (rx - ry) * w % q
         assert all(v < (2 << M) * q for v in lazy)
         assert [v % q for v in lazy] == ref
+
+
+def _u128_sub(hi, lo, x):
+    """The kernel's sub_from on (hi, lo) words: borrow from the low word into the high one."""
+    borrow = 1 if lo < (x & M64) else 0
+    return (hi - (x >> 64) - borrow) & M64, (lo - (x & M64)) & M64
+
+
+@pytest.mark.parametrize("bits", [36, 50, 60])
+def test_karatsuba_middle_term_equals_the_two_products(bits):
+    rng = random.Random(bits)
+    for q in _primes(bits, 2):
+        for _ in range(3000):
+            a0, a1, b0, b1 = (rng.randrange(4 * q) for _ in range(4))
+            if rng.random() < 0.05:
+                a0 = a1 = b0 = b1 = 4 * q - 1
+            s_a, s_b = a0 + a1, b0 + b1
+            assert s_a <= M64 and s_b <= M64
+            m = s_a * s_b
+            assert m < 1 << 128
+            hi, lo = m >> 64, m & M64
+            hi, lo = _u128_sub(hi, lo, a0 * b0)
+            hi, lo = _u128_sub(hi, lo, a1 * b1)
+            assert (hi << 64) | lo == a0 * b1 + a1 * b0
+
+
+@pytest.mark.parametrize("bits", [30, 50, 55])
+def test_inverse_scale_folded_into_the_last_stage(bits):
+    rng = random.Random(bits + 1)
+    for q in _primes(bits, 2):
+        n = pow(1 << 16, -1, q)
+        for _ in range(3000):
+            w1 = rng.randrange(1, q)
+            x, y = rng.randrange(2 * q), rng.randrange(2 * q)
+            # unfolded: Gentleman-Sande stage, then every output times n
+            u, v = (x + y) % q * n % q, (x - y) * w1 % q * n % q
+            # folded: two products by the precomputed n and w1 n (offset 2q keeps x - y non-negative)
+            assert (x + y) * n % q == u
+            assert (x - y + 2 * q) * (w1 * n % q) % q == v
