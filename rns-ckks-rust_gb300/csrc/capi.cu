@@ -660,7 +660,17 @@ void tensor_core(rc_context* c, const std::vector<const uint64_t*>& lhs, const s
     launch_check("tensor (fused)");
     return;
   }
-  ntt_forward(c->ntt(), src, dst, 4 * J, limbs, qmap(c, limbs), s);
+  // the forward outputs go only to the tensor's Montgomery products: left unreduced (below B q, B = 4 log N + 1
+  // lazy, else 4) when every prime keeps a0 b1 + a1 b0 < 2 B^2 q^2 below q 2^64, the bound of its reduction;
+  // the products' residues, and so the canonical outputs of the inverse transform, are the same
+  NttArgs fwd = c->ntt();
+  {
+    const uint64_t B = fwd.lazy ? 4 * (uint64_t)c->log_n + 1 : 4;
+    bool ok = true;
+    for (int i = 0; i < limbs; ++i) ok = ok && (u128h)2 * B * B * c->mod[i] < ((u128h)1 << 64);
+    fwd.raw_out = ok ? 1 : 0;
+  }
+  ntt_forward(fwd, src, dst, 4 * J, limbs, qmap(c, limbs), s);
   launch_check("ntt_forward(tensor)");
   // the tensor's Montgomery products carry a factor 2^-64, taken out by the inverse transform's scale
   NttArgs inv = c->ntt();

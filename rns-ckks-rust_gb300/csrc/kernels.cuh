@@ -78,6 +78,10 @@ struct NttArgs {
   int row_polys = 16;  // row passes: polynomials per block sharing one twiddle staging (8 or 16)
   int tensor_jobs = 4;  // tensor + inverse row pass: jobs per block sharing one twiddle staging (tunable)
   int r16 = r16::R16_DEFAULT;  // N = 2^16 split 2^8 x 2^8: passes in the 16-residues-per-lane form (bits above)
+  // forward row passes at N = 2^16 (2^8 x 2^8): outputs left unreduced, below (4 log N + 1) q (lazy) or 4q, for
+  // the tensor, whose Montgomery products reduce them (set only when those bounds keep its 128-bit sums below
+  // q 2^64); other ring sizes and passes, and every caller that did not set it, write outputs in [0, q)
+  int raw_out = 0;
 };
 
 // Negacyclic NTT over `polys` x `limbs` limbs, src -> dst (may alias).

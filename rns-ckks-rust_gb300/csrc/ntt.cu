@@ -94,6 +94,12 @@ void fwd_fast(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int polys,
     ProfScope p("ntt_fwd_rows", s);
     with_rp(a.row_polys, [&](auto rp) {
       dim3 g2(N1 / (ROW_WARPS * core::Geo<M2>::SUBS), limbs, (polys + rp.value - 1) / rp.value);
+      if constexpr (M1 == 8 && M2 == 8) {  // unreduced outputs for the tensor at N = 2^16 (NttArgs::raw_out)
+        if (a.raw_out) {
+          k_rows_f<M1, M2, LAZY, true, rp.value, true><<<g2, 32 * ROW_WARPS, 0, s>>>(a, dst, dst, map, polys);
+          return;
+        }
+      }
       k_rows_f<M1, M2, LAZY, true, rp.value><<<g2, 32 * ROW_WARPS, 0, s>>>(a, dst, dst, map, polys);
     });
   }
@@ -118,9 +124,9 @@ bool r16_fwd_rows(const NttArgs& a, const PtrTab& data, int polys, int limbs, Li
   if (!r16::applies(a, r16::R16_ROWS) || !r16::aligned(data, polys)) return false;
   ProfScope p("ntt_fwd_rows", s);
   with_rp(a.row_polys, [&](auto rp) {
-    k16_rows<LAZY, true, rp.value>
-        <<<dim3(256 / (2 * r16::RW), limbs, (polys + rp.value - 1) / rp.value), 32 * r16::RW, 0, s>>>(a, data, data, map,
-                                                                                                   polys);
+    const dim3 g(256 / (2 * r16::RW), limbs, (polys + rp.value - 1) / rp.value);
+    if (a.raw_out) k16_rows<LAZY, true, rp.value, true><<<g, 32 * r16::RW, 0, s>>>(a, data, data, map, polys);
+    else k16_rows<LAZY, true, rp.value><<<g, 32 * r16::RW, 0, s>>>(a, data, data, map, polys);
   });
   return true;
 }
@@ -138,7 +144,8 @@ bool r16_forward(const NttArgs& a, const PtrTab& src, const PtrTab& dst, int pol
     ProfScope p("ntt_fwd_rows", s);
     with_rp(a.row_polys, [&](auto rp) {
       dim3 g2(256 / (ROW_WARPS * core::Geo<8>::SUBS), limbs, (polys + rp.value - 1) / rp.value);
-      k_rows_f<8, 8, LAZY, true, rp.value><<<g2, 32 * ROW_WARPS, 0, s>>>(a, dst, dst, map, polys);
+      if (a.raw_out) k_rows_f<8, 8, LAZY, true, rp.value, true><<<g2, 32 * ROW_WARPS, 0, s>>>(a, dst, dst, map, polys);
+      else k_rows_f<8, 8, LAZY, true, rp.value><<<g2, 32 * ROW_WARPS, 0, s>>>(a, dst, dst, map, polys);
     });
   }
   return true;

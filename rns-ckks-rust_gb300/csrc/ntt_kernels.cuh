@@ -124,8 +124,9 @@ constexpr int ROW_WARPS = 4;
 
 // Row phase: each warp transforms SUBS rows of 2^M2 contiguous residues of polynomials
 // blockIdx.z * RP .. below `polys`, loading the next polynomial's rows while transforming the current
-// one; the CTA stages the rows' twiddle tables in shared memory once.
-template <int M1, int M2, bool LAZY, bool FWD, int RP>
+// one; the CTA stages the rows' twiddle tables in shared memory once.  Forward outputs in [0, q), or (RAW,
+// for the tensor: NttArgs::raw_out) left below (4 log N + 1) q (LAZY) or 4q.
+template <int M1, int M2, bool LAZY, bool FWD, int RP, bool RAW = false>
 __global__ __launch_bounds__(32 * ROW_WARPS) void k_rows_f(NttArgs a, PtrTab src, PtrTab dst, LimbMap map,
                                                            int polys) {
   using G = core::Geo<M2>;
@@ -165,7 +166,7 @@ __global__ __launch_bounds__(32 * ROW_WARPS) void k_rows_f(NttArgs a, PtrTab src
     if (FWD) {
       core::fwd_sub<M2, LAZY>(v, buf, l, twl[rl], pc.q);
 #pragma unroll
-      for (int k = 0; k < 8; ++k) out[core::last_idx<M2>(l, k)] = reduce_out<LAZY>(v[k], pc);
+      for (int k = 0; k < 8; ++k) out[core::last_idx<M2>(l, k)] = RAW ? v[k] : reduce_out<LAZY>(v[k], pc);
     } else {
       core::inv_sub<M2>(v, buf, l, twl[rl], pc.q);
 #pragma unroll

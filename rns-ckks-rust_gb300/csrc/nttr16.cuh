@@ -398,9 +398,9 @@ __global__ __launch_bounds__(256, 2) void k16_cols(NttArgs a, PtrTab src, PtrTab
 
 // Row phase: each warp transforms two rows (one per 16-lane half) of the polynomials blockIdx.z * RP .. below
 // `polys`, the next polynomial's rows loaded while the current one is transformed; the block stages its 8
-// rows' twiddle tables once.  Forward outputs reduced to [0, q) (LAZY: from below 65q by a Shoup product by 1);
-// inverse outputs in [0, 2q).
-template <bool LAZY, bool FWD, int RP>
+// rows' twiddle tables once.  Forward outputs reduced to [0, q) (LAZY: from below 65q by a Shoup product by 1),
+// or (RAW, for the tensor: NttArgs::raw_out) left below 65q (LAZY) or 4q; inverse outputs in [0, 2q).
+template <bool LAZY, bool FWD, int RP, bool RAW = false>
 __global__ __launch_bounds__(32 * r16::RW) void k16_rows(NttArgs a, PtrTab src, PtrTab dst, LimbMap map,
                                                                int polys) {
   using namespace r16;
@@ -442,7 +442,8 @@ __global__ __launch_bounds__(32 * r16::RW) void k16_rows(NttArgs a, PtrTab src, 
 #pragma unroll
       for (int j = 0; j < 8; ++j)
         *reinterpret_cast<ulonglong2*>(out + 16 * lam + 2 * j) =
-            make_ulonglong2(reduce_fwd<LAZY>(v[2 * j], pc), reduce_fwd<LAZY>(v[2 * j + 1], pc));
+            RAW ? make_ulonglong2(v[2 * j], v[2 * j + 1])
+                      : make_ulonglong2(reduce_fwd<LAZY>(v[2 * j], pc), reduce_fwd<LAZY>(v[2 * j + 1], pc));
     } else {
       inv_b<false>(v, tw + lam, q);
       exchange<1, 17>(v, xbb, xa);

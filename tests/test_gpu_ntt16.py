@@ -86,24 +86,27 @@ def test_r16_mult_relinearized_matches_oracle_and_eight_residue_passes(C, pkg, o
     key, D = _key(rng, params, len(q))
     pairs = [(rand_ct(rng, q, n), rand_ct(rng, q, n)) for _ in range(5)]
     results = {}
-    for r16 in (63, 9, 0):
+    # (ntt_r16, lazy_ntt): the forward row passes leave their outputs to the tensor unreduced, below 65q (lazy)
+    # or 4q, in both row forms; the results stay the same
+    for r16, lazy in ((63, 1), (9, 1), (0, 1), (9, 0)):
         ctx = C.RnsCkksContext(params)
         _tune(C, ctx, "ntt_r16", r16)
         _tune(C, ctx, "fuse_tensor", fuse_tensor)
+        _tune(C, ctx, "lazy_ntt", lazy)
         ksk = ctx.upload_keyswitch_key(key, len(q) - 1, 2)  # the key's wide form is built by these passes too
         lhs = [C.RnsCiphertext(C.to_device(a), 40) for a, _ in pairs]
         rhs = [C.RnsCiphertext(C.to_device(b), 40) for _, b in pairs]
         batched = [o.numpy() for o in ctx.mult_relinearized_batch(lhs, rhs, [ksk] * len(pairs))]
         single = ctx.mult_relinearized(lhs[1], rhs[1], ksk).numpy()
         assert np.array_equal(single, batched[1])
-        results[r16] = batched
-    for r16 in (63, 9):
-        for x, y in zip(results[r16], results[0]):
+        results[r16, lazy] = batched
+    for cfg in ((63, 1), (9, 1), (9, 0)):
+        for x, y in zip(results[cfg], results[0, 1]):
             assert np.array_equal(x, y)
     qpl, ppl = oracle.Plans(n, params.primes), oracle.Plans(n, params.aux_primes)
     a, b = pairs[0]
     m0, m1 = oracle.mult_relinearized(qpl, ppl, a[0], a[1], b[0], b[1], key, D)
-    assert np.array_equal(results[63][0][0], m0) and np.array_equal(results[63][0][1], m1)
+    assert np.array_equal(results[63, 1][0][0], m0) and np.array_equal(results[63, 1][0][1], m1)
 
 
 def test_r16_mixed_level_relinearize_rescale_equals_eight_residue_passes(C, pkg):
