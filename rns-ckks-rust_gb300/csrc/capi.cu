@@ -1047,9 +1047,14 @@ extern "C" int rc_context_create(const rc_params* p, rc_context** out) {
         for (int i = 0; i < 4; ++i) {
           const uint64_t q = w[i];
           wp.q[i] = (uint32_t)q;
-          wp.n_inv[i] = (uint32_t)invmod_h(N % q, q);
+          // N^-1 2^32: the key product's Montgomery outputs carry 2^-32 (WidePrimes)
+          wp.n_inv[i] = (uint32_t)mulmod_h(invmod_h(N % q, q), (1ull << 32) % q, q);
           wp.n_inv_s[i] = shoup32(wp.n_inv[i], q);
           wp.bar[i] = (~0ull) / q;
+          uint32_t qi = (uint32_t)q;  // Newton iteration for q^-1 mod 2^32
+          for (int it = 0; it < 5; ++it) qi *= 2u - (uint32_t)q * qi;
+          wp.qinv_neg[i] = 0u - qi;
+          wp.kq[i] = (uint32_t)(((1ull << 31) / q) * q);
           uint64_t psi = 0;  // any primitive 2N-th root of unity (these primes never meet user data)
           for (uint64_t x = 2; x < 100000 && !psi; ++x) {
             const uint64_t cand = powmod_h(x, (q - 1) / (2 * N), q);

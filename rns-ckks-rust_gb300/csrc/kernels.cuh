@@ -189,9 +189,13 @@ void decompose(const PrimeConst* pc, const DecompTab& dt, const PtrTab& src, int
 // (w0, w1), (w2, w3) whose residues sit side by side in a uint2.
 struct WidePrimes {
   uint32_t q[4];
-  uint32_t n_inv[4], n_inv_s[4];  // N^-1 mod q and its Shoup companion
-  uint32_t w1n[4], w1n_s[4];      // the inverse transform's stage-0 twiddle times N^-1 (+ Shoup), see InvScale2
+  // the inverse transform's scale: N^-1 2^32 mod q (+ Shoup), since the key product's outputs, the only values
+  // it transforms, carry the factor 2^-32 of their Montgomery reduction (mont64_32)
+  uint32_t n_inv[4], n_inv_s[4];
+  uint32_t w1n[4], w1n_s[4];      // the inverse transform's stage-0 twiddle times that scale (+ Shoup), InvScale2
   u64 bar[4];                     // floor(2^64 / q): 64-bit -> residue reduction
+  uint32_t qinv_neg[4];           // -q^-1 mod 2^32
+  uint32_t kq[4];                 // floor(2^31 / q) q
   const Tw2* tw_fwd;              // [2 pairs][N]: psi^bitrev(k)
   const Tw2* tw_inv;              // [2 pairs][N]: psi^-bitrev(k)
   int log_n;

@@ -362,7 +362,8 @@ template <int BC, bool FOLD, class KT>
 __device__ __forceinline__ void w_mac_unit(const KT& kt, const uint2* __restrict__ kwt, const uint2* dsm, int run,
                                            uint2* ring, uint32_t rs, int D, int key_digits, int total, int j,
                                            int pair, int xb, int log_n, int slane, int bstart, int nloc,
-                                           uint32_t q0, uint32_t q1, u64 bar0, u64 bar1, uint2* acc) {
+                                           uint32_t q0, uint32_t q1, u64 bar0, u64 bar1, uint32_t qn0, uint32_t qn1,
+                                           uint32_t kq0, uint32_t kq1, uint2* acc) {
   const int lane = threadIdx.x & 31, N = 1 << log_n, tiles = N >> 5;
   const size_t krun = (size_t)key_digits * 2 * 32;
   const uint2* kp = kwt + (((size_t)j * 2 + pair) * tiles + xb) * krun + lane;
@@ -427,9 +428,11 @@ __device__ __forceinline__ void w_mac_unit(const KT& kt, const uint2* __restrict
   for (int b = 0; b < BC; ++b) {
     if (b < nloc) {
       const size_t ab = kt.acc_first(bstart + b, total);
-      acc[((ab + j) * 2 + pair) * N + x] = make_uint2(reduce64_32(a0[b], q0, bar0), reduce64_32(a1[b], q1, bar1));
+      // the sums times 2^-32 (Montgomery), taken out by the inverse transform's scale (WidePrimes::n_inv)
+      acc[((ab + j) * 2 + pair) * N + x] =
+          make_uint2(mont64_32(a0[b], q0, qn0, kq0), mont64_32(a1[b], q1, qn1, kq1));
       acc[((ab + total + j) * 2 + pair) * N + x] =
-          make_uint2(reduce64_32(c0[b], q0, bar0), reduce64_32(c1[b], q1, bar1));
+          make_uint2(mont64_32(c0[b], q0, qn0, kq0), mont64_32(c1[b], q1, qn1, kq1));
     }
   }
 }
@@ -524,13 +527,15 @@ __global__ __launch_bounds__(32 * w_mac_warps<BC>(), BC >= 8 ? 2 : (BC >= 4 ? 3 
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const uint32_t q0 = pick(w.q, pair, 0), q1 = pick(w.q, pair, 1);
   const u64 bar0 = pick(w.bar, pair, 0), bar1 = pick(w.bar, pair, 1);
+  const uint32_t qn0 = pick(w.qinv_neg, pair, 0), qn1 = pick(w.qinv_neg, pair, 1);
+  const uint32_t kq0 = pick(w.kq, pair, 0), kq1 = pick(w.kq, pair, 1);
   // this lane's slots of the warp's key ring: slot u holds (k0, k1) of one digit at ring[u][0|1][lane]
   uint2* ring = dsm + (size_t)BC * run + (size_t)warp * W_PF * 64 + lane;
   const uint32_t rs = (uint32_t)__cvta_generic_to_shared(ring);
 #pragma unroll 1
   for (int j = warp; j < total; j += w_mac_warps<BC>())
     w_mac_unit<BC, FOLD>(kt, kwt, dsm, run, ring, rs, D, key_digits, total, j, pair, xb, w.log_n, slane, bstart,
-                         nloc, q0, q1, bar0, bar1, acc);
+                         nloc, q0, q1, bar0, bar1, qn0, qn1, kq0, kq1, acc);
 }
 
 // D: the largest digit count of the launch (sizes the shared memory); ctas: grid.x
@@ -664,7 +669,8 @@ __global__ __launch_bounds__(32 * WP_WARPS, 1) void k_w_mac_p(WidePrimes w, UniM
     const int slane = gal > 1 ? (int)(galois_source((uint32_t)xb * 32 + (uint32_t)lane, gal, w.log_n) & 31) : lane;
     w_mac_unit<BC, false>(kt, kt.kwt, dsm + (size_t)buf * BC * run, run, ring, rs, D, kt.key_digits, total, j, pair,
                           xb, w.log_n, slane, bstart, nloc, pick(w.q, pair, 0), pick(w.q, pair, 1),
-                          pick(w.bar, pair, 0), pick(w.bar, pair, 1), acc);
+                          pick(w.bar, pair, 0), pick(w.bar, pair, 1), pick(w.qinv_neg, pair, 0),
+                          pick(w.qinv_neg, pair, 1), pick(w.kq, pair, 0), pick(w.kq, pair, 1), acc);
     // every lane's reads of the buffer are done (ordered by the warp barrier and the fence) before the unit
     // counts; the tile's last unit hands the buffer to the bulk copies of tile i + 2
     __syncwarp();

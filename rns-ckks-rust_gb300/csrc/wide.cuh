@@ -16,6 +16,19 @@ __device__ __forceinline__ uint32_t reduce64_32(u64 x, uint32_t q, u64 bar) {
   return (uint32_t)(r >= q ? r - q : r);
 }
 
+// x 2^-32 mod q in [0, q) for any 64-bit x, q < 2^29 (qn = -q^-1 mod 2^32, kq = floor(2^31 / q) q): one 32-bit
+// and one 32 x 32 -> 64-bit multiply instead of reduce64_32's 64 x 64 high product.  An x at or above 2^63 first
+// loses kq 2^32 (a multiple of q, at most 2^63 and above 2^63 - q 2^32), so x + m q stays below 2^63 + 2^62;
+// the quotient by 2^32 is then below 3 2^30 < 8q, and three conditional subtractions finish it
+__device__ __forceinline__ uint32_t mont64_32(u64 x, uint32_t q, uint32_t qn, uint32_t kq) {
+  if (x >> 63) x -= (u64)kq << 32;
+  const uint32_t m = (uint32_t)x * qn;
+  uint32_t t = (uint32_t)((x + (u64)m * q) >> 32);
+  t = t >= 4 * q ? t - 4 * q : t;
+  t = t >= 2 * q ? t - 2 * q : t;
+  return t >= q ? t - q : t;
+}
+
 // a - b mod q for a, b < q
 __device__ __forceinline__ uint32_t sub32(uint32_t a, uint32_t b, uint32_t q) { return a >= b ? a - b : a + q - b; }
 

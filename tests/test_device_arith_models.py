@@ -12,7 +12,9 @@ exact arithmetic (CPU only).
 * the tensor pass's middle term by Karatsuba: (a0 + a1)(b0 + b1) - a0 b0 - a1 b1 in two 64-bit words with
   borrows equals the 128-bit a0 b1 + a1 b0 for inputs below 4q, q < 2^61;
 * the inverse transforms' scale folded into their last stage: (x + y) n and (x - y + off)(w1 n) equal the
-  unfolded stage followed by the product by n.
+  unfolded stage followed by the product by n;
+* the key product's Montgomery 64 -> 32-bit reduction (mont64_32) over the four internal primes: x 2^-32 mod q
+  in [0, q) for every 64-bit x, with no 64-bit overflow on the way.
 """
 import random
 
@@ -235,3 +237,45 @@ def test_inverse_scale_folded_into_the_last_stage(bits):
             # folded: two products by the precomputed n and w1 n (offset 2q keeps x - y non-negative)
             assert (x + y) * n % q == u
             assert (x - y + 2 * q) * (w1 * n % q) % q == v
+
+
+def _internal_primes():
+    """The four largest primes k 2^17 + 1 below 2^29 (the wide key product's internal primes)."""
+    out = []
+    k = ((1 << 29) - 2) >> 17
+    while len(out) < 4 and k > 0:
+        q = (k << 17) + 1
+        if all(q % d for d in range(3, int(q ** 0.5) + 1, 2)):
+            out.append(q)
+        k -= 1
+    return out
+
+
+def _mont64_32(x, q, qn, kq):
+    """The kernel's steps, with every intermediate checked against its machine width."""
+    if x >> 63:
+        x -= kq << 32
+        assert x >= 0
+    m = ((x & 0xFFFFFFFF) * qn) & 0xFFFFFFFF
+    s = x + m * q
+    assert s < 1 << 64 and s & 0xFFFFFFFF == 0
+    t = s >> 32
+    assert t < 8 * q and t < 1 << 32
+    for c in (4, 2, 1):
+        if t >= c * q:
+            t -= c * q
+    return t
+
+
+def test_montgomery_64_to_32_reduction_over_the_internal_primes():
+    rng = random.Random(64)
+    primes = _internal_primes()
+    assert len(primes) == 4 and all(q < 1 << 29 for q in primes)
+    for q in primes:
+        qn = (-pow(q, -1, 1 << 32)) % (1 << 32)
+        kq = ((1 << 31) // q) * q
+        rinv = pow(1 << 32, -1, q)
+        xs = [rng.randrange(1 << 64) for _ in range(20000)]
+        xs += [0, 1, q, (1 << 63) - 1, 1 << 63, (1 << 64) - 1, 40 * (q - 1) ** 2, 64 * (q - 1) ** 2 + q - 1]
+        for x in xs:
+            assert _mont64_32(x, q, qn, kq) == x * rinv % q
