@@ -293,31 +293,33 @@ __device__ __forceinline__ void ld16(T (&v)[16], const T* p) {
 }
 
 // copies a 16-column tile (256 rows of 16 elements at stride 256) into the tile layout: 16 8-byte asynchronous
-// copies per thread of a 256-thread block (one row per sixteen threads, coalesced)
+// copies per thread of a 256-thread block (one row per sixteen threads, coalesced).  Thread t takes row
+// 16 it + t/16 and column t mod 16 at copy it, i.e. a per-thread base plus the constant offsets TBLK it (tile)
+// and 4096 it (global), which the copies take as immediates
 template <class T>
 __device__ __forceinline__ void tile_load(T* tile, const T* in, int t) {
   static_assert(sizeof(T) == 8, "8-byte elements");
+  const int r0 = t >> 4, c = t & 15;
+  T* s = tile + TROW * r0 + c;
+  const T* g = in + r0 * 256 + c;
 #pragma unroll
-  for (int it = 0; it < 16; ++it) {
-    const int id = it * 256 + t, row = id >> 4, c = id & 15;
-    core::cp_async8(tile + tile_row(row) + c, in + (size_t)row * 256 + c);
-  }
+  for (int it = 0; it < 16; ++it) core::cp_async8(s + TBLK * it, g + 4096 * it);
 }
 // the same for 4-byte words (int32 digits) in the word version of the layout
 __device__ __forceinline__ void tile_load_words(int32_t* tile, const int32_t* in, int t) {
+  const int r0 = t >> 4, c = t & 15;
+  int32_t* s = tile + TROW * r0 + c;
+  const int32_t* g = in + r0 * 256 + c;
 #pragma unroll
-  for (int it = 0; it < 16; ++it) {
-    const int id = it * 256 + t, row = id >> 4, c = id & 15;
-    core::cp_async4(tile + tile_row(row) + c, in + (size_t)row * 256 + c);
-  }
+  for (int it = 0; it < 16; ++it) core::cp_async4(s + TBLK * it, g + 4096 * it);
 }
 template <class T>
 __device__ __forceinline__ void tile_store(T* out, const T* tile, int t) {
+  const int r0 = t >> 4, c = t & 15;
+  const T* s = tile + TROW * r0 + c;
+  T* g = out + r0 * 256 + c;
 #pragma unroll
-  for (int it = 0; it < 16; ++it) {
-    const int id = it * 256 + t, row = id >> 4, c = id & 15;
-    out[(size_t)row * 256 + c] = tile[tile_row(row) + c];
-  }
+  for (int it = 0; it < 16; ++it) g[4096 * it] = s[TBLK * it];
 }
 // tile index -> (limb, polynomial, first column): 16 column blocks per limb, limbs per polynomial
 __device__ __forceinline__ void tile_at(int tile, int limbs, int& limb, int& poly, int& c0) {
@@ -349,22 +351,22 @@ __global__ __launch_bounds__(256, 2) void k16_cols(NttArgs a, PtrTab src, PtrTab
   Twiddle* twb = reinterpret_cast<Twiddle*>(dsm16 + 2 * TILE_SLOTS);  // [2][256]
   const int t = threadIdx.x;
   const Twiddle* twg = FWD ? a.tw_fwd : a.tw_inv;
+  // (limb, polynomial, first column) of a tile, found once when its copies are issued and kept for its turn
+  int limb = 0, poly = 0, c0 = 0, nlimb = 0, npoly = 0, nc0 = 0;
   auto issue = [&](int tile, int b) {
-    int limb, poly, c0;
-    tile_at(tile, limbs, limb, poly, c0);
-    tile_load(dsm16 + b * TILE_SLOTS, src.p[poly] + (size_t)limb * N + c0, t);
-    if (t > 0) stage_tw(twb + 256 * b, twg + (size_t)map.prime(limb) * N, 1, t);
+    tile_at(tile, limbs, nlimb, npoly, nc0);
+    tile_load(dsm16 + b * TILE_SLOTS, src.p[npoly] + (size_t)nlimb * N + nc0, t);
+    if (t > 0) stage_tw(twb + 256 * b, twg + (size_t)map.prime(nlimb) * N, 1, t);
   };
   int tile = blockIdx.x;
   if (tile < ntiles) issue(tile, 0);
   const int lane = t & 31, lam = lane & 15, col = 2 * (t >> 5) + (lane >> 4);
 #pragma unroll 1
   for (int b = 0; tile < ntiles; tile += gridDim.x, b ^= 1) {
+    limb = nlimb, poly = npoly, c0 = nc0;
     core::cp_async_wait_all();
     __syncthreads();  // tile landed; every thread is done with the other buffer
     if (tile + (int)gridDim.x < ntiles) issue(tile + gridDim.x, b ^ 1);
-    int limb, poly, c0;
-    tile_at(tile, limbs, limb, poly, c0);
     const PrimeConst& pc = a.pc[map.prime(limb)];
     const u64 q = pc.q;
     u64* tl = dsm16 + b * TILE_SLOTS;
