@@ -214,8 +214,8 @@ __device__ __forceinline__ void gs2(uint2& xr, uint2& yr, const Tw2& w, uint32_t
   const uint32_t t0 = q0 << 1, t1 = q1 << 1;
   const uint2 x = xr, y = yr;
   uint32_t a0 = x.x + y.x, a1 = x.y + y.y;
-  a0 = a0 >= t0 ? a0 - t0 : a0;
-  a1 = a1 >= t1 ? a1 - t1 : a1;
+  a0 = min(a0, a0 - t0);  // a0 - t0 wraps above a0 when a0 < t0 (a0 < 2 t0 < 2^32)
+  a1 = min(a1, a1 - t1);
   xr = make_uint2(a0, a1);
   yr = make_uint2(core::mul_shoup32_lazy(x.x - y.x + t0, w.w0, w.s0, q0),
                   core::mul_shoup32_lazy(x.y - y.y + t1, w.w1, w.s1, q1));
