@@ -73,15 +73,18 @@ __global__ __launch_bounds__(256, CC) void k_cols_f(NttArgs a, PtrTab src, PtrTa
   const u64 q = pc.q;
   const InvScale sc = a.mont_out ? InvScale{pc.n_inv_r, pc.n_inv_r_s, pc.w1nr, pc.w1nr_s}
                                   : InvScale{pc.n_inv, pc.n_inv_s, pc.w1n, pc.w1n_s};
-  const u64* in = src.p[poly] + (size_t)limb * N;
-  u64* out = dst.p[poly] + (size_t)limb * N;
+  // thread t copies column t mod COLS of rows it R + t / COLS (R = 256 / COLS rows per round): a per-thread
+  // base plus constant offsets, the swizzled row being it R + (r0 ^ swz_h(it R / 16)) with r0 = t / COLS < R
+  constexpr int R = 256 / COLS, ROUNDS = N1 * COLS / 256;
+  static_assert(R * COLS == 256, "tile rounds");  // and swz_h < R: below 16 = R (M1 7, 8), at most 2 < R = 8 (M1 6)
+  const int r0 = threadIdx.x / COLS, cc = threadIdx.x % COLS;
+  const u64* in = src.p[poly] + (size_t)limb * N + (size_t)r0 * N2 + c0 + cc;
+  u64* out = dst.p[poly] + (size_t)limb * N + (size_t)r0 * N2 + c0 + cc;
+  u64* tc = tile + cc * G::STRIDE;
   // tile and twiddles by asynchronous copies, all in flight together
-#pragma unroll 4
-  for (int it = 0; it < N1 * COLS / 256; ++it) {
-    const int idx = it * 256 + threadIdx.x;
-    const int r = idx / COLS, c = idx % COLS;
-    core::cp_async8(&tile[c * G::STRIDE + core::swz<M1>(r)], &in[(size_t)r * N2 + c0 + c]);
-  }
+#pragma unroll
+  for (int it = 0; it < ROUNDS; ++it)
+    core::cp_async8(tc + it * R + (r0 ^ core::swz_h<M1>((it * R) >> 4)), in + (size_t)it * R * N2);
   core::stage_twiddles_async<M1>(twl, (FWD ? a.tw_fwd : a.tw_inv) + (size_t)prime * N, 1, threadIdx.x, 256);
   core::cp_async_wait_all();
   __syncthreads();
@@ -109,13 +112,8 @@ __global__ __launch_bounds__(256, CC) void k_cols_f(NttArgs a, PtrTab src, PtrTa
     }
   }
   __syncthreads();
-#pragma unroll 4
-  for (int it = 0; it < N1 * COLS / 256; ++it) {
-    const int idx = it * 256 + threadIdx.x;
-    const int r = idx / COLS, c = idx % COLS;
-    const u64 x = tile[c * G::STRIDE + core::swz<M1>(r)];
-    out[(size_t)r * N2 + c0 + c] = x;
-  }
+#pragma unroll
+  for (int it = 0; it < ROUNDS; ++it) out[(size_t)it * R * N2] = tc[it * R + (r0 ^ core::swz_h<M1>((it * R) >> 4))];
 }
 
 constexpr int ROW_WARPS = 4;

@@ -142,13 +142,18 @@ __device__ __forceinline__ int gidx(int l, int k) {
 
 // conflict-free XOR swizzle (found by exhaustive search over GF(2)-linear maps)
 template <int M>
+__host__ __device__ __forceinline__ constexpr int swz_h(int v) {
+  return M == 8 ? ((v & 1) ? 1 : 0) ^ ((v & 2) ? 6 : 0) ^ ((v & 4) ? 8 : 0)
+                : (M == 7 ? ((v & 1) ? 3 : 0) ^ ((v & 2) ? 4 : 0) ^ ((v & 4) ? 8 : 0) : ((v & 2) ? 2 : 0));
+}
+template <int M>
 __device__ __forceinline__ int swz(int r) {
   const int v = r >> 4;
   int h;
   if (M == 8) h = ((v & 1) ? 1 : 0) ^ ((v & 2) ? 6 : 0) ^ ((v & 4) ? 8 : 0);
   else if (M == 7) h = ((v & 1) ? 3 : 0) ^ ((v & 2) ? 4 : 0) ^ ((v & 4) ? 8 : 0);
   else h = (v & 2) ? 2 : 0;
-  return r ^ h;
+  return r ^ h;  // = r ^ swz_h<M>(r >> 4)
 }
 
 // Cooley-Tukey butterflies of one group.  LAZY: inputs are not reduced and the twiddle products take the
