@@ -68,17 +68,20 @@ __global__ __launch_bounds__(256, 2) void k_w_cols_fwd(WidePrimes w, const void*
   const size_t poly = (size_t)p0 + blockIdx.z;
   const uint32_t q0 = pick(w.q, pair, 0), q1 = pick(w.q, pair, 1);
   // tile (digits: the int32 into the element's first word, converted at first use) and twiddles by
-  // asynchronous copies, all in flight together
-#pragma unroll 4
-  for (int it = 0; it < N1 * COLS / 256; ++it) {
-    const int idx = it * 256 + threadIdx.x;
-    const int r = idx / COLS, c = idx % COLS;
+  // asynchronous copies, all in flight together; thread t copies column t mod COLS of rows it R + t / COLS
+  // from one per-thread base (the swizzled row it R + (r0 ^ swz_h(it R / 16)), as in k_cols_f)
+  constexpr int R = 256 / COLS, ROUNDS = N1 * COLS / 256;
+  static_assert(R * COLS == 256, "tile rounds");
+  const int r0 = threadIdx.x / COLS, cc = threadIdx.x % COLS;
+  uint2* tc = tile + cc * G::STRIDE;
+  const size_t goff = (size_t)r0 * N2 + c0 + cc;
+#pragma unroll
+  for (int it = 0; it < ROUNDS; ++it) {
+    uint2* s = tc + it * R + (r0 ^ core::swz_h<M1>((it * R) >> 4));
     if (SRC == 0)
-      core::cp_async4(&tile[c * G::STRIDE + core::swz<M1>(r)].x,
-                      static_cast<const int32_t*>(src) + poly * N + (size_t)r * N2 + c0 + c);
+      core::cp_async4(&s->x, static_cast<const int32_t*>(src) + poly * N + goff + (size_t)it * R * N2);
     else
-      core::cp_async8(&tile[c * G::STRIDE + core::swz<M1>(r)],
-                      static_cast<const uint2*>(src) + (poly * 2 + pair) * N + (size_t)r * N2 + c0 + c);
+      core::cp_async8(s, static_cast<const uint2*>(src) + (poly * 2 + pair) * N + goff + (size_t)it * R * N2);
   }
   core::stage_twiddles_async<M1>(twl, w.tw_fwd + (size_t)pair * N, 1, threadIdx.x, 256);
   core::cp_async_wait_all();
@@ -104,13 +107,9 @@ __global__ __launch_bounds__(256, 2) void k_w_cols_fwd(WidePrimes w, const void*
     for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::last_idx<M1>(l, k))] = v[k];
   }
   __syncthreads();
-  uint2* o = out + (poly * 2 + pair) * N;
-#pragma unroll 4
-  for (int it = 0; it < N1 * COLS / 256; ++it) {
-    const int idx = it * 256 + threadIdx.x;
-    const int r = idx / COLS, c = idx % COLS;
-    o[(size_t)r * N2 + c0 + c] = tile[c * G::STRIDE + core::swz<M1>(r)];
-  }
+  uint2* o = out + (poly * 2 + pair) * N + goff;
+#pragma unroll
+  for (int it = 0; it < ROUNDS; ++it) o[(size_t)it * R * N2] = tc[it * R + (r0 ^ core::swz_h<M1>((it * R) >> 4))];
 }
 
 // Row kernels: a block transforms the same ROWS rows of W_ROW_POLYS consecutive polynomials, so each row's
@@ -270,13 +269,15 @@ __global__ __launch_bounds__(256, 3) void k_w_cols_inv(WidePrimes w, uint2* data
   const uint32_t q0 = pick(w.q, pair, 0), q1 = pick(w.q, pair, 1);
   const InvScale2 sc{pick(w.n_inv, pair, 0), pick(w.n_inv_s, pair, 0), pick(w.w1n, pair, 0), pick(w.w1n_s, pair, 0),
                      pick(w.n_inv, pair, 1), pick(w.n_inv_s, pair, 1), pick(w.w1n, pair, 1), pick(w.w1n_s, pair, 1)};
-  uint2* io = data + (poly * 2 + pair) * N;
-#pragma unroll 4
-  for (int it = 0; it < N1 * COLS / 256; ++it) {
-    const int idx = it * 256 + threadIdx.x;
-    const int r = idx / COLS, c = idx % COLS;
-    core::cp_async8(&tile[c * G::STRIDE + core::swz<M1>(r)], &io[(size_t)r * N2 + c0 + c]);
-  }
+  // thread t copies column t mod COLS of rows it R + t / COLS from one per-thread base (as in k_cols_f)
+  constexpr int R = 256 / COLS, ROUNDS = N1 * COLS / 256;
+  static_assert(R * COLS == 256, "tile rounds");
+  const int r0 = threadIdx.x / COLS, cc = threadIdx.x % COLS;
+  uint2* tc = tile + cc * G::STRIDE;
+  uint2* io = data + (poly * 2 + pair) * N + (size_t)r0 * N2 + c0 + cc;
+#pragma unroll
+  for (int it = 0; it < ROUNDS; ++it)
+    core::cp_async8(tc + it * R + (r0 ^ core::swz_h<M1>((it * R) >> 4)), io + (size_t)it * R * N2);
   core::stage_twiddles_async<M1>(twl, w.tw_inv + (size_t)pair * N, 1, threadIdx.x, 256);
   core::cp_async_wait_all();
   __syncthreads();
@@ -295,12 +296,8 @@ __global__ __launch_bounds__(256, 3) void k_w_cols_inv(WidePrimes w, uint2* data
     for (int k = 0; k < 8; ++k) buf[core::swz<M1>(core::first_idx<M1>(l, k))] = v[k];
   }
   __syncthreads();
-#pragma unroll 4
-  for (int it = 0; it < N1 * COLS / 256; ++it) {
-    const int idx = it * 256 + threadIdx.x;
-    const int r = idx / COLS, c = idx % COLS;
-    io[(size_t)r * N2 + c0 + c] = tile[c * G::STRIDE + core::swz<M1>(r)];
-  }
+#pragma unroll
+  for (int it = 0; it < ROUNDS; ++it) io[(size_t)it * R * N2] = tc[it * R + (r0 ^ core::swz_h<M1>((it * R) >> 4))];
 }
 
 // acc[b][c][j][pair][x] = sum_i DT[b][pair][x][i] * KW[j][pair][x][i][c] for
