@@ -10,7 +10,9 @@ exact arithmetic (CPU only).
   products, remainder in [0, 4q); the unreduced forward pass it feeds stays below (4 log N + 1) q < 2^64 for
   primes below 2^57, and the unreduced inverse column pass keeps its 2^(c+1) q bounds;
 * the tensor pass's middle term by Karatsuba: (a0 + a1)(b0 + b1) - a0 b0 - a1 b1 in two 64-bit words with
-  borrows equals the 128-bit a0 b1 + a1 b0 for inputs below 4q, q < 2^61;
+  borrows equals the 128-bit a0 b1 + a1 b0 for inputs below 4q, q < 2^61, and for the forward row pass's
+  unreduced outputs (below (4 log N + 1) q) wherever the host allows them (2 B^2 q < 2^64): every Montgomery
+  input then stays below q 2^64;
 * the inverse transforms' scale folded into their last stage: (x + y) n and (x - y + off)(w1 n) equal the
   unfolded stage followed by the product by n;
 * the key product's Montgomery 64 -> 32-bit reduction (mont64_32) over the four internal primes: x 2^-32 mod q
@@ -279,3 +281,33 @@ def test_montgomery_64_to_32_reduction_over_the_internal_primes():
         xs += [0, 1, q, (1 << 63) - 1, 1 << 63, (1 << 64) - 1, 40 * (q - 1) ** 2, 64 * (q - 1) ** 2 + q - 1]
         for x in xs:
             assert _mont64_32(x, q, qn, kq) == x * rinv % q
+
+
+def _raw_out_allowed(q, log_n, lazy):
+    """The host's condition for unreduced forward outputs into the tensor (B = 4 log N + 1 lazy, else 4)."""
+    b = 4 * log_n + 1 if lazy else 4
+    return 2 * b * b * q < 1 << 64, b
+
+
+@pytest.mark.parametrize("bits", [40, 50, 51])
+def test_unreduced_forward_outputs_keep_the_tensor_exact(bits):
+    rng = random.Random(bits + 7)
+    for q in _primes(bits, 2):
+        for log_n, lazy in ((16, True), (12, True), (16, False)):
+            ok, b = _raw_out_allowed(q, log_n, lazy)
+            if not ok:
+                assert bits == 51 and lazy  # 51-bit primes exceed the lazy bound: canonical outputs instead
+                continue
+            for _ in range(2000):
+                a0, a1, b0, b1 = (rng.randrange(b * q) for _ in range(4))
+                if rng.random() < 0.05:
+                    a0 = a1 = b0 = b1 = b * q - 1
+                assert a0 + a1 <= M64 and b0 + b1 <= M64
+                m = (a0 + a1) * (b0 + b1)
+                hi, lo = m >> 64, m & M64
+                hi, lo = _u128_sub(hi, lo, a0 * b0)
+                hi, lo = _u128_sub(hi, lo, a1 * b1)
+                mid = (hi << 64) | lo
+                assert mid == a0 * b1 + a1 * b0
+                for t in (a0 * b0, mid, a1 * b1):  # the Montgomery reduction's input bound
+                    assert t < q << 64
