@@ -313,6 +313,12 @@ __device__ __forceinline__ void cp_async8(uint32_t dst, const void* src) {
   asm volatile("cp.async.ca.shared.global [%0], [%1], 8;" ::"r"(dst), "l"(src) : "memory");
 }
 __device__ __forceinline__ void cp_async_commit() { asm volatile("cp.async.commit_group;" ::: "memory"); }
+// 8 bytes from global address g + OFF to shared address s + OFF: the offset is an immediate of the instruction,
+// so copies at constant distances from one base need no address arithmetic of their own
+template <int OFF>
+__device__ __forceinline__ void cp_async8_at(uint32_t s, const void* g) {
+  asm volatile("cp.async.ca.shared.global [%0+%2], [%1+%2], 8;" ::"r"(s), "l"(g), "n"(OFF) : "memory");
+}
 template <int N>
 __device__ __forceinline__ void cp_async_wait() {
   asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
@@ -407,10 +413,20 @@ __device__ __forceinline__ void w_mac_unit(const KT& kt, const uint2* __restrict
           c0[b] += (u64)d.x * k1.x;
           c1[b] += (u64)d.y * k1.y;
         }
-        // refill the slot with digit i + W_PF once its words have been used
+        // refill the slot with digit i + W_PF once its words have been used: words k0 and k1 of slot u sit
+        // 512 u and 512 u + 256 bytes past rs, and digit i + W_PF's words the same distances past kn (the
+        // switch on the unrolled, hence constant, u selects one pair of immediate-offset copies)
         if (i + W_PF < D) {
-          cp_async8(rs + 8u * (64 * u), kn + 64 * u);
-          cp_async8(rs + 8u * (64 * u + 32), kn + 64 * u + 32);
+          static_assert(W_PF == 8, "one case per ring slot");
+          switch (u) {
+#define RC_REFILL(U)                          \
+  case U:                                     \
+    cp_async8_at<512 * U>(rs, kn);            \
+    cp_async8_at<512 * U + 256>(rs, kn);      \
+    break;
+            RC_REFILL(0) RC_REFILL(1) RC_REFILL(2) RC_REFILL(3) RC_REFILL(4) RC_REFILL(5) RC_REFILL(6) RC_REFILL(7)
+#undef RC_REFILL
+          }
         }
         cp_async_commit();
       }
